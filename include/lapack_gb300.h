@@ -1,0 +1,210 @@
+/*
+ * lapack_gb300.h -- C ABI of the GB300 dense LU solve library.
+ *
+ * Three layers, all plain C types (no CUDA or torch types in signatures;
+ * a stream is passed as void*):
+ *
+ *  1. The LAPACK Fortran ABI for the LU solve path, so an existing Fortran
+ *     or C program links against liblapack_gb300.so in place of the
+ *     reference LAPACK for these routines.  Host pointers, column-major,
+ *     1-based IPIV, INFO as in the reference; the library copies to the GPU
+ *     and back inside each call and retains no pointer.  Hidden CHARACTER
+ *     lengths come last (LAPACK_FORTRAN_STRLEN_END convention).
+ *  2. The LAPACKE C interface for the same routines (row/column major,
+ *     NaN checks, INFO shifts, LAPACKE_NANCHECK).
+ *  3. gb300_* device-pointer entry points for callers whose data already
+ *     lives in GPU memory (no reference counterpart), plus option and
+ *     status controls.
+ *
+ * lapack_int is 32-bit (LP64), matching the reference default.
+ */
+#ifndef LAPACK_GB300_H
+#define LAPACK_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lapack_int;
+
+/* ---------------------------------------------------------------------
+ * 1. Fortran ABI (LAPACKE/include/lapack.h prototypes)
+ * ------------------------------------------------------------------- */
+
+/* LU with partial pivoting, blocked right-looking.
+ * Replaces SRC/dgetrf.f:105 (prototype LAPACKE/include/lapack.h:4349-4355). */
+void dgetrf_(const lapack_int* m, const lapack_int* n, double* a, const lapack_int* lda,
+             lapack_int* ipiv, lapack_int* info);
+/* Replaces SRC/sgetrf.f (lapack.h:4363-4369). */
+void sgetrf_(const lapack_int* m, const lapack_int* n, float* a, const lapack_int* lda,
+             lapack_int* ipiv, lapack_int* info);
+/* Recursive panel LU.  Replaces SRC/dgetrf2.f:112 (lapack.h:4373-4379). */
+void dgetrf2_(const lapack_int* m, const lapack_int* n, double* a, const lapack_int* lda,
+              lapack_int* ipiv, lapack_int* info);
+/* Replaces SRC/sgetrf2.f (lapack.h:4387-4393). */
+void sgetrf2_(const lapack_int* m, const lapack_int* n, float* a, const lapack_int* lda,
+              lapack_int* ipiv, lapack_int* info);
+/* Solve with the LU factors, TRANS = 'N', 'T' or 'C'.
+ * Replaces SRC/dgetrs.f:118 (lapack.h:4436-4451). */
+void dgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const double* a,
+             const lapack_int* lda, const lapack_int* ipiv, double* b, const lapack_int* ldb,
+             lapack_int* info, size_t trans_len);
+/* Replaces SRC/sgetrs.f (lapack.h:4453-4468). */
+void sgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const float* a,
+             const lapack_int* lda, const lapack_int* ipiv, float* b, const lapack_int* ldb,
+             lapack_int* info, size_t trans_len);
+/* Driver: DGETRF then DGETRS('N').  Replaces SRC/dgesv.f:121 (lapack.h:3706-3712). */
+void dgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+            lapack_int* ipiv, double* b, const lapack_int* ldb, lapack_int* info);
+/* Replaces SRC/sgesv.f (lapack.h sgesv prototype). */
+void sgesv_(const lapack_int* n, const lapack_int* nrhs, float* a, const lapack_int* lda,
+            lapack_int* ipiv, float* b, const lapack_int* ldb, lapack_int* info);
+/* Mixed-precision iterative refinement driver.
+ * Replaces SRC/dsgesv.f:191 (lapack.h:3727-3735).  WORK and SWORK are
+ * accepted for ABI compatibility; the computation uses device memory. */
+void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+             lapack_int* ipiv, const double* b, const lapack_int* ldb, double* x,
+             const lapack_int* ldx, double* work, float* swork, lapack_int* iter, lapack_int* info);
+/* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
+void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
+             const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
+/* Replaces SRC/slaswp.f (lapack.h slaswp prototype). */
+void slaswp_(const lapack_int* n, float* a, const lapack_int* lda, const lapack_int* k1,
+             const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
+/* Precision conversions.  Replace SRC/dlag2s.f:105 and SRC/slag2d.f:101
+ * (lapack.h:9748-9760). */
+void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda,
+             float* sa, const lapack_int* ldsa, lapack_int* info);
+void slag2d_(const lapack_int* m, const lapack_int* n, const float* sa, const lapack_int* ldsa,
+             double* a, const lapack_int* lda, lapack_int* info);
+/* Matrix norm, NORM = 'M', '1'/'O', 'I'.  Replaces SRC/dlange.f:111 for
+ * those norms (lapack.h dlange prototype). */
+double dlange_(const char* norm, const lapack_int* m, const lapack_int* n, const double* a,
+               const lapack_int* lda, double* work, size_t norm_len);
+/* Machine parameters.  Replace INSTALL/dlamch.f:68 and INSTALL/slamch.f. */
+double dlamch_(const char* cmach, size_t len);
+float slamch_(const char* cmach, size_t len);
+/* Error handler.  Replaces SRC/xerbla.f:67: prints the reference message and
+ * stops the program, unless gb300_xerbla_capture(1) is in effect.  Weak:
+ * a program may supply its own xerbla_. */
+void xerbla_(const char* srname, const lapack_int* info, size_t srname_len);
+
+/* ---------------------------------------------------------------------
+ * 2. LAPACKE (LAPACKE/include/lapacke.h)
+ * ------------------------------------------------------------------- */
+#define LAPACK_ROW_MAJOR 101
+#define LAPACK_COL_MAJOR 102
+#define LAPACK_WORK_MEMORY_ERROR -1010
+#define LAPACK_TRANSPOSE_MEMORY_ERROR -1011
+
+/* LAPACKE/include/lapacke.h:939-952 */
+lapack_int LAPACKE_dgesv(int matrix_layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                         lapack_int* ipiv, double* b, lapack_int ldb);
+lapack_int LAPACKE_dgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                              lapack_int* ipiv, double* b, lapack_int ldb);
+lapack_int LAPACKE_sgesv(int matrix_layout, lapack_int n, lapack_int nrhs, float* a, lapack_int lda,
+                         lapack_int* ipiv, float* b, lapack_int ldb);
+lapack_int LAPACKE_sgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, float* a, lapack_int lda,
+                              lapack_int* ipiv, float* b, lapack_int ldb);
+/* LAPACKE/include/lapacke.h:1129-1167 */
+lapack_int LAPACKE_dgetrf(int matrix_layout, lapack_int m, lapack_int n, double* a, lapack_int lda,
+                          lapack_int* ipiv);
+lapack_int LAPACKE_dgetrf_work(int matrix_layout, lapack_int m, lapack_int n, double* a, lapack_int lda,
+                               lapack_int* ipiv);
+lapack_int LAPACKE_dgetrf2(int matrix_layout, lapack_int m, lapack_int n, double* a, lapack_int lda,
+                           lapack_int* ipiv);
+lapack_int LAPACKE_dgetrf2_work(int matrix_layout, lapack_int m, lapack_int n, double* a, lapack_int lda,
+                                lapack_int* ipiv);
+lapack_int LAPACKE_sgetrf(int matrix_layout, lapack_int m, lapack_int n, float* a, lapack_int lda,
+                          lapack_int* ipiv);
+lapack_int LAPACKE_sgetrf_work(int matrix_layout, lapack_int m, lapack_int n, float* a, lapack_int lda,
+                               lapack_int* ipiv);
+lapack_int LAPACKE_dgetrs(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const double* a,
+                          lapack_int lda, const lapack_int* ipiv, double* b, lapack_int ldb);
+lapack_int LAPACKE_dgetrs_work(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const double* a,
+                               lapack_int lda, const lapack_int* ipiv, double* b, lapack_int ldb);
+lapack_int LAPACKE_sgetrs(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const float* a,
+                          lapack_int lda, const lapack_int* ipiv, float* b, lapack_int ldb);
+lapack_int LAPACKE_sgetrs_work(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const float* a,
+                               lapack_int lda, const lapack_int* ipiv, float* b, lapack_int ldb);
+/* LAPACKE/include/lapacke.h:2577 (dsgesv) */
+lapack_int LAPACKE_dsgesv(int matrix_layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                          lapack_int* ipiv, const double* b, lapack_int ldb, double* x, lapack_int ldx,
+                          lapack_int* iter);
+lapack_int LAPACKE_dsgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                               lapack_int* ipiv, const double* b, lapack_int ldb, double* x, lapack_int ldx,
+                               double* work, float* swork, lapack_int* iter);
+/* LAPACKE/include/lapacke.h (dlaswp, slaswp) */
+lapack_int LAPACKE_dlaswp(int matrix_layout, lapack_int n, double* a, lapack_int lda, lapack_int k1,
+                          lapack_int k2, const lapack_int* ipiv, lapack_int incx);
+lapack_int LAPACKE_dlaswp_work(int matrix_layout, lapack_int n, double* a, lapack_int lda, lapack_int k1,
+                               lapack_int k2, const lapack_int* ipiv, lapack_int incx);
+lapack_int LAPACKE_slaswp(int matrix_layout, lapack_int n, float* a, lapack_int lda, lapack_int k1,
+                          lapack_int k2, const lapack_int* ipiv, lapack_int incx);
+lapack_int LAPACKE_slaswp_work(int matrix_layout, lapack_int n, float* a, lapack_int lda, lapack_int k1,
+                               lapack_int k2, const lapack_int* ipiv, lapack_int incx);
+/* LAPACKE/include/lapacke.h (dlag2s, slag2d) */
+lapack_int LAPACKE_dlag2s(int matrix_layout, lapack_int m, lapack_int n, const double* a, lapack_int lda,
+                          float* sa, lapack_int ldsa);
+lapack_int LAPACKE_dlag2s_work(int matrix_layout, lapack_int m, lapack_int n, const double* a, lapack_int lda,
+                               float* sa, lapack_int ldsa);
+lapack_int LAPACKE_slag2d(int matrix_layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa,
+                          double* a, lapack_int lda);
+lapack_int LAPACKE_slag2d_work(int matrix_layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa,
+                               double* a, lapack_int lda);
+/* LAPACKE/src/lapacke_nancheck.c:97-115 */
+int LAPACKE_get_nancheck(void);
+void LAPACKE_set_nancheck(int flag);
+/* LAPACKE/utils/lapacke_xerbla.c */
+void LAPACKE_xerbla(const char* name, lapack_int info);
+/* LAPACKE/src/lapacke_alloc.c:57-61 */
+void LAPACKE_set_alloc(void* (*malloc_fn)(size_t), void (*free_fn)(void*));
+void* LAPACKE_malloc_proxy(size_t size);
+void LAPACKE_free_proxy(void* ptr);
+
+/* ---------------------------------------------------------------------
+ * 3. Device-pointer entry points (no reference counterpart)
+ *
+ * Arrays are in GPU global memory of the current device, column-major.
+ * The call queues its work on `stream` (NULL: the legacy default stream)
+ * and returns when the result is complete; *info (host) receives the
+ * LAPACK INFO.  Return value: 0 on success, a negative argument index for
+ * an illegal argument (no xerbla_ call), or a positive CUDA / library
+ * status code on a device failure.
+ * ------------------------------------------------------------------- */
+int gb300_dgetrf_dev(int m, int n, double* dA, int lda, int* dIpiv, int* info, void* stream);
+int gb300_sgetrf_dev(int m, int n, float* dA, int lda, int* dIpiv, int* info, void* stream);
+int gb300_dgetrs_dev(char trans, int n, int nrhs, const double* dA, int lda, const int* dIpiv, double* dB,
+                     int ldb, void* stream);
+int gb300_sgetrs_dev(char trans, int n, int nrhs, const float* dA, int lda, const int* dIpiv, float* dB,
+                     int ldb, void* stream);
+int gb300_dgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, double* dB, int ldb, int* info,
+                    void* stream);
+int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX,
+                     int ldx, int* iter, int* info, void* stream);
+
+/* Options: "exact" (0/1: products rounded separately, bitwise the
+ * reference's operation order), "nb64" / "nb32" (outer block sizes),
+ * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32
+ * factorization), "sgetrf" (same choice for SGETRF itself).  Returns the
+ * previous value, or -1 for an unknown name.  Not thread-safe: set at
+ * start-up. */
+int gb300_set_option(const char* name, int value);
+int gb300_get_option(const char* name);
+/* Reads (and with clear=1 resets) the device status word that kernels with
+ * bounded waits set when a wait runs out: 0 means none did. */
+int gb300_status(int clear);
+/* xerbla_ capture: with on=1, illegal-argument reports are recorded instead
+ * of stopping the program; gb300_xerbla_last returns the last INFO and
+ * copies the routine name. */
+void gb300_xerbla_capture(int on);
+int gb300_xerbla_last(char* name, int cap);
+const char* gb300_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LAPACK_GB300_H */

@@ -1,0 +1,271 @@
+"""GB300-native LAPACK dense LU solve path.
+
+Python mirror of the library's C ABI (``include/lapack_gb300.h``): the
+reference routine names and argument meanings (DGETRF, DGETRS, DGESV,
+DSGESV, DLASWP, ... with column-major arrays, 1-based IPIV and LAPACK INFO
+codes), called through ``liblapack_gb300.so``.  All arithmetic runs in the
+hand-written sm_103a kernels of that library; there is no CPU path.  If the
+shared library is missing, importing the bindings raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liblapack_gb300.so")
+_LIB = None
+
+_i = ctypes.c_int
+_p = ctypes.c_void_p
+_ip = ctypes.POINTER(ctypes.c_int)
+_sz = ctypes.c_size_t
+
+FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
+                   "dsgesv_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_", "slamch_",
+                   "xerbla_"]
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def build(force=False):
+    """Compiles liblapack_gb300.so in-tree (see buildlib.py)."""
+    from . import buildlib
+    return buildlib.build(force=force)
+
+
+def lib():
+    """The loaded shared library (raises LibraryMissing if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(f"{LIB_PATH} not built; run lapack_gb300.build()")
+        L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+        L.dlange_.restype = ctypes.c_double
+        L.dlamch_.restype = ctypes.c_double
+        L.slamch_.restype = ctypes.c_float
+        L.gb300_version.restype = ctypes.c_char_p
+        L.gb300_set_option.argtypes = [ctypes.c_char_p, _i]
+        L.gb300_get_option.argtypes = [ctypes.c_char_p]
+        L.gb300_xerbla_last.argtypes = [ctypes.c_char_p, _i]
+        for nm in ("gb300_dgetrf_dev", "gb300_sgetrf_dev"):
+            getattr(L, nm).argtypes = [_i, _i, _p, _i, _p, _ip, _p]
+        for nm in ("gb300_dgetrs_dev", "gb300_sgetrs_dev"):
+            getattr(L, nm).argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _p, _i, _p]
+        L.gb300_dgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
+        L.gb300_dsgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _ip, _ip, _p]
+        _LIB = L
+    return _LIB
+
+
+def _ref(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _fortran(a, dtype):
+    return np.asfortranarray(np.array(a, dtype=dtype, copy=True))
+
+
+def _pre(dtype):
+    return "d" if np.dtype(dtype) == np.float64 else "s"
+
+
+# ------------------------------------------------------------------ options
+def set_option(name, value):
+    """Library options: 'exact' (0/1), 'nb64', 'nb32', 'mixed' (0 BF16x3
+    tensor cores, 1 FP32 CUDA cores), 'sgetrf'.  Returns the old value."""
+    return lib().gb300_set_option(name.encode(), int(value))
+
+
+def get_option(name):
+    return lib().gb300_get_option(name.encode())
+
+
+def status(clear=True):
+    return lib().gb300_status(int(clear))
+
+
+def xerbla_capture(on=True):
+    lib().gb300_xerbla_capture(int(on))
+
+
+def xerbla_last():
+    buf = ctypes.create_string_buffer(16)
+    info = lib().gb300_xerbla_last(buf, 16)
+    return buf.value.decode(), info
+
+
+# ------------------------------------------------- LAPACK routines (host data)
+def getrf(a, dtype=None):
+    """xGETRF (SRC/dgetrf.f): returns (lu, ipiv, info) for a copy of ``a``."""
+    dtype = np.dtype(dtype or (a.dtype if a.dtype in (np.float32, np.float64) else np.float64))
+    a = _fortran(a, dtype)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}getrf_")(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv), ctypes.byref(info))
+    return a, ipiv[: min(m, n)], info.value
+
+
+def getrf2(a, dtype=None):
+    """xGETRF2 (SRC/dgetrf2.f)."""
+    dtype = np.dtype(dtype or (a.dtype if a.dtype in (np.float32, np.float64) else np.float64))
+    a = _fortran(a, dtype)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}getrf2_")(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv), ctypes.byref(info))
+    return a, ipiv[: min(m, n)], info.value
+
+
+def getrs(lu, ipiv, b, trans="N"):
+    """xGETRS (SRC/dgetrs.f): returns (x, info)."""
+    dtype = lu.dtype
+    lu = _fortran(lu, dtype)
+    b2 = _fortran(np.asarray(b).reshape(lu.shape[0], -1), dtype)
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}getrs_")(ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(lu),
+                                           _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)),
+                                           ctypes.byref(info), _sz(1))
+    return b2.reshape(np.asarray(b).shape), info.value
+
+
+def gesv(a, b, dtype=None):
+    """xGESV (SRC/dgesv.f): returns (lu, ipiv, x, info)."""
+    dtype = np.dtype(dtype or (a.dtype if a.dtype in (np.float32, np.float64) else np.float64))
+    a = _fortran(a, dtype)
+    n = a.shape[0]
+    b2 = _fortran(np.asarray(b).reshape(n, -1), dtype)
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}gesv_")(_ref(n), _ref(b2.shape[1]), _ptr(a), _ref(max(1, n)), _ptr(ipiv),
+                                          _ptr(b2), _ref(max(1, n)), ctypes.byref(info))
+    return a, ipiv[:n], b2.reshape(np.asarray(b).shape), info.value
+
+
+def dsgesv(a, b):
+    """DSGESV (SRC/dsgesv.f): returns (a_out, ipiv, x, iter, info)."""
+    a = _fortran(a, np.float64)
+    n = a.shape[0]
+    b2 = _fortran(np.asarray(b).reshape(n, -1), np.float64)
+    nrhs = b2.shape[1]
+    x = np.zeros((n, nrhs), dtype=np.float64, order="F")
+    work = np.zeros(max(1, n * nrhs), dtype=np.float64)
+    swork = np.zeros(1, dtype=np.float32)          # the GPU works in device memory
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    it = ctypes.c_int(0)
+    info = ctypes.c_int(0)
+    lib().dsgesv_(_ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)), _ptr(x),
+                  _ref(max(1, n)), _ptr(work), _ptr(swork), ctypes.byref(it), ctypes.byref(info))
+    return a, ipiv[:n], x.reshape(np.asarray(b).shape), it.value, info.value
+
+
+def laswp(a, k1, k2, ipiv, incx=1):
+    """xLASWP (SRC/dlaswp.f) on a copy of ``a``."""
+    a = _fortran(a, a.dtype)
+    m, n = a.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    getattr(lib(), f"{_pre(a.dtype)}laswp_")(_ref(n), _ptr(a), _ref(max(1, m)), _ref(k1), _ref(k2), _ptr(ipiv),
+                                             _ref(incx))
+    return a
+
+
+def dlag2s(a):
+    a = _fortran(a, np.float64)
+    m, n = a.shape
+    sa = np.zeros((m, n), dtype=np.float32, order="F")
+    info = ctypes.c_int(0)
+    lib().dlag2s_(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(sa), _ref(max(1, m)), ctypes.byref(info))
+    return sa, info.value
+
+
+def slag2d(sa):
+    sa = _fortran(sa, np.float32)
+    m, n = sa.shape
+    a = np.zeros((m, n), dtype=np.float64, order="F")
+    info = ctypes.c_int(0)
+    lib().slag2d_(_ref(m), _ref(n), _ptr(sa), _ref(max(1, m)), _ptr(a), _ref(max(1, m)), ctypes.byref(info))
+    return a, info.value
+
+
+def dlange(norm, a):
+    a = _fortran(a, np.float64)
+    m, n = a.shape
+    work = np.zeros(max(1, m), dtype=np.float64)
+    return lib().dlange_(ctypes.c_char_p(norm.encode()), _ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(work),
+                         _sz(1))
+
+
+# ------------------------------------------- device entry points (torch data)
+def _colmajor_view(t):
+    """(ld, data_ptr) of a CUDA tensor holding a column-major matrix: shape
+    (m, n) with stride (1, ld)."""
+    if t.dim() != 2 or (t.stride(0) != 1 and t.shape[0] > 1):
+        raise ValueError("expected a column-major (m, n) tensor with stride (1, ld)")
+    return max(1, t.stride(1) if t.shape[1] > 1 else t.shape[0]), t.data_ptr()
+
+
+def _stream_ptr(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+def getrf_dev(A, ipiv, stream=None):
+    """xGETRF on device memory; A (m, n) column-major float64/float32 CUDA
+    tensor, ipiv int32 CUDA tensor of length min(m, n).  Returns INFO."""
+    import torch
+    ld, pa = _colmajor_view(A)
+    info = ctypes.c_int(0)
+    fn = lib().gb300_dgetrf_dev if A.dtype == torch.float64 else lib().gb300_sgetrf_dev
+    rc = fn(A.shape[0], A.shape[1], ctypes.c_void_p(pa), ld, ctypes.c_void_p(ipiv.data_ptr()), ctypes.byref(info),
+            _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 getrf failed with status {rc}")
+    return info.value
+
+
+def getrs_dev(A, ipiv, B, trans="N", stream=None):
+    import torch
+    ld, pa = _colmajor_view(A)
+    ldb, pb = _colmajor_view(B)
+    fn = lib().gb300_dgetrs_dev if A.dtype == torch.float64 else lib().gb300_sgetrs_dev
+    rc = fn(trans.encode(), A.shape[0], B.shape[1], ctypes.c_void_p(pa), ld, ctypes.c_void_p(ipiv.data_ptr()),
+            ctypes.c_void_p(pb), ldb, _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 getrs failed with status {rc}")
+
+
+def dsgesv_dev(A, ipiv, B, X, stream=None):
+    """DSGESV on device memory; returns (iter, info)."""
+    ld, pa = _colmajor_view(A)
+    ldb, pb = _colmajor_view(B)
+    ldx, px = _colmajor_view(X)
+    it = ctypes.c_int(0)
+    info = ctypes.c_int(0)
+    rc = lib().gb300_dsgesv_dev(A.shape[0], B.shape[1], ctypes.c_void_p(pa), ld, ctypes.c_void_p(ipiv.data_ptr()),
+                                ctypes.c_void_p(pb), ldb, ctypes.c_void_p(px), ldx, ctypes.byref(it),
+                                ctypes.byref(info), _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 dsgesv failed with status {rc}")
+    return it.value, info.value
+
+
+def colmajor_empty(m, n, dtype, device="cuda"):
+    """A column-major (m, n) CUDA tensor (stride (1, m))."""
+    import torch
+    return torch.empty((n, m), dtype=dtype, device=device).t()
+
+
+def to_colmajor(a_np, device="cuda"):
+    import torch
+    a = np.asarray(a_np)
+    return torch.from_numpy(np.ascontiguousarray(a.T)).to(device).t()

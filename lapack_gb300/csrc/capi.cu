@@ -1,0 +1,508 @@
+// C ABI of the library: the LAPACK Fortran-ABI routines (host pointers, the
+// library stages data through GPU memory inside each call) and the gb300_*
+// device-pointer entry points.
+#include "../../include/lapack_gb300.h"
+#include "driver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+using gb::DevScratch;
+using gb::options;
+
+namespace {
+
+// ------------------------------------------------------------ xerbla_
+std::mutex g_xerbla_mu;
+int g_xerbla_capture = 0;
+char g_xerbla_name[16] = {0};
+int g_xerbla_info = 0;
+
+bool lsame(char a, char b) { return (a | 0x20) == (b | 0x20); }
+
+void call_xerbla(const char* name, int info) {
+  lapack_int i = info;
+  xerbla_(name, &i, strlen(name));
+}
+
+// Per-host-thread non-blocking stream for the host-pointer routines.
+cudaStream_t thread_stream() {
+  thread_local cudaStream_t s = nullptr;
+  thread_local int dev_of_s = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!s || dev_of_s != dev) {
+    cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    dev_of_s = dev;
+  }
+  return s;
+}
+
+// A device failure inside a LAPACK-ABI routine has no reference INFO code;
+// it is reported on stderr and as INFO = -1000 - code.
+void device_failure(const char* name, int code, lapack_int* info) {
+  fprintf(stderr, "lapack_gb300: %s failed on the GPU (status %d: %s)\n", name, code,
+          code > 0 && code < 1000 ? cudaGetErrorString((cudaError_t)code) : "bounded wait or capacity");
+  if (info) *info = -1000 - code;
+}
+
+int finish(cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return (int)e;
+  int st = gb::check_status(gb::device_status_word(), s);
+  if (st != 0) {
+    int zero = 0;
+    cudaMemcpy(gb::device_status_word(), &zero, sizeof(int), cudaMemcpyHostToDevice);
+    return 1000 + st;
+  }
+  return 0;
+}
+
+template <typename T>
+int h2d(T* d, int ldd, const T* h, int ldh, int m, int n, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  return (int)cudaMemcpy2DAsync(d, sizeof(T) * (size_t)ldd, h, sizeof(T) * (size_t)ldh, sizeof(T) * (size_t)m, n,
+                                cudaMemcpyHostToDevice, s);
+}
+template <typename T>
+int d2h(T* h, int ldh, const T* d, int ldd, int m, int n, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  return (int)cudaMemcpy2DAsync(h, sizeof(T) * (size_t)ldh, d, sizeof(T) * (size_t)ldd, sizeof(T) * (size_t)m, n,
+                                cudaMemcpyDeviceToHost, s);
+}
+
+inline int ld_dev(int m) { return std::max(1, (m + 31) / 32 * 32); }
+
+// ------------------------------------------------------------ GETRF
+template <typename T>
+void getrf_host(const char* name, const lapack_int* m, const lapack_int* n, T* a, const lapack_int* lda,
+                lapack_int* ipiv, lapack_int* info, int nb, int gemm_mode) {
+  *info = 0;
+  if (*m < 0) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*lda < std::max(1, *m)) *info = -4;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*m == 0 || *n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M), mn = std::min(M, N);
+  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dP(sizeof(int) * (mn + 1), s);
+  if (!dA.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  int* dInfo = dP.as<int>() + mn;
+  int rc = h2d(dA.as<T>(), ld, a, *lda, M, N, s);
+  if (!rc) rc = gb::getrf_dev<T>(M, N, dA.as<T>(), ld, dP.as<int>(), dInfo, s, gemm_mode, nb);
+  if (!rc) rc = d2h(a, *lda, dA.as<T>(), ld, M, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.as<int>(), sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
+  int hinfo = 0;
+  if (!rc) rc = (int)cudaMemcpyAsync(&hinfo, dInfo, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure(name, rc, info); return; }
+  *info = hinfo;
+}
+
+// ------------------------------------------------------------ GETRS
+template <typename T>
+void getrs_host(const char* name, const char* trans, const lapack_int* n, const lapack_int* nrhs, const T* a,
+                const lapack_int* lda, const lapack_int* ipiv, T* b, const lapack_int* ldb, lapack_int* info) {
+  *info = 0;
+  const bool notran = lsame(*trans, 'N');
+  if (!notran && !lsame(*trans, 'T') && !lsame(*trans, 'C')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -8;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0 || *nrhs == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dB(sizeof(T) * (size_t)ld * R, s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<T>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::getrs_dev<T>(notran ? 'N' : 'T', N, R, dA.as<T>(), ld, dP.as<int>(), nullptr, dB.as<T>(), ld, s);
+  if (!rc) rc = d2h(b, *ldb, dB.as<T>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure(name, rc, info);
+}
+
+// ------------------------------------------------------------ GESV
+template <typename T>
+void gesv_host(const char* name, const lapack_int* n, const lapack_int* nrhs, T* a, const lapack_int* lda,
+               lapack_int* ipiv, T* b, const lapack_int* ldb, lapack_int* info, int nb, int gemm_mode) {
+  *info = 0;
+  if (*n < 0) *info = -1;
+  else if (*nrhs < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dB(sizeof(T) * (size_t)ld * std::max(R, 1), s),
+      dP(sizeof(int) * (N + 1), s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  int* dInfo = dP.as<int>() + N;
+  int hinfo = 0;
+  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<T>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::getrf_dev<T>(N, N, dA.as<T>(), ld, dP.as<int>(), dInfo, s, gemm_mode, nb);
+  if (!rc) rc = (int)cudaMemcpyAsync(&hinfo, dInfo, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (!rc && hinfo == 0 && R > 0)   // SRC/dgesv.f:166: solve only for a nonsingular U
+    rc = gb::getrs_dev<T>('N', N, R, dA.as<T>(), ld, dP.as<int>(), nullptr, dB.as<T>(), ld, s);
+  if (!rc) rc = d2h(a, *lda, dA.as<T>(), ld, N, N, s);
+  if (!rc && hinfo == 0) rc = d2h(b, *ldb, dB.as<T>(), ld, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure(name, rc, info); return; }
+  *info = hinfo;
+}
+
+// ------------------------------------------------------------ LASWP
+template <typename T>
+void laswp_host(const lapack_int* n, T* a, const lapack_int* lda, const lapack_int* k1, const lapack_int* k2,
+                const lapack_int* ipiv, const lapack_int* incx) {
+  // DLASWP has no argument checks and no INFO (SRC/dlaswp.f:136-150)
+  const int inc = *incx;
+  if (inc == 0 || *n <= 0) return;
+  const int K1 = *k1, K2 = *k2;
+  if (K2 < K1) return;
+  // the row window touched: rows K1..K2 and every interchange target
+  int lo = K1, hi = K2;
+  for (int i = K1; i <= K2; ++i) {
+    int p = ipiv[K1 - 1 + (i - K1) * std::abs(inc)];
+    lo = std::min(lo, p);
+    hi = std::max(hi, p);
+  }
+  if (lo < 1) return;   // the reference would index before A(1,.)
+  const int span = hi - lo + 1, N = *n, LDA = *lda;
+  const int nidx = K1 + (K2 - K1) * std::abs(inc);
+  cudaStream_t s = thread_stream();
+  // the device copy holds rows lo..hi only, so IPIV is re-based to that window
+  std::vector<int> shifted(ipiv, ipiv + nidx);
+  for (auto& v : shifted) v -= (lo - 1);
+  DevScratch dA(sizeof(T) * (size_t)span * N, s), dP(sizeof(int) * (size_t)nidx, s);
+  if (!dA.p || !dP.p) { device_failure("DLASWP", (int)cudaErrorMemoryAllocation, nullptr); return; }
+  int rc = h2d(dA.as<T>(), span, a + (lo - 1), LDA, span, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, shifted.data(), sizeof(int) * nidx, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::laswp_dev<T>(N, dA.as<T>(), span, K1 - (lo - 1), K2 - (lo - 1), dP.as<int>(), inc, 0, span, s);
+  if (!rc) rc = d2h(a + (lo - 1), LDA, dA.as<T>(), span, span, N, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure("DLASWP", rc, nullptr);
+}
+
+}  // namespace
+
+extern "C" {
+
+__attribute__((weak)) void xerbla_(const char* srname, const lapack_int* info, size_t len) {
+  char nm[16] = {0};
+  size_t l = std::min<size_t>(len, 15);
+  memcpy(nm, srname, l);
+  while (l > 0 && nm[l - 1] == ' ') nm[--l] = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_xerbla_mu);
+    memcpy(g_xerbla_name, nm, 16);
+    g_xerbla_info = *info;
+    if (g_xerbla_capture) return;
+  }
+  // SRC/xerbla.f:86-88
+  printf(" ** On entry to %s parameter number %2d had an illegal value\n", nm, *info);
+  fflush(stdout);
+  exit(0);
+}
+
+void gb300_xerbla_capture(int on) {
+  std::lock_guard<std::mutex> lk(g_xerbla_mu);
+  g_xerbla_capture = on;
+  g_xerbla_info = 0;
+  g_xerbla_name[0] = 0;
+}
+
+int gb300_xerbla_last(char* name, int cap) {
+  std::lock_guard<std::mutex> lk(g_xerbla_mu);
+  if (name && cap > 0) snprintf(name, (size_t)cap, "%s", g_xerbla_name);
+  return g_xerbla_info;
+}
+
+const char* gb300_version(void) { return "lapack_gb300 0.1 (sm_103a)"; }
+
+void dgetrf_(const lapack_int* m, const lapack_int* n, double* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info) {
+  getrf_host<double>("DGETRF", m, n, a, lda, ipiv, info, options().nb_f64, 0);
+}
+void sgetrf_(const lapack_int* m, const lapack_int* n, float* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info) {
+  getrf_host<float>("SGETRF", m, n, a, lda, ipiv, info, options().nb_f32, options().sgetrf_mode);
+}
+// DGETRF2 is the unblocked recursive panel routine of the reference; on the
+// GPU it runs the same recursion without an outer blocking loop.
+void dgetrf2_(const lapack_int* m, const lapack_int* n, double* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info) {
+  getrf_host<double>("DGETRF2", m, n, a, lda, ipiv, info, std::max(1, std::min(*m, *n)), 0);
+}
+void sgetrf2_(const lapack_int* m, const lapack_int* n, float* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info) {
+  getrf_host<float>("SGETRF2", m, n, a, lda, ipiv, info, std::max(1, std::min(*m, *n)), options().sgetrf_mode);
+}
+void dgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const double* a, const lapack_int* lda,
+             const lapack_int* ipiv, double* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  getrs_host<double>("DGETRS", trans, n, nrhs, a, lda, ipiv, b, ldb, info);
+}
+void sgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const float* a, const lapack_int* lda,
+             const lapack_int* ipiv, float* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  getrs_host<float>("SGETRS", trans, n, nrhs, a, lda, ipiv, b, ldb, info);
+}
+void dgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda, lapack_int* ipiv,
+            double* b, const lapack_int* ldb, lapack_int* info) {
+  gesv_host<double>("DGESV ", n, nrhs, a, lda, ipiv, b, ldb, info, options().nb_f64, 0);
+}
+void sgesv_(const lapack_int* n, const lapack_int* nrhs, float* a, const lapack_int* lda, lapack_int* ipiv,
+            float* b, const lapack_int* ldb, lapack_int* info) {
+  gesv_host<float>("SGESV ", n, nrhs, a, lda, ipiv, b, ldb, info, options().nb_f32, options().sgetrf_mode);
+}
+void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1, const lapack_int* k2,
+             const lapack_int* ipiv, const lapack_int* incx) {
+  laswp_host<double>(n, a, lda, k1, k2, ipiv, incx);
+}
+void slaswp_(const lapack_int* n, float* a, const lapack_int* lda, const lapack_int* k1, const lapack_int* k2,
+             const lapack_int* ipiv, const lapack_int* incx) {
+  laswp_host<float>(n, a, lda, k1, k2, ipiv, incx);
+}
+
+void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda, lapack_int* ipiv,
+             const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double*, float*,
+             lapack_int* iter, lapack_int* info) {
+  *info = 0;
+  *iter = 0;
+  if (*n < 0) *info = -1;
+  else if (*nrhs < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  else if (*ldx < std::max(1, *n)) *info = -9;
+  if (*info != 0) { call_xerbla("DSGESV", -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dB(sizeof(double) * (size_t)ld * std::max(R, 1), s),
+      dX(sizeof(double) * (size_t)ld * std::max(R, 1), s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dX.p || !dP.p) { device_failure("DSGESV", (int)cudaErrorMemoryAllocation, info); return; }
+  int it = 0, inf = 0;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::dsgesv_dev(N, R, dA.as<double>(), ld, dP.as<int>(), dB.as<double>(), ld, dX.as<double>(), ld,
+                               &it, &inf, s);
+  if (!rc) rc = finish(s);
+  // A is returned unchanged when ITER >= 0 and holds the FP64 LU otherwise
+  if (!rc && it < 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
+  if (!rc && inf == 0) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DSGESV", rc, info); return; }
+  *iter = it;
+  *info = inf;
+}
+
+void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
+             const lapack_int* ldsa, lapack_int* info) {
+  // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
+  // stops at the first |a| > SLAMCH('O') with INFO = 1, leaving later
+  // elements of SA untouched.
+  *info = 0;
+  if (*m <= 0 || *n <= 0) return;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dS(sizeof(float) * (size_t)ld * N, s);
+  if (!dA.p || !dS.p) { device_failure("DLAG2S", (int)cudaErrorMemoryAllocation, info); return; }
+  long long first = -1;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, M, N, s);
+  if (!rc) rc = h2d(dS.as<float>(), ld, sa, *ldsa, M, N, s);   // keeps the untouched tail on overflow
+  if (!rc) rc = gb::dlag2s_dev(M, N, dA.as<double>(), ld, dS.as<float>(), ld, &first, s);
+  if (!rc) rc = d2h(sa, *ldsa, dS.as<float>(), ld, M, N, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DLAG2S", rc, info); return; }
+  *info = first >= 0 ? 1 : 0;
+}
+void slag2d_(const lapack_int* m, const lapack_int* n, const float* sa, const lapack_int* ldsa, double* a,
+             const lapack_int* lda, lapack_int* info) {
+  *info = 0;
+  if (*m <= 0 || *n <= 0) return;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dS(sizeof(float) * (size_t)ld * N, s);
+  if (!dA.p || !dS.p) { device_failure("SLAG2D", (int)cudaErrorMemoryAllocation, info); return; }
+  int rc = h2d(dS.as<float>(), ld, sa, *ldsa, M, N, s);
+  if (!rc) rc = gb::slag2d_dev(M, N, dS.as<float>(), ld, dA.as<double>(), ld, s);
+  if (!rc) rc = d2h(a, *lda, dA.as<double>(), ld, M, N, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure("SLAG2D", rc, info);
+}
+
+double dlamch_(const char* c, size_t) {
+  switch (*c | 0x20) {
+    case 'e': return 1.1102230246251565e-16;
+    case 's': return 2.2250738585072014e-308;
+    case 'o': return 1.7976931348623157e308;
+    case 'p': return 2.220446049250313e-16;
+    case 'b': return 2.0;
+    case 'u': return 2.2250738585072014e-308;
+    case 'n': return 53.0;
+    case 'r': return 1.0;
+    case 'm': return -1021.0;
+    case 'l': return 1024.0;
+    default: return 0.0;
+  }
+}
+float slamch_(const char* c, size_t) {
+  switch (*c | 0x20) {
+    case 'e': return 5.96046448e-08f;
+    case 's': return 1.17549435e-38f;
+    case 'o': return 3.40282347e38f;
+    case 'p': return 1.1920929e-07f;
+    case 'b': return 2.0f;
+    case 'u': return 1.17549435e-38f;
+    case 'n': return 24.0f;
+    case 'r': return 1.0f;
+    case 'm': return -125.0f;
+    case 'l': return 128.0f;
+    default: return 0.0f;
+  }
+}
+
+double dlange_(const char* norm, const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda,
+               double* work, size_t) {
+  (void)work;
+  if (std::min(*m, *n) <= 0) return 0.0;
+  int which;
+  if (lsame(*norm, 'M')) which = 0;
+  else if (lsame(*norm, 'O') || *norm == '1') which = 1;
+  else if (lsame(*norm, 'I')) which = 2;
+  else if (lsame(*norm, 'F') || lsame(*norm, 'E')) which = 3;
+  else return 0.0;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s);
+  if (!dA.p) { device_failure("DLANGE", (int)cudaErrorMemoryAllocation, nullptr); return 0.0; }
+  double v = 0.0;
+  int err = h2d(dA.as<double>(), ld, a, *lda, M, N, s);
+  if (!err) err = gb::dlange_dev(which, M, N, dA.as<double>(), ld, &v, s);
+  if (!err) err = finish(s);
+  if (err) device_failure("DLANGE", err, nullptr);
+  return v;
+}
+
+// ------------------------------------------------------ device entry points
+int gb300_dgetrf_dev(int m, int n, double* dA, int lda, int* dIpiv, int* info, void* stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, m)) return -4;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevScratch di(sizeof(int), s);
+  if (!di.p) return (int)cudaErrorMemoryAllocation;
+  int rc = gb::getrf_dev<double>(m, n, dA, lda, dIpiv, di.as<int>(), s, 0, options().nb_f64);
+  int h = 0;
+  if (!rc) rc = (int)cudaMemcpyAsync(&h, di.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (info) *info = h;
+  return rc;
+}
+int gb300_sgetrf_dev(int m, int n, float* dA, int lda, int* dIpiv, int* info, void* stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, m)) return -4;
+  cudaStream_t s = (cudaStream_t)stream;
+  DevScratch di(sizeof(int), s);
+  if (!di.p) return (int)cudaErrorMemoryAllocation;
+  int rc = gb::getrf_dev<float>(m, n, dA, lda, dIpiv, di.as<int>(), s, options().sgetrf_mode, options().nb_f32);
+  int h = 0;
+  if (!rc) rc = (int)cudaMemcpyAsync(&h, di.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (info) *info = h;
+  return rc;
+}
+int gb300_dgetrs_dev(char trans, int n, int nrhs, const double* dA, int lda, const int* dIpiv, double* dB, int ldb,
+                     void* stream) {
+  if (!lsame(trans, 'N') && !lsame(trans, 'T') && !lsame(trans, 'C')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, n)) return -8;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::getrs_dev<double>(lsame(trans, 'N') ? 'N' : 'T', n, nrhs, dA, lda, dIpiv, nullptr, dB, ldb, s);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+int gb300_sgetrs_dev(char trans, int n, int nrhs, const float* dA, int lda, const int* dIpiv, float* dB, int ldb,
+                     void* stream) {
+  if (!lsame(trans, 'N') && !lsame(trans, 'T') && !lsame(trans, 'C')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, n)) return -8;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::getrs_dev<float>(lsame(trans, 'N') ? 'N' : 'T', n, nrhs, dA, lda, dIpiv, nullptr, dB, ldb, s);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+int gb300_dgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, double* dB, int ldb, int* info, void* stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  if (ldb < std::max(1, n)) return -7;
+  int h = 0;
+  int rc = gb300_dgetrf_dev(n, n, dA, lda, dIpiv, &h, stream);
+  if (!rc && h == 0 && n > 0 && nrhs > 0) rc = gb300_dgetrs_dev('N', n, nrhs, dA, lda, dIpiv, dB, ldb, stream);
+  if (info) *info = h;
+  return rc;
+}
+int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX,
+                     int ldx, int* iter, int* info, void* stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  if (ldb < std::max(1, n)) return -7;
+  if (ldx < std::max(1, n)) return -9;
+  cudaStream_t s = (cudaStream_t)stream;
+  int it = 0, inf = 0;
+  int rc = gb::dsgesv_dev(n, nrhs, dA, lda, dIpiv, dB, ldb, dX, ldx, &it, &inf, s);
+  if (!rc) rc = finish(s);
+  if (iter) *iter = it;
+  if (info) *info = inf;
+  return rc;
+}
+
+int gb300_set_option(const char* name, int value) {
+  gb::Options& o = options();
+  int old;
+  if (!strcmp(name, "exact")) { old = o.exact; o.exact = value != 0; }
+  else if (!strcmp(name, "nb64")) { old = o.nb_f64; o.nb_f64 = std::max(1, value); }
+  else if (!strcmp(name, "nb32")) { old = o.nb_f32; o.nb_f32 = std::max(1, value); }
+  else if (!strcmp(name, "mixed")) { old = o.mixed_mode; o.mixed_mode = value; }
+  else if (!strcmp(name, "sgetrf")) { old = o.sgetrf_mode; o.sgetrf_mode = value; }
+  else return -1;
+  return old;
+}
+int gb300_get_option(const char* name) {
+  gb::Options& o = options();
+  if (!strcmp(name, "exact")) return o.exact;
+  if (!strcmp(name, "nb64")) return o.nb_f64;
+  if (!strcmp(name, "nb32")) return o.nb_f32;
+  if (!strcmp(name, "mixed")) return o.mixed_mode;
+  if (!strcmp(name, "sgetrf")) return o.sgetrf_mode;
+  return -1;
+}
+int gb300_status(int clear) {
+  int* w = gb::device_status_word();
+  if (!w) return -1;
+  int h = 0;
+  cudaMemcpy(&h, w, sizeof(int), cudaMemcpyDeviceToHost);
+  if (clear) cudaMemset(w, 0, sizeof(int));
+  return h;
+}
+
+}  // extern "C"

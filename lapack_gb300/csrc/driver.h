@@ -1,0 +1,75 @@
+// Internal host-side interface of the GB300 LU solve library.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+
+namespace gb {
+
+// How the FP32 factorization inside DSGESV computes its trailing updates.
+enum MixedMode : int {
+  kMixedBf16x3 = 0,   // tcgen05 BF16 tensor cores, hi*hi + hi*lo + lo*hi, FP32 accumulation
+  kMixedFp32 = 1,     // FFMA on the CUDA cores (the SGETRF arithmetic)
+};
+
+struct Options {
+  bool exact = false;       // separately rounded products (bitwise reference order)
+  int nb_f64 = 64;          // outer block size of the FP64 factorization
+  int nb_f32 = 256;         // outer block size of the FP32 factorization
+  int mixed_mode = kMixedFp32;
+  int sgetrf_mode = kMixedFp32;   // sgetrf_ itself: plain FP32 by default
+};
+Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
+
+int device_sm_count();
+
+// Scratch device memory, stream ordered (cudaMallocAsync / cudaFreeAsync).
+struct DevScratch {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DevScratch() = default;
+  DevScratch(size_t bytes, cudaStream_t st);
+  ~DevScratch();
+  DevScratch(const DevScratch&) = delete;
+  DevScratch& operator=(const DevScratch&) = delete;
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Device-pointer routines.  Return 0 or a CUDA / status error code; the
+// LAPACK INFO goes to the device int *dInfo.  All work is queued on `s`.
+template <typename T>
+int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb);
+template <typename T>
+int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
+              T* dB, int ldb, cudaStream_t s);
+// Gather permutation of a factorization: position r of P*A holds row perm[r].
+int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s);
+template <typename T>
+int laswp_dev(int ncols, T* dA, int lda, int k1, int k2, const int* dIpiv, int incx, int lo, int span,
+              cudaStream_t s);
+template <typename T>
+int gemm_update_dev(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+                    cudaStream_t s, int gemm_mode);
+template <typename T>
+int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode);
+
+// BF16x3 tensor-core update C -= A*B for FP32 operands (tcgen05).
+int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                    cudaStream_t s);
+
+// DSGESV on device memory.  *iter and *info are host outputs.
+int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
+               int* iter, int* info, cudaStream_t s);
+double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, int* err);
+// DLANGE on device memory: which = 0 'M', 1 '1', 2 'I', 3 'F'.  *out is a
+// host double, valid after the stream synchronises.
+int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, cudaStream_t s);
+// DLAG2S with the reference's stop-at-first-overflow semantics; *first
+// (host) receives the column-major index of the first overflow or -1.
+int dlag2s_dev(int m, int n, const double* dA, int lda, float* dS, int lds, long long* first, cudaStream_t s);
+int slag2d_dev(int m, int n, const float* dS, int lds, double* dA, int lda, cudaStream_t s);
+
+// Kernel launch status of the last failing bounded wait, 0 if none.
+int check_status(int* dStatus, cudaStream_t s);
+int* device_status_word();
+
+}  // namespace gb

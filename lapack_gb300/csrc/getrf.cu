@@ -1,0 +1,373 @@
+// Host orchestration of DGETRF / SGETRF and DGETRS / SGETRS on one GPU.
+//
+// DGETRF (SRC/dgetrf.f:174-219) is a blocked right-looking LU: for each
+// block column of width NB, factor the panel (SRC/dgetrf2.f, here a
+// recursion whose leaves of width <= 64 are the cooperative panel kernel),
+// apply its interchanges to the other columns, form the block row of U with
+// a triangular solve, then update the trailing matrix with one GEMM.
+#include "driver.h"
+#include "gemm_simt.cuh"
+#include "lu_kernels.cuh"
+#include "solve_kernels.cuh"
+
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+
+namespace gb {
+
+// ----------------------------------------------------------------- options
+static int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  return (v && *v) ? atoi(v) : dflt;
+}
+
+Options& options() {
+  static Options o = [] {
+    Options x;
+    x.exact = env_int("LAPACK_GB300_EXACT", 0) != 0;
+    x.nb_f64 = std::max(1, env_int("LAPACK_GB300_NB64", 64));
+    x.nb_f32 = std::max(1, env_int("LAPACK_GB300_NB32", 256));
+    const char* mm = getenv("LAPACK_GB300_MIXED");
+    if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
+    if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
+    const char* sm = getenv("LAPACK_GB300_SGETRF");
+    if (sm && strcmp(sm, "bf16x3") == 0) x.sgetrf_mode = kMixedBf16x3;
+    return x;
+  }();
+  return o;
+}
+
+int device_sm_count() {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static int cache[64] = {0};
+  if (dev < 64 && cache[dev]) return cache[dev];
+  int n = 0;
+  cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+  if (dev < 64) cache[dev] = n;
+  return n;
+}
+
+DevScratch::DevScratch(size_t bytes, cudaStream_t st) : s(st) {
+  if (bytes && cudaMallocAsync(&p, bytes, st) != cudaSuccess) p = nullptr;
+}
+DevScratch::~DevScratch() {
+  if (p) cudaFreeAsync(p, s);
+}
+
+int check_status(int* dStatus, cudaStream_t s) {
+  int h = 0;
+  if (cudaMemcpyAsync(&h, dStatus, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+  if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+  return h;
+}
+
+// Per-device status word written by kernels whose bounded waits ran out.
+int* device_status_word() {
+  static std::mutex mu;
+  static int* words[64] = {nullptr};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  if (!words[dev]) {
+    int* p = nullptr;
+    if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, sizeof(int));
+    cudaDeviceSynchronize();
+    // keep stream-ordered scratch cached between calls instead of returning it to the OS
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    words[dev] = p;
+  }
+  return words[dev];
+}
+
+// ------------------------------------------------------------------- GEMM
+template <>
+int gemm_update_dev<double>(int M, int N, int K, const double* A, int lda, const double* B, int ldb, double* C,
+                            int ldc, cudaStream_t s, int) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  dim3 grid((M + 127) / 128, (N + 63) / 64);
+  if (options().exact)
+    gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  else
+    gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  return (int)cudaGetLastError();
+}
+
+template <>
+int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                           cudaStream_t s, int mode) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  if (mode == kMixedBf16x3) return gemm_bf16x3_dev(M, N, K, A, lda, B, ldb, C, ldc, s);
+  dim3 grid((M + 127) / 128, (N + 127) / 128);
+  if (options().exact)
+    gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  else
+    gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  return (int)cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- TRSM
+// B := L^{-1} B, L unit lower k x k: 64-wide leaves, GEMM for the coupling.
+template <typename T>
+int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode) {
+  if (k <= 0 || ncols <= 0) return 0;
+  if (k <= kLeafMax) {
+    int grid = (ncols + TrsmSlab<T>::BC - 1) / TrsmSlab<T>::BC;
+    if (options().exact)
+      trsm_llnu_leaf_kernel<T, true><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols);
+    else
+      trsm_llnu_leaf_kernel<T, false><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols);
+    return (int)cudaGetLastError();
+  }
+  int k1 = ((k / 2) + kLeafMax - 1) / kLeafMax * kLeafMax;
+  if (k1 >= k) k1 = kLeafMax;
+  int rc = trsm_llnu_dev<T>(k1, ncols, L, ldl, B, ldb, s, gemm_mode);
+  if (rc) return rc;
+  rc = gemm_update_dev<T>(k - k1, ncols, k1, L + k1, ldl, B, ldb, B + k1, ldb, s, gemm_mode);
+  if (rc) return rc;
+  return trsm_llnu_dev<T>(k - k1, ncols, L + k1 + (size_t)k1 * ldl, ldl, B + k1, ldb, s, gemm_mode);
+}
+template int trsm_llnu_dev<double>(int, int, const double*, int, double*, int, cudaStream_t, int);
+template int trsm_llnu_dev<float>(int, int, const float*, int, float*, int, cudaStream_t, int);
+
+// ------------------------------------------------------------------ panel
+template <typename T>
+struct PanelCtx {
+  PanelScratch<T> ps;
+  int* status;
+  int max_optin;
+};
+
+template <typename T, bool EXACT>
+static int launch_leaf(T* P, int lda, int M, int JB, int row0, int* ipiv, int* info, PanelCtx<T>& cx,
+                       cudaStream_t s) {
+  const int nsm = device_sm_count();
+  int R = std::max(32, (M + nsm - 1) / nsm);
+  int G = (M + R - 1) / R;
+  size_t smem = (size_t)JB * R * sizeof(T) + (size_t)R * sizeof(int) + 16;
+  auto kern = leaf_panel_kernel<T, EXACT>;
+  static bool attr_done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const int dyn_cap = cx.max_optin - 2048;
+  if (!attr_done[dev]) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap);
+    attr_done[dev] = true;
+  }
+  if ((long long)smem > dyn_cap) return 1000 + kStatusCapacity;   // panel taller than the GPU's shared memory holds
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kPanelThreads, smem);
+  if (occ * nsm < G) return 1000 + kStatusCapacity;
+  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.counter, 0, 2 * sizeof(int), s));
+  PanelScratch<T> ps = cx.ps;
+  int* status = cx.status;
+  void* args[] = {&P, &lda, &M, &JB, &R, &row0, &ipiv, &info, &ps, &status};
+  return (int)cudaLaunchCooperativeKernel((void*)kern, G, kPanelThreads, args, smem, s);
+}
+
+template <typename T>
+static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, PanelCtx<T>& cx, cudaStream_t s) {
+  int warps = c0 + (ncols - c1);
+  if (warps <= 0) return 0;
+  int blocks = (warps * 32 + 255) / 256;
+  laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(A, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
+                                                cx.ps.pair_count, ntop);
+  return (int)cudaGetLastError();
+}
+
+// DGETRF2-shaped recursion on the panel of columns [c0, c0+w), rows [c0, m).
+// Each leaf applies its interchanges to every other column of the matrix
+// (left: the DLASWP of SRC/dgetrf.f:193, right: SRC/dgetrf2.f:236 and
+// SRC/dgetrf.f:199), so the recursion never re-applies them.
+template <typename T>
+static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int* info, PanelCtx<T>& cx,
+                     cudaStream_t s, int gemm_mode) {
+  if (w <= kLeafMax) {
+    T* P = A + c0 + (size_t)c0 * lda;
+    int rc = options().exact ? launch_leaf<T, true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                             : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+    if (rc) return rc;
+    return laswp_pairs<T>(A, lda, n, c0, c0 + w, w, cx, s);
+  }
+  int n1 = ((w / 2) + 31) / 32 * 32;
+  if (n1 >= w) n1 = w / 2;
+  int rc = getrf_rec<T>(A, lda, m, n, c0, n1, ipiv, info, cx, s, gemm_mode);
+  if (rc) return rc;
+  T* A11 = A + c0 + (size_t)c0 * lda;
+  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gemm_mode);
+  if (rc) return rc;
+  rc = gemm_update_dev<T>(m - c0 - n1, w - n1, n1, A11 + n1, lda, A11 + (size_t)n1 * lda, lda,
+                          A11 + n1 + (size_t)n1 * lda, lda, s, gemm_mode);
+  if (rc) return rc;
+  return getrf_rec<T>(A, lda, m, n, c0 + n1, w - n1, ipiv, info, cx, s, gemm_mode);
+}
+
+template <typename T>
+int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb) {
+  GB_CUDA_TRY(cudaMemsetAsync(dInfo, 0, sizeof(int), s));
+  if (m <= 0 || n <= 0) return 0;
+  const int nsm = device_sm_count();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int G = nsm;
+  size_t bytes = 0;
+  auto carve = [&](size_t b) { size_t off = bytes; bytes += (b + 255) / 256 * 256; return off; };
+  size_t o_cand = carve(sizeof(Cand<T>) * 2 * G);
+  size_t o_clab = carve(sizeof(int) * 2 * G);
+  size_t o_crow = carve(sizeof(T) * 2 * G * kLeafMax);
+  size_t o_rowk = carve(sizeof(T) * 2 * kLeafMax);
+  size_t o_rkl = carve(sizeof(int) * 2);
+  size_t o_ctl = carve(sizeof(int) * 2);
+  size_t o_pd = carve(sizeof(int) * 2 * kLeafMax);
+  size_t o_psrc = carve(sizeof(int) * 2 * kLeafMax);
+  DevScratch ws(bytes, s);
+  if (!ws.p) return (int)cudaErrorMemoryAllocation;
+  char* base = ws.as<char>();
+  PanelCtx<T> cx;
+  cx.ps.cand = reinterpret_cast<Cand<T>*>(base + o_cand);
+  cx.ps.cand_label = reinterpret_cast<int*>(base + o_clab);
+  cx.ps.cand_row = reinterpret_cast<T*>(base + o_crow);
+  cx.ps.row_k = reinterpret_cast<T*>(base + o_rowk);
+  cx.ps.row_k_label = reinterpret_cast<int*>(base + o_rkl);
+  cx.ps.counter = reinterpret_cast<unsigned*>(base + o_ctl);
+  cx.ps.pair_count = reinterpret_cast<int*>(base + o_ctl) + 1;
+  cx.ps.pair_dst = reinterpret_cast<int*>(base + o_pd);
+  cx.ps.pair_src = reinterpret_cast<int*>(base + o_psrc);
+  cx.status = device_status_word();
+  cx.max_optin = optin;
+  if (!cx.status) return (int)cudaErrorMemoryAllocation;
+
+  const int mn = std::min(m, n);
+  if (nb < 1) nb = 1;
+  for (int j = 0; j < mn; j += nb) {
+    const int jb = std::min(nb, mn - j);
+    int rc = getrf_rec<T>(dA, lda, m, n, j, jb, dIpiv, dInfo, cx, s, gemm_mode);
+    if (rc) return rc;
+    if (j + jb < n) {
+      T* Ajj = dA + j + (size_t)j * lda;
+      rc = trsm_llnu_dev<T>(jb, n - j - jb, Ajj, lda, Ajj + (size_t)jb * lda, lda, s, gemm_mode);
+      if (rc) return rc;
+      if (j + jb < m) {
+        rc = gemm_update_dev<T>(m - j - jb, n - j - jb, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,
+                                Ajj + jb + (size_t)jb * lda, lda, s, gemm_mode);
+        if (rc) return rc;
+      }
+    }
+  }
+  return (int)cudaGetLastError();
+}
+template int getrf_dev<double>(int, int, double*, int, int*, int*, cudaStream_t, int, int);
+template int getrf_dev<float>(int, int, float*, int, int*, int*, cudaStream_t, int, int);
+
+// ------------------------------------------------------------- permutation
+int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s) {
+  if (span <= 0) return 0;
+  int* status = device_status_word();
+  if (!status) return (int)cudaErrorMemoryAllocation;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  size_t smem = (size_t)span * sizeof(int);
+  if ((long long)smem <= optin - 1024) {
+    static bool attr[64] = {false};
+    if (!attr[dev]) {
+      cudaFuncSetAttribute(ipiv_to_perm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
+      attr[dev] = true;
+    }
+    ipiv_to_perm_kernel<true><<<1, 1024, smem, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, nullptr, status);
+  } else {
+    DevScratch lab(smem, s);
+    if (!lab.p) return (int)cudaErrorMemoryAllocation;
+    ipiv_to_perm_kernel<false><<<1, 1024, 0, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, lab.as<int>(), status);
+  }
+  return (int)cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- DLASWP
+// General DLASWP (SRC/dlaswp.f) on device memory.  The caller names the row
+// window [lo, lo+span) that holds rows K1..K2 and every IPIV target; the
+// interchanges are replayed into a permutation of that window, the window
+// is gathered out, then copied back.  Rows are 1-based in IPIV.
+template <typename T>
+int laswp_dev(int ncols, T* dA, int lda, int k1, int k2, const int* dIpiv, int incx, int lo, int span,
+              cudaStream_t s) {
+  if (ncols <= 0 || incx == 0 || span <= 0) return 0;
+  DevScratch perm(sizeof(int) * (size_t)span, s);
+  DevScratch tmp(sizeof(T) * (size_t)span * ncols, s);
+  if (!perm.p || !tmp.p) return (int)cudaErrorMemoryAllocation;
+  int rc = ipiv_perm_dev(dIpiv, k1, k2, incx, lo, span, perm.as<int>(), s);
+  if (rc) return rc;
+  size_t tot = (size_t)span * ncols;
+  unsigned blocks = (unsigned)((tot + 255) / 256);
+  perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dA, lda, tmp.as<T>(), span, perm.as<int>(), 0, span, ncols);
+  copy_cols_kernel<T><<<blocks, 256, 0, s>>>(tmp.as<T>(), span, dA + lo, lda, span, ncols);
+  return (int)cudaGetLastError();
+}
+template int laswp_dev<double>(int, double*, int, int, int, const int*, int, int, int, cudaStream_t);
+template int laswp_dev<float>(int, float*, int, int, int, const int*, int, int, int, cudaStream_t);
+
+// ------------------------------------------------------------------- GETRS
+template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
+static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s) {
+  const int nblk = (n + kSolveBS - 1) / kSolveBS;
+  DevScratch ctl(sizeof(int) * (size_t)(nblk + 1), s);
+  if (!ctl.p) return (int)cudaErrorMemoryAllocation;
+  GB_CUDA_TRY(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (size_t)(nblk + 1), s));
+  int* flags = ctl.as<int>();
+  unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
+  trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, flags, ticket,
+                                                                        device_status_word());
+  return (int)cudaGetLastError();
+}
+
+template <typename T, bool EXACT>
+static int getrs_impl(char trans, int n, int nrhs, const T* dA, int lda, const int* dPerm, T* dB, int ldb,
+                      cudaStream_t s) {
+  DevScratch w(sizeof(T) * (size_t)n * nrhs, s);
+  if (!w.p) return (int)cudaErrorMemoryAllocation;
+  T* W = w.as<T>();
+  size_t tot = (size_t)n * nrhs;
+  unsigned blocks = (unsigned)((tot + 255) / 256);
+  int rc;
+  if (trans == 'N') {
+    perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dB, ldb, W, n, dPerm, 0, n, nrhs);
+    if ((rc = launch_trsv<T, EXACT, true, true, false>(dA, lda, n, W, n, nrhs, s))) return rc;
+    if ((rc = launch_trsv<T, EXACT, false, false, false>(dA, lda, n, W, n, nrhs, s))) return rc;
+    copy_cols_kernel<T><<<blocks, 256, 0, s>>>(W, n, dB, ldb, n, nrhs);
+  } else {
+    copy_cols_kernel<T><<<blocks, 256, 0, s>>>(dB, ldb, W, n, n, nrhs);
+    if ((rc = launch_trsv<T, EXACT, true, false, true>(dA, lda, n, W, n, nrhs, s))) return rc;
+    if ((rc = launch_trsv<T, EXACT, false, true, true>(dA, lda, n, W, n, nrhs, s))) return rc;
+    perm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(W, n, dB, ldb, dPerm, 0, n, nrhs);
+  }
+  return (int)cudaGetLastError();
+}
+
+template <typename T>
+int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm, T* dB, int ldb,
+              cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return 0;
+  DevScratch permbuf(dPerm ? 0 : sizeof(int) * (size_t)n, s);
+  if (!dPerm) {
+    if (!permbuf.p) return (int)cudaErrorMemoryAllocation;
+    int rc = ipiv_perm_dev(dIpiv, 1, n, 1, 0, n, permbuf.as<int>(), s);
+    if (rc) return rc;
+    dPerm = permbuf.as<int>();
+  }
+  char t = (trans == 'n' || trans == 'N') ? 'N' : 'T';
+  return options().exact ? getrs_impl<T, true>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s)
+                         : getrs_impl<T, false>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s);
+}
+template int getrs_dev<double>(char, int, int, const double*, int, const int*, const int*, double*, int, cudaStream_t);
+template int getrs_dev<float>(char, int, int, const float*, int, const int*, const int*, float*, int, cudaStream_t);
+
+}  // namespace gb

@@ -1,0 +1,414 @@
+// LAPACKE C interface over the Fortran-ABI routines of this library.
+// Semantics follow the reference wrappers (LAPACKE/src/lapacke_<name>.c and
+// lapacke_<name>_work.c): layout check (-1), optional NaN check of the
+// inputs (on by default, LAPACKE_NANCHECK / LAPACKE_set_nancheck), INFO
+// shifted by one for the extra layout argument, row-major inputs transposed
+// into column-major scratch, IPIV left as the row indices of the transposed
+// problem, and the reference's leading-dimension error codes.
+#include "../../include/lapack_gb300.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+namespace {
+
+void* (*g_malloc)(size_t) = malloc;
+void (*g_free)(void*) = free;
+int g_nancheck = -1;
+
+template <typename T>
+bool ge_has_nan(int layout, lapack_int m, lapack_int n, const T* a, lapack_int lda) {
+  // LAPACKE/utils/lapacke_dge_nancheck.c: scan min(m, lda) rows of n columns
+  // (column major) or min(n, lda) columns of m rows (row major)
+  if (!a) return false;
+  if (layout == LAPACK_COL_MAJOR) {
+    for (lapack_int j = 0; j < n; ++j)
+      for (lapack_int i = 0; i < std::min(m, lda); ++i)
+        if (a[i + (size_t)j * lda] != a[i + (size_t)j * lda]) return true;
+  } else {
+    for (lapack_int i = 0; i < m; ++i)
+      for (lapack_int j = 0; j < std::min(n, lda); ++j)
+        if (a[(size_t)i * lda + j] != a[(size_t)i * lda + j]) return true;
+  }
+  return false;
+}
+
+// Layout change of an m x n matrix given in `layout` (LAPACKE/utils/
+// lapacke_dge_trans.c): out(j, i) = in(i, j), clipped by the leading
+// dimensions exactly as the reference does.
+template <typename T>
+void ge_trans(int layout, lapack_int m, lapack_int n, const T* in, lapack_int ldin, T* out, lapack_int ldout) {
+  if (!in || !out) return;
+  lapack_int x, y;
+  if (layout == LAPACK_COL_MAJOR) { x = n; y = m; }
+  else if (layout == LAPACK_ROW_MAJOR) { x = m; y = n; }
+  else return;
+  for (lapack_int i = 0; i < std::min(y, ldin); ++i)
+    for (lapack_int j = 0; j < std::min(x, ldout); ++j) out[(size_t)i * ldout + j] = in[(size_t)j * ldin + i];
+}
+
+template <typename T>
+T* alloc(size_t count) { return static_cast<T*>(LAPACKE_malloc_proxy(sizeof(T) * std::max<size_t>(1, count))); }
+
+bool nancheck() { return LAPACKE_get_nancheck() != 0; }
+
+// ---- GESV
+template <typename T, typename F>
+lapack_int gesv_work(const char* nm, F fort, int layout, lapack_int n, lapack_int nrhs, T* a, lapack_int lda,
+                     lapack_int* ipiv, T* b, lapack_int ldb) {
+  lapack_int info = 0;
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&n, &nrhs, a, &lda, ipiv, b, &ldb, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -8); return -8; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  T* b_t = alloc<T>((size_t)ldb_t * std::max(1, nrhs));
+  if (!b_t) { LAPACKE_free_proxy(a_t); LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  fort(&n, &nrhs, a_t, &lda_t, ipiv, b_t, &ldb_t, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, n, a_t, lda_t, a, lda);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, b_t, ldb_t, b, ldb);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+
+// ---- GETRF / GETRF2
+template <typename T, typename F>
+lapack_int getrf_work(const char* nm, F fort, int layout, lapack_int m, lapack_int n, T* a, lapack_int lda,
+                      lapack_int* ipiv) {
+  lapack_int info = 0;
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&m, &n, a, &lda, ipiv, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, m);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, m, n, a, lda, a_t, lda_t);
+  fort(&m, &n, a_t, &lda_t, ipiv, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, m, n, a_t, lda_t, a, lda);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+
+// ---- GETRS
+template <typename T, typename F>
+lapack_int getrs_work(const char* nm, F fort, int layout, char trans, lapack_int n, lapack_int nrhs, const T* a,
+                      lapack_int lda, const lapack_int* ipiv, T* b, lapack_int ldb) {
+  lapack_int info = 0;
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&trans, &n, &nrhs, a, &lda, ipiv, b, &ldb, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -6); return -6; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -9); return -9; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  T* b_t = alloc<T>((size_t)ldb_t * std::max(1, nrhs));
+  if (!b_t) { LAPACKE_free_proxy(a_t); LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  fort(&trans, &n, &nrhs, a_t, &lda_t, ipiv, b_t, &ldb_t, &info, 1);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, b_t, ldb_t, b, ldb);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+
+// ---- LASWP
+template <typename T, typename F>
+lapack_int laswp_work(const char* nm, F fort, int layout, lapack_int n, T* a, lapack_int lda, lapack_int k1,
+                      lapack_int k2, const lapack_int* ipiv, lapack_int incx) {
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&n, a, &lda, &k1, &k2, ipiv, &incx);
+    return 0;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  // rows referenced: up to K2 and every IPIV target (LAPACKE/src/lapacke_dlaswp_work.c)
+  lapack_int lda_t = std::max(1, k2);
+  for (lapack_int i = k1; i <= k2; ++i) lda_t = std::max(lda_t, ipiv[k1 + (i - k1) * std::abs(incx) - 1]);
+  if (lda < n) { LAPACKE_xerbla(nm, -4); return -4; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, lda_t, n, a, lda, a_t, lda_t);
+  fort(&n, a_t, &lda_t, &k1, &k2, ipiv, &incx);
+  ge_trans(LAPACK_COL_MAJOR, lda_t, n, a_t, lda_t, a, lda);
+  LAPACKE_free_proxy(a_t);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* LAPACKE_malloc_proxy(size_t size) { return g_malloc(size); }
+void LAPACKE_free_proxy(void* ptr) { g_free(ptr); }
+void LAPACKE_set_alloc(void* (*malloc_fn)(size_t), void (*free_fn)(void*)) {
+  g_malloc = malloc_fn ? malloc_fn : malloc;
+  g_free = free_fn ? free_fn : free;
+}
+
+void LAPACKE_set_nancheck(int flag) { g_nancheck = flag ? 1 : 0; }
+int LAPACKE_get_nancheck(void) {
+  if (g_nancheck != -1) return g_nancheck;
+  const char* env = getenv("LAPACKE_NANCHECK");   // read once; enabled unless set to 0
+  g_nancheck = env ? (atoi(env) ? 1 : 0) : 1;
+  return g_nancheck;
+}
+
+void LAPACKE_xerbla(const char* name, lapack_int info) {
+  // LAPACKE/utils/lapacke_xerbla.c messages
+  if (info == LAPACK_WORK_MEMORY_ERROR) printf("Not enough memory to allocate work array in %s\n", name);
+  else if (info == LAPACK_TRANSPOSE_MEMORY_ERROR) printf("Not enough memory to transpose matrix in %s\n", name);
+  else if (info < 0) printf("Wrong parameter %d in %s\n", -(int)info, name);
+}
+
+// ---------------------------------------------------------------- GESV
+lapack_int LAPACKE_dgesv_work(int layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda, lapack_int* ipiv,
+                              double* b, lapack_int ldb) {
+  return gesv_work<double>("LAPACKE_dgesv_work", dgesv_, layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_sgesv_work(int layout, lapack_int n, lapack_int nrhs, float* a, lapack_int lda, lapack_int* ipiv,
+                              float* b, lapack_int ldb) {
+  return gesv_work<float>("LAPACKE_sgesv_work", sgesv_, layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_dgesv(int layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda, lapack_int* ipiv,
+                         double* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  return LAPACKE_dgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_sgesv(int layout, lapack_int n, lapack_int nrhs, float* a, lapack_int lda, lapack_int* ipiv,
+                         float* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_sgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  return LAPACKE_sgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+
+// ---------------------------------------------------------------- GETRF
+lapack_int LAPACKE_dgetrf_work(int layout, lapack_int m, lapack_int n, double* a, lapack_int lda, lapack_int* ipiv) {
+  return getrf_work<double>("LAPACKE_dgetrf_work", dgetrf_, layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_dgetrf2_work(int layout, lapack_int m, lapack_int n, double* a, lapack_int lda, lapack_int* ipiv) {
+  return getrf_work<double>("LAPACKE_dgetrf2_work", dgetrf2_, layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_sgetrf_work(int layout, lapack_int m, lapack_int n, float* a, lapack_int lda, lapack_int* ipiv) {
+  return getrf_work<float>("LAPACKE_sgetrf_work", sgetrf_, layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_dgetrf(int layout, lapack_int m, lapack_int n, double* a, lapack_int lda, lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgetrf", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, a, lda)) return -4;
+  return LAPACKE_dgetrf_work(layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_dgetrf2(int layout, lapack_int m, lapack_int n, double* a, lapack_int lda, lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgetrf2", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, a, lda)) return -4;
+  return LAPACKE_dgetrf2_work(layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_sgetrf(int layout, lapack_int m, lapack_int n, float* a, lapack_int lda, lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_sgetrf", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, a, lda)) return -4;
+  return LAPACKE_sgetrf_work(layout, m, n, a, lda, ipiv);
+}
+
+// ---------------------------------------------------------------- GETRS
+lapack_int LAPACKE_dgetrs_work(int layout, char trans, lapack_int n, lapack_int nrhs, const double* a, lapack_int lda,
+                               const lapack_int* ipiv, double* b, lapack_int ldb) {
+  return getrs_work<double>("LAPACKE_dgetrs_work", dgetrs_, layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_sgetrs_work(int layout, char trans, lapack_int n, lapack_int nrhs, const float* a, lapack_int lda,
+                               const lapack_int* ipiv, float* b, lapack_int ldb) {
+  return getrs_work<float>("LAPACKE_sgetrs_work", sgetrs_, layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_dgetrs(int layout, char trans, lapack_int n, lapack_int nrhs, const double* a, lapack_int lda,
+                          const lapack_int* ipiv, double* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgetrs", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -8;
+  }
+  return LAPACKE_dgetrs_work(layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_sgetrs(int layout, char trans, lapack_int n, lapack_int nrhs, const float* a, lapack_int lda,
+                          const lapack_int* ipiv, float* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_sgetrs", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -8;
+  }
+  return LAPACKE_sgetrs_work(layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+
+// ---------------------------------------------------------------- DSGESV
+lapack_int LAPACKE_dsgesv_work(int layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda, lapack_int* ipiv,
+                               const double* b, lapack_int ldb, double* x, lapack_int ldx, double* work, float* swork,
+                               lapack_int* iter) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dsgesv_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dsgesv_(&n, &nrhs, a, &lda, ipiv, b, &ldb, x, &ldx, work, swork, iter, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n), ldx_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -8); return -8; }
+  if (ldx < nrhs) { LAPACKE_xerbla(nm, -10); return -10; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  double* b_t = a_t ? alloc<double>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  double* x_t = b_t ? alloc<double>((size_t)ldx_t * std::max(1, nrhs)) : nullptr;
+  if (!x_t) {
+    if (b_t) LAPACKE_free_proxy(b_t);
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  dsgesv_(&n, &nrhs, a_t, &lda_t, ipiv, b_t, &ldb_t, x_t, &ldx_t, work, swork, iter, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, n, a_t, lda_t, a, lda);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, x_t, ldx_t, x, ldx);
+  LAPACKE_free_proxy(x_t);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dsgesv(int layout, lapack_int n, lapack_int nrhs, double* a, lapack_int lda, lapack_int* ipiv,
+                          const double* b, lapack_int ldb, double* x, lapack_int ldx, lapack_int* iter) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dsgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  // WORK / SWORK as LAPACKE_dsgesv sizes them (LAPACKE/src/lapacke_dsgesv.c:59-68)
+  float* swork = alloc<float>((size_t)std::max(1, n) * std::max(1, n + nrhs));
+  double* work = swork ? alloc<double>((size_t)std::max(1, n) * std::max(1, nrhs)) : nullptr;
+  if (!work) {
+    if (swork) LAPACKE_free_proxy(swork);
+    LAPACKE_xerbla("LAPACKE_dsgesv", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_dsgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb, x, ldx, work, swork, iter);
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(swork);
+  return info;
+}
+
+// ---------------------------------------------------------------- LASWP
+lapack_int LAPACKE_dlaswp_work(int layout, lapack_int n, double* a, lapack_int lda, lapack_int k1, lapack_int k2,
+                               const lapack_int* ipiv, lapack_int incx) {
+  return laswp_work<double>("LAPACKE_dlaswp_work", dlaswp_, layout, n, a, lda, k1, k2, ipiv, incx);
+}
+lapack_int LAPACKE_slaswp_work(int layout, lapack_int n, float* a, lapack_int lda, lapack_int k1, lapack_int k2,
+                               const lapack_int* ipiv, lapack_int incx) {
+  return laswp_work<float>("LAPACKE_slaswp_work", slaswp_, layout, n, a, lda, k1, k2, ipiv, incx);
+}
+lapack_int LAPACKE_dlaswp(int layout, lapack_int n, double* a, lapack_int lda, lapack_int k1, lapack_int k2,
+                          const lapack_int* ipiv, lapack_int incx) {
+  // the reference disables the NaN check of DLASWP (LAPACKE/src/lapacke_dlaswp.c:44-58)
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dlaswp", -1); return -1; }
+  return LAPACKE_dlaswp_work(layout, n, a, lda, k1, k2, ipiv, incx);
+}
+lapack_int LAPACKE_slaswp(int layout, lapack_int n, float* a, lapack_int lda, lapack_int k1, lapack_int k2,
+                          const lapack_int* ipiv, lapack_int incx) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_slaswp", -1); return -1; }
+  return LAPACKE_slaswp_work(layout, n, a, lda, k1, k2, ipiv, incx);
+}
+
+// ---------------------------------------------------------------- LAG2S / LAG2D
+lapack_int LAPACKE_dlag2s_work(int layout, lapack_int m, lapack_int n, const double* a, lapack_int lda, float* sa,
+                               lapack_int ldsa) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dlag2s_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dlag2s_(&m, &n, a, &lda, sa, &ldsa, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, m), ldsa_t = std::max(1, m);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  if (ldsa < n) { LAPACKE_xerbla(nm, -7); return -7; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  float* sa_t = a_t ? alloc<float>((size_t)ldsa_t * std::max(1, n)) : nullptr;
+  if (!sa_t) {
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, m, n, a, lda, a_t, lda_t);
+  dlag2s_(&m, &n, a_t, &lda_t, sa_t, &ldsa_t, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, m, n, sa_t, ldsa_t, sa, ldsa);
+  LAPACKE_free_proxy(sa_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dlag2s(int layout, lapack_int m, lapack_int n, const double* a, lapack_int lda, float* sa,
+                          lapack_int ldsa) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dlag2s", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, a, lda)) return -4;
+  return LAPACKE_dlag2s_work(layout, m, n, a, lda, sa, ldsa);
+}
+lapack_int LAPACKE_slag2d_work(int layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa, double* a,
+                               lapack_int lda) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_slag2d_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    slag2d_(&m, &n, sa, &ldsa, a, &lda, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int ldsa_t = std::max(1, m), lda_t = std::max(1, m);
+  if (lda < n) { LAPACKE_xerbla(nm, -7); return -7; }
+  if (ldsa < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  float* sa_t = alloc<float>((size_t)ldsa_t * std::max(1, n));
+  double* a_t = sa_t ? alloc<double>((size_t)lda_t * std::max(1, n)) : nullptr;
+  if (!a_t) {
+    if (sa_t) LAPACKE_free_proxy(sa_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, m, n, sa, ldsa, sa_t, ldsa_t);
+  slag2d_(&m, &n, sa_t, &ldsa_t, a_t, &lda_t, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, m, n, a_t, lda_t, a, lda);
+  LAPACKE_free_proxy(a_t);
+  LAPACKE_free_proxy(sa_t);
+  return info;
+}
+lapack_int LAPACKE_slag2d(int layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa, double* a,
+                          lapack_int lda) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_slag2d", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, sa, ldsa)) return -4;
+  return LAPACKE_slag2d_work(layout, m, n, sa, ldsa, a, lda);
+}
+
+}  // extern "C"

@@ -1,0 +1,189 @@
+// DSGESV on the GPU (SRC/dsgesv.f:243-429): FP32 LU of a converted copy of
+// A, FP32 solves, FP64 residual / update / convergence test on the device,
+// ITERMAX = 30 refinement steps, then the FP64 DGETRF/DGETRS fallback with
+// the reference's ITER codes (-2 conversion overflow, -3 FP32 LU singular,
+// -31 no convergence).
+#include "driver.h"
+#include "solve_kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+namespace gb {
+
+double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, int* err) {
+  *err = 0;
+  if (m <= 0 || n <= 0) return 0.0;
+  DevScratch buf(sizeof(double) * ((size_t)m + 1), s);
+  if (!buf.p) { *err = (int)cudaErrorMemoryAllocation; return 0.0; }
+  double* rows = buf.as<double>();
+  row_abs_sum_kernel<double><<<(m + 63) / 64, 64, 0, s>>>(dA, lda, m, n, rows);
+  max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, m, rows + m);
+  double h = 0;
+  cudaMemcpyAsync(&h, rows + m, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) *err = (int)cudaGetLastError();
+  return h;
+}
+
+static int residual(int n, int nrhs, const double* A, int lda, const double* X, int ldx, const double* B, int ldb,
+                    double* R, int ldr, cudaStream_t s) {
+  unsigned grid = (unsigned)((n + kResidRows - 1) / kResidRows);
+  if (options().exact)
+    residual_kernel<true><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs);
+  else
+    residual_kernel<false><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs);
+  return (int)cudaGetLastError();
+}
+
+static unsigned blocks_for(size_t n) { return (unsigned)((n + 255) / 256); }
+
+int dlag2s_dev(int m, int n, const double* dA, int lda, float* dS, int lds, long long* first, cudaStream_t s) {
+  *first = -1;
+  if (m <= 0 || n <= 0) return 0;
+  DevScratch f(sizeof(unsigned long long), s);
+  if (!f.p) return (int)cudaErrorMemoryAllocation;
+  GB_CUDA_TRY(cudaMemsetAsync(f.p, 0xff, sizeof(unsigned long long), s));
+  size_t tot = (size_t)m * n;
+  first_overflow_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, f.as<unsigned long long>());
+  lag2s_upto_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, dS, lds, m, n, f.as<unsigned long long>());
+  unsigned long long h = 0;
+  GB_CUDA_TRY(cudaMemcpyAsync(&h, f.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  *first = (h == ~0ull) ? -1 : (long long)h;
+  return 0;
+}
+
+int slag2d_dev(int m, int n, const float* dS, int lds, double* dA, int lda, cudaStream_t s) {
+  if (m <= 0 || n <= 0) return 0;
+  slag2d_kernel<<<blocks_for((size_t)m * n), 256, 0, s>>>(dS, lds, dA, lda, m, n);
+  return (int)cudaGetLastError();
+}
+
+int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, cudaStream_t s) {
+  *out = 0.0;
+  if (m <= 0 || n <= 0) return 0;
+  if (which == 2) {
+    int err = 0;
+    *out = dlange_inf_dev(m, n, dA, lda, s, &err);
+    return err;
+  }
+  size_t tot = (size_t)m * n;
+  if (which == 1) {
+    DevScratch cs(sizeof(double) * ((size_t)n + 1), s);
+    if (!cs.p) return (int)cudaErrorMemoryAllocation;
+    col_abs_sum_kernel<double><<<(n + 31) / 32, 1024, 0, s>>>(dA, lda, m, n, cs.as<double>());
+    max_nan_kernel<double><<<1, 1024, 0, s>>>(cs.as<double>(), n, cs.as<double>() + n);
+    GB_CUDA_TRY(cudaMemcpyAsync(out, cs.as<double>() + n, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return 0;
+  }
+  DevScratch w(32, s);
+  if (!w.p) return (int)cudaErrorMemoryAllocation;
+  GB_CUDA_TRY(cudaMemsetAsync(w.p, 0, 32, s));
+  unsigned long long* bits = w.as<unsigned long long>();
+  int* nanflag = reinterpret_cast<int*>(w.as<char>() + 8);
+  double* acc = reinterpret_cast<double*>(w.as<char>() + 16);
+  max_abs_kernel<double><<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, nanflag);
+  if (which == 3) sumsq_scaled_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, acc);
+  unsigned long long hb = 0;
+  int hn = 0;
+  double ha = 0;
+  GB_CUDA_TRY(cudaMemcpyAsync(&hb, bits, 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&hn, nanflag, 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&ha, acc, 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  double mx;
+  memcpy(&mx, &hb, 8);
+  if (hn) { *out = NAN; return 0; }
+  if (which == 0) { *out = mx; return 0; }
+  *out = (mx > 0 && !std::isinf(mx)) ? mx * std::sqrt(ha) : mx;   // Frobenius by scaled sum of squares
+  return 0;
+}
+
+
+int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
+               int* iter, int* info, cudaStream_t s) {
+  const int itermax = 30;
+  *iter = 0;
+  *info = 0;
+  if (n == 0) return 0;
+  const Options& opt = options();
+  // device scratch: SA (n x n FP32), SX (n x nrhs FP32), R (n x nrhs FP64),
+  // the gather permutation, ||A||_inf, flags
+  size_t nn = (size_t)n * n, nr = (size_t)n * nrhs;
+  size_t bytes = 0;
+  auto carve = [&](size_t b) { size_t off = bytes; bytes += (b + 255) / 256 * 256; return off; };
+  size_t o_sa = carve(sizeof(float) * nn);
+  size_t o_sx = carve(sizeof(float) * nr);
+  size_t o_r = carve(sizeof(double) * nr);
+  size_t o_perm = carve(sizeof(int) * n);
+  size_t o_anrm = carve(sizeof(double));
+  size_t o_flags = carve(sizeof(int) * 4);     // [0] overflow, [1] notconv, [2] sgetrf info
+  DevScratch ws(bytes, s);
+  if (!ws.p) return (int)cudaErrorMemoryAllocation;
+  char* base = ws.as<char>();
+  float* SA = reinterpret_cast<float*>(base + o_sa);
+  float* SX = reinterpret_cast<float*>(base + o_sx);
+  double* R = reinterpret_cast<double*>(base + o_r);
+  int* perm = reinterpret_cast<int*>(base + o_perm);
+  double* anrm = reinterpret_cast<double*>(base + o_anrm);
+  int* flags = reinterpret_cast<int*>(base + o_flags);
+  int hflags[4];
+  int rc;
+
+  // ANRM = DLANGE('I'), kept on the device for the convergence test
+  {
+    DevScratch rows(sizeof(double) * (size_t)n, s);
+    if (!rows.p) return (int)cudaErrorMemoryAllocation;
+    row_abs_sum_kernel<double><<<(n + 63) / 64, 64, 0, s>>>(dA, lda, n, n, rows.as<double>());
+    max_nan_kernel<double><<<1, 1024, 0, s>>>(rows.as<double>(), n, anrm);
+  }
+  GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
+  // SX = DLAG2S(B), SA = DLAG2S(A)
+  dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags);
+  dlag2s_kernel<<<blocks_for(nn), 256, 0, s>>>(dA, lda, SA, n, n, n, flags);
+  GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hflags[0]) { *iter = -2; goto fallback; }
+  // SGETRF(SA)
+  rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32);
+  if (rc) return rc;
+  GB_CUDA_TRY(cudaMemcpyAsync(hflags + 2, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hflags[2] != 0) { *iter = -3; goto fallback; }
+  if ((rc = ipiv_perm_dev(dIpiv, 1, n, 1, 0, n, perm, s))) return rc;
+  // SX = SA^{-1} SX, X = SLAG2D(SX), R = B - A X
+  if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
+  slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs);
+  if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
+  ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr);
+  GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hflags[1] == 0) { *iter = 0; return 0; }
+  for (int it = 1; it <= itermax; ++it) {
+    GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2, s));
+    dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(R, n, SX, n, n, nrhs, flags);
+    if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
+    lag2d_axpy_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs);
+    if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
+    ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr);
+    GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hflags[0]) { *iter = -2; goto fallback; }
+    if (hflags[1] == 0) { *iter = it; return 0; }
+  }
+  *iter = -itermax - 1;
+fallback:
+  // FP64 DGETRF on A in place, X = B, DGETRS (SRC/dsgesv.f:415-429)
+  rc = getrf_dev<double>(n, n, dA, lda, dIpiv, flags + 3, s, 0, opt.nb_f64);
+  if (rc) return rc;
+  GB_CUDA_TRY(cudaMemcpyAsync(hflags + 3, flags + 3, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  *info = hflags[3];
+  if (*info != 0) return 0;
+  copy_cols_kernel<double><<<blocks_for(nr), 256, 0, s>>>(dB, ldb, dX, ldx, n, nrhs);
+  return getrs_dev<double>('N', n, nrhs, dA, lda, dIpiv, nullptr, dX, ldx, s);
+}
+
+}  // namespace gb

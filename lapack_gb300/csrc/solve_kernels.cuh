@@ -1,0 +1,418 @@
+// Kernels of the solve phase (DGETRS) and of the mixed-precision refinement
+// driver (DSGESV): row permutations, blocked triangular solves, norms,
+// precision conversions and the FP64 residual.
+#pragma once
+#include "common.cuh"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// IPIV -> permutation.  DLASWP (SRC/dlaswp.f:138-183) applies the
+// interchanges one after another; the net effect on rows lo..lo+span-1 is a
+// permutation, computed here by replaying the swaps on row labels.  After
+// the replay, position r holds original row perm[r] (a gather index).  One
+// CTA; `lab` is shared memory when the window fits, global scratch
+// otherwise.  An IPIV entry outside the window is reported through `status`
+// and skipped (the reference would index out of bounds).
+template <bool SHARED>
+__global__ void __launch_bounds__(1024)
+ipiv_to_perm_kernel(const int* __restrict__ ipiv, int k1, int k2, int incx, int lo, int span,
+                    int* __restrict__ perm_out, int* __restrict__ lab_global, int* __restrict__ status) {
+  extern __shared__ int lab_sh[];
+  int* lab = SHARED ? lab_sh : lab_global;
+  for (int i = threadIdx.x; i < span; i += blockDim.x) lab[i] = lo + i;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int i1, i2, inc, ix;
+    if (incx > 0) { i1 = k1; i2 = k2; inc = 1; ix = k1; }
+    else { i1 = k2; i2 = k1; inc = -1; ix = k1 + (k1 - k2) * incx; }
+    for (int i = i1;; i += inc) {
+      int p = ipiv[ix - 1];
+      int a = i - 1 - lo, b = p - 1 - lo;
+      if (a >= 0 && a < span && b >= 0 && b < span) {
+        if (a != b) { int t = lab[a]; lab[a] = lab[b]; lab[b] = t; }
+      } else {
+        atomicCAS(status, kStatusOk, kStatusCapacity);
+      }
+      ix += incx;
+      if (i == i2) break;
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < span; i += blockDim.x) perm_out[i] = lab[i];
+}
+
+// W(r, s) = B(perm[r], s)  (gather), or W(perm[r], s) = B(r, s)  (scatter).
+template <typename T, bool SCATTER>
+__global__ void perm_rows_kernel(const T* __restrict__ B, int ldb, T* __restrict__ W, int ldw,
+                                 const int* __restrict__ perm, int perm_base, int n, int ncols) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t total = (size_t)n * ncols;
+  if (e >= total) return;
+  int c = (int)(e / n), r = (int)(e - (size_t)c * n);
+  int p = perm[r] - perm_base;
+  if (SCATTER) W[(size_t)p + (size_t)c * ldw] = B[(size_t)r + (size_t)c * ldb];
+  else W[(size_t)r + (size_t)c * ldw] = B[(size_t)p + (size_t)c * ldb];
+}
+
+template <typename T>
+__global__ void copy_cols_kernel(const T* __restrict__ S, int lds, T* __restrict__ D, int ldd, int m, int ncols) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * ncols) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  D[(size_t)r + (size_t)c * ldd] = S[(size_t)r + (size_t)c * lds];
+}
+
+// ---------------------------------------------------------------------------
+// Blocked triangular solve with several right-hand sides, X := op(T)^{-1} X,
+// for the four DGETRS cases (SRC/dgetrs.f:187-217 calling
+// BLAS/SRC/dtrsm.f:272-329).  The matrix is cut into 64-row blocks; CTAs
+// take blocks in solve order from a ticket counter, fold in the finished
+// blocks as they complete (a per-block flag, released after the block's
+// solution is written), then solve their diagonal block.  Every wait is
+// bounded.  FORWARD: blocks in increasing order (L, or U^T); otherwise
+// decreasing (U, or L^T).  TRANS reads T(k, r) for element (r, k).
+// In increasing / decreasing order of k each element receives its updates in
+// the reference loop order (N cases and U^T); the L^T case folds k in
+// decreasing order, which the reference folds in increasing order.
+constexpr int kSolveBS = 64;
+constexpr int kSolveRQ = 4;   // right-hand sides per pass (256 threads = 64 rows x 4)
+
+template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
+__global__ void __launch_bounds__(256)
+trsv_blocked_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, int ldx, int nrhs,
+                    int* __restrict__ flags, unsigned* __restrict__ ticket, int* __restrict__ status) {
+  __shared__ T tile[kSolveBS][kSolveBS + 1];
+  __shared__ T xsrc[kSolveBS][kSolveRQ];
+  __shared__ T xs[kSolveBS][kSolveRQ];
+  __shared__ unsigned t_s;
+  __shared__ int ok_s;
+  const int tid = threadIdx.x;
+  const int r = tid & 63, q = tid >> 6;
+  const int nblk = (n + kSolveBS - 1) / kSolveBS;
+  if (tid == 0) t_s = atomicAdd(ticket, 1u);
+  __syncthreads();
+  const int t = (int)t_s;
+  const int bi = FORWARD ? t : nblk - 1 - t;
+  const int r0 = bi * kSolveBS;
+  const int nr = min(kSolveBS, n - r0);
+  auto tile_elem = [&](int row, int col) -> T {   // op(T)(row, col), global indices
+    return TRANS ? A[(size_t)col + (size_t)row * lda] : A[(size_t)row + (size_t)col * lda];
+  };
+  bool ok = true;
+  for (int q0 = 0; q0 < nrhs; q0 += kSolveRQ) {
+    const int s = q0 + q;
+    const bool active = (r < nr) && (s < nrhs);
+    T acc = active ? X[(size_t)(r0 + r) + (size_t)s * ldx] : T(0);
+    const int nsrc = FORWARD ? bi : nblk - 1 - bi;
+    for (int step = 0; step < nsrc; ++step) {
+      const int bj = FORWARD ? step : nblk - 1 - step;
+      const int c0 = bj * kSolveBS;
+      const int nc = min(kSolveBS, n - c0);
+      if (q0 == 0) {
+        if (tid == 0) {
+          unsigned spins = 0;
+          int okk = 1;
+          while (ld_acquire_s32(flags + bj) == 0) {
+            if (++spins > kSpinLimit || *(volatile int*)status != kStatusOk) {
+              atomicCAS(status, kStatusOk, kStatusFlagTimeout);
+              okk = 0;
+              break;
+            }
+            __nanosleep(32);
+          }
+          ok_s = okk;
+        }
+        __syncthreads();
+        if (!ok_s) { ok = false; break; }
+      }
+      for (int e = tid; e < kSolveBS * kSolveBS; e += 256) {
+        // consecutive threads walk the contiguous index of the stored matrix
+        int rr, cc;
+        if (TRANS) { rr = e / kSolveBS; cc = e - rr * kSolveBS; }
+        else { cc = e / kSolveBS; rr = e - cc * kSolveBS; }
+        if (rr < nr && cc < nc) tile[rr][cc] = tile_elem(r0 + rr, c0 + cc);
+      }
+      for (int e = tid; e < nc * kSolveRQ; e += 256) {
+        int cc = e % nc, qq = e / nc;
+        xsrc[cc][qq] = (q0 + qq < nrhs) ? ldcg(X + (size_t)(c0 + cc) + (size_t)(q0 + qq) * ldx) : T(0);
+      }
+      __syncthreads();
+      if (active) {
+        if (FORWARD) {
+          for (int kk = 0; kk < nc; ++kk) acc = fnmadd<EXACT>(tile[r][kk], xsrc[kk][q], acc);
+        } else {
+          for (int kk = nc - 1; kk >= 0; --kk) acc = fnmadd<EXACT>(tile[r][kk], xsrc[kk][q], acc);
+        }
+      }
+      __syncthreads();
+    }
+    if (!ok) break;
+    // diagonal block
+    for (int e = tid; e < kSolveBS * kSolveBS; e += 256) {
+      int rr, cc;
+      if (TRANS) { rr = e / kSolveBS; cc = e - rr * kSolveBS; }
+      else { cc = e / kSolveBS; rr = e - cc * kSolveBS; }
+      if (rr < nr && cc < nr) tile[rr][cc] = tile_elem(r0 + rr, r0 + cc);
+    }
+    xs[r][q] = acc;
+    __syncthreads();
+    if (FORWARD) {
+      for (int k = 0; k < nr; ++k) {
+        if (!UNIT) {
+          if (r == k && active) xs[k][q] = xs[k][q] / tile[k][k];
+          __syncthreads();
+        }
+        if (active && r > k) xs[r][q] = fnmadd<EXACT>(tile[r][k], xs[k][q], xs[r][q]);
+        __syncthreads();
+      }
+    } else {
+      for (int k = nr - 1; k >= 0; --k) {
+        if (!UNIT) {
+          if (r == k && active) xs[k][q] = xs[k][q] / tile[k][k];
+          __syncthreads();
+        }
+        if (active && r < k) xs[r][q] = fnmadd<EXACT>(tile[r][k], xs[k][q], xs[r][q]);
+        __syncthreads();
+      }
+    }
+    if (active) X[(size_t)(r0 + r) + (size_t)s * ldx] = xs[r][q];
+    __syncthreads();
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release_s32(flags + bi, ok ? 1 : -1);
+}
+
+// ---------------------------------------------------------------------------
+// DLANGE('I') (SRC/dlange.f:173-189): row absolute sums in column order,
+// then the maximum with NaN propagation.  One thread per row keeps the
+// reference summation order; 32 independent loads are kept in flight.
+template <typename T>
+__global__ void __launch_bounds__(64)
+row_abs_sum_kernel(const T* __restrict__ A, int lda, int m, int n, T* __restrict__ rowsum) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const T* p = A + i;
+  T s = 0;
+  int j = 0;
+  for (; j + 32 <= n; j += 32) {
+    T v[32];
+#pragma unroll
+    for (int u = 0; u < 32; ++u) v[u] = p[(size_t)(j + u) * lda];
+#pragma unroll
+    for (int u = 0; u < 32; ++u) s = s + (v[u] < 0 ? -v[u] : v[u]);
+  }
+  for (; j < n; ++j) {
+    T v = p[(size_t)j * lda];
+    s = s + (v < 0 ? -v : v);
+  }
+  rowsum[i] = s;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024)
+max_nan_kernel(const T* __restrict__ x, int m, T* __restrict__ out) {
+  __shared__ T red[32];
+  __shared__ int nan_s;
+  if (threadIdx.x == 0) nan_s = 0;
+  __syncthreads();
+  T v = 0;
+  int hasnan = 0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    T t = x[i];
+    if (t != t) hasnan = 1;
+    else if (t > v) v = t;
+  }
+  if (hasnan) nan_s = 1;
+  for (int off = 16; off > 0; off >>= 1) { T o = __shfl_xor_sync(0xffffffffu, v, off); v = o > v ? o : v; }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = (threadIdx.x < (blockDim.x + 31) / 32) ? red[threadIdx.x] : T(0);
+    for (int off = 16; off > 0; off >>= 1) { T o = __shfl_xor_sync(0xffffffffu, v, off); v = o > v ? o : v; }
+    if (threadIdx.x == 0) *out = nan_s ? T(NAN) : v;
+  }
+}
+
+// DLAG2S (SRC/dlag2s.f:135-146): FP64 -> FP32, flag = 1 if any |a| > FLT_MAX
+// (a NaN passes, as in the reference).
+static __global__ void dlag2s_kernel(const double* __restrict__ A, int lda, float* __restrict__ S, int lds, int m, int n,
+                              int* __restrict__ overflow) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  double v = A[(size_t)r + (size_t)c * lda];
+  const double rmax = 3.4028234663852886e38;
+  if (v < -rmax || v > rmax) *overflow = 1;
+  S[(size_t)r + (size_t)c * lds] = (float)v;
+}
+
+// SLAG2D (SRC/slag2d.f:123-128).
+static __global__ void slag2d_kernel(const float* __restrict__ S, int lds, double* __restrict__ A, int lda, int m, int n) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  A[(size_t)r + (size_t)c * lda] = (double)S[(size_t)r + (size_t)c * lds];
+}
+
+// SLAG2D followed by DAXPY with alpha = 1 (SRC/dsgesv.f:373-377):
+// X(:,j) := X(:,j) + double(SX(:,j)).
+static __global__ void lag2d_axpy_kernel(const float* __restrict__ S, int lds, double* __restrict__ X, int ldx, int n, int nrhs) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)n * nrhs) return;
+  int c = (int)(e / n), r = (int)(e - (size_t)c * n);
+  X[(size_t)r + (size_t)c * ldx] = X[(size_t)r + (size_t)c * ldx] + (double)S[(size_t)r + (size_t)c * lds];
+}
+
+// R = B - A*X in FP64 (DLACPY + DGEMM('N','N', alpha=-1, beta=1),
+// SRC/dsgesv.f:328-332): one thread per row, columns folded in increasing
+// order as the reference DGEMM does; up to 16 right-hand sides per pass so
+// A is read once for nrhs <= 16.  X chunks are staged in shared memory.
+constexpr int kResidRows = 64;
+constexpr int kResidMaxRhs = 16;
+template <bool EXACT>
+__global__ void __launch_bounds__(kResidRows)
+residual_kernel(const double* __restrict__ A, int lda, const double* __restrict__ X, int ldx,
+                const double* __restrict__ B, int ldb, double* __restrict__ R, int ldr, int n, int nrhs) {
+  __shared__ double xs[32][kResidMaxRhs];
+  const int i = blockIdx.x * kResidRows + threadIdx.x;
+  for (int q0 = 0; q0 < nrhs; q0 += kResidMaxRhs) {
+    const int nq = min(kResidMaxRhs, nrhs - q0);
+    double acc[kResidMaxRhs];
+#pragma unroll
+    for (int q = 0; q < kResidMaxRhs; ++q) acc[q] = (i < n && q < nq) ? B[(size_t)i + (size_t)(q0 + q) * ldb] : 0.0;
+    for (int l0 = 0; l0 < n; l0 += 32) {
+      const int nl = min(32, n - l0);
+      __syncthreads();
+      for (int e = threadIdx.x; e < 32 * kResidMaxRhs; e += kResidRows) {
+        int l = e % 32, q = e / 32;
+        xs[l][q] = (l < nl && q < nq) ? X[(size_t)(l0 + l) + (size_t)(q0 + q) * ldx] : 0.0;
+      }
+      __syncthreads();
+      if (i < n) {
+        double a[32];
+#pragma unroll
+        for (int u = 0; u < 32; ++u) a[u] = (u < nl) ? A[(size_t)i + (size_t)(l0 + u) * lda] : 0.0;
+#pragma unroll
+        for (int u = 0; u < 32; ++u) {
+          if (u < nl) {
+#pragma unroll
+            for (int q = 0; q < kResidMaxRhs; ++q)
+              if (q < nq) acc[q] = fnmadd<EXACT>(xs[u][q], a[u], acc[q]);
+          }
+        }
+      }
+    }
+    if (i < n) {
+#pragma unroll
+      for (int q = 0; q < kResidMaxRhs; ++q)
+        if (q < nq) R[(size_t)i + (size_t)(q0 + q) * ldr] = acc[q];
+    }
+  }
+}
+
+// Convergence test of SRC/dsgesv.f:337-342 for every right-hand side:
+// XNRM = |X(IDAMAX(X(:,j)),j)|, RNRM likewise, not converged when
+// RNRM > XNRM*CTE with CTE = ||A||_inf * eps * sqrt(n).  One CTA per
+// right-hand side; `notconv` counts the failing ones.
+static __global__ void __launch_bounds__(256)
+ir_check_kernel(const double* __restrict__ X, int ldx, const double* __restrict__ R, int ldr, int n,
+                const double* __restrict__ anrm, int* __restrict__ notconv, double* __restrict__ norms_out) {
+  __shared__ Cand<double> red[2][8];
+  const int j = blockIdx.x, tid = threadIdx.x;
+  Cand<double> bx{0, -1, -1}, br{0, -1, -1};
+  for (int i = tid; i < n; i += 256) {
+    Cand<double> cx = make_cand(X[(size_t)i + (size_t)j * ldx], i, 0);
+    Cand<double> cr = make_cand(R[(size_t)i + (size_t)j * ldr], i, 0);
+    if (cand_better(cx, bx)) bx = cx;
+    if (cand_better(cr, br)) br = cr;
+  }
+  bx = warp_best(bx);
+  br = warp_best(br);
+  if ((tid & 31) == 0) { red[0][tid >> 5] = bx; red[1][tid >> 5] = br; }
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 1; w < 8; ++w) {
+      if (cand_better(red[0][w], red[0][0])) red[0][0] = red[0][w];
+      if (cand_better(red[1][w], red[1][0])) red[1][0] = red[1][w];
+    }
+    int ix = red[0][0].row, ir = red[1][0].row;
+    double xv = ix >= 0 ? X[(size_t)ix + (size_t)j * ldx] : 0.0;
+    double rv = ir >= 0 ? R[(size_t)ir + (size_t)j * ldr] : 0.0;
+    double xnrm = fabs(xv), rnrm = fabs(rv);
+    const double eps = 1.1102230246251565e-16;
+    double cte = (*anrm) * eps * sqrt((double)n) * 1.0;
+    if (rnrm > xnrm * cte) atomicAdd(notconv, 1);
+    if (norms_out) { norms_out[2 * j] = xnrm; norms_out[2 * j + 1] = rnrm; }
+  }
+}
+
+
+// DLAG2S stop-at-first-overflow (SRC/dlag2s.f:137-144): the first pass finds
+// the smallest column-major index with |a| > FLT_MAX, the second converts
+// only the elements before it.
+static __global__ void first_overflow_kernel(const double* __restrict__ A, int lda, int m, int n,
+                                      unsigned long long* __restrict__ first) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  double v = A[(size_t)r + (size_t)c * lda];
+  const double rmax = 3.4028234663852886e38;
+  if (v < -rmax || v > rmax) atomicMin(first, (unsigned long long)e);
+}
+static __global__ void lag2s_upto_kernel(const double* __restrict__ A, int lda, float* __restrict__ S, int lds, int m, int n,
+                                  const unsigned long long* __restrict__ first) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n || e >= *first) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  S[(size_t)r + (size_t)c * lds] = (float)A[(size_t)r + (size_t)c * lda];
+}
+
+// DLANGE('1') column sums (SRC/dlange.f:155-163) in row order: a 32 x 32
+// tile is staged through shared memory so each thread folds one column's
+// values in increasing row order.
+template <typename T>
+__global__ void __launch_bounds__(1024)
+col_abs_sum_kernel(const T* __restrict__ A, int lda, int m, int n, T* __restrict__ colsum) {
+  __shared__ T tile[32][33];
+  const int c0 = blockIdx.x * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  T s = 0;
+  for (int r0 = 0; r0 < m; r0 += 32) {
+    int r = r0 + tx, c = c0 + ty;
+    tile[ty][tx] = (r < m && c < n) ? A[(size_t)r + (size_t)c * lda] : T(0);
+    __syncthreads();
+    if (ty == 0) {
+      int nr = min(32, m - r0);
+      for (int k = 0; k < nr; ++k) { T v = tile[tx][k]; s = s + (v < 0 ? -v : v); }
+    }
+    __syncthreads();
+  }
+  if (ty == 0 && c0 + tx < n) colsum[c0 + tx] = s;
+}
+
+// max |a| with NaN propagation (DLANGE 'M', SRC/dlange.f:141-152).
+template <typename T>
+__global__ void max_abs_kernel(const T* __restrict__ A, int lda, int m, int n, unsigned long long* __restrict__ bits,
+                               int* __restrict__ nanflag) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  double v = (double)A[(size_t)r + (size_t)c * lda];
+  if (v != v) { *nanflag = 1; return; }
+  v = fabs(v);
+  atomicMax(bits, (unsigned long long)__double_as_longlong(v));
+}
+static __global__ void sumsq_scaled_kernel(const double* __restrict__ A, int lda, int m, int n,
+                                    const unsigned long long* __restrict__ bits, double* __restrict__ acc) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  int c = (int)(e / m), r = (int)(e - (size_t)c * m);
+  double scale = __longlong_as_double((long long)*bits);
+  if (!(scale > 0) || isinf(scale)) return;
+  double v = A[(size_t)r + (size_t)c * lda] / scale;
+  atomicAdd(acc, v * v);
+}
+
+}  // namespace gb

@@ -1,0 +1,231 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes bindings to ``liboracle.so``, the plain-C restatement of the reference
+LAPACK dense LU solve path (see ``oracle.c`` for the per-routine citations),
+plus seeded input generators.  Only ``tests/``, ``__graft_entry__.smoke`` and
+the CPU-baseline leg of ``bench.py`` import this package, and only as the
+checker or the timed CPU baseline.  The GPU library never calls into it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+_i = ctypes.c_int
+_d = ctypes.c_double
+_f = ctypes.c_float
+_p = ctypes.c_void_p
+_c = ctypes.c_char
+
+
+def build(ref=False):
+    """Compile liboracle.so (and, with ref=True and the reference tree
+    present, the reference LAPACKE wrappers over it into _ref/)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        src = [os.path.join(_HERE, f) for f in ("oracle.c", "oracle_lu.inc")]
+        if not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in src):
+            build()
+        L = ctypes.CDLL(path)
+        for pre, T in (("d", _d), ("s", _f)):
+            getattr(L, f"or_{pre}getrf_nb").argtypes = [_i, _i, _p, _i, _p, _p, _i]
+            getattr(L, f"or_{pre}getrf_margins").argtypes = [_i, _i, _p, _i, _p, _p, _i, _p]
+            getattr(L, f"or_{pre}getrf2").argtypes = [_i, _i, _p, _i, _p, _p]
+            getattr(L, f"or_{pre}getrs").argtypes = [_c, _i, _i, _p, _i, _p, _p, _i, _p]
+            getattr(L, f"or_{pre}gesv").argtypes = [_i, _i, _p, _i, _p, _p, _i, _p]
+            getattr(L, f"or_{pre}laswp").argtypes = [_i, _p, _i, _i, _i, _p, _i]
+            getattr(L, f"or_{pre}gemm").argtypes = [_c, _c, _i, _i, _i, T, _p, _i, _p, _i, T, _p, _i]
+            getattr(L, f"or_{pre}trsm_left").argtypes = [_c, _c, _c, _i, _i, T, _p, _i, _p, _i]
+            getattr(L, f"or_{pre}lange").argtypes = [_c, _i, _i, _p, _i, _p]
+            getattr(L, f"or_{pre}lange").restype = T
+            getattr(L, f"or_{pre}iamax").argtypes = [_i, _p, _i]
+        L.or_dsgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p]
+        L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
+        L.or_slag2d.argtypes = [_i, _i, _p, _i, _p, _i, _p]
+        L.or_dlaruv.argtypes = [_p, _i, _p]
+        L.or_dlarnv.argtypes = [_i, _p, ctypes.c_longlong, _p]
+        L.or_dlaruv_power.argtypes = [_i, _p]
+        L.or_seed_from_int.argtypes = [ctypes.c_longlong, _p]
+        L.or_xerbla_last.argtypes = [_p, _i]
+        L.or_dlamch.argtypes = [_c]
+        L.or_dlamch.restype = _d
+        L.or_slamch.argtypes = [_c]
+        L.or_slamch.restype = _f
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _pre(a):
+    return "d" if a.dtype == np.float64 else "s"
+
+
+def _colmajor(a, dtype):
+    return np.asfortranarray(np.array(a, dtype=dtype, copy=True))
+
+
+# ---------------------------------------------------------------- routines
+def getrf(a, nb=64, margins=False):
+    """xGETRF (SRC/dgetrf.f) on a copy of ``a``: returns (lu, ipiv, info[, margin])."""
+    a = _colmajor(a, a.dtype if a.dtype in (np.float32, np.float64) else np.float64)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    L = lib()
+    lda = max(1, m)
+    if margins:
+        mg = np.ones(max(1, min(m, n)), dtype=np.float64)
+        getattr(L, f"or_{_pre(a)}getrf_margins")(m, n, _ptr(a), lda, _ptr(ipiv), _ptr(info), nb, _ptr(mg))
+        return a, ipiv[: min(m, n)], int(info[0]), mg[: min(m, n)]
+    getattr(L, f"or_{_pre(a)}getrf_nb")(m, n, _ptr(a), lda, _ptr(ipiv), _ptr(info), nb)
+    return a, ipiv[: min(m, n)], int(info[0])
+
+
+def getrs(lu, ipiv, b, trans="N"):
+    """xGETRS (SRC/dgetrs.f) on a copy of ``b``: returns (x, info)."""
+    lu = _colmajor(lu, lu.dtype)
+    b2 = _colmajor(b.reshape(b.shape[0], -1), lu.dtype)
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    getattr(lib(), f"or_{_pre(lu)}getrs")(trans.encode(), n, nrhs, _ptr(lu), max(1, n), _ptr(ipiv),
+                                          _ptr(b2), max(1, n), _ptr(info))
+    return b2.reshape(b.shape), int(info[0])
+
+
+def gesv(a, b):
+    """xGESV (SRC/dgesv.f): returns (lu, ipiv, x, info)."""
+    a = _colmajor(a, a.dtype)
+    b2 = _colmajor(b.reshape(b.shape[0], -1), a.dtype)
+    n = a.shape[0]
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    getattr(lib(), f"or_{_pre(a)}gesv")(n, b2.shape[1], _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2),
+                                        max(1, n), _ptr(info))
+    return a, ipiv[:n], b2.reshape(b.shape), int(info[0])
+
+
+def dsgesv(a, b):
+    """DSGESV (SRC/dsgesv.f): returns (a_out, ipiv, x, iter, info)."""
+    a = _colmajor(a, np.float64)
+    b2 = _colmajor(b.reshape(b.shape[0], -1), np.float64)
+    n, nrhs = b2.shape
+    x = np.zeros((n, nrhs), dtype=np.float64, order="F")
+    work = np.zeros(max(1, n * nrhs), dtype=np.float64)
+    swork = np.zeros(max(1, n * (n + nrhs)), dtype=np.float32)
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    it = np.zeros(1, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dsgesv(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(x), max(1, n),
+                    _ptr(work), _ptr(swork), _ptr(it), _ptr(info))
+    return a, ipiv[:n], x.reshape(b.shape), int(it[0]), int(info[0])
+
+
+def laswp(a, k1, k2, ipiv, incx=1):
+    a = _colmajor(a, a.dtype)
+    m, n = a.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    getattr(lib(), f"or_{_pre(a)}laswp")(n, _ptr(a), max(1, m), k1, k2, _ptr(ipiv), incx)
+    return a
+
+
+def lange(norm, a):
+    a = _colmajor(a, a.dtype)
+    m, n = a.shape
+    work = np.zeros(max(1, m), dtype=a.dtype)
+    return float(getattr(lib(), f"or_{_pre(a)}lange")(norm.encode(), m, n, _ptr(a), max(1, m), _ptr(work)))
+
+
+def dlag2s(a):
+    a = _colmajor(a, np.float64)
+    m, n = a.shape
+    sa = np.zeros((m, n), dtype=np.float32, order="F")
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dlag2s(m, n, _ptr(a), max(1, m), _ptr(sa), max(1, m), _ptr(info))
+    return sa, int(info[0])
+
+
+def xerbla_last():
+    buf = ctypes.create_string_buffer(16)
+    info = lib().or_xerbla_last(buf, 16)
+    return buf.value.decode(), info
+
+
+def xerbla_reset():
+    lib().or_xerbla_reset()
+
+
+# ------------------------------------------------------------- generators
+def seed_to_iseed(seed):
+    iseed = np.zeros(4, dtype=np.int32)
+    lib().or_seed_from_int(int(seed), _ptr(iseed))
+    return iseed
+
+
+def dlarnv(idist, iseed, n):
+    """DLARNV (SRC/dlarnv.f); ``iseed`` (int32[4]) is advanced in place."""
+    x = np.empty(int(n), dtype=np.float64)
+    lib().or_dlarnv(int(idist), _ptr(iseed), int(n), _ptr(x))
+    return x
+
+
+def dlaruv_power(i):
+    limbs = np.zeros(4, dtype=np.int32)
+    lib().or_dlaruv_power(int(i), _ptr(limbs))
+    return [int(v) for v in limbs]
+
+
+def random_matrix(m, n, seed, idist=3, dtype=np.float64):
+    """m x n column-major matrix of DLARNV(idist) draws from the scalar seed,
+    filled column by column (the order the reference test generators use)."""
+    iseed = seed_to_iseed(seed)
+    x = dlarnv(idist, iseed, m * n)
+    return np.asfortranarray(x.reshape(n, m).T.astype(dtype)), iseed
+
+
+def config_dgesv_small(n=1024, seed=0):
+    """Plain DGESV case: A iid N(0,1) from the seed, b iid N(0,1) drawn next
+    from the same stream."""
+    iseed = seed_to_iseed(seed)
+    a = dlarnv(3, iseed, n * n).reshape(n, n).T
+    b = dlarnv(3, iseed, n).reshape(n, 1)
+    return np.asfortranarray(a), np.asfortranarray(b)
+
+
+def householder_vectors(n, count, iseed):
+    """``count`` DLARNV N(0,1) vectors of length n (the DLAGGE construction,
+    TESTING/MATGEN/dlagge.f:185-232, draws its reflector vectors this way)."""
+    return dlarnv(3, iseed, n * count).reshape(count, n)
+
+
+def config_dsgesv_matrix(n, kappa, seed, nrefl=64):
+    """A = Q1 diag(s) Q2^T with Qi products of ``nrefl`` Householder
+    reflectors H = I - 2 v v^T / (v^T v) (v from DLARNV N(0,1)) and
+    s_i = kappa^(-(i-1)/(n-1)) (DLATMS MODE 3, TESTING/MATGEN/dlatms.f:160).
+    Returns (A, s, V1, V2).  Uses numpy for the dense products: input
+    construction only."""
+    iseed = seed_to_iseed(seed)
+    v1 = householder_vectors(n, nrefl, iseed)
+    v2 = householder_vectors(n, nrefl, iseed)
+    i = np.arange(n, dtype=np.float64)
+    s = kappa ** (-(i / (n - 1))) if n > 1 else np.ones(1)
+    a = np.diag(s)
+    for v in v1:            # A <- H A   (Q1 = H_1 H_2 ... H_k applied right to left)
+        a -= np.outer(v, (2.0 / v.dot(v)) * (v @ a))
+    for v in v2:            # A <- A H   (Q2^T = H_k ... H_1)
+        a -= np.outer(a @ v, (2.0 / v.dot(v)) * v)
+    return np.asfortranarray(a), s, v1, v2

@@ -1,0 +1,130 @@
+"""ORACLE test infrastructure: the reference test-suite ratios restated in
+numpy (TESTING/LIN).  Each returns the same scaled quantity the reference
+test prints; a result passes when it is below THRESH (30 in
+TESTING/dtest.in), or below sqrt(N) for DSGESV with ITER >= 0
+(TESTING/LIN/ddrvab.f:362-365)."""
+import numpy as np
+
+EPS64 = np.finfo(np.float64).eps / 2      # DLAMCH('Epsilon'), INSTALL/dlamch.f:101-110
+EPS32 = np.finfo(np.float32).eps / 2
+
+
+def _eps(dtype):
+    return EPS64 if np.dtype(dtype) == np.float64 else EPS32
+
+
+def unpack_lu(lu, ipiv):
+    """P, L, U from the LAPACK packed factor and 1-based IPIV (sequential swaps)."""
+    m, n = lu.shape
+    k = min(m, n)
+    L = np.tril(lu[:, :k], -1) + np.eye(m, k)
+    U = np.triu(lu[:k, :])
+    perm = np.arange(m)
+    for i in range(k):
+        p = int(ipiv[i]) - 1
+        perm[i], perm[p] = perm[p], perm[i]
+    return perm, L, U
+
+
+def dget01(a, lu, ipiv):
+    """||P L U - A||_1 / (N ||A||_1 eps)  (TESTING/LIN/dget01.f:147-207)."""
+    a = np.asarray(a, dtype=np.float64)
+    m, n = a.shape
+    if m == 0 or n == 0:
+        return 0.0
+    eps = _eps(lu.dtype)
+    perm, L, U = unpack_lu(np.asarray(lu, dtype=np.float64), ipiv)
+    prod = L @ U
+    pa = a[perm, :]
+    anorm = np.abs(a).sum(axis=0).max()
+    resid = np.abs(prod - pa).sum(axis=0).max()
+    if anorm <= 0:
+        return 0.0 if resid == 0 else 1.0 / eps
+    return ((resid / n) / anorm) / eps
+
+
+def dget02(a, x, b, trans="N", eps=None):
+    """max_j ||b_j - op(A) x_j||_1 / (||op(A)||_1 ||x_j||_1 eps)
+    (TESTING/LIN/dget02.f:176-219)."""
+    a = np.asarray(a, dtype=np.float64)
+    x = np.asarray(x, dtype=np.float64).reshape(a.shape[1] if trans == "N" else a.shape[0], -1)
+    b = np.asarray(b, dtype=np.float64).reshape(x.shape[0], -1)
+    eps = EPS64 if eps is None else eps
+    if a.size == 0 or x.shape[1] == 0:
+        return 0.0
+    opa = a if trans == "N" else a.T
+    anorm = np.abs(a).sum(axis=0).max() if trans == "N" else np.abs(a).sum(axis=1).max()
+    if anorm <= 0:
+        return 1.0 / eps
+    r = b - opa @ x
+    resid = 0.0
+    for j in range(x.shape[1]):
+        xn = np.abs(x[:, j]).sum()
+        if xn <= 0:
+            return 1.0 / eps
+        resid = max(resid, ((np.abs(r[:, j]).sum() / anorm) / xn) / eps)
+    return resid
+
+
+def dget04(x, xact, rcond, eps=None):
+    """max_j ||x_j - xact_j||_inf / (||xact_j||_inf * eps) * rcond
+    (TESTING/LIN/dget04.f:138-171)."""
+    eps = EPS64 if eps is None else eps
+    x = np.asarray(x, dtype=np.float64).reshape(np.asarray(xact).shape[0], -1)
+    xact = np.asarray(xact, dtype=np.float64).reshape(x.shape)
+    resid = 0.0
+    for j in range(x.shape[1]):
+        xn = np.abs(xact[:, j]).max() if x.shape[0] else 0.0
+        d = np.abs(x[:, j] - xact[:, j]).max() if x.shape[0] else 0.0
+        if xn <= 0:
+            if d > 0:
+                resid = 1.0 / eps
+        else:
+            resid = max(resid, (d / xn) * rcond)
+    if resid * eps < 1.0:
+        resid = resid / eps
+    return resid
+
+
+def dget08(a, x, b, eps=None):
+    """max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf eps)
+    (TESTING/LIN/dget08.f:175-214)."""
+    a = np.asarray(a, dtype=np.float64)
+    eps = EPS64 if eps is None else eps
+    x = np.asarray(x, dtype=np.float64).reshape(a.shape[1], -1)
+    b = np.asarray(b, dtype=np.float64).reshape(a.shape[0], -1)
+    if a.size == 0 or x.shape[1] == 0:
+        return 0.0
+    anorm = np.abs(a).sum(axis=1).max()
+    if anorm <= 0:
+        return 1.0 / eps
+    r = b - a @ x
+    resid = 0.0
+    for j in range(x.shape[1]):
+        xn = np.abs(x[:, j]).max()
+        if xn <= 0:
+            return 1.0 / eps
+        resid = max(resid, ((np.abs(r[:, j]).max() / anorm) / xn) / eps)
+    return resid
+
+
+def scaled_residual(a, x, b):
+    """||b - A x||_inf / (||A||_inf ||x||_inf n eps): the parity measure the
+    GPU result must meet (at or below the oracle's own value)."""
+    a = np.asarray(a, dtype=np.float64)
+    n = a.shape[0]
+    x = np.asarray(x, dtype=np.float64).reshape(n, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(n, -1)
+    r = b - a @ x
+    an = np.abs(a).sum(axis=1).max()
+    out = 0.0
+    for j in range(x.shape[1]):
+        out = max(out, np.abs(r[:, j]).max() / (an * np.abs(x[:, j]).max() * n * EPS64))
+    return out
+
+
+def lu_rel_diff(lu_a, lu_b, a):
+    """max |LU_a - LU_b| / (||A||_max * n * eps) -- the L/U agreement measure."""
+    n = a.shape[0]
+    scale = max(np.abs(a).max(), 1e-300) * max(n, 1) * _eps(lu_a.dtype)
+    return float(np.abs(np.asarray(lu_a, np.float64) - np.asarray(lu_b, np.float64)).max() / scale)

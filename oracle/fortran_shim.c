@@ -1,0 +1,66 @@
+/*
+ * ORACLE test infrastructure: Fortran-ABI entry points (dgesv_, dgetrf_, ...)
+ * over the C restatement, so that the reference's own LAPACKE C wrappers can
+ * be compiled from the reference sources and run on top of the oracle.
+ * Argument lists follow LAPACKE/include/lapack.h (hidden CHARACTER lengths
+ * at the end, LAPACK_FORTRAN_STRLEN_END).  Linked only into _ref/.
+ */
+#include <stddef.h>
+void or_dgesv(int, int, double *, int, int *, double *, int, int *);
+void or_sgesv(int, int, float *, int, int *, float *, int, int *);
+void or_dgetrf(int, int, double *, int, int *, int *);
+void or_sgetrf(int, int, float *, int, int *, int *);
+void or_dgetrf2(int, int, double *, int, int *, int *);
+void or_sgetrf2(int, int, float *, int, int *, int *);
+void or_dgetrs(char, int, int, const double *, int, const int *, double *, int, int *);
+void or_sgetrs(char, int, int, const float *, int, const int *, float *, int, int *);
+void or_dlaswp(int, double *, int, int, int, const int *, int);
+void or_slaswp(int, float *, int, int, int, const int *, int);
+void or_dlag2s(int, int, const double *, int, float *, int, int *);
+void or_slag2d(int, int, const float *, int, double *, int, int *);
+void or_dsgesv(int, int, double *, int, int *, const double *, int, double *, int, double *, float *, int *, int *);
+
+void dgesv_(const int *n, const int *nrhs, double *a, const int *lda, int *ipiv, double *b, const int *ldb, int *info) {
+  or_dgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void sgesv_(const int *n, const int *nrhs, float *a, const int *lda, int *ipiv, float *b, const int *ldb, int *info) {
+  or_sgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void dgetrf_(const int *m, const int *n, double *a, const int *lda, int *ipiv, int *info) {
+  or_dgetrf(*m, *n, a, *lda, ipiv, info);
+}
+void sgetrf_(const int *m, const int *n, float *a, const int *lda, int *ipiv, int *info) {
+  or_sgetrf(*m, *n, a, *lda, ipiv, info);
+}
+void dgetrf2_(const int *m, const int *n, double *a, const int *lda, int *ipiv, int *info) {
+  or_dgetrf2(*m, *n, a, *lda, ipiv, info);
+}
+void sgetrf2_(const int *m, const int *n, float *a, const int *lda, int *ipiv, int *info) {
+  or_sgetrf2(*m, *n, a, *lda, ipiv, info);
+}
+void dgetrs_(const char *trans, const int *n, const int *nrhs, const double *a, const int *lda, const int *ipiv,
+             double *b, const int *ldb, int *info, size_t trans_len) {
+  (void)trans_len;
+  or_dgetrs(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void sgetrs_(const char *trans, const int *n, const int *nrhs, const float *a, const int *lda, const int *ipiv,
+             float *b, const int *ldb, int *info, size_t trans_len) {
+  (void)trans_len;
+  or_sgetrs(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void dlaswp_(const int *n, double *a, const int *lda, const int *k1, const int *k2, const int *ipiv, const int *incx) {
+  or_dlaswp(*n, a, *lda, *k1, *k2, ipiv, *incx);
+}
+void slaswp_(const int *n, float *a, const int *lda, const int *k1, const int *k2, const int *ipiv, const int *incx) {
+  or_slaswp(*n, a, *lda, *k1, *k2, ipiv, *incx);
+}
+void dlag2s_(const int *m, const int *n, const double *a, const int *lda, float *sa, const int *ldsa, int *info) {
+  or_dlag2s(*m, *n, a, *lda, sa, *ldsa, info);
+}
+void slag2d_(const int *m, const int *n, const float *sa, const int *ldsa, double *a, const int *lda, int *info) {
+  or_slag2d(*m, *n, sa, *ldsa, a, *lda, info);
+}
+void dsgesv_(const int *n, const int *nrhs, double *a, const int *lda, int *ipiv, const double *b, const int *ldb,
+             double *x, const int *ldx, double *work, float *swork, int *iter, int *info) {
+  or_dsgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, work, swork, iter, info);
+}

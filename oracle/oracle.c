@@ -1,0 +1,263 @@
+/*
+ * ORACLE -- test infrastructure, not product code.
+ *
+ * A plain-C restatement of the reference LAPACK 3.12.1 routines on the dense
+ * LU solve path (DGETRF/DGETRF2/DLASWP/DGETRS/DGESV, their single-precision
+ * twins, DSGESV with DLAG2S/SLAG2D/DLANGE/DLACPY) and of the reference BLAS
+ * they call (xGEMM, xTRSM, IxAMAX, xSCAL, xAXPY), plus the seeded generator
+ * DLARUV/DLARNV used to build test matrices.  Only the tests, the smoke check
+ * and the CPU-baseline leg of the benchmark load this library, and only to
+ * check or time against; the GPU library never links it.
+ *
+ * Build with -O2 -ffp-contract=off (gfortran on x86 does not contract a*b+c
+ * into an FMA; aarch64 gcc does unless told not to).  The optional OpenMP
+ * split is over independent columns only, so results are bit-identical with
+ * and without it.
+ *
+ * Parity pins: no golden output vectors exist in the reference.  The oracle
+ * is pinned by (1) the DLARUV multiplier table read from the reference's own
+ * SRC/dlaruv.f (tests/golden), (2) the reference LAPACKE C wrappers compiled
+ * from the reference sources over this oracle's Fortran-ABI shim and checked
+ * case by case, and (3) the reference test-suite ratios (DGET01/02/04/08,
+ * TESTING/LIN) restated in oracle/checks.py, all passing under THRESH=30.
+ */
+#include <math.h>
+#include <float.h>
+#include <stdio.h>
+#include <stdint.h>
+#include <string.h>
+
+/* ---- XERBLA: SRC/xerbla.f:67-95 prints and STOPs.  Like the test-suite
+ * XERBLA (TESTING/LIN/xerbla.f:74-130) the oracle records the call instead
+ * so that error-exit tests can inspect it. */
+static char or_xerbla_name[16];
+static int or_xerbla_info = 0;
+static int or_xerbla_count = 0;
+void or_xerbla(const char *name, int info) {
+  snprintf(or_xerbla_name, sizeof or_xerbla_name, "%s", name);
+  or_xerbla_info = info;
+  or_xerbla_count++;
+}
+int or_xerbla_last(char *name_out, int cap) {
+  if (name_out && cap > 0) snprintf(name_out, (size_t)cap, "%s", or_xerbla_name);
+  return or_xerbla_info;
+}
+int or_xerbla_calls(void) { return or_xerbla_count; }
+void or_xerbla_reset(void) { or_xerbla_count = 0; or_xerbla_info = 0; or_xerbla_name[0] = 0; }
+
+/* ---- DLAMCH/SLAMCH (INSTALL/dlamch.f:101-141): eps is EPSILON*0.5 for a
+ * rounding arithmetic, sfmin is TINY (1/HUGE is smaller), 'O' is HUGE. */
+double or_dlamch(char c) {
+  switch (c) {
+    case 'E': case 'e': return DBL_EPSILON * 0.5;
+    case 'S': case 's': return DBL_MIN;
+    case 'O': case 'o': return DBL_MAX;
+    case 'P': case 'p': return DBL_EPSILON;
+    case 'B': case 'b': return 2.0;
+    case 'U': case 'u': return DBL_MIN;
+    default: return 0.0;
+  }
+}
+float or_slamch(char c) {
+  switch (c) {
+    case 'E': case 'e': return FLT_EPSILON * 0.5f;
+    case 'S': case 's': return FLT_MIN;
+    case 'O': case 'o': return FLT_MAX;
+    case 'P': case 'p': return FLT_EPSILON;
+    case 'B': case 'b': return 2.0f;
+    case 'U': case 'u': return FLT_MIN;
+    default: return 0.0f;
+  }
+}
+
+#define T double
+#define P d
+#define PNAME "D"
+#define ABS_T fabs
+#define SFMIN_T DBL_MIN
+#include "oracle_lu.inc"
+#undef T
+#undef P
+#undef PNAME
+#undef ABS_T
+#undef SFMIN_T
+
+#define T float
+#define P s
+#define PNAME "S"
+#define ABS_T fabsf
+#define SFMIN_T FLT_MIN
+#include "oracle_lu.inc"
+#undef T
+#undef P
+#undef PNAME
+#undef ABS_T
+#undef SFMIN_T
+
+/* ---- DLAG2S: SRC/dlag2s.f:135-146.  INFO=1 (and stop converting) at the
+ * first |a| > SLAMCH('O'); a NaN passes the test and converts to NaN. */
+void or_dlag2s(int m, int n, const double *a, int lda, float *sa, int ldsa, int *info) {
+  double rmax = (double)FLT_MAX;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) {
+      double v = a[(size_t)i + (size_t)j * lda];
+      if (v < -rmax || v > rmax) { *info = 1; return; }
+      sa[(size_t)i + (size_t)j * ldsa] = (float)v;
+    }
+  *info = 0;
+}
+
+/* ---- SLAG2D: SRC/slag2d.f:123-128. */
+void or_slag2d(int m, int n, const float *sa, int ldsa, double *a, int lda, int *info) {
+  *info = 0;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) a[(size_t)i + (size_t)j * lda] = (double)sa[(size_t)i + (size_t)j * ldsa];
+}
+
+/* ---- DSGESV: SRC/dsgesv.f:243-429.  FP32 LU (SGETRF, NB=64) plus FP64
+ * iterative refinement; ITERMAX=30, BWDMAX=1, CTE=||A||_inf*eps*sqrt(n).
+ * Falls back to FP64 DGETRF/DGETRS with ITER<0 exactly as the reference. */
+void or_dsgesv(int n, int nrhs, double *a, int lda, int *ipiv, const double *b, int ldb,
+               double *x, int ldx, double *work, float *swork, int *iter, int *info) {
+  const int itermax = 30;
+  const double bwdmax = 1.0;
+  *info = 0;
+  *iter = 0;
+  if (n < 0) *info = -1;
+  else if (nrhs < 0) *info = -2;
+  else if (lda < (n > 1 ? n : 1)) *info = -4;
+  else if (ldb < (n > 1 ? n : 1)) *info = -7;
+  else if (ldx < (n > 1 ? n : 1)) *info = -9;
+  if (*info != 0) { or_xerbla("DSGESV", -*info); return; }
+  if (n == 0) return;
+  double anrm = or_dlange('I', n, n, a, lda, work);
+  double eps = or_dlamch('E');
+  double cte = anrm * eps * sqrt((double)n) * bwdmax;
+  float *sa = swork;
+  float *sx = swork + (size_t)n * n;
+  or_dlag2s(n, nrhs, b, ldb, sx, n, info);
+  if (*info != 0) { *iter = -2; goto fallback; }
+  or_dlag2s(n, n, a, lda, sa, n, info);
+  if (*info != 0) { *iter = -2; goto fallback; }
+  or_sgetrf(n, n, sa, n, ipiv, info);
+  if (*info != 0) { *iter = -3; goto fallback; }
+  or_sgetrs('N', n, nrhs, sa, n, ipiv, sx, n, info);
+  or_slag2d(n, nrhs, sx, n, x, ldx, info);
+  or_dlacpy(n, nrhs, b, ldb, work, n);
+  or_dgemm('N', 'N', n, nrhs, n, -1.0, a, lda, x, ldx, 1.0, work, n);
+  {
+    int conv = 1;
+    for (int i = 0; i < nrhs; i++) {
+      double xnrm = fabs(x[(size_t)(or_diamax(n, x + (size_t)i * ldx, 1) - 1) + (size_t)i * ldx]);
+      double rnrm = fabs(work[(size_t)(or_diamax(n, work + (size_t)i * n, 1) - 1) + (size_t)i * n]);
+      if (rnrm > xnrm * cte) { conv = 0; break; }
+    }
+    if (conv) { *iter = 0; return; }
+  }
+  for (int iiter = 1; iiter <= itermax; iiter++) {
+    or_dlag2s(n, nrhs, work, n, sx, n, info);
+    if (*info != 0) { *iter = -2; goto fallback; }
+    or_sgetrs('N', n, nrhs, sa, n, ipiv, sx, n, info);
+    or_slag2d(n, nrhs, sx, n, work, n, info);
+    for (int i = 0; i < nrhs; i++) or_daxpy(n, 1.0, work + (size_t)i * n, 1, x + (size_t)i * ldx, 1);
+    or_dlacpy(n, nrhs, b, ldb, work, n);
+    or_dgemm('N', 'N', n, nrhs, n, -1.0, a, lda, x, ldx, 1.0, work, n);
+    int conv = 1;
+    for (int i = 0; i < nrhs; i++) {
+      double xnrm = fabs(x[(size_t)(or_diamax(n, x + (size_t)i * ldx, 1) - 1) + (size_t)i * ldx]);
+      double rnrm = fabs(work[(size_t)(or_diamax(n, work + (size_t)i * n, 1) - 1) + (size_t)i * n]);
+      if (rnrm > xnrm * cte) { conv = 0; break; }
+    }
+    if (conv) { *iter = iiter; return; }
+  }
+  *iter = -itermax - 1;
+fallback:
+  or_dgetrf(n, n, a, lda, ipiv, info);
+  if (*info != 0) return;
+  or_dlacpy(n, nrhs, b, ldb, x, ldx);
+  or_dgetrs('N', n, nrhs, a, lda, ipiv, x, ldx, info);
+}
+
+/* ---- DLARUV: SRC/dlaruv.f:92-447.  48-bit multiplicative congruential
+ * generator; x_i = seed * a^i mod 2^48 for i = 1..n, the new seed is
+ * seed * a^n.  The reference stores a^i (i = 1..128) as a table of 12-bit
+ * limbs; here the powers are computed from the base multiplier
+ * a = 33952834046453 (the table's first row), and the tests compare them
+ * with the table read from the reference source. */
+static const uint64_t OR_RUV_A = 33952834046453ULL;
+static const uint64_t OR_M48 = (1ULL << 48) - 1;
+
+void or_dlaruv_power(int i, int limbs[4]) {
+  uint64_t p = 1;
+  for (int k = 0; k < i; k++) p = (p * OR_RUV_A) & OR_M48;   /* products fit: wraps mod 2^64 then masked */
+  limbs[0] = (int)((p >> 36) & 4095);
+  limbs[1] = (int)((p >> 24) & 4095);
+  limbs[2] = (int)((p >> 12) & 4095);
+  limbs[3] = (int)(p & 4095);
+}
+
+static uint64_t or_seed_pack(const int iseed[4]) {
+  return ((uint64_t)iseed[0] << 36) | ((uint64_t)iseed[1] << 24) | ((uint64_t)iseed[2] << 12) | (uint64_t)iseed[3];
+}
+static void or_seed_unpack(uint64_t s, int iseed[4]) {
+  iseed[0] = (int)((s >> 36) & 4095);
+  iseed[1] = (int)((s >> 24) & 4095);
+  iseed[2] = (int)((s >> 12) & 4095);
+  iseed[3] = (int)(s & 4095);
+}
+/* 48-bit value -> real in (0,1) with the reference's nesting:
+ * R*(IT1 + R*(IT2 + R*(IT3 + R*IT4))), R = 1/4096 (every step exact). */
+static double or_ruv_real(uint64_t v) {
+  const double r = 1.0 / 4096.0;
+  double it1 = (double)((v >> 36) & 4095), it2 = (double)((v >> 24) & 4095);
+  double it3 = (double)((v >> 12) & 4095), it4 = (double)(v & 4095);
+  return r * (it1 + r * (it2 + r * (it3 + r * it4)));
+}
+
+void or_dlaruv(int iseed[4], int n, double *x) {
+  if (n < 1) return;
+  int lv = n < 128 ? n : 128;
+  uint64_t s = or_seed_pack(iseed);
+  uint64_t pw[129];
+  pw[0] = 1;
+  for (int k = 1; k <= lv; k++) pw[k] = (pw[k - 1] * OR_RUV_A) & OR_M48;
+  uint64_t it = s;
+  for (int i = 1; i <= lv; i++) {
+    for (;;) {
+      it = (s * pw[i]) & OR_M48;
+      x[i - 1] = or_ruv_real(it);
+      if (x[i - 1] != 1.0) break;
+      s = it;                             /* dlaruv.f:424-433: iterate again */
+    }
+  }
+  or_seed_unpack(it, iseed);
+}
+
+/* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
+ * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */
+void or_dlarnv(int idist, int iseed[4], long long n, double *x) {
+  const double twopi = 6.28318530717958647692528676655900576839;
+  double u[128];
+  for (long long iv = 1; iv <= n; iv += 64) {
+    int il = (int)((n - iv + 1) < 64 ? (n - iv + 1) : 64);
+    int il2 = (idist == 3) ? 2 * il : il;
+    or_dlaruv(iseed, il2, u);
+    if (idist == 1) {
+      for (int i = 0; i < il; i++) x[iv - 1 + i] = u[i];
+    } else if (idist == 2) {
+      for (int i = 0; i < il; i++) x[iv - 1 + i] = 2.0 * u[i] - 1.0;
+    } else if (idist == 3) {
+      for (int i = 0; i < il; i++) x[iv - 1 + i] = sqrt(-2.0 * log(u[2 * i])) * cos(twopi * u[2 * i + 1]);
+    }
+  }
+}
+
+/* Scalar-seed convention of this project (the reference has none): seed s
+ * maps to ISEED = (0, 0, (2s+1)/4096 mod 4096, (2s+1) mod 4096); ISEED(4)
+ * is odd as DLARUV requires. */
+void or_seed_from_int(long long seed, int iseed[4]) {
+  uint64_t v = ((uint64_t)(2 * seed + 1)) & OR_M48;
+  or_seed_unpack(v, iseed);
+  iseed[0] = 0;
+  iseed[1] = 0;
+}
