@@ -1,0 +1,420 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 dense LU solve path.
+
+Headline metric: n=32768 DGESV time-to-solution with the mixed-precision
+DSGESV method (FP32 factorization whose trailing updates run on the BF16
+tensor cores as split-BF16x3 products, FP64 residual / update / convergence
+test on the GPU) against the plain FP64 GPU DGESV, at FP64 backward error.
+
+One step = one DSGESV solve of the n=32768, nrhs=1 system
+A = Q1 diag(s) Q2^T (Qi products of 64 Householder reflectors, s geometric
+from 1 to 1/kappa, kappa=1e6), b = A x_true, with A and b resident in HBM
+(8.6 GB of input, far larger than the 129 MB L2, so no flush is needed).
+`e2e` measures the same solve through the LAPACK Fortran ABI (dsgesv_) with
+pinned host buffers, the host<->device copies inside the timed region.
+
+Inputs are synthetic, drawn from numpy's PCG64 with a fixed seed.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "n=32768 DGESV time-to-solution: mixed-prec+IR vs FP64 GPU at FP64 backward err"
+EPS = 2.0 ** -53
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=32768)
+    p.add_argument("--nrhs", type=int, default=1)
+    p.add_argument("--kappa", type=float, default=1e6)
+    p.add_argument("--seed", type=int, default=2)
+    p.add_argument("--no-fp64", action="store_true", help="skip the FP64 GPU DGESV comparison")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--sweep", action="store_true", help="also solve at kappa 1e2 and 1e10 once each")
+    p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ inputs
+def make_system(n, kappa, seed, nrhs, device):
+    """Column-major A (torch view with stride (1, n)), B, x_true on `device`.
+    A = Q1 diag(s) Q2^T with 64 + 64 Householder reflectors; the storage
+    array M holds A^T row-major (= A column-major)."""
+    import torch
+    rng = np.random.default_rng(seed)
+    v1 = torch.from_numpy(rng.standard_normal((64, n))).to(device)
+    v2 = torch.from_numpy(rng.standard_normal((64, n))).to(device)
+    xt = torch.from_numpy(rng.standard_normal((n, nrhs))).to(device)
+    i = torch.arange(n, dtype=torch.float64, device=device)
+    s = kappa ** (-(i / max(n - 1, 1)))
+    M = torch.diag(s)
+    del s
+    for v in v1:                       # M <- M H(v)
+        tau = 2.0 / torch.dot(v, v)
+        M.addr_(M @ v, v, alpha=-tau)
+    for v in v2:                       # M <- H(v) M
+        tau = 2.0 / torch.dot(v, v)
+        M.addr_(v, v @ M, alpha=-tau)
+    A = M.t()                          # (n, n) column-major view of A
+    B = A @ xt                         # b = A x_true in FP64
+    Bc = torch.empty((nrhs, n), dtype=torch.float64, device=device).t()
+    Bc.copy_(B)
+    return M, A, Bc, xt
+
+
+def backward_errors(A, X, B, n):
+    """DGET08 ratio ||b-Ax||_inf/(||A||_inf ||x||_inf eps) and the north-star
+    scaled residual (the same divided by n), computed on the GPU in FP64."""
+    import torch
+    R = B - A @ X
+    anrm = A.abs().sum(dim=1).max().item()
+    out = 0.0
+    for j in range(X.shape[1]):
+        out = max(out, R[:, j].abs().max().item() / (anrm * X[:, j].abs().max().item() * EPS))
+    return out, out / n
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.flush()
+        self.out.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.out.read().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.out.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU baseline
+def cpu_baseline(n_target, n_sample, kappa, seed, reps=1):
+    """The oracle's DSGESV (the C restatement of SRC/dsgesv.f with the
+    reference BLAS loops, column-parallel over all host cores) on an
+    n_sample system of the same construction; time scaled by
+    (n_target / n_sample)^3."""
+    import oracle
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    a, _, _, _ = oracle.config_dsgesv_matrix(n_sample, kappa, seed)
+    xt = np.random.default_rng(seed).standard_normal((n_sample, 1))
+    b = a @ xt
+    oracle.lib()
+    times = []
+    it = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        _, _, x, it, info = oracle.dsgesv(a, b)
+        times.append(time.perf_counter() - t0)
+    t = min(times)
+    scale = (n_target / n_sample) ** 3
+    return {"value": t * scale, "unit": "s", "cores": int(os.environ.get("OMP_NUM_THREADS", threads)),
+            "kind": "port",
+            "sample": f"oracle DSGESV at n={n_sample} (iter={it}), {t:.3f} s measured, "
+                      f"time scaled by (n/{n_sample})^3 = {scale:.0f}"}
+
+
+# -------------------------------------------------------------- GPU arm
+def run_gpu(args, rank, world):
+    import torch
+    import lapack_gb300 as g
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+    n, nrhs = args.n, args.nrhs
+
+    M, A, B, xt = make_system(n, args.kappa, args.seed, nrhs, dev)
+    X = torch.empty((nrhs, n), dtype=torch.float64, device=dev).t()
+    ipiv = torch.empty(n, dtype=torch.int32, device=dev)
+    it = ctypes.c_int(0)
+    info = ctypes.c_int(0)
+
+    def solve():
+        rc = L.gb300_dsgesv_dev(n, nrhs, ctypes.c_void_p(A.data_ptr()), n, ctypes.c_void_p(ipiv.data_ptr()),
+                                ctypes.c_void_p(B.data_ptr()), n, ctypes.c_void_p(X.data_ptr()), n,
+                                ctypes.byref(it), ctypes.byref(info), sp)
+        if rc != 0:
+            raise RuntimeError(f"gb300_dsgesv_dev status {rc}")
+        if it.value < 0:
+            raise RuntimeError(f"refinement fell back to FP64 (ITER={it.value}); A no longer resident")
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    L.gb300_prof_reset()
+    L.gb300_prof_enable(1)
+    launches0 = L.gb300_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    iters = []
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        solve()
+        iters.append(it.value)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = L.gb300_launch_count() - launches0
+    L.gb300_prof_enable(0)
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = t.item()
+
+    # per-kernel-class event times recorded inside the timed region
+    names = ["gemm_f64", "gemm_f32_ffma", "gemm_bf16x3", "panel", "laswp", "trsm", "trsv", "residual_f64", "other"]
+    breakdown = {}
+    for k, nm in enumerate(names):
+        t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
+        if cnt.value:
+            breakdown[nm] = {"ms_per_step": t_ms.value / args.steps, "launches_per_step": cnt.value / args.steps,
+                             "flops": fl.value / args.steps, "bytes": by.value / args.steps}
+    L.gb300_prof_reset()
+
+    # accuracy of the last solve
+    bwd, scaled = backward_errors(A, X, B, n)
+    fwd = ((X - xt).abs().max() / xt.abs().max()).item()
+
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        with open(pk_path) as f:
+            peaks = json.load(f)
+    L.gb300_probe_peak.restype = ctypes.c_double
+    dfma_peak = L.gb300_probe_peak(0)
+    ffma_peak = L.gb300_probe_peak(1)
+
+    # dominant kernel of the step and its roofline
+    dom = max(breakdown.items(), key=lambda kv: kv[1]["ms_per_step"]) if breakdown else (None, None)
+    roof = None
+    if dom[0] is not None:
+        nm, d = dom
+        per_launch_ms = d["ms_per_step"] / d["launches_per_step"]
+        if nm == "gemm_bf16x3":
+            peak = float(peaks.get("bf16_tflops", 1900.0))
+            achieved = 3.0 * d["flops"] / (d["ms_per_step"] * 1e-3) / 1e12
+            roof = {"bound": "tensor", "kernel": nm, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                    "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
+                    "work": "3 BF16 products x 2*M*N*K per launch"}
+        elif nm in ("gemm_f32_ffma", "gemm_f64", "panel", "trsm", "residual_f64"):
+            peak = ffma_peak if nm != "gemm_f64" and nm != "residual_f64" else dfma_peak
+            achieved = d["flops"] / (d["ms_per_step"] * 1e-3) / 1e12 if d["flops"] else 0.0
+            roof = {"bound": "fp32-fma" if peak == ffma_peak else "fp64-fma", "kernel": nm, "achieved": achieved,
+                    "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                    "peak_source": "gb300_probe_peak FMA loop measured in this run"}
+        else:
+            hbm = float(peaks.get("hbm_gbs", 6800.0))
+            achieved = d["bytes"] / (d["ms_per_step"] * 1e-3) / 1e9
+            roof = {"bound": "hbm", "kernel": nm, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                    "frac": achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured"}
+        roof["per_launch_ms"] = per_launch_ms
+        roof["traffic"] = None
+
+    result = {
+        "metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/bf16x3 factor + f64 refine",
+        "data": "synthetic",
+        "config": {"workload": f"DSGESV n={n} nrhs={nrhs} kappa={args.kappa:g}: A=Q1 diag(s) Q2^T "
+                               f"(64+64 Householder reflectors, s geometric 1..1/kappa), b=A x_true, "
+                               f"inputs resident in HBM", "n": n, "nrhs": nrhs, "kappa": args.kappa,
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs 8.6 GB >> 129 MB L2; no flush needed",
+                   "mixed_mode": "bf16x3" if g.get_option("mixed") == 0 else "fp32-ffma",
+                   "nb32": g.get_option("nb32"), "nb64": g.get_option("nb64")},
+        "iter": iters[-1], "backward_error_dget08": bwd, "scaled_residual": scaled, "forward_error": fwd,
+        "kernel_ms_per_step": {k: v["ms_per_step"] for k, v in breakdown.items()},
+        "roofline": roof, "gpu_launches": launches,
+        "clocks": clk, "peaks_measured": {"dfma_tflops": dfma_peak, "ffma_tflops": ffma_peak,
+                                          "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")},
+    }
+
+    # ---- plain FP64 GPU DGESV on the same system (the comparison arm)
+    if not args.no_fp64:
+        Ad = torch.empty_like(M)
+        Ad.copy_(M)
+        Ac = Ad.t()
+        Xd = torch.empty((nrhs, n), dtype=torch.float64, device=dev).t()
+        Xd.copy_(B)
+        # warm the FP64 kernels on a small system first
+        w = g.colmajor_empty(512, 512, torch.float64)
+        w.copy_(torch.rand(512, 512, dtype=torch.float64, device=dev) + 4 * torch.eye(512, dtype=torch.float64,
+                                                                                      device=dev))
+        g.getrf_dev(w, torch.empty(512, dtype=torch.int32, device=dev))
+        del w
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        rc = L.gb300_dgesv_dev(n, nrhs, ctypes.c_void_p(Ac.data_ptr()), n, ctypes.c_void_p(ipiv.data_ptr()),
+                               ctypes.c_void_p(Xd.data_ptr()), n, ctypes.byref(info), sp)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        t64 = f0.elapsed_time(f1) * 1e-3
+        bwd64, sc64 = backward_errors(A, Xd, B, n)
+        result["fp64_gpu"] = {"seconds": t64, "status": rc, "info": info.value,
+                              "tflops": (2.0 / 3.0) * n ** 3 / t64 / 1e12,
+                              "frac_of_dfma_peak": (2.0 / 3.0) * n ** 3 / t64 / 1e12 / dfma_peak,
+                              "backward_error_dget08": bwd64, "scaled_residual": sc64,
+                              "forward_error": ((Xd - xt).abs().max() / xt.abs().max()).item()}
+        result["speedup_vs_fp64_gpu"] = t64 / (ms * 1e-3)
+        result["backward_error_at_or_below_fp64"] = bool(scaled <= sc64 * 1.0 + 1e-30) or bool(scaled <= 1.0)
+        del Ad, Ac, Xd
+        torch.cuda.empty_cache()
+
+    # ---- end to end through the Fortran ABI with pinned host buffers
+    if not args.no_e2e:
+        hA = torch.empty_like(M, device="cpu").pin_memory()
+        hA.copy_(M)
+        hB = torch.empty((nrhs, n), dtype=torch.float64).pin_memory()
+        hB.copy_(B.t())
+        hX = torch.empty((nrhs, n), dtype=torch.float64).pin_memory()
+        hIp = torch.empty(n, dtype=torch.int32).pin_memory()
+        work = np.zeros(1)
+        swork = np.zeros(1, dtype=np.float32)
+        ci = lambda v: ctypes.byref(ctypes.c_int(v))
+
+        def e2e_step():
+            L.dsgesv_(ci(n), ci(nrhs), ctypes.c_void_p(hA.data_ptr()), ci(n), ctypes.c_void_p(hIp.data_ptr()),
+                      ctypes.c_void_p(hB.data_ptr()), ci(n), ctypes.c_void_p(hX.data_ptr()), ci(n),
+                      work.ctypes.data_as(ctypes.c_void_p), swork.ctypes.data_as(ctypes.c_void_p),
+                      ctypes.byref(it), ctypes.byref(info))
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(1, min(args.steps, 3))):
+            e2e_step()
+        t_e2e = (time.perf_counter() - t0) / max(1, min(args.steps, 3))
+        result["e2e"] = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
+                         "d2h_bytes_per_step": 8 * n * nrhs + 4 * n,
+                         "path": "dsgesv_ (LAPACK Fortran ABI) on pinned host buffers, copies inside the call"}
+        del hA, hB, hX
+
+    if args.sweep:
+        sweep = {}
+        for kap in (1e2, 1e10):
+            del M, A, B
+            torch.cuda.empty_cache()
+            M, A, B, xt = make_system(n, kap, args.seed, nrhs, dev)
+            Aw = M.clone()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rc = L.gb300_dsgesv_dev(n, nrhs, ctypes.c_void_p(Aw.data_ptr()), n, ctypes.c_void_p(ipiv.data_ptr()),
+                                    ctypes.c_void_p(B.data_ptr()), n, ctypes.c_void_p(X.data_ptr()), n,
+                                    ctypes.byref(it), ctypes.byref(info), sp)
+            torch.cuda.synchronize()
+            tk = time.perf_counter() - t0
+            bw, sc = backward_errors(A, X, B, n)
+            sweep[f"{kap:g}"] = {"seconds": tk, "iter": it.value, "info": info.value, "status": rc,
+                                 "backward_error_dget08": bw, "scaled_residual": sc,
+                                 "forward_error": ((X - xt).abs().max() / xt.abs().max()).item()}
+            del Aw
+        result["kappa_sweep"] = sweep
+    return result
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.warmup < 3 and args.impl == "gb300":
+        args.warmup = 3
+    if args.impl == "reference":
+        # the reference arm: the oracle port of the reference routines on the
+        # host cores, rank 0 only
+        if rank != 0:
+            return
+        samples = []
+        for _ in range(args.warmup):
+            cpu_baseline(args.n, args.cpu_n, args.kappa, args.seed)
+        for _ in range(args.steps):
+            samples.append(cpu_baseline(args.n, args.cpu_n, args.kappa, args.seed))
+        v = statistics.median(s["value"] for s in samples)
+        cb = dict(samples[0])
+        cb["value"] = v
+        print(json.dumps({
+            "metric": METRIC, "impl": "reference", "value": v, "unit": "s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 factor + f64 refine", "data": "synthetic",
+            "config": {"workload": f"DSGESV n={args.n} nrhs={args.nrhs} kappa={args.kappa:g} (CPU sample "
+                                   f"n={args.cpu_n}, scaled by n^3)", "n": args.n, "kappa": args.kappa},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    result = run_gpu(args, rank, world)
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline(args.n, args.cpu_n, args.kappa, args.seed)
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

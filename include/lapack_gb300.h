@@ -204,6 +204,20 @@ void gb300_xerbla_capture(int on);
 int gb300_xerbla_last(char* name, int cap);
 const char* gb300_version(void);
 
+/* Instrumentation (no reference counterpart).  gb300_launch_count: kernels
+ * this library has launched so far in the process.  With profiling enabled,
+ * every launch of the timed kernel classes is bracketed by CUDA events on
+ * its own stream; gb300_prof_read sums, for one class (0 FP64 update, 1
+ * FP32 update, 2 BF16x3 update, 3 panel, 4 row interchanges, 5 TRSM, 6
+ * triangular solves, 7 FP64 residual, 8 other), the event time in ms, the
+ * algorithmic flops and bytes, and the launch count. */
+long long gb300_launch_count(void);
+int gb300_prof_enable(int on);
+void gb300_prof_reset(void);
+int gb300_prof_read(int kind, double* ms, double* flops, double* bytes, long long* launches);
+/* Measured FMA throughput of the current GPU in TFLOP/s (0: FP64, 1: FP32). */
+double gb300_probe_peak(int which);
+
 #ifdef __cplusplus
 }
 #endif

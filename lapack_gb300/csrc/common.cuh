@@ -4,6 +4,8 @@
 #include <cstdint>
 #include <cstdio>
 
+#include "prof.h"
+
 namespace gb {
 
 // Error status words written by kernels whose waits are bounded.  A wait
@@ -150,6 +152,13 @@ __device__ __forceinline__ Cand<T> warp_best(Cand<T> c) {
 }
 
 }  // namespace gb
+
+// Launches a kernel of this library and counts it.
+#define GB_LAUNCH(...)        \
+  do {                        \
+    __VA_ARGS__;              \
+    ::gb::count_launch();     \
+  } while (0)
 
 #define GB_CUDA_TRY(expr)                                                         \
   do {                                                                            \

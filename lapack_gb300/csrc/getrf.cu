@@ -6,6 +6,7 @@
 // apply its interchanges to the other columns, form the block row of U with
 // a triangular solve, then update the trailing matrix with one GEMM.
 #include "driver.h"
+#include "prof.h"
 #include "gemm_simt.cuh"
 #include "lu_kernels.cuh"
 #include "solve_kernels.cuh"
@@ -93,10 +94,12 @@ int gemm_update_dev<double>(int M, int N, int K, const double* A, int lda, const
                             int ldc, cudaStream_t s, int) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   dim3 grid((M + 127) / 128, (N + 63) / 64);
+  prof_begin(kProfGemmF64, s);
   if (options().exact)
-    gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    GB_LAUNCH(gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
   else
-    gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    GB_LAUNCH(gemm_nn_update_kernel<double, 128, 64, 16, 8, 4, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  prof_end(kProfGemmF64, s, 2.0 * M * N * (double)K, 8.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
   return (int)cudaGetLastError();
 }
 
@@ -106,10 +109,12 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   if (mode == kMixedBf16x3) return gemm_bf16x3_dev(M, N, K, A, lda, B, ldb, C, ldc, s);
   dim3 grid((M + 127) / 128, (N + 127) / 128);
+  prof_begin(kProfGemmF32, s);
   if (options().exact)
-    gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
   else
-    gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc);
+    GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  prof_end(kProfGemmF32, s, 2.0 * M * N * (double)K, 4.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
   return (int)cudaGetLastError();
 }
 
@@ -120,10 +125,12 @@ int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStre
   if (k <= 0 || ncols <= 0) return 0;
   if (k <= kLeafMax) {
     int grid = (ncols + TrsmSlab<T>::BC - 1) / TrsmSlab<T>::BC;
+    prof_begin(kProfTrsm, s);
     if (options().exact)
-      trsm_llnu_leaf_kernel<T, true><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols);
+      GB_LAUNCH(trsm_llnu_leaf_kernel<T, true><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols));
     else
-      trsm_llnu_leaf_kernel<T, false><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols);
+      GB_LAUNCH(trsm_llnu_leaf_kernel<T, false><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols));
+    prof_end(kProfTrsm, s, (double)k * k * ncols, sizeof(T) * ((double)k * k + 2.0 * k * ncols));
     return (int)cudaGetLastError();
   }
   int k1 = ((k / 2) + kLeafMax - 1) / kLeafMax * kLeafMax;
@@ -169,7 +176,13 @@ static int launch_leaf(T* P, int lda, int M, int JB, int row0, int* ipiv, int* i
   PanelScratch<T> ps = cx.ps;
   int* status = cx.status;
   void* args[] = {&P, &lda, &M, &JB, &R, &row0, &ipiv, &info, &ps, &status};
-  return (int)cudaLaunchCooperativeKernel((void*)kern, G, kPanelThreads, args, smem, s);
+  prof_begin(kProfPanel, s);
+  int rc = (int)cudaLaunchCooperativeKernel((void*)kern, G, kPanelThreads, args, smem, s);
+  count_launch();
+  // algorithmic work of the leaf: M x JB panel read and written once,
+  // sum over columns of the rank-1 updates
+  prof_end(kProfPanel, s, (double)M * JB * JB, 2.0 * sizeof(T) * (double)M * JB);
+  return rc;
 }
 
 template <typename T>
@@ -177,8 +190,10 @@ static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, Panel
   int warps = c0 + (ncols - c1);
   if (warps <= 0) return 0;
   int blocks = (warps * 32 + 255) / 256;
-  laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(A, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
-                                                cx.ps.pair_count, ntop);
+  prof_begin(kProfLaswp, s);
+  GB_LAUNCH(laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(A, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
+                                                cx.ps.pair_count, ntop));
+  prof_end(kProfLaswp, s, 0.0, 2.0 * sizeof(T) * 2.0 * ntop * warps);
   return (int)cudaGetLastError();
 }
 
@@ -283,11 +298,11 @@ int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, 
       cudaFuncSetAttribute(ipiv_to_perm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - 1024);
       attr[dev] = true;
     }
-    ipiv_to_perm_kernel<true><<<1, 1024, smem, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, nullptr, status);
+    GB_LAUNCH(ipiv_to_perm_kernel<true><<<1, 1024, smem, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, nullptr, status));
   } else {
     DevScratch lab(smem, s);
     if (!lab.p) return (int)cudaErrorMemoryAllocation;
-    ipiv_to_perm_kernel<false><<<1, 1024, 0, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, lab.as<int>(), status);
+    GB_LAUNCH(ipiv_to_perm_kernel<false><<<1, 1024, 0, s>>>(dIpiv, k1, k2, incx, lo, span, dPerm, lab.as<int>(), status));
   }
   return (int)cudaGetLastError();
 }
@@ -308,8 +323,8 @@ int laswp_dev(int ncols, T* dA, int lda, int k1, int k2, const int* dIpiv, int i
   if (rc) return rc;
   size_t tot = (size_t)span * ncols;
   unsigned blocks = (unsigned)((tot + 255) / 256);
-  perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dA, lda, tmp.as<T>(), span, perm.as<int>(), 0, span, ncols);
-  copy_cols_kernel<T><<<blocks, 256, 0, s>>>(tmp.as<T>(), span, dA + lo, lda, span, ncols);
+  GB_LAUNCH(perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dA, lda, tmp.as<T>(), span, perm.as<int>(), 0, span, ncols));
+  GB_LAUNCH(copy_cols_kernel<T><<<blocks, 256, 0, s>>>(tmp.as<T>(), span, dA + lo, lda, span, ncols));
   return (int)cudaGetLastError();
 }
 template int laswp_dev<double>(int, double*, int, int, int, const int*, int, int, int, cudaStream_t);
@@ -324,8 +339,10 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
   GB_CUDA_TRY(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (size_t)(nblk + 1), s));
   int* flags = ctl.as<int>();
   unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
-  trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, flags, ticket,
-                                                                        device_status_word());
+  prof_begin(kProfTrsv, s);
+  GB_LAUNCH(trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, flags, ticket,
+                                                                        device_status_word()));
+  prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
   return (int)cudaGetLastError();
 }
 
@@ -339,15 +356,15 @@ static int getrs_impl(char trans, int n, int nrhs, const T* dA, int lda, const i
   unsigned blocks = (unsigned)((tot + 255) / 256);
   int rc;
   if (trans == 'N') {
-    perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dB, ldb, W, n, dPerm, 0, n, nrhs);
+    GB_LAUNCH(perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dB, ldb, W, n, dPerm, 0, n, nrhs));
     if ((rc = launch_trsv<T, EXACT, true, true, false>(dA, lda, n, W, n, nrhs, s))) return rc;
     if ((rc = launch_trsv<T, EXACT, false, false, false>(dA, lda, n, W, n, nrhs, s))) return rc;
-    copy_cols_kernel<T><<<blocks, 256, 0, s>>>(W, n, dB, ldb, n, nrhs);
+    GB_LAUNCH(copy_cols_kernel<T><<<blocks, 256, 0, s>>>(W, n, dB, ldb, n, nrhs));
   } else {
-    copy_cols_kernel<T><<<blocks, 256, 0, s>>>(dB, ldb, W, n, n, nrhs);
+    GB_LAUNCH(copy_cols_kernel<T><<<blocks, 256, 0, s>>>(dB, ldb, W, n, n, nrhs));
     if ((rc = launch_trsv<T, EXACT, true, false, true>(dA, lda, n, W, n, nrhs, s))) return rc;
     if ((rc = launch_trsv<T, EXACT, false, true, true>(dA, lda, n, W, n, nrhs, s))) return rc;
-    perm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(W, n, dB, ldb, dPerm, 0, n, nrhs);
+    GB_LAUNCH(perm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(W, n, dB, ldb, dPerm, 0, n, nrhs));
   }
   return (int)cudaGetLastError();
 }

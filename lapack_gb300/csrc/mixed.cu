@@ -4,6 +4,7 @@
 // the reference's ITER codes (-2 conversion overflow, -3 FP32 LU singular,
 // -31 no convergence).
 #include "driver.h"
+#include "prof.h"
 #include "solve_kernels.cuh"
 
 #include <algorithm>
@@ -18,8 +19,8 @@ double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, i
   DevScratch buf(sizeof(double) * ((size_t)m + 1), s);
   if (!buf.p) { *err = (int)cudaErrorMemoryAllocation; return 0.0; }
   double* rows = buf.as<double>();
-  row_abs_sum_kernel<double><<<(m + 63) / 64, 64, 0, s>>>(dA, lda, m, n, rows);
-  max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, m, rows + m);
+  GB_LAUNCH(row_abs_sum_kernel<double><<<(m + 63) / 64, 64, 0, s>>>(dA, lda, m, n, rows));
+  GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, m, rows + m));
   double h = 0;
   cudaMemcpyAsync(&h, rows + m, sizeof(double), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) *err = (int)cudaGetLastError();
@@ -29,10 +30,12 @@ double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, i
 static int residual(int n, int nrhs, const double* A, int lda, const double* X, int ldx, const double* B, int ldb,
                     double* R, int ldr, cudaStream_t s) {
   unsigned grid = (unsigned)((n + kResidRows - 1) / kResidRows);
+  prof_begin(kProfResidual, s);
   if (options().exact)
-    residual_kernel<true><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs);
+    GB_LAUNCH(residual_kernel<true><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs));
   else
-    residual_kernel<false><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs);
+    GB_LAUNCH(residual_kernel<false><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs));
+  prof_end(kProfResidual, s, 2.0 * n * (double)n * nrhs, 8.0 * ((double)n * n + 3.0 * n * nrhs));
   return (int)cudaGetLastError();
 }
 
@@ -45,8 +48,8 @@ int dlag2s_dev(int m, int n, const double* dA, int lda, float* dS, int lds, long
   if (!f.p) return (int)cudaErrorMemoryAllocation;
   GB_CUDA_TRY(cudaMemsetAsync(f.p, 0xff, sizeof(unsigned long long), s));
   size_t tot = (size_t)m * n;
-  first_overflow_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, f.as<unsigned long long>());
-  lag2s_upto_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, dS, lds, m, n, f.as<unsigned long long>());
+  GB_LAUNCH(first_overflow_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, f.as<unsigned long long>()));
+  GB_LAUNCH(lag2s_upto_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, dS, lds, m, n, f.as<unsigned long long>()));
   unsigned long long h = 0;
   GB_CUDA_TRY(cudaMemcpyAsync(&h, f.p, sizeof(h), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -56,7 +59,7 @@ int dlag2s_dev(int m, int n, const double* dA, int lda, float* dS, int lds, long
 
 int slag2d_dev(int m, int n, const float* dS, int lds, double* dA, int lda, cudaStream_t s) {
   if (m <= 0 || n <= 0) return 0;
-  slag2d_kernel<<<blocks_for((size_t)m * n), 256, 0, s>>>(dS, lds, dA, lda, m, n);
+  GB_LAUNCH(slag2d_kernel<<<blocks_for((size_t)m * n), 256, 0, s>>>(dS, lds, dA, lda, m, n));
   return (int)cudaGetLastError();
 }
 
@@ -72,8 +75,8 @@ int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, 
   if (which == 1) {
     DevScratch cs(sizeof(double) * ((size_t)n + 1), s);
     if (!cs.p) return (int)cudaErrorMemoryAllocation;
-    col_abs_sum_kernel<double><<<(n + 31) / 32, 1024, 0, s>>>(dA, lda, m, n, cs.as<double>());
-    max_nan_kernel<double><<<1, 1024, 0, s>>>(cs.as<double>(), n, cs.as<double>() + n);
+    GB_LAUNCH(col_abs_sum_kernel<double><<<(n + 31) / 32, 1024, 0, s>>>(dA, lda, m, n, cs.as<double>()));
+    GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(cs.as<double>(), n, cs.as<double>() + n));
     GB_CUDA_TRY(cudaMemcpyAsync(out, cs.as<double>() + n, sizeof(double), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     return 0;
@@ -84,8 +87,8 @@ int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, 
   unsigned long long* bits = w.as<unsigned long long>();
   int* nanflag = reinterpret_cast<int*>(w.as<char>() + 8);
   double* acc = reinterpret_cast<double*>(w.as<char>() + 16);
-  max_abs_kernel<double><<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, nanflag);
-  if (which == 3) sumsq_scaled_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, acc);
+  GB_LAUNCH(max_abs_kernel<double><<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, nanflag));
+  if (which == 3) GB_LAUNCH(sumsq_scaled_kernel<<<blocks_for(tot), 256, 0, s>>>(dA, lda, m, n, bits, acc));
   unsigned long long hb = 0;
   int hn = 0;
   double ha = 0;
@@ -136,13 +139,13 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   {
     DevScratch rows(sizeof(double) * (size_t)n, s);
     if (!rows.p) return (int)cudaErrorMemoryAllocation;
-    row_abs_sum_kernel<double><<<(n + 63) / 64, 64, 0, s>>>(dA, lda, n, n, rows.as<double>());
-    max_nan_kernel<double><<<1, 1024, 0, s>>>(rows.as<double>(), n, anrm);
+    GB_LAUNCH(row_abs_sum_kernel<double><<<(n + 63) / 64, 64, 0, s>>>(dA, lda, n, n, rows.as<double>()));
+    GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows.as<double>(), n, anrm));
   }
   GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
   // SX = DLAG2S(B), SA = DLAG2S(A)
-  dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags);
-  dlag2s_kernel<<<blocks_for(nn), 256, 0, s>>>(dA, lda, SA, n, n, n, flags);
+  GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
+  GB_LAUNCH(dlag2s_kernel<<<blocks_for(nn), 256, 0, s>>>(dA, lda, SA, n, n, n, flags));
   GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[0]) { *iter = -2; goto fallback; }
@@ -155,19 +158,19 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   if ((rc = ipiv_perm_dev(dIpiv, 1, n, 1, 0, n, perm, s))) return rc;
   // SX = SA^{-1} SX, X = SLAG2D(SX), R = B - A X
   if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
-  slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs);
+  GB_LAUNCH(slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
   if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
-  ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr);
+  GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
   GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[1] == 0) { *iter = 0; return 0; }
   for (int it = 1; it <= itermax; ++it) {
     GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2, s));
-    dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(R, n, SX, n, n, nrhs, flags);
+    GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(R, n, SX, n, n, nrhs, flags));
     if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
-    lag2d_axpy_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs);
+    GB_LAUNCH(lag2d_axpy_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
     if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
-    ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr);
+    GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
     GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     if (hflags[0]) { *iter = -2; goto fallback; }
@@ -182,7 +185,7 @@ fallback:
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   *info = hflags[3];
   if (*info != 0) return 0;
-  copy_cols_kernel<double><<<blocks_for(nr), 256, 0, s>>>(dB, ldb, dX, ldx, n, nrhs);
+  GB_LAUNCH(copy_cols_kernel<double><<<blocks_for(nr), 256, 0, s>>>(dB, ldb, dX, ldx, n, nrhs));
   return getrs_dev<double>('N', n, nrhs, dA, lda, dIpiv, nullptr, dX, ldx, s);
 }
 
