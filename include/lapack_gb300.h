@@ -185,6 +185,19 @@ int gb300_dgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, double* dB
                     void* stream);
 int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX,
                      int ldx, int* iter, int* info, void* stream);
+/* DGETRS on device memory that allocates nothing.  No counterpart in the
+ * reference: it exists for callers that may not allocate GPU memory at the
+ * point of the solve (a fixed device-memory budget reserved at start-up, a
+ * latency-critical loop where an allocation could synchronise, code inside
+ * an allocator callback).  Its scratch is one fixed array of about 1.1 MB
+ * compiled into the library, held on every GPU that loads it until exit, so
+ * it accepts n <= 16384 and n*nrhs <= 131072 and returns -100 for larger
+ * problems.  The first call on a device looks up that array's address and
+ * should come before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU race, so issue them one after another.  Same
+ * arguments, results and return codes as gb300_dgetrs_dev otherwise. */
+int gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double* dA, int lda, const int* dIpiv, double* dB,
+                         int ldb, void* stream);
 
 /* Options: "exact" (0/1: products rounded separately, bitwise the
  * reference's operation order), "nb64" / "nb32" (outer block sizes),
