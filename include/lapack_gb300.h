@@ -199,6 +199,14 @@ int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const dou
 int gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double* dA, int lda, const int* dIpiv, double* dB,
                          int ldb, void* stream);
 
+/* Trailing-matrix update C := C - A*B, column-major (the DGEMM('N','N',
+ * alpha=-1, beta=1) call of SRC/dgetrf.f:212-216 and its SGEMM twin).  The
+ * FP32 form takes mode 0 (split-BF16x3 on the tensor cores) or 1 (FP32 FMA). */
+int gb300_dgemm_update_dev(int m, int n, int k, const double* dA, int lda, const double* dB, int ldb, double* dC,
+                           int ldc, void* stream);
+int gb300_sgemm_update_dev(int mode, int m, int n, int k, const float* dA, int lda, const float* dB, int ldb,
+                           float* dC, int ldc, void* stream);
+
 /* Options: "exact" (0/1: products rounded separately, bitwise the
  * reference's operation order), "nb64" / "nb32" (outer block sizes),
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32

@@ -476,6 +476,34 @@ int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const dou
   return rc;
 }
 
+int gb300_dgemm_update_dev(int m, int n, int k, const double* dA, int lda, const double* dB, int ldb, double* dC,
+                           int ldc, void* stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (k < 0) return -3;
+  if (lda < std::max(1, m)) return -5;
+  if (ldb < std::max(1, k)) return -7;
+  if (ldc < std::max(1, m)) return -9;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::gemm_update_dev<double>(m, n, k, dA, lda, dB, ldb, dC, ldc, s, 0);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+int gb300_sgemm_update_dev(int mode, int m, int n, int k, const float* dA, int lda, const float* dB, int ldb,
+                           float* dC, int ldc, void* stream) {
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (k < 0) return -4;
+  if (lda < std::max(1, m)) return -6;
+  if (ldb < std::max(1, k)) return -8;
+  if (ldc < std::max(1, m)) return -10;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::gemm_update_dev<float>(m, n, k, dA, lda, dB, ldb, dC, ldc, s,
+                                      mode == 0 ? gb::kMixedBf16x3 : gb::kMixedFp32);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+
 int gb300_set_option(const char* name, int value) {
   gb::Options& o = options();
   int old;

@@ -15,7 +15,7 @@ struct Options {
   bool exact = false;       // separately rounded products (bitwise reference order)
   int nb_f64 = 64;          // outer block size of the FP64 factorization
   int nb_f32 = 256;         // outer block size of the FP32 factorization
-  int mixed_mode = kMixedFp32;
+  int mixed_mode = kMixedBf16x3;
   int sgetrf_mode = kMixedFp32;   // sgetrf_ itself: plain FP32 by default
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables

@@ -1,10 +1,328 @@
-// BF16x3 tensor-core trailing update for the FP32 factorization (tcgen05).
+// Trailing-matrix update of the FP32 factorization on the BF16 tensor cores
+// (tcgen05, sm_103a): C := C - A*B for FP32 column-major A (M x K), B (K x N),
+// C (M x N), the SGEMM('N','N', alpha=-1, beta=1) call of SRC/sgetrf.f, as
+// split-BF16x3 products: with a = ah + al and b = bh + bl (ah = bf16(a),
+// al = bf16(a - ah)), a*b ~ ah*bh + ah*bl + al*bh, the three products
+// accumulated in FP32 in tensor memory.
+//
+// Two steps per call:
+//  1. split kernels write ah/al and bh/bl as K-major bf16 arrays (row r holds
+//     K contiguous values, K padded with zeros to a multiple of 64);
+//  2. the MMA kernel: one CTA per 128 x 128 tile of C.  Per 64-wide K block
+//     one thread issues the four TMA loads (128B-swizzled tiles) on an
+//     mbarrier, then twelve tcgen05.mma (M=128, N=128, K=16, three products x
+//     four K steps) into a 128-column TMEM accumulator, and commits them to a
+//     second mbarrier.  The four warps then read the accumulator with
+//     tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = tile rows) and apply
+//     C -= acc with coalesced column accesses.  64 KB of shared memory per CTA
+//     lets three CTAs share an SM so one CTA's epilogue overlaps another's
+//     loads and MMAs.
+// Every mbarrier wait is bounded; on timeout the kernel records a status,
+// skips the epilogue and still frees its TMEM.
 #include "driver.h"
+#include "prof.h"
+#include "common.cuh"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
 
 namespace gb {
+namespace {
 
-int gemm_bf16x3_dev(int, int, int, const float*, int, const float*, int, float*, int, cudaStream_t) {
-  return (int)cudaErrorNotSupported;
+constexpr int kTcBM = 128;
+constexpr int kTcBN = 128;
+constexpr int kTcBK = 64;                      // one 128-byte swizzle row of bf16
+constexpr int kTcThreads = 128;
+constexpr int kTileBytesA = kTcBM * kTcBK * 2;  // 16 KB
+constexpr int kTileBytesB = kTcBN * kTcBK * 2;  // 16 KB
+constexpr int kStageBytes = 2 * kTileBytesA + 2 * kTileBytesB;   // hi + lo of A and B
+constexpr int kTcSmem = kStageBytes + 1024;    // + alignment slack for the 1024-byte swizzle atoms
+constexpr uint32_t kTmemCols = 128;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// Bounded parity wait; returns false after ~kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned spins = 0; spins < kSpinLimit; ++spins) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Shared-memory matrix descriptor of a K-major, 128B-swizzled bf16 tile whose
+// rows are 128 bytes and whose 8-row swizzle atoms are 1024 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);           // start address
+  d |= (uint64_t)(16 >> 4) << 16;                   // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;                 // stride byte offset: next 8-row group
+  d |= (uint64_t)1 << 46;                           // descriptor version for tcgen05
+  d |= (uint64_t)2 << 61;                           // 128-byte swizzle
+  return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M x N.
+__host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+      ::"r"(tmem_d), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__global__ void __launch_bounds__(kTcThreads)
+gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_constant__ CUtensorMap tm_al,
+                   const __grid_constant__ CUtensorMap tm_bh, const __grid_constant__ CUtensorMap tm_bl,
+                   float* __restrict__ C, int ldc, int M, int N, int nkb, int* __restrict__ status) {
+  extern __shared__ unsigned char tc_smem_raw[];
+  __shared__ __align__(8) uint64_t bar_load;
+  __shared__ __align__(8) uint64_t bar_mma;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int ok_s;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * kTcBM, n0 = blockIdx.y * kTcBN;
+  // 1024-byte aligned stage: [ah | al | bh | bl]
+  const uint32_t raw = smem_u32(tc_smem_raw);
+  unsigned char* stage = tc_smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  unsigned char* s_ah = stage;
+  unsigned char* s_al = stage + kTileBytesA;
+  unsigned char* s_bh = stage + 2 * kTileBytesA;
+  unsigned char* s_bl = stage + 2 * kTileBytesA + kTileBytesB;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    mbar_init(&bar_load, 1);
+    mbar_init(&bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    ok_s = 1;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  if (tid == 0) {
+    const uint32_t idesc = idesc_bf16_f32(kTcBM, kTcBN);
+    const uint32_t a_hi = smem_u32(s_ah), a_lo = smem_u32(s_al), b_hi = smem_u32(s_bh), b_lo = smem_u32(s_bl);
+    for (int kb = 0; kb < nkb; ++kb) {
+      mbar_expect_tx(&bar_load, kStageBytes);
+      tma_load_2d(s_ah, &tm_ah, kb * kTcBK, m0, &bar_load);
+      tma_load_2d(s_al, &tm_al, kb * kTcBK, m0, &bar_load);
+      tma_load_2d(s_bh, &tm_bh, kb * kTcBK, n0, &bar_load);
+      tma_load_2d(s_bl, &tm_bl, kb * kTcBK, n0, &bar_load);
+      if (!mbar_wait(&bar_load, kb & 1)) {
+        atomicCAS(status, kStatusOk, kStatusFlagTimeout);
+        ok_s = 0;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < kTcBK / 16; ++kk) {
+        const uint32_t off = kk * 32;   // 16 bf16 along K = 32 bytes inside the swizzled row
+        const uint64_t dah = smem_desc_sw128(a_hi + off), dal = smem_desc_sw128(a_lo + off);
+        const uint64_t dbh = smem_desc_sw128(b_hi + off), dbl = smem_desc_sw128(b_lo + off);
+        const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+        mma_bf16(tmem, dal, dbh, idesc, acc0);   // small terms first
+        mma_bf16(tmem, dah, dbl, idesc, 1u);
+        mma_bf16(tmem, dah, dbh, idesc, 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&bar_mma))
+                   : "memory");
+      // single-stage buffer: the next K block's loads wait for these MMAs
+      if (!mbar_wait(&bar_mma, kb & 1)) {
+        atomicCAS(status, kStatusOk, kStatusFlagTimeout);
+        ok_s = 0;
+        break;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+  if (ok_s && nkb > 0) {
+    // warp w reads TMEM lanes 32w..32w+31 = rows m0 + 32w + lane of the tile
+    const int m = m0 + warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c0 = 0; c0 < kTcBN; c0 += 32) {
+      float v[32];
+      tmem_ld_32cols(lane_base + (uint32_t)c0, v);
+      if (m < M) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int n = n0 + c0 + j;
+          if (n < N) {
+            float* p = C + (size_t)m + (size_t)n * ldc;
+            *p = *p - v[j];
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// A (M x K, column-major) -> ah/al [M][Kp] row-major bf16 (K contiguous),
+// through a 32 x 32 shared-memory transpose; zero for k >= K.
+__global__ void __launch_bounds__(256)
+split_a_kernel(const float* __restrict__ A, int lda, int M, int K, int Kp, __nv_bfloat16* __restrict__ ah,
+               __nv_bfloat16* __restrict__ al) {
+  __shared__ float t[32][33];
+  const int m0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+  for (int i = ty; i < 32; i += 8) {
+    int m = m0 + tx, k = k0 + i;
+    t[i][tx] = (m < M && k < K) ? A[(size_t)m + (size_t)k * lda] : 0.f;
+  }
+  __syncthreads();
+  for (int i = ty; i < 32; i += 8) {
+    int m = m0 + i, k = k0 + tx;
+    if (m < M && k < Kp) {
+      float x = t[tx][i];
+      __nv_bfloat16 h = __float2bfloat16_rn(x);
+      __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+      ah[(size_t)m * Kp + k] = h;
+      al[(size_t)m * Kp + k] = l;
+    }
+  }
+}
+
+// B (K x N, column-major: K contiguous per column) -> bh/bl [N][Kp].
+__global__ void __launch_bounds__(256)
+split_b_kernel(const float* __restrict__ B, int ldb, int K, int N, int Kp, __nv_bfloat16* __restrict__ bh,
+               __nv_bfloat16* __restrict__ bl) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)N * Kp) return;
+  int n = (int)(e / Kp), k = (int)(e - (size_t)n * Kp);
+  float x = k < K ? B[(size_t)k + (size_t)n * ldb] : 0.f;
+  __nv_bfloat16 h = __float2bfloat16_rn(x);
+  __nv_bfloat16 l = __float2bfloat16_rn(x - __bfloat162float(h));
+  bh[e] = h;
+  bl[e] = l;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// 2D map over a row-major bf16 array [rows][Kp], box 64 (K) x box_rows.
+bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 2};
+  cuuint32_t box[2] = {(cuuint32_t)kTcBK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+
+
+int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
+                    cudaStream_t s) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  const int Kp = (K + kTcBK - 1) / kTcBK * kTcBK;
+  const size_t bytes_a = (size_t)M * Kp * 2, bytes_b = (size_t)N * Kp * 2;
+  auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+  DevScratch ws(2 * up(bytes_a) + 2 * up(bytes_b), s);
+  if (!ws.p) return (int)cudaErrorMemoryAllocation;
+  char* base = ws.as<char>();
+  __nv_bfloat16* ah = reinterpret_cast<__nv_bfloat16*>(base);
+  __nv_bfloat16* al = reinterpret_cast<__nv_bfloat16*>(base + up(bytes_a));
+  __nv_bfloat16* bh = reinterpret_cast<__nv_bfloat16*>(base + 2 * up(bytes_a));
+  __nv_bfloat16* bl = reinterpret_cast<__nv_bfloat16*>(base + 2 * up(bytes_a) + up(bytes_b));
+
+  prof_begin(kProfGemmBf16x3, s);
+  dim3 ga((M + 31) / 32, (Kp + 31) / 32);
+  GB_LAUNCH(split_a_kernel<<<ga, 256, 0, s>>>(A, lda, M, K, Kp, ah, al));
+  size_t nb = (size_t)N * Kp;
+  GB_LAUNCH(split_b_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B, ldb, K, N, Kp, bh, bl));
+
+  CUtensorMap m_ah, m_al, m_bh, m_bl;
+  if (!make_map(&m_ah, ah, M, Kp, kTcBM) || !make_map(&m_al, al, M, Kp, kTcBM) ||
+      !make_map(&m_bh, bh, N, Kp, kTcBN) || !make_map(&m_bl, bl, N, Kp, kTcBN))
+    return (int)cudaErrorInvalidValue;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+    attr = true;
+  }
+  dim3 grid((M + kTcBM - 1) / kTcBM, (N + kTcBN - 1) / kTcBN);
+  GB_LAUNCH(gemm_bf16x3_kernel<<<grid, kTcThreads, kTcSmem, s>>>(m_ah, m_al, m_bh, m_bl, C, ldc, M, N, Kp / kTcBK,
+                                                                 device_status_word()));
+  prof_end(kProfGemmBf16x3, s, 2.0 * M * N * (double)K, 4.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
+  return (int)cudaGetLastError();
 }
 
 }  // namespace gb

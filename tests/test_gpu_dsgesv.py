@@ -1,0 +1,113 @@
+"""DSGESV on the GPU against the oracle's restatement of SRC/dsgesv.f.
+
+* FP32 CUDA-core factorization in exact mode: ITER, IPIV and X bitwise
+  identical to the oracle.
+* BF16x3 tensor-core factorization (the default): ITER >= 0 and the DDRVAB
+  pass rule DGET08 < sqrt(n) (TESTING/LIN/ddrvab.f:362-365) wherever the
+  refinement converges; the kappa = 1e10 case exhausts ITERMAX and falls back
+  to FP64 (ITER = -31, A holds the FP64 LU) exactly as the reference does.
+* INFO / ITER codes for a singular FP32 factor (ITER = -3) and an FP32
+  overflow in the conversion (ITER = -2).
+"""
+import numpy as np
+import pytest
+
+import oracle
+import oracle.checks as ck
+
+pytestmark = pytest.mark.gpu
+
+NLIST = [1, 2, 13, 17, 45, 78, 91, 101, 120, 132]          # TESTING/dstest.in N values
+NRHS = [1, 2, 15, 16]
+
+
+@pytest.fixture()
+def fp32_mode(gpu):
+    old = gpu.set_option("mixed", 1)
+    yield
+    gpu.set_option("mixed", old)
+
+
+@pytest.fixture()
+def bf16_mode(gpu):
+    old = gpu.set_option("mixed", 0)
+    yield
+    gpu.set_option("mixed", old)
+
+
+@pytest.mark.parametrize("n", NLIST)
+@pytest.mark.parametrize("nrhs", [1, 15])
+def test_dsgesv_exact_matches_oracle(gpu, exact_mode, fp32_mode, n, nrhs):
+    a = oracle.random_matrix(n, n, 2006 + n, idist=2)[0]
+    b = oracle.random_matrix(n, nrhs, 2007 + n, idist=2)[0]
+    ao_r, ip_r, x_r, it_r, info_r = oracle.dsgesv(a, b)
+    ao_g, ip_g, x_g, it_g, info_g = gpu.dsgesv(a, b)
+    assert (it_g, info_g) == (it_r, info_r)
+    np.testing.assert_array_equal(ip_g, ip_r)
+    assert x_g.tobytes() == x_r.tobytes()
+    assert ao_g.tobytes() == ao_r.tobytes()
+
+
+@pytest.mark.parametrize("n", [132, 1024, 2048])
+@pytest.mark.parametrize("kappa", [1e2, 1e6])
+def test_dsgesv_bf16x3_converges(gpu, bf16_mode, n, kappa):
+    a, s, _, _ = oracle.config_dsgesv_matrix(n, kappa, 3)
+    xt = np.random.default_rng(n).standard_normal((n, 2))
+    b = a @ xt
+    ao, ip, x, it, info = gpu.dsgesv(a, b)
+    assert info == 0
+    assert it >= 0, f"refinement did not converge (ITER={it})"
+    assert np.array_equal(ao, a)                     # A unchanged when ITER >= 0
+    assert ck.dget08(a, x, b) < np.sqrt(n)
+    assert ck.scaled_residual(a, x, b) <= 1.0
+
+
+def test_dsgesv_fallback_no_convergence(gpu, bf16_mode):
+    # kappa = 1e12: kappa * u_fp32 >> 1, refinement cannot converge
+    n = 512
+    a, s, _, _ = oracle.config_dsgesv_matrix(n, 1e12, 4)
+    b = a @ np.ones((n, 1))
+    ao, ip, x, it, info = gpu.dsgesv(a, b)
+    assert info == 0 and it == -31
+    lu_r, ip_r, info_r = oracle.getrf(a)
+    np.testing.assert_array_equal(ip, ip_r)
+    assert ck.lu_rel_diff(ao, lu_r, a) <= 64.0        # A holds the FP64 LU
+    assert ck.dget08(a, x, b) < 30.0
+
+
+@pytest.mark.parametrize("n", [512, 2048])
+def test_dsgesv_kappa_1e10_semantics(gpu, bf16_mode, n):
+    """At kappa = 1e10 refinement either converges slowly (ITER in 1..30, A
+    unchanged) or falls back (ITER = -31, A = FP64 LU); both end at FP64
+    backward error."""
+    a, s, _, _ = oracle.config_dsgesv_matrix(n, 1e10, 5)
+    b = a @ np.ones((n, 1))
+    ao, ip, x, it, info = gpu.dsgesv(a, b)
+    assert info == 0
+    if it >= 0:
+        assert np.array_equal(ao, a)
+        assert ck.dget08(a, x, b) < np.sqrt(n)
+    else:
+        assert it == -31
+        assert ck.dget08(a, x, b) < 30.0
+
+
+def test_dsgesv_singular_fp32(gpu):
+    n = 40
+    a = oracle.random_matrix(n, n, 9, idist=2)[0]
+    a[:, 5] = 0.0
+    b = np.ones((n, 1))
+    ao, ip, x, it, info = gpu.dsgesv(a, b)
+    _, _, _, it_r, info_r = oracle.dsgesv(a, b)
+    assert (it, info) == (it_r, info_r) == (-3, 6)
+
+
+def test_dsgesv_overflow_fp32(gpu):
+    n = 30
+    a = oracle.random_matrix(n, n, 10, idist=2)[0]
+    a[3, 4] = 1e300
+    b = np.ones((n, 1))
+    ao, ip, x, it, info = gpu.dsgesv(a, b)
+    _, _, x_r, it_r, info_r = oracle.dsgesv(a, b)
+    assert (it, info) == (it_r, info_r)
+    assert it == -2
