@@ -114,6 +114,16 @@ __device__ __forceinline__ void tmem_ld_32cols(uint32_t taddr, float (&v)[32]) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 consecutive columns of row m of C (zero outside the matrix).
+__device__ __forceinline__ void load_c_chunk(const float* __restrict__ C, int ldc, int M, int N, int m, int n_beg,
+                                             float (&out)[32]) {
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int n = n_beg + j;
+    out[j] = (m < M && n < N) ? __ldg(C + (size_t)m + (size_t)n * ldc) : 0.f;
+  }
+}
+
 __global__ void __launch_bounds__(kTcThreads)
 gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_constant__ CUtensorMap tm_al,
                    const __grid_constant__ CUtensorMap tm_bh, const __grid_constant__ CUtensorMap tm_bl,
@@ -150,6 +160,10 @@ gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_const
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
+  const int m = m0 + warp * 32 + lane;
+  // the first C chunk is fetched while the tensor cores work
+  float cpre[32];
+  load_c_chunk(C, ldc, M, N, m, n0, cpre);
 
   if (tid == 0) {
     const uint32_t idesc = idesc_bf16_f32(kTcBM, kTcBN);
@@ -192,21 +206,26 @@ gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_const
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
   if (ok_s && nkb > 0) {
-    // warp w reads TMEM lanes 32w..32w+31 = rows m0 + 32w + lane of the tile
-    const int m = m0 + warp * 32 + lane;
+    // warp w reads TMEM lanes 32w..32w+31 = rows m0 + 32w + lane of the tile;
+    // C is read a 32-column chunk ahead of the subtraction (all loads of a
+    // chunk issued before any store)
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    float nxt[32];
+#pragma unroll
+    for (int j = 0; j < 32; ++j) nxt[j] = cpre[j];
 #pragma unroll 1
     for (int c0 = 0; c0 < kTcBN; c0 += 32) {
+      float cur[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) cur[j] = nxt[j];
+      if (c0 + 32 < kTcBN) load_c_chunk(C, ldc, M, N, m, n0 + c0 + 32, nxt);
       float v[32];
       tmem_ld_32cols(lane_base + (uint32_t)c0, v);
       if (m < M) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int n = n0 + c0 + j;
-          if (n < N) {
-            float* p = C + (size_t)m + (size_t)n * ldc;
-            *p = *p - v[j];
-          }
+          if (n < N) C[(size_t)m + (size_t)n * ldc] = cur[j] - v[j];
         }
       }
     }

@@ -31,10 +31,35 @@ static int residual(int n, int nrhs, const double* A, int lda, const double* X, 
                     double* R, int ldr, cudaStream_t s) {
   unsigned grid = (unsigned)((n + kResidRows - 1) / kResidRows);
   prof_begin(kProfResidual, s);
-  if (options().exact)
+  if (options().exact) {
+    // the reference order: one sequential sum per row (SRC/dsgesv.f:328-332)
     GB_LAUNCH(residual_kernel<true><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs));
-  else
-    GB_LAUNCH(residual_kernel<false><<<grid, kResidRows, 0, s>>>(A, lda, X, ldx, B, ldb, R, ldr, n, nrhs));
+  } else {
+    // enough independent chains to keep the FP64 pipe busy: ~16 column
+    // chunks of >= 256 columns; right-hand sides in passes of 1, 2 or 4
+    int nsplit = std::max(1, std::min(16, n / 256));
+    int chunk = ((n + nsplit - 1) / nsplit + 31) / 32 * 32;
+    nsplit = (n + chunk - 1) / chunk;
+    const int rq = nrhs >= 4 ? 4 : (nrhs >= 2 ? 2 : 1);
+    DevScratch part(sizeof(double) * (size_t)nsplit * rq * n, s);
+    if (!part.p) return (int)cudaErrorMemoryAllocation;
+    for (int q0 = 0; q0 < nrhs; q0 += rq) {
+      dim3 g2(grid, nsplit);
+      size_t tot = (size_t)n * std::min(rq, nrhs - q0);
+      unsigned gr = (unsigned)((tot + 255) / 256);
+      double* P = part.as<double>();
+      if (rq == 4) {
+        GB_LAUNCH(residual_partial_kernel<4><<<g2, kResidRows, 0, s>>>(A, lda, X, ldx, n, nrhs, q0, chunk, P));
+        GB_LAUNCH(residual_reduce_kernel<4><<<gr, 256, 0, s>>>(P, nsplit, B, ldb, R, ldr, n, nrhs, q0));
+      } else if (rq == 2) {
+        GB_LAUNCH(residual_partial_kernel<2><<<g2, kResidRows, 0, s>>>(A, lda, X, ldx, n, nrhs, q0, chunk, P));
+        GB_LAUNCH(residual_reduce_kernel<2><<<gr, 256, 0, s>>>(P, nsplit, B, ldb, R, ldr, n, nrhs, q0));
+      } else {
+        GB_LAUNCH(residual_partial_kernel<1><<<g2, kResidRows, 0, s>>>(A, lda, X, ldx, n, nrhs, q0, chunk, P));
+        GB_LAUNCH(residual_reduce_kernel<1><<<gr, 256, 0, s>>>(P, nsplit, B, ldb, R, ldr, n, nrhs, q0));
+      }
+    }
+  }
   prof_end(kProfResidual, s, 2.0 * n * (double)n * nrhs, 8.0 * ((double)n * n + 3.0 * n * nrhs));
   return (int)cudaGetLastError();
 }

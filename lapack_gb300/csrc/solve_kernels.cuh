@@ -312,6 +312,61 @@ residual_kernel(const double* __restrict__ A, int lda, const double* __restrict_
   }
 }
 
+
+// Split-column form of the FP64 residual for the default (fused) mode.  On
+// GB300 one dependent DFMA chain per row cannot fill the FP64 pipe, so the
+// columns are cut into `nsplit` chunks: partial[s][q][i] is the sum over
+// chunk s of A(i,l)*X(l,q), and residual_reduce_kernel folds the chunks in
+// fixed order s = 0..nsplit-1 (deterministic run to run).
+template <int RQ>
+__global__ void __launch_bounds__(kResidRows)
+residual_partial_kernel(const double* __restrict__ A, int lda, const double* __restrict__ X, int ldx, int n,
+                        int nrhs, int q0, int chunk, double* __restrict__ partial) {
+  __shared__ double xs[32][RQ];
+  const int i = blockIdx.x * kResidRows + threadIdx.x;
+  const int s = blockIdx.y;
+  const int l_beg = s * chunk, l_end = min(n, l_beg + chunk);
+  const int nq = min(RQ, nrhs - q0);
+  double acc[RQ];
+#pragma unroll
+  for (int q = 0; q < RQ; ++q) acc[q] = 0.0;
+  for (int l0 = l_beg; l0 < l_end; l0 += 32) {
+    const int nl = min(32, l_end - l0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * RQ; e += kResidRows) {
+      int l = e % 32, q = e / 32;
+      xs[l][q] = (l < nl && q < nq) ? X[(size_t)(l0 + l) + (size_t)(q0 + q) * ldx] : 0.0;
+    }
+    __syncthreads();
+    if (i < n) {
+      double a[32];
+#pragma unroll
+      for (int u = 0; u < 32; ++u) a[u] = (u < nl) ? A[(size_t)i + (size_t)(l0 + u) * lda] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 32; ++u)
+#pragma unroll
+        for (int q = 0; q < RQ; ++q) acc[q] = fma(a[u], xs[u][q], acc[q]);
+    }
+  }
+  if (i < n) {
+#pragma unroll
+    for (int q = 0; q < RQ; ++q)
+      if (q < nq) partial[((size_t)s * RQ + q) * n + i] = acc[q];
+  }
+}
+
+template <int RQ>
+__global__ void residual_reduce_kernel(const double* __restrict__ partial, int nsplit, const double* __restrict__ B,
+                                       int ldb, double* __restrict__ R, int ldr, int n, int nrhs, int q0) {
+  size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nq = min(RQ, nrhs - q0);
+  if (e >= (size_t)n * nq) return;
+  int q = (int)(e / n), i = (int)(e - (size_t)q * n);
+  double sum = 0.0;
+  for (int s = 0; s < nsplit; ++s) sum += partial[((size_t)s * RQ + q) * n + i];
+  R[(size_t)i + (size_t)(q0 + q) * ldr] = B[(size_t)i + (size_t)(q0 + q) * ldb] - sum;
+}
+
 // Convergence test of SRC/dsgesv.f:337-342 for every right-hand side:
 // XNRM = |X(IDAMAX(X(:,j)),j)|, RNRM likewise, not converged when
 // RNRM > XNRM*CTE with CTE = ||A||_inf * eps * sqrt(n).  One CTA per
