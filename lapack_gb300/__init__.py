@@ -42,7 +42,7 @@ def lib():
     if _LIB is None:
         if not os.path.exists(LIB_PATH):
             raise LibraryMissing(f"{LIB_PATH} not built; run lapack_gb300.build()")
-        L = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_GLOBAL)
+        L = ctypes.CDLL(LIB_PATH)
         L.dlange_.restype = ctypes.c_double
         L.dlamch_.restype = ctypes.c_double
         L.slamch_.restype = ctypes.c_float
@@ -62,6 +62,11 @@ def lib():
 
 def _ref(v):
     return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _as2d(b):
+    b = np.asarray(b)
+    return b.reshape(b.shape[0], b.shape[1] if b.ndim == 2 else 1)
 
 
 def _ptr(a):
@@ -128,7 +133,7 @@ def getrs(lu, ipiv, b, trans="N"):
     """xGETRS (SRC/dgetrs.f): returns (x, info)."""
     dtype = lu.dtype
     lu = _fortran(lu, dtype)
-    b2 = _fortran(np.asarray(b).reshape(lu.shape[0], -1), dtype)
+    b2 = _fortran(_as2d(b), dtype)
     n, nrhs = b2.shape
     ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
     info = ctypes.c_int(0)
@@ -143,7 +148,7 @@ def gesv(a, b, dtype=None):
     dtype = np.dtype(dtype or (a.dtype if a.dtype in (np.float32, np.float64) else np.float64))
     a = _fortran(a, dtype)
     n = a.shape[0]
-    b2 = _fortran(np.asarray(b).reshape(n, -1), dtype)
+    b2 = _fortran(_as2d(b), dtype)
     ipiv = np.zeros(max(1, n), dtype=np.int32)
     info = ctypes.c_int(0)
     getattr(lib(), f"{_pre(dtype)}gesv_")(_ref(n), _ref(b2.shape[1]), _ptr(a), _ref(max(1, n)), _ptr(ipiv),
@@ -155,7 +160,7 @@ def dsgesv(a, b):
     """DSGESV (SRC/dsgesv.f): returns (a_out, ipiv, x, iter, info)."""
     a = _fortran(a, np.float64)
     n = a.shape[0]
-    b2 = _fortran(np.asarray(b).reshape(n, -1), np.float64)
+    b2 = _fortran(_as2d(b), np.float64)
     nrhs = b2.shape[1]
     x = np.zeros((n, nrhs), dtype=np.float64, order="F")
     work = np.zeros(max(1, n * nrhs), dtype=np.float64)

@@ -66,6 +66,11 @@ def lib():
     return _LIB
 
 
+def _as2d(b):
+    b = np.asarray(b)
+    return b.reshape(b.shape[0], b.shape[1] if b.ndim == 2 else 1)
+
+
 def _ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
@@ -98,7 +103,7 @@ def getrf(a, nb=64, margins=False):
 def getrs(lu, ipiv, b, trans="N"):
     """xGETRS (SRC/dgetrs.f) on a copy of ``b``: returns (x, info)."""
     lu = _colmajor(lu, lu.dtype)
-    b2 = _colmajor(b.reshape(b.shape[0], -1), lu.dtype)
+    b2 = _colmajor(_as2d(b), lu.dtype)
     n, nrhs = b2.shape
     ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
     info = np.zeros(1, dtype=np.int32)
@@ -110,7 +115,7 @@ def getrs(lu, ipiv, b, trans="N"):
 def gesv(a, b):
     """xGESV (SRC/dgesv.f): returns (lu, ipiv, x, info)."""
     a = _colmajor(a, a.dtype)
-    b2 = _colmajor(b.reshape(b.shape[0], -1), a.dtype)
+    b2 = _colmajor(_as2d(b), a.dtype)
     n = a.shape[0]
     ipiv = np.zeros(max(1, n), dtype=np.int32)
     info = np.zeros(1, dtype=np.int32)
@@ -122,7 +127,7 @@ def gesv(a, b):
 def dsgesv(a, b):
     """DSGESV (SRC/dsgesv.f): returns (a_out, ipiv, x, iter, info)."""
     a = _colmajor(a, np.float64)
-    b2 = _colmajor(b.reshape(b.shape[0], -1), np.float64)
+    b2 = _colmajor(_as2d(b), np.float64)
     n, nrhs = b2.shape
     x = np.zeros((n, nrhs), dtype=np.float64, order="F")
     work = np.zeros(max(1, n * nrhs), dtype=np.float64)
@@ -229,3 +234,46 @@ def config_dsgesv_matrix(n, kappa, seed, nrefl=64):
     for v in v2:            # A <- A H   (Q2^T = H_k ... H_1)
         a -= np.outer(a @ v, (2.0 / v.dot(v)) * v)
     return np.asfortranarray(a), s, v1, v2
+
+
+def ge_test_matrix(m, n, imat, seed):
+    """A matrix of the reference GE test type `imat` (TESTING/LIN/dlatb4.f:437-465,
+    zero columns as TESTING/LIN/dchkge.f:325-347), built from DLARNV draws:
+    1 diagonal, 2 upper / 3 lower triangular, 4 random kappa=2, 5/6/7 first /
+    last / trailing-half columns zeroed, 8 kappa = sqrt(0.1/eps), 9 kappa =
+    0.1/eps, 10 scaled near underflow, 11 near overflow.  Singular values are
+    geometric (DLATMS MODE 3) between 1 and 1/kappa; the orthogonal factors come
+    from QR of DLARNV normal matrices.  Returns (A, izero) with izero the
+    expected INFO for types 5-7 (0 otherwise)."""
+    eps = 2.0 ** -52
+    kappa = {8: np.sqrt(0.1 / eps), 9: 0.1 / eps}.get(imat, 2.0)
+    k = min(m, n)
+    if k == 0:
+        return np.zeros((m, n), order="F"), 0
+    iseed = seed_to_iseed(seed)
+    sv = kappa ** (-(np.arange(k) / max(k - 1, 1)))
+    if imat == 1:
+        a = np.zeros((m, n))
+        a[np.arange(k), np.arange(k)] = sv * np.sign(dlarnv(2, iseed, k) + 1e-300)
+    else:
+        u, _ = np.linalg.qr(dlarnv(3, iseed, m * m).reshape(m, m))
+        v, _ = np.linalg.qr(dlarnv(3, iseed, n * n).reshape(n, n))
+        a = (u[:, :k] * sv) @ v[:, :k].T
+        if imat == 2:
+            a = np.triu(a)
+            a[np.arange(k), np.arange(k)] = np.where(np.abs(np.diag(a)[:k]) < 0.5, 1.0, np.diag(a)[:k])
+        elif imat == 3:
+            a = np.tril(a)
+            a[np.arange(k), np.arange(k)] = np.where(np.abs(np.diag(a)[:k]) < 0.5, 1.0, np.diag(a)[:k])
+    if imat == 10:
+        a = a * 1e-290
+    elif imat == 11:
+        a = a * 1e290
+    izero = 0
+    if 5 <= imat <= 7:
+        izero = 1 if imat == 5 else (k if imat == 6 else k // 2 + 1)
+        if imat < 7:
+            a[:, izero - 1] = 0.0
+        else:
+            a[:, izero - 1:] = 0.0
+    return np.asfortranarray(a), izero

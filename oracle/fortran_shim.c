@@ -64,3 +64,13 @@ void dsgesv_(const int *n, const int *nrhs, double *a, const int *lda, int *ipiv
              double *x, const int *ldx, double *work, float *swork, int *iter, int *info) {
   or_dsgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, work, swork, iter, info);
 }
+
+/* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */
+int lsame_(const char *ca, const char *cb, size_t la, size_t lb) {
+  (void)la;
+  (void)lb;
+  char a = *ca, b = *cb;
+  if (a >= 'a' && a <= 'z') a = (char)(a - 32);
+  if (b >= 'a' && b <= 'z') b = (char)(b - 32);
+  return a == b;
+}

@@ -1,0 +1,115 @@
+"""The C-ABI boundary on the CPU (no GPU work is started): the shared
+library loads and exports every function declared in include/lapack_gb300.h,
+argument errors are reported through xerbla_ with the reference's INFO codes
+(the INFOT tables of TESTING/LIN/derrge.f and derrab.f) before any device
+work, and the LAPACKE layer's own argument checks return the reference codes."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "lapack_gb300.h")
+
+
+def _declared():
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    names = re.findall(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", txt)
+    skip = {"if", "defined", "sizeof", "void"}
+    return sorted({n for n in names if n not in skip and not n.isupper() and n not in ("malloc_fn", "free_fn")})
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import lapack_gb300
+    try:
+        return lapack_gb300.lib()
+    except lapack_gb300.LibraryMissing:
+        lapack_gb300.build()
+        return lapack_gb300.lib()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = _declared()
+    assert len(names) > 50
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+ERR_GETRF = [((-1, 0, 1), 1), ((0, -1, 1), 2), ((2, 1, 1), 4)]
+ERR_GETRS = [(("/", 0, 0, 1, 1), 1), (("N", -1, 0, 1, 1), 2), (("N", 0, -1, 1, 1), 3),
+             (("N", 2, 1, 1, 2), 5), (("N", 2, 1, 2, 1), 8)]
+ERR_GESV = [((-1, 0, 1, 1), 1), ((0, -1, 1, 1), 2), ((2, 1, 1, 2), 4), ((2, 1, 2, 1), 7)]
+ERR_DSGESV = [((-1, 0, 1, 1, 1), 1), ((0, -1, 1, 1, 1), 2), ((2, 1, 1, 2, 2), 4), ((2, 1, 2, 1, 2), 7),
+              ((2, 1, 2, 2, 1), 9)]
+
+
+def _i(v):
+    return ctypes.byref(ctypes.c_int(v))
+
+
+def test_fortran_abi_error_exits(lib):
+    import lapack_gb300 as g
+    g.xerbla_capture(True)
+    try:
+        a = np.zeros(16)
+        ip = np.zeros(4, dtype=np.int32)
+        p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+        info = ctypes.c_int(0)
+        for (m, n, lda), code in ERR_GETRF:
+            lib.dgetrf_(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("DGETRF", code)
+            lib.sgetrf_(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("SGETRF", code)
+        for (tr, n, nrhs, lda, ldb), code in ERR_GETRS:
+            lib.dgetrs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb),
+                        ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DGETRS", code)
+        for (n, nrhs, lda, ldb), code in ERR_GESV:
+            lib.dgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("DGESV", code)
+        it = ctypes.c_int(0)
+        for (n, nrhs, lda, ldb, ldx), code in ERR_DSGESV:
+            lib.dsgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), p(a), _i(ldx), p(a), p(a),
+                        ctypes.byref(it), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("DSGESV", code)
+        # quick returns touch nothing
+        lib.dgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
+        assert info.value == 0
+    finally:
+        g.xerbla_capture(False)
+
+
+def test_lapacke_argument_codes(lib, capfd):
+    """LAPACKE_dgesv.c / _work.c codes: bad layout -1; NaN in A -4, in B -7;
+    row-major lda < n -5, ldb < nrhs -8 (no GPU work reached)."""
+    import lapack_gb300 as g
+    g.xerbla_capture(True)
+    try:
+        p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+        a = np.eye(3)
+        b = np.ones((3, 1))
+        ip = np.zeros(3, dtype=np.int32)
+        lib.LAPACKE_set_nancheck(1)
+        assert lib.LAPACKE_dgesv(7, 3, 1, p(a), 3, p(ip), p(b), 3) == -1
+        an = a.copy()
+        an[1, 1] = np.nan
+        assert lib.LAPACKE_dgesv(102, 3, 1, p(an), 3, p(ip), p(b), 3) == -4
+        bn = b.copy()
+        bn[2, 0] = np.nan
+        assert lib.LAPACKE_dgesv(102, 3, 1, p(a), 3, p(ip), p(bn), 3) == -7
+        assert lib.LAPACKE_dgesv(101, 3, 1, p(a), 2, p(ip), p(b), 1) == -5
+        assert lib.LAPACKE_dgesv(101, 3, 2, p(a), 3, p(ip), p(b), 1) == -8
+        assert lib.LAPACKE_dgetrs(101, ord("N"), 3, 1, p(a), 2, p(ip), p(b), 1) == -6
+        assert lib.LAPACKE_dsgesv(101, 3, 2, p(a), 3, p(ip), p(b), 2, p(b), 1, p(ip)) == -10
+        # column-major argument errors come back from the Fortran routine shifted by one
+        assert lib.LAPACKE_dgesv(102, 3, 1, p(a), 2, p(ip), p(b), 3) == -5
+        ctypes.CDLL(None).fflush(None)
+        out = capfd.readouterr().out
+        assert "Wrong parameter 1 in LAPACKE_dgesv" in out
+        assert "Wrong parameter 5 in LAPACKE_dgesv_work" in out
+    finally:
+        g.xerbla_capture(False)

@@ -1,0 +1,143 @@
+"""This library's LAPACKE layer against the reference's own LAPACKE C
+sources, both compiled over the oracle's Fortran-ABI shim
+(`make -C oracle ref ours`), so the arithmetic underneath is identical and
+any difference is a difference in the wrapper semantics: layouts, NaN
+checks, INFO shifts, leading-dimension codes, transposition, IPIV handling.
+Needs the reference tree (to compile its LAPACKE sources); skipped where it
+is absent."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE = os.path.join(ROOT, "oracle")
+REF_SRC = "/root/reference/LAPACKE"
+
+
+@pytest.fixture(scope="module")
+def libs():
+    if not os.path.isdir(REF_SRC):
+        pytest.skip("reference LAPACKE sources not present")
+    subprocess.run(["make", "-s", "-C", ORACLE, "ref", "ours"], check=True)
+    ref = ctypes.CDLL(os.path.join(ORACLE, "_ref", "libref_lapacke.so"))
+    ours = ctypes.CDLL(os.path.join(ORACLE, "_ref", "libours_lapacke.so"))
+    return ref, ours
+
+
+def p(v):
+    return v.ctypes.data_as(ctypes.c_void_p)
+
+
+def _mat(m, n, seed, layout, ld_extra=0):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((m, n))
+    if layout == 102:          # column-major storage with ld = m + extra
+        ld = max(1, m + ld_extra)
+        buf = np.full((max(n, 1), ld), 7.25)
+        buf[:n, :m] = a.T
+    else:                      # row-major, ld = n + extra
+        ld = max(1, n + ld_extra)
+        buf = np.full((max(m, 1), ld), 7.25)
+        buf[:m, :n] = a
+    return buf, ld
+
+
+def _both(libs, fname, build, capfd):
+    outs = []
+    for L in libs:
+        args, arrays = build()
+        L.LAPACKE_set_nancheck(1)
+        rc = getattr(L, fname)(*args)
+        ctypes.CDLL(None).fflush(None)
+        printed = capfd.readouterr().out
+        outs.append((rc, [x.copy() for x in arrays], printed))
+    (r1, a1, p1), (r2, a2, p2) = outs
+    assert r1 == r2, (fname, r1, r2)
+    for x, y in zip(a1, a2):
+        assert x.tobytes() == y.tobytes(), fname
+    assert p1 == p2, (p1, p2)
+    return r1
+
+
+CASES = [(layout, n, nrhs, extra) for layout in (101, 102) for n in (0, 1, 5, 17) for nrhs in (0, 1, 3)
+         for extra in (0, 2)]
+
+
+@pytest.mark.parametrize("layout,n,nrhs,extra", CASES)
+def test_gesv_getrf_getrs_dsgesv(libs, capfd, layout, n, nrhs, extra):
+    def gesv():
+        a, lda = _mat(n, n, 1 + n, layout, extra)
+        b, ldb = _mat(n, nrhs, 2 + n, layout, extra)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        return (layout, n, nrhs, p(a), lda, p(ip), p(b), ldb), (a, b, ip)
+    _both(libs, "LAPACKE_dgesv", gesv, capfd)
+
+    def getrf():
+        a, lda = _mat(n, n + 2, 3 + n, layout, extra)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        return (layout, n, n + 2, p(a), lda, p(ip)), (a, ip)
+    _both(libs, "LAPACKE_dgetrf", getrf, capfd)
+
+    for tr in (b"N", b"T"):
+        def getrs():
+            a, lda = _mat(n, n, 4 + n, layout, extra)
+            a[np.arange(min(a.shape)), np.arange(min(a.shape))] += 4.0
+            b, ldb = _mat(n, nrhs, 5 + n, layout, extra)
+            ip = np.arange(1, max(n, 1) + 1, dtype=np.int32)[::-1].copy()
+            ip = np.maximum(ip, np.arange(1, max(n, 1) + 1, dtype=np.int32))
+            return (layout, ctypes.c_char(tr), n, nrhs, p(a), lda, p(ip), p(b), ldb), (b,)
+        _both(libs, "LAPACKE_dgetrs", getrs, capfd)
+
+    def dsgesv():
+        a, lda = _mat(n, n, 6 + n, layout, extra)
+        b, ldb = _mat(n, nrhs, 7 + n, layout, extra)
+        x, ldx = _mat(n, nrhs, 8 + n, layout, extra)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        it = np.zeros(1, dtype=np.int32)
+        return (layout, n, nrhs, p(a), lda, p(ip), p(b), ldb, p(x), ldx, p(it)), (a, x, ip, it)
+    _both(libs, "LAPACKE_dsgesv", dsgesv, capfd)
+
+
+@pytest.mark.parametrize("layout", [101, 102])
+def test_error_and_nan_paths(libs, capfd, layout):
+    def bad_layout():
+        a = np.eye(3)
+        b = np.ones(3)
+        ip = np.zeros(3, dtype=np.int32)
+        return (55, 3, 1, p(a), 3, p(ip), p(b), 3), (a,)
+    assert _both(libs, "LAPACKE_dgesv", bad_layout, capfd) == -1
+
+    def nan_a():
+        a, lda = _mat(4, 4, 1, layout)
+        a.flat[1] = np.nan
+        b, ldb = _mat(4, 1, 2, layout)
+        ip = np.zeros(4, dtype=np.int32)
+        return (layout, 4, 1, p(a), lda, p(ip), p(b), ldb), (a, b)
+    assert _both(libs, "LAPACKE_dgesv", nan_a, capfd) == -4
+
+    def small_ld():
+        a, lda = _mat(4, 4, 1, layout)
+        b, ldb = _mat(4, 2, 2, layout)
+        ip = np.zeros(4, dtype=np.int32)
+        return (layout, 4, 2, p(a), 3, p(ip), p(b), ldb), (a, b)
+    _both(libs, "LAPACKE_dgesv", small_ld, capfd)
+
+    for fn in ("LAPACKE_dlag2s",):
+        def lag2s():
+            a, lda = _mat(5, 3, 9, layout)
+            sa = np.full(a.shape, 1.5, dtype=np.float32)
+            return (layout, 5, 3, p(a), lda, p(sa), lda), (sa,)
+        _both(libs, fn, lag2s, capfd)
+
+
+@pytest.mark.parametrize("layout", [101, 102])
+@pytest.mark.parametrize("incx", [1, -1])
+def test_laswp(libs, capfd, layout, incx):
+    def laswp():
+        a, lda = _mat(9, 4, 3, layout)
+        ip = np.array([1, 3, 2, 9, 5, 5], dtype=np.int32)   # IPIV(K1..K2) = IPIV(2..6) is read
+        return (layout, 4, p(a), lda, 2, 6, p(ip), incx), (a,)
+    _both(libs, "LAPACKE_dlaswp", laswp, capfd)

@@ -1,0 +1,150 @@
+"""The oracle (C restatement of the reference routines) against the
+reference's own pins: the DLARUV multiplier table read from SRC/dlaruv.f,
+the TESTING/LIN test ratios over the TESTING/dtest.in and dstest.in grids,
+the error-exit tables, and an independent LU (OpenBLAS via scipy)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.checks as ck
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+INPUTS = json.load(open(os.path.join(GOLDEN, "test_inputs.json")))
+THRESH = INPUTS["dtest"]["thresh"]
+
+
+def test_dlaruv_multipliers_match_reference_table():
+    mm = json.load(open(os.path.join(GOLDEN, "dlaruv_mm.json")))["mm"]
+    assert len(mm) == 128
+    for i, row in enumerate(mm, start=1):
+        assert oracle.dlaruv_power(i) == row, f"MM({i},:)"
+
+
+def test_dlarnv_stream_properties():
+    it1 = oracle.seed_to_iseed(7)
+    a = oracle.dlarnv(1, it1, 200)
+    it2 = oracle.seed_to_iseed(7)
+    b = np.concatenate([oracle.dlarnv(1, it2, 64), oracle.dlarnv(1, it2, 136)])
+    assert np.array_equal(a, b)                 # chunking does not change the stream
+    assert np.all((a > 0) & (a < 1))
+    assert np.array_equal(it1, it2)
+    u = oracle.dlarnv(2, oracle.seed_to_iseed(1), 100000)
+    assert np.all((u > -1) & (u < 1)) and abs(u.mean()) < 0.02
+    z = oracle.dlarnv(3, oracle.seed_to_iseed(0), 100000)
+    assert abs(z.mean()) < 0.02 and abs(z.std() - 1) < 0.02
+
+
+@pytest.mark.parametrize("imat", range(1, 12))
+@pytest.mark.parametrize("nb", sorted(set(INPUTS["dtest"]["nb"])))
+def test_dgetrf_dchkge_ratios(imat, nb):
+    """DCHKGE tests 1, 3, 4 (TESTING/LIN/dchkge.f:280-583) on every M x N of
+    dtest.in: INFO = IZERO for the zero-column types, DGET01 < THRESH,
+    and for square nonsingular systems DGET02 / DGET04 < THRESH."""
+    for m in INPUTS["dtest"]["m"]:
+        for n in INPUTS["dtest"]["n"]:
+            if 5 <= imat <= 7 and n < imat - 4:
+                continue
+            a, izero = oracle.ge_test_matrix(m, n, imat, 1988 + 7 * m + n)
+            lu, ipiv, info = oracle.getrf(a, nb=nb)
+            assert info == izero, (m, n, imat, info, izero)
+            if m and n:
+                assert ck.dget01(a, lu, ipiv) < THRESH, (m, n, imat)
+            if m == n and n > 0 and izero == 0:
+                for nrhs in INPUTS["dtest"]["nrhs"]:
+                    xact = oracle.random_matrix(n, nrhs, 5 + n + nrhs, idist=2)[0]
+                    for trans in "NTC":
+                        b = (a if trans == "N" else a.T) @ xact
+                        x, info = oracle.getrs(lu, ipiv, b, trans)
+                        assert info == 0
+                        assert ck.dget02(a, x, b, "N" if trans == "N" else "T") < THRESH
+                        rcond = 1.0 / np.linalg.cond(a, 1)
+                        assert ck.dget04(x, xact, rcond) < THRESH
+
+
+@pytest.mark.parametrize("nrhs", INPUTS["dstest"]["nrhs"])
+def test_dsgesv_ddrvab_ratios(nrhs):
+    """DDRVAB (TESTING/LIN/ddrvab.f): DGET08 < sqrt(N) when ITER >= 0, else <
+    THRESH, INFO = IZERO, on the dstest.in N list for GE types 1-11."""
+    for n in INPUTS["dstest"]["n"]:
+        for imat in range(1, 12):
+            if 5 <= imat <= 7 and n < imat - 4:
+                continue
+            a, izero = oracle.ge_test_matrix(n, n, imat, 2006 + n + imat)
+            xact = oracle.random_matrix(n, nrhs, 2009 + n, idist=2)[0]
+            b = a @ xact
+            ao, ip, x, it, info = oracle.dsgesv(a, b)
+            assert info == izero, (n, imat, info, izero)
+            if n == 0 or izero:
+                continue
+            r = ck.dget08(a, x, b)
+            if it >= 0:
+                assert r < np.sqrt(n) or r < 1.0, (n, imat, it, r)
+                assert np.array_equal(ao, a)
+            else:
+                assert r < THRESH, (n, imat, it, r)
+
+
+def test_oracle_ipiv_matches_openblas():
+    scipy_linalg = pytest.importorskip("scipy.linalg")
+    for n, seed in ((64, 1), (200, 2), (513, 3)):
+        a = oracle.random_matrix(n, n, seed, idist=3)[0]
+        lu, ip, info = oracle.getrf(a)
+        lu2, piv2 = scipy_linalg.lu_factor(a)
+        assert np.array_equal(piv2 + 1, ip)
+        assert ck.lu_rel_diff(lu, lu2, a) < 64.0
+
+
+def test_pivot_margins_recorded():
+    a = oracle.random_matrix(100, 100, 4, idist=3)[0]
+    lu, ip, info, margin = oracle.getrf(a, margins=True)
+    assert margin.shape == (100,) and np.all(margin >= 0) and np.all(margin <= 1)
+    b = a.copy()
+    b[0, 0] = b[1, 0] = 10.0                      # exact tie in column 1: IDAMAX takes the first
+    lu, ip, info, margin = oracle.getrf(b, margins=True)
+    assert ip[0] == 1 and margin[0] == 0.0
+
+
+def test_idamax_nan_rule():
+    # BLAS/SRC/idamax.f:101-107: a NaN is only chosen when it is element 1
+    L = oracle.lib()
+    x = np.array([1.0, np.nan, 3.0, -3.0])
+    assert L.or_diamax(4, x.ctypes.data_as(oracle.ctypes.c_void_p), 1) == 3
+    y = np.array([np.nan, 5.0, 7.0])
+    assert L.or_diamax(3, y.ctypes.data_as(oracle.ctypes.c_void_p), 1) == 1
+
+
+ERR_GETRF = [((-1, 0, 1), -1), ((0, -1, 1), -2), ((2, 1, 1), -4)]          # TESTING/LIN/derrge.f:133-142
+ERR_GETRS = [(("/", 0, 0, 1, 1), -1), (("N", -1, 0, 1, 1), -2), (("N", 0, -1, 1, 1), -3),
+             (("N", 2, 1, 1, 2), -5), (("N", 2, 1, 2, 1), -8)]              # derrge.f:169-184
+ERR_DSGESV = [((-1, 0, 1, 1, 1), -1), ((0, -1, 1, 1, 1), -2), ((2, 1, 1, 2, 2), -4),
+              ((2, 1, 2, 1, 2), -7), ((2, 1, 2, 2, 1), -9)]                 # TESTING/LIN/derrab.f:113-127
+
+
+def _oracle_err(fn, *args):
+    oracle.xerbla_reset()
+    fn(*args)
+    return oracle.xerbla_last()
+
+
+def test_oracle_error_exits():
+    import ctypes
+    L = oracle.lib()
+    a = np.zeros(16)
+    ip = np.zeros(4, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    for (m, n, lda), code in ERR_GETRF:
+        name, inf = _oracle_err(L.or_dgetrf_nb, m, n, p(a), lda, p(ip), p(info), 64)
+        assert (name, inf) == ("DGETRF", -code)
+    for (tr, n, nrhs, lda, ldb), code in ERR_GETRS:
+        name, inf = _oracle_err(L.or_dgetrs, tr.encode(), n, nrhs, p(a), lda, p(ip), p(a), ldb, p(info))
+        assert (name, inf) == ("DGETRS", -code)
+    L.or_dsgesv.argtypes = [ctypes.c_int] * 2 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                  ctypes.c_int, ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 4
+    for (n, nrhs, lda, ldb, ldx), code in ERR_DSGESV:
+        name, inf = _oracle_err(L.or_dsgesv, n, nrhs, p(a), lda, p(ip), p(a), ldb, p(a), ldx, p(a), p(a),
+                                p(info), p(info))
+        assert (name, inf) == ("DSGESV", -code)
