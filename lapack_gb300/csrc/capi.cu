@@ -512,6 +512,9 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "nb32")) { old = o.nb_f32; o.nb_f32 = std::max(1, value); }
   else if (!strcmp(name, "mixed")) { old = o.mixed_mode; o.mixed_mode = value; }
   else if (!strcmp(name, "sgetrf")) { old = o.sgetrf_mode; o.sgetrf_mode = value; }
+  else if (!strcmp(name, "panel_ctas64")) { old = o.panel_ctas_f64; o.panel_ctas_f64 = value; }
+  else if (!strcmp(name, "panel_ctas32")) { old = o.panel_ctas_f32; o.panel_ctas_f32 = value; }
+  else if (!strcmp(name, "cluster_panel")) { old = o.cluster_panel; o.cluster_panel = value; }
   else return -1;
   return old;
 }
@@ -522,6 +525,9 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "nb32")) return o.nb_f32;
   if (!strcmp(name, "mixed")) return o.mixed_mode;
   if (!strcmp(name, "sgetrf")) return o.sgetrf_mode;
+  if (!strcmp(name, "panel_ctas64")) return o.panel_ctas_f64;
+  if (!strcmp(name, "panel_ctas32")) return o.panel_ctas_f32;
+  if (!strcmp(name, "cluster_panel")) return o.cluster_panel;
   return -1;
 }
 int gb300_status(int clear) {

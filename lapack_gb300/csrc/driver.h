@@ -17,6 +17,9 @@ struct Options {
   int nb_f32 = 256;         // outer block size of the FP32 factorization
   int mixed_mode = kMixedBf16x3;
   int sgetrf_mode = kMixedFp32;   // sgetrf_ itself: plain FP32 by default
+  int panel_ctas_f64 = 0;         // CTAs of the cooperative panel (0: all SMs)
+  int panel_ctas_f32 = 0;
+  int cluster_panel = 1;          // FP32 leaves on one thread-block cluster (DSMEM exchange)
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 

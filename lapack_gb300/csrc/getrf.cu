@@ -9,6 +9,7 @@
 #include "prof.h"
 #include "gemm_simt.cuh"
 #include "lu_kernels.cuh"
+#include "panel_cluster.cuh"
 #include "solve_kernels.cuh"
 
 #include <algorithm>
@@ -30,6 +31,9 @@ Options& options() {
     x.exact = env_int("LAPACK_GB300_EXACT", 0) != 0;
     x.nb_f64 = std::max(1, env_int("LAPACK_GB300_NB64", 64));
     x.nb_f32 = std::max(1, env_int("LAPACK_GB300_NB32", 256));
+    x.panel_ctas_f64 = env_int("LAPACK_GB300_PANEL_CTAS64", 0);
+    x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
+    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 1);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -150,29 +154,40 @@ struct PanelCtx {
   PanelScratch<T> ps;
   int* status;
   int max_optin;
+  size_t words_bytes;    // candidate words + pair count, zeroed before each leaf
 };
 
 template <typename T, bool EXACT>
 static int launch_leaf(T* P, int lda, int M, int JB, int row0, int* ipiv, int* info, PanelCtx<T>& cx,
                        cudaStream_t s) {
   const int nsm = device_sm_count();
-  int R = std::max(32, (M + nsm - 1) / nsm);
+  // CTAs taking part in the panel: all SMs for FP64 (its FMA rate is low, the
+  // rank-1 updates need every SM); fewer for FP32, where the per-column grid
+  // barrier dominates and a smaller grid synchronises faster
+  const Options& opt = options();
+  int gmax = sizeof(T) == 8 ? opt.panel_ctas_f64 : opt.panel_ctas_f32;
+  if (gmax <= 0 || gmax > nsm) gmax = nsm;
+  int R = std::max(32, (M + gmax - 1) / gmax);
   int G = (M + R - 1) / R;
   size_t smem = (size_t)JB * R * sizeof(T) + (size_t)R * sizeof(int) + 16;
   auto kern = leaf_panel_kernel<T, EXACT>;
-  static bool attr_done[64] = {false};
+  static int dyn_cap_dev[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
-  const int dyn_cap = cx.max_optin - 2048;
-  if (!attr_done[dev]) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap);
-    attr_done[dev] = true;
+  if (!dyn_cap_dev[dev]) {
+    cudaFuncAttributes fa;
+    GB_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)kern));
+    const int cap = cx.max_optin - (int)fa.sharedSizeBytes;
+    GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, cap));
+    dyn_cap_dev[dev] = cap;
   }
+  const int dyn_cap = dyn_cap_dev[dev];
   if ((long long)smem > dyn_cap) return 1000 + kStatusCapacity;   // panel taller than the GPU's shared memory holds
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kPanelThreads, smem);
   if (occ * nsm < G) return 1000 + kStatusCapacity;
-  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.counter, 0, 2 * sizeof(int), s));
+  if (G > device_sm_count()) return 1000 + kStatusCapacity;   // scratch is sized for one CTA per SM
+  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.word, 0, cx.words_bytes, s));
   PanelScratch<T> ps = cx.ps;
   int* status = cx.status;
   void* args[] = {&P, &lda, &M, &JB, &R, &row0, &ipiv, &info, &ps, &status};
@@ -197,6 +212,92 @@ static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, Panel
   return (int)cudaGetLastError();
 }
 
+// ---- cluster leaf (FP32): availability, width and launch
+struct ClusterCaps {
+  bool ok = false;
+  int dyn_cap = 0;
+};
+
+template <bool EXACT>
+static ClusterCaps cluster_caps() {
+  static ClusterCaps caps[64];
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!done[dev]) {
+    done[dev] = true;
+    auto kern = leaf_panel_cluster_kernel<EXACT>;
+    cudaFuncAttributes fa;
+    int optin = 0;
+    if (cudaFuncGetAttributes(&fa, (const void*)kern) == cudaSuccess &&
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess) {
+      const int cap = optin - (int)fa.sharedSizeBytes;
+      if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, cap) == cudaSuccess &&
+          cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kClusterCtas;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(kClusterCtas);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = cap;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int nclusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
+          caps[dev].ok = true;
+          caps[dev].dyn_cap = cap;
+        }
+      }
+    }
+    cudaGetLastError();   // clear any error from an unsupported query
+  }
+  return caps[dev];
+}
+
+// Widest leaf (64, 32, 16 or 8 columns) whose M-row panel fits the shared
+// memory of one cluster; 0 when the cluster leaf cannot be used.
+template <typename T>
+static int cluster_leaf_width(int M) {
+  if (sizeof(T) != 4 || options().cluster_panel == 0) return 0;
+  ClusterCaps c = options().exact ? cluster_caps<true>() : cluster_caps<false>();
+  if (!c.ok) return 0;
+  const long long R = (M + kClusterCtas - 1) / kClusterCtas;
+  for (int lw = kLeafMax; lw >= 8; lw /= 2)
+    if ((long long)(lw + 1) * R * 4 + 16 <= c.dyn_cap) return lw;
+  return 0;
+}
+
+template <bool EXACT>
+static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
+                               PanelCtx<float>& cx, cudaStream_t s) {
+  ClusterCaps c = cluster_caps<EXACT>();
+  const int R = (M + kClusterCtas - 1) / kClusterCtas;
+  size_t smem = (size_t)JB * R * 4 + (size_t)R * 4 + 16;
+  if (!c.ok || (long long)smem > c.dyn_cap) return 1000 + kStatusCapacity;
+  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  prof_begin(kProfPanel, s);
+  int rc = (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT>, P, lda, M, JB, R, row0, ipiv, info,
+                                   cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status);
+  count_launch();
+  prof_end(kProfPanel, s, (double)M * JB * JB, 2.0 * 4.0 * (double)M * JB);
+  return rc;
+}
+
 // DGETRF2-shaped recursion on the panel of columns [c0, c0+w), rows [c0, m).
 // Each leaf applies its interchanges to every other column of the matrix
 // (left: the DLASWP of SRC/dgetrf.f:193, right: SRC/dgetrf2.f:236 and
@@ -204,14 +305,26 @@ static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, Panel
 template <typename T>
 static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int* info, PanelCtx<T>& cx,
                      cudaStream_t s, int gemm_mode) {
-  if (w <= kLeafMax) {
+  const int clw = cluster_leaf_width<T>(m - c0);
+  const int leaf = clw ? clw : kLeafMax;
+  if (w <= leaf) {
     T* P = A + c0 + (size_t)c0 * lda;
-    int rc = options().exact ? launch_leaf<T, true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+    int rc;
+    if constexpr (sizeof(T) == 4) {
+      if (clw)
+        rc = options().exact ? launch_leaf_cluster<true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                             : launch_leaf_cluster<false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+      else
+        rc = options().exact ? launch_leaf<T, true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
                              : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+    } else {
+      rc = options().exact ? launch_leaf<T, true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                           : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+    }
     if (rc) return rc;
     return laswp_pairs<T>(A, lda, n, c0, c0 + w, w, cx, s);
   }
-  int n1 = ((w / 2) + 31) / 32 * 32;
+  int n1 = ((w / 2) + 7) / 8 * 8;
   if (n1 >= w) n1 = w / 2;
   int rc = getrf_rec<T>(A, lda, m, n, c0, n1, ipiv, info, cx, s, gemm_mode);
   if (rc) return rc;
@@ -236,27 +349,28 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   const int G = nsm;
   size_t bytes = 0;
   auto carve = [&](size_t b) { size_t off = bytes; bytes += (b + 255) / 256 * 256; return off; };
-  size_t o_cand = carve(sizeof(Cand<T>) * 2 * G);
+  size_t o_word = carve(sizeof(unsigned long long) * 2 * G + sizeof(int));   // words, then the pair count
+  size_t o_abs = carve(sizeof(T) * 2 * G);
   size_t o_clab = carve(sizeof(int) * 2 * G);
   size_t o_crow = carve(sizeof(T) * 2 * G * kLeafMax);
   size_t o_rowk = carve(sizeof(T) * 2 * kLeafMax);
   size_t o_rkl = carve(sizeof(int) * 2);
-  size_t o_ctl = carve(sizeof(int) * 2);
   size_t o_pd = carve(sizeof(int) * 2 * kLeafMax);
   size_t o_psrc = carve(sizeof(int) * 2 * kLeafMax);
   DevScratch ws(bytes, s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
   char* base = ws.as<char>();
   PanelCtx<T> cx;
-  cx.ps.cand = reinterpret_cast<Cand<T>*>(base + o_cand);
+  cx.ps.word = reinterpret_cast<unsigned long long*>(base + o_word);
+  cx.ps.pair_count = reinterpret_cast<int*>(base + o_word + sizeof(unsigned long long) * 2 * G);
+  cx.ps.absval = reinterpret_cast<T*>(base + o_abs);
   cx.ps.cand_label = reinterpret_cast<int*>(base + o_clab);
   cx.ps.cand_row = reinterpret_cast<T*>(base + o_crow);
   cx.ps.row_k = reinterpret_cast<T*>(base + o_rowk);
   cx.ps.row_k_label = reinterpret_cast<int*>(base + o_rkl);
-  cx.ps.counter = reinterpret_cast<unsigned*>(base + o_ctl);
-  cx.ps.pair_count = reinterpret_cast<int*>(base + o_ctl) + 1;
   cx.ps.pair_dst = reinterpret_cast<int*>(base + o_pd);
   cx.ps.pair_src = reinterpret_cast<int*>(base + o_psrc);
+  cx.words_bytes = sizeof(unsigned long long) * 2 * G + sizeof(int);
   cx.status = device_status_word();
   cx.max_optin = optin;
   if (!cx.status) return (int)cudaErrorMemoryAllocation;

@@ -9,28 +9,74 @@ constexpr int kPanelThreads = 256;
 constexpr int kLeafMax = 64;      // widest panel the cooperative leaf kernel factors
 
 // Global scratch of one leaf-panel launch (sized for G CTAs and JB <= 64).
+// Per column k, CTA g publishes its pivot candidate in word[k&1][g]: the
+// upper 32 bits an order-preserving key of the candidate (see cand_key), the
+// lower 32 bits its row (25 bits) and the column sequence number k+1
+// (7 bits).  For double the key cannot hold |a| exactly, so |a| itself goes
+// to absval[k&1][g] before the word is released.  Readers poll the words
+// (acquire) until every sequence number reads k+1: that poll is both the
+// grid barrier and the candidate exchange.
 template <typename T>
 struct PanelScratch {
-  Cand<T>* cand;       // [2][G]
-  int* cand_label;     // [2][G]
-  T* cand_row;         // [2][G][kLeafMax]
-  T* row_k;            // [2][kLeafMax]
-  int* row_k_label;    // [2]
-  unsigned* counter;   // grid-barrier counter, zeroed before the launch
-  int* pair_dst;       // [2*kLeafMax] global 0-based destination rows
-  int* pair_src;       // [2*kLeafMax] global 0-based source rows
-  int* pair_count;     // number of valid pairs
+  unsigned long long* word;   // [2][G], zeroed before the launch
+  T* absval;                  // [2][G]   (double only)
+  int* cand_label;            // [2][G]
+  T* cand_row;                // [2][G][kLeafMax]
+  T* row_k;                   // [2][kLeafMax]
+  int* row_k_label;           // [2]
+  int* pair_dst;              // [2*kLeafMax] global 0-based destination rows
+  int* pair_src;              // [2*kLeafMax] global 0-based source rows
+  int* pair_count;            // number of valid pairs beyond the JB top rows, zeroed before the launch
 };
+
+// 32-bit key, larger is better, that orders candidates as cand_better does
+// on class and |value| (row ties are broken separately): 0 = NaN elsewhere,
+// 1 + bits(|v|) for an ordinary value (float; for double the high word of
+// |v|, refined by absval), 0xFFFFFFFF = leading NaN.
+template <typename T>
+__device__ __forceinline__ unsigned cand_key(const Cand<T>& c) {
+  if (c.cls == 2) return 0xFFFFFFFFu;
+  if (c.cls <= 0) return 0u;
+  if constexpr (sizeof(T) == 4) return __float_as_uint((float)c.absval) + 1u;
+  else return (unsigned)(__double_as_longlong((double)c.absval) >> 32) + 1u;
+}
+
+// Copies JB <= 64 elements with 16-byte accesses (all loads issued before
+// the stores); both pointers 16-byte aligned, the tail past JB is copied too
+// (the buffers hold kLeafMax elements).
+template <typename T, bool SRC_GLOBAL_CG>
+__device__ __forceinline__ void copy_row64(T* __restrict__ dst, const T* __restrict__ src) {
+  constexpr int NV = kLeafMax * (int)sizeof(T) / 16;
+  const uint4* s4 = reinterpret_cast<const uint4*>(src);
+  uint4* d4 = reinterpret_cast<uint4*>(dst);
+  uint4 v[NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = SRC_GLOBAL_CG ? __ldcg(s4 + i) : s4[i];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) d4[i] = v[i];
+}
+
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 
 // Leaf panel factorization, DGETRF2 semantics (SRC/dgetrf2.f:170-265) on an
 // M x JB panel (JB <= 64) whose top-left element is row `row0` of the
 // matrix.  The panel is spread over the co-resident CTAs of a cooperative
-// grid, R consecutive rows per CTA held in shared memory.  For each column:
-// every CTA finds its best candidate (IDAMAX order), publishes it together
-// with its whole row, one grid barrier, then every CTA picks the same winner,
-// swaps, scales (reciprocal when |pivot| >= sfmin, else divides) and applies
-// the rank-1 update to its rows.  The interchanges of whole panel rows are
-// summarised at the end as (dst, src) row pairs for the other columns.
+// grid, R consecutive rows per CTA held in shared memory (column-major tile).
+// Per column k, warp 0 of every CTA finds the CTA's best candidate among its
+// rows >= k (IDAMAX order), publishes it with its whole row, passes the grid
+// barrier, reduces the G published candidates to the same winner, fetches
+// the winning row and performs the row interchange in shared memory; then
+// all threads scale the column below the pivot (reciprocal when
+// |pivot| >= sfmin, else division) and apply the rank-1 update to the rest of
+// their rows.  Two block-wide barriers per column.  The interchanges of
+// whole panel rows are summarised at the end as (dst, src) row pairs.
 template <typename T, bool EXACT>
 __global__ void __launch_bounds__(kPanelThreads)
 leaf_panel_kernel(T* __restrict__ P, int lda, int M, int JB, int R, int row0,
@@ -39,11 +85,13 @@ leaf_panel_kernel(T* __restrict__ P, int lda, int M, int JB, int R, int row0,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* tile = reinterpret_cast<T*>(smem_raw);                       // [JB][R]
   int* label = reinterpret_cast<int*>(tile + (size_t)JB * R);     // [R]
-  __shared__ T urow[kLeafMax];
-  __shared__ Cand<T> red[kPanelThreads / 32];
-  __shared__ int redw[kPanelThreads / 32];
-  __shared__ Cand<T> win_s;
-  __shared__ int win_cta_s;
+  __shared__ __align__(16) T urow[kLeafMax];
+  __shared__ __align__(16) T rowk_s[kLeafMax];
+  __shared__ __align__(16) T stage_c[kLeafMax];
+  __shared__ __align__(16) T stage_k[kLeafMax];
+  __shared__ int win_label_s, rowk_label_s;
+  __shared__ T pv_s;
+  __shared__ int ok_s;
 
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -55,124 +103,144 @@ leaf_panel_kernel(T* __restrict__ P, int lda, int M, int JB, int R, int row0,
     tile[c * R + r] = P[(size_t)(rbeg + r) + (size_t)c * lda];
   }
   for (int r = tid; r < nrows; r += kPanelThreads) label[r] = rbeg + r;
+  if (tid == 0) ok_s = 1;
   __syncthreads();
 
-  bool ok = true;
-  for (int k = 0; k < JB && ok; ++k) {
+  for (int k = 0; k < JB; ++k) {
     const int par = k & 1;
-    // 1. local candidate among owned rows >= k
-    Cand<T> best;
-    best.absval = 0; best.row = -1; best.cls = -1;
-    for (int r = tid; r < nrows; r += kPanelThreads) {
-      int g = rbeg + r;
-      if (g >= k) {
-        Cand<T> c = make_cand(tile[k * R + r], g, k);
+    if (warp == 0) {
+      // 1. the CTA's candidate among its rows >= k
+      Cand<T> best;
+      best.absval = 0; best.row = -1; best.cls = -1;
+      for (int r = max(0, k - rbeg) + lane; r < nrows; r += 32) {
+        Cand<T> c = make_cand(tile[k * R + r], rbeg + r, k);
         if (cand_better(c, best)) best = c;
       }
-    }
-    best = warp_best(best);
-    if (lane == 0) red[warp] = best;
-    __syncthreads();
-    if (warp == 0) {
-      Cand<T> c = (lane < kPanelThreads / 32) ? red[lane] : Cand<T>{0, -1, -1};
-      c = warp_best(c);
+      best = warp_best(best);
+      const bool own_k = (k >= rbeg && k < rbeg + nrows);
+      const unsigned seq = (unsigned)(k + 1);
+      // 2. lane 0 alone writes what this CTA publishes for column k (its
+      //    candidate row, row k if it owns it) and then releases the word
+      // the warp gathers the rows from the column-major tile into staging
+      if (best.row >= 0)
+        for (int c = lane; c < kLeafMax; c += 32) stage_c[c] = c < JB ? tile[c * R + (best.row - rbeg)] : T(0);
+      if (own_k)
+        for (int c = lane; c < kLeafMax; c += 32) stage_k[c] = c < JB ? tile[c * R + (k - rbeg)] : T(0);
+      __syncwarp();
       if (lane == 0) {
-        win_s = c;
-        w.cand[par * G + b] = c;
+        if (best.row >= 0) {
+          copy_row64<T, false>(w.cand_row + ((size_t)par * G + b) * kLeafMax, stage_c);
+          w.cand_label[par * G + b] = label[best.row - rbeg];
+        }
+        if (own_k) {
+          copy_row64<T, false>(w.row_k + par * kLeafMax, stage_k);
+          w.row_k_label[par] = label[k - rbeg];
+        }
+        if constexpr (sizeof(T) == 8) w.absval[par * G + b] = best.absval;
+        const unsigned rowbits = (unsigned)(best.row < 0 ? 0x1FFFFFF : best.row) & 0x1FFFFFFu;
+        const unsigned long long wv =
+            ((unsigned long long)cand_key(best) << 32) | ((unsigned long long)rowbits << 7) | (unsigned long long)seq;
+        st_release_u64(w.word + par * G + b, wv);
       }
-    }
-    __syncthreads();
-    if (win_s.row >= 0) {
-      int lr = win_s.row - rbeg;
-      for (int c = tid; c < JB; c += kPanelThreads) w.cand_row[((size_t)par * G + b) * kLeafMax + c] = tile[c * R + lr];
-      if (tid == 0) w.cand_label[par * G + b] = label[lr];
-    }
-    if (k >= rbeg && k < rbeg + nrows) {
-      int lk = k - rbeg;
-      for (int c = tid; c < JB; c += kPanelThreads) w.row_k[par * kLeafMax + c] = tile[c * R + lk];
-      if (tid == 0) w.row_k_label[par] = label[lk];
-    }
-    // 2. one grid barrier per column
-    ok = grid_barrier(w.counter, (unsigned)k, status);
-    if (!ok) break;
-    // 3. every CTA reduces the same G candidates to the same winner
-    Cand<T> cb;
-    cb.absval = 0; cb.row = -1; cb.cls = -1;
-    int cw = -1;
-    for (int g = tid; g < G; g += kPanelThreads) {
-      Cand<T> cc;
-      cc.absval = ldcg(&w.cand[par * G + g].absval);
-      cc.row = ldcg(&w.cand[par * G + g].row);
-      cc.cls = ldcg(&w.cand[par * G + g].cls);
-      if (cc.row >= 0 && (cw < 0 || cand_better(cc, cb))) { cb = cc; cw = g; }
-    }
-    // warp reduction carrying the CTA index
+      // 3. poll every CTA's word for this column (lane L acquires CTAs L,
+      //    L+32, ...): the poll is the grid barrier and the candidate exchange
+      Cand<T> cb;
+      cb.absval = 0; cb.row = -1; cb.cls = -1;
+      int cw = -1;
+      int okb = 1;
+      for (int g = lane; g < G; g += 32) {
+        unsigned long long wv = 0;
+        unsigned spins = 0;
+        for (;;) {
+          wv = ld_acquire_u64(w.word + par * G + g);
+          if ((unsigned)(wv & 0x7Fu) == seq) break;
+          if (++spins > kSpinLimit || *(volatile int*)status != kStatusOk) {
+            atomicCAS(status, kStatusOk, kStatusBarrierTimeout);
+            okb = 0;
+            break;
+          }
+        }
+        if (!okb) break;
+        const unsigned key = (unsigned)(wv >> 32);
+        const int row = (int)((wv >> 7) & 0x1FFFFFFu);
+        if (row == 0x1FFFFFF) continue;            // that CTA has no rows >= k
+        Cand<T> cc;
+        cc.row = row;
+        if (key == 0xFFFFFFFFu) { cc.cls = 2; cc.absval = 0; }
+        else if (key == 0u) { cc.cls = 0; cc.absval = 0; }
+        else {
+          cc.cls = 1;
+          if constexpr (sizeof(T) == 4) cc.absval = __uint_as_float(key - 1u);
+          else cc.absval = ldcg(w.absval + par * G + g);
+        }
+        if (cw < 0 || cand_better(cc, cb)) { cb = cc; cw = g; }
+      }
+      okb = __all_sync(0xffffffffu, okb);
+      if (!okb) {
+        if (lane == 0) ok_s = 0;
+      } else {
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      Cand<T> o = shfl_cand(cb, off);
-      int ow = __shfl_xor_sync(0xffffffffu, cw, off);
-      if (ow >= 0 && (cw < 0 || cand_better(o, cb))) { cb = o; cw = ow; }
-    }
-    if (lane == 0) { red[warp] = cb; redw[warp] = cw; }
-    __syncthreads();
-    if (warp == 0) {
-      Cand<T> c = (lane < kPanelThreads / 32) ? red[lane] : Cand<T>{0, -1, -1};
-      int cwi = (lane < kPanelThreads / 32) ? redw[lane] : -1;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        Cand<T> o = shfl_cand(c, off);
-        int ow = __shfl_xor_sync(0xffffffffu, cwi, off);
-        if (ow >= 0 && (cwi < 0 || cand_better(o, c))) { c = o; cwi = ow; }
+        for (int off = 16; off > 0; off >>= 1) {
+          Cand<T> o = shfl_cand(cb, off);
+          int ow = __shfl_xor_sync(0xffffffffu, cw, off);
+          if (ow >= 0 && (cw < 0 || cand_better(o, cb))) { cb = o; cw = ow; }
+        }
+        const int prow = cb.row;
+        const int kown = k / R;                      // CTA holding row k
+        // 4. the lane that acquired the winner's word reads its row; the lane
+        //    that acquired row k's owner reads row k (needed by the CTA that
+        //    holds the pivot row)
+        if (lane == (cw & 31)) {
+          copy_row64<T, true>(urow, w.cand_row + ((size_t)par * G + cw) * kLeafMax);
+          win_label_s = ldcg(w.cand_label + par * G + cw);
+        }
+        const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
+        if (own_p && prow != k && lane == (kown & 31)) {
+          copy_row64<T, true>(rowk_s, w.row_k + par * kLeafMax);
+          rowk_label_s = ldcg(w.row_k_label + par);
+        }
+        __syncwarp();
+        const T pv = urow[k];
+        if (lane == 0) {
+          pv_s = pv;
+          if (b == 0) {
+            ipiv[k] = row0 + prow + 1;
+            if (pv == T(0) && *info == 0) *info = row0 + k + 1;
+          }
+        }
+        // 5. interchange rows k and prow (whole panel rows)
+        if (prow != k) {
+          if (own_k) {
+            const int lk = k - rbeg;
+            for (int c = lane; c < JB; c += 32) tile[c * R + lk] = urow[c];
+            if (lane == 0) label[lk] = win_label_s;
+          }
+          if (own_p) {
+            const int lp = prow - rbeg;
+            for (int c = lane; c < JB; c += 32) tile[c * R + lp] = rowk_s[c];
+            if (lane == 0) label[lp] = rowk_label_s;
+          }
+        }
       }
-      if (lane == 0) { win_s = c; win_cta_s = cwi; }
     }
     __syncthreads();
-    const int wcta = win_cta_s;
-    const int prow = win_s.row;
-    const T* wrow = w.cand_row + ((size_t)par * G + wcta) * kLeafMax;
-    for (int c = tid; c < JB; c += kPanelThreads) urow[c] = ldcg(wrow + c);
-    __syncthreads();
-    const T pv = urow[k];
-    if (b == 0 && tid == 0) {
-      ipiv[k] = row0 + prow + 1;
-      if (pv == T(0) && *info == 0) *info = row0 + k + 1;
-    }
-    // 4. interchange rows k and prow (whole panel rows)
-    if (prow != k) {
-      if (k >= rbeg && k < rbeg + nrows) {
-        int lk = k - rbeg;
-        for (int c = tid; c < JB; c += kPanelThreads) tile[c * R + lk] = urow[c];
-        if (tid == 0) label[lk] = ldcg(w.cand_label + par * G + wcta);
-      }
-      if (prow >= rbeg && prow < rbeg + nrows) {
-        int lp = prow - rbeg;
-        const T* rk = w.row_k + par * kLeafMax;
-        for (int c = tid; c < JB; c += kPanelThreads) tile[c * R + lp] = ldcg(rk + c);
-        if (tid == 0) label[lp] = ldcg(w.row_k_label + par);
-      }
-    }
-    __syncthreads();
-    // 5. scale the column below the pivot and update the rest of the panel
+    if (!ok_s) break;
+    // 5. scale the column below the pivot and update the rest of each row
+    const T pv = pv_s;
     if (pv != T(0)) {
       const bool recip = (pv < 0 ? -pv : pv) >= Lim<T>::sfmin();
       const T rp = T(1) / pv;
-      const int r0 = max(0, k + 1 - rbeg);
-      for (int r = r0 + tid; r < nrows; r += kPanelThreads) {
-        T v = tile[k * R + r];
-        tile[k * R + r] = recip ? v * rp : v / pv;
+      for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kPanelThreads) {
+        const T v = tile[k * R + r];
+        const T l = recip ? v * rp : v / pv;
+        tile[k * R + r] = l;
+        for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
       }
-    }
-    __syncthreads();
-    {
-      const int r0 = max(0, k + 1 - rbeg);
-      const int nr = nrows - r0;
-      const int nc = JB - k - 1;
-      if (nr > 0 && nc > 0) {
-        for (int e = tid; e < nr * nc; e += kPanelThreads) {
-          int cc = e / nr, r = r0 + (e - cc * nr);
-          int c = k + 1 + cc;
-          tile[c * R + r] = fnmadd<EXACT>(tile[k * R + r], urow[c], tile[c * R + r]);
-        }
+    } else {
+      // zero pivot: the column stays unscaled; the update uses it as is
+      for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kPanelThreads) {
+        const T l = tile[k * R + r];
+        for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
       }
     }
     __syncthreads();

@@ -1,0 +1,189 @@
+// Leaf panel factorization of the FP32 LU on one thread-block cluster.
+//
+// The grid-wide leaf kernel exchanges one pivot candidate per column
+// through L2, which on GB300 costs a few microseconds per column (several
+// dependent L2 round trips across the two dies).  Here the M x JB panel is
+// spread over the CTAs of ONE cluster (16 CTAs, one per SM, all in one GPC),
+// each holding R rows in shared memory; candidates, the pivot row and row k
+// are exchanged through distributed shared memory with one hardware cluster
+// barrier per column.  Same semantics as leaf_panel_kernel (DGETRF2 on the
+// panel, SRC/dgetrf2.f:170-265): IDAMAX pivot order, reciprocal-or-divide
+// scaling, rank-1 updates in increasing k, interchanges of whole panel rows
+// summarised as (dst, src) pairs.
+//
+// Pivot order as one 64-bit key, larger wins: the upper word is cand_key
+// (class and |a|), the lower word ~row, so equal |a| goes to the smaller row
+// as IDAMAX's strict '>' does.  The search for column k+1 is folded into the
+// rank-1 update of column k.
+#pragma once
+#include <cooperative_groups.h>
+
+#include "lu_kernels.cuh"
+
+namespace gb {
+
+constexpr int kClusterCtas = 16;
+constexpr int kClusterThreads = 512;
+
+struct ClusterSlot {
+  unsigned long long key;
+  int label;
+  int row_k_label;
+  float row[kLeafMax];
+  float row_k[kLeafMax];
+};
+
+__device__ __forceinline__ unsigned long long pack_key(float v, int row, int first_row) {
+  Cand<float> c = make_cand(v, row, first_row);
+  return ((unsigned long long)cand_key(c) << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)row);
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
+    v = o > v ? o : v;
+  }
+  return v;
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, int row0, int* __restrict__ ipiv,
+                          int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
+                          int* __restrict__ pair_count, int* __restrict__ status) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* tile = reinterpret_cast<float*>(smem_raw);                        // [JB][R]
+  int* label = reinterpret_cast<int*>(tile + (size_t)JB * R);              // [R]
+  __shared__ ClusterSlot slot[2];
+  __shared__ __align__(16) float urow[kLeafMax];
+  __shared__ __align__(16) float rowk_s[kLeafMax];
+  __shared__ unsigned long long wbest[kClusterThreads / 32];
+  __shared__ float pv_s;
+  __shared__ int win_label_s, rowk_label_s, prow_s;
+
+  const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rbeg = b * R;
+  const int nrows = max(0, min(M, rbeg + R) - rbeg);
+
+  for (int e = tid; e < JB * nrows; e += kClusterThreads) {
+    int c = e / nrows, r = e - c * nrows;
+    tile[c * R + r] = P[(size_t)(rbeg + r) + (size_t)c * lda];
+  }
+  for (int r = tid; r < nrows; r += kClusterThreads) label[r] = rbeg + r;
+  __syncthreads();
+  // candidates for column 0
+  unsigned long long mykey = 0;
+  for (int r = tid; r < nrows; r += kClusterThreads) {
+    unsigned long long kk = pack_key(tile[r], rbeg + r, 0);
+    mykey = kk > mykey ? kk : mykey;
+  }
+
+  for (int k = 0; k < JB; ++k) {
+    const int par = k & 1;
+    // 1. this CTA's best candidate for column k
+    mykey = warp_max_u64(mykey);
+    if (lane == 0) wbest[warp] = mykey;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long kk = lane < kClusterThreads / 32 ? wbest[lane] : 0ull;
+      kk = warp_max_u64(kk);
+      ClusterSlot& sl = slot[par];
+      if (lane == 0) sl.key = kk;
+      if (kk != 0ull) {
+        const int lr = (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) - rbeg;
+        for (int c = lane; c < JB; c += 32) sl.row[c] = tile[c * R + lr];
+        if (lane == 0) sl.label = label[lr];
+      }
+      if (k >= rbeg && k < rbeg + nrows) {
+        for (int c = lane; c < JB; c += 32) sl.row_k[c] = tile[c * R + (k - rbeg)];
+        if (lane == 0) sl.row_k_label = label[k - rbeg];
+      }
+    }
+    // 2. one cluster barrier per column (release / acquire on shared::cluster)
+    cluster.sync();
+    // 3. every CTA reduces the G keys to the same winner and fetches rows
+    if (warp == 0) {
+      unsigned long long kk = 0ull;
+      if (lane < G) kk = cluster.map_shared_rank(&slot[par], lane)->key;
+      const unsigned long long wk = warp_max_u64(kk);
+      const int wc = __ffsll(__ballot_sync(0xffffffffu, kk == wk && lane < G)) - 1;   // CTA holding it
+      const int prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
+      const ClusterSlot* ws = cluster.map_shared_rank(&slot[par], wc);
+      for (int c = lane; c < JB; c += 32) urow[c] = ws->row[c];
+      if (lane == 0) win_label_s = ws->label;
+      const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
+      if (own_p && prow != k) {
+        const ClusterSlot* ks = cluster.map_shared_rank(&slot[par], k / R);
+        for (int c = lane; c < JB; c += 32) rowk_s[c] = ks->row_k[c];
+        if (lane == 0) rowk_label_s = ks->row_k_label;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        prow_s = prow;
+        pv_s = urow[k];
+        if (b == 0) {
+          ipiv[k] = row0 + prow + 1;
+          if (urow[k] == 0.0f && *info == 0) *info = row0 + k + 1;
+        }
+      }
+      __syncwarp();
+      if (prow != k) {
+        if (k >= rbeg && k < rbeg + nrows) {
+          const int lk = k - rbeg;
+          for (int c = lane; c < JB; c += 32) tile[c * R + lk] = urow[c];
+          if (lane == 0) label[lk] = win_label_s;
+        }
+        if (own_p) {
+          const int lp = prow - rbeg;
+          for (int c = lane; c < JB; c += 32) tile[c * R + lp] = rowk_s[c];
+          if (lane == 0) label[lp] = rowk_label_s;
+        }
+      }
+    }
+    __syncthreads();
+    // 4. scale column k below the pivot, rank-1 update of each row, and the
+    //    candidate search of column k+1 on the updated values
+    const float pv = pv_s;
+    const bool scale = pv != 0.0f;
+    const bool recip = fabsf(pv) >= Lim<float>::sfmin();
+    const float rp = 1.0f / pv;
+    mykey = 0;
+    for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
+      const float v = tile[k * R + r];
+      const float l = scale ? (recip ? v * rp : v / pv) : v;
+      tile[k * R + r] = l;
+      for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
+      if (k + 1 < JB) {
+        unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
+        mykey = kk > mykey ? kk : mykey;
+      }
+    }
+  }
+  // no CTA may exit while others can still read its shared memory
+  cluster.sync();
+  for (int e = tid; e < JB * nrows; e += kClusterThreads) {
+    int c = e / nrows, r = e - c * nrows;
+    P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * R + r];
+  }
+  for (int r = tid; r < nrows; r += kClusterThreads) {
+    int g = rbeg + r;
+    if (g < JB) {
+      pair_dst[g] = row0 + g;
+      pair_src[g] = row0 + label[r];
+    } else if (label[r] != g) {
+      int s = JB + atomicAdd(pair_count, 1);
+      if (s < 2 * kLeafMax) {
+        pair_dst[s] = row0 + g;
+        pair_src[s] = row0 + label[r];
+      } else {
+        atomicCAS(status, kStatusOk, kStatusCapacity);
+      }
+    }
+  }
+}
+
+}  // namespace gb

@@ -90,10 +90,12 @@ def test_dsgesv_ill_conditioned_semantics(gpu, bf16_mode, n, kappa):
         assert np.array_equal(ao, a)
         assert ck.dget08(a, x, b) < np.sqrt(n)
     else:
+        # A holds an FP64 LU of A.  At kappa >= 1e10 elementwise agreement with
+        # the oracle's LU is not expected (rounding differences grow like
+        # kappa*eps in the trailing factors), so the factorization is checked
+        # by its backward error, as DGET01 does.
         assert it in (-31, -2), it
-        lu_r, ip_r, info_r = oracle.getrf(a)
-        np.testing.assert_array_equal(ip, ip_r)
-        assert ck.lu_rel_diff(ao, lu_r, a) <= 64.0
+        assert ck.dget01(a, ao, ip) < 30.0
         assert ck.dget08(a, x, b) < 30.0
 
 
