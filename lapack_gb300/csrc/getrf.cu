@@ -453,8 +453,15 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
   GB_CUDA_TRY(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (size_t)(nblk + 1), s));
   int* flags = ctl.as<int>();
   unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
+  static bool smem_set[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!smem_set[dev]) {
+    GB_CUDA_TRY((trsv_set_smem<T, EXACT, FORWARD, UNIT, TRANS>()));
+    smem_set[dev] = true;
+  }
   prof_begin(kProfTrsv, s);
-  GB_LAUNCH(trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS><<<nblk, 256, 0, s>>>(A, lda, n, X, ldx, nrhs, flags, ticket,
+  GB_LAUNCH(trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS><<<nblk, 256, kTrsvSmem<T>, s>>>(A, lda, n, X, ldx, nrhs, flags, ticket,
                                                                         device_status_word()));
   prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
   return (int)cudaGetLastError();

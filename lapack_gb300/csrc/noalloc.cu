@@ -22,8 +22,8 @@
 //
 // On the first call on a device the library looks up the array's device
 // address (cudaGetSymbolAddress) with that device current and sets the
-// kernel attributes it needs; make that first call before any stream
-// capture.  No cudaMalloc, cudaFree or allocating library routine is called.
+// shared-memory attributes of the kernels it launches; make that first call
+// before any stream capture.  No cudaMalloc, cudaFree or allocating library routine is called.
 #include "../../include/lapack_gb300.h"
 #include "common.cuh"
 #include "prof.h"
@@ -55,7 +55,7 @@ std::mutex g_setup_mu;
 DeviceSetup g_setup[64];
 
 // Once per device, with that device current: the array's device address and
-// the shared-memory attribute of the permutation kernel.
+// the shared-memory attributes of the permutation and solve kernels.
 int setup_device(unsigned char** base) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -69,6 +69,10 @@ int setup_device(unsigned char** base) {
     e = cudaFuncSetAttribute(ipiv_to_perm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(int) * kNoAllocMaxN));
     if (e != cudaSuccess) return (int)e;
+    if ((e = trsv_set_smem<double, false, true, true, false>()) != cudaSuccess) return (int)e;
+    if ((e = trsv_set_smem<double, false, false, false, false>()) != cudaSuccess) return (int)e;
+    if ((e = trsv_set_smem<double, false, true, false, true>()) != cudaSuccess) return (int)e;
+    if ((e = trsv_set_smem<double, false, false, true, true>()) != cudaSuccess) return (int)e;
     g_setup[dev].base = static_cast<unsigned char*>(p);
     g_setup[dev].done = true;
   }
@@ -81,7 +85,7 @@ void launch_solve(const double* A, int lda, int n, double* W, int nrhs, int* fla
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
   unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
   cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), s);
-  GB_LAUNCH(trsv_blocked_kernel<double, false, FORWARD, UNIT, TRANS><<<nblk, 256, 0, s>>>(A, lda, n, W, n, nrhs, flags,
+  GB_LAUNCH(trsv_blocked_kernel<double, false, FORWARD, UNIT, TRANS><<<nblk, 256, kTrsvSmem<double>, s>>>(A, lda, n, W, n, nrhs, flags,
                                                                                         ticket, status));
 }
 

@@ -67,121 +67,181 @@ __global__ void copy_cols_kernel(const T* __restrict__ S, int lds, T* __restrict
 // Blocked triangular solve with several right-hand sides, X := op(T)^{-1} X,
 // for the four DGETRS cases (SRC/dgetrs.f:187-217 calling
 // BLAS/SRC/dtrsm.f:272-329).  The matrix is cut into 64-row blocks; CTAs
-// take blocks in solve order from a ticket counter, fold in the finished
-// blocks as they complete (a per-block flag, released after the block's
-// solution is written), then solve their diagonal block.  Every wait is
-// bounded.  FORWARD: blocks in increasing order (L, or U^T); otherwise
-// decreasing (U, or L^T).  TRANS reads T(k, r) for element (r, k).
-// In increasing / decreasing order of k each element receives its updates in
-// the reference loop order (N cases and U^T); the L^T case folds k in
-// decreasing order, which the reference folds in increasing order.
+// take blocks in solve order from a ticket counter.  A CTA streams the
+// 64 x 64 tiles of its block row (prefetched with cp.async, double
+// buffered, independent of any dependency), folds in each source block's
+// solution as soon as that block's flag is released, then solves its
+// diagonal block with one warp per right-hand side (two rows per lane,
+// shuffle broadcast, no block barriers), writes its solution and releases
+// its own flag.  Every wait is bounded.  FORWARD: blocks in increasing order
+// (L, or U^T); otherwise decreasing (U, or L^T).  TRANS reads T(k, r) for
+// element (r, k).  In increasing / decreasing order of k each element
+// receives its updates in the reference loop order (N cases and U^T); the
+// L^T case folds k in decreasing order, which the reference folds in
+// increasing order.
 constexpr int kSolveBS = 64;
 constexpr int kSolveRQ = 4;   // right-hand sides per pass (256 threads = 64 rows x 4)
+constexpr int kSolveLd = kSolveBS + 1;
+template <typename T>
+constexpr int kTrsvSmem = 2 * kSolveBS * kSolveLd * (int)sizeof(T);   // 33 KB (float) / 66.6 KB (double)
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
 __global__ void __launch_bounds__(256)
 trsv_blocked_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, int ldx, int nrhs,
                     int* __restrict__ flags, unsigned* __restrict__ ticket, int* __restrict__ status) {
-  __shared__ T tile[kSolveBS][kSolveBS + 1];
-  __shared__ T xsrc[kSolveBS][kSolveRQ];
+  extern __shared__ __align__(16) unsigned char trsv_smem[];
+  T* tiles = reinterpret_cast<T*>(trsv_smem);     // [2][64][65]: raw column-major copies
+  __shared__ T xsrc[2][kSolveBS][kSolveRQ];
   __shared__ T xs[kSolveBS][kSolveRQ];
   __shared__ unsigned t_s;
   __shared__ int ok_s;
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int r = tid & 63, q = tid >> 6;
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
-  if (tid == 0) t_s = atomicAdd(ticket, 1u);
+  if (tid == 0) { t_s = atomicAdd(ticket, 1u); ok_s = 1; }
   __syncthreads();
   const int t = (int)t_s;
   const int bi = FORWARD ? t : nblk - 1 - t;
   const int r0 = bi * kSolveBS;
   const int nr = min(kSolveBS, n - r0);
-  auto tile_elem = [&](int row, int col) -> T {   // op(T)(row, col), global indices
-    return TRANS ? A[(size_t)col + (size_t)row * lda] : A[(size_t)row + (size_t)col * lda];
+  const int nsrc = FORWARD ? bi : nblk - 1 - bi;
+
+  // raw copy of the stored block behind op(T)(r0.., c0..): rows r0.., cols c0..
+  // (non-transposed) or rows c0.., cols r0.. (transposed); element (rr, cc)
+  // of the stored block lands at tile[cc * 65 + rr]
+  auto issue_tile = [&](int bj, T* dst) {
+    const int c0 = bj * kSolveBS;
+    const int nc = min(kSolveBS, n - c0);
+    const int srow = TRANS ? c0 : r0, scol = TRANS ? r0 : c0;
+    const int nsr = TRANS ? nc : nr, nsc = TRANS ? nr : nc;
+    for (int e = tid; e < kSolveBS * kSolveBS; e += 256) {
+      const int cc = e >> 6, rr = e & 63;
+      if (rr < nsr && cc < nsc) cp_async_elem(dst + cc * kSolveLd + rr, A + (size_t)(srow + rr) + (size_t)(scol + cc) * lda);
+    }
   };
-  bool ok = true;
-  for (int q0 = 0; q0 < nrhs; q0 += kSolveRQ) {
-    const int s = q0 + q;
-    const bool active = (r < nr) && (s < nrhs);
-    T acc = active ? X[(size_t)(r0 + r) + (size_t)s * ldx] : T(0);
-    const int nsrc = FORWARD ? bi : nblk - 1 - bi;
+  // op(T)(row rr of this block, column kk of the source block)
+  auto op_elem = [&](const T* tl, int rr, int kk) -> T { return TRANS ? tl[rr * kSolveLd + kk] : tl[kk * kSolveLd + rr]; };
+
+  for (int q0 = 0; q0 < nrhs && ok_s; q0 += kSolveRQ) {
+    const int nq = min(kSolveRQ, nrhs - q0);
+    const bool active = (r < nr) && (q < nq);
+    T acc = active ? X[(size_t)(r0 + r) + (size_t)(q0 + q) * ldx] : T(0);
+    if (nsrc > 0) issue_tile(FORWARD ? 0 : nblk - 1, tiles);
+    cp_async_commit();
     for (int step = 0; step < nsrc; ++step) {
       const int bj = FORWARD ? step : nblk - 1 - step;
       const int c0 = bj * kSolveBS;
       const int nc = min(kSolveBS, n - c0);
-      if (q0 == 0) {
-        if (tid == 0) {
+      const int buf = step & 1;
+      // warp 0: wait for block bj's solution (every lane acquires), read it
+      if (warp == 0) {
+        int okw = 1;
+        if (q0 == 0) {
           unsigned spins = 0;
-          int okk = 1;
           while (ld_acquire_s32(flags + bj) == 0) {
             if (++spins > kSpinLimit || *(volatile int*)status != kStatusOk) {
               atomicCAS(status, kStatusOk, kStatusFlagTimeout);
-              okk = 0;
+              okw = 0;
               break;
             }
-            __nanosleep(32);
           }
-          ok_s = okk;
         }
-        __syncthreads();
-        if (!ok_s) { ok = false; break; }
+        okw = __all_sync(0xffffffffu, okw);
+        if (!okw) {
+          if (lane == 0) ok_s = 0;
+        } else {
+          for (int e = lane; e < kSolveBS * kSolveRQ; e += 32) {
+            const int cc = e % kSolveBS, qq = e / kSolveBS;
+            xsrc[buf][cc][qq] = (cc < nc && qq < nq) ? ldcg(X + (size_t)(c0 + cc) + (size_t)(q0 + qq) * ldx) : T(0);
+          }
+        }
       }
-      for (int e = tid; e < kSolveBS * kSolveBS; e += 256) {
-        // consecutive threads walk the contiguous index of the stored matrix
-        int rr, cc;
-        if (TRANS) { rr = e / kSolveBS; cc = e - rr * kSolveBS; }
-        else { cc = e / kSolveBS; rr = e - cc * kSolveBS; }
-        if (rr < nr && cc < nc) tile[rr][cc] = tile_elem(r0 + rr, c0 + cc);
-      }
-      for (int e = tid; e < nc * kSolveRQ; e += 256) {
-        int cc = e % nc, qq = e / nc;
-        xsrc[cc][qq] = (q0 + qq < nrhs) ? ldcg(X + (size_t)(c0 + cc) + (size_t)(q0 + qq) * ldx) : T(0);
-      }
+      cp_async_wait<0>();
       __syncthreads();
+      if (!ok_s) break;
+      // prefetch the next tile into the other buffer while this one is used
+      if (step + 1 < nsrc) issue_tile(FORWARD ? step + 1 : nblk - 2 - step, tiles + (buf ^ 1) * kSolveBS * kSolveLd);
+      cp_async_commit();
+      const T* tl = tiles + buf * kSolveBS * kSolveLd;
       if (active) {
         if (FORWARD) {
-          for (int kk = 0; kk < nc; ++kk) acc = fnmadd<EXACT>(tile[r][kk], xsrc[kk][q], acc);
+          for (int kk = 0; kk < nc; ++kk) acc = fnmadd<EXACT>(op_elem(tl, r, kk), xsrc[buf][kk][q], acc);
         } else {
-          for (int kk = nc - 1; kk >= 0; --kk) acc = fnmadd<EXACT>(tile[r][kk], xsrc[kk][q], acc);
+          for (int kk = nc - 1; kk >= 0; --kk) acc = fnmadd<EXACT>(op_elem(tl, r, kk), xsrc[buf][kk][q], acc);
         }
       }
-      __syncthreads();
     }
-    if (!ok) break;
-    // diagonal block
-    for (int e = tid; e < kSolveBS * kSolveBS; e += 256) {
-      int rr, cc;
-      if (TRANS) { rr = e / kSolveBS; cc = e - rr * kSolveBS; }
-      else { cc = e / kSolveBS; rr = e - cc * kSolveBS; }
-      if (rr < nr && cc < nr) tile[rr][cc] = tile_elem(r0 + rr, r0 + cc);
-    }
-    xs[r][q] = acc;
+    cp_async_wait<0>();
     __syncthreads();
-    if (FORWARD) {
-      for (int k = 0; k < nr; ++k) {
-        if (!UNIT) {
-          if (r == k && active) xs[k][q] = xs[k][q] / tile[k][k];
-          __syncthreads();
+    if (!ok_s) break;
+    // diagonal block: stage it in buffer 0, one warp per right-hand side
+    issue_tile(bi, tiles);
+    cp_async_commit();
+    xs[r][q] = acc;
+    cp_async_wait<0>();
+    __syncthreads();
+    if (warp < nq) {
+      const T* D = tiles;
+      const int qq = warp;
+      T x0 = lane < nr ? xs[lane][qq] : T(0);
+      T x1 = lane + 32 < nr ? xs[lane + 32][qq] : T(0);
+      if (FORWARD) {
+        for (int k = 0; k < nr; ++k) {
+          const bool hi = k >= 32;
+          T xk = hi ? x1 : x0;
+          if (!UNIT) {
+            if ((k & 31) == lane) {
+              xk = xk / op_elem(D, k, k);
+              if (hi) x1 = xk; else x0 = xk;
+            }
+          }
+          xk = __shfl_sync(0xffffffffu, xk, k & 31);
+          if (lane > k && lane < nr) x0 = fnmadd<EXACT>(op_elem(D, lane, k), xk, x0);
+          if (lane + 32 > k && lane + 32 < nr) x1 = fnmadd<EXACT>(op_elem(D, lane + 32, k), xk, x1);
         }
-        if (active && r > k) xs[r][q] = fnmadd<EXACT>(tile[r][k], xs[k][q], xs[r][q]);
-        __syncthreads();
-      }
-    } else {
-      for (int k = nr - 1; k >= 0; --k) {
-        if (!UNIT) {
-          if (r == k && active) xs[k][q] = xs[k][q] / tile[k][k];
-          __syncthreads();
+      } else {
+        for (int k = nr - 1; k >= 0; --k) {
+          const bool hi = k >= 32;
+          T xk = hi ? x1 : x0;
+          if (!UNIT) {
+            if ((k & 31) == lane) {
+              xk = xk / op_elem(D, k, k);
+              if (hi) x1 = xk; else x0 = xk;
+            }
+          }
+          xk = __shfl_sync(0xffffffffu, xk, k & 31);
+          if (lane < k) x0 = fnmadd<EXACT>(op_elem(D, lane, k), xk, x0);
+          if (lane + 32 < k) x1 = fnmadd<EXACT>(op_elem(D, lane + 32, k), xk, x1);
         }
-        if (active && r < k) xs[r][q] = fnmadd<EXACT>(tile[r][k], xs[k][q], xs[r][q]);
-        __syncthreads();
       }
+      if (lane < nr) X[(size_t)(r0 + lane) + (size_t)(q0 + qq) * ldx] = x0;
+      if (lane + 32 < nr) X[(size_t)(r0 + lane + 32) + (size_t)(q0 + qq) * ldx] = x1;
     }
-    if (active) X[(size_t)(r0 + r) + (size_t)s * ldx] = xs[r][q];
     __syncthreads();
   }
   __threadfence();
   __syncthreads();
-  if (tid == 0) st_release_s32(flags + bi, ok ? 1 : -1);
+  if (tid == 0) st_release_s32(flags + bi, ok_s ? 1 : -1);
+}
+
+// Raises the dynamic shared-memory limit of one instantiation (needed for
+// the 66.6 KB double tiles); returns the CUDA status of the attribute call.
+template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
+cudaError_t trsv_set_smem() {
+  return cudaFuncSetAttribute(trsv_blocked_kernel<T, EXACT, FORWARD, UNIT, TRANS>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, kTrsvSmem<T>);
 }
 
 // ---------------------------------------------------------------------------
