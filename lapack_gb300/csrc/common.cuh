@@ -35,6 +35,26 @@ __device__ __forceinline__ void st_release_s32(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+// Copies `total` elements, element e from src(e) to dst(e), with NT threads:
+// each thread issues U independent loads into registers before storing, so
+// the copy pays one memory latency per U elements instead of one per element.
+template <int U, int NT, typename T, typename Src, typename Dst>
+__device__ __forceinline__ void batched_copy(int total, int tid, Src src, Dst dst) {
+  for (int e0 = tid; e0 < total; e0 += U * NT) {
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * NT;
+      if (e < total) v[u] = src(e);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = e0 + u * NT;
+      if (e < total) dst(e, v[u]);
+    }
+  }
+}
+
 // Loads of data written by other CTAs of the same launch go through L2.
 template <typename T>
 __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }

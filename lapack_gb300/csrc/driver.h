@@ -19,7 +19,7 @@ struct Options {
   int sgetrf_mode = kMixedFp32;   // sgetrf_ itself: plain FP32 by default
   int panel_ctas_f64 = 0;         // CTAs of the cooperative panel (0: all SMs)
   int panel_ctas_f32 = 0;
-  int cluster_panel = 1;          // FP32 leaves on one thread-block cluster (DSMEM exchange)
+  int cluster_panel = 2;          // FP32 leaves on one thread-block cluster: 2 shared-memory kernel, 1 register kernel, 0 off
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 
@@ -39,8 +39,10 @@ struct DevScratch {
 
 // Device-pointer routines.  Return 0 or a CUDA / status error code; the
 // LAPACK INFO goes to the device int *dInfo.  All work is queued on `s`.
+// dPerm (optional, m ints): receives the gather permutation of P*A.
 template <typename T>
-int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb);
+int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb,
+              int* dPerm = nullptr);
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
               T* dB, int ldb, cudaStream_t s);

@@ -33,7 +33,7 @@ Options& options() {
     x.nb_f32 = std::max(1, env_int("LAPACK_GB300_NB32", 256));
     x.panel_ctas_f64 = env_int("LAPACK_GB300_PANEL_CTAS64", 0);
     x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
-    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 1);
+    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -123,17 +123,41 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
 }
 
 // ------------------------------------------------------------------- TRSM
-// B := L^{-1} B, L unit lower k x k: 64-wide leaves, GEMM for the coupling.
+template <typename T, bool EXACT, int KMAX>
+static int launch_trsm_leaf_k(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(trsm_llnu_leaf_kernel<T, EXACT, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     trsm_leaf_smem<T, KMAX>()));
+    attr[dev] = true;
+  }
+  GB_LAUNCH(trsm_llnu_leaf_kernel<T, EXACT, KMAX><<<grid, kTrsmThreads, trsm_leaf_smem<T, KMAX>(), s>>>(L, ldl, B, ldb,
+                                                                                                     k, ncols));
+  return 0;
+}
+
+// the unrolled solve is sized to the leaf: 16, 32 or 64 rows
+template <typename T, bool EXACT>
+static int launch_trsm_leaf(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
+  prof_begin(kProfTrsm, s);
+  int rc;
+  if (k <= 16) rc = launch_trsm_leaf_k<T, EXACT, 16>(grid, L, ldl, B, ldb, k, ncols, s);
+  else if (k <= 32) rc = launch_trsm_leaf_k<T, EXACT, 32>(grid, L, ldl, B, ldb, k, ncols, s);
+  else rc = launch_trsm_leaf_k<T, EXACT, 64>(grid, L, ldl, B, ldb, k, ncols, s);
+  return rc;
+}
+
+// B := L^{-1} B, L unit lower k x k: leaves of at most 64 rows, GEMM for the coupling.
 template <typename T>
 int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode) {
   if (k <= 0 || ncols <= 0) return 0;
   if (k <= kLeafMax) {
-    int grid = (ncols + TrsmSlab<T>::BC - 1) / TrsmSlab<T>::BC;
-    prof_begin(kProfTrsm, s);
-    if (options().exact)
-      GB_LAUNCH(trsm_llnu_leaf_kernel<T, true><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols));
-    else
-      GB_LAUNCH(trsm_llnu_leaf_kernel<T, false><<<grid, 256, 0, s>>>(L, ldl, B, ldb, k, ncols));
+    int grid = (ncols + kTrsmCols - 1) / kTrsmCols;
+    int rc = options().exact ? launch_trsm_leaf<T, true>(grid, L, ldl, B, ldb, k, ncols, s)
+                             : launch_trsm_leaf<T, false>(grid, L, ldl, B, ldb, k, ncols, s);
+    if (rc) return rc;
     prof_end(kProfTrsm, s, (double)k * k * ncols, sizeof(T) * ((double)k * k + 2.0 * k * ncols));
     return (int)cudaGetLastError();
   }
@@ -155,6 +179,7 @@ struct PanelCtx {
   int* status;
   int max_optin;
   size_t words_bytes;    // candidate words + pair count, zeroed before each leaf
+  int* perm = nullptr;    // optional running row permutation (gather index), updated with every leaf
 };
 
 template <typename T, bool EXACT>
@@ -202,12 +227,12 @@ static int launch_leaf(T* P, int lda, int M, int JB, int row0, int* ipiv, int* i
 
 template <typename T>
 static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, PanelCtx<T>& cx, cudaStream_t s) {
-  int warps = c0 + (ncols - c1);
+  int warps = c0 + (ncols - c1) + (cx.perm ? 1 : 0);
   if (warps <= 0) return 0;
   int blocks = (warps * 32 + 255) / 256;
   prof_begin(kProfLaswp, s);
   GB_LAUNCH(laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(A, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
-                                                cx.ps.pair_count, ntop));
+                                                cx.ps.pair_count, ntop, cx.perm));
   prof_end(kProfLaswp, s, 0.0, 2.0 * sizeof(T) * 2.0 * ntop * warps);
   return (int)cudaGetLastError();
 }
@@ -257,17 +282,59 @@ static ClusterCaps cluster_caps() {
   return caps[dev];
 }
 
-// Widest leaf (64, 32, 16 or 8 columns) whose M-row panel fits the shared
-// memory of one cluster; 0 when the cluster leaf cannot be used.
+// Leaf plan of the FP32 cluster path for an M-row panel: the register
+// kernel (kind 1) with 32-column leaves up to M = 16384 and 16-column leaves
+// up to M = 32768 (64 row values per thread), else the shared-memory cluster
+// kernel (kind 2) with the widest leaf (64..8) that fits; 0 when neither
+// applies.  Returns the leaf width.
 template <typename T>
-static int cluster_leaf_width(int M) {
+static int cluster_leaf_width(int M, int* kind) {
+  *kind = 0;
   if (sizeof(T) != 4 || options().cluster_panel == 0) return 0;
   ClusterCaps c = options().exact ? cluster_caps<true>() : cluster_caps<false>();
   if (!c.ok) return 0;
   const long long R = (M + kClusterCtas - 1) / kClusterCtas;
+  if (options().cluster_panel == 1) {
+    if (R <= 2 * kClusterThreads) { *kind = 1; return 32; }
+    if (R <= 4 * kClusterThreads) { *kind = 1; return 16; }
+  }
   for (int lw = kLeafMax; lw >= 8; lw /= 2)
-    if ((long long)(lw + 1) * R * 4 + 16 <= c.dyn_cap) return lw;
+    if ((long long)(lw + 1) * R * 4 + 16 <= c.dyn_cap) { *kind = 2; return lw; }
   return 0;
+}
+
+template <bool EXACT, int JB>
+static int launch_leaf_cluster_reg(float* P, int lda, int M, int jb, int row0, int* ipiv, int* info,
+                                   PanelCtx<float>& cx, cudaStream_t s) {
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(leaf_panel_cluster_reg_kernel<EXACT, JB>,
+                                     cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[dev] = true;
+  }
+  const int R = (M + kClusterCtas - 1) / kClusterCtas;
+  if (R > (64 / JB) * kClusterThreads || jb > JB) return 1000 + kStatusCapacity;
+  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kClusterCtas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(kClusterCtas);
+  cfg.blockDim = dim3(kClusterThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  prof_begin(kProfPanel, s);
+  int rc = (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_reg_kernel<EXACT, JB>, P, lda, M, jb, R, row0, ipiv, info,
+                                   cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status);
+  count_launch();
+  prof_end(kProfPanel, s, (double)M * jb * jb, 2.0 * 4.0 * (double)M * jb);
+  return rc;
 }
 
 template <bool EXACT>
@@ -305,15 +372,23 @@ static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* 
 template <typename T>
 static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int* info, PanelCtx<T>& cx,
                      cudaStream_t s, int gemm_mode) {
-  const int clw = cluster_leaf_width<T>(m - c0);
+  int ckind = 0;
+  const int clw = cluster_leaf_width<T>(m - c0, &ckind);
   const int leaf = clw ? clw : kLeafMax;
   if (w <= leaf) {
     T* P = A + c0 + (size_t)c0 * lda;
     int rc;
     if constexpr (sizeof(T) == 4) {
-      if (clw)
-        rc = options().exact ? launch_leaf_cluster<true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
-                             : launch_leaf_cluster<false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+      const bool ex = options().exact;
+      if (ckind == 1 && clw == 32)
+        rc = ex ? launch_leaf_cluster_reg<true, 32>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                : launch_leaf_cluster_reg<false, 32>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+      else if (ckind == 1)
+        rc = ex ? launch_leaf_cluster_reg<true, 16>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                : launch_leaf_cluster_reg<false, 16>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
+      else if (ckind == 2)
+        rc = ex ? launch_leaf_cluster<true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
+                : launch_leaf_cluster<false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
       else
         rc = options().exact ? launch_leaf<T, true>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s)
                              : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
@@ -337,10 +412,17 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
   return getrf_rec<T>(A, lda, m, n, c0 + n1, w - n1, ipiv, info, cx, s, gemm_mode);
 }
 
+static __global__ void iota_kernel(int* p, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = i;
+}
+
 template <typename T>
-int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb) {
+int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb,
+              int* dPerm) {
   GB_CUDA_TRY(cudaMemsetAsync(dInfo, 0, sizeof(int), s));
   if (m <= 0 || n <= 0) return 0;
+  if (dPerm) GB_LAUNCH(iota_kernel<<<(m + 255) / 256, 256, 0, s>>>(dPerm, m));
   const int nsm = device_sm_count();
   int dev = 0;
   cudaGetDevice(&dev);
@@ -371,6 +453,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   cx.ps.pair_dst = reinterpret_cast<int*>(base + o_pd);
   cx.ps.pair_src = reinterpret_cast<int*>(base + o_psrc);
   cx.words_bytes = sizeof(unsigned long long) * 2 * G + sizeof(int);
+  cx.perm = dPerm;
   cx.status = device_status_word();
   cx.max_optin = optin;
   if (!cx.status) return (int)cudaErrorMemoryAllocation;
@@ -394,8 +477,8 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   }
   return (int)cudaGetLastError();
 }
-template int getrf_dev<double>(int, int, double*, int, int*, int*, cudaStream_t, int, int);
-template int getrf_dev<float>(int, int, float*, int, int*, int*, cudaStream_t, int, int);
+template int getrf_dev<double>(int, int, double*, int, int*, int*, cudaStream_t, int, int, int*);
+template int getrf_dev<float>(int, int, float*, int, int*, int*, cudaStream_t, int, int, int*);
 
 // ------------------------------------------------------------- permutation
 int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s) {

@@ -98,10 +98,11 @@ leaf_panel_kernel(T* __restrict__ P, int lda, int M, int JB, int R, int row0,
   const int rbeg = b * R;
   const int nrows = max(0, min(M, rbeg + R) - rbeg);
 
-  for (int e = tid; e < JB * nrows; e += kPanelThreads) {
-    int c = e / nrows, r = e - c * nrows;
-    tile[c * R + r] = P[(size_t)(rbeg + r) + (size_t)c * lda];
-  }
+  if (nrows > 0)
+    batched_copy<8, kPanelThreads, T>(
+        JB * nrows, tid,
+        [&](int e) { const int c = e / nrows, r = e - c * nrows; return P[(size_t)(rbeg + r) + (size_t)c * lda]; },
+        [&](int e, T v) { const int c = e / nrows, r = e - c * nrows; tile[c * R + r] = v; });
   for (int r = tid; r < nrows; r += kPanelThreads) label[r] = rbeg + r;
   if (tid == 0) ok_s = 1;
   __syncthreads();
@@ -275,13 +276,30 @@ template <typename T>
 __global__ void __launch_bounds__(256)
 laswp_pairs_kernel(T* __restrict__ A, int lda, int ncols, int c_skip0, int c_skip1,
                    const int* __restrict__ pair_dst, const int* __restrict__ pair_src,
-                   const int* __restrict__ pair_count_ext, int ntop) {
+                   const int* __restrict__ pair_count_ext, int ntop, int* __restrict__ perm) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int nleft = c_skip0, nright = ncols - c_skip1;
+  const int np = ntop + *pair_count_ext;
+  if (perm && warp == nleft + nright) {
+    // the same gather on the running row permutation of the factorization
+    constexpr int kMaxPer = (2 * kLeafMax + 31) / 32;
+    int v[kMaxPer];
+#pragma unroll
+    for (int s = 0; s < kMaxPer; ++s) {
+      int i = lane + 32 * s;
+      if (i < np) v[s] = perm[pair_src[i]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < kMaxPer; ++s) {
+      int i = lane + 32 * s;
+      if (i < np) perm[pair_dst[i]] = v[s];
+    }
+    return;
+  }
   if (warp >= nleft + nright) return;
   const int col = warp < nleft ? warp : c_skip1 + (warp - nleft);
-  const int np = ntop + *pair_count_ext;
   T* Ac = A + (size_t)col * lda;
   constexpr int kMaxPer = (2 * kLeafMax + 31) / 32;
   T v[kMaxPer];
@@ -299,44 +317,69 @@ laswp_pairs_kernel(T* __restrict__ A, int lda, int ncols, int c_skip0, int c_ski
 }
 
 // B := L^{-1} B for a unit lower triangular L (k x k, k <= 64) and B of k
-// rows; one CTA per slab of BC columns of B (BC = 64 for float, 16 for
-// double, keeping static shared memory under 48 KB).  Forward substitution
-// in the reference order (BLAS/SRC/dtrsm.f:290-300): for each k, rows below
-// k get B(i,j) - B(k,j)*A(i,k).
-template <typename T>
-struct TrsmSlab { static constexpr int BC = sizeof(T) == 8 ? 16 : 64; };
+// rows.  Four lanes per column of B: lane s of a group holds rows s, s+4,
+// s+8, ... of that column in registers; at step kk the lane holding row kk
+// broadcasts it with a shuffle and every lane updates its rows below kk --
+// forward substitution in the reference order (BLAS/SRC/dtrsm.f:290-300:
+// for each k, rows below k get B(i,j) - B(k,j)*A(i,k)) with no block
+// barriers inside the solve.  L is staged in shared memory (padded rows).
+constexpr int kTrsmThreads = 256;
+constexpr int kTrsmCols = kTrsmThreads / 4;
 
-template <typename T, bool EXACT>
-__global__ void __launch_bounds__(256)
+template <typename T, int KMAX>
+constexpr int trsm_leaf_smem() {
+  return (KMAX * (KMAX + 1) + KMAX * (kTrsmCols + 1)) * (int)sizeof(T);
+}
+
+template <typename T, bool EXACT, int KMAX>
+__global__ void __launch_bounds__(kTrsmThreads)
 trsm_llnu_leaf_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int ldb, int k, int ncols) {
-  constexpr int BC = TrsmSlab<T>::BC;
-  constexpr int RG = 256 / BC;              // row groups
-  __shared__ T Ls[kLeafMax][kLeafMax];
-  __shared__ T Bs[kLeafMax][BC + 1];
+  constexpr int RPL = KMAX / 4;                              // rows per lane
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  T* Ls = reinterpret_cast<T*>(trsm_smem);                  // Ls[i * (KMAX+1) + j] = L(i, j)
+  T* Bs = Ls + KMAX * (KMAX + 1);                           // [KMAX][kTrsmCols + 1]
   const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * BC;
-  const int nc = min(BC, ncols - c0);
-  for (int e = tid; e < k * k; e += 256) {
-    int c = e / k, r = e - c * k;
-    Ls[r][c] = L[(size_t)r + (size_t)c * ldl];
+  const int c0 = blockIdx.x * kTrsmCols;
+  const int nc = min(kTrsmCols, ncols - c0);
+  // stage L (k x k) and this CTA's columns of B, loads batched per thread
+  batched_copy<8, kTrsmThreads, T>(
+      k * k, tid, [&](int e) { const int c = e / k, r = e - c * k; return L[(size_t)r + (size_t)c * ldl]; },
+      [&](int e, T v) { const int c = e / k, r = e - c * k; Ls[r * (KMAX + 1) + c] = v; });
+  batched_copy<8, kTrsmThreads, T>(
+      k * nc, tid, [&](int e) { const int c = e / k, r = e - c * k; return B[(size_t)r + (size_t)(c0 + c) * ldb]; },
+      [&](int e, T v) { const int c = e / k, r = e - c * k; Bs[r * (kTrsmCols + 1) + c] = v; });
+  __syncthreads();
+  const int col = tid >> 2, sub = tid & 3;
+  const unsigned gmask = 0xFu << ((tid & 31) & ~3);
+  T x[RPL];
+#pragma unroll
+  for (int t = 0; t < RPL; ++t) {
+    const int i = sub + 4 * t;
+    x[t] = (col < nc && i < k) ? Bs[i * (kTrsmCols + 1) + col] : T(0);
   }
-  for (int e = tid; e < k * nc; e += 256) {
-    int c = e / k, r = e - c * k;
-    Bs[r][c] = B[(size_t)r + (size_t)(c0 + c) * ldb];
+#pragma unroll
+  for (int kk = 0; kk < KMAX - 1; ++kk) {
+    if (kk < k - 1) {
+      const T xk = __shfl_sync(0xffffffffu, x[kk / 4], ((tid & 31) & ~3) | (kk & 3));
+      (void)gmask;
+#pragma unroll
+      for (int t = 0; t < RPL; ++t) {
+        const int i = sub + 4 * t;
+        if (i > kk && i < k) x[t] = fnmadd<EXACT>(xk, Ls[i * (KMAX + 1) + kk], x[t]);
+      }
+    }
+  }
+  if (col < nc) {
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+      const int i = sub + 4 * t;
+      if (i < k) Bs[i * (kTrsmCols + 1) + col] = x[t];
+    }
   }
   __syncthreads();
-  const int c = tid % BC;
-  const int rq = tid / BC;
-  for (int kk = 0; kk < k - 1; ++kk) {
-    if (c < nc) {
-      T bk = Bs[kk][c];
-      for (int r = kk + 1 + rq; r < k; r += RG) Bs[r][c] = fnmadd<EXACT>(bk, Ls[r][kk], Bs[r][c]);
-    }
-    __syncthreads();
-  }
-  for (int e = tid; e < k * nc; e += 256) {
-    int cc = e / k, r = e - cc * k;
-    B[(size_t)r + (size_t)(c0 + cc) * ldb] = Bs[r][cc];
+  for (int e = tid; e < k * nc; e += kTrsmThreads) {
+    const int c = e / k, r = e - c * k;
+    B[(size_t)r + (size_t)(c0 + c) * ldb] = Bs[r * (kTrsmCols + 1) + c];
   }
 }
 

@@ -13,16 +13,35 @@
 
 namespace gb {
 
+// DLANGE('I') into a device double: exact mode sums each row in column order
+// (SRC/dlange.f:173-189); otherwise the columns are cut into chunks whose
+// partial row sums are folded in fixed order (deterministic, more parallel).
+static int row_abs_sums(int m, int n, const double* dA, int lda, double* d_out, cudaStream_t s) {
+  const int nsplit = options().exact ? 1 : std::max(1, std::min(16, n / 512));
+  const int chunk = (n + nsplit - 1) / nsplit;
+  DevScratch buf(sizeof(double) * (size_t)m * (nsplit + 1), s);
+  if (!buf.p) return (int)cudaErrorMemoryAllocation;
+  double* part = buf.as<double>();
+  double* rows = part + (size_t)m * nsplit;
+  if (nsplit == 1) {
+    GB_LAUNCH(row_abs_sum_kernel<double><<<(m + 63) / 64, 64, 0, s>>>(dA, lda, m, n, rows));
+  } else {
+    dim3 g((m + 63) / 64, nsplit);
+    GB_LAUNCH(row_abs_sum_split_kernel<<<g, 64, 0, s>>>(dA, lda, m, n, chunk, part));
+    GB_LAUNCH(fold_partials_kernel<<<(m + 255) / 256, 256, 0, s>>>(part, nsplit, m, rows));
+  }
+  GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, m, d_out));
+  return (int)cudaGetLastError();
+}
+
 double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, int* err) {
   *err = 0;
   if (m <= 0 || n <= 0) return 0.0;
-  DevScratch buf(sizeof(double) * ((size_t)m + 1), s);
+  DevScratch buf(sizeof(double), s);
   if (!buf.p) { *err = (int)cudaErrorMemoryAllocation; return 0.0; }
-  double* rows = buf.as<double>();
-  GB_LAUNCH(row_abs_sum_kernel<double><<<(m + 63) / 64, 64, 0, s>>>(dA, lda, m, n, rows));
-  GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, m, rows + m));
+  if ((*err = row_abs_sums(m, n, dA, lda, buf.as<double>(), s))) return 0.0;
   double h = 0;
-  cudaMemcpyAsync(&h, rows + m, sizeof(double), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(&h, buf.as<double>(), sizeof(double), cudaMemcpyDeviceToHost, s);
   if (cudaStreamSynchronize(s) != cudaSuccess) *err = (int)cudaGetLastError();
   return h;
 }
@@ -161,12 +180,7 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   int rc;
 
   // ANRM = DLANGE('I'), kept on the device for the convergence test
-  {
-    DevScratch rows(sizeof(double) * (size_t)n, s);
-    if (!rows.p) return (int)cudaErrorMemoryAllocation;
-    GB_LAUNCH(row_abs_sum_kernel<double><<<(n + 63) / 64, 64, 0, s>>>(dA, lda, n, n, rows.as<double>()));
-    GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows.as<double>(), n, anrm));
-  }
+  if ((rc = row_abs_sums(n, n, dA, lda, anrm, s))) return rc;
   GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
   // SX = DLAG2S(B), SA = DLAG2S(A)
   GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
@@ -175,12 +189,12 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[0]) { *iter = -2; goto fallback; }
   // SGETRF(SA)
-  rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32);
+  // the factorization also returns the gather permutation the solves reuse
+  rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32, perm);
   if (rc) return rc;
   GB_CUDA_TRY(cudaMemcpyAsync(hflags + 2, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[2] != 0) { *iter = -3; goto fallback; }
-  if ((rc = ipiv_perm_dev(dIpiv, 1, n, 1, 0, n, perm, s))) return rc;
   // SX = SA^{-1} SX, X = SLAG2D(SX), R = B - A X
   if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
   GB_LAUNCH(slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));

@@ -69,10 +69,11 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   const int rbeg = b * R;
   const int nrows = max(0, min(M, rbeg + R) - rbeg);
 
-  for (int e = tid; e < JB * nrows; e += kClusterThreads) {
-    int c = e / nrows, r = e - c * nrows;
-    tile[c * R + r] = P[(size_t)(rbeg + r) + (size_t)c * lda];
-  }
+  if (nrows > 0)
+    batched_copy<8, kClusterThreads, float>(
+        JB * nrows, tid,
+        [&](int e) { const int c = e / nrows, r = e - c * nrows; return P[(size_t)(rbeg + r) + (size_t)c * lda]; },
+        [&](int e, float v) { const int c = e / nrows, r = e - c * nrows; tile[c * R + r] = v; });
   for (int r = tid; r < nrows; r += kClusterThreads) label[r] = rbeg + r;
   __syncthreads();
   // candidates for column 0
@@ -181,6 +182,195 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
         pair_src[s] = row0 + label[r];
       } else {
         atomicCAS(status, kStatusOk, kStatusCapacity);
+      }
+    }
+  }
+}
+
+}  // namespace gb
+
+namespace gb {
+
+// Register-resident form of the cluster leaf: each thread owns RPT rows of
+// its CTA (local rows t, t+512, ...) and keeps their JB values in registers
+// for the whole leaf (JB * RPT = 64), so the rank-1 updates never touch
+// shared memory.  Only the published candidate row, row k and the pivot row
+// travel through (distributed) shared memory.  Column indices that depend on
+// k are resolved with unrolled selects so the row arrays stay in registers.
+template <bool EXACT, int JB>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+leaf_panel_cluster_reg_kernel(float* __restrict__ P, int lda, int M, int jb, int R, int row0, int* __restrict__ ipiv,
+                              int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
+                              int* __restrict__ pair_count, int* __restrict__ status) {
+  namespace cg = cooperative_groups;
+  constexpr int RPT = 64 / JB;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ ClusterSlot slot[2];
+  __shared__ __align__(16) float urow[kLeafMax];
+  __shared__ __align__(16) float rowk_s[kLeafMax];
+  __shared__ unsigned long long wbest[kClusterThreads / 32];
+  __shared__ float pv_s;
+  __shared__ int win_label_s, rowk_label_s, prow_s;
+
+  const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rbeg = b * R;
+  const int nrows = max(0, min(M, rbeg + R) - rbeg);
+
+  float a[RPT][JB];
+  int lab[RPT];
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + i * kClusterThreads;
+    lab[i] = rbeg + r;
+#pragma unroll
+    for (int c = 0; c < JB; ++c) a[i][c] = (r < nrows && c < jb) ? P[(size_t)(rbeg + r) + (size_t)c * lda] : 0.0f;
+  }
+  unsigned long long mykey = 0;
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + i * kClusterThreads;
+    if (r < nrows) {
+      const unsigned long long kk = pack_key(a[i][0], rbeg + r, 0);
+      mykey = kk > mykey ? kk : mykey;
+    }
+  }
+
+  for (int k = 0; k < jb; ++k) {
+    const int par = k & 1;
+    // 1. the CTA's best candidate, known to every warp
+    mykey = warp_max_u64(mykey);
+    if (lane == 0) wbest[warp] = mykey;
+    __syncthreads();
+    unsigned long long ck = lane < kClusterThreads / 32 ? wbest[lane] : 0ull;
+    ck = warp_max_u64(ck);
+    ClusterSlot& sl = slot[par];
+    if (tid == 0) sl.key = ck;
+    // the owner of that row publishes it; the owner of row k publishes row k
+    const int cand_local = ck ? (int)(0xFFFFFFFFu - (unsigned)(ck & 0xFFFFFFFFull)) - rbeg : -1;
+    const int k_local = (k >= rbeg && k < rbeg + nrows) ? k - rbeg : -1;
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + i * kClusterThreads;
+      if (r == cand_local) {
+#pragma unroll
+        for (int c = 0; c < JB; ++c) sl.row[c] = a[i][c];
+        sl.label = lab[i];
+      }
+      if (r == k_local) {
+#pragma unroll
+        for (int c = 0; c < JB; ++c) sl.row_k[c] = a[i][c];
+        sl.row_k_label = lab[i];
+      }
+    }
+    // 2. one cluster barrier per column
+    cluster.sync();
+    // 3. winner and rows, fetched through distributed shared memory
+    if (warp == 0) {
+      unsigned long long kk = 0ull;
+      if (lane < G) kk = cluster.map_shared_rank(&slot[par], lane)->key;
+      const unsigned long long wk = warp_max_u64(kk);
+      const int wc = __ffsll(__ballot_sync(0xffffffffu, kk == wk && lane < G)) - 1;
+      const int prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
+      const ClusterSlot* ws = cluster.map_shared_rank(&slot[par], wc);
+      if (lane < JB) urow[lane] = ws->row[lane];
+      if (lane == 0) win_label_s = ws->label;
+      const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
+      if (own_p && prow != k) {
+        const ClusterSlot* ks = cluster.map_shared_rank(&slot[par], k / R);
+        if (lane < JB) rowk_s[lane] = ks->row_k[lane];
+        if (lane == 0) rowk_label_s = ks->row_k_label;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        prow_s = prow;
+        pv_s = urow[k];
+        if (b == 0) {
+          ipiv[k] = row0 + prow + 1;
+          if (urow[k] == 0.0f && *info == 0) *info = row0 + k + 1;
+        }
+      }
+    }
+    __syncthreads();
+    // 4. interchange rows k and prow in the owners' registers
+    const int prow = prow_s;
+    const int p_local = (prow >= rbeg && prow < rbeg + nrows) ? prow - rbeg : -1;
+    if (prow != k) {
+#pragma unroll
+      for (int i = 0; i < RPT; ++i) {
+        const int r = tid + i * kClusterThreads;
+        if (r == k_local) {
+#pragma unroll
+          for (int c = 0; c < JB; ++c) a[i][c] = urow[c];
+          lab[i] = win_label_s;
+        }
+        if (r == p_local) {
+#pragma unroll
+          for (int c = 0; c < JB; ++c) a[i][c] = rowk_s[c];
+          lab[i] = rowk_label_s;
+        }
+      }
+    }
+    // 5. scale, rank-1 update and the candidate search of column k+1
+    const float pv = pv_s;
+    const bool scale = pv != 0.0f;
+    const bool recip = fabsf(pv) >= Lim<float>::sfmin();
+    const float rp = 1.0f / pv;
+    // the pivot row in registers for 16-wide leaves; 32-wide leaves read it
+    // from shared memory (broadcast) to stay within 128 registers per thread
+    constexpr bool kURegs = JB <= 16;
+    float u[kURegs ? JB : 1];
+    if constexpr (kURegs) {
+#pragma unroll
+      for (int c = 0; c < JB; ++c) u[c] = urow[c];
+    }
+    mykey = 0;
+#pragma unroll
+    for (int i = 0; i < RPT; ++i) {
+      const int r = tid + i * kClusterThreads;
+      if (r < nrows && rbeg + r > k) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < JB; ++c)
+          if (c == k) v = a[i][c];
+        const float l = scale ? (recip ? v * rp : v / pv) : v;
+#pragma unroll
+        for (int c = 0; c < JB; ++c) {
+          if (c == k) a[i][c] = l;
+          else if (c > k) a[i][c] = fnmadd<EXACT>(l, kURegs ? u[kURegs ? c : 0] : urow[c], a[i][c]);
+        }
+        if (k + 1 < jb) {
+          float nx = 0.0f;
+#pragma unroll
+          for (int c = 0; c < JB; ++c)
+            if (c == k + 1) nx = a[i][c];
+          const unsigned long long kk = pack_key(nx, rbeg + r, k + 1);
+          mykey = kk > mykey ? kk : mykey;
+        }
+      }
+    }
+  }
+  // no CTA may exit while others can still read its shared memory
+  cluster.sync();
+#pragma unroll
+  for (int i = 0; i < RPT; ++i) {
+    const int r = tid + i * kClusterThreads;
+    if (r < nrows) {
+#pragma unroll
+      for (int c = 0; c < JB; ++c)
+        if (c < jb) P[(size_t)(rbeg + r) + (size_t)c * lda] = a[i][c];
+      const int g = rbeg + r;
+      if (g < jb) {
+        pair_dst[g] = row0 + g;
+        pair_src[g] = row0 + lab[i];
+      } else if (lab[i] != g) {
+        int s = jb + atomicAdd(pair_count, 1);
+        if (s < 2 * kLeafMax) {
+          pair_dst[s] = row0 + g;
+          pair_src[s] = row0 + lab[i];
+        } else {
+          atomicCAS(status, kStatusOk, kStatusCapacity);
+        }
       }
     }
   }

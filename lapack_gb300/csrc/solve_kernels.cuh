@@ -270,6 +270,33 @@ row_abs_sum_kernel(const T* __restrict__ A, int lda, int m, int n, T* __restrict
   rowsum[i] = s;
 }
 
+// Chunked row sums: part[s][i] = sum of |A(i, l)| over chunk s of the columns.
+static __global__ void __launch_bounds__(64)
+row_abs_sum_split_kernel(const double* __restrict__ A, int lda, int m, int n, int chunk, double* __restrict__ part) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int l0 = blockIdx.y * chunk, l1 = min(n, l0 + chunk);
+  const double* p = A + i;
+  double s = 0;
+  int j = l0;
+  for (; j + 16 <= l1; j += 16) {
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) v[u] = p[(size_t)(j + u) * lda];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) s = s + fabs(v[u]);
+  }
+  for (; j < l1; ++j) s = s + fabs(p[(size_t)j * lda]);
+  part[(size_t)blockIdx.y * m + i] = s;
+}
+static __global__ void fold_partials_kernel(const double* __restrict__ part, int nsplit, int m, double* __restrict__ out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double s = 0;
+  for (int k = 0; k < nsplit; ++k) s = s + part[(size_t)k * m + i];
+  out[i] = s;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(1024)
 max_nan_kernel(const T* __restrict__ x, int m, T* __restrict__ out) {
