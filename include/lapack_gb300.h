@@ -207,6 +207,26 @@ int gb300_dgemm_update_dev(int m, int n, int k, const double* dA, int lda, const
 int gb300_sgemm_update_dev(int mode, int m, int n, int k, const float* dA, int lda, const float* dB, int ldb,
                            float* dC, int ldc, void* stream);
 
+/* Batched solves of many independent systems of uneven size (n <= 512,
+ * nrhs <= 4) in one persistent launch; no reference counterpart (each
+ * system is DGESV, SRC/dgesv.f, or DGETRF for the getrf form).  Arrays of
+ * per-system device pointers and sizes, all in device memory; IPIV and
+ * INFO per system (INFO = -1 for n > 512).  Asynchronous: nothing is
+ * copied back and the host is not synchronised, so the call can be
+ * captured into a CUDA graph. */
+int gb300_dgesv_vbatched_dev(int batch, const int* d_n, const int* d_nrhs, double* const* dA_array, const int* d_lda,
+                             int* const* dIpiv_array, double* const* dB_array, const int* d_ldb, int* d_info,
+                             void* stream);
+int gb300_sgesv_vbatched_dev(int batch, const int* d_n, const int* d_nrhs, float* const* dA_array, const int* d_lda,
+                             int* const* dIpiv_array, float* const* dB_array, const int* d_ldb, int* d_info,
+                             void* stream);
+int gb300_dgetrf_vbatched_dev(int batch, const int* d_n, double* const* dA_array, const int* d_lda,
+                              int* const* dIpiv_array, int* d_info, void* stream);
+/* Panel width used for each 64-row size bucket (8 entries; dtype 0 double,
+ * 1 float), as chosen by the autotuner (lapack_gb300.autotune_batched). */
+int gb300_vbatched_set_nb(int dtype, const int* table);
+int gb300_vbatched_get_nb(int dtype, int* table);
+
 /* Options: "exact" (0/1: products rounded separately, bitwise the
  * reference's operation order), "nb64" / "nb32" (outer block sizes),
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32

@@ -274,3 +274,84 @@ def to_colmajor(a_np, device="cuda"):
     import torch
     a = np.asarray(a_np)
     return torch.from_numpy(np.ascontiguousarray(a.T)).to(device).t()
+
+
+# ------------------------------------------------------- batched (device)
+class VBatch:
+    """Device storage for a batch of independent systems of uneven size:
+    packed column-major matrices plus the per-system pointer and size
+    arrays the batched entry points take."""
+
+    def __init__(self, As, Bs, dtype=None, device="cuda"):
+        import torch
+        dtype = dtype or torch.float64
+        self.dtype = dtype
+        self.ns = [int(a.shape[0]) for a in As]
+        self.nrhs = [int(np.asarray(b).reshape(a.shape[0], -1).shape[1]) for a, b in zip(As, Bs)]
+        ne = np.dtype(np.float64 if dtype == torch.float64 else np.float32)
+        aoff = np.cumsum([0] + [n * n for n in self.ns])
+        boff = np.cumsum([0] + [n * r for n, r in zip(self.ns, self.nrhs)])
+        poff = np.cumsum([0] + self.ns)
+        ha = np.concatenate([np.asarray(a, dtype=ne).T.reshape(-1) for a in As]) if As else np.zeros(0, ne)
+        hb = np.concatenate([np.asarray(b, dtype=ne).reshape(n, -1).T.reshape(-1) for b, n in zip(Bs, self.ns)])
+        self.A = torch.from_numpy(ha).to(device)
+        self.B = torch.from_numpy(hb).to(device)
+        self.ipiv = torch.zeros(int(poff[-1]), dtype=torch.int32, device=device)
+        es = self.A.element_size()
+        self.aoff, self.boff, self.poff = aoff, boff, poff
+        self.d_n = torch.tensor(self.ns, dtype=torch.int32, device=device)
+        self.d_nrhs = torch.tensor(self.nrhs, dtype=torch.int32, device=device)
+        self.d_ld = self.d_n.clone()
+        self.d_Ap = torch.tensor([self.A.data_ptr() + int(o) * es for o in aoff[:-1]], dtype=torch.int64, device=device)
+        self.d_Bp = torch.tensor([self.B.data_ptr() + int(o) * es for o in boff[:-1]], dtype=torch.int64, device=device)
+        self.d_Pp = torch.tensor([self.ipiv.data_ptr() + int(o) * 4 for o in poff[:-1]], dtype=torch.int64,
+                                 device=device)
+        self.info = torch.zeros(len(self.ns), dtype=torch.int32, device=device)
+
+    def launch(self, stream=None, factor_only=False):
+        import torch
+        L = lib()
+        p = lambda t: ctypes.c_void_p(t.data_ptr())
+        batch = len(self.ns)
+        if factor_only:
+            rc = L.gb300_dgetrf_vbatched_dev(batch, p(self.d_n), p(self.d_Ap), p(self.d_ld), p(self.d_Pp),
+                                             p(self.info), _stream_ptr(stream))
+        else:
+            fn = L.gb300_dgesv_vbatched_dev if self.dtype == torch.float64 else L.gb300_sgesv_vbatched_dev
+            rc = fn(batch, p(self.d_n), p(self.d_nrhs), p(self.d_Ap), p(self.d_ld), p(self.d_Pp), p(self.d_Bp),
+                    p(self.d_ld), p(self.info), _stream_ptr(stream))
+        if rc != 0:
+            raise RuntimeError(f"gb300 batched solve failed with status {rc}")
+
+    def results(self):
+        """Lists (lu, ipiv, x) on the host and the INFO array."""
+        ha = self.A.cpu().numpy()
+        hb = self.B.cpu().numpy()
+        hp = self.ipiv.cpu().numpy()
+        lus, ips, xs = [], [], []
+        for i, n in enumerate(self.ns):
+            lus.append(ha[self.aoff[i]:self.aoff[i + 1]].reshape(n, n).T)
+            xs.append(hb[self.boff[i]:self.boff[i + 1]].reshape(self.nrhs[i], n).T)
+            ips.append(hp[self.poff[i]:self.poff[i + 1]])
+        return lus, ips, xs, self.info.cpu().numpy()
+
+
+def gesv_vbatched(As, Bs, dtype=None):
+    """Batched xGESV of independent systems (n <= 512, nrhs <= 4) in one
+    persistent launch.  Returns (lu list, ipiv list, x list, info array)."""
+    vb = VBatch(As, Bs, dtype)
+    vb.launch()
+    import torch
+    torch.cuda.synchronize()
+    return vb.results()
+
+
+def vbatched_nb(dtype_code):
+    tab = (ctypes.c_int * 8)()
+    lib().gb300_vbatched_get_nb(int(dtype_code), tab)
+    return list(tab)
+
+
+def set_vbatched_nb(dtype_code, table):
+    arr = (ctypes.c_int * 8)(*[int(v) for v in table])
+    return lib().gb300_vbatched_set_nb(int(dtype_code), arr)
