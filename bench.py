@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweep", action="store_true", help="also solve at kappa 1e2 and 1e10 once each")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
+    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched"],
+                   help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
+    p.add_argument("--dtype", default="d", choices=["d", "s"], help="precision of the batched workload")
+    p.add_argument("--batch", type=int, default=20000)
     return p.parse_args()
 
 
@@ -375,8 +379,118 @@ def run_gpu(args, rank, world):
     return result
 
 
+def run_batched(args):
+    """20000 independent systems, n uniform in [8, 512] (seeded), nrhs in
+    {1, 2, 4}, entries N(0,1) with n*I added to every other system, solved in
+    one persistent launch captured in a CUDA graph.  One step = one graph
+    replay over the whole batch (inputs restored between steps, outside the
+    timed region)."""
+    import torch
+    import lapack_gb300 as g
+    from lapack_gb300 import autotune
+    autotune.load()
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    dtype = torch.float64 if args.dtype == "d" else torch.float32
+    es = 8 if args.dtype == "d" else 4
+    rng = np.random.default_rng(args.seed)
+    ns = rng.integers(8, 513, args.batch).astype(np.int64)
+    nrhs = rng.choice([1, 2, 4], args.batch).astype(np.int64)
+    aoff = np.concatenate([[0], np.cumsum(ns * ns)])
+    boff = np.concatenate([[0], np.cumsum(ns * nrhs)])
+    poff = np.concatenate([[0], np.cumsum(ns)])
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    A = torch.randn(int(aoff[-1]), dtype=dtype, device=dev, generator=gen)
+    B = torch.randn(int(boff[-1]), dtype=dtype, device=dev, generator=gen)
+    # n*I on every other system's diagonal
+    diag = np.concatenate([aoff[i] + np.arange(ns[i]) * (ns[i] + 1) for i in range(0, args.batch, 2)])
+    vals = np.concatenate([np.full(ns[i], float(ns[i])) for i in range(0, args.batch, 2)])
+    A.index_add_(0, torch.from_numpy(diag).to(dev), torch.from_numpy(vals).to(dev, dtype))
+    A0, B0 = A.clone(), B.clone()
+    ipiv = torch.zeros(int(poff[-1]), dtype=torch.int32, device=dev)
+    info = torch.zeros(args.batch, dtype=torch.int32, device=dev)
+    d_n = torch.from_numpy(ns.astype(np.int32)).to(dev)
+    d_r = torch.from_numpy(nrhs.astype(np.int32)).to(dev)
+    Ap = torch.from_numpy((A.data_ptr() + aoff[:-1] * es).astype(np.int64)).to(dev)
+    Bp = torch.from_numpy((B.data_ptr() + boff[:-1] * es).astype(np.int64)).to(dev)
+    Pp = torch.from_numpy((ipiv.data_ptr() + poff[:-1] * 4).astype(np.int64)).to(dev)
+    fn = L.gb300_dgesv_vbatched_dev if args.dtype == "d" else L.gb300_sgesv_vbatched_dev
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def launch(stream):
+        rc = fn(args.batch, vp(d_n), vp(d_r), vp(Ap), vp(d_n), vp(Pp), vp(Bp), vp(d_n), vp(info),
+                ctypes.c_void_p(stream.cuda_stream))
+        if rc:
+            raise RuntimeError(f"batched solve status {rc}")
+
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        launch(s)                      # warm-up (kernel attributes, pool)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    A.copy_(A0)
+    B.copy_(B0)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        graph.capture_begin()
+        launch(s)
+        graph.capture_end()
+    times = []
+    launches0 = L.gb300_launch_count()
+    clocks = ClockSampler(dev.index)
+    clocks.start()
+    for it in range(args.warmup + args.steps):
+        A.copy_(A0)
+        B.copy_(B0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        graph.replay()
+        e1.record()
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    ms = sum(times) / len(times)
+    flops = float(np.sum(2.0 / 3.0 * ns.astype(np.float64) ** 3 + 2.0 * ns ** 2 * nrhs))
+    bytes_ = float(np.sum(es * (2.0 * ns * ns + 2.0 * ns * nrhs) + 4.0 * ns))
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    L.gb300_probe_peak.restype = ctypes.c_double
+    fma_peak = L.gb300_probe_peak(0 if args.dtype == "d" else 1)
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    # residual spot check of a few systems
+    hA, hB = A0.cpu().numpy(), B0.cpu().numpy()
+    X = B.cpu().numpy()
+    worst = 0.0
+    for i in list(range(0, args.batch, max(1, args.batch // 8))):
+        n, r = int(ns[i]), int(nrhs[i])
+        a = hA[aoff[i]:aoff[i + 1]].reshape(n, n).T.astype(np.float64)
+        b = hB[boff[i]:boff[i + 1]].reshape(r, n).T.astype(np.float64)
+        x = X[boff[i]:boff[i + 1]].reshape(r, n).T.astype(np.float64)
+        res = np.abs(b - a @ x).max() / (np.abs(a).sum(1).max() * np.abs(x).max() * n * (2.0 ** -53 if args.dtype == "d" else 2.0 ** -24))
+        worst = max(worst, res)
+    return {
+        "metric": f"batched uneven {'D' if args.dtype == 'd' else 'S'}GESV: {args.batch} systems, n in [8,512], nrhs in {{1,2,4}}, one persistent launch",
+        "value": ms * 1e-3, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "dtype": "f64" if args.dtype == "d" else "f32", "data": "synthetic",
+        "config": {"workload": "batched uneven solves in one CUDA-graph-captured persistent launch", "batch": args.batch,
+                   "nb_table": g.vbatched_nb(0 if args.dtype == "d" else 1),
+                   "l2": f"inputs {bytes_ / 2e9:.1f} GB >> L2"},
+        "gflops": flops / ms / 1e6, "fma_peak_tflops": fma_peak, "frac_of_fma_peak": flops / ms / 1e9 / fma_peak,
+        "hbm_gbs": bytes_ / ms / 1e6, "frac_of_hbm": bytes_ / ms / 1e6 / hbm, "algorithmic_bytes": bytes_,
+        "algorithmic_flops": flops, "info_nonzero": int((info != 0).sum().item()), "worst_scaled_residual": worst,
+        "gpu_launches": (L.gb300_launch_count() - launches0) // max(1, args.steps + args.warmup), "clocks": clk,
+    }
+
+
 def main():
     args = parse()
+    if args.workload == "batched" and args.impl == "gb300":
+        print(json.dumps(run_batched(args)))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.warmup < 3 and args.impl == "gb300":

@@ -355,3 +355,10 @@ def vbatched_nb(dtype_code):
 def set_vbatched_nb(dtype_code, table):
     arr = (ctypes.c_int * 8)(*[int(v) for v in table])
     return lib().gb300_vbatched_set_nb(int(dtype_code), arr)
+
+
+def autotune_batched(dtype_code, count=600):
+    """Times every candidate panel width per size bucket and installs the
+    fastest (see lapack_gb300.autotune)."""
+    from . import autotune
+    return autotune.tune_batched(dtype_code, count)
