@@ -227,6 +227,18 @@ int gb300_dgetrf_vbatched_dev(int batch, const int* d_n, double* const* dA_array
 int gb300_vbatched_set_nb(int dtype, const int* table);
 int gb300_vbatched_get_nb(int dtype, int* table);
 
+/* Adjoint of X = A^{-1} B from the stored factors (no reference counterpart;
+ * the building blocks are DGETRS('T'), SRC/dgetrs.f:199-217, and
+ * DGEMM('N','T'), BLAS/SRC/dgemm.f:363-383): gB = A^{-T} gX and, when dGA
+ * is not NULL, gA = -gB X^T.  nrhs <= 16.  Synchronous. */
+int gb300_dgesv_adjoint_dev(int n, int nrhs, const double* dLU, int ldlu, const int* dIpiv, const double* dX, int ldx,
+                            const double* dGX, int ldgx, double* dGB, int ldgb, double* dGA, int ldga, void* stream);
+/* The same for a uniform-size batch packed with element strides. */
+int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dLU, long long stride_lu,
+                                    const int* dIpiv, long long stride_ipiv, const double* dX, long long stride_x,
+                                    const double* dGX, long long stride_gx, double* dGB, long long stride_gb,
+                                    double* dGA, long long stride_ga, void* stream);
+
 /* Options: "exact" (0/1: products rounded separately, bitwise the
  * reference's operation order), "nb64" / "nb32" (outer block sizes),
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32

@@ -362,3 +362,68 @@ def autotune_batched(dtype_code, count=600):
     fastest (see lapack_gb300.autotune)."""
     from . import autotune
     return autotune.tune_batched(dtype_code, count)
+
+
+# ------------------------------------------------------------------ adjoint
+def adjoint_dev(LU, ipiv, X, gX, want_gA=True, stream=None):
+    """gB = A^{-T} gX and gA = -gB X^T from stored factors (column-major CUDA
+    float64 tensors).  Returns (gB, gA)."""
+    import torch
+    n, nrhs = X.shape
+    ldlu, plu = _colmajor_view(LU)
+    ldx, px = _colmajor_view(X)
+    ldg, pg = _colmajor_view(gX)
+    gB = colmajor_empty(n, nrhs, torch.float64, X.device)
+    gA = colmajor_empty(n, n, torch.float64, X.device) if want_gA else None
+    ldgb, pgb = _colmajor_view(gB)
+    vp = ctypes.c_void_p
+    rc = lib().gb300_dgesv_adjoint_dev(n, nrhs, vp(plu), ldlu, vp(ipiv.data_ptr()), vp(px), ldx, vp(pg), ldg, vp(pgb),
+                                       ldgb, vp(gA.data_ptr()) if want_gA else None, n, _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 adjoint failed with status {rc}")
+    return gB, gA
+
+
+def _solve_autograd_class():
+    import torch
+
+    class Solve(torch.autograd.Function):
+        """X = A^{-1} B on the GPU (DGETRF + DGETRS); the backward pass runs
+        the library's adjoint on the saved factors.  Meant for gradient
+        checks, not as a training op."""
+
+        @staticmethod
+        def forward(ctx, A, B):
+            n = A.shape[0]
+            LU = colmajor_empty(n, n, torch.float64, A.device)
+            LU.copy_(A)
+            ipiv = torch.empty(n, dtype=torch.int32, device=A.device)
+            info = getrf_dev(LU, ipiv)
+            if info != 0:
+                raise RuntimeError(f"singular matrix (INFO={info})")
+            X = colmajor_empty(n, B.shape[1], torch.float64, A.device)
+            X.copy_(B)
+            getrs_dev(LU, ipiv, X)
+            ctx.save_for_backward(LU, ipiv, X)
+            return X.clone()
+
+        @staticmethod
+        def backward(ctx, gX):
+            LU, ipiv, X = ctx.saved_tensors
+            g = colmajor_empty(gX.shape[0], gX.shape[1], torch.float64, gX.device)
+            g.copy_(gX)
+            gB, gA = adjoint_dev(LU, ipiv, X, g, want_gA=ctx.needs_input_grad[0])
+            return gA, gB
+
+    return Solve
+
+
+_SOLVE = None
+
+
+def solve(A, B):
+    """Differentiable X = A^{-1} B (float64 CUDA tensors, B of shape (n, nrhs))."""
+    global _SOLVE
+    if _SOLVE is None:
+        _SOLVE = _solve_autograd_class()
+    return _SOLVE.apply(A, B)

@@ -73,6 +73,10 @@ int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, 
 int dlag2s_dev(int m, int n, const double* dA, int lda, float* dS, int lds, long long* first, cudaStream_t s);
 int slag2d_dev(int m, int n, const float* dS, int lds, double* dA, int lda, cudaStream_t s);
 
+// gB = A^{-T} gX, gA = -gB X^T from the stored factors (gA skipped if null).
+int adjoint_dev(int n, int nrhs, const double* dLU, int ldlu, const int* dIpiv, const double* dX, int ldx,
+                const double* dGX, int ldgx, double* dGB, int ldgb, double* dGA, int ldga, cudaStream_t s);
+
 // Kernel launch status of the last failing bounded wait, 0 if none.
 int check_status(int* dStatus, cudaStream_t s);
 int* device_status_word();
