@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--sweep", action="store_true", help="also solve at kappa 1e2 and 1e10 once each")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
-    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched"],
+    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint"],
                    help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
     p.add_argument("--dtype", default="d", choices=["d", "s"], help="precision of the batched workload")
     p.add_argument("--batch", type=int, default=20000)
@@ -486,10 +486,82 @@ def run_batched(args):
     }
 
 
+def run_adjoint(args):
+    """The differentiable batched solve: 64 systems of n = 2048,
+    A = N(0,1)/sqrt(n) + I, B and gX of 8 columns.  One step = the adjoint of
+    the whole batch (gB = A^{-T} gX by the transposed solve on the stored
+    factors, gA = -gB X^T written in full: 2 GiB), factors resident."""
+    import torch
+    import lapack_gb300 as g
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    batch, n, nrhs = 64, 2048, 8
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    LU = torch.randn(batch, n, n, dtype=torch.float64, device=dev, generator=gen) / n ** 0.5
+    LU += torch.eye(n, dtype=torch.float64, device=dev)
+    X = torch.randn(batch, nrhs, n, dtype=torch.float64, device=dev, generator=gen)
+    GX = torch.randn(batch, nrhs, n, dtype=torch.float64, device=dev, generator=gen)
+    ip = torch.empty(batch, n, dtype=torch.int32, device=dev)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    info = ctypes.c_int(0)
+    vp = ctypes.c_void_p
+    t0 = time.perf_counter()
+    for k in range(batch):
+        L.gb300_dgesv_dev(n, nrhs, vp(LU[k].data_ptr()), n, vp(ip[k].data_ptr()), vp(X[k].data_ptr()), n,
+                          ctypes.byref(info), s)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    GB = torch.empty_like(GX)
+    GA = torch.empty_like(LU)
+
+    def step():
+        rc = L.gb300_dgesv_adjoint_batched_dev(batch, n, nrhs, vp(LU.data_ptr()), n * n, vp(ip.data_ptr()), n,
+                                               vp(X.data_ptr()), n * nrhs, vp(GX.data_ptr()), n * nrhs,
+                                               vp(GB.data_ptr()), n * nrhs, vp(GA.data_ptr()), n * n, s)
+        if rc:
+            raise RuntimeError(f"adjoint status {rc}")
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    L.gb300_prof_reset()
+    L.gb300_prof_enable(1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    L.gb300_prof_enable(0)
+    ms = e0.elapsed_time(e1) / args.steps
+    parts = {}
+    for k, nm in enumerate(["gemm_f64", "gemm_f32_ffma", "gemm_bf16x3", "panel", "laswp", "trsm", "trsv",
+                            "residual_f64", "rank_update_gA"]):
+        t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
+        if cnt.value:
+            parts[nm] = {"ms_per_step": t_ms.value / args.steps, "gbs": by.value / max(t_ms.value, 1e-9) / 1e6}
+    L.gb300_prof_reset()
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_ = batch * (8.0 * n * n * 2 + 8.0 * n * nrhs * 4)     # LU read by the solves + gA written + vectors
+    return {"metric": "adjoint of X = A^{-1}B: 64 systems n=2048 nrhs=8 (gB by transposed solve, gA = -gB X^T)",
+            "value": ms * 1e-3, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "adjoint batch 64 x n=2048 x nrhs=8, factors resident", "forward_s": t_fwd},
+            "kernels": parts, "algorithmic_bytes": bytes_, "hbm_gbs": bytes_ / ms / 1e6,
+            "frac_of_hbm": bytes_ / ms / 1e6 / hbm}
+
+
 def main():
     args = parse()
     if args.workload == "batched" and args.impl == "gb300":
         print(json.dumps(run_batched(args)))
+        return
+    if args.workload == "adjoint" and args.impl == "gb300":
+        print(json.dumps(run_adjoint(args)))
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
