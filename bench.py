@@ -36,6 +36,16 @@ sys.path.insert(0, ROOT)
 METRIC = "n=32768 DGESV time-to-solution: mixed-prec+IR vs FP64 GPU at FP64 backward err"
 EPS = 2.0 ** -53
 
+# DRAM bytes (read + write) of one launch, as a fraction of the launch's
+# algorithmic bytes, from one ncu capture of the same kernel on a smaller
+# case (profiles/gemm_bf16x3_trailing_update_n8192.md: M = N = 7936, K = 256,
+# 459.5 MB measured against 520.1 MB algorithmic).  The traffic grows with
+# M*N like the algorithmic bytes, so the ratio carries to n = 32768.
+TRAFFIC_RATIO = {
+    "gemm_bf16x3": (459.5 / 520.1, "ncu dram__bytes_read.sum + dram__bytes_write.sum of gemm_bf16x3_kernel at "
+                                   "M=N=7936 K=256, scaled by algorithmic bytes"),
+}
+
 
 def parse():
     p = argparse.ArgumentParser()
@@ -257,11 +267,28 @@ def run_gpu(args, rank, world):
         nm, d = dom
         per_launch_ms = d["ms_per_step"] / d["launches_per_step"]
         if nm == "gemm_bf16x3":
-            peak = float(peaks.get("bf16_tflops", 1900.0))
-            achieved = 3.0 * d["flops"] / (d["ms_per_step"] * 1e-3) / 1e12
-            roof = {"bound": "tensor", "kernel": nm, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                    "frac": achieved / peak, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured",
-                    "work": "3 BF16 products x 2*M*N*K per launch"}
+            # C -= A B with K = 256: 3 BF16 products (6K flop) per 8 bytes of
+            # C read+written, 192 flop/B, below the BF16/HBM ridge (~286
+            # flop/B), so the update is HBM-bound; the tensor fraction is
+            # reported beside it.
+            tpeak = float(peaks.get("bf16_tflops", 1900.0))
+            hbm = float(peaks.get("hbm_gbs", 6800.0))
+            secs = d["ms_per_step"] * 1e-3
+            tens = 3.0 * d["flops"] / secs / 1e12
+            intensity = 3.0 * d["flops"] / d["bytes"]
+            ridge = tpeak * 1e12 / (hbm * 1e9)
+            if intensity < ridge:
+                achieved = d["bytes"] / secs / 1e9
+                roof = {"bound": "hbm", "kernel": nm, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                        "frac": achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured"}
+            else:
+                achieved = tens
+                roof = {"bound": "tensor", "kernel": nm, "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
+                        "frac": achieved / tpeak, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
+            roof.update({"work": "per trailing update: 4*(M*K + K*N + 2*M*N) bytes (fp32 A, B read; C read "
+                                 "and written), 3 BF16 products x 2*M*N*K flop",
+                         "intensity_flop_per_byte": intensity, "ridge_flop_per_byte": ridge,
+                         "tensor_tflops": tens, "tensor_frac": tens / tpeak})
         elif nm in ("gemm_f32_ffma", "gemm_f64", "panel", "trsm", "residual_f64"):
             peak = ffma_peak if nm != "gemm_f64" and nm != "residual_f64" else dfma_peak
             achieved = d["flops"] / (d["ms_per_step"] * 1e-3) / 1e12 if d["flops"] else 0.0
@@ -275,6 +302,11 @@ def run_gpu(args, rank, world):
                     "frac": achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured"}
         roof["per_launch_ms"] = per_launch_ms
         roof["traffic"] = None
+        if nm in TRAFFIC_RATIO and d["bytes"]:
+            ratio, src = TRAFFIC_RATIO[nm]
+            roof["traffic"] = ratio * d["bytes"] / d["launches_per_step"]
+            roof["traffic_unit"] = "bytes per launch"
+            roof["traffic_source"] = src
 
     result = {
         "metric": METRIC, "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps,
