@@ -210,12 +210,41 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         solve()
     torch.cuda.synchronize()
+
+    # one more untimed step with every kernel class bracketed by events: the
+    # per-class breakdown and the dominant class
+    names = ["gemm_f64", "gemm_f32_ffma", "gemm_bf16x3", "panel", "laswp", "trsm", "trsv", "residual_f64", "other"]
+    L.gb300_prof_mask.restype = ctypes.c_uint
+    L.gb300_prof_mask.argtypes = [ctypes.c_uint]
+
+    def read_prof(steps):
+        out = {}
+        for k, nm in enumerate(names):
+            t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+            L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
+            if cnt.value:
+                out[nm] = {"ms_per_step": t_ms.value / steps, "launches_per_step": cnt.value / steps,
+                           "flops": fl.value / steps, "bytes": by.value / steps}
+        return out
+
+    L.gb300_prof_reset()
+    L.gb300_prof_mask(0xFFFFFFFF)
+    L.gb300_prof_enable(1)
+    solve()
+    torch.cuda.synchronize()
+    L.gb300_prof_enable(0)
+    breakdown = read_prof(1)
+    L.gb300_prof_reset()
+    dom_name = max(breakdown, key=lambda k: breakdown[k]["ms_per_step"]) if breakdown else None
+
     if world > 1:
         torch.distributed.barrier()
     clocks = ClockSampler(dev.index)
     clocks.start()
-    L.gb300_prof_reset()
-    L.gb300_prof_enable(1)
+    # inside the timed region only the dominant class carries events
+    if dom_name is not None:
+        L.gb300_prof_mask(1 << names.index(dom_name))
+        L.gb300_prof_enable(1)
     launches0 = L.gb300_launch_count()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -236,16 +265,10 @@ def run_gpu(args, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = t.item()
 
-    # per-kernel-class event times recorded inside the timed region
-    names = ["gemm_f64", "gemm_f32_ffma", "gemm_bf16x3", "panel", "laswp", "trsm", "trsv", "residual_f64", "other"]
-    breakdown = {}
-    for k, nm in enumerate(names):
-        t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
-        L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
-        if cnt.value:
-            breakdown[nm] = {"ms_per_step": t_ms.value / args.steps, "launches_per_step": cnt.value / args.steps,
-                             "flops": fl.value / args.steps, "bytes": by.value / args.steps}
+    # the dominant class's event times recorded inside the timed region
+    timed = read_prof(args.steps)
     L.gb300_prof_reset()
+    L.gb300_prof_mask(0xFFFFFFFF)
 
     # accuracy of the last solve
     bwd, scaled = backward_errors(A, X, B, n)
@@ -261,7 +284,7 @@ def run_gpu(args, rank, world):
     ffma_peak = L.gb300_probe_peak(1)
 
     # dominant kernel of the step and its roofline
-    dom = max(breakdown.items(), key=lambda kv: kv[1]["ms_per_step"]) if breakdown else (None, None)
+    dom = (dom_name, timed.get(dom_name, breakdown.get(dom_name))) if dom_name else (None, None)
     roof = None
     if dom[0] is not None:
         nm, d = dom
@@ -319,7 +342,8 @@ def run_gpu(args, rank, world):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "l2": "inputs 8.6 GB >> 129 MB L2; no flush needed",
                    "mixed_mode": "bf16x3" if g.get_option("mixed") == 0 else "fp32-ffma",
-                   "nb32": g.get_option("nb32"), "nb64": g.get_option("nb64")},
+                   "nb32": g.get_option("nb32"), "nb64": g.get_option("nb64"),
+                   "lookahead": g.get_option("lookahead")},
         "iter": iters[-1], "backward_error_dget08": bwd, "scaled_residual": scaled, "forward_error": fwd,
         "kernel_ms_per_step": {k: v["ms_per_step"] for k, v in breakdown.items()},
         "roofline": roof, "gpu_launches": launches,

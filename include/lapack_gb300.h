@@ -242,9 +242,14 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
 /* Options: "exact" (0/1: products rounded separately, bitwise the
  * reference's operation order), "nb64" / "nb32" (outer block sizes),
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32
- * factorization), "sgetrf" (same choice for SGETRF itself).  Returns the
- * previous value, or -1 for an unknown name.  Not thread-safe: set at
- * start-up. */
+ * factorization), "sgetrf" (same choice for SGETRF itself),
+ * "panel_ctas64" / "panel_ctas32" (CTAs of the grid-wide panel kernel, 0:
+ * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 2
+ * shared-memory kernel, 1 register kernel, 0 off), "lookahead" (1: the
+ * FP32 factorization factors block column k+1 on a second, high-priority
+ * stream while the trailing update of block column k runs; 0: one stream).
+ * Returns the previous value, or -1 for an unknown name.  Not thread-safe:
+ * set at start-up. */
 int gb300_set_option(const char* name, int value);
 int gb300_get_option(const char* name);
 /* Reads (and with clear=1 resets) the device status word that kernels with
@@ -263,9 +268,13 @@ const char* gb300_version(void);
  * its own stream; gb300_prof_read sums, for one class (0 FP64 update, 1
  * FP32 update, 2 BF16x3 update, 3 panel, 4 row interchanges, 5 TRSM, 6
  * triangular solves, 7 FP64 residual, 8 other), the event time in ms, the
- * algorithmic flops and bytes, and the launch count. */
+ * algorithmic flops and bytes, and the launch count.  gb300_prof_mask
+ * limits the bracketed classes to the bits set in mask (bit k = class k;
+ * default all), so that a timed run can carry events around one class only;
+ * returns the previous mask. */
 long long gb300_launch_count(void);
 int gb300_prof_enable(int on);
+unsigned gb300_prof_mask(unsigned mask);
 void gb300_prof_reset(void);
 int gb300_prof_read(int kind, double* ms, double* flops, double* bytes, long long* launches);
 /* Measured FMA throughput of the current GPU in TFLOP/s (0: FP64, 1: FP32). */

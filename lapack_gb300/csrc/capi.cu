@@ -515,6 +515,7 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "panel_ctas64")) { old = o.panel_ctas_f64; o.panel_ctas_f64 = value; }
   else if (!strcmp(name, "panel_ctas32")) { old = o.panel_ctas_f32; o.panel_ctas_f32 = value; }
   else if (!strcmp(name, "cluster_panel")) { old = o.cluster_panel; o.cluster_panel = value; }
+  else if (!strcmp(name, "lookahead")) { old = o.lookahead; o.lookahead = value; }
   else return -1;
   return old;
 }
@@ -528,6 +529,7 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "panel_ctas64")) return o.panel_ctas_f64;
   if (!strcmp(name, "panel_ctas32")) return o.panel_ctas_f32;
   if (!strcmp(name, "cluster_panel")) return o.cluster_panel;
+  if (!strcmp(name, "lookahead")) return o.lookahead;
   return -1;
 }
 int gb300_status(int clear) {

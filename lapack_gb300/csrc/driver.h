@@ -20,6 +20,7 @@ struct Options {
   int panel_ctas_f64 = 0;         // CTAs of the cooperative panel (0: all SMs)
   int panel_ctas_f32 = 0;
   int cluster_panel = 2;          // FP32 leaves on one thread-block cluster: 2 shared-memory kernel, 1 register kernel, 0 off
+  int lookahead = 1;              // FP32 cluster path: factor the next block column beside the trailing update
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 

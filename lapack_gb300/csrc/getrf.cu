@@ -34,6 +34,7 @@ Options& options() {
     x.panel_ctas_f64 = env_int("LAPACK_GB300_PANEL_CTAS64", 0);
     x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
     x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
+    x.lookahead = env_int("LAPACK_GB300_LOOKAHEAD", 1);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -86,6 +87,10 @@ int* device_status_word() {
     if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
       uint64_t thr = UINT64_MAX;
       cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      // scratch freed on one stream is not reused on another by inserting a
+      // wait between the two (the look-ahead streams must stay independent)
+      int no = 0;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no);
     }
     words[dev] = p;
   }
@@ -180,6 +185,15 @@ struct PanelCtx {
   int max_optin;
   size_t words_bytes;    // candidate words + pair count, zeroed before each leaf
   int* perm = nullptr;    // optional running row permutation (gather index), updated with every leaf
+  // Look-ahead: each leaf writes its pair list into the next slot of the
+  // block column's log and applies it at once only to the columns
+  // [imm_lo, imm_hi) (the block column); the rest is replayed later.
+  bool logging = false;
+  int imm_lo = 0, imm_hi = 0;
+  int* log_dst = nullptr;
+  int* log_src = nullptr;
+  int* log_cnt = nullptr;   // [kMaxLogSlots], zeroed before the block column
+  PairLogArgs log{};
 };
 
 template <typename T, bool EXACT>
@@ -225,15 +239,38 @@ static int launch_leaf(T* P, int lda, int M, int JB, int row0, int* ipiv, int* i
   return rc;
 }
 
+// A leaf's interchanges on the columns [lo, c0) and [c1, hi).
 template <typename T>
-static int laswp_pairs(T* A, int lda, int ncols, int c0, int c1, int ntop, PanelCtx<T>& cx, cudaStream_t s) {
-  int warps = c0 + (ncols - c1) + (cx.perm ? 1 : 0);
+static int laswp_pairs(T* A, int lda, int lo, int hi, int c0, int c1, int ntop, PanelCtx<T>& cx, cudaStream_t s,
+                       int* perm) {
+  T* Ab = A + (size_t)lo * lda;
+  const int ncols = hi - lo;
+  c0 -= lo;
+  c1 -= lo;
+  int warps = c0 + (ncols - c1) + (perm ? 1 : 0);
   if (warps <= 0) return 0;
   int blocks = (warps * 32 + 255) / 256;
   prof_begin(kProfLaswp, s);
-  GB_LAUNCH(laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(A, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
-                                                cx.ps.pair_count, ntop, cx.perm));
+  GB_LAUNCH(laswp_pairs_kernel<T><<<blocks, 256, 0, s>>>(Ab, lda, ncols, c0, c1, cx.ps.pair_dst, cx.ps.pair_src,
+                                                cx.ps.pair_count, ntop, perm));
   prof_end(kProfLaswp, s, 0.0, 2.0 * sizeof(T) * 2.0 * ntop * warps);
+  return (int)cudaGetLastError();
+}
+
+// A block column's logged interchanges on the columns [a0, a1) and [b0, b1).
+template <typename T>
+static int laswp_log(T* A, int lda, int a0, int a1, int b0, int b1, const PanelCtx<T>& cx, int* perm,
+                     cudaStream_t s) {
+  a1 = std::max(a0, a1);
+  b1 = std::max(b0, b1);
+  const int warps = (a1 - a0) + (b1 - b0) + (perm ? 1 : 0);
+  if (warps <= 0 || cx.log.nslots == 0) return 0;
+  int rows = 0;
+  for (int q = 0; q < cx.log.nslots; ++q) rows += 2 * cx.log.ntop[q];
+  prof_begin(kProfLaswp, s);
+  GB_LAUNCH(laswp_log_kernel<T><<<(warps * 32 + 255) / 256, 256, 0, s>>>(A, lda, a0, a1, b0, b1, cx.log_dst,
+                                                                        cx.log_src, cx.log_cnt, cx.log, perm));
+  prof_end(kProfLaswp, s, 0.0, 2.0 * sizeof(T) * (double)rows * warps);
   return (int)cudaGetLastError();
 }
 
@@ -378,6 +415,15 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
   if (w <= leaf) {
     T* P = A + c0 + (size_t)c0 * lda;
     int rc;
+    if (cx.logging) {
+      const int sl = cx.log.nslots;
+      if (sl >= kMaxLogSlots) return 1000 + kStatusCapacity;
+      cx.ps.pair_dst = cx.log_dst + (size_t)sl * 2 * kLeafMax;
+      cx.ps.pair_src = cx.log_src + (size_t)sl * 2 * kLeafMax;
+      cx.ps.pair_count = cx.log_cnt + sl;
+      cx.log.ntop[sl] = w;
+      cx.log.nslots = sl + 1;
+    }
     if constexpr (sizeof(T) == 4) {
       const bool ex = options().exact;
       if (ckind == 1 && clw == 32)
@@ -397,7 +443,8 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
                            : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
     }
     if (rc) return rc;
-    return laswp_pairs<T>(A, lda, n, c0, c0 + w, w, cx, s);
+    if (cx.logging) return laswp_pairs<T>(A, lda, cx.imm_lo, cx.imm_hi, c0, c0 + w, w, cx, s, nullptr);
+    return laswp_pairs<T>(A, lda, 0, n, c0, c0 + w, w, cx, s, cx.perm);
   }
   int n1 = ((w / 2) + 7) / 8 * 8;
   if (n1 >= w) n1 = w / 2;
@@ -410,6 +457,48 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
                           A11 + n1 + (size_t)n1 * lda, lda, s, gemm_mode);
   if (rc) return rc;
   return getrf_rec<T>(A, lda, m, n, c0 + n1, w - n1, ipiv, info, cx, s, gemm_mode);
+}
+
+// Leaves the recursion of getrf_rec makes for the block column [c0, c0+w).
+template <typename T>
+static int count_leaves(int m, int c0, int w) {
+  int ckind = 0;
+  const int clw = cluster_leaf_width<T>(m - c0, &ckind);
+  const int leaf = clw ? clw : kLeafMax;
+  if (w <= leaf) return 1;
+  int n1 = ((w / 2) + 7) / 8 * 8;
+  if (n1 >= w) n1 = w / 2;
+  return count_leaves<T>(m, c0, n1) + count_leaves<T>(m, c0 + n1, w - n1);
+}
+
+// Per-device second stream (highest priority) and events of the look-ahead
+// schedule.  The mutex is held while one factorization queues its work.
+struct LookaheadRes {
+  std::mutex mu;
+  bool ok = false, tried = false;
+  cudaStream_t sp = nullptr;
+  cudaEvent_t fork = nullptr, P[2] = {nullptr, nullptr}, L[2] = {nullptr, nullptr};
+};
+
+static LookaheadRes* lookahead_res() {
+  static LookaheadRes res[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  LookaheadRes& r = res[dev];
+  std::lock_guard<std::mutex> lk(r.mu);
+  if (!r.tried) {
+    r.tried = true;
+    int lo = 0, hi = 0;
+    bool ok = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&r.sp, cudaStreamNonBlocking, hi) == cudaSuccess;
+    const unsigned fl = cudaEventDisableTiming;
+    ok = ok && cudaEventCreateWithFlags(&r.fork, fl) == cudaSuccess;
+    for (int i = 0; i < 2 && ok; ++i)
+      ok = cudaEventCreateWithFlags(&r.P[i], fl) == cudaSuccess && cudaEventCreateWithFlags(&r.L[i], fl) == cudaSuccess;
+    r.ok = ok;
+    cudaGetLastError();
+  }
+  return r.ok ? &r : nullptr;
 }
 
 static __global__ void iota_kernel(int* p, int n) {
@@ -439,6 +528,10 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   size_t o_rkl = carve(sizeof(int) * 2);
   size_t o_pd = carve(sizeof(int) * 2 * kLeafMax);
   size_t o_psrc = carve(sizeof(int) * 2 * kLeafMax);
+  // look-ahead: two block-column logs (pair lists of up to kMaxLogSlots leaves)
+  const size_t log_ints = (size_t)kMaxLogSlots * 2 * kLeafMax;
+  size_t o_log = carve(sizeof(int) * 4 * log_ints);
+  size_t o_lcnt = carve(sizeof(int) * 2 * kMaxLogSlots);
   DevScratch ws(bytes, s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
   char* base = ws.as<char>();
@@ -460,6 +553,73 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
 
   const int mn = std::min(m, n);
   if (nb < 1) nb = 1;
+
+  // Look-ahead schedule (FP32 cluster leaves, two or more block columns):
+  // block column k is factored on the second stream sp while the user
+  // stream s finishes the trailing update of block column k-1; s then
+  // applies column k's interchanges, forms U and updates the next block
+  // column first (event L), so that sp can start on it, and the rest of
+  // the trailing matrix after.  The work per element and its order are
+  // those of the one-stream loop below.
+  bool la = sizeof(T) == 4 && options().lookahead != 0 && mn > nb;
+  if (la) {
+    int ck = 0;
+    la = cluster_leaf_width<T>(m, &ck) != 0;
+    for (int j = 0; la && j < mn; j += nb)
+      la = count_leaves<T>(m, j, std::min(nb, mn - j)) <= kMaxLogSlots;
+  }
+  LookaheadRes* lr = la ? lookahead_res() : nullptr;
+  if (lr) {
+    std::lock_guard<std::mutex> lk(lr->mu);
+    cudaStream_t sp = lr->sp;
+    int* logs = reinterpret_cast<int*>(base + o_log);
+    int* lcnt = reinterpret_cast<int*>(base + o_lcnt);
+    GB_CUDA_TRY(cudaEventRecord(lr->fork, s));
+    GB_CUDA_TRY(cudaStreamWaitEvent(sp, lr->fork, 0));
+    int k = 0;
+    for (int j = 0; j < mn; j += nb, ++k) {
+      const int jb = std::min(nb, mn - j);
+      const int b = k & 1;
+      if (k > 0) GB_CUDA_TRY(cudaStreamWaitEvent(sp, lr->L[b ^ 1], 0));
+      cx.logging = true;
+      cx.imm_lo = j;
+      cx.imm_hi = j + jb;
+      cx.log_dst = logs + (size_t)(2 * b) * log_ints;
+      cx.log_src = logs + (size_t)(2 * b + 1) * log_ints;
+      cx.log_cnt = lcnt + b * kMaxLogSlots;
+      cx.log.nslots = 0;
+      GB_CUDA_TRY(cudaMemsetAsync(cx.log_cnt, 0, sizeof(int) * kMaxLogSlots, sp));
+      int rc = getrf_rec<T>(dA, lda, m, n, j, jb, dIpiv, dInfo, cx, sp, gemm_mode);
+      if (rc) return rc;
+      GB_CUDA_TRY(cudaEventRecord(lr->P[b], sp));
+      GB_CUDA_TRY(cudaStreamWaitEvent(s, lr->P[b], 0));
+      const int j2 = j + jb;
+      const int nb2 = j2 < mn ? std::min(nb, mn - j2) : 0;   // next block column
+      T* Ajj = dA + j + (size_t)j * lda;
+      // next block column first
+      if (nb2 > 0) {
+        rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
+        if (!rc) rc = trsm_llnu_dev<T>(jb, nb2, Ajj, lda, Ajj + (size_t)jb * lda, lda, s, gemm_mode);
+        if (!rc && j2 < m)
+          rc = gemm_update_dev<T>(m - j2, nb2, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,
+                                  Ajj + jb + (size_t)jb * lda, lda, s, gemm_mode);
+        if (rc) return rc;
+      }
+      GB_CUDA_TRY(cudaEventRecord(lr->L[b], s));
+      // then the columns left of the block column and the rest of the trailing matrix
+      const int c2 = j2 + nb2;
+      rc = laswp_log<T>(dA, lda, 0, j, c2, n, cx, cx.perm, s);
+      if (!rc && c2 < n) {
+        rc = trsm_llnu_dev<T>(jb, n - c2, Ajj, lda, Ajj + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
+        if (!rc && j2 < m)
+          rc = gemm_update_dev<T>(m - j2, n - c2, jb, Ajj + jb, lda, Ajj + (size_t)(c2 - j) * lda, lda,
+                                  Ajj + jb + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
+      }
+      if (rc) return rc;
+    }
+    return (int)cudaGetLastError();
+  }
+
   for (int j = 0; j < mn; j += nb) {
     const int jb = std::min(nb, mn - j);
     int rc = getrf_rec<T>(dA, lda, m, n, j, jb, dIpiv, dInfo, cx, s, gemm_mode);

@@ -316,6 +316,75 @@ laswp_pairs_kernel(T* __restrict__ A, int lda, int ncols, int c_skip0, int c_ski
   }
 }
 
+// Row interchanges of a whole block column, kept as the ordered list of its
+// leaves' (dst, src) pair lists, replayed later on the columns outside the
+// block column.  This is the DLASWP of SRC/dgetrf.f:193 (columns left of
+// the panel) and SRC/dgetrf.f:199 (columns right of it), deferred so that
+// the next panel can be factored while those columns are still being
+// updated.  Slot s holds ntop[s] + counts[s] pairs at dst/src + s*2*kLeafMax.
+constexpr int kMaxLogSlots = 64;
+
+struct PairLogArgs {
+  int nslots;
+  int ntop[kMaxLogSlots];
+};
+
+// Replays the logged pair lists, in order, on the columns [a0, a1) and
+// [b0, b1) (one warp per column) and, when perm is given, on the running
+// row permutation (one extra warp).
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_log_kernel(T* __restrict__ A, int lda, int a0, int a1, int b0, int b1, const int* __restrict__ log_dst,
+                 const int* __restrict__ log_src, const int* __restrict__ counts, PairLogArgs la,
+                 int* __restrict__ perm) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int na = a1 - a0, nbc = b1 - b0;
+  constexpr int kMaxPer = (2 * kLeafMax + 31) / 32;
+  if (perm && warp == na + nbc) {
+    for (int s = 0; s < la.nslots; ++s) {
+      const int* dst = log_dst + (size_t)s * 2 * kLeafMax;
+      const int* src = log_src + (size_t)s * 2 * kLeafMax;
+      const int np = min(la.ntop[s] + counts[s], 2 * kLeafMax);
+      int v[kMaxPer];
+#pragma unroll
+      for (int q = 0; q < kMaxPer; ++q) {
+        int i = lane + 32 * q;
+        if (i < np) v[q] = perm[src[i]];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < kMaxPer; ++q) {
+        int i = lane + 32 * q;
+        if (i < np) perm[dst[i]] = v[q];
+      }
+      __syncwarp();
+    }
+    return;
+  }
+  if (warp >= na + nbc) return;
+  const int col = warp < na ? a0 + warp : b0 + (warp - na);
+  T* Ac = A + (size_t)col * lda;
+  for (int s = 0; s < la.nslots; ++s) {
+    const int* dst = log_dst + (size_t)s * 2 * kLeafMax;
+    const int* src = log_src + (size_t)s * 2 * kLeafMax;
+    const int np = min(la.ntop[s] + counts[s], 2 * kLeafMax);
+    T v[kMaxPer];
+#pragma unroll
+    for (int q = 0; q < kMaxPer; ++q) {
+      int i = lane + 32 * q;
+      if (i < np) v[q] = Ac[src[i]];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int q = 0; q < kMaxPer; ++q) {
+      int i = lane + 32 * q;
+      if (i < np) Ac[dst[i]] = v[q];
+    }
+    __syncwarp();
+  }
+}
+
 // B := L^{-1} B for a unit lower triangular L (k x k, k <= 64) and B of k
 // rows.  Four lanes per column of B: lane s of a group holds rows s, s+4,
 // s+8, ... of that column in registers; at step kk the lane holding row kk

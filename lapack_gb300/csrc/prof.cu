@@ -11,6 +11,7 @@ namespace gb {
 
 static std::atomic<long long> g_launches{0};
 static bool g_prof = false;
+static unsigned g_mask = ~0u;
 static std::mutex g_mu;
 struct Rec { cudaEvent_t a, b; int kind; double flops, bytes; };
 static std::vector<Rec> g_recs;
@@ -28,7 +29,7 @@ void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool prof_on() { return g_prof; }
 
 void prof_begin(int kind, cudaStream_t s) {
-  if (!g_prof) return;
+  if (!g_prof || !((g_mask >> kind) & 1u)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaEvent_t e = get_event();
   cudaEventRecord(e, s);
@@ -36,7 +37,7 @@ void prof_begin(int kind, cudaStream_t s) {
 }
 
 void prof_end(int kind, cudaStream_t s, double flops, double bytes) {
-  if (!g_prof) return;
+  if (!g_prof || !((g_mask >> kind) & 1u)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaEvent_t e = get_event();
   cudaEventRecord(e, s);
@@ -63,6 +64,12 @@ __global__ void probe_fma_kernel(T* out, int iters, T a, T b) {
 extern "C" {
 
 long long gb300_launch_count(void) { return gb::g_launches.load(); }
+
+unsigned gb300_prof_mask(unsigned mask) {
+  unsigned old = gb::g_mask;
+  gb::g_mask = mask;
+  return old;
+}
 
 int gb300_prof_enable(int on) {
   int old = gb::g_prof;
