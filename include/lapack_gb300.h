@@ -247,7 +247,9 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 2
  * shared-memory kernel, 1 register kernel, 0 off), "lookahead" (1: the
  * FP32 factorization factors block column k+1 on a second, high-priority
- * stream while the trailing update of block column k runs; 0: one stream).
+ * stream while the trailing update of block column k runs; 0: one stream),
+ * "trsv_inv" (1: DSGESV's FP32 correction solves apply each 64 x 64
+ * diagonal block as its inverse, formed in the solve; 0: substitution).
  * Returns the previous value, or -1 for an unknown name.  Not thread-safe:
  * set at start-up. */
 int gb300_set_option(const char* name, int value);

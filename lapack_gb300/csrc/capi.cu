@@ -516,6 +516,7 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "panel_ctas32")) { old = o.panel_ctas_f32; o.panel_ctas_f32 = value; }
   else if (!strcmp(name, "cluster_panel")) { old = o.cluster_panel; o.cluster_panel = value; }
   else if (!strcmp(name, "lookahead")) { old = o.lookahead; o.lookahead = value; }
+  else if (!strcmp(name, "trsv_inv")) { old = o.trsv_inv; o.trsv_inv = value; }
   else return -1;
   return old;
 }
@@ -530,6 +531,7 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "panel_ctas32")) return o.panel_ctas_f32;
   if (!strcmp(name, "cluster_panel")) return o.cluster_panel;
   if (!strcmp(name, "lookahead")) return o.lookahead;
+  if (!strcmp(name, "trsv_inv")) return o.trsv_inv;
   return -1;
 }
 int gb300_status(int clear) {

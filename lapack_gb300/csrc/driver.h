@@ -21,6 +21,7 @@ struct Options {
   int panel_ctas_f32 = 0;
   int cluster_panel = 2;          // FP32 leaves on one thread-block cluster: 2 shared-memory kernel, 1 register kernel, 0 off
   int lookahead = 1;              // FP32 cluster path: factor the next block column beside the trailing update
+  int trsv_inv = 1;               // DSGESV's FP32 solves: diagonal blocks applied as their inverses
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 
@@ -46,7 +47,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
               int* dPerm = nullptr);
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
-              T* dB, int ldb, cudaStream_t s);
+              T* dB, int ldb, cudaStream_t s, bool inv_diag = false);   // inv_diag: diagonal blocks by their inverses
 // Gather permutation of a factorization: position r of P*A holds row perm[r].
 int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s);
 template <typename T>

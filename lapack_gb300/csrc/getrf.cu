@@ -11,6 +11,7 @@
 #include "lu_kernels.cuh"
 #include "panel_cluster.cuh"
 #include "solve_kernels.cuh"
+#include "trsv_stream.cuh"
 
 #include <algorithm>
 #include <cstdlib>
@@ -35,6 +36,7 @@ Options& options() {
     x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
     x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
     x.lookahead = env_int("LAPACK_GB300_LOOKAHEAD", 1);
+    x.trsv_inv = env_int("LAPACK_GB300_TRSV_INV", 1);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -689,16 +691,47 @@ template int laswp_dev<float>(int, float*, int, int, int, const int*, int, int, 
 
 // ------------------------------------------------------------------- GETRS
 template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
-static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s) {
+static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s, bool inv_diag) {
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if constexpr (!EXACT) {
+    // streaming solve: the publication array (sentinel-filled, all bits
+    // set), then the ticket
+    const size_t pub_bytes = ((size_t)n * nrhs * sizeof(T) + 255) / 256 * 256;
+    DevScratch ctl(pub_bytes + 256, s);
+    if (!ctl.p) return (int)cudaErrorMemoryAllocation;
+    T* pub = ctl.as<T>();
+    unsigned* ticket = reinterpret_cast<unsigned*>(ctl.as<char>() + pub_bytes);
+    GB_CUDA_TRY(cudaMemsetAsync(pub, 0xFF, pub_bytes, s));
+    GB_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned), s));
+    // inverted diagonal blocks only for the FP32 solves
+    if constexpr (sizeof(T) != 4) inv_diag = false;
+    static bool set_inv[64] = {false}, set_sub[64] = {false};
+    bool& set = inv_diag ? set_inv[dev] : set_sub[dev];
+    auto kern = trsv_stream_kernel<T, FORWARD, UNIT, TRANS, false>;
+    int smem = ts_smem_bytes<T, false>();
+    if constexpr (sizeof(T) == 4) {
+      if (inv_diag) {
+        kern = trsv_stream_kernel<T, FORWARD, UNIT, TRANS, true>;
+        smem = ts_smem_bytes<T, true>();
+      }
+    }
+    if (!set) {
+      GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      set = true;
+    }
+    prof_begin(kProfTrsv, s);
+    GB_LAUNCH(kern<<<nblk, kTsThreads, smem, s>>>(A, lda, n, X, ldx, nrhs, pub, ticket, device_status_word()));
+    prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
+    return (int)cudaGetLastError();
+  }
   DevScratch ctl(sizeof(int) * (size_t)(nblk + 1), s);
   if (!ctl.p) return (int)cudaErrorMemoryAllocation;
   GB_CUDA_TRY(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (size_t)(nblk + 1), s));
   int* flags = ctl.as<int>();
   unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
   static bool smem_set[64] = {false};
-  int dev = 0;
-  cudaGetDevice(&dev);
   if (!smem_set[dev]) {
     GB_CUDA_TRY((trsv_set_smem<T, EXACT, FORWARD, UNIT, TRANS>()));
     smem_set[dev] = true;
@@ -712,7 +745,7 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
 
 template <typename T, bool EXACT>
 static int getrs_impl(char trans, int n, int nrhs, const T* dA, int lda, const int* dPerm, T* dB, int ldb,
-                      cudaStream_t s) {
+                      cudaStream_t s, bool inv) {
   DevScratch w(sizeof(T) * (size_t)n * nrhs, s);
   if (!w.p) return (int)cudaErrorMemoryAllocation;
   T* W = w.as<T>();
@@ -721,13 +754,13 @@ static int getrs_impl(char trans, int n, int nrhs, const T* dA, int lda, const i
   int rc;
   if (trans == 'N') {
     GB_LAUNCH(perm_rows_kernel<T, false><<<blocks, 256, 0, s>>>(dB, ldb, W, n, dPerm, 0, n, nrhs));
-    if ((rc = launch_trsv<T, EXACT, true, true, false>(dA, lda, n, W, n, nrhs, s))) return rc;
-    if ((rc = launch_trsv<T, EXACT, false, false, false>(dA, lda, n, W, n, nrhs, s))) return rc;
+    if ((rc = launch_trsv<T, EXACT, true, true, false>(dA, lda, n, W, n, nrhs, s, inv))) return rc;
+    if ((rc = launch_trsv<T, EXACT, false, false, false>(dA, lda, n, W, n, nrhs, s, inv))) return rc;
     GB_LAUNCH(copy_cols_kernel<T><<<blocks, 256, 0, s>>>(W, n, dB, ldb, n, nrhs));
   } else {
     GB_LAUNCH(copy_cols_kernel<T><<<blocks, 256, 0, s>>>(dB, ldb, W, n, n, nrhs));
-    if ((rc = launch_trsv<T, EXACT, true, false, true>(dA, lda, n, W, n, nrhs, s))) return rc;
-    if ((rc = launch_trsv<T, EXACT, false, true, true>(dA, lda, n, W, n, nrhs, s))) return rc;
+    if ((rc = launch_trsv<T, EXACT, true, false, true>(dA, lda, n, W, n, nrhs, s, inv))) return rc;
+    if ((rc = launch_trsv<T, EXACT, false, true, true>(dA, lda, n, W, n, nrhs, s, inv))) return rc;
     GB_LAUNCH(perm_rows_kernel<T, true><<<blocks, 256, 0, s>>>(W, n, dB, ldb, dPerm, 0, n, nrhs));
   }
   return (int)cudaGetLastError();
@@ -735,7 +768,7 @@ static int getrs_impl(char trans, int n, int nrhs, const T* dA, int lda, const i
 
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm, T* dB, int ldb,
-              cudaStream_t s) {
+              cudaStream_t s, bool inv_diag) {
   if (n <= 0 || nrhs <= 0) return 0;
   DevScratch permbuf(dPerm ? 0 : sizeof(int) * (size_t)n, s);
   if (!dPerm) {
@@ -745,10 +778,12 @@ int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpi
     dPerm = permbuf.as<int>();
   }
   char t = (trans == 'n' || trans == 'N') ? 'N' : 'T';
-  return options().exact ? getrs_impl<T, true>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s)
-                         : getrs_impl<T, false>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s);
+  return options().exact ? getrs_impl<T, true>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s, false)
+                         : getrs_impl<T, false>(t, n, nrhs, dA, lda, dPerm, dB, ldb, s, inv_diag);
 }
-template int getrs_dev<double>(char, int, int, const double*, int, const int*, const int*, double*, int, cudaStream_t);
-template int getrs_dev<float>(char, int, int, const float*, int, const int*, const int*, float*, int, cudaStream_t);
+template int getrs_dev<double>(char, int, int, const double*, int, const int*, const int*, double*, int, cudaStream_t,
+                               bool);
+template int getrs_dev<float>(char, int, int, const float*, int, const int*, const int*, float*, int, cudaStream_t,
+                              bool);
 
 }  // namespace gb

@@ -196,7 +196,7 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[2] != 0) { *iter = -3; goto fallback; }
   // SX = SA^{-1} SX, X = SLAG2D(SX), R = B - A X
-  if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
+  if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s, opt.trsv_inv != 0))) return rc;
   GB_LAUNCH(slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
   if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
   GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
@@ -206,7 +206,7 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   for (int it = 1; it <= itermax; ++it) {
     GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2, s));
     GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(R, n, SX, n, n, nrhs, flags));
-    if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s))) return rc;
+    if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s, opt.trsv_inv != 0))) return rc;
     GB_LAUNCH(lag2d_axpy_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
     if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
     GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
