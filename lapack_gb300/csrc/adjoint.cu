@@ -20,7 +20,10 @@ constexpr int kAdjMaxRhs = 16;
 template <bool EXACT>
 __global__ void __launch_bounds__(256)
 rank_update_neg_kernel(int n, int nrhs, const double* __restrict__ GB, int ldgb, const double* __restrict__ X, int ldx,
-                       double* __restrict__ GA, int ldga) {
+                       double* __restrict__ GA, int ldga, long long sgb = 0, long long sx = 0, long long sga = 0) {
+  GB += blockIdx.z * sgb;     // system of a batch
+  X += blockIdx.z * sx;
+  GA += blockIdx.z * sga;
   __shared__ double gbs[kAdjMaxRhs][kAdjRows];
   __shared__ double xs[kAdjMaxRhs][kAdjCols];
   const int i0 = blockIdx.x * kAdjRows, j0 = blockIdx.y * kAdjCols;
@@ -46,7 +49,106 @@ rank_update_neg_kernel(int n, int nrhs, const double* __restrict__ GB, int ldgb,
   }
 }
 
+// Batched preparation of the transposed solve: each CTA replays its
+// system's IPIV (staged in shared memory first) into the row permutation,
+// and copies its gX into the contiguous work array.
+__global__ void __launch_bounds__(1024)
+adj_prep_kernel(int n, int nrhs, const int* __restrict__ ipiv, long long sip, const double* __restrict__ GX,
+                long long sgx, double* __restrict__ W, int* __restrict__ perm, int* __restrict__ status) {
+  extern __shared__ int adj_sh[];
+  int* lab = adj_sh;           // [n]
+  int* piv = adj_sh + n;       // [n]
+  const int b = blockIdx.x;
+  ipiv += b * sip;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    lab[i] = i;
+    piv[i] = ipiv[i];
+  }
+  const double* gx = GX + b * sgx;
+  double* w = W + (size_t)b * n * nrhs;
+  for (size_t e = threadIdx.x; e < (size_t)n * nrhs; e += blockDim.x) w[e] = gx[e];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < n; ++i) {
+      const int p = piv[i] - 1;
+      if (p < 0 || p >= n) {
+        atomicCAS(status, kStatusOk, kStatusCapacity);
+        continue;
+      }
+      if (p != i) { const int t = lab[i]; lab[i] = lab[p]; lab[p] = t; }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[(size_t)b * n + i] = lab[i];
+}
+
+// gB(perm[r], :) = W(r, :) for every system: x = P^T w.
+__global__ void adj_scatter_kernel(int n, int nrhs, int batch, const double* __restrict__ W, const int* __restrict__ perm,
+                                   double* __restrict__ GB, long long sgb) {
+  const size_t per = (size_t)n * nrhs;
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= per * batch) return;
+  const int b = (int)(e / per);
+  const size_t k = e - (size_t)b * per;
+  const int q = (int)(k / n), r = (int)(k - (size_t)q * n);
+  GB[b * sgb + perm[(size_t)b * n + r] + (size_t)q * n] = W[e];
+}
+
 }  // namespace
+
+// Uniform-size batch with every matrix and vector of leading dimension n:
+// one preparation launch, two batched transposed solves (all systems'
+// block chains in flight together), one scatter, one rank update.
+int adjoint_batched_dev(int batch, int n, int nrhs, const double* dLU, long long slu, const int* dIpiv, long long sip,
+                        const double* dX, long long sx, const double* dGX, long long sgx, double* dGB, long long sgb,
+                        double* dGA, long long sga, cudaStream_t s) {
+  if (batch <= 0 || n <= 0 || nrhs <= 0) return 0;
+  if (nrhs > kAdjMaxRhs) return (int)cudaErrorInvalidValue;
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const size_t smem = 2 * sizeof(int) * (size_t)n;
+  int* status = device_status_word();
+  if (!status) return (int)cudaErrorMemoryAllocation;
+  if ((long long)smem > optin) {
+    // IPIV of a system too long for one CTA's shared memory: system by system
+    for (int b = 0; b < batch; ++b) {
+      int rc = adjoint_dev(n, nrhs, dLU + b * slu, n, dIpiv + b * sip, dX + b * sx, n, dGX + b * sgx, n, dGB + b * sgb,
+                           n, dGA ? dGA + b * sga : nullptr, n, s);
+      if (rc) return rc;
+    }
+    return 0;
+  }
+  static bool attr[64] = {false};
+  if (!attr[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(adj_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    attr[dev] = true;
+  }
+  const size_t per = (size_t)n * nrhs;
+  DevScratch ws(sizeof(double) * per * batch + sizeof(int) * (size_t)n * batch, s);
+  if (!ws.p) return (int)cudaErrorMemoryAllocation;
+  double* W = ws.as<double>();
+  int* perm = reinterpret_cast<int*>(W + per * batch);
+  prof_begin(kProfOther, s);
+  GB_LAUNCH(adj_prep_kernel<<<batch, 1024, smem, s>>>(n, nrhs, dIpiv, sip, dGX, sgx, W, perm, status));
+  prof_end(kProfOther, s, 0.0, (double)batch * (8.0 * 2.0 * per + 8.0 * n));
+  // U^T w = gX, then L^T w = w
+  int rc = trsv_batched_dev<double>(false, true, n, nrhs, dLU, n, slu, W, n, (long long)per, batch, s);
+  if (!rc) rc = trsv_batched_dev<double>(true, true, n, nrhs, dLU, n, slu, W, n, (long long)per, batch, s);
+  if (rc) return rc;
+  const size_t tot = per * batch;
+  GB_LAUNCH(adj_scatter_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, nrhs, batch, W, perm, dGB, sgb));
+  if (dGA) {
+    dim3 grid((n + kAdjRows - 1) / kAdjRows, (n + kAdjCols - 1) / kAdjCols, batch);
+    prof_begin(kProfOther, s);
+    if (options().exact)
+      GB_LAUNCH(rank_update_neg_kernel<true><<<grid, 256, 0, s>>>(n, nrhs, dGB, n, dX, n, dGA, n, sgb, sx, sga));
+    else
+      GB_LAUNCH(rank_update_neg_kernel<false><<<grid, 256, 0, s>>>(n, nrhs, dGB, n, dX, n, dGA, n, sgb, sx, sga));
+    prof_end(kProfOther, s, 2.0 * batch * n * (double)n * nrhs, 8.0 * batch * ((double)n * n + 2.0 * n * nrhs));
+  }
+  return (int)cudaGetLastError();
+}
 
 int adjoint_dev(int n, int nrhs, const double* dLU, int ldlu, const int* dIpiv, const double* dX, int ldx,
                 const double* dGX, int ldgx, double* dGB, int ldgb, double* dGA, int ldga, cudaStream_t s) {
@@ -98,11 +200,9 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
   if (n < 0) return -2;
   if (nrhs < 0 || nrhs > 16) return -3;
   cudaStream_t s = (cudaStream_t)stream;
-  for (int b = 0; b < batch; ++b) {
-    int rc = gb::adjoint_dev(n, nrhs, dLU + b * stride_lu, n, dIpiv + b * stride_ipiv, dX + b * stride_x, n,
-                             dGX + b * stride_gx, n, dGB + b * stride_gb, n, dGA ? dGA + b * stride_ga : nullptr, n, s);
-    if (rc) return rc;
-  }
+  int rc = gb::adjoint_batched_dev(batch, n, nrhs, dLU, stride_lu, dIpiv, stride_ipiv, dX, stride_x, dGX, stride_gx, dGB,
+                                   stride_gb, dGA, stride_ga, s);
+  if (rc) return rc;
   return (int)cudaStreamSynchronize(s);
 }
 

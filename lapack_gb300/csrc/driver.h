@@ -48,6 +48,11 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
               T* dB, int ldb, cudaStream_t s, bool inv_diag = false);   // inv_diag: diagonal blocks by their inverses
+// op(T) X = B for nbatch systems of one size, T the unit lower (lower) or
+// upper triangle of stored LU factors; strides between systems in elements.
+template <typename T>
+int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int lda, long long sA, T* dX, int ldx,
+                     long long sX, int nbatch, cudaStream_t s);
 // Gather permutation of a factorization: position r of P*A holds row perm[r].
 int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s);
 template <typename T>

@@ -691,14 +691,15 @@ template int laswp_dev<float>(int, float*, int, int, int, const int*, int, int, 
 
 // ------------------------------------------------------------------- GETRS
 template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
-static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s, bool inv_diag) {
+static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s, bool inv_diag,
+                       int nbatch = 1, long long sA = 0, long long sX = 0) {
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
   int dev = 0;
   cudaGetDevice(&dev);
   if constexpr (!EXACT) {
     // streaming solve: the publication array (sentinel-filled, all bits
     // set), then the ticket
-    const size_t pub_bytes = ((size_t)n * nrhs * sizeof(T) + 255) / 256 * 256;
+    const size_t pub_bytes = ((size_t)n * nrhs * nbatch * sizeof(T) + 255) / 256 * 256;
     DevScratch ctl(pub_bytes + 256, s);
     if (!ctl.p) return (int)cudaErrorMemoryAllocation;
     T* pub = ctl.as<T>();
@@ -722,9 +723,18 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
       set = true;
     }
     prof_begin(kProfTrsv, s);
-    GB_LAUNCH(kern<<<nblk, kTsThreads, smem, s>>>(A, lda, n, X, ldx, nrhs, pub, ticket, device_status_word()));
-    prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
+    GB_LAUNCH(kern<<<(unsigned)nblk * (unsigned)nbatch, kTsThreads, smem, s>>>(A, lda, n, X, ldx, nrhs, pub, ticket,
+                                                                             device_status_word(), sA, sX));
+    prof_end(kProfTrsv, s, (double)nbatch * n * n * nrhs,
+             (double)nbatch * sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
     return (int)cudaGetLastError();
+  }
+  if (nbatch > 1) {
+    for (int b = 0; b < nbatch; ++b) {
+      int rc = launch_trsv<T, EXACT, FORWARD, UNIT, TRANS>(A + b * sA, lda, n, X + b * sX, ldx, nrhs, s, inv_diag);
+      if (rc) return rc;
+    }
+    return 0;
   }
   DevScratch ctl(sizeof(int) * (size_t)(nblk + 1), s);
   if (!ctl.p) return (int)cudaErrorMemoryAllocation;
@@ -785,5 +795,29 @@ template int getrs_dev<double>(char, int, int, const double*, int, const int*, c
                                bool);
 template int getrs_dev<float>(char, int, int, const float*, int, const int*, const int*, float*, int, cudaStream_t,
                               bool);
+
+// op(T) X = B for a batch of systems of one size (T unit lower L or upper U
+// of stored LU factors), X overwritten in place; strides in elements.
+template <typename T>
+int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int lda, long long sA, T* dX, int ldx,
+                     long long sX, int nbatch, cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0 || nbatch <= 0) return 0;
+  // solve order: forward for L and for U^T, backward for U and for L^T
+  const bool ex = options().exact;
+  if (!trans) {
+    if (lower)
+      return ex ? launch_trsv<T, true, true, true, false>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
+                : launch_trsv<T, false, true, true, false>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
+    return ex ? launch_trsv<T, true, false, false, false>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
+              : launch_trsv<T, false, false, false, false>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
+  }
+  if (lower)
+    return ex ? launch_trsv<T, true, false, true, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
+              : launch_trsv<T, false, false, true, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
+  return ex ? launch_trsv<T, true, true, false, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
+            : launch_trsv<T, false, true, false, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
+}
+template int trsv_batched_dev<double>(bool, bool, int, int, const double*, int, long long, double*, int, long long,
+                                      int, cudaStream_t);
 
 }  // namespace gb

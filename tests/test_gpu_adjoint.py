@@ -135,7 +135,7 @@ def test_adjoint_batch_64x2048(gpu):
                                            vp(X.data_ptr()), n * nrhs, vp(GX.data_ptr()), n * nrhs,
                                            vp(GB.data_ptr()), n * nrhs, vp(GA.data_ptr()), n * n, s)
     assert rc == 0
-    for k in (0, batch - 1):
+    for k in (0, 1, 31, batch - 1):
         lu_h = LU[k].cpu().numpy().T            # column-major view of the packed factors
         ip_h = ip[k].cpu().numpy()
         gx_h = GX[k].cpu().numpy().T
@@ -147,3 +147,40 @@ def test_adjoint_batch_64x2048(gpu):
         # the solve itself: A X = B
         a_h = A0[k].cpu().numpy().T
         assert np.abs(a_h @ X[k].cpu().numpy().T - B0[k].cpu().numpy().T).max() < 1e-10
+
+
+@pytest.mark.parametrize("n,nrhs,batch", [(100, 3, 5), (129, 1, 3), (64, 16, 2)])
+def test_adjoint_batched_ragged_all_systems(gpu, n, nrhs, batch):
+    """Batched adjoint at sizes off the 64-row blocks: every system's gB
+    and gA against the oracle's DGETRS('T') and DGEMM."""
+    import torch
+    rng = np.random.default_rng(n + nrhs)
+    a = rng.standard_normal((batch, n, n)) + 3 * np.eye(n)
+    lus, ips = [], []
+    for k in range(batch):
+        lu, ip, info = oracle.getrf(np.asfortranarray(a[k]))
+        assert info == 0
+        lus.append(lu)
+        ips.append(ip)
+    x = rng.standard_normal((batch, n, nrhs))
+    gx = rng.standard_normal((batch, n, nrhs))
+    # device copies, column-major per system (stored as the transpose of a row-major (cols, rows) array)
+    LU = torch.from_numpy(np.stack([l.T for l in lus])).cuda().contiguous()
+    IP = torch.from_numpy(np.stack(ips).astype(np.int32)).cuda().contiguous()
+    X = torch.from_numpy(np.ascontiguousarray(np.transpose(x, (0, 2, 1)))).cuda()
+    GX = torch.from_numpy(np.ascontiguousarray(np.transpose(gx, (0, 2, 1)))).cuda()
+    GB = torch.empty_like(GX)
+    GA = torch.empty_like(LU)
+    L = gpu.lib()
+    vp = ctypes.c_void_p
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    rc = L.gb300_dgesv_adjoint_batched_dev(batch, n, nrhs, vp(LU.data_ptr()), n * n, vp(IP.data_ptr()), n,
+                                           vp(X.data_ptr()), n * nrhs, vp(GX.data_ptr()), n * nrhs,
+                                           vp(GB.data_ptr()), n * nrhs, vp(GA.data_ptr()), n * n, s)
+    assert rc == 0
+    for k in range(batch):
+        gb_ref, _ = oracle.getrs(lus[k], ips[k], gx[k], "T")
+        gb_gpu = GB[k].cpu().numpy().T
+        assert np.abs(gb_gpu - gb_ref).max() <= np.abs(gb_ref).max() * 1e-11
+        ga_ref = _oracle_dgemm_nt(gb_ref, x[k])
+        assert np.abs(GA[k].cpu().numpy().T - ga_ref).max() <= np.abs(ga_ref).max() * 1e-11
