@@ -346,6 +346,7 @@ def run_gpu(args, rank, world):
                    "lookahead": g.get_option("lookahead")},
         "iter": iters[-1], "backward_error_dget08": bwd, "scaled_residual": scaled, "forward_error": fwd,
         "kernel_ms_per_step": {k: v["ms_per_step"] for k, v in breakdown.items()},
+        "kernel_launches_per_step": {k: v["launches_per_step"] for k, v in breakdown.items()},
         "roofline": roof, "gpu_launches": launches,
         "clocks": clk, "peaks_measured": {"dfma_tflops": dfma_peak, "ffma_tflops": ffma_peak,
                                           "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")},

@@ -453,10 +453,14 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
   int rc = getrf_rec<T>(A, lda, m, n, c0, n1, ipiv, info, cx, s, gemm_mode);
   if (rc) return rc;
   T* A11 = A + c0 + (size_t)c0 * lda;
-  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gemm_mode);
+  // narrow updates inside the panel (64 columns or fewer) run on the FP32
+  // FMA kernel: one launch, no operand split, K <= 64 would be padded to a
+  // full BF16 K block anyway
+  const int gm = (gemm_mode == kMixedBf16x3 && w - n1 <= 64) ? kMixedFp32 : gemm_mode;
+  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gm);
   if (rc) return rc;
   rc = gemm_update_dev<T>(m - c0 - n1, w - n1, n1, A11 + n1, lda, A11 + (size_t)n1 * lda, lda,
-                          A11 + n1 + (size_t)n1 * lda, lda, s, gemm_mode);
+                          A11 + n1 + (size_t)n1 * lda, lda, s, gm);
   if (rc) return rc;
   return getrf_rec<T>(A, lda, m, n, c0 + n1, w - n1, ipiv, info, cx, s, gemm_mode);
 }
