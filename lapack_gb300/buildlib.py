@@ -14,7 +14,7 @@ NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default",
           "--expt-relaxed-constexpr"]
-SOURCES = ["getrf.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "lapacke.cpp"]
+SOURCES = ["getrf.cu", "trsm.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "lapacke.cpp"]
 
 
 def _sources():

@@ -62,11 +62,12 @@ template <typename T>
 int gemm_update_dev(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                     cudaStream_t s, int gemm_mode);
 template <typename T>
-int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode);
+int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode,
+                  bool one_launch = true);   // false: leaf kernel + GEMM only (small shared memory)
 
 // BF16x3 tensor-core update C -= A*B for FP32 operands (tcgen05).
 int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                    cudaStream_t s);
+                    cudaStream_t s, bool overwrite = false);   // overwrite: C = A*B
 
 // DSGESV on device memory.  *iter and *info are host outputs.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,

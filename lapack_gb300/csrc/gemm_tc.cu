@@ -1,6 +1,8 @@
 // Trailing-matrix update of the FP32 factorization on the BF16 tensor cores
 // (tcgen05, sm_103a): C := C - A*B for FP32 column-major A (M x K), B (K x N),
-// C (M x N), the SGEMM('N','N', alpha=-1, beta=1) call of SRC/sgetrf.f, as
+// C (M x N), the SGEMM('N','N', alpha=-1, beta=1) call of SRC/sgetrf.f (or,
+// with overwrite, C := A*B, which may alias B: B is split before C is
+// written), as
 // split-BF16x3 products: with a = ah + al and b = bh + bl (ah = bf16(a),
 // al = bf16(a - ah)), a*b ~ ah*bh + ah*bl + al*bh, the three products
 // accumulated in FP32 in tensor memory.
@@ -127,7 +129,7 @@ __device__ __forceinline__ void load_c_chunk(const float* __restrict__ C, int ld
 __global__ void __launch_bounds__(kTcThreads)
 gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_constant__ CUtensorMap tm_al,
                    const __grid_constant__ CUtensorMap tm_bh, const __grid_constant__ CUtensorMap tm_bl,
-                   float* __restrict__ C, int ldc, int M, int N, int nkb, int* __restrict__ status) {
+                   float* __restrict__ C, int ldc, int M, int N, int nkb, int* __restrict__ status, int overwrite) {
   extern __shared__ unsigned char tc_smem_raw[];
   __shared__ __align__(8) uint64_t bar_load;
   __shared__ __align__(8) uint64_t bar_mma;
@@ -163,7 +165,7 @@ gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_const
   const int m = m0 + warp * 32 + lane;
   // the first C chunk is fetched while the tensor cores work
   float cpre[32];
-  load_c_chunk(C, ldc, M, N, m, n0, cpre);
+  if (!overwrite) load_c_chunk(C, ldc, M, N, m, n0, cpre);
 
   if (tid == 0) {
     const uint32_t idesc = idesc_bf16_f32(kTcBM, kTcBN);
@@ -218,14 +220,14 @@ gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_const
       float cur[32];
 #pragma unroll
       for (int j = 0; j < 32; ++j) cur[j] = nxt[j];
-      if (c0 + 32 < kTcBN) load_c_chunk(C, ldc, M, N, m, n0 + c0 + 32, nxt);
+      if (!overwrite && c0 + 32 < kTcBN) load_c_chunk(C, ldc, M, N, m, n0 + c0 + 32, nxt);
       float v[32];
       tmem_ld_32cols(lane_base + (uint32_t)c0, v);
       if (m < M) {
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
           const int n = n0 + c0 + j;
-          if (n < N) C[(size_t)m + (size_t)n * ldc] = cur[j] - v[j];
+          if (n < N) C[(size_t)m + (size_t)n * ldc] = overwrite ? v[j] : cur[j] - v[j];
         }
       }
     }
@@ -309,7 +311,7 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int box_rows
 
 
 int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                    cudaStream_t s) {
+                    cudaStream_t s, bool overwrite) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   const int Kp = (K + kTcBK - 1) / kTcBK * kTcBK;
   const size_t bytes_a = (size_t)M * Kp * 2, bytes_b = (size_t)N * Kp * 2;
@@ -339,8 +341,9 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
   }
   dim3 grid((M + kTcBM - 1) / kTcBM, (N + kTcBN - 1) / kTcBN);
   GB_LAUNCH(gemm_bf16x3_kernel<<<grid, kTcThreads, kTcSmem, s>>>(m_ah, m_al, m_bh, m_bl, C, ldc, M, N, Kp / kTcBK,
-                                                                 device_status_word()));
-  prof_end(kProfGemmBf16x3, s, 2.0 * M * N * (double)K, 4.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
+                                                                 device_status_word(), overwrite ? 1 : 0));
+  prof_end(kProfGemmBf16x3, s, 2.0 * M * N * (double)K,
+           4.0 * ((double)M * K + (double)K * N + (overwrite ? 1.0 : 2.0) * M * N));
   return (int)cudaGetLastError();
 }
 

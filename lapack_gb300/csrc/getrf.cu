@@ -129,55 +129,6 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
   return (int)cudaGetLastError();
 }
 
-// ------------------------------------------------------------------- TRSM
-template <typename T, bool EXACT, int KMAX>
-static int launch_trsm_leaf_k(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
-  static bool attr[64] = {false};
-  int dev = 0;
-  cudaGetDevice(&dev);
-  if (!attr[dev]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(trsm_llnu_leaf_kernel<T, EXACT, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     trsm_leaf_smem<T, KMAX>()));
-    attr[dev] = true;
-  }
-  GB_LAUNCH(trsm_llnu_leaf_kernel<T, EXACT, KMAX><<<grid, kTrsmThreads, trsm_leaf_smem<T, KMAX>(), s>>>(L, ldl, B, ldb,
-                                                                                                     k, ncols));
-  return 0;
-}
-
-// the unrolled solve is sized to the leaf: 16, 32 or 64 rows
-template <typename T, bool EXACT>
-static int launch_trsm_leaf(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
-  prof_begin(kProfTrsm, s);
-  int rc;
-  if (k <= 16) rc = launch_trsm_leaf_k<T, EXACT, 16>(grid, L, ldl, B, ldb, k, ncols, s);
-  else if (k <= 32) rc = launch_trsm_leaf_k<T, EXACT, 32>(grid, L, ldl, B, ldb, k, ncols, s);
-  else rc = launch_trsm_leaf_k<T, EXACT, 64>(grid, L, ldl, B, ldb, k, ncols, s);
-  return rc;
-}
-
-// B := L^{-1} B, L unit lower k x k: leaves of at most 64 rows, GEMM for the coupling.
-template <typename T>
-int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode) {
-  if (k <= 0 || ncols <= 0) return 0;
-  if (k <= kLeafMax) {
-    int grid = (ncols + kTrsmCols - 1) / kTrsmCols;
-    int rc = options().exact ? launch_trsm_leaf<T, true>(grid, L, ldl, B, ldb, k, ncols, s)
-                             : launch_trsm_leaf<T, false>(grid, L, ldl, B, ldb, k, ncols, s);
-    if (rc) return rc;
-    prof_end(kProfTrsm, s, (double)k * k * ncols, sizeof(T) * ((double)k * k + 2.0 * k * ncols));
-    return (int)cudaGetLastError();
-  }
-  int k1 = ((k / 2) + kLeafMax - 1) / kLeafMax * kLeafMax;
-  if (k1 >= k) k1 = kLeafMax;
-  int rc = trsm_llnu_dev<T>(k1, ncols, L, ldl, B, ldb, s, gemm_mode);
-  if (rc) return rc;
-  rc = gemm_update_dev<T>(k - k1, ncols, k1, L + k1, ldl, B, ldb, B + k1, ldb, s, gemm_mode);
-  if (rc) return rc;
-  return trsm_llnu_dev<T>(k - k1, ncols, L + k1 + (size_t)k1 * ldl, ldl, B + k1, ldb, s, gemm_mode);
-}
-template int trsm_llnu_dev<double>(int, int, const double*, int, double*, int, cudaStream_t, int);
-template int trsm_llnu_dev<float>(int, int, const float*, int, float*, int, cudaStream_t, int);
 
 // ------------------------------------------------------------------ panel
 template <typename T>
@@ -457,7 +408,7 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
   // FMA kernel: one launch, no operand split, K <= 64 would be padded to a
   // full BF16 K block anyway
   const int gm = (gemm_mode == kMixedBf16x3 && w - n1 <= 64) ? kMixedFp32 : gemm_mode;
-  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gm);
+  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gm, false);
   if (rc) return rc;
   rc = gemm_update_dev<T>(m - c0 - n1, w - n1, n1, A11 + n1, lda, A11 + (size_t)n1 * lda, lda,
                           A11 + n1 + (size_t)n1 * lda, lda, s, gm);
@@ -507,6 +458,38 @@ static LookaheadRes* lookahead_res() {
   return r.ok ? &r : nullptr;
 }
 
+// Columns of the trailing block row from which U12 is formed with the
+// inverse of L11 (one BF16x3 product) instead of the substitution.
+constexpr int kInvMinCols = 2048;
+
+template <typename T>
+static __global__ void set_identity_kernel(T* X, int n) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n * n) X[e] = (e % (n + 1) == 0) ? T(1) : T(0);
+}
+
+// U12 = L11^{-1} A12 for the columns [c_beg, c_end) of the block row of
+// block column j (SRC/dgetrf.f:204).  The next block column always uses the
+// substitution; a wider rest of the block row uses the inverse of L11 and
+// one BF16x3 product when linv is given.  Both schedules (look-ahead or
+// not) cut the block row at the same columns, so they compute the same.
+template <typename T>
+static int block_row_u(T* dA, int lda, int j, int jb, int c_beg, int c_end, bool rest, T* linv, cudaStream_t s,
+                       int gemm_mode) {
+  if (c_end <= c_beg) return 0;
+  T* Ajj = dA + j + (size_t)j * lda;
+  T* U = dA + j + (size_t)c_beg * lda;
+  if constexpr (sizeof(T) == 4) {
+    if (rest && linv && c_end - c_beg > kInvMinCols) {
+      GB_LAUNCH(set_identity_kernel<<<(jb * jb + 255) / 256, 256, 0, s>>>(linv, jb));
+      int rc = trsm_llnu_dev<T>(jb, jb, Ajj, lda, linv, jb, s, gemm_mode);
+      if (rc) return rc;
+      return gemm_bf16x3_dev(jb, c_end - c_beg, jb, linv, jb, U, lda, U, lda, s, true);
+    }
+  }
+  return trsm_llnu_dev<T>(jb, c_end - c_beg, Ajj, lda, U, lda, s, gemm_mode);
+}
+
 static __global__ void iota_kernel(int* p, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = i;
@@ -538,6 +521,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   const size_t log_ints = (size_t)kMaxLogSlots * 2 * kLeafMax;
   size_t o_log = carve(sizeof(int) * 4 * log_ints);
   size_t o_lcnt = carve(sizeof(int) * 2 * kMaxLogSlots);
+  size_t o_linv = carve(sizeof(T) * 256 * 256);
   DevScratch ws(bytes, s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
   char* base = ws.as<char>();
@@ -574,6 +558,11 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     for (int j = 0; la && j < mn; j += nb)
       la = count_leaves<T>(m, j, std::min(nb, mn - j)) <= kMaxLogSlots;
   }
+  // inverse of the block column's unit lower triangle (BF16x3 mode only:
+  // the exact and FP32 modes keep the substitution of SRC/dgetrf.f:204)
+  T* linv = (sizeof(T) == 4 && gemm_mode == kMixedBf16x3 && !options().exact && nb <= 256)
+                ? reinterpret_cast<T*>(base + o_linv)
+                : nullptr;
   LookaheadRes* lr = la ? lookahead_res() : nullptr;
   if (lr) {
     std::lock_guard<std::mutex> lk(lr->mu);
@@ -605,7 +594,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       // next block column first
       if (nb2 > 0) {
         rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
-        if (!rc) rc = trsm_llnu_dev<T>(jb, nb2, Ajj, lda, Ajj + (size_t)jb * lda, lda, s, gemm_mode);
+        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, false, linv, s, gemm_mode);
         if (!rc && j2 < m)
           rc = gemm_update_dev<T>(m - j2, nb2, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,
                                   Ajj + jb + (size_t)jb * lda, lda, s, gemm_mode);
@@ -616,7 +605,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       const int c2 = j2 + nb2;
       rc = laswp_log<T>(dA, lda, 0, j, c2, n, cx, cx.perm, s);
       if (!rc && c2 < n) {
-        rc = trsm_llnu_dev<T>(jb, n - c2, Ajj, lda, Ajj + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
+        rc = block_row_u<T>(dA, lda, j, jb, c2, n, true, linv, s, gemm_mode);
         if (!rc && j2 < m)
           rc = gemm_update_dev<T>(m - j2, n - c2, jb, Ajj + jb, lda, Ajj + (size_t)(c2 - j) * lda, lda,
                                   Ajj + jb + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
@@ -632,7 +621,10 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     if (rc) return rc;
     if (j + jb < n) {
       T* Ajj = dA + j + (size_t)j * lda;
-      rc = trsm_llnu_dev<T>(jb, n - j - jb, Ajj, lda, Ajj + (size_t)jb * lda, lda, s, gemm_mode);
+      const int j2 = j + jb;
+      const int c2 = j2 + (j2 < mn ? std::min(nb, mn - j2) : 0);   // next block column, then the rest
+      rc = block_row_u<T>(dA, lda, j, jb, j2, std::min(c2, n), false, linv, s, gemm_mode);
+      if (!rc) rc = block_row_u<T>(dA, lda, j, jb, c2, n, true, linv, s, gemm_mode);
       if (rc) return rc;
       if (j + jb < m) {
         rc = gemm_update_dev<T>(m - j - jb, n - j - jb, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,

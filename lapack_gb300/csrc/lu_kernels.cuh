@@ -452,4 +452,80 @@ trsm_llnu_leaf_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int l
   }
 }
 
+// The same solve for k up to KMAX = 128 or 256 in one launch (the block
+// row of U: k = NB = 256).  The strictly lower triangle of L is kept packed
+// in shared memory (column j's rows j+1.. at tri_off(j); 130 KB for 256
+// FP32 rows), staged with cp.async; LPC lanes share a column, lane s holding
+// rows s, s+LPC, ... in registers; per k the lane holding row k broadcasts
+// it and every lane updates its rows below k, in the reference order
+// (BLAS/SRC/dtrsm.f:296-298).  More lanes per column shorten the chain of
+// the k steps (the look-ahead's 256-column solve); fewer cost less staging
+// per column (the wide solve of the rest of the block row).
+template <int KMAX>
+__host__ __device__ constexpr int tri_off(int j) {
+  return j * (2 * KMAX - j - 1) / 2;
+}
+
+template <typename T, int KMAX, int LPC>
+constexpr int trsm_tri_smem() {
+  return (KMAX * (KMAX - 1) / 2 + KMAX * (kTrsmThreads / LPC + 1)) * (int)sizeof(T);
+}
+
+template <typename T, bool EXACT, int KMAX, int LPC>
+__global__ void __launch_bounds__(kTrsmThreads, 1)
+trsm_llnu_tri_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int ldb, int k, int ncols) {
+  constexpr int RPL = KMAX / LPC;                        // rows per lane
+  constexpr int CPB = kTrsmThreads / LPC;                // columns per CTA
+  constexpr int BLD = CPB + 1;
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  T* Lp = reinterpret_cast<T*>(trsm_smem);
+  T* Bs = Lp + KMAX * (KMAX - 1) / 2;                    // [KMAX][CPB + 1]
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int c0 = blockIdx.x * CPB;
+  const int nc = min(CPB, ncols - c0);
+  for (int j = 0; j < k - 1; ++j) {
+    const int off = tri_off<KMAX>(j);
+    for (int i = j + 1 + tid; i < k; i += kTrsmThreads) cp_async_elem(Lp + off + (i - j - 1), L + (size_t)i + (size_t)j * ldl);
+  }
+  for (int e = tid; e < k * nc; e += kTrsmThreads) {
+    const int c = e / k, r = e - c * k;
+    cp_async_elem(Bs + r * BLD + c, B + (size_t)r + (size_t)(c0 + c) * ldb);
+  }
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  const int col = tid / LPC, sub = tid % LPC;
+  const int gbase = lane & ~(LPC - 1);
+  T x[RPL];
+#pragma unroll
+  for (int t = 0; t < RPL; ++t) {
+    const int i = sub + LPC * t;
+    x[t] = (col < nc && i < k) ? Bs[i * BLD + col] : T(0);
+  }
+#pragma unroll
+  for (int kk = 0; kk < KMAX - 1; ++kk) {
+    if (kk < k - 1) {
+      const T xk = __shfl_sync(0xffffffffu, x[kk / LPC], gbase | (kk % LPC));
+      const T* Lc = Lp + tri_off<KMAX>(kk) - kk - 1;     // Lc[i] = L(i, kk) for i > kk
+#pragma unroll
+      for (int t = kk / LPC; t < RPL; ++t) {
+        const int i = sub + LPC * t;
+        if (i > kk && i < k) x[t] = fnmadd<EXACT>(xk, Lc[i], x[t]);
+      }
+    }
+  }
+  if (col < nc) {
+#pragma unroll
+    for (int t = 0; t < RPL; ++t) {
+      const int i = sub + LPC * t;
+      if (i < k) Bs[i * BLD + col] = x[t];
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < k * nc; e += kTrsmThreads) {
+    const int c = e / k, r = e - c * k;
+    B[(size_t)r + (size_t)(c0 + c) * ldb] = Bs[r * BLD + c];
+  }
+}
+
 }  // namespace gb

@@ -85,17 +85,7 @@ constexpr int kSolveLd = kSolveBS + 1;
 template <typename T>
 constexpr int kTrsvSmem = 2 * kSolveBS * kSolveLd * (int)sizeof(T);   // 33 KB (float) / 66.6 KB (double)
 
-template <typename T>
-__device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-  if constexpr (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
-  else
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 
 template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
 __global__ void __launch_bounds__(256)
