@@ -241,7 +241,7 @@ static ClusterCaps cluster_caps() {
   cudaGetDevice(&dev);
   if (!done[dev]) {
     done[dev] = true;
-    auto kern = leaf_panel_cluster_kernel<EXACT>;
+    auto kern = leaf_panel_cluster_kernel<EXACT, 64>;
     cudaFuncAttributes fa;
     int optin = 0;
     if (cudaFuncGetAttributes(&fa, (const void*)kern) == cudaSuccess &&
@@ -327,14 +327,19 @@ static int launch_leaf_cluster_reg(float* P, int lda, int M, int jb, int row0, i
   return rc;
 }
 
-template <bool EXACT>
-static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
-                               PanelCtx<float>& cx, cudaStream_t s) {
-  ClusterCaps c = cluster_caps<EXACT>();
-  const int R = (M + kClusterCtas - 1) / kClusterCtas;
-  size_t smem = (size_t)JB * R * 4 + (size_t)R * 4 + 16;
-  if (!c.ok || (long long)smem > c.dyn_cap) return 1000 + kStatusCapacity;
-  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
+template <bool EXACT, int JBT>
+static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t smem, int row0, int* ipiv, int* info,
+                                 PanelCtx<float>& cx, cudaStream_t s, int dyn_cap) {
+  static bool attr[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!attr[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(leaf_panel_cluster_kernel<EXACT, JBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     dyn_cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute(leaf_panel_cluster_kernel<EXACT, JBT>,
+                                     cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    attr[dev] = true;
+  }
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -347,9 +352,24 @@ static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* 
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  return (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT, JBT>, P, lda, M, JB, R, row0, ipiv, info,
+                                 cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status);
+}
+
+template <bool EXACT>
+static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
+                               PanelCtx<float>& cx, cudaStream_t s) {
+  ClusterCaps c = cluster_caps<EXACT>();
+  const int R = (M + kClusterCtas - 1) / kClusterCtas;
+  size_t smem = (size_t)JB * R * 4 + (size_t)R * 4 + 16;
+  if (!c.ok || (long long)smem > c.dyn_cap || JB > 64) return 1000 + kStatusCapacity;
+  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
   prof_begin(kProfPanel, s);
-  int rc = (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT>, P, lda, M, JB, R, row0, ipiv, info,
-                                   cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status);
+  int rc;
+  if (JB <= 8) rc = launch_leaf_cluster_w<EXACT, 8>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else if (JB <= 16) rc = launch_leaf_cluster_w<EXACT, 16>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else if (JB <= 32) rc = launch_leaf_cluster_w<EXACT, 32>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else rc = launch_leaf_cluster_w<EXACT, 64>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
   count_launch();
   prof_end(kProfPanel, s, (double)M * JB * JB, 2.0 * 4.0 * (double)M * JB);
   return rc;

@@ -47,7 +47,9 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
-template <bool EXACT>
+// JBT: the leaf-width capacity (8, 16, 32 or 64), so the rank-1 update's
+// column loop is unrolled; JB <= JBT is the actual width.
+template <bool EXACT, int JBT>
 __global__ void __launch_bounds__(kClusterThreads, 1)
 leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, int row0, int* __restrict__ ipiv,
                           int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
@@ -69,12 +71,14 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   const int rbeg = b * R;
   const int nrows = max(0, min(M, rbeg + R) - rbeg);
 
-  if (nrows > 0)
-    batched_copy<8, kClusterThreads, float>(
-        JB * nrows, tid,
-        [&](int e) { const int c = e / nrows, r = e - c * nrows; return P[(size_t)(rbeg + r) + (size_t)c * lda]; },
-        [&](int e, float v) { const int c = e / nrows, r = e - c * nrows; tile[c * R + r] = v; });
+  // stage the CTA's rows: every element an asynchronous copy, all in flight
+  // at once (the panel streams from L2/HBM at the SM's bandwidth)
+  for (int c = 0; c < JB; ++c)
+    for (int r = tid; r < nrows; r += kClusterThreads)
+      cp_async_elem(tile + c * R + r, P + (size_t)(rbeg + r) + (size_t)c * lda);
+  cp_async_commit();
   for (int r = tid; r < nrows; r += kClusterThreads) label[r] = rbeg + r;
+  cp_async_wait<0>();
   __syncthreads();
   // candidates for column 0
   unsigned long long mykey = 0;
@@ -108,19 +112,73 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
     cluster.sync();
     // 3. every CTA reduces the G keys to the same winner and fetches rows
     if (warp == 0) {
-      unsigned long long kk = 0ull;
-      if (lane < G) kk = cluster.map_shared_rank(&slot[par], lane)->key;
-      const unsigned long long wk = warp_max_u64(kk);
-      const int wc = __ffsll(__ballot_sync(0xffffffffu, kk == wk && lane < G)) - 1;   // CTA holding it
-      const int prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
-      const ClusterSlot* ws = cluster.map_shared_rank(&slot[par], wc);
-      for (int c = lane; c < JB; c += 32) urow[c] = ws->row[c];
-      if (lane == 0) win_label_s = ws->label;
-      const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
-      if (own_p && prow != k) {
-        const ClusterSlot* ks = cluster.map_shared_rank(&slot[par], k / R);
-        for (int c = lane; c < JB; c += 32) rowk_s[c] = ks->row_k[c];
-        if (lane == 0) rowk_label_s = ks->row_k_label;
+      int prow;
+      bool own_p;
+      if constexpr (JBT <= 16) {
+        // one round trip: lanes q and q+16 read CTA q's key, label and one half
+        // each of its candidate row (and of row k, from the CTA holding it)
+        constexpr int H = JBT / 2;
+        const int q = lane & 15, half = lane >> 4;
+        const ClusterSlot* qs = cluster.map_shared_rank(&slot[par], q < G ? q : 0);
+        const bool holds_k = q == k / R;
+        unsigned long long kk = 0ull;
+        int qlabel = 0, klabel = 0;
+        float hrow[H], hrowk[H];
+        if (q < G) {
+          kk = qs->key;
+          qlabel = qs->label;
+  #pragma unroll
+          for (int j = 0; j < H; ++j) {
+            const int c = half * H + j;
+            hrow[j] = c < JB ? qs->row[c] : 0.0f;
+          }
+          if (holds_k) {
+            klabel = qs->row_k_label;
+  #pragma unroll
+            for (int j = 0; j < H; ++j) {
+              const int c = half * H + j;
+              hrowk[j] = c < JB ? qs->row_k[c] : 0.0f;
+            }
+          }
+        }
+        const unsigned long long wk = warp_max_u64(kk);
+        const int wc = __ffsll(__ballot_sync(0xffffffffu, kk == wk && lane < G)) - 1;   // CTA holding it
+        const int prow_ = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
+        if (q == wc) {
+  #pragma unroll
+          for (int j = 0; j < H; ++j) {
+            const int c = half * H + j;
+            if (c < JB) urow[c] = hrow[j];
+          }
+          if (half == 0) win_label_s = qlabel;
+        }
+        const bool own_p_ = (prow_ >= rbeg && prow_ < rbeg + nrows);
+        if (own_p_ && prow_ != k && holds_k) {
+  #pragma unroll
+          for (int j = 0; j < H; ++j) {
+            const int c = half * H + j;
+            if (c < JB) rowk_s[c] = hrowk[j];
+          }
+          if (half == 0) rowk_label_s = klabel;
+        }
+        prow = prow_;
+        own_p = own_p_;
+      } else {
+        // key round trip, then the winner's row (and row k for the pivot's owner)
+        unsigned long long kk = 0ull;
+        if (lane < G) kk = cluster.map_shared_rank(&slot[par], lane)->key;
+        const unsigned long long wk = warp_max_u64(kk);
+        const int wc = __ffsll(__ballot_sync(0xffffffffu, kk == wk && lane < G)) - 1;   // CTA holding it
+        prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
+        const ClusterSlot* ws = cluster.map_shared_rank(&slot[par], wc);
+        for (int c = lane; c < JB; c += 32) urow[c] = ws->row[c];
+        if (lane == 0) win_label_s = ws->label;
+        own_p = (prow >= rbeg && prow < rbeg + nrows);
+        if (own_p && prow != k) {
+          const ClusterSlot* ks = cluster.map_shared_rank(&slot[par], k / R);
+          for (int c = lane; c < JB; c += 32) rowk_s[c] = ks->row_k[c];
+          if (lane == 0) rowk_label_s = ks->row_k_label;
+        }
       }
       __syncwarp();
       if (lane == 0) {
@@ -153,23 +211,69 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
     const bool recip = fabsf(pv) >= Lim<float>::sfmin();
     const float rp = 1.0f / pv;
     mykey = 0;
-    for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
-      const float v = tile[k * R + r];
-      const float l = scale ? (recip ? v * rp : v / pv) : v;
-      tile[k * R + r] = l;
-      for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
+    if (R <= 2 * kClusterThreads) {
+      // one or two rows per thread
+      for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
+        const float v = tile[k * R + r];
+        const float l = scale ? (recip ? v * rp : v / pv) : v;
+        tile[k * R + r] = l;
+        for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
+        if (k + 1 < JB) {
+          unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
+          mykey = kk > mykey ? kk : mykey;
+        }
+      }
+      continue;
+    }
+    // three or more rows per thread: rows r, r+512, r+1024, r+1536 are
+    // updated together, so their shared-memory read-modify-writes overlap
+    for (int r0 = max(0, k + 1 - rbeg) + tid; r0 < nrows; r0 += 4 * kClusterThreads) {
+      int rr[4];
+      bool act[4];
+      float l[4], nk[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        rr[i] = r0 + i * kClusterThreads;
+        act[i] = rr[i] < nrows;
+        const float v = act[i] ? tile[k * R + rr[i]] : 0.0f;
+        l[i] = scale ? (recip ? v * rp : v / pv) : v;
+        if (act[i]) tile[k * R + rr[i]] = l[i];
+        nk[i] = 0.0f;
+      }
       if (k + 1 < JB) {
-        unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
-        mykey = kk > mykey ? kk : mykey;
+        // column k+1 first: its new values are the next pivot candidates
+        const float uc = urow[k + 1];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (act[i]) {
+            float* pc = tile + (k + 1) * R + rr[i];
+            nk[i] = fnmadd<EXACT>(l[i], uc, *pc);
+            *pc = nk[i];
+          }
+      }
+      for (int c = k + 2; c < JB; ++c) {
+        const float uc = urow[c];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (act[i]) {
+            float* pc = tile + c * R + rr[i];
+            *pc = fnmadd<EXACT>(l[i], uc, *pc);
+          }
+      }
+      if (k + 1 < JB) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (act[i]) {
+            unsigned long long kk = pack_key(nk[i], rbeg + rr[i], k + 1);
+            mykey = kk > mykey ? kk : mykey;
+          }
       }
     }
   }
   // no CTA may exit while others can still read its shared memory
   cluster.sync();
-  for (int e = tid; e < JB * nrows; e += kClusterThreads) {
-    int c = e / nrows, r = e - c * nrows;
-    P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * R + r];
-  }
+  for (int c = 0; c < JB; ++c)
+    for (int r = tid; r < nrows; r += kClusterThreads) P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * R + r];
   for (int r = tid; r < nrows; r += kClusterThreads) {
     int g = rbeg + r;
     if (g < JB) {
