@@ -38,13 +38,13 @@ __device__ __forceinline__ unsigned long long pack_key(float v, int row, int fir
   return ((unsigned long long)cand_key(c) << 32) | (unsigned long long)(0xFFFFFFFFu - (unsigned)row);
 }
 
+// Warp maximum of 64-bit keys: the maximum upper word, then the maximum
+// lower word among the lanes that hold it (two redux instructions).
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_xor_sync(0xffffffffu, v, off);
-    v = o > v ? o : v;
-  }
-  return v;
+  const unsigned hi = (unsigned)(v >> 32);
+  const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+  const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? (unsigned)v : 0u);
+  return ((unsigned long long)mhi << 32) | mlo;
 }
 
 // JBT: the leaf-width capacity (8, 16, 32 or 64), so the rank-1 update's
@@ -211,13 +211,17 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
     const bool recip = fabsf(pv) >= Lim<float>::sfmin();
     const float rp = 1.0f / pv;
     mykey = 0;
+    // the panel rows and the pivot row never overlap in shared memory
+    float* __restrict__ tl = tile;
+    const float* __restrict__ ur = urow;
     if (R <= 2 * kClusterThreads) {
       // one or two rows per thread
       for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
         const float v = tile[k * R + r];
         const float l = scale ? (recip ? v * rp : v / pv) : v;
         tile[k * R + r] = l;
-        for (int c = k + 1; c < JB; ++c) tile[c * R + r] = fnmadd<EXACT>(l, urow[c], tile[c * R + r]);
+#pragma unroll 4
+        for (int c = k + 1; c < JB; ++c) tl[c * R + r] = fnmadd<EXACT>(l, ur[c], tl[c * R + r]);
         if (k + 1 < JB) {
           unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
           mykey = kk > mykey ? kk : mykey;
@@ -235,28 +239,29 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
       for (int i = 0; i < 4; ++i) {
         rr[i] = r0 + i * kClusterThreads;
         act[i] = rr[i] < nrows;
-        const float v = act[i] ? tile[k * R + rr[i]] : 0.0f;
+        const float v = act[i] ? tl[k * R + rr[i]] : 0.0f;
         l[i] = scale ? (recip ? v * rp : v / pv) : v;
-        if (act[i]) tile[k * R + rr[i]] = l[i];
+        if (act[i]) tl[k * R + rr[i]] = l[i];
         nk[i] = 0.0f;
       }
       if (k + 1 < JB) {
         // column k+1 first: its new values are the next pivot candidates
-        const float uc = urow[k + 1];
+        const float uc = ur[k + 1];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
           if (act[i]) {
-            float* pc = tile + (k + 1) * R + rr[i];
+            float* __restrict__ pc = tl + (k + 1) * R + rr[i];
             nk[i] = fnmadd<EXACT>(l[i], uc, *pc);
             *pc = nk[i];
           }
       }
+#pragma unroll 2
       for (int c = k + 2; c < JB; ++c) {
-        const float uc = urow[c];
+        const float uc = ur[c];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
           if (act[i]) {
-            float* pc = tile + c * R + rr[i];
+            float* __restrict__ pc = tl + c * R + rr[i];
             *pc = fnmadd<EXACT>(l[i], uc, *pc);
           }
       }
