@@ -352,8 +352,17 @@ static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t
   cfg.stream = s;
   cfg.attrs = at;
   cfg.numAttrs = 1;
+  // with the interchange log, the leaf also applies its interchanges to the
+  // rest of its block column
+  int a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+  if (cx.logging) {
+    a0 = cx.imm_lo;
+    a1 = row0;
+    b0 = row0 + JB;
+    b1 = cx.imm_hi;
+  }
   return (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT, JBT>, P, lda, M, JB, R, row0, ipiv, info,
-                                 cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status);
+                                 cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status, a0, a1, b0, b1);
 }
 
 template <bool EXACT>
@@ -416,6 +425,7 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
                            : launch_leaf<T, false>(P, lda, m - c0, w, c0, ipiv + c0, info, cx, s);
     }
     if (rc) return rc;
+    if (cx.logging && sizeof(T) == 4 && ckind == 2) return 0;   // applied inside the cluster leaf
     if (cx.logging) return laswp_pairs<T>(A, lda, cx.imm_lo, cx.imm_hi, c0, c0 + w, w, cx, s, nullptr);
     return laswp_pairs<T>(A, lda, 0, n, c0, c0 + w, w, cx, s, cx.perm);
   }

@@ -53,7 +53,8 @@ template <bool EXACT, int JBT>
 __global__ void __launch_bounds__(kClusterThreads, 1)
 leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, int row0, int* __restrict__ ipiv,
                           int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
-                          int* __restrict__ pair_count, int* __restrict__ status) {
+                          int* __restrict__ pair_count, int* __restrict__ status, int swap_a0, int swap_a1,
+                          int swap_b0, int swap_b1) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -291,6 +292,35 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
         pair_src[s] = row0 + label[r];
       } else {
         atomicCAS(status, kStatusOk, kStatusCapacity);
+      }
+    }
+  }
+  // The leaf's interchanges on the matrix columns [swap_a0, swap_a1) and
+  // [swap_b0, swap_b1) (the rest of its block column when the other columns
+  // get them later from the log): once every CTA has written its pairs, CTA
+  // b's warps take columns b*16+w, +256, ...; one warp per column gathers
+  // all source rows before writing any destination.
+  const int na = max(0, swap_a1 - swap_a0), nb = max(0, swap_b1 - swap_b0);
+  if (na + nb > 0) {
+    __threadfence();
+    cluster.sync();
+    float* Am = P - (size_t)row0 - (size_t)row0 * lda;
+    const int np = min(JB + *(volatile int*)pair_count, 2 * kLeafMax);
+    constexpr int kPer = (2 * kLeafMax + 31) / 32;
+    for (int idx = b * (kClusterThreads / 32) + warp; idx < na + nb; idx += G * (kClusterThreads / 32)) {
+      const int col = idx < na ? swap_a0 + idx : swap_b0 + (idx - na);
+      float* Ac = Am + (size_t)col * lda;
+      float v[kPer];
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        const int i = lane + 32 * q;
+        if (i < np) v[q] = Ac[__ldcg(pair_src + i)];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        const int i = lane + 32 * q;
+        if (i < np) Ac[__ldcg(pair_dst + i)] = v[q];
       }
     }
   }
