@@ -119,12 +119,27 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
                            cudaStream_t s, int mode) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   if (mode == kMixedBf16x3) return gemm_bf16x3_dev(M, N, K, A, lda, B, ldb, C, ldc, s);
-  dim3 grid((M + 127) / 128, (N + 127) / 128);
   prof_begin(kProfGemmF32, s);
-  if (options().exact)
-    GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
-  else
-    GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  const bool ex = options().exact;
+  // tile width follows N: the narrow updates of the panel recursion (N <= 64)
+  // get 128 x 16/32/64 tiles instead of computing mostly padding
+  if (N <= 16) {
+    dim3 grid((M + 127) / 128, (N + 15) / 16);
+    if (ex) GB_LAUNCH(gemm_nn_update_kernel<float, 128, 16, 16, 4, 2, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+    else GB_LAUNCH(gemm_nn_update_kernel<float, 128, 16, 16, 4, 2, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  } else if (N <= 32) {
+    dim3 grid((M + 127) / 128, (N + 31) / 32);
+    if (ex) GB_LAUNCH(gemm_nn_update_kernel<float, 128, 32, 8, 4, 4, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+    else GB_LAUNCH(gemm_nn_update_kernel<float, 128, 32, 8, 4, 4, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  } else if (N <= 64) {
+    dim3 grid((M + 127) / 128, (N + 63) / 64);
+    if (ex) GB_LAUNCH(gemm_nn_update_kernel<float, 128, 64, 8, 4, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+    else GB_LAUNCH(gemm_nn_update_kernel<float, 128, 64, 8, 4, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  } else {
+    dim3 grid((M + 127) / 128, (N + 127) / 128);
+    if (ex) GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, true><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+    else GB_LAUNCH(gemm_nn_update_kernel<float, 128, 128, 8, 8, 8, false><<<grid, 256, 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  }
   prof_end(kProfGemmF32, s, 2.0 * M * N * (double)K, 4.0 * ((double)M * K + (double)K * N + 2.0 * M * N));
   return (int)cudaGetLastError();
 }
