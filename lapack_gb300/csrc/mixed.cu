@@ -179,12 +179,24 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   int hflags[4];
   int rc;
 
-  // ANRM = DLANGE('I'), kept on the device for the convergence test
-  if ((rc = row_abs_sums(n, n, dA, lda, anrm, s))) return rc;
   GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
-  // SX = DLAG2S(B), SA = DLAG2S(A)
+  // SX = DLAG2S(B)
   GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
-  GB_LAUNCH(dlag2s_kernel<<<blocks_for(nn), 256, 0, s>>>(dA, lda, SA, n, n, n, flags));
+  // ANRM = DLANGE('I') (kept on the device for the convergence test) and
+  // SA = DLAG2S(A), in one pass over A; exact mode sums each row in column
+  // order, otherwise column chunks are folded in fixed order
+  {
+    const int nsplit = opt.exact ? 1 : std::max(1, std::min(16, n / 512));
+    const int chunk = (n + nsplit - 1) / nsplit;
+    DevScratch buf(sizeof(double) * (size_t)n * (nsplit + 1), s);
+    if (!buf.p) return (int)cudaErrorMemoryAllocation;
+    double* part = buf.as<double>();
+    double* rows = part + (size_t)n * nsplit;
+    dim3 g((n + 127) / 128, nsplit);
+    GB_LAUNCH(dlag2s_rowsum_kernel<<<g, 128, 0, s>>>(dA, lda, n, n, chunk, SA, n, part, flags));
+    GB_LAUNCH(fold_partials_kernel<<<(n + 255) / 256, 256, 0, s>>>(part, nsplit, n, rows));
+    GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, n, anrm));
+  }
   GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hflags[0]) { *iter = -2; goto fallback; }

@@ -221,8 +221,21 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
         const float v = tile[k * R + r];
         const float l = scale ? (recip ? v * rp : v / pv) : v;
         tile[k * R + r] = l;
-#pragma unroll 4
-        for (int c = k + 1; c < JB; ++c) tl[c * R + r] = fnmadd<EXACT>(l, ur[c], tl[c * R + r]);
+        // four columns at a time: all loads before any store (the compiler
+        // cannot see that rows c*R and (c+1)*R differ)
+        int c = k + 1;
+        for (; c + 3 < JB; c += 4) {
+          float* p0 = tl + c * R + r;
+          const float t0 = p0[0], t1 = p0[R], t2 = p0[2 * R], t3 = p0[3 * R];
+          const float u0 = ur[c], u1 = ur[c + 1], u2 = ur[c + 2], u3 = ur[c + 3];
+          const float n0 = fnmadd<EXACT>(l, u0, t0), n1 = fnmadd<EXACT>(l, u1, t1);
+          const float n2 = fnmadd<EXACT>(l, u2, t2), n3 = fnmadd<EXACT>(l, u3, t3);
+          p0[0] = n0;
+          p0[R] = n1;
+          p0[2 * R] = n2;
+          p0[3 * R] = n3;
+        }
+        for (; c < JB; ++c) tl[c * R + r] = fnmadd<EXACT>(l, ur[c], tl[c * R + r]);
         if (k + 1 < JB) {
           unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
           mykey = kk > mykey ? kk : mykey;

@@ -325,6 +325,44 @@ static __global__ void dlag2s_kernel(const double* __restrict__ A, int lda, floa
   S[(size_t)r + (size_t)c * lds] = (float)v;
 }
 
+// DLANGE('I') row sums and DLAG2S in one pass over A (SRC/dlange.f:173-189,
+// SRC/dlag2s.f:135-146): thread i of the grid owns row i of the column chunk
+// blockIdx.y, converts every element to FP32 (flagging |a| > SLAMCH('O')) and
+// sums |a| in column order; part[chunk][i] receives the chunk's sum.  Loads
+// of 16 columns are issued together.
+static __global__ void __launch_bounds__(128)
+dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int chunk, float* __restrict__ S, int lds,
+                     double* __restrict__ part, int* __restrict__ overflow) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int l0 = blockIdx.y * chunk, l1 = min(n, l0 + chunk);
+  const double rmax = 3.4028234663852886e38;
+  const double* p = A + i;
+  float* q = S + i;
+  double s = 0;
+  bool ovf = false;
+  int j = l0;
+  for (; j + 16 <= l1; j += 16) {
+    double v[16];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) v[u] = p[(size_t)(j + u) * lda];
+#pragma unroll
+    for (int u = 0; u < 16; ++u) {
+      s = s + fabs(v[u]);
+      ovf |= (v[u] < -rmax || v[u] > rmax);
+      q[(size_t)(j + u) * lds] = (float)v[u];
+    }
+  }
+  for (; j < l1; ++j) {
+    const double v = p[(size_t)j * lda];
+    s = s + fabs(v);
+    ovf |= (v < -rmax || v > rmax);
+    q[(size_t)j * lds] = (float)v;
+  }
+  part[(size_t)blockIdx.y * m + i] = s;
+  if (ovf) *overflow = 1;
+}
+
 // SLAG2D (SRC/slag2d.f:123-128).
 static __global__ void slag2d_kernel(const float* __restrict__ S, int lds, double* __restrict__ A, int lda, int m, int n) {
   size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
