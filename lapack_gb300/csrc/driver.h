@@ -48,6 +48,9 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
               T* dB, int ldb, cudaStream_t s, bool inv_diag = false);   // inv_diag: diagonal blocks by their inverses
+// X = L^{-1} for a unit lower triangular k x k L (k <= 512), FP32.
+template <typename T>
+int unit_lower_inverse_dev(int k, const T* L, int ldl, T* X, int ldx, cudaStream_t s);
 // op(T) X = B for nbatch systems of one size, T the unit lower (lower) or
 // upper triangle of stored LU factors; strides between systems in elements.
 template <typename T>

@@ -503,36 +503,29 @@ static LookaheadRes* lookahead_res() {
   return r.ok ? &r : nullptr;
 }
 
-// Columns of the trailing block row from which U12 is formed with the
-// inverse of L11 (one BF16x3 product) instead of the substitution.
-constexpr int kInvMinCols = 2048;
-
-template <typename T>
-static __global__ void set_identity_kernel(T* X, int n) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e < n * n) X[e] = (e % (n + 1) == 0) ? T(1) : T(0);
-}
-
 // U12 = L11^{-1} A12 for the columns [c_beg, c_end) of the block row of
-// block column j (SRC/dgetrf.f:204).  The next block column always uses the
-// substitution; a wider rest of the block row uses the inverse of L11 and
-// one BF16x3 product when linv is given.  Both schedules (look-ahead or
-// not) cut the block row at the same columns, so they compute the same.
+// block column j (SRC/dgetrf.f:204).  With linv (the BF16x3 mode, the
+// inverse of L11 formed once per block column by form_linv) as one BF16x3
+// product, else by substitution.  Both schedules (look-ahead or not) use
+// the same method for every column, so they compute the same.
 template <typename T>
-static int block_row_u(T* dA, int lda, int j, int jb, int c_beg, int c_end, bool rest, T* linv, cudaStream_t s,
+static int block_row_u(T* dA, int lda, int j, int jb, int c_beg, int c_end, const T* linv, cudaStream_t s,
                        int gemm_mode) {
   if (c_end <= c_beg) return 0;
   T* Ajj = dA + j + (size_t)j * lda;
   T* U = dA + j + (size_t)c_beg * lda;
   if constexpr (sizeof(T) == 4) {
-    if (rest && linv && c_end - c_beg > kInvMinCols) {
-      GB_LAUNCH(set_identity_kernel<<<(jb * jb + 255) / 256, 256, 0, s>>>(linv, jb));
-      int rc = trsm_llnu_dev<T>(jb, jb, Ajj, lda, linv, jb, s, gemm_mode);
-      if (rc) return rc;
-      return gemm_bf16x3_dev(jb, c_end - c_beg, jb, linv, jb, U, lda, U, lda, s, true);
-    }
+    if (linv) return gemm_bf16x3_dev(jb, c_end - c_beg, jb, linv, jb, U, lda, U, lda, s, true);
   }
   return trsm_llnu_dev<T>(jb, c_end - c_beg, Ajj, lda, U, lda, s, gemm_mode);
+}
+
+template <typename T>
+static int form_linv(T* dA, int lda, int j, int jb, T* linv, cudaStream_t s) {
+  if constexpr (sizeof(T) == 4) {
+    if (linv) return unit_lower_inverse_dev<T>(jb, dA + j + (size_t)j * lda, lda, linv, jb, s);
+  }
+  return 0;
 }
 
 static __global__ void iota_kernel(int* p, int n) {
@@ -636,10 +629,12 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       const int j2 = j + jb;
       const int nb2 = j2 < mn ? std::min(nb, mn - j2) : 0;   // next block column
       T* Ajj = dA + j + (size_t)j * lda;
+      rc = form_linv<T>(dA, lda, j, jb, linv, s);
+      if (rc) return rc;
       // next block column first
       if (nb2 > 0) {
         rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
-        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, false, linv, s, gemm_mode);
+        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, linv, s, gemm_mode);
         if (!rc && j2 < m)
           rc = gemm_update_dev<T>(m - j2, nb2, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,
                                   Ajj + jb + (size_t)jb * lda, lda, s, gemm_mode);
@@ -650,7 +645,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       const int c2 = j2 + nb2;
       rc = laswp_log<T>(dA, lda, 0, j, c2, n, cx, cx.perm, s);
       if (!rc && c2 < n) {
-        rc = block_row_u<T>(dA, lda, j, jb, c2, n, true, linv, s, gemm_mode);
+        rc = block_row_u<T>(dA, lda, j, jb, c2, n, linv, s, gemm_mode);
         if (!rc && j2 < m)
           rc = gemm_update_dev<T>(m - j2, n - c2, jb, Ajj + jb, lda, Ajj + (size_t)(c2 - j) * lda, lda,
                                   Ajj + jb + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
@@ -668,8 +663,9 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       T* Ajj = dA + j + (size_t)j * lda;
       const int j2 = j + jb;
       const int c2 = j2 + (j2 < mn ? std::min(nb, mn - j2) : 0);   // next block column, then the rest
-      rc = block_row_u<T>(dA, lda, j, jb, j2, std::min(c2, n), false, linv, s, gemm_mode);
-      if (!rc) rc = block_row_u<T>(dA, lda, j, jb, c2, n, true, linv, s, gemm_mode);
+      rc = form_linv<T>(dA, lda, j, jb, linv, s);
+      if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, std::min(c2, n), linv, s, gemm_mode);
+      if (!rc) rc = block_row_u<T>(dA, lda, j, jb, c2, n, linv, s, gemm_mode);
       if (rc) return rc;
       if (j + jb < m) {
         rc = gemm_update_dev<T>(m - j - jb, n - j - jb, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,

@@ -496,30 +496,38 @@ trsm_llnu_tri_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int ld
   __syncthreads();
   const int col = tid / LPC, sub = tid % LPC;
   const int gbase = lane & ~(LPC - 1);
+  // sliding window: during block kb (steps kb*LPC .. kb*LPC+LPC-1) x[t]
+  // holds row sub + LPC*(t + kb); the block's rows leave through x[0] when
+  // the block ends.  Only one block of steps is unrolled, so the code stays
+  // small enough for the instruction cache.
   T x[RPL];
 #pragma unroll
   for (int t = 0; t < RPL; ++t) {
     const int i = sub + LPC * t;
     x[t] = (col < nc && i < k) ? Bs[i * BLD + col] : T(0);
   }
+  for (int kb = 0; kb < RPL; ++kb) {
+    const int kbase = kb * LPC;
 #pragma unroll
-  for (int kk = 0; kk < KMAX - 1; ++kk) {
-    if (kk < k - 1) {
-      const T xk = __shfl_sync(0xffffffffu, x[kk / LPC], gbase | (kk % LPC));
-      const T* Lc = Lp + tri_off<KMAX>(kk) - kk - 1;     // Lc[i] = L(i, kk) for i > kk
+    for (int kk = 0; kk < LPC; ++kk) {
+      const int kcur = kbase + kk;
+      if (kcur < k - 1) {
+        const T xk = __shfl_sync(0xffffffffu, x[0], gbase | kk);
+        const T* Lc = Lp + tri_off<KMAX>(kcur) - kcur - 1;   // Lc[i] = L(i, kcur) for i > kcur
 #pragma unroll
-      for (int t = kk / LPC; t < RPL; ++t) {
-        const int i = sub + LPC * t;
-        if (i > kk && i < k) x[t] = fnmadd<EXACT>(xk, Lc[i], x[t]);
+        for (int t = 0; t < RPL; ++t) {
+          const int i = sub + LPC * (t + kb);
+          if (i > kcur && i < k) x[t] = fnmadd<EXACT>(xk, Lc[i], x[t]);
+        }
       }
     }
-  }
-  if (col < nc) {
-#pragma unroll
-    for (int t = 0; t < RPL; ++t) {
-      const int i = sub + LPC * t;
-      if (i < k) Bs[i * BLD + col] = x[t];
+    {
+      const int i = sub + kbase;
+      if (col < nc && i < k) Bs[i * BLD + col] = x[0];
     }
+#pragma unroll
+    for (int t = 0; t < RPL - 1; ++t) x[t] = x[t + 1];
+    x[RPL - 1] = T(0);
   }
   __syncthreads();
   for (int e = tid; e < k * nc; e += kTrsmThreads) {

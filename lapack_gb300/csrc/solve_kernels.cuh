@@ -336,7 +336,12 @@ dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int ch
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int l0 = blockIdx.y * chunk, l1 = min(n, l0 + chunk);
-  const double rmax = 3.4028234663852886e38;
+  // |a| and the overflow test |a| > SLAMCH('O') (false for NaN) on the bit
+  // pattern with integer operations: the FP64 units, a few per SM on this
+  // GPU, are left with the sum and the conversion
+  constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
+  constexpr unsigned long long kRmaxBits = 0x47EFFFFFE0000000ull;   // 3.4028234663852886e38
+  constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
   const double* p = A + i;
   float* q = S + i;
   double s = 0;
@@ -348,15 +353,17 @@ dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int ch
     for (int u = 0; u < 16; ++u) v[u] = p[(size_t)(j + u) * lda];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      s = s + fabs(v[u]);
-      ovf |= (v[u] < -rmax || v[u] > rmax);
+      const unsigned long long ab = (unsigned long long)__double_as_longlong(v[u]) & kAbs;
+      s = s + __longlong_as_double((long long)ab);
+      ovf |= (ab > kRmaxBits) & (ab <= kInfBits);
       q[(size_t)(j + u) * lds] = (float)v[u];
     }
   }
   for (; j < l1; ++j) {
     const double v = p[(size_t)j * lda];
-    s = s + fabs(v);
-    ovf |= (v < -rmax || v > rmax);
+    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & kAbs;
+    s = s + __longlong_as_double((long long)ab);
+    ovf |= (ab > kRmaxBits) & (ab <= kInfBits);
     q[(size_t)j * lds] = (float)v;
   }
   part[(size_t)blockIdx.y * m + i] = s;
