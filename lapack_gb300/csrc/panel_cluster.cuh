@@ -24,6 +24,7 @@ namespace gb {
 
 constexpr int kClusterCtas = 16;
 constexpr int kClusterThreads = 512;
+constexpr int kDefer = 4;   // columns whose rank-1 updates the cluster leaf applies together
 
 struct ClusterSlot {
   unsigned long long key;
@@ -66,6 +67,8 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   __shared__ unsigned long long wbest[kClusterThreads / 32];
   __shared__ float pv_s;
   __shared__ int win_label_s, rowk_label_s, prow_s;
+  // pivot rows of the columns whose updates are still pending (slot k % kDefer)
+  __shared__ __align__(16) float uh[kDefer][kLeafMax];
 
   const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -90,6 +93,9 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
 
   for (int k = 0; k < JB; ++k) {
     const int par = k & 1;
+    // updates of columns kfirst .. k-1 (slots 0 .. s_slot-1) to the columns
+    // after k+... are still pending in the tile (see step 6)
+    const int s_slot = k % kDefer, kfirst = k - s_slot;
     // 1. this CTA's best candidate for column k
     mykey = warp_max_u64(mykey);
     if (lane == 0) wbest[warp] = mykey;
@@ -100,8 +106,15 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
       ClusterSlot& sl = slot[par];
       if (lane == 0) sl.key = kk;
       if (kk != 0ull) {
+        // the candidate row is published up to date: its columns after k get
+        // the pending updates, in column order (it may become row k of U)
         const int lr = (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) - rbeg;
-        for (int c = lane; c < JB; c += 32) sl.row[c] = tile[c * R + lr];
+        for (int c = lane; c < JB; c += 32) {
+          float v = tile[c * R + lr];
+          if (c > k)
+            for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * R + lr], uh[d][c], v);
+          sl.row[c] = v;
+        }
         if (lane == 0) sl.label = label[lr];
       }
       if (k >= rbeg && k < rbeg + nrows) {
@@ -191,101 +204,58 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
         }
       }
       __syncwarp();
-      if (prow != k) {
-        if (k >= rbeg && k < rbeg + nrows) {
-          const int lk = k - rbeg;
-          for (int c = lane; c < JB; c += 32) tile[c * R + lk] = urow[c];
-          if (lane == 0) label[lk] = win_label_s;
-        }
-        if (own_p) {
-          const int lp = prow - rbeg;
-          for (int c = lane; c < JB; c += 32) tile[c * R + lp] = rowk_s[c];
-          if (lane == 0) label[lp] = rowk_label_s;
-        }
+      // row k becomes the (up-to-date) pivot row even without an interchange;
+      // the row it displaces moves with its multipliers and still pending
+      // updates, which step 6 applies at its new place
+      if (k >= rbeg && k < rbeg + nrows) {
+        const int lk = k - rbeg;
+        for (int c = lane; c < JB; c += 32) tile[c * R + lk] = urow[c];
+        if (lane == 0 && prow != k) label[lk] = win_label_s;
       }
+      if (prow != k && own_p) {
+        const int lp = prow - rbeg;
+        for (int c = lane; c < JB; c += 32) tile[c * R + lp] = rowk_s[c];
+        if (lane == 0) label[lp] = rowk_label_s;
+      }
+      for (int c = lane; c < JB; c += 32) uh[s_slot][c] = urow[c];
     }
     __syncthreads();
-    // 4. scale column k below the pivot, rank-1 update of each row, and the
-    //    candidate search of column k+1 on the updated values
+    // 6. scale column k below the pivot; column k+1 receives the pending
+    //    updates and this column's at once (its values are the next pivot
+    //    candidates); every kDefer columns the later columns receive the
+    //    group's kDefer updates in one pass (one read-modify-write of shared
+    //    memory per element per group instead of per column).  Every element
+    //    still receives its updates in column order.
     const float pv = pv_s;
     const bool scale = pv != 0.0f;
     const bool recip = fabsf(pv) >= Lim<float>::sfmin();
     const float rp = 1.0f / pv;
-    mykey = 0;
-    // the panel rows and the pivot row never overlap in shared memory
+    const bool flush = s_slot == kDefer - 1;
     float* __restrict__ tl = tile;
-    const float* __restrict__ ur = urow;
-    if (R <= 2 * kClusterThreads) {
-      // one or two rows per thread
-      for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
-        const float v = tile[k * R + r];
-        const float l = scale ? (recip ? v * rp : v / pv) : v;
-        tile[k * R + r] = l;
-        // four columns at a time: all loads before any store (the compiler
-        // cannot see that rows c*R and (c+1)*R differ)
-        int c = k + 1;
-        for (; c + 3 < JB; c += 4) {
-          float* p0 = tl + c * R + r;
-          const float t0 = p0[0], t1 = p0[R], t2 = p0[2 * R], t3 = p0[3 * R];
-          const float u0 = ur[c], u1 = ur[c + 1], u2 = ur[c + 2], u3 = ur[c + 3];
-          const float n0 = fnmadd<EXACT>(l, u0, t0), n1 = fnmadd<EXACT>(l, u1, t1);
-          const float n2 = fnmadd<EXACT>(l, u2, t2), n3 = fnmadd<EXACT>(l, u3, t3);
-          p0[0] = n0;
-          p0[R] = n1;
-          p0[2 * R] = n2;
-          p0[3 * R] = n3;
-        }
-        for (; c < JB; ++c) tl[c * R + r] = fnmadd<EXACT>(l, ur[c], tl[c * R + r]);
-        if (k + 1 < JB) {
-          unsigned long long kk = pack_key(tile[(k + 1) * R + r], rbeg + r, k + 1);
-          mykey = kk > mykey ? kk : mykey;
-        }
-      }
-      continue;
-    }
-    // three or more rows per thread: rows r, r+512, r+1024, r+1536 are
-    // updated together, so their shared-memory read-modify-writes overlap
-    for (int r0 = max(0, k + 1 - rbeg) + tid; r0 < nrows; r0 += 4 * kClusterThreads) {
-      int rr[4];
-      bool act[4];
-      float l[4], nk[4];
+    mykey = 0;
+    for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
+      const float v = tl[k * R + r];
+      const float l = scale ? (recip ? v * rp : v / pv) : v;
+      tl[k * R + r] = l;
+      float ld[kDefer];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        rr[i] = r0 + i * kClusterThreads;
-        act[i] = rr[i] < nrows;
-        const float v = act[i] ? tl[k * R + rr[i]] : 0.0f;
-        l[i] = scale ? (recip ? v * rp : v / pv) : v;
-        if (act[i]) tl[k * R + rr[i]] = l[i];
-        nk[i] = 0.0f;
-      }
+      for (int d = 0; d < kDefer; ++d) ld[d] = d < s_slot ? tl[(kfirst + d) * R + r] : (d == s_slot ? l : 0.0f);
       if (k + 1 < JB) {
-        // column k+1 first: its new values are the next pivot candidates
-        const float uc = ur[k + 1];
+        float t = tl[(k + 1) * R + r];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (act[i]) {
-            float* __restrict__ pc = tl + (k + 1) * R + rr[i];
-            nk[i] = fnmadd<EXACT>(l[i], uc, *pc);
-            *pc = nk[i];
-          }
+        for (int d = 0; d < kDefer; ++d)
+          if (d <= s_slot) t = fnmadd<EXACT>(ld[d], uh[d][k + 1], t);
+        tl[(k + 1) * R + r] = t;
+        unsigned long long kk = pack_key(t, rbeg + r, k + 1);
+        mykey = kk > mykey ? kk : mykey;
       }
-#pragma unroll 2
-      for (int c = k + 2; c < JB; ++c) {
-        const float uc = ur[c];
+      if (flush) {
+        for (int c = k + 2; c < JB; ++c) {
+          float t = tl[c * R + r];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (act[i]) {
-            float* __restrict__ pc = tl + c * R + rr[i];
-            *pc = fnmadd<EXACT>(l[i], uc, *pc);
-          }
-      }
-      if (k + 1 < JB) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (act[i]) {
-            unsigned long long kk = pack_key(nk[i], rbeg + rr[i], k + 1);
-            mykey = kk > mykey ? kk : mykey;
-          }
+          for (int d = 0; d < kDefer; ++d) t = fnmadd<EXACT>(ld[d], uh[d][c], t);
+          tl[c * R + r] = t;
+        }
       }
     }
   }
