@@ -290,8 +290,8 @@ static ClusterCaps cluster_caps() {
 // Leaf plan of the FP32 cluster path for an M-row panel: the register
 // kernel (kind 1) with 32-column leaves up to M = 16384 and 16-column leaves
 // up to M = 32768 (64 row values per thread), else the shared-memory cluster
-// kernel (kind 2) with the widest leaf (64..8) that fits; 0 when neither
-// applies.  Returns the leaf width.
+// kernel (kind 2) with the widest leaf of 64, 32, 24, 16 or 8 columns that
+// fits; 0 when neither applies.  Returns the leaf width.
 template <typename T>
 static int cluster_leaf_width(int M, int* kind) {
   *kind = 0;
@@ -303,7 +303,9 @@ static int cluster_leaf_width(int M, int* kind) {
     if (R <= 2 * kClusterThreads) { *kind = 1; return 32; }
     if (R <= 4 * kClusterThreads) { *kind = 1; return 16; }
   }
-  for (int lw = kLeafMax; lw >= 8; lw /= 2)
+  // 64, 32, 24, 16 or 8 columns (widths between 32 and 64 would split a
+  // 64-column block into unequal leaves)
+  for (int lw : {64, 32, 24, 16, 8})
     if ((long long)(lw + 1) * R * 4 + 16 <= c.dyn_cap) { *kind = 2; return lw; }
   return 0;
 }
@@ -399,6 +401,22 @@ static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* 
   return rc;
 }
 
+// Left width of a recursion split of w > leaf columns: halves above 64
+// columns (the internal updates stay <= 64 wide or a multiple of 64 deep),
+// whole leaves, about half on the left, within 64 columns (e.g. 24 + 24 + 16
+// instead of four leaves of 16).
+static inline int split_cols(int w, int leaf) {
+  int n1;
+  if (w > 64) {
+    n1 = (w / 2 + 7) / 8 * 8;
+  } else {
+    const int nleaf = (w + leaf - 1) / leaf;
+    n1 = leaf * ((nleaf + 1) / 2);
+  }
+  if (n1 >= w || n1 <= 0) n1 = w / 2;
+  return n1;
+}
+
 // DGETRF2-shaped recursion on the panel of columns [c0, c0+w), rows [c0, m).
 // Each leaf applies its interchanges to every other column of the matrix
 // (left: the DLASWP of SRC/dgetrf.f:193, right: SRC/dgetrf2.f:236 and
@@ -444,8 +462,7 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
     if (cx.logging) return laswp_pairs<T>(A, lda, cx.imm_lo, cx.imm_hi, c0, c0 + w, w, cx, s, nullptr);
     return laswp_pairs<T>(A, lda, 0, n, c0, c0 + w, w, cx, s, cx.perm);
   }
-  int n1 = ((w / 2) + 7) / 8 * 8;
-  if (n1 >= w) n1 = w / 2;
+  const int n1 = split_cols(w, leaf);
   int rc = getrf_rec<T>(A, lda, m, n, c0, n1, ipiv, info, cx, s, gemm_mode);
   if (rc) return rc;
   T* A11 = A + c0 + (size_t)c0 * lda;
@@ -468,8 +485,7 @@ static int count_leaves(int m, int c0, int w) {
   const int clw = cluster_leaf_width<T>(m - c0, &ckind);
   const int leaf = clw ? clw : kLeafMax;
   if (w <= leaf) return 1;
-  int n1 = ((w / 2) + 7) / 8 * 8;
-  if (n1 >= w) n1 = w / 2;
+  const int n1 = split_cols(w, leaf);
   return count_leaves<T>(m, c0, n1) + count_leaves<T>(m, c0 + n1, w - n1);
 }
 
