@@ -597,7 +597,7 @@ def run_adjoint(args):
     ms = e0.elapsed_time(e1) / args.steps
     parts = {}
     for k, nm in enumerate(["gemm_f64", "gemm_f32_ffma", "gemm_bf16x3", "panel", "laswp", "trsm", "trsv",
-                            "residual_f64", "rank_update_gA"]):
+                            "residual_f64", "ipiv_replay_and_gA"]):
         t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
         L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
         if cnt.value:
@@ -607,12 +607,22 @@ def run_adjoint(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     bytes_ = batch * (8.0 * n * n * 2 + 8.0 * n * nrhs * 4)     # LU read by the solves + gA written + vectors
+    # both halves do 2*n^2*nrhs flop per system (the two triangular solves
+    # together, and gA = -gB X^T): 2 flop per byte of LU read or gA written,
+    # above the FP64/HBM ridge, so the step is FP64-FMA-bound
+    flops = batch * 4.0 * n * n * nrhs
+    L.gb300_probe_peak.restype = ctypes.c_double
+    dfma = L.gb300_probe_peak(0)
+    tf = flops / (ms * 1e-3) / 1e12
     return {"metric": "adjoint of X = A^{-1}B: 64 systems n=2048 nrhs=8 (gB by transposed solve, gA = -gB X^T)",
             "value": ms * 1e-3, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "adjoint batch 64 x n=2048 x nrhs=8, factors resident", "forward_s": t_fwd},
             "kernels": parts, "algorithmic_bytes": bytes_, "hbm_gbs": bytes_ / ms / 1e6,
-            "frac_of_hbm": bytes_ / ms / 1e6 / hbm}
+            "frac_of_hbm": bytes_ / ms / 1e6 / hbm,
+            "roofline": {"bound": "fp64-fma", "achieved": tf, "peak": dfma, "unit": "TFLOP/s", "frac": tf / dfma,
+                         "peak_source": "gb300_probe_peak FP64 FMA loop measured in this run",
+                         "work": "4*n^2*nrhs flop per system"}}
 
 
 def main():

@@ -211,6 +211,15 @@ def config_dgesv_small(n=1024, seed=0):
     return np.asfortranarray(a), np.asfortranarray(b)
 
 
+def config_dgesv_fp64(n=16384, nrhs=16, seed=1):
+    """FP64 DGESV case: A iid U[-1,1] (DLARNV idist 2) from the seed, B iid
+    N(0,1) (idist 3) drawn next from the same stream, n x nrhs."""
+    iseed = seed_to_iseed(seed)
+    a = dlarnv(2, iseed, n * n).reshape(n, n).T
+    b = dlarnv(3, iseed, n * nrhs).reshape(nrhs, n).T
+    return np.asfortranarray(a), np.asfortranarray(b)
+
+
 def householder_vectors(n, count, iseed):
     """``count`` DLARNV N(0,1) vectors of length n (the DLAGGE construction,
     TESTING/MATGEN/dlagge.f:185-232, draws its reflector vectors this way)."""
