@@ -1,5 +1,6 @@
 // Shared device helpers for the GB300 LU solve library (sm_103a).
 #pragma once
+#include "fp_convert.h"
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -183,6 +184,7 @@ __device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 
 }  // namespace gb
 

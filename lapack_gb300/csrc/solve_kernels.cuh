@@ -336,9 +336,9 @@ dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int ch
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int l0 = blockIdx.y * chunk, l1 = min(n, l0 + chunk);
-  // |a| and the overflow test |a| > SLAMCH('O') (false for NaN) on the bit
-  // pattern with integer operations: the FP64 units, a few per SM on this
-  // GPU, are left with the sum and the conversion
+  // |a|, the overflow test |a| > SLAMCH('O') (false for NaN) and the
+  // rounding to FP32 on the bit pattern with integer operations: the FP64
+  // units, a few per SM on this GPU, are left with the sum
   constexpr unsigned long long kAbs = 0x7FFFFFFFFFFFFFFFull;
   constexpr unsigned long long kRmaxBits = 0x47EFFFFFE0000000ull;   // 3.4028234663852886e38
   constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
@@ -353,18 +353,19 @@ dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int ch
     for (int u = 0; u < 16; ++u) v[u] = p[(size_t)(j + u) * lda];
 #pragma unroll
     for (int u = 0; u < 16; ++u) {
-      const unsigned long long ab = (unsigned long long)__double_as_longlong(v[u]) & kAbs;
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(v[u]);
+      const unsigned long long ab = bits & kAbs;
       s = s + __longlong_as_double((long long)ab);
       ovf |= (ab > kRmaxBits) & (ab <= kInfBits);
-      q[(size_t)(j + u) * lds] = (float)v[u];
+      q[(size_t)(j + u) * lds] = __uint_as_float(f64_bits_to_f32_bits_rn(bits));
     }
   }
   for (; j < l1; ++j) {
-    const double v = p[(size_t)j * lda];
-    const unsigned long long ab = (unsigned long long)__double_as_longlong(v) & kAbs;
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(p[(size_t)j * lda]);
+    const unsigned long long ab = bits & kAbs;
     s = s + __longlong_as_double((long long)ab);
     ovf |= (ab > kRmaxBits) & (ab <= kInfBits);
-    q[(size_t)j * lds] = (float)v;
+    q[(size_t)j * lds] = __uint_as_float(f64_bits_to_f32_bits_rn(bits));
   }
   part[(size_t)blockIdx.y * m + i] = s;
   if (ovf) *overflow = 1;
