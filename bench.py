@@ -97,8 +97,9 @@ def make_system(n, kappa, seed, nrhs, device):
 
 
 def backward_errors(A, X, B, n):
-    """DGET08 ratio ||b-Ax||_inf/(||A||_inf ||x||_inf eps) and the north-star
-    scaled residual (the same divided by n), computed on the GPU in FP64."""
+    """DGET08 ratio ||b-Ax||_inf/(||A||_inf ||x||_inf eps) and the scaled
+    residual of the headline metric (the same divided by n), computed on the
+    GPU in FP64."""
     import torch
     R = B - A @ X
     anrm = A.abs().sum(dim=1).max().item()

@@ -14,12 +14,17 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 ORACLE = os.path.join(ROOT, "oracle")
-REF_SRC = "/root/reference/LAPACKE"
+
+
+def _ref_tree():
+    """The reference tree the oracle recipe reads (its REF variable)."""
+    out = subprocess.run(["make", "-s", "-C", ORACLE, "ref-path"], capture_output=True, text=True)
+    return out.stdout.strip()
 
 
 @pytest.fixture(scope="module")
 def libs():
-    if not os.path.isdir(REF_SRC):
+    if not os.path.isdir(os.path.join(_ref_tree(), "LAPACKE")):
         pytest.skip("reference LAPACKE sources not present")
     subprocess.run(["make", "-s", "-C", ORACLE, "ref", "ours"], check=True)
     ref = ctypes.CDLL(os.path.join(ORACLE, "_ref", "libref_lapacke.so"))
