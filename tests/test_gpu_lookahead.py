@@ -85,3 +85,18 @@ def test_lookahead_dsgesv_identical(gpu):
     x1, it1, info1 = r1[2], r1[3], r1[4]
     assert info0 == info1 == 0 and it0 == it1 and it0 > 0
     assert x0.tobytes() == x1.tobytes()
+
+
+@pytest.mark.parametrize("cluster_panel", [0, 1, 2])      # grid-wide leaf / register cluster leaf / shared-memory cluster leaf
+@pytest.mark.parametrize("m,n,nb", [(700, 700, 64), (1500, 1500, 256), (2100, 900, 128)])
+def test_panel_variants_exact_bitwise(gpu, exact_mode, cluster_panel, m, n, nb):
+    """Every FP32 leaf kernel applies the DGETRF2 pivot and update rules in
+    the reference order (SRC/dgetrf2.f:170-265): LU, IPIV and INFO match the
+    oracle bit for bit whichever of them factors the leaves."""
+    a = _rand(m, n, 41 + m + n)
+    lu_r, ip_r, info_r = oracle.getrf(a)
+    with _opts(gpu, nb32=nb, cluster_panel=cluster_panel):
+        lu_g, ip_g, info_g = gpu.getrf(a)
+    assert info_g == info_r
+    np.testing.assert_array_equal(ip_g, ip_r)
+    assert lu_g.tobytes(order="F") == lu_r.tobytes(order="F")
