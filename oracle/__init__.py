@@ -51,6 +51,8 @@ def lib():
             getattr(L, f"or_{pre}lange").restype = T
             getattr(L, f"or_{pre}iamax").argtypes = [_i, _p, _i]
         L.or_dsgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p]
+        L.or_dgerfs.argtypes = [_c, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p]
+        L.or_dlacn2.argtypes = [_i, _p, _p, _p, _p, _p, _p]
         L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
         L.or_slag2d.argtypes = [_i, _i, _p, _i, _p, _i, _p]
         L.or_dlaruv.argtypes = [_p, _i, _p]
@@ -110,6 +112,26 @@ def getrs(lu, ipiv, b, trans="N"):
     getattr(lib(), f"or_{_pre(lu)}getrs")(trans.encode(), n, nrhs, _ptr(lu), max(1, n), _ptr(ipiv),
                                           _ptr(b2), max(1, n), _ptr(info))
     return b2.reshape(b.shape), int(info[0])
+
+
+def gerfs(a, af, ipiv, b, x, trans="N"):
+    """DGERFS (SRC/dgerfs.f): refines a copy of ``x`` with the factors
+    ``af``/``ipiv`` of ``a``; returns (x, ferr, berr, info)."""
+    a = _colmajor(a, np.float64)
+    af = _colmajor(af, np.float64)
+    b2 = _colmajor(_as2d(b), np.float64)
+    x2 = _colmajor(_as2d(x), np.float64).copy(order="F")
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    work = np.zeros(3 * max(n, 1))
+    iwork = np.zeros(max(n, 1), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    ld = max(1, n)
+    lib().or_dgerfs(trans.encode(), n, nrhs, _ptr(a), ld, _ptr(af), ld, _ptr(ipiv), _ptr(b2), ld, _ptr(x2), ld,
+                    _ptr(ferr), _ptr(berr), _ptr(work), _ptr(iwork), _ptr(info))
+    return x2.reshape(np.asarray(x).shape), ferr[:nrhs], berr[:nrhs], int(info[0])
 
 
 def gesv(a, b):

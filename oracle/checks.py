@@ -127,6 +127,43 @@ def dget08(a, x, b, eps=None):
     return resid
 
 
+def dget07(a, b, x, xact, ferr, berr, trans="N", chkferr=True, eps=None):
+    """RESLTS(1), RESLTS(2) of TESTING/LIN/dget07.f:203-276: the forward error
+    bound test max_j (||x_j - xact_j||_inf / ||x_j||_inf) / FERR(j) (1/eps when
+    the bound is violated) and the backward error test
+    max_j BERR(j) / ((n+1) eps + (n+1) unfl / max(min_i (|b| + |op(A)||x|)_i, (n+1) unfl))."""
+    a = np.asarray(a, dtype=np.float64)
+    n = a.shape[0]
+    eps = EPS64 if eps is None else eps
+    x = np.asarray(x, dtype=np.float64).reshape(n, -1)
+    xact = np.asarray(xact, dtype=np.float64).reshape(n, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(n, -1)
+    nrhs = x.shape[1]
+    if n <= 0 or nrhs <= 0:
+        return 0.0, 0.0
+    unfl = np.finfo(np.float64).tiny                 # DLAMCH('Safe minimum')
+    ovfl = 1.0 / unfl
+    errbnd = 0.0
+    if chkferr:
+        for j in range(nrhs):
+            xnorm = max(np.abs(x[:, j]).max(), unfl)
+            diff = np.abs(x[:, j] - xact[:, j]).max()
+            if not (xnorm > 1.0 or diff <= ovfl * xnorm):
+                errbnd = 1.0 / eps
+                continue
+            if diff / xnorm <= ferr[j]:
+                errbnd = max(errbnd, (diff / xnorm) / ferr[j])
+            else:
+                errbnd = 1.0 / eps
+    opa = np.abs(a if trans == "N" else a.T)
+    r2 = 0.0
+    for k in range(nrhs):
+        axbi = (np.abs(b[:, k]) + opa @ np.abs(x[:, k])).min()
+        tmp = berr[k] / ((n + 1) * eps + (n + 1) * unfl / max(axbi, (n + 1) * unfl))
+        r2 = tmp if k == 0 else max(r2, tmp)
+    return errbnd, r2
+
+
 def scaled_residual(a, x, b):
     """||b - A x||_inf / (||A||_inf ||x||_inf n eps): the parity measure the
     GPU result must meet (at or below the oracle's own value)."""

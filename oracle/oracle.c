@@ -233,6 +233,202 @@ void or_dlaruv(int iseed[4], int n, double *x) {
   or_seed_unpack(it, iseed);
 }
 
+/* ---- DGEMV with alpha = -1, beta = 1, as DGERFS calls it
+ * (BLAS/SRC/dgemv.f:256-276 for 'N': y += (-x(j)) * A(:,j) column by column;
+ * :292-311 for 'T': y(j) += -1 * (sum_i A(i,j) x(i))). */
+static void or_dgemv_m1(char trans, int n, const double *a, int lda, const double *x, double *y) {
+  if (trans == 'N' || trans == 'n') {
+    for (int j = 0; j < n; j++) {
+      const double temp = -x[j];
+      for (int i = 0; i < n; i++) y[i] = y[i] + temp * a[i + (size_t)j * lda];
+    }
+  } else {
+    for (int j = 0; j < n; j++) {
+      double temp = 0.0;
+      for (int i = 0; i < n; i++) temp = temp + a[i + (size_t)j * lda] * x[i];
+      y[j] = y[j] + (-1.0) * temp;
+    }
+  }
+}
+
+static double or_dasum(int n, const double *x) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s = s + fabs(x[i]);
+  return s;
+}
+
+/* ---- DLACN2: SRC/dlacn2.f:134-263 (Hager / Higham 1-norm estimator,
+ * reverse communication: KASE 1 asks for x := A x, KASE 2 for x := A^T x). */
+void or_dlacn2(int n, double *v, double *x, int *isgn, double *est, int *kase, int isave[3]) {
+  const int itmax = 5;
+  if (*kase == 0) {
+    for (int i = 0; i < n; i++) x[i] = 1.0 / (double)n;
+    *kase = 1;
+    isave[0] = 1;
+    return;
+  }
+  switch (isave[0]) {
+    case 1: {
+      if (n == 1) {
+        v[0] = x[0];
+        *est = fabs(v[0]);
+        *kase = 0;
+        return;
+      }
+      *est = or_dasum(n, x);
+      for (int i = 0; i < n; i++) {
+        x[i] = (x[i] >= 0.0) ? 1.0 : -1.0;
+        isgn[i] = (int)lrint(x[i]);
+      }
+      *kase = 2;
+      isave[0] = 2;
+      return;
+    }
+    case 2:
+      isave[1] = or_diamax(n, x, 1);
+      isave[2] = 2;
+      goto L50;
+    case 3: {
+      for (int i = 0; i < n; i++) v[i] = x[i];
+      const double estold = *est;
+      *est = or_dasum(n, v);
+      int changed = 0;
+      for (int i = 0; i < n; i++) {
+        const double xs = (x[i] >= 0.0) ? 1.0 : -1.0;
+        if ((int)lrint(xs) != isgn[i]) { changed = 1; break; }
+      }
+      if (!changed || *est <= estold) goto L120;
+      for (int i = 0; i < n; i++) {
+        x[i] = (x[i] >= 0.0) ? 1.0 : -1.0;
+        isgn[i] = (int)lrint(x[i]);
+      }
+      *kase = 2;
+      isave[0] = 4;
+      return;
+    }
+    case 4: {
+      const int jlast = isave[1];
+      isave[1] = or_diamax(n, x, 1);
+      if (x[jlast - 1] != fabs(x[isave[1] - 1]) && isave[2] < itmax) {
+        isave[2] = isave[2] + 1;
+        goto L50;
+      }
+      goto L120;
+    }
+    case 5: {
+      const double temp = 2.0 * (or_dasum(n, x) / (double)(3 * n));
+      if (temp > *est) {
+        for (int i = 0; i < n; i++) v[i] = x[i];
+        *est = temp;
+      }
+      *kase = 0;
+      return;
+    }
+  }
+  return;
+L50:
+  for (int i = 0; i < n; i++) x[i] = 0.0;
+  x[isave[1] - 1] = 1.0;
+  *kase = 1;
+  isave[0] = 3;
+  return;
+L120: {
+    double altsgn = 1.0;
+    for (int i = 0; i < n; i++) {
+      x[i] = altsgn * (1.0 + (double)i / (double)(n - 1));
+      altsgn = -altsgn;
+    }
+    *kase = 1;
+    isave[0] = 5;
+    return;
+  }
+}
+
+/* ---- DGERFS: SRC/dgerfs.f:186-424.  Iterative refinement of X with the
+ * factors AF/IPIV (ITMAX = 5), componentwise backward error BERR and the
+ * DLACN2 estimate of the forward error bound FERR.  work: 3n doubles, iwork:
+ * n ints. */
+void or_dgerfs(char trans, int n, int nrhs, const double *a, int lda, const double *af, int ldaf, const int *ipiv,
+               const double *b, int ldb, double *x, int ldx, double *ferr, double *berr, double *work, int *iwork,
+               int *info) {
+  const int itmax = 5;
+  *info = 0;
+  const int notran = (trans == 'N' || trans == 'n');
+  if (!notran && trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') *info = -1;
+  else if (n < 0) *info = -2;
+  else if (nrhs < 0) *info = -3;
+  else if (lda < (n > 1 ? n : 1)) *info = -5;
+  else if (ldaf < (n > 1 ? n : 1)) *info = -7;
+  else if (ldb < (n > 1 ? n : 1)) *info = -10;
+  else if (ldx < (n > 1 ? n : 1)) *info = -12;
+  if (*info != 0) { or_xerbla("DGERFS", -*info); return; }
+  if (n == 0 || nrhs == 0) {
+    for (int j = 0; j < nrhs; j++) { ferr[j] = 0.0; berr[j] = 0.0; }
+    return;
+  }
+  const char transt = notran ? 'T' : 'N';
+  const int nz = n + 1;
+  const double eps = or_dlamch('E'), safmin = or_dlamch('S');
+  const double safe1 = nz * safmin, safe2 = safe1 / eps;
+  double *w = work, *r = work + n, *v = work + 2 * n;
+  for (int j = 0; j < nrhs; j++) {
+    const double *bj = b + (size_t)j * ldb;
+    double *xj = x + (size_t)j * ldx;
+    int count = 1;
+    double lstres = 3.0;
+    for (;;) {
+      for (int i = 0; i < n; i++) r[i] = bj[i];
+      or_dgemv_m1(notran ? 'N' : 'T', n, a, lda, xj, r);
+      for (int i = 0; i < n; i++) w[i] = fabs(bj[i]);
+      if (notran) {
+        for (int k = 0; k < n; k++) {
+          const double xk = fabs(xj[k]);
+          for (int i = 0; i < n; i++) w[i] = w[i] + fabs(a[i + (size_t)k * lda]) * xk;
+        }
+      } else {
+        for (int k = 0; k < n; k++) {
+          double s = 0.0;
+          for (int i = 0; i < n; i++) s = s + fabs(a[i + (size_t)k * lda]) * fabs(xj[i]);
+          w[k] = w[k] + s;
+        }
+      }
+      double s = 0.0;
+      for (int i = 0; i < n; i++) {
+        const double q = (w[i] > safe2) ? fabs(r[i]) / w[i] : (fabs(r[i]) + safe1) / (w[i] + safe1);
+        s = (q > s) ? q : s;
+      }
+      berr[j] = s;
+      if (berr[j] > eps && 2.0 * berr[j] <= lstres && count <= itmax) {
+        int inf2 = 0;
+        or_dgetrs(trans, n, 1, af, ldaf, ipiv, r, n, &inf2);
+        for (int i = 0; i < n; i++) xj[i] = xj[i] + 1.0 * r[i];
+        lstres = berr[j];
+        count++;
+        continue;
+      }
+      break;
+    }
+    for (int i = 0; i < n; i++)
+      w[i] = (w[i] > safe2) ? fabs(r[i]) + nz * eps * w[i] : fabs(r[i]) + nz * eps * w[i] + safe1;
+    int kase = 0, isave[3] = {0, 0, 0};
+    for (;;) {
+      or_dlacn2(n, v, r, iwork, &ferr[j], &kase, isave);
+      if (kase == 0) break;
+      int inf2 = 0;
+      if (kase == 1) {
+        or_dgetrs(transt, n, 1, af, ldaf, ipiv, r, n, &inf2);
+        for (int i = 0; i < n; i++) r[i] = w[i] * r[i];
+      } else {
+        for (int i = 0; i < n; i++) r[i] = w[i] * r[i];
+        or_dgetrs(trans, n, 1, af, ldaf, ipiv, r, n, &inf2);
+      }
+    }
+    lstres = 0.0;
+    for (int i = 0; i < n; i++) lstres = (fabs(xj[i]) > lstres) ? fabs(xj[i]) : lstres;
+    if (lstres != 0.0) ferr[j] = ferr[j] / lstres;
+  }
+}
+
 /* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
  * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */
 void or_dlarnv(int idist, int iseed[4], long long n, double *x) {

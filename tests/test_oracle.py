@@ -87,6 +87,34 @@ def test_dsgesv_ddrvab_ratios(nrhs):
                 assert r < THRESH, (n, imat, it, r)
 
 
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_dgerfs_dchkge_ratios(imat):
+    """DCHKGE tests 5, 6, 7 (TESTING/LIN/dchkge.f:496-520): after DGERFS
+    refines the DGETRS solution, DGET04 and both DGET07 ratios (forward error
+    bound, componentwise backward error) stay below THRESH, for every square
+    nonsingular N of dtest.in, every NRHS and TRANS = N, T, C."""
+    for n in INPUTS["dtest"]["n"]:
+        if n == 0 or (5 <= imat <= 7 and n < imat - 4):
+            continue
+        a, izero = oracle.ge_test_matrix(n, n, imat, 1988 + 7 * n + n)
+        if izero:
+            continue
+        lu, ipiv, info = oracle.getrf(a)
+        assert info == 0
+        for nrhs in INPUTS["dtest"]["nrhs"]:
+            xact = oracle.random_matrix(n, nrhs, 5 + n + nrhs, idist=2)[0]
+            for trans in "NTC":
+                op = a if trans == "N" else a.T
+                rcond = 1.0 / np.linalg.cond(op, 1)
+                b = op @ xact
+                x0, info = oracle.getrs(lu, ipiv, b, trans)
+                x, ferr, berr, info = oracle.gerfs(a, lu, ipiv, b, x0, trans)
+                assert info == 0
+                assert ck.dget04(x, xact, rcond) < THRESH, (n, imat, nrhs, trans)
+                r1, r2 = ck.dget07(a, b, x, xact, ferr, berr, "N" if trans == "N" else "T")
+                assert r1 < THRESH and r2 < THRESH, (n, imat, nrhs, trans, r1, r2)
+
+
 def test_oracle_ipiv_matches_openblas():
     scipy_linalg = pytest.importorskip("scipy.linalg")
     for n, seed in ((64, 1), (200, 2), (513, 3)):
@@ -121,6 +149,9 @@ ERR_GETRS = [(("/", 0, 0, 1, 1), -1), (("N", -1, 0, 1, 1), -2), (("N", 0, -1, 1,
              (("N", 2, 1, 1, 2), -5), (("N", 2, 1, 2, 1), -8)]              # derrge.f:169-184
 ERR_DSGESV = [((-1, 0, 1, 1, 1), -1), ((0, -1, 1, 1, 1), -2), ((2, 1, 1, 2, 2), -4),
               ((2, 1, 2, 1, 2), -7), ((2, 1, 2, 2, 1), -9)]                 # TESTING/LIN/derrab.f:113-127
+ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), -1), (("N", -1, 0, 1, 1, 1, 1), -2), (("N", 0, -1, 1, 1, 1, 1), -3),
+             (("N", 2, 1, 1, 2, 2, 2), -5), (("N", 2, 1, 2, 1, 2, 2), -7), (("N", 2, 1, 2, 2, 1, 2), -10),
+             (("N", 2, 1, 2, 2, 2, 1), -12)]                                 # TESTING/LIN/derrge.f:186-216
 
 
 def _oracle_err(fn, *args):
@@ -148,3 +179,9 @@ def test_oracle_error_exits():
         name, inf = _oracle_err(L.or_dsgesv, n, nrhs, p(a), lda, p(ip), p(a), ldb, p(a), ldx, p(a), p(a),
                                 p(info), p(info))
         assert (name, inf) == ("DSGESV", -code)
+    w = np.zeros(8)
+    iw = np.zeros(4, dtype=np.int32)
+    for (tr, n, nrhs, lda, ldaf, ldb, ldx), code in ERR_GERFS:
+        name, inf = _oracle_err(L.or_dgerfs, tr.encode(), n, nrhs, p(a), lda, p(a), ldaf, p(ip), p(a), ldb, p(a),
+                                ldx, p(w), p(w), p(w), p(iw), p(info))
+        assert (name, inf) == ("DGERFS", -code)
