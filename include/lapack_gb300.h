@@ -68,6 +68,15 @@ void sgesv_(const lapack_int* n, const lapack_int* nrhs, float* a, const lapack_
 void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
              lapack_int* ipiv, const double* b, const lapack_int* ldb, double* x,
              const lapack_int* ldx, double* work, float* swork, lapack_int* iter, lapack_int* info);
+/* Iterative refinement with error bounds.  Replaces SRC/dgerfs.f:181
+ * (lapack.h:3158-3174).  X is refined in place with the factors AF/IPIV of
+ * A (from DGETRF); FERR/BERR receive the forward error bound and the
+ * componentwise backward error of each column.  WORK (3N) and IWORK (N) are
+ * accepted and unused: the vectors live in GPU memory. */
+void dgerfs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const double* a,
+             const lapack_int* lda, const double* af, const lapack_int* ldaf, const lapack_int* ipiv,
+             const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* ferr,
+             double* berr, double* work, lapack_int* iwork, lapack_int* info, size_t trans_len);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -185,6 +194,13 @@ int gb300_dgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, double* dB
                     void* stream);
 int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX,
                      int ldx, int* iter, int* info, void* stream);
+/* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
+ * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
+ * return value is 0, the negative index of an illegal argument as DGERFS
+ * numbers them, or a positive device status. */
+int gb300_dgerfs_dev(char trans, int n, int nrhs, const double* dA, int lda, const double* dAF, int ldaf,
+                     const int* dIpiv, const double* dB, int ldb, double* dX, int ldx, double* dFerr,
+                     double* dBerr, void* stream);
 /* DGETRS on device memory that allocates nothing.  No counterpart in the
  * reference: it exists for callers that may not allocate GPU memory at the
  * point of the solve (a fixed device-memory budget reserved at start-up, a

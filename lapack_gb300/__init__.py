@@ -22,8 +22,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _sz = ctypes.c_size_t
 
 FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
-                   "dsgesv_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_", "slamch_",
-                   "xerbla_"]
+                   "dsgesv_", "dgerfs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
+                   "slamch_", "xerbla_"]
 
 
 class LibraryMissing(RuntimeError):
@@ -56,6 +56,7 @@ def lib():
             getattr(L, nm).argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _p, _i, _p]
         L.gb300_dgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
         L.gb300_dsgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _ip, _ip, _p]
+        L.gb300_dgerfs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p]
         _LIB = L
     return _LIB
 
@@ -173,6 +174,27 @@ def dsgesv(a, b):
     return a, ipiv[:n], x.reshape(np.asarray(b).shape), it.value, info.value
 
 
+def gerfs(a, af, ipiv, b, x, trans="N"):
+    """DGERFS (SRC/dgerfs.f): refines a copy of ``x`` with the factors
+    ``af``/``ipiv`` of ``a``; returns (x, ferr, berr, info)."""
+    a = _fortran(a, np.float64)
+    af = _fortran(af, np.float64)
+    b2 = _fortran(_as2d(b), np.float64)
+    x2 = _fortran(_as2d(x), np.float64)
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    work = np.zeros(3 * max(n, 1))
+    iwork = np.zeros(max(n, 1), dtype=np.int32)
+    info = ctypes.c_int(0)
+    ld = max(1, n)
+    lib().dgerfs_(ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(a), _ref(ld), _ptr(af), _ref(ld),
+                  _ptr(ipiv), _ptr(b2), _ref(ld), _ptr(x2), _ref(ld), _ptr(ferr), _ptr(berr), _ptr(work),
+                  _ptr(iwork), ctypes.byref(info), _sz(1))
+    return x2.reshape(np.asarray(x).shape), ferr[:nrhs], berr[:nrhs], info.value
+
+
 def laswp(a, k1, k2, ipiv, incx=1):
     """xLASWP (SRC/dlaswp.f) on a copy of ``a``."""
     a = _fortran(a, a.dtype)
@@ -262,6 +284,21 @@ def dsgesv_dev(A, ipiv, B, X, stream=None):
     if rc != 0:
         raise RuntimeError(f"gb300 dsgesv failed with status {rc}")
     return it.value, info.value
+
+
+def gerfs_dev(A, AF, ipiv, B, X, ferr, berr, trans="N", stream=None):
+    """DGERFS on device memory: X refined in place; ferr, berr float64 CUDA
+    tensors of length nrhs."""
+    ld, pa = _colmajor_view(A)
+    ldf, pf = _colmajor_view(AF)
+    ldb, pb = _colmajor_view(B)
+    ldx, px = _colmajor_view(X)
+    rc = lib().gb300_dgerfs_dev(trans.encode(), A.shape[0], B.shape[1], ctypes.c_void_p(pa), ld, ctypes.c_void_p(pf),
+                                ldf, ctypes.c_void_p(ipiv.data_ptr()), ctypes.c_void_p(pb), ldb, ctypes.c_void_p(px),
+                                ldx, ctypes.c_void_p(ferr.data_ptr()), ctypes.c_void_p(berr.data_ptr()),
+                                _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 dgerfs failed with status {rc}")
 
 
 def colmajor_empty(m, n, dtype, device="cuda"):

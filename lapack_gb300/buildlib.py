@@ -12,9 +12,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblapack_gb300.so")
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is compiled without floating-point contraction (-ffp-contract=off):
+# host-side arithmetic then rounds the same on x86-64 and on AArch64
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default",
-          "--expt-relaxed-constexpr"]
-SOURCES = ["getrf.cu", "trsm.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "lapacke.cpp"]
+          "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
+SOURCES = ["getrf.cu", "trsm.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "refine.cu", "lapacke.cpp"]
 
 
 def _sources():

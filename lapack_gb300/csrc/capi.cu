@@ -308,6 +308,49 @@ void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapac
   *info = inf;
 }
 
+void dgerfs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const double* a, const lapack_int* lda,
+             const double* af, const lapack_int* ldaf, const lapack_int* ipiv, const double* b, const lapack_int* ldb,
+             double* x, const lapack_int* ldx, double* ferr, double* berr, double*, lapack_int*, lapack_int* info,
+             size_t) {
+  // argument checks of SRC/dgerfs.f:239-261
+  *info = 0;
+  const bool notran = lsame(*trans, 'N');
+  if (!notran && !lsame(*trans, 'T') && !lsame(*trans, 'C')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldaf < std::max(1, *n)) *info = -7;
+  else if (*ldb < std::max(1, *n)) *info = -10;
+  else if (*ldx < std::max(1, *n)) *info = -12;
+  if (*info != 0) { call_xerbla("DGERFS", -*info); return; }
+  if (*n == 0 || *nrhs == 0) {
+    for (int j = 0; j < *nrhs; ++j) ferr[j] = berr[j] = 0.0;
+    return;
+  }
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dAF(sizeof(double) * (size_t)ld * N, s),
+      dB(sizeof(double) * (size_t)ld * R, s), dX(sizeof(double) * (size_t)ld * R, s),
+      dE(sizeof(double) * 2 * (size_t)R, s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dAF.p || !dB.p || !dX.p || !dE.p || !dP.p) {
+    device_failure("DGERFS", (int)cudaErrorMemoryAllocation, info);
+    return;
+  }
+  double* dF = dE.as<double>();
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dAF.as<double>(), ld, af, *ldaf, N, N, s);
+  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = h2d(dX.as<double>(), ld, x, *ldx, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::dgerfs_dev(notran ? 'N' : 'T', N, R, dA.as<double>(), ld, dAF.as<double>(), ld, dP.as<int>(),
+                               dB.as<double>(), ld, dX.as<double>(), ld, dF, dF + R, s);
+  if (!rc) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ferr, dF, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(berr, dF + R, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure("DGERFS", rc, info);
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -473,6 +516,23 @@ int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const dou
   if (!rc) rc = finish(s);
   if (iter) *iter = it;
   if (info) *info = inf;
+  return rc;
+}
+
+int gb300_dgerfs_dev(char trans, int n, int nrhs, const double* dA, int lda, const double* dAF, int ldaf,
+                     const int* dIpiv, const double* dB, int ldb, double* dX, int ldx, double* dFerr, double* dBerr,
+                     void* stream) {
+  if (!lsame(trans, 'N') && !lsame(trans, 'T') && !lsame(trans, 'C')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldaf < std::max(1, n)) return -7;
+  if (ldb < std::max(1, n)) return -10;
+  if (ldx < std::max(1, n)) return -12;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::dgerfs_dev(lsame(trans, 'N') ? 'N' : 'T', n, nrhs, dA, lda, dAF, ldaf, dIpiv, dB, ldb, dX, ldx, dFerr,
+                          dBerr, s);
+  if (!rc) rc = finish(s);
   return rc;
 }
 

@@ -75,6 +75,9 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
 // DSGESV on device memory.  *iter and *info are host outputs.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
                int* iter, int* info, cudaStream_t s);
+// DGERFS on device memory; FERR/BERR are device arrays of nrhs doubles.
+int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const double* AF, int ldaf, const int* ipiv,
+               const double* B, int ldb, double* X, int ldx, double* ferr, double* berr, cudaStream_t s);
 double dlange_inf_dev(int m, int n, const double* dA, int lda, cudaStream_t s, int* err);
 // DLANGE on device memory: which = 0 'M', 1 '1', 2 'I', 3 'F'.  *out is a
 // host double, valid after the stream synchronises.

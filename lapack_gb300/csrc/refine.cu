@@ -1,0 +1,194 @@
+// DGERFS on the GPU (SRC/dgerfs.f:186-424): iterative refinement of the
+// solutions X of op(A) X = B with the LU factors AF/IPIV, the componentwise
+// backward error BERR, and the forward error bound FERR from the DLACN2
+// estimate of || |inv(op(A))| (|R| + NZ*EPS*(|op(A)||X| + |B|)) ||.
+//
+// All vectors stay in device memory.  The host only reads, per pass, the
+// BERR values (to apply the reference's stopping test column by column)
+// and, per estimator step, each column's KASE (to group the columns that
+// need a solve with op(A) and with op(A)^T into one multi-right-hand-side
+// DGETRS each).  A column's arithmetic does not depend on which other
+// columns share a pass, so X, FERR and BERR of each column are those of the
+// reference's one-column-at-a-time loop; in exact mode they are bitwise the
+// reference's.
+#include "driver.h"
+#include "prof.h"
+#include "refine_kernels.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace gb {
+
+namespace {
+
+unsigned blocks256(size_t n) { return (unsigned)((n + 255) / 256); }
+
+// Splits a column set into launch lists of at most kRfsMaxList entries.
+std::vector<ColList> make_lists(const std::vector<int>& cols) {
+  std::vector<ColList> out;
+  for (size_t b = 0; b < cols.size(); b += kRfsMaxList) {
+    ColList l{};
+    l.n = (int)std::min<size_t>(kRfsMaxList, cols.size() - b);
+    for (int t = 0; t < l.n; ++t) l.c[t] = cols[b + t];
+    out.push_back(l);
+  }
+  return out;
+}
+
+// R(:, c) = B(:, c) - op(A) X(:, c) and W(:, c) = |B(:, c)| + |op(A)||X(:, c)|
+// for the listed columns.
+int residual_bound(bool notran, int n, const double* A, int lda, const double* B, int ldb, const double* X, int ldx,
+                   double* R, double* W, int ldr, const ColList& cols, cudaStream_t s) {
+  prof_begin(kProfResidual, s);
+  if (options().exact) {
+    dim3 g((unsigned)((n + 127) / 128), (unsigned)cols.n);
+    if (notran) GB_LAUNCH(rfs_resid_exact_kernel<false><<<g, 128, 0, s>>>(A, lda, B, ldb, X, ldx, R, W, ldr, n, cols));
+    else GB_LAUNCH(rfs_resid_exact_kernel<true><<<g, 128, 0, s>>>(A, lda, B, ldb, X, ldx, R, W, ldr, n, cols));
+  } else if (notran) {
+    // column chunks depend on n only (never on how many columns share the
+    // pass), so each column's sums are the same alone or in a batch
+    int nsplit = std::max(1, std::min(16, n / 256));
+    int chunk = ((n + nsplit - 1) / nsplit + 31) / 32 * 32;
+    nsplit = (n + chunk - 1) / chunk;
+    DevScratch part(sizeof(double) * (size_t)nsplit * kRfsRq * 2 * n, s);
+    if (!part.p) return (int)cudaErrorMemoryAllocation;
+    const unsigned rows = (unsigned)((n + kRfsRows - 1) / kRfsRows);
+    for (int t0 = 0; t0 < cols.n; t0 += kRfsRq) {
+      ColList sub{};
+      sub.n = std::min(kRfsRq, cols.n - t0);
+      for (int t = 0; t < sub.n; ++t) sub.c[t] = cols.c[t0 + t];
+      dim3 g(rows, nsplit, 1);
+      GB_LAUNCH(rfs_resid_partial_n_kernel<<<g, kRfsRows, 0, s>>>(A, lda, X, ldx, n, chunk, sub, part.as<double>()));
+      GB_LAUNCH(rfs_resid_fold_kernel<<<blocks256((size_t)n * sub.n), 256, 0, s>>>(part.as<double>(), nsplit, B, ldb,
+                                                                                     R, W, ldr, n, sub));
+    }
+  } else {
+    dim3 g((unsigned)((n + 7) / 8), (unsigned)((cols.n + kRfsRq - 1) / kRfsRq));
+    GB_LAUNCH(rfs_resid_t_kernel<<<g, 256, 0, s>>>(A, lda, B, ldb, X, ldx, R, W, ldr, n, cols));
+  }
+  prof_end(kProfResidual, s, 4.0 * n * (double)n * cols.n, 8.0 * ((double)n * n + 4.0 * n * cols.n));
+  return (int)cudaGetLastError();
+}
+
+// D(:, 0..k-1) = Src(:, cols) [times Wpre(:, cols)], one DGETRS with op = `t`
+// on D, then Dst(:, cols) = D [times Wpost(:, cols)], or Dst(:, cols) += D.
+int solve_listed(char t, int n, const double* AF, int ldaf, const int* ipiv, const int* perm, const double* Src,
+                 int lds, const double* Wpre, double* Dst, int ldd, const double* Wpost, int ldw, bool add,
+                 const std::vector<int>& cols, double* D, cudaStream_t s) {
+  const int k = (int)cols.size();
+  if (k == 0) return 0;
+  std::vector<ColList> lists = make_lists(cols);
+  int base = 0;
+  for (const ColList& l : lists) {
+    GB_LAUNCH(rfs_gather_kernel<<<blocks256((size_t)n * l.n), 256, 0, s>>>(Src, lds, Wpre, ldw, D, n, n, l, base));
+    base += l.n;
+  }
+  int rc = getrs_dev<double>(t, n, k, AF, ldaf, ipiv, perm, D, n, s);
+  if (rc) return rc;
+  base = 0;
+  for (const ColList& l : lists) {
+    GB_LAUNCH(rfs_scatter_kernel<<<blocks256((size_t)n * l.n), 256, 0, s>>>(D, n, Wpost, ldw, Dst, ldd, n, l, base,
+                                                                            add ? 1 : 0));
+    base += l.n;
+  }
+  return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const double* AF, int ldaf, const int* ipiv,
+               const double* B, int ldb, double* X, int ldx, double* ferr, double* berr, cudaStream_t s) {
+  if (nrhs <= 0) return 0;
+  if (n <= 0) {   // SRC/dgerfs.f:263-269
+    GB_CUDA_TRY(cudaMemsetAsync(ferr, 0, sizeof(double) * nrhs, s));
+    GB_CUDA_TRY(cudaMemsetAsync(berr, 0, sizeof(double) * nrhs, s));
+    return 0;
+  }
+  const bool notran = (trans == 'N' || trans == 'n');
+  const char tr = notran ? 'N' : 'T', trt = notran ? 'T' : 'N';
+  const int itmax = 5;                                   // SRC/dgerfs.f:208
+  const int nz = n + 1;
+  const double eps = 1.1102230246251565e-16;             // DLAMCH('Epsilon')
+  const double safmin = 2.2250738585072014e-308;         // DLAMCH('Safe minimum')
+  const double safe1 = nz * safmin, safe2 = safe1 / eps;
+
+  const size_t vec = (size_t)n * nrhs;
+  DevScratch perm(sizeof(int) * (size_t)n, s), rw(sizeof(double) * vec * 5, s), ib(sizeof(int) * vec, s),
+      stb(sizeof(LacnState) * (size_t)nrhs, s);
+  if (!perm.p || !rw.p || !ib.p || !stb.p) return (int)cudaErrorMemoryAllocation;
+  double* R = rw.as<double>();
+  double* W = R + vec;
+  double* D = W + vec;
+  double* Xe = D + vec;
+  double* V = Xe + vec;
+  int* Isgn = ib.as<int>();
+  LacnState* st = stb.as<LacnState>();
+  int rc = ipiv_perm_dev(ipiv, 1, n, 1, 0, n, perm.as<int>(), s);
+  if (rc) return rc;
+
+  // ---- refinement (SRC/dgerfs.f:286-399)
+  std::vector<int> active(nrhs), count(nrhs, 1);
+  std::vector<double> lstres(nrhs, 3.0), hberr(nrhs);
+  for (int j = 0; j < nrhs; ++j) active[j] = j;
+  while (!active.empty()) {
+    for (const ColList& l : make_lists(active)) {
+      if ((rc = residual_bound(notran, n, A, lda, B, ldb, X, ldx, R, W, n, l, s))) return rc;
+      GB_LAUNCH(rfs_berr_kernel<<<l.n, 256, 0, s>>>(R, W, n, n, safe1, safe2, l, berr));
+    }
+    GB_CUDA_TRY(cudaMemcpyAsync(hberr.data(), berr, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int> again;
+    for (int j : active) {
+      if (hberr[j] > eps && 2.0 * hberr[j] <= lstres[j] && count[j] <= itmax) {
+        again.push_back(j);
+        lstres[j] = hberr[j];
+        count[j] += 1;
+      }
+    }
+    // X(:, j) += op(A)^{-1} R(:, j) for the columns that refine again
+    if ((rc = solve_listed(tr, n, AF, ldaf, ipiv, perm.as<int>(), R, n, nullptr, X, ldx, nullptr, n, true, again, D,
+                           s)))
+      return rc;
+    active.swap(again);
+  }
+
+  // ---- forward error bound (SRC/dgerfs.f:401-459)
+  std::vector<int> all(nrhs);
+  for (int j = 0; j < nrhs; ++j) all[j] = j;
+  const double nzeps = (double)nz * eps;
+  const bool ex = options().exact;
+  GB_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(LacnState) * (size_t)nrhs, s));
+  for (const ColList& l : make_lists(all)) {
+    GB_LAUNCH(rfs_ferr_weights_kernel<<<blocks256((size_t)n * l.n), 256, 0, s>>>(R, W, n, n, nzeps, safe1, safe2, l));
+    if (ex) GB_LAUNCH(lacn2_step_kernel<true><<<l.n, 256, 0, s>>>(n, Xe, n, V, Isgn, st, l));
+    else GB_LAUNCH(lacn2_step_kernel<false><<<l.n, 256, 0, s>>>(n, Xe, n, V, Isgn, st, l));
+  }
+  std::vector<LacnState> hst(nrhs);
+  for (;;) {
+    GB_CUDA_TRY(cudaMemcpyAsync(hst.data(), st, sizeof(LacnState) * (size_t)nrhs, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    std::vector<int> g1, g2;
+    for (int j = 0; j < nrhs; ++j) {
+      if (hst[j].kase == 1) g1.push_back(j);
+      else if (hst[j].kase == 2) g2.push_back(j);
+    }
+    if (g1.empty() && g2.empty()) break;
+    // KASE 1: x := diag(W) op(A)^{-T} x;  KASE 2: x := op(A)^{-1} diag(W) x
+    if ((rc = solve_listed(trt, n, AF, ldaf, ipiv, perm.as<int>(), Xe, n, nullptr, Xe, n, W, n, false, g1, D, s)))
+      return rc;
+    if ((rc = solve_listed(tr, n, AF, ldaf, ipiv, perm.as<int>(), Xe, n, W, Xe, n, nullptr, n, false, g2, D, s)))
+      return rc;
+    std::vector<int> both(g1);
+    both.insert(both.end(), g2.begin(), g2.end());
+    for (const ColList& l : make_lists(both)) {
+      if (ex) GB_LAUNCH(lacn2_step_kernel<true><<<l.n, 256, 0, s>>>(n, Xe, n, V, Isgn, st, l));
+      else GB_LAUNCH(lacn2_step_kernel<false><<<l.n, 256, 0, s>>>(n, Xe, n, V, Isgn, st, l));
+    }
+  }
+  for (const ColList& l : make_lists(all))
+    GB_LAUNCH(rfs_ferr_finish_kernel<<<l.n, 256, 0, s>>>(X, ldx, n, st, l, ferr));
+  return (int)cudaGetLastError();
+}
+
+}  // namespace gb

@@ -45,6 +45,9 @@ ERR_GETRS = [(("/", 0, 0, 1, 1), 1), (("N", -1, 0, 1, 1), 2), (("N", 0, -1, 1, 1
 ERR_GESV = [((-1, 0, 1, 1), 1), ((0, -1, 1, 1), 2), ((2, 1, 1, 2), 4), ((2, 1, 2, 1), 7)]
 ERR_DSGESV = [((-1, 0, 1, 1, 1), 1), ((0, -1, 1, 1, 1), 2), ((2, 1, 1, 2, 2), 4), ((2, 1, 2, 1, 2), 7),
               ((2, 1, 2, 2, 1), 9)]
+ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), 1), (("N", -1, 0, 1, 1, 1, 1), 2), (("N", 0, -1, 1, 1, 1, 1), 3),
+             (("N", 2, 1, 1, 2, 2, 2), 5), (("N", 2, 1, 2, 1, 2, 2), 7), (("N", 2, 1, 2, 2, 1, 2), 10),
+             (("N", 2, 1, 2, 2, 2, 1), 12)]        # TESTING/LIN/derrge.f:186-216
 
 
 def _i(v):
@@ -76,9 +79,18 @@ def test_fortran_abi_error_exits(lib):
             lib.dsgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), p(a), _i(ldx), p(a), p(a),
                         ctypes.byref(it), ctypes.byref(info))
             assert info.value == -code and g.xerbla_last() == ("DSGESV", code)
-        # quick returns touch nothing
+        w = np.zeros(8)
+        for (tr, n, nrhs, lda, ldaf, ldb, ldx), code in ERR_GERFS:
+            lib.dgerfs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldaf), p(ip), p(a),
+                        _i(ldb), p(a), _i(ldx), p(w), p(w), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DGERFS", code)
+        # quick returns touch nothing on the device
         lib.dgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
         assert info.value == 0
+        fb = np.full(4, 7.0)
+        lib.dgerfs_(ctypes.c_char_p(b"T"), _i(0), _i(2), p(a), _i(1), p(a), _i(1), p(ip), p(a), _i(1), p(a), _i(1),
+                    p(fb), p(fb[2:]), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
+        assert info.value == 0 and np.array_equal(fb, [0.0, 0.0, 0.0, 0.0])   # DGERFS: FERR = BERR = 0 for N = 0
     finally:
         g.xerbla_capture(False)
 
