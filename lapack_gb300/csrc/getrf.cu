@@ -789,6 +789,14 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
     }
     return 0;
   }
+  if constexpr (TRANS && !FORWARD) {
+    // L^T in exact mode: the reference folds each element's sum in
+    // increasing k, which the blocked kernel's backward order does not
+    prof_begin(kProfTrsv, s);
+    GB_LAUNCH(trsv_lt_exact_kernel<T, UNIT><<<(unsigned)((nrhs + 63) / 64), 64, 0, s>>>(A, lda, n, X, ldx, nrhs));
+    prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
+    return (int)cudaGetLastError();
+  }
   DevScratch ctl(sizeof(int) * (size_t)(nblk + 1), s);
   if (!ctl.p) return (int)cudaErrorMemoryAllocation;
   GB_CUDA_TRY(cudaMemsetAsync(ctl.p, 0, sizeof(int) * (size_t)(nblk + 1), s));

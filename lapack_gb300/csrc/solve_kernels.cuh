@@ -77,8 +77,8 @@ __global__ void copy_cols_kernel(const T* __restrict__ S, int lds, T* __restrict
 // (L, or U^T); otherwise decreasing (U, or L^T).  TRANS reads T(k, r) for
 // element (r, k).  In increasing / decreasing order of k each element
 // receives its updates in the reference loop order (N cases and U^T); the
-// L^T case folds k in decreasing order, which the reference folds in
-// increasing order.
+// L^T case would fold k in decreasing order where the reference folds in
+// increasing order, so exact mode solves L^T with trsv_lt_exact_kernel.
 constexpr int kSolveBS = 64;
 constexpr int kSolveRQ = 4;   // right-hand sides per pass (256 threads = 64 rows x 4)
 constexpr int kSolveLd = kSolveBS + 1;
@@ -224,6 +224,26 @@ trsv_blocked_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, 
   __threadfence();
   __syncthreads();
   if (tid == 0) st_release_s32(flags + bi, ok_s ? 1 : -1);
+}
+
+// X := L^{-T} X in the reference order, for exact mode: DTRSM('L','L','T',
+// diag) (BLAS/SRC/dtrsm.f:317-328) forms each X(i) as one dot product,
+// TEMP = X(i) - sum_{k=i+1..n} L(k,i) X(k) folded in increasing k, after every
+// X(k), k > i, is final.  That order is one dependent chain per right-hand
+// side, so one thread solves one right-hand side.
+template <typename T, bool UNIT>
+__global__ void __launch_bounds__(64)
+trsv_lt_exact_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, int ldx, int nrhs) {
+  const int j = blockIdx.x * 64 + threadIdx.x;
+  if (j >= nrhs) return;
+  T* x = X + (size_t)j * ldx;
+  for (int i = n - 1; i >= 0; --i) {
+    const T* col = A + (size_t)i * lda;
+    T temp = x[i];
+    for (int k = i + 1; k < n; ++k) temp = fnmadd<true>(col[k], x[k], temp);
+    if (!UNIT) temp = temp / col[i];
+    x[i] = temp;
+  }
 }
 
 // Raises the dynamic shared-memory limit of one instantiation (needed for

@@ -85,13 +85,14 @@ def test_getrs(gpu, n, nrhs, trans):
     assert ck.dget02(a, x_g, b, trans) < 30.0
 
 
-def test_getrs_exact_bitwise(gpu, exact_mode):
+@pytest.mark.parametrize("trans", ["N", "T"])
+def test_getrs_exact_bitwise(gpu, exact_mode, trans):
     a = _rand(700, 700, 3)
     b = _rand(700, 5, 4)
     lu, ip, _ = oracle.getrf(a)
-    x_r, _ = oracle.getrs(lu, ip, b, "N")
-    x_g, _ = gpu.getrs(lu, ip, b, "N")
-    assert np.array_equal(x_g, x_r)
+    x_r, _ = oracle.getrs(lu, ip, b, trans)
+    x_g, _ = gpu.getrs(lu, ip, b, trans)
+    assert x_g.tobytes() == x_r.tobytes()
 
 
 def test_dgesv_plain_case_n1024(gpu):
