@@ -53,6 +53,9 @@ def lib():
         L.or_dsgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p]
         L.or_dgerfs.argtypes = [_c, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p]
         L.or_dlacn2.argtypes = [_i, _p, _p, _p, _p, _p, _p]
+        L.or_dgecon.argtypes = [_c, _i, _p, _i, ctypes.c_double, _p, _p, _p, _p]
+        L.or_dlatrs.argtypes = [_c, _c, _c, _c, _i, _p, _i, _p, _p, _p, _p]
+        L.or_dtrsv.argtypes = [_c, _c, _c, _i, _p, _i, _p]
         L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
         L.or_slag2d.argtypes = [_i, _i, _p, _i, _p, _i, _p]
         L.or_dlaruv.argtypes = [_p, _i, _p]
@@ -132,6 +135,33 @@ def gerfs(a, af, ipiv, b, x, trans="N"):
     lib().or_dgerfs(trans.encode(), n, nrhs, _ptr(a), ld, _ptr(af), ld, _ptr(ipiv), _ptr(b2), ld, _ptr(x2), ld,
                     _ptr(ferr), _ptr(berr), _ptr(work), _ptr(iwork), _ptr(info))
     return x2.reshape(np.asarray(x).shape), ferr[:nrhs], berr[:nrhs], int(info[0])
+
+
+def gecon(lu, anorm, norm="1"):
+    """DGECON (SRC/dgecon.f): reciprocal condition number from the LU
+    factors and the norm of A; returns (rcond, info)."""
+    lu = _colmajor(lu, np.float64)
+    n = lu.shape[0]
+    rcond = np.zeros(1)
+    work = np.zeros(4 * max(n, 1))
+    iwork = np.zeros(max(n, 1), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dgecon(norm.encode(), n, _ptr(lu), max(1, n), float(anorm), _ptr(rcond), _ptr(work), _ptr(iwork),
+                    _ptr(info))
+    return float(rcond[0]), int(info[0])
+
+
+def latrs(t, x, uplo, trans, diag):
+    """DLATRS (SRC/dlatrs.f) on the triangle of ``t``: returns (x, scale, cnorm)."""
+    t = _colmajor(t, np.float64)
+    n = t.shape[0]
+    x = np.array(x, dtype=np.float64, copy=True)
+    scale = np.zeros(1)
+    cnorm = np.zeros(max(n, 1))
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dlatrs(uplo.encode(), trans.encode(), diag.encode(), b"N", n, _ptr(t), max(1, n), _ptr(x),
+                    _ptr(scale), _ptr(cnorm), _ptr(info))
+    return x, float(scale[0]), cnorm[:n]
 
 
 def gesv(a, b):

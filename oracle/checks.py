@@ -164,6 +164,18 @@ def dget07(a, b, x, xact, ferr, berr, trans="N", chkferr=True, eps=None):
     return errbnd, r2
 
 
+def dget06(rcond, rcondc, eps=None):
+    """TESTING/LIN/dget06.f:101-120: max(RCOND, RCONDC)/min(RCOND, RCONDC) -
+    (1 - eps), or the nonzero one over eps when the other is zero."""
+    eps = EPS64 if eps is None else eps
+    if rcond > 0:
+        if rcondc > 0:
+            return max(rcond, rcondc) / min(rcond, rcondc) - (1 - eps)
+        return rcond / eps
+    if rcondc > 0:
+        return rcondc / eps
+    return 0.0
+
 def scaled_residual(a, x, b):
     """||b - A x||_inf / (||A||_inf ||x||_inf n eps): the parity measure the
     GPU result must meet (at or below the oracle's own value)."""

@@ -429,6 +429,405 @@ void or_dgerfs(char trans, int n, int nrhs, const double *a, int lda, const doub
   }
 }
 
+/* ---- DDOT: BLAS/SRC/ddot.f:82-112 (incx = incy = 1): one running sum in
+ * index order (the unrolled loop adds left to right). */
+static double or_ddot(int n, const double *x, const double *y) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s = s + x[i] * y[i];
+  return s;
+}
+
+/* ---- DTRSV, INCX = 1: BLAS/SRC/dtrsv.f:219-320.  'N': column sweeps
+ * X(i) -= X(j)*A(i,j); 'T' upper: dot products over i = 1..j-1 in increasing
+ * order; 'T' lower: over i = N..j+1 in decreasing order. */
+void or_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x) {
+  const int upper = (uplo == 'U' || uplo == 'u');
+  const int notr = (trans == 'N' || trans == 'n');
+  const int nounit = (diag == 'N' || diag == 'n');
+  if (n == 0) return;
+#define A_(i, j) a[(size_t)(i) + (size_t)(j) * lda]
+  if (notr) {
+    if (upper) {
+      for (int j = n - 1; j >= 0; j--) {
+        if (nounit) x[j] = x[j] / A_(j, j);
+        const double temp = x[j];
+        for (int i = j - 1; i >= 0; i--) x[i] = x[i] - temp * A_(i, j);
+      }
+    } else {
+      for (int j = 0; j < n; j++) {
+        if (nounit) x[j] = x[j] / A_(j, j);
+        const double temp = x[j];
+        for (int i = j + 1; i < n; i++) x[i] = x[i] - temp * A_(i, j);
+      }
+    }
+  } else {
+    if (upper) {
+      for (int j = 0; j < n; j++) {
+        double temp = x[j];
+        for (int i = 0; i < j; i++) temp = temp - A_(i, j) * x[i];
+        if (nounit) temp = temp / A_(j, j);
+        x[j] = temp;
+      }
+    } else {
+      for (int j = n - 1; j >= 0; j--) {
+        double temp = x[j];
+        for (int i = n - 1; i > j; i--) temp = temp - A_(i, j) * x[i];
+        if (nounit) temp = temp / A_(j, j);
+        x[j] = temp;
+      }
+    }
+  }
+#undef A_
+}
+
+/* ---- DRSCL: SRC/drscl.f:105-133.  X := X / SA in steps of SMLNUM or
+ * BIGNUM so that no intermediate overflows or underflows. */
+void or_drscl(int n, double sa, double *x) {
+  if (n <= 0) return;
+  const double smlnum = or_dlamch('S'), bignum = 1.0 / smlnum;
+  double cden = sa, cnum = 1.0;
+  for (;;) {
+    const double cden1 = cden * smlnum, cnum1 = cnum / bignum;
+    double mul;
+    int done;
+    if (fabs(cden1) > fabs(cnum) && cnum != 0.0) {
+      mul = smlnum;
+      done = 0;
+      cden = cden1;
+    } else if (fabs(cnum1) > fabs(cden)) {
+      mul = bignum;
+      done = 0;
+      cnum = cnum1;
+    } else {
+      mul = cnum / cden;
+      done = 1;
+    }
+    or_dscal(n, mul, x, 1);
+    if (done) break;
+  }
+}
+
+/* ---- DLATRS: SRC/dlatrs.f:264-847.  Triangular solve op(A) x = s*b with
+ * a scale factor s <= 1 chosen so that no intermediate result overflows:
+ * column norms CNORM of the off-diagonal part, a growth bound, then DTRSV
+ * when the bound allows it, else the careful column-by-column solve.
+ * MIN / MAX are fmin / fmax. */
+void or_dlatrs(char uplo, char trans, char diag, char normin, int n, const double *a, int lda, double *x,
+               double *scale, double *cnorm, int *info) {
+  const int upper = (uplo == 'U' || uplo == 'u');
+  const int notran = (trans == 'N' || trans == 'n');
+  const int nounit = (diag == 'N' || diag == 'n');
+  *info = 0;
+  if (!upper && uplo != 'L' && uplo != 'l') *info = -1;
+  else if (!notran && trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') *info = -2;
+  else if (!nounit && diag != 'U' && diag != 'u') *info = -3;
+  else if (normin != 'Y' && normin != 'y' && normin != 'N' && normin != 'n') *info = -4;
+  else if (n < 0) *info = -5;
+  else if (lda < (n > 1 ? n : 1)) *info = -7;
+  if (*info != 0) { or_xerbla("DLATRS", -*info); return; }
+  *scale = 1.0;
+  if (n == 0) return;
+#define A_(i, j) a[(size_t)(i) + (size_t)(j) * lda]
+  const double smlnum = or_dlamch('S') / or_dlamch('P');
+  const double bignum = 1.0 / smlnum;
+  const double ovfl = or_dlamch('O');
+  if (normin == 'N' || normin == 'n') {                       /* dlatrs.f:322-338 */
+    if (upper) {
+      for (int j = 0; j < n; j++) cnorm[j] = or_dasum(j, &A_(0, j));
+    } else {
+      for (int j = 0; j < n - 1; j++) cnorm[j] = or_dasum(n - j - 1, &A_(j + 1, j));
+      cnorm[n - 1] = 0.0;
+    }
+  }
+  int imax = or_diamax(n, cnorm, 1);                          /* dlatrs.f:343-397 */
+  double tmax = cnorm[imax - 1];
+  double tscal;
+  if (tmax <= bignum) {
+    tscal = 1.0;
+  } else if (tmax <= ovfl) {
+    tscal = 1.0 / (smlnum * tmax);
+    or_dscal(n, tscal, cnorm, 1);
+  } else {
+    tmax = 0.0;
+    for (int j = 0; j < n; j++) {
+      const int i0 = upper ? 0 : j + 1, i1 = upper ? j : n;   /* the off-diagonal part of column j */
+      double m = 0.0;
+      for (int i = i0; i < i1; i++) {
+        const double t = fabs(A_(i, j));
+        if (m < t || isnan(t)) m = t;
+      }
+      if (i1 > i0) tmax = fmax(m, tmax);
+    }
+    if (tmax <= ovfl) {
+      tscal = 1.0 / (smlnum * tmax);
+      for (int j = 0; j < n; j++) {
+        if (cnorm[j] <= ovfl) {
+          cnorm[j] = cnorm[j] * tscal;
+        } else {
+          cnorm[j] = 0.0;
+          const int i0 = upper ? 0 : j + 1, i1 = upper ? j : n;
+          for (int i = i0; i < i1; i++) cnorm[j] = cnorm[j] + tscal * fabs(A_(i, j));
+        }
+      }
+    } else {
+      or_dtrsv(uplo, trans, diag, n, a, lda, x);
+      return;
+    }
+  }
+  int jx = or_diamax(n, x, 1);                                /* dlatrs.f:401-497 */
+  double xmax = fabs(x[jx - 1]);
+  double xbnd = xmax, grow;
+  int jfirst, jlast, jinc;
+  if (notran) {
+    if (upper) { jfirst = n - 1; jlast = 0; jinc = -1; }
+    else { jfirst = 0; jlast = n - 1; jinc = 1; }
+  } else {
+    if (upper) { jfirst = 0; jlast = n - 1; jinc = 1; }
+    else { jfirst = n - 1; jlast = 0; jinc = -1; }
+  }
+  if (tscal != 1.0) {
+    grow = 0.0;
+  } else if (notran) {
+    if (nounit) {
+      grow = 1.0 / fmax(xbnd, smlnum);
+      xbnd = grow;
+      int cut = 0;
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        if (grow <= smlnum) { cut = 1; break; }
+        const double tjj = fabs(A_(j, j));
+        xbnd = fmin(xbnd, fmin(1.0, tjj) * grow);
+        if (tjj + cnorm[j] >= smlnum) grow = grow * (tjj / (tjj + cnorm[j]));
+        else grow = 0.0;
+      }
+      if (!cut) grow = xbnd;
+    } else {
+      grow = fmin(1.0, 1.0 / fmax(xbnd, smlnum));
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        if (grow <= smlnum) break;
+        grow = grow * (1.0 / (1.0 + cnorm[j]));
+      }
+    }
+  } else {
+    if (nounit) {
+      grow = 1.0 / fmax(xbnd, smlnum);
+      xbnd = grow;
+      int cut = 0;
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        if (grow <= smlnum) { cut = 1; break; }
+        const double xj = 1.0 + cnorm[j];
+        grow = fmin(grow, xbnd / xj);
+        const double tjj = fabs(A_(j, j));
+        if (xj > tjj) xbnd = xbnd * (tjj / xj);
+      }
+      if (!cut) grow = fmin(grow, xbnd);
+    } else {
+      grow = fmin(1.0, 1.0 / fmax(xbnd, smlnum));
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        if (grow <= smlnum) break;
+        const double xj = 1.0 + cnorm[j];
+        grow = grow / xj;
+      }
+    }
+  }
+  if (grow * tscal > smlnum) {                                /* dlatrs.f:499-503 */
+    or_dtrsv(uplo, trans, diag, n, a, lda, x);
+  } else {
+    if (xmax > bignum) {                                      /* dlatrs.f:509-516 */
+      *scale = bignum / xmax;
+      or_dscal(n, *scale, x, 1);
+      xmax = bignum;
+    }
+    if (notran) {                                             /* dlatrs.f:518-640 */
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        double xj = fabs(x[j]), tjjs, rec;
+        int skip = 0;
+        if (nounit) {
+          tjjs = A_(j, j) * tscal;
+        } else {
+          tjjs = tscal;
+          if (tscal == 1.0) skip = 1;
+        }
+        if (!skip) {
+          const double tjj = fabs(tjjs);
+          if (tjj > smlnum) {
+            if (tjj < 1.0 && xj > tjj * bignum) {
+              rec = 1.0 / xj;
+              or_dscal(n, rec, x, 1);
+              *scale = *scale * rec;
+              xmax = xmax * rec;
+            }
+            x[j] = x[j] / tjjs;
+            xj = fabs(x[j]);
+          } else if (tjj > 0.0) {
+            if (xj > tjj * bignum) {
+              rec = (tjj * bignum) / xj;
+              if (cnorm[j] > 1.0) rec = rec / cnorm[j];
+              or_dscal(n, rec, x, 1);
+              *scale = *scale * rec;
+              xmax = xmax * rec;
+            }
+            x[j] = x[j] / tjjs;
+            xj = fabs(x[j]);
+          } else {
+            for (int i = 0; i < n; i++) x[i] = 0.0;
+            x[j] = 1.0;
+            xj = 1.0;
+            *scale = 0.0;
+            xmax = 0.0;
+          }
+        }
+        if (xj > 1.0) {
+          rec = 1.0 / xj;
+          if (cnorm[j] > (bignum - xmax) * rec) {
+            rec = rec * 0.5;
+            or_dscal(n, rec, x, 1);
+            *scale = *scale * rec;
+          }
+        } else if (xj * cnorm[j] > (bignum - xmax)) {
+          or_dscal(n, 0.5, x, 1);
+          *scale = *scale * 0.5;
+        }
+        if (upper) {
+          if (j > 0) {
+            or_daxpy(j, -x[j] * tscal, &A_(0, j), 1, x, 1);
+            const int i = or_diamax(j, x, 1);
+            xmax = fabs(x[i - 1]);
+          }
+        } else if (j < n - 1) {
+          or_daxpy(n - j - 1, -x[j] * tscal, &A_(j + 1, j), 1, x + j + 1, 1);
+          const int i = j + or_diamax(n - j - 1, x + j + 1, 1);
+          xmax = fabs(x[i]);
+        }
+      }
+    } else {                                                  /* dlatrs.f:642-764 */
+      for (int j = jfirst; j != jlast + jinc; j += jinc) {
+        double xj = fabs(x[j]), uscal = tscal, tjjs = 0.0, tjj;
+        double rec = 1.0 / fmax(xmax, 1.0);
+        if (cnorm[j] > (bignum - xj) * rec) {
+          rec = rec * 0.5;
+          tjjs = nounit ? A_(j, j) * tscal : tscal;
+          tjj = fabs(tjjs);
+          if (tjj > 1.0) {
+            rec = fmin(1.0, rec * tjj);
+            uscal = uscal / tjjs;
+          }
+          if (rec < 1.0) {
+            or_dscal(n, rec, x, 1);
+            *scale = *scale * rec;
+            xmax = xmax * rec;
+          }
+        }
+        double sumj = 0.0;
+        if (uscal == 1.0) {
+          if (upper) sumj = or_ddot(j, &A_(0, j), x);
+          else if (j < n - 1) sumj = or_ddot(n - j - 1, &A_(j + 1, j), x + j + 1);
+        } else {
+          if (upper) {
+            for (int i = 0; i < j; i++) sumj = sumj + (A_(i, j) * uscal) * x[i];
+          } else if (j < n - 1) {
+            for (int i = j + 1; i < n; i++) sumj = sumj + (A_(i, j) * uscal) * x[i];
+          }
+        }
+        if (uscal == tscal) {
+          x[j] = x[j] - sumj;
+          xj = fabs(x[j]);
+          int skip = 0;
+          if (nounit) {
+            tjjs = A_(j, j) * tscal;
+          } else {
+            tjjs = tscal;
+            if (tscal == 1.0) skip = 1;
+          }
+          if (!skip) {
+            tjj = fabs(tjjs);
+            if (tjj > smlnum) {
+              if (tjj < 1.0 && xj > tjj * bignum) {
+                rec = 1.0 / xj;
+                or_dscal(n, rec, x, 1);
+                *scale = *scale * rec;
+                xmax = xmax * rec;
+              }
+              x[j] = x[j] / tjjs;
+            } else if (tjj > 0.0) {
+              if (xj > tjj * bignum) {
+                rec = (tjj * bignum) / xj;
+                or_dscal(n, rec, x, 1);
+                *scale = *scale * rec;
+                xmax = xmax * rec;
+              }
+              x[j] = x[j] / tjjs;
+            } else {
+              for (int i = 0; i < n; i++) x[i] = 0.0;
+              x[j] = 1.0;
+              *scale = 0.0;
+              xmax = 0.0;
+            }
+          }
+        } else {
+          x[j] = x[j] / tjjs - sumj;
+        }
+        xmax = fmax(xmax, fabs(x[j]));
+      }
+    }
+    *scale = *scale / tscal;
+  }
+  if (tscal != 1.0) or_dscal(n, 1.0 / tscal, cnorm, 1);          /* dlatrs.f:770-772 */
+#undef A_
+}
+
+/* ---- DGECON: SRC/dgecon.f:166-252.  Reciprocal condition number in the
+ * 1- or infinity-norm from the LU factors: DLACN2 estimate of
+ * ||inv(A)|| with DLATRS solves.  work: 4n doubles, iwork: n ints. */
+void or_dgecon(char norm, int n, const double *a, int lda, double anorm, double *rcond, double *work, int *iwork,
+               int *info) {
+  const double hugeval = or_dlamch('O');
+  const int onenrm = (norm == '1' || norm == 'O' || norm == 'o');
+  *info = 0;
+  if (!onenrm && norm != 'I' && norm != 'i') *info = -1;
+  else if (n < 0) *info = -2;
+  else if (lda < (n > 1 ? n : 1)) *info = -4;
+  else if (anorm < 0.0) *info = -5;
+  if (*info != 0) { or_xerbla("DGECON", -*info); return; }
+  *rcond = 0.0;
+  if (n == 0) { *rcond = 1.0; return; }
+  if (anorm == 0.0) return;
+  if (isnan(anorm)) { *rcond = anorm; *info = -5; return; }
+  if (anorm > hugeval) { *info = -5; return; }
+  const double smlnum = or_dlamch('S');
+  double ainvnm = 0.0;
+  char normin = 'N';
+  const int kase1 = onenrm ? 1 : 2;
+  int kase = 0, isave[3] = {0, 0, 0};
+  double *x = work, *v = work + n, *cl = work + 2 * (size_t)n, *cu = work + 3 * (size_t)n;
+  for (;;) {
+    or_dlacn2(n, v, x, iwork, &ainvnm, &kase, isave);
+    if (kase == 0) break;
+    double sl = 1.0, su = 1.0;
+    int inf2 = 0;
+    if (kase == kase1) {
+      or_dlatrs('L', 'N', 'U', normin, n, a, lda, x, &sl, cl, &inf2);
+      or_dlatrs('U', 'N', 'N', normin, n, a, lda, x, &su, cu, &inf2);
+    } else {
+      or_dlatrs('U', 'T', 'N', normin, n, a, lda, x, &su, cu, &inf2);
+      or_dlatrs('L', 'T', 'U', normin, n, a, lda, x, &sl, cl, &inf2);
+    }
+    const double scale = sl * su;
+    normin = 'Y';
+    if (scale != 1.0) {
+      const int ix = or_diamax(n, x, 1);
+      if (scale < fabs(x[ix - 1]) * smlnum || scale == 0.0) return;
+      or_drscl(n, scale, x);
+    }
+  }
+  if (ainvnm != 0.0) {
+    *rcond = (1.0 / ainvnm) / anorm;
+  } else {
+    *info = 1;
+    return;
+  }
+  if (isnan(*rcond) || *rcond > hugeval) *info = 1;
+}
+
 /* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
  * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */
 void or_dlarnv(int idist, int iseed[4], long long n, double *x) {

@@ -115,6 +115,52 @@ def test_dgerfs_dchkge_ratios(imat):
                 assert r1 < THRESH and r2 < THRESH, (n, imat, nrhs, trans, r1, r2)
 
 
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_dgecon_dchkge_ratios(imat):
+    """DCHKGE test 8 (TESTING/LIN/dchkge.f:536-579): DGET06(RCOND, RCONDC) <
+    THRESH for NORM = '1' and 'I', RCONDC from the explicit inverse, on every
+    square nonsingular N of dtest.in."""
+    for n in INPUTS["dtest"]["n"]:
+        if n == 0 or (5 <= imat <= 7 and n < imat - 4):
+            continue
+        a, izero = oracle.ge_test_matrix(n, n, imat, 1988 + 7 * n + n)
+        if izero:
+            continue
+        lu, ipiv, info = oracle.getrf(a)
+        ainv = np.linalg.inv(a)
+        for norm, p in (("1", 1), ("I", np.inf)):
+            anorm = np.linalg.norm(a, p)
+            rcondc = (1.0 / anorm) / np.linalg.norm(ainv, p)
+            rcond, info = oracle.gecon(lu, anorm, norm)
+            assert info == 0
+            assert ck.dget06(rcond, rcondc) < THRESH, (n, imat, norm, rcond, rcondc)
+
+
+@pytest.mark.parametrize("uplo,trans,diag", [("U", "N", "N"), ("L", "N", "U"), ("U", "T", "N"), ("L", "T", "U")])
+def test_dlatrs_careful_path(uplo, trans, diag):
+    """DLATRS (SRC/dlatrs.f) on a triangle whose growth bound rejects DTRSV
+    (n = 6, diagonal 1e-80, off-diagonal O(1), so x would reach ~1e480): the
+    careful solve returns a finite x with 0 < SCALE < 1 and op(T) x = SCALE * b
+    to working accuracy."""
+    n = 6
+    rng = np.random.default_rng(3)
+    t = rng.standard_normal((n, n))
+    t = np.triu(t) if uplo == "U" else np.tril(t)
+    np.fill_diagonal(t, 1e-80 if diag == "N" else 1.0)
+    if diag == "U":
+        t = t * 1e80                        # a unit triangle whose solution grows past overflow
+        np.fill_diagonal(t, 1.0)
+    b = rng.standard_normal(n)
+    x, scale, cnorm = oracle.latrs(t, b, uplo, trans, diag)
+    assert np.all(np.isfinite(x)) and 0.0 < scale <= 1.0
+    assert scale < 1.0                        # the scaled path was taken
+    tt = t if trans == "N" else t.T
+    # scale the check down to stay clear of overflow in the product
+    m = np.abs(x).max()
+    r = tt @ (x / m) - (scale / m) * b
+    assert np.abs(r).max() <= 1e3 * n * ck.EPS64 * np.abs(tt).max() * 1.0
+
+
 def test_oracle_ipiv_matches_openblas():
     scipy_linalg = pytest.importorskip("scipy.linalg")
     for n, seed in ((64, 1), (200, 2), (513, 3)):
@@ -152,6 +198,7 @@ ERR_DSGESV = [((-1, 0, 1, 1, 1), -1), ((0, -1, 1, 1, 1), -2), ((2, 1, 1, 2, 2), 
 ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), -1), (("N", -1, 0, 1, 1, 1, 1), -2), (("N", 0, -1, 1, 1, 1, 1), -3),
              (("N", 2, 1, 1, 2, 2, 2), -5), (("N", 2, 1, 2, 1, 2, 2), -7), (("N", 2, 1, 2, 2, 1, 2), -10),
              (("N", 2, 1, 2, 2, 2, 1), -12)]                                 # TESTING/LIN/derrge.f:186-216
+ERR_GECON = [(("/", 0, 1), -1), (("1", -1, 1), -2), (("1", 2, 1), -4)]     # TESTING/LIN/derrge.f:218-229
 
 
 def _oracle_err(fn, *args):
@@ -185,3 +232,7 @@ def test_oracle_error_exits():
         name, inf = _oracle_err(L.or_dgerfs, tr.encode(), n, nrhs, p(a), lda, p(a), ldaf, p(ip), p(a), ldb, p(a),
                                 ldx, p(w), p(w), p(w), p(iw), p(info))
         assert (name, inf) == ("DGERFS", -code)
+    rc = np.zeros(1)
+    for (nm, n, lda), code in ERR_GECON:
+        name, inf = _oracle_err(L.or_dgecon, nm.encode(), n, p(a), lda, 1.0, p(rc), p(w), p(iw), p(info))
+        assert (name, inf) == ("DGECON", -code)
