@@ -77,6 +77,17 @@ void dgerfs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, con
              const lapack_int* lda, const double* af, const lapack_int* ldaf, const lapack_int* ipiv,
              const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* ferr,
              double* berr, double* work, lapack_int* iwork, lapack_int* info, size_t trans_len);
+/* Reciprocal condition number from the LU factors.  Replaces SRC/dgecon.f:124
+ * (lapack.h:1513-1526).  WORK (4N) and IWORK (N) are accepted and unused. */
+void dgecon_(const char* norm, const lapack_int* n, const double* a, const lapack_int* lda,
+             const double* anorm, double* rcond, double* work, lapack_int* iwork, lapack_int* info,
+             size_t norm_len);
+/* Triangular solve with overflow protection, op(A) x = s*b.  Replaces
+ * SRC/dlatrs.f:238 (the auxiliary routine DGECON calls).  CNORM is input
+ * when NORMIN = 'Y', else output; SCALE receives s. */
+void dlatrs_(const char* uplo, const char* trans, const char* diag, const char* normin, const lapack_int* n,
+             const double* a, const lapack_int* lda, double* x, double* scale, double* cnorm, lapack_int* info,
+             size_t uplo_len, size_t trans_len, size_t diag_len, size_t normin_len);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -194,6 +205,15 @@ int gb300_dgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, double* dB
                     void* stream);
 int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX,
                      int ldx, int* iter, int* info, void* stream);
+/* DGECON on device memory (SRC/dgecon.f:124): dA holds the LU factors;
+ * *rcond and *info are host outputs.  Returns 0, the negative index of an
+ * illegal argument, or a positive device status. */
+int gb300_dgecon_dev(char norm, int n, const double* dA, int lda, double anorm, double* rcond, int* info,
+                     void* stream);
+/* DLATRS on device memory (SRC/dlatrs.f:238): dA (n x n), dX and dCnorm
+ * (n) are device arrays; *scale is a host output. */
+int gb300_dlatrs_dev(char uplo, char trans, char diag, char normin, int n, const double* dA, int lda, double* dX,
+                     double* scale, double* dCnorm, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

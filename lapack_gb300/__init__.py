@@ -22,7 +22,7 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _sz = ctypes.c_size_t
 
 FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
-                   "dsgesv_", "dgerfs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
+                   "dsgesv_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
                    "slamch_", "xerbla_"]
 
 
@@ -56,6 +56,7 @@ def lib():
             getattr(L, nm).argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _p, _i, _p]
         L.gb300_dgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
         L.gb300_dsgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _ip, _ip, _p]
+        L.gb300_dgecon_dev.argtypes = [ctypes.c_char, _i, _p, _i, ctypes.c_double, _p, _ip, _p]
         L.gb300_dgerfs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p]
         _LIB = L
     return _LIB
@@ -195,6 +196,39 @@ def gerfs(a, af, ipiv, b, x, trans="N"):
     return x2.reshape(np.asarray(x).shape), ferr[:nrhs], berr[:nrhs], info.value
 
 
+def gecon(lu, anorm, norm="1"):
+    """DGECON (SRC/dgecon.f): reciprocal condition number from the LU
+    factors ``lu`` and the norm ``anorm`` of A; returns (rcond, info)."""
+    lu = _fortran(lu, np.float64)
+    n = lu.shape[0]
+    rcond = ctypes.c_double(0.0)
+    info = ctypes.c_int(0)
+    work = np.zeros(4 * max(n, 1))
+    iwork = np.zeros(max(n, 1), dtype=np.int32)
+    lib().dgecon_(ctypes.c_char_p(norm.encode()), _ref(n), _ptr(lu), _ref(max(1, n)),
+                  ctypes.byref(ctypes.c_double(float(anorm))), ctypes.byref(rcond), _ptr(work), _ptr(iwork),
+                  ctypes.byref(info), _sz(1))
+    return rcond.value, info.value
+
+
+def latrs(t, x, uplo, trans, diag, cnorm=None):
+    """DLATRS (SRC/dlatrs.f) on the triangle of ``t``: returns (x, scale,
+    cnorm); ``cnorm`` given means NORMIN = 'Y'."""
+    t = _fortran(t, np.float64)
+    n = t.shape[0]
+    x = np.array(x, dtype=np.float64, copy=True)
+    normin = b"N" if cnorm is None else b"Y"
+    cn = np.zeros(max(n, 1)) if cnorm is None else np.array(cnorm, dtype=np.float64, copy=True)
+    scale = ctypes.c_double(0.0)
+    info = ctypes.c_int(0)
+    lib().dlatrs_(ctypes.c_char_p(uplo.encode()), ctypes.c_char_p(trans.encode()), ctypes.c_char_p(diag.encode()),
+                  ctypes.c_char_p(normin), _ref(n), _ptr(t), _ref(max(1, n)), _ptr(x), ctypes.byref(scale),
+                  _ptr(cn), ctypes.byref(info), _sz(1), _sz(1), _sz(1), _sz(1))
+    if info.value != 0:
+        raise RuntimeError(f"dlatrs failed with INFO = {info.value}")
+    return x, scale.value, cn[:n]
+
+
 def laswp(a, k1, k2, ipiv, incx=1):
     """xLASWP (SRC/dlaswp.f) on a copy of ``a``."""
     a = _fortran(a, a.dtype)
@@ -284,6 +318,18 @@ def dsgesv_dev(A, ipiv, B, X, stream=None):
     if rc != 0:
         raise RuntimeError(f"gb300 dsgesv failed with status {rc}")
     return it.value, info.value
+
+
+def gecon_dev(LU, anorm, norm="1", stream=None):
+    """DGECON on device memory; returns (rcond, info)."""
+    ld, pa = _colmajor_view(LU)
+    rcond = ctypes.c_double(0.0)
+    info = ctypes.c_int(0)
+    rc = lib().gb300_dgecon_dev(norm.encode(), LU.shape[0], ctypes.c_void_p(pa), ld, float(anorm),
+                                ctypes.byref(rcond), ctypes.byref(info), _stream_ptr(stream))
+    if rc != 0:
+        raise RuntimeError(f"gb300 dgecon failed with status {rc}")
+    return rcond.value, info.value
 
 
 def gerfs_dev(A, AF, ipiv, B, X, ferr, berr, trans="N", stream=None):

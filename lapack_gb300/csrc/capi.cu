@@ -351,6 +351,72 @@ void dgerfs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, con
   if (rc) device_failure("DGERFS", rc, info);
 }
 
+void dgecon_(const char* norm, const lapack_int* n, const double* a, const lapack_int* lda, const double* anorm,
+             double* rcond, double*, lapack_int*, lapack_int* info, size_t) {
+  // argument checks of SRC/dgecon.f:183-195
+  *info = 0;
+  const bool onenrm = *norm == '1' || lsame(*norm, 'O');
+  if (!onenrm && !lsame(*norm, 'I')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  else if (*anorm < 0.0) *info = -5;
+  if (*info != 0) { call_xerbla("DGECON", -*info); return; }
+  if (*n == 0 || *anorm == 0.0 || *anorm != *anorm || *anorm > 1.7976931348623157e308) {
+    int inf = 0;
+    gb::dgecon_dev(onenrm ? '1' : 'I', *n, nullptr, std::max(1, *n), *anorm, rcond, &inf, nullptr);
+    *info = inf;
+    return;
+  }
+  cudaStream_t s = thread_stream();
+  const int N = *n, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s);
+  if (!dA.p) { device_failure("DGECON", (int)cudaErrorMemoryAllocation, info); return; }
+  int inf = 0;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = gb::dgecon_dev(onenrm ? '1' : 'I', N, dA.as<double>(), ld, *anorm, rcond, &inf, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DGECON", rc, info); return; }
+  *info = inf;
+}
+
+namespace {
+int latrs_args(char uplo, char trans, char diag, char normin, int n, int lda) {
+  // argument checks of SRC/dlatrs.f:287-306
+  if (!lsame(uplo, 'U') && !lsame(uplo, 'L')) return -1;
+  if (!lsame(trans, 'N') && !lsame(trans, 'T') && !lsame(trans, 'C')) return -2;
+  if (!lsame(diag, 'N') && !lsame(diag, 'U')) return -3;
+  if (!lsame(normin, 'Y') && !lsame(normin, 'N')) return -4;
+  if (n < 0) return -5;
+  if (lda < std::max(1, n)) return -7;
+  return 0;
+}
+}  // namespace
+
+void dlatrs_(const char* uplo, const char* trans, const char* diag, const char* normin, const lapack_int* n,
+             const double* a, const lapack_int* lda, double* x, double* scale, double* cnorm, lapack_int* info, size_t,
+             size_t, size_t, size_t) {
+  *info = latrs_args(*uplo, *trans, *diag, *normin, *n, *lda);
+  if (*info != 0) { call_xerbla("DLATRS", -*info); return; }
+  *scale = 1.0;
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dV(sizeof(double) * 2 * (size_t)N, s);
+  if (!dA.p || !dV.p) { device_failure("DLATRS", (int)cudaErrorMemoryAllocation, info); return; }
+  double* dX = dV.as<double>();
+  double* dC = dX + N;
+  const bool normin_y = lsame(*normin, 'Y');
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dX, x, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+  if (!rc && normin_y) rc = (int)cudaMemcpyAsync(dC, cnorm, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::dlatrs_dev(lsame(*uplo, 'U'), !lsame(*trans, 'N'), lsame(*diag, 'U'), normin_y, N,
+                               dA.as<double>(), ld, dX, scale, dC, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(x, dX, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(cnorm, dC, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure("DLATRS", rc, info);
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -516,6 +582,36 @@ int gb300_dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const dou
   if (!rc) rc = finish(s);
   if (iter) *iter = it;
   if (info) *info = inf;
+  return rc;
+}
+
+int gb300_dgecon_dev(char norm, int n, const double* dA, int lda, double anorm, double* rcond, int* info,
+                     void* stream) {
+  const bool onenrm = norm == '1' || lsame(norm, 'O');
+  if (!onenrm && !lsame(norm, 'I')) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  if (anorm < 0.0) return -5;
+  cudaStream_t s = (cudaStream_t)stream;
+  double r = 0.0;
+  int inf = 0;
+  int rc = gb::dgecon_dev(onenrm ? '1' : 'I', n, dA, lda, anorm, &r, &inf, s);
+  if (!rc) rc = finish(s);
+  if (rcond) *rcond = r;
+  if (info) *info = inf;
+  return rc;
+}
+
+int gb300_dlatrs_dev(char uplo, char trans, char diag, char normin, int n, const double* dA, int lda, double* dX,
+                     double* scale, double* dCnorm, void* stream) {
+  const int bad = latrs_args(uplo, trans, diag, normin, n, lda);
+  if (bad) return bad;
+  cudaStream_t s = (cudaStream_t)stream;
+  double sc = 1.0;
+  int rc = gb::dlatrs_dev(lsame(uplo, 'U'), !lsame(trans, 'N'), lsame(diag, 'U'), lsame(normin, 'Y'), n, dA, lda, dX,
+                          &sc, dCnorm, s);
+  if (!rc) rc = finish(s);
+  if (scale) *scale = sc;
   return rc;
 }
 

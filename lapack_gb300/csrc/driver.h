@@ -53,9 +53,17 @@ template <typename T>
 int unit_lower_inverse_dev(int k, const T* L, int ldl, T* X, int ldx, cudaStream_t s);
 // op(T) X = B for nbatch systems of one size, T the unit lower (lower) or
 // upper triangle of stored LU factors; strides between systems in elements.
+// dtrsv_order: in exact mode, each element's sum in the DTRSV loop order
+// (BLAS/SRC/dtrsv.f) rather than the DTRSM order of DGETRS.
 template <typename T>
 int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int lda, long long sA, T* dX, int ldx,
-                     long long sX, int nbatch, cudaStream_t s);
+                     long long sX, int nbatch, cudaStream_t s, bool dtrsv_order = false);
+// DTRSV on one device vector (X has n elements, unit stride).
+int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int lda, double* dX, cudaStream_t s);
+// DLATRS (SRC/dlatrs.f) on one device vector: *scale (host) receives SCALE;
+// dCnorm (n doubles) is read when normin_y, else computed.
+int dlatrs_dev(bool upper, bool trans, bool unit, bool normin_y, int n, const double* dA, int lda, double* dX,
+               double* scale, double* dCnorm, cudaStream_t s);
 // Gather permutation of a factorization: position r of P*A holds row perm[r].
 int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s);
 template <typename T>
@@ -75,6 +83,8 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
 // DSGESV on device memory.  *iter and *info are host outputs.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
                int* iter, int* info, cudaStream_t s);
+// DGECON on device memory: *rcond and *info are host outputs.
+int dgecon_dev(char norm, int n, const double* LU, int lda, double anorm, double* rcond, int* info, cudaStream_t s);
 // DGERFS on device memory; FERR/BERR are device arrays of nrhs doubles.
 int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const double* AF, int ldaf, const int* ipiv,
                const double* B, int ldb, double* X, int ldx, double* ferr, double* berr, cudaStream_t s);

@@ -745,7 +745,7 @@ template int laswp_dev<float>(int, float*, int, int, int, const int*, int, int, 
 // ------------------------------------------------------------------- GETRS
 template <typename T, bool EXACT, bool FORWARD, bool UNIT, bool TRANS>
 static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cudaStream_t s, bool inv_diag,
-                       int nbatch = 1, long long sA = 0, long long sX = 0) {
+                       int nbatch = 1, long long sA = 0, long long sX = 0, bool dtrsv_order = false) {
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -784,18 +784,22 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
   }
   if (nbatch > 1) {
     for (int b = 0; b < nbatch; ++b) {
-      int rc = launch_trsv<T, EXACT, FORWARD, UNIT, TRANS>(A + b * sA, lda, n, X + b * sX, ldx, nrhs, s, inv_diag);
+      int rc = launch_trsv<T, EXACT, FORWARD, UNIT, TRANS>(A + b * sA, lda, n, X + b * sX, ldx, nrhs, s, inv_diag,
+                                                           1, 0, 0, dtrsv_order);
       if (rc) return rc;
     }
     return 0;
   }
   if constexpr (TRANS && !FORWARD) {
-    // L^T in exact mode: the reference folds each element's sum in
-    // increasing k, which the blocked kernel's backward order does not
-    prof_begin(kProfTrsv, s);
-    GB_LAUNCH(trsv_lt_exact_kernel<T, UNIT><<<(unsigned)((nrhs + 63) / 64), 64, 0, s>>>(A, lda, n, X, ldx, nrhs));
-    prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
-    return (int)cudaGetLastError();
+    // L^T in exact mode: DTRSM folds each element's sum in increasing k,
+    // which the blocked kernel's backward order does not; DTRSV folds it in
+    // decreasing k (BLAS/SRC/dtrsv.f:296-303), which the blocked kernel does
+    if (!dtrsv_order) {
+      prof_begin(kProfTrsv, s);
+      GB_LAUNCH(trsv_lt_exact_kernel<T, UNIT><<<(unsigned)((nrhs + 63) / 64), 64, 0, s>>>(A, lda, n, X, ldx, nrhs));
+      prof_end(kProfTrsv, s, (double)n * n * nrhs, sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
+      return (int)cudaGetLastError();
+    }
   }
   DevScratch ctl(sizeof(int) * (size_t)(nblk + 1), s);
   if (!ctl.p) return (int)cudaErrorMemoryAllocation;
@@ -861,7 +865,7 @@ template int getrs_dev<float>(char, int, int, const float*, int, const int*, con
 // of stored LU factors), X overwritten in place; strides in elements.
 template <typename T>
 int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int lda, long long sA, T* dX, int ldx,
-                     long long sX, int nbatch, cudaStream_t s) {
+                     long long sX, int nbatch, cudaStream_t s, bool dtrsv_order) {
   if (n <= 0 || nrhs <= 0 || nbatch <= 0) return 0;
   // solve order: forward for L and for U^T, backward for U and for L^T
   const bool ex = options().exact;
@@ -873,12 +877,33 @@ int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int l
               : launch_trsv<T, false, false, false, false>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
   }
   if (lower)
-    return ex ? launch_trsv<T, true, false, true, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
+    return ex ? launch_trsv<T, true, false, true, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX,
+                                                        dtrsv_order)
               : launch_trsv<T, false, false, true, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
   return ex ? launch_trsv<T, true, true, false, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX)
             : launch_trsv<T, false, true, false, true>(dA, lda, n, dX, ldx, nrhs, s, false, nbatch, sA, sX);
 }
 template int trsv_batched_dev<double>(bool, bool, int, int, const double*, int, long long, double*, int, long long,
-                                      int, cudaStream_t);
+                                      int, cudaStream_t, bool);
+
+// DTRSV (BLAS/SRC/dtrsv.f, INCX = 1) on one device vector for any UPLO,
+// TRANS, DIAG: in exact mode each element's sum in the DTRSV loop order.
+int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int lda, double* dX, cudaStream_t s) {
+  if (n <= 0) return 0;
+  // solve order: forward for L and for U^T, backward for U and for L^T
+  const bool ex = options().exact;
+#define GB_TRSV(FWD, UN, TR)                                                                                \
+  return ex ? launch_trsv<double, true, FWD, UN, TR>(dA, lda, n, dX, n, 1, s, false, 1, 0, 0, true)        \
+            : launch_trsv<double, false, FWD, UN, TR>(dA, lda, n, dX, n, 1, s, false, 1, 0, 0, true)
+  if (!trans) {
+    if (!upper) { if (unit) GB_TRSV(true, true, false); else GB_TRSV(true, false, false); }
+    if (unit) GB_TRSV(false, true, false);
+    GB_TRSV(false, false, false);
+  }
+  if (upper) { if (unit) GB_TRSV(true, true, true); else GB_TRSV(true, false, true); }
+  if (unit) GB_TRSV(false, true, true);
+  GB_TRSV(false, false, true);
+#undef GB_TRSV
+}
 
 }  // namespace gb

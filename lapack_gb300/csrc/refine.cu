@@ -1,4 +1,6 @@
-// DGERFS on the GPU (SRC/dgerfs.f:186-424): iterative refinement of the
+// DGERFS and DGECON on the GPU.
+//
+// DGERFS (SRC/dgerfs.f:186-424): iterative refinement of the
 // solutions X of op(A) X = B with the LU factors AF/IPIV, the componentwise
 // backward error BERR, and the forward error bound FERR from the DLACN2
 // estimate of || |inv(op(A))| (|R| + NZ*EPS*(|op(A)||X| + |B|)) ||.
@@ -11,9 +13,14 @@
 // columns share a pass, so X, FERR and BERR of each column are those of the
 // reference's one-column-at-a-time loop; in exact mode they are bitwise the
 // reference's.
+//
+// DGECON (SRC/dgecon.f:166-252): the same DLACN2 steps on one device vector,
+// each product with inv(A) or inv(A)^T done as two DLATRS solves
+// (SRC/dlatrs.f) whose CNORM vectors are computed once; the host reads the
+// estimator state and each DLATRS plan (DTRSV or the careful solve).
 #include "driver.h"
 #include "prof.h"
-#include "refine_kernels.cuh"
+#include "condest_kernels.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -93,6 +100,34 @@ int solve_listed(char t, int n, const double* AF, int ldaf, const int* ipiv, con
     base += l.n;
   }
   return (int)cudaGetLastError();
+}
+
+// One DLATRS call on the device vector x: the triangle of A selected by
+// `upper`, op = N (notran) or T, unit or non-unit diagonal.  CNORM is
+// computed unless normin_y; the plan (and SCALE) goes to *plan.
+int latrs_dev(bool upper, bool notran, bool unit, int n, const double* A, int lda, double* x, double* cnorm,
+              bool normin_y, LatrsPlan* plan, cudaStream_t s) {
+  const bool ex = options().exact;
+  const int nounit = unit ? 0 : 1;
+  if (!normin_y) {
+    if (ex) GB_LAUNCH(latrs_cnorm_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(upper, n, A, lda, cnorm));
+    else GB_LAUNCH(latrs_cnorm_kernel<false><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(upper, n, A, lda, cnorm));
+  }
+  GB_LAUNCH(latrs_plan_kernel<<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm, plan));
+  LatrsPlan hp;
+  GB_CUDA_TRY(cudaMemcpyAsync(&hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hp.mode == kLatrsCareful) {
+    if (ex)
+      GB_LAUNCH(latrs_careful_kernel<true><<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm,
+                                                                     plan));
+    else
+      GB_LAUNCH(latrs_careful_kernel<false><<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm,
+                                                                      plan));
+    return (int)cudaGetLastError();
+  }
+  // DTRSV (dlatrs.f:499-503, or :395 when even TMAX overflows)
+  return dtrsv_dev(upper, !notran, unit, n, A, lda, x, s);
 }
 
 }  // namespace
@@ -189,6 +224,87 @@ int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const doub
   for (const ColList& l : make_lists(all))
     GB_LAUNCH(rfs_ferr_finish_kernel<<<l.n, 256, 0, s>>>(X, ldx, n, st, l, ferr));
   return (int)cudaGetLastError();
+}
+
+int dgecon_dev(char norm, int n, const double* LU, int lda, double anorm, double* rcond, int* info,
+               cudaStream_t s) {
+  // SRC/dgecon.f:197-212 (argument errors are the caller's)
+  const double hugeval = kOvfl;
+  const bool onenrm = (norm == '1' || norm == 'O' || norm == 'o');
+  *info = 0;
+  *rcond = 0.0;
+  if (n == 0) { *rcond = 1.0; return 0; }
+  if (anorm == 0.0) return 0;
+  if (anorm != anorm) { *rcond = anorm; *info = -5; return 0; }
+  if (anorm > hugeval) { *info = -5; return 0; }
+  DevScratch vb(sizeof(double) * 4 * (size_t)n, s), ib(sizeof(int) * (size_t)n + 256, s),
+      sb(sizeof(LacnState) + 2 * sizeof(LatrsPlan) + 64, s);
+  if (!vb.p || !ib.p || !sb.p) return (int)cudaErrorMemoryAllocation;
+  double* x = vb.as<double>();
+  double* v = x + n;
+  double* cl = v + n;
+  double* cu = cl + n;
+  int* isgn = ib.as<int>();
+  int* stop = isgn + n;
+  LacnState* st = sb.as<LacnState>();
+  LatrsPlan* plans = reinterpret_cast<LatrsPlan*>(sb.as<char>() + 64);   // [0] L, [1] U
+  GB_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(LacnState), s));
+  GB_CUDA_TRY(cudaMemsetAsync(stop, 0, sizeof(int), s));
+  const bool ex = options().exact;
+  ColList one{};
+  one.n = 1;
+  one.c[0] = 0;
+  const int kase1 = onenrm ? 1 : 2;
+  bool normin_y = false;
+  int rc;
+  for (int guard = 0; guard < 64; ++guard) {
+    if (ex) GB_LAUNCH(lacn2_step_kernel<true><<<1, 256, 0, s>>>(n, x, n, v, isgn, st, one));
+    else GB_LAUNCH(lacn2_step_kernel<false><<<1, 256, 0, s>>>(n, x, n, v, isgn, st, one));
+    LacnState hs;
+    GB_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs.kase == 0) {
+      // RCOND = (1/AINVNM)/ANORM (dgecon.f:242-250)
+      if (hs.est != 0.0) {
+        *rcond = (1.0 / hs.est) / anorm;
+      } else {
+        *info = 1;
+        return 0;
+      }
+      if (*rcond != *rcond || *rcond > hugeval) *info = 1;
+      return 0;
+    }
+    if (hs.kase == kase1) {   // inv(L) then inv(U)
+      if ((rc = latrs_dev(false, true, true, n, LU, lda, x, cl, normin_y, plans + 0, s))) return rc;
+      if ((rc = latrs_dev(true, true, false, n, LU, lda, x, cu, normin_y, plans + 1, s))) return rc;
+    } else {                  // inv(U)^T then inv(L)^T
+      if ((rc = latrs_dev(true, false, false, n, LU, lda, x, cu, normin_y, plans + 1, s))) return rc;
+      if ((rc = latrs_dev(false, false, true, n, LU, lda, x, cl, normin_y, plans + 0, s))) return rc;
+    }
+    normin_y = true;
+    GB_LAUNCH(gecon_rescale_kernel<<<1, kCtaThreads, 0, s>>>(n, x, plans + 0, plans + 1, stop));
+    int hstop = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&hstop, stop, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hstop) return 0;   // dgecon.f:236: RCOND stays 0
+  }
+  return 1000 + kStatusCapacity;   // DLACN2 ends within a dozen steps; more means corrupted state
+}
+
+int dlatrs_dev(bool upper, bool trans, bool unit, bool normin_y, int n, const double* dA, int lda, double* dX,
+               double* scale, double* dCnorm, cudaStream_t s) {
+  *scale = 1.0;
+  if (n <= 0) return 0;
+  DevScratch pb(sizeof(LatrsPlan), s);
+  if (!pb.p) return (int)cudaErrorMemoryAllocation;
+  LatrsPlan* plan = pb.as<LatrsPlan>();
+  int rc = latrs_dev(upper, !trans, unit, n, dA, lda, dX, dCnorm, normin_y, plan, s);
+  if (rc) return rc;
+  LatrsPlan hp;
+  GB_CUDA_TRY(cudaMemcpyAsync(&hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  *scale = hp.scale;
+  return 0;
 }
 
 }  // namespace gb

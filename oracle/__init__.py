@@ -151,17 +151,19 @@ def gecon(lu, anorm, norm="1"):
     return float(rcond[0]), int(info[0])
 
 
-def latrs(t, x, uplo, trans, diag):
-    """DLATRS (SRC/dlatrs.f) on the triangle of ``t``: returns (x, scale, cnorm)."""
+def latrs(t, x, uplo, trans, diag, cnorm=None):
+    """DLATRS (SRC/dlatrs.f) on the triangle of ``t``: returns (x, scale,
+    cnorm); ``cnorm`` given means NORMIN = 'Y'."""
     t = _colmajor(t, np.float64)
     n = t.shape[0]
     x = np.array(x, dtype=np.float64, copy=True)
     scale = np.zeros(1)
-    cnorm = np.zeros(max(n, 1))
+    normin = b"N" if cnorm is None else b"Y"
+    cn = np.zeros(max(n, 1)) if cnorm is None else np.array(cnorm, dtype=np.float64, copy=True)
     info = np.zeros(1, dtype=np.int32)
-    lib().or_dlatrs(uplo.encode(), trans.encode(), diag.encode(), b"N", n, _ptr(t), max(1, n), _ptr(x),
-                    _ptr(scale), _ptr(cnorm), _ptr(info))
-    return x, float(scale[0]), cnorm[:n]
+    lib().or_dlatrs(uplo.encode(), trans.encode(), diag.encode(), normin, n, _ptr(t), max(1, n), _ptr(x),
+                    _ptr(scale), _ptr(cn), _ptr(info))
+    return x, float(scale[0]), cn[:n]
 
 
 def gesv(a, b):

@@ -48,6 +48,11 @@ ERR_DSGESV = [((-1, 0, 1, 1, 1), 1), ((0, -1, 1, 1, 1), 2), ((2, 1, 1, 2, 2), 4)
 ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), 1), (("N", -1, 0, 1, 1, 1, 1), 2), (("N", 0, -1, 1, 1, 1, 1), 3),
              (("N", 2, 1, 1, 2, 2, 2), 5), (("N", 2, 1, 2, 1, 2, 2), 7), (("N", 2, 1, 2, 2, 1, 2), 10),
              (("N", 2, 1, 2, 2, 2, 1), 12)]        # TESTING/LIN/derrge.f:186-216
+ERR_LATRS = [(("/", "N", "N", "N", 0, 1), 1), (("U", "/", "N", "N", 0, 1), 2), (("U", "N", "/", "N", 0, 1), 3),
+             (("U", "N", "N", "/", 0, 1), 4), (("U", "N", "N", "N", -1, 1), 5),
+             (("U", "N", "N", "N", 2, 1), 7)]       # TESTING/LIN/derrtr.f:228-247
+ERR_GECON = [(("/", 0, 1, 1.0), 1), (("1", -1, 1, 1.0), 2), (("1", 2, 1, 1.0), 4),
+             (("1", 2, 2, -1.0), 5)]                # derrge.f:218-229, and ANORM < 0
 
 
 def _i(v):
@@ -84,7 +89,24 @@ def test_fortran_abi_error_exits(lib):
             lib.dgerfs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldaf), p(ip), p(a),
                         _i(ldb), p(a), _i(ldx), p(w), p(w), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
             assert info.value == -code and g.xerbla_last() == ("DGERFS", code)
-        # quick returns touch nothing on the device
+        rc = ctypes.c_double(0.0)
+        for (ul, tr, dg, nm, n, lda), code in ERR_LATRS:
+            c = lambda ch: ctypes.c_char_p(ch.encode())
+            lib.dlatrs_(c(ul), c(tr), c(dg), c(nm), _i(n), p(a), _i(lda), p(w), ctypes.byref(rc), p(w),
+                        ctypes.byref(info), *([ctypes.c_size_t(1)] * 4))
+            assert info.value == -code and g.xerbla_last() == ("DLATRS", code)
+        for (nm, n, lda, anorm), code in ERR_GECON:
+            lib.dgecon_(ctypes.c_char_p(nm.encode()), _i(n), p(a), _i(lda), ctypes.byref(ctypes.c_double(anorm)),
+                        ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DGECON", code)
+        # quick returns touch nothing on the device (SRC/dgecon.f:197-212)
+        for n, anorm, want_rc, want_info in ((0, 1.0, 1.0, 0), (2, 0.0, 0.0, 0), (2, float("inf"), 0.0, -5)):
+            lib.dgecon_(ctypes.c_char_p(b"I"), _i(n), p(a), _i(2), ctypes.byref(ctypes.c_double(anorm)),
+                        ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
+            assert rc.value == want_rc and info.value == want_info
+        lib.dgecon_(ctypes.c_char_p(b"O"), _i(2), p(a), _i(2), ctypes.byref(ctypes.c_double(float("nan"))),
+                    ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
+        assert np.isnan(rc.value) and info.value == -5
         lib.dgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
         assert info.value == 0
         fb = np.full(4, 7.0)
