@@ -887,14 +887,16 @@ template int trsv_batched_dev<double>(bool, bool, int, int, const double*, int, 
                                       int, cudaStream_t, bool);
 
 // DTRSV (BLAS/SRC/dtrsv.f, INCX = 1) on one device vector for any UPLO,
-// TRANS, DIAG: in exact mode each element's sum in the DTRSV loop order.
+// TRANS, DIAG, in every mode with the reference's operations: each element's
+// sum in the DTRSV loop order and a true division by the diagonal.  DLATRS
+// relies on this: its growth bound admits the plain solve for values near
+// underflow, where a reciprocal of the diagonal can overflow although the
+// quotient does not.
 int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int lda, double* dX, cudaStream_t s) {
   if (n <= 0) return 0;
   // solve order: forward for L and for U^T, backward for U and for L^T
-  const bool ex = options().exact;
-#define GB_TRSV(FWD, UN, TR)                                                                                \
-  return ex ? launch_trsv<double, true, FWD, UN, TR>(dA, lda, n, dX, n, 1, s, false, 1, 0, 0, true)        \
-            : launch_trsv<double, false, FWD, UN, TR>(dA, lda, n, dX, n, 1, s, false, 1, 0, 0, true)
+#define GB_TRSV(FWD, UN, TR) \
+  return launch_trsv<double, true, FWD, UN, TR>(dA, lda, n, dX, n, 1, s, false, 1, 0, 0, true)
   if (!trans) {
     if (!upper) { if (unit) GB_TRSV(true, true, false); else GB_TRSV(true, false, false); }
     if (unit) GB_TRSV(false, true, false);

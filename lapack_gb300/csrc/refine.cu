@@ -113,17 +113,12 @@ int latrs_dev(bool upper, bool notran, bool unit, int n, const double* A, int ld
     if (ex) GB_LAUNCH(latrs_cnorm_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(upper, n, A, lda, cnorm));
     else GB_LAUNCH(latrs_cnorm_kernel<false><<<(unsigned)((n + 7) / 8), 256, 0, s>>>(upper, n, A, lda, cnorm));
   }
-  GB_LAUNCH(latrs_plan_kernel<<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm, plan));
+  GB_LAUNCH(latrs_plan_kernel<<<1, 1, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm, plan));
   LatrsPlan hp;
   GB_CUDA_TRY(cudaMemcpyAsync(&hp, plan, sizeof(hp), cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   if (hp.mode == kLatrsCareful) {
-    if (ex)
-      GB_LAUNCH(latrs_careful_kernel<true><<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm,
-                                                                     plan));
-    else
-      GB_LAUNCH(latrs_careful_kernel<false><<<1, kCtaThreads, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm,
-                                                                      plan));
+    GB_LAUNCH(latrs_careful_kernel<<<1, 1, 0, s>>>(upper, notran, nounit, n, A, lda, x, cnorm, plan));
     return (int)cudaGetLastError();
   }
   // DTRSV (dlatrs.f:499-503, or :395 when even TMAX overflows)
@@ -282,7 +277,7 @@ int dgecon_dev(char norm, int n, const double* LU, int lda, double anorm, double
       if ((rc = latrs_dev(false, false, true, n, LU, lda, x, cl, normin_y, plans + 0, s))) return rc;
     }
     normin_y = true;
-    GB_LAUNCH(gecon_rescale_kernel<<<1, kCtaThreads, 0, s>>>(n, x, plans + 0, plans + 1, stop));
+    GB_LAUNCH(gecon_rescale_kernel<<<1, 1, 0, s>>>(n, x, plans + 0, plans + 1, stop));
     int hstop = 0;
     GB_CUDA_TRY(cudaMemcpyAsync(&hstop, stop, sizeof(int), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));

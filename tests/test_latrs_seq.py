@@ -1,0 +1,196 @@
+"""The sequential DLATRS plan / careful solve and DGECON rescaling step
+(lapack_gb300/csrc/latrs_seq.h, run on the GPU as one-thread kernels)
+compiled with g++ from the same header and composed into DLATRS and DGECON
+exactly as the library composes them (CNORM by sequential column sums, the
+plain solve by DTRSV in the reference loop order, DLACN2 for the estimate),
+then checked bit for bit against the oracle's or_dlatrs / or_dgecon
+(SRC/dlatrs.f, SRC/dgecon.f): x, SCALE and CNORM for every UPLO / TRANS /
+DIAG on well-scaled, badly scaled and overflowing triangles, and RCOND on
+the DCHKGE matrix types and on factors with tiny pivots."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "..", "lapack_gb300", "csrc")
+ORACLE_DIR = os.path.join(HERE, "..", "oracle")
+
+HARNESS = r"""
+#include <cstddef>
+#include "latrs_seq.h"
+extern "C" {
+void or_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x);
+void or_dlacn2(int n, double *v, double *x, int *isgn, double *est, int *kase, int isave[3]);
+
+// DLATRS as the library runs it: CNORM (NORMIN = 'N'), plan, then the
+// careful sweep or DTRSV.
+void seq_dlatrs(int upper, int notran, int nounit, int normin_y, int n, const double *a, int lda, double *x,
+                double *scale, double *cnorm) {
+  *scale = 1.0;
+  if (n == 0) return;
+  if (!normin_y)
+    for (int j = 0; j < n; ++j) {
+      const int i0 = upper ? 0 : j + 1, i1 = upper ? j : n;
+      double s = 0.0;
+      for (int i = i0; i < i1; ++i) s = s + fabs(a[(size_t)i + (size_t)j * lda]);
+      cnorm[j] = s;
+    }
+  gb::LatrsPlan p;
+  gb::latrs_plan_seq(upper, notran, nounit, n, a, lda, x, cnorm, &p);
+  if (p.mode == gb::kLatrsCareful) {
+    gb::latrs_careful_seq(upper, notran, nounit, n, a, lda, x, cnorm, &p);
+    *scale = p.scale;
+  } else {
+    or_dtrsv(upper ? 'U' : 'L', notran ? 'N' : 'T', nounit ? 'N' : 'U', n, a, lda, x);
+  }
+}
+
+// DGECON as the library's host loop runs it (n > 0, 0 < ANORM finite).
+double seq_dgecon(int onenrm, int n, const double *a, int lda, double anorm, double *work, int *iwork) {
+  double ainvnm = 0.0;
+  int kase = 0, isave[3] = {0, 0, 0}, normin_y = 0;
+  const int kase1 = onenrm ? 1 : 2;
+  double *x = work, *v = work + n, *cl = work + 2 * (size_t)n, *cu = work + 3 * (size_t)n;
+  for (;;) {
+    or_dlacn2(n, v, x, iwork, &ainvnm, &kase, isave);
+    if (kase == 0) break;
+    double sl = 1.0, su = 1.0;
+    if (kase == kase1) {
+      seq_dlatrs(0, 1, 0, normin_y, n, a, lda, x, &sl, cl);
+      seq_dlatrs(1, 1, 1, normin_y, n, a, lda, x, &su, cu);
+    } else {
+      seq_dlatrs(1, 0, 1, normin_y, n, a, lda, x, &su, cu);
+      seq_dlatrs(0, 0, 0, normin_y, n, a, lda, x, &sl, cl);
+    }
+    normin_y = 1;
+    if (gb::gecon_rescale_seq(n, x, sl, su)) return 0.0;
+  }
+  return ainvnm != 0.0 ? (1.0 / ainvnm) / anorm : 0.0;
+}
+}
+"""
+
+
+@pytest.fixture(scope="module")
+def seq(tmp_path_factory):
+    if shutil.which("g++") is None:
+        pytest.skip("needs g++")
+    d = tmp_path_factory.mktemp("latrs")
+    src = d / "seq.cpp"
+    src.write_text(HARNESS)
+    so = d / "libseq.so"
+    oracle.lib()   # builds liboracle.so when missing
+    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", CSRC, str(src), "-o", str(so),
+           "-L", ORACLE_DIR, "-loracle", "-Wl,-rpath," + os.path.abspath(ORACLE_DIR)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    L = ctypes.CDLL(str(so))
+    p = ctypes.c_void_p
+    L.seq_dlatrs.argtypes = [ctypes.c_int] * 5 + [p, ctypes.c_int, p, p, p]
+    L.seq_dgecon.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, ctypes.c_double, p, p]
+    L.seq_dgecon.restype = ctypes.c_double
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _seq_latrs(L, t, b, uplo, trans, diag, cnorm=None):
+    t = np.asfortranarray(t, dtype=np.float64)
+    n = t.shape[0]
+    x = np.array(b, dtype=np.float64, copy=True)
+    cn = np.zeros(max(n, 1)) if cnorm is None else np.array(cnorm, dtype=np.float64, copy=True)
+    sc = np.zeros(1)
+    L.seq_dlatrs(int(uplo == "U"), int(trans == "N"), int(diag == "N"), int(cnorm is not None), n, _ptr(t),
+                 max(1, n), _ptr(x), _ptr(sc), _ptr(cn))
+    return x, float(sc[0]), cn[:n]
+
+
+COMBOS = [(u, t, d) for u in "UL" for t in "NT" for d in "NU"]
+
+
+def _cases(uplo, diag, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for n, kind in ((1, "plain"), (7, "plain"), (120, "plain"), (6, "tiny"), (33, "tiny"), (200, "tiny"),
+                    (40, "mixed"), (25, "huge")):
+        t = rng.standard_normal((n, n))
+        if kind == "plain":
+            t[np.diag_indices(n)] = 2.0 + rng.random(n)
+        elif kind == "tiny":
+            if diag == "N":
+                t[np.diag_indices(n)] = 1e-80 * (1 + rng.random(n))
+            else:
+                t *= 1e80
+        elif kind == "mixed":
+            d = np.ones(n)
+            d[::7] = 1e-60
+            t[np.diag_indices(n)] = d
+        else:   # column sums beyond BIGNUM and beyond overflow: the TSCAL branches
+            t *= 1e300
+            t[0, n - 1] = t[n - 1, 0] = 1.7e308
+        t = np.triu(t) if uplo == "U" else np.tril(t)
+        out.append((n, kind, t, rng.standard_normal(n)))
+    return out
+
+
+@pytest.mark.parametrize("uplo,trans,diag", COMBOS)
+def test_dlatrs_seq_bitwise_vs_oracle(seq, uplo, trans, diag):
+    took_careful = False
+    for n, kind, t, b in _cases(uplo, diag, 7 + ord(uplo) * 3 + ord(trans) * 5 + ord(diag)):
+        xr, sr, cr = oracle.latrs(t, b, uplo, trans, diag)
+        xs, ss, cs = _seq_latrs(seq, t, b, uplo, trans, diag)
+        assert np.float64(ss).tobytes() == np.float64(sr).tobytes(), (n, kind, ss, sr)
+        assert xs.tobytes() == xr.tobytes(), (n, kind)
+        assert cs.tobytes() == cr.tobytes(), (n, kind)
+        took_careful |= sr < 1.0
+        # NORMIN = 'Y' with the CNORM just returned
+        xr2, sr2, _ = oracle.latrs(t, b, uplo, trans, diag, cnorm=cr)
+        xs2, ss2, _ = _seq_latrs(seq, t, b, uplo, trans, diag, cnorm=cs)
+        assert xs2.tobytes() == xr2.tobytes() and ss2 == sr2 or (np.isnan(ss2) and np.isnan(sr2))
+    assert took_careful
+
+
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_dgecon_seq_bitwise_vs_oracle(seq, imat):
+    for n in (1, 2, 5, 10, 50, 120):
+        if 5 <= imat <= 7 and n < imat - 4:
+            continue
+        a, izero = oracle.ge_test_matrix(n, n, imat, 31 + 5 * n + imat)
+        if izero:
+            continue
+        lu, ipiv, info = oracle.getrf(a)
+        luf = np.asfortranarray(lu)
+        for norm, p in (("1", 1), ("I", np.inf)):
+            anorm = np.linalg.norm(a, p)
+            r_ref, _ = oracle.gecon(lu, anorm, norm)
+            work = np.zeros(4 * n)
+            iwork = np.zeros(n, dtype=np.int32)
+            r_seq = seq.seq_dgecon(int(norm == "1"), n, _ptr(luf), n, anorm, _ptr(work), _ptr(iwork))
+            assert np.float64(r_seq).tobytes() == np.float64(r_ref).tobytes(), (n, imat, norm, r_seq, r_ref)
+
+
+@pytest.mark.parametrize("tiny", [1e-40, 1e-60, 1e-80, 1e-150])
+def test_dgecon_seq_tiny_pivots(seq, tiny):
+    """Factors whose U has tiny pivots every 7th column: the careful solve
+    and the rescaling step run; RCOND (or the early 0) equals the oracle's."""
+    n = 40
+    rng = np.random.default_rng(int(-np.log10(tiny)))
+    lu = rng.standard_normal((n, n))
+    d = np.ones(n)
+    d[::7] = tiny
+    lu[np.diag_indices(n)] = d
+    luf = np.asfortranarray(lu)
+    for norm in "1I":
+        r_ref, _ = oracle.gecon(lu, 3.0, norm)
+        work = np.zeros(4 * n)
+        iwork = np.zeros(n, dtype=np.int32)
+        r_seq = seq.seq_dgecon(int(norm == "1"), n, _ptr(luf), n, 3.0, _ptr(work), _ptr(iwork))
+        assert np.float64(r_seq).tobytes() == np.float64(r_ref).tobytes(), (tiny, norm, r_seq, r_ref)
