@@ -27,3 +27,13 @@ def exact_mode(gpu):
     old = gpu.set_option("exact", 1)
     yield
     gpu.set_option("exact", old)
+
+
+# Routines beyond the solve path itself (refinement with error bounds,
+# condition estimation) run after the solve-path tests, so that a run
+# stopped at its first failure (-x) still reports the solve path in full.
+_AFTER_SOLVE_PATH = {"test_gpu_refine.py": 1, "test_gpu_condest.py": 2}
+
+
+def pytest_collection_modifyitems(session, config, items):
+    items.sort(key=lambda it: _AFTER_SOLVE_PATH.get(it.fspath.basename, 0))
