@@ -54,6 +54,9 @@ def lib():
         L.or_dgerfs.argtypes = [_c, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p]
         L.or_dlacn2.argtypes = [_i, _p, _p, _p, _p, _p, _p]
         L.or_dgecon.argtypes = [_c, _i, _p, _i, ctypes.c_double, _p, _p, _p, _p]
+        L.or_dgesvx.argtypes = [_c, _c, _i, _i, _p, _i, _p, _i, _p, _p, _p, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p,
+                                _p]
+        L.or_dgeequ.argtypes = [_i, _i, _p, _i, _p, _p, _p, _p, _p, _p]
         L.or_dlatrs.argtypes = [_c, _c, _c, _c, _i, _p, _i, _p, _p, _p, _p]
         L.or_dtrsv.argtypes = [_c, _c, _c, _i, _p, _i, _p]
         L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
@@ -164,6 +167,46 @@ def latrs(t, x, uplo, trans, diag, cnorm=None):
     lib().or_dlatrs(uplo.encode(), trans.encode(), diag.encode(), normin, n, _ptr(t), max(1, n), _ptr(x),
                     _ptr(scale), _ptr(cn), _ptr(info))
     return x, float(scale[0]), cn[:n]
+
+
+def gesvx(a, b, fact="N", trans="N", af=None, ipiv=None, equed="N", r=None, c=None):
+    """DGESVX (SRC/dgesvx.f).  Returns a dict with the outputs: a (possibly
+    equilibrated), af, ipiv, equed, r, c, b (possibly scaled), x, rcond,
+    ferr, berr, rpvgrw (WORK(1)), info."""
+    a = _colmajor(a, np.float64).copy(order="F")
+    b2 = _colmajor(_as2d(b), np.float64).copy(order="F")
+    n, nrhs = b2.shape[0], b2.shape[1]
+    ld = max(1, n)
+    af = np.zeros((n, n), order="F") if af is None else _colmajor(af, np.float64).copy(order="F")
+    ipiv = np.zeros(ld, dtype=np.int32) if ipiv is None else np.array(ipiv, dtype=np.int32)
+    r = np.zeros(ld) if r is None else np.array(r, dtype=np.float64)
+    c = np.zeros(ld) if c is None else np.array(c, dtype=np.float64)
+    eq = ctypes.create_string_buffer(equed.encode(), 2)
+    x = np.zeros((n, nrhs), order="F")
+    rcond = np.zeros(1)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    work = np.zeros(4 * ld)
+    iwork = np.zeros(ld, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dgesvx(fact.encode(), trans.encode(), n, nrhs, _ptr(a), ld, _ptr(af), ld, _ptr(ipiv),
+                    ctypes.cast(eq, ctypes.c_void_p), _ptr(r), _ptr(c), _ptr(b2), ld, _ptr(x), ld, _ptr(rcond),
+                    _ptr(ferr), _ptr(berr), _ptr(work), _ptr(iwork), _ptr(info))
+    return dict(a=a, af=af, ipiv=ipiv[:n], equed=eq.value.decode(), r=r[:n], c=c[:n], b=b2, x=x,
+                rcond=float(rcond[0]), ferr=ferr[:nrhs], berr=berr[:nrhs], rpvgrw=float(work[0]), info=int(info[0]))
+
+
+def geequ(a):
+    """DGEEQU (SRC/dgeequ.f): returns (r, c, rowcnd, colcnd, amax, info)."""
+    a = _colmajor(a, np.float64)
+    m, n = a.shape
+    r = np.zeros(max(m, 1))
+    c = np.zeros(max(n, 1))
+    sc = np.zeros(3)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dgeequ(m, n, _ptr(a), max(1, m), _ptr(r), _ptr(c), _ptr(sc[0:]), _ptr(sc[1:]), _ptr(sc[2:]),
+                    _ptr(info))
+    return r[:m], c[:n], float(sc[0]), float(sc[1]), float(sc[2]), int(info[0])
 
 
 def gesv(a, b):

@@ -828,6 +828,193 @@ void or_dgecon(char norm, int n, const double *a, int lda, double anorm, double 
   if (isnan(*rcond) || *rcond > hugeval) *info = 1;
 }
 
+/* ---- DGEEQU: SRC/dgeequ.f:139-226.  Row scalings R(i) = 1/max_j |A(i,j)|,
+ * then column scalings C(j) = 1/max_i |A(i,j)|*R(i), each clamped to
+ * [SMLNUM, BIGNUM]; INFO = i (row i zero) or M + j (column j zero). */
+void or_dgeequ(int m, int n, const double *a, int lda, double *r, double *c, double *rowcnd, double *colcnd,
+               double *amax, int *info) {
+  *info = 0;
+  if (m < 0) *info = -1;
+  else if (n < 0) *info = -2;
+  else if (lda < (m > 1 ? m : 1)) *info = -4;
+  if (*info != 0) { or_xerbla("DGEEQU", -*info); return; }
+  if (m == 0 || n == 0) {
+    *rowcnd = 1.0;
+    *colcnd = 1.0;
+    *amax = 0.0;
+    return;
+  }
+  const double smlnum = or_dlamch('S'), bignum = 1.0 / smlnum;
+  for (int i = 0; i < m; i++) r[i] = 0.0;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) r[i] = fmax(r[i], fabs(a[i + (size_t)j * lda]));
+  double rcmin = bignum, rcmax = 0.0;
+  for (int i = 0; i < m; i++) {
+    rcmax = fmax(rcmax, r[i]);
+    rcmin = fmin(rcmin, r[i]);
+  }
+  *amax = rcmax;
+  if (rcmin == 0.0) {
+    for (int i = 0; i < m; i++)
+      if (r[i] == 0.0) { *info = i + 1; return; }
+  } else {
+    for (int i = 0; i < m; i++) r[i] = 1.0 / fmin(fmax(r[i], smlnum), bignum);
+    *rowcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+  }
+  for (int j = 0; j < n; j++) c[j] = 0.0;
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) c[j] = fmax(c[j], fabs(a[i + (size_t)j * lda]) * r[i]);
+  rcmin = bignum;
+  rcmax = 0.0;
+  for (int j = 0; j < n; j++) {
+    rcmin = fmin(rcmin, c[j]);
+    rcmax = fmax(rcmax, c[j]);
+  }
+  if (rcmin == 0.0) {
+    for (int j = 0; j < n; j++)
+      if (c[j] == 0.0) { *info = m + j + 1; return; }
+  } else {
+    for (int j = 0; j < n; j++) c[j] = 1.0 / fmin(fmax(c[j], smlnum), bignum);
+    *colcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+  }
+}
+
+/* ---- DLAQGE: SRC/dlaqge.f:145-189 (THRESH = 0.1).  Returns EQUED. */
+char or_dlaqge(int m, int n, double *a, int lda, const double *r, const double *c, double rowcnd, double colcnd,
+               double amax) {
+  const double thresh = 0.1;
+  if (m <= 0 || n <= 0) return 'N';
+  const double small = or_dlamch('S') / or_dlamch('P'), large = 1.0 / small;
+  if (rowcnd >= thresh && amax >= small && amax <= large) {
+    if (colcnd >= thresh) return 'N';
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < m; i++) a[i + (size_t)j * lda] = c[j] * a[i + (size_t)j * lda];
+    return 'C';
+  }
+  if (colcnd >= thresh) {
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < m; i++) a[i + (size_t)j * lda] = r[i] * a[i + (size_t)j * lda];
+    return 'R';
+  }
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < m; i++) a[i + (size_t)j * lda] = c[j] * r[i] * a[i + (size_t)j * lda];
+  return 'B';
+}
+
+/* ---- DLANTR('M', 'U', 'N'): SRC/dlantr.f:173-182, max |A(i,j)| over
+ * i <= min(m, j), NaN propagating. */
+double or_dlantr_mun(int m, int n, const double *a, int lda) {
+  if ((m < n ? m : n) == 0) return 0.0;
+  double value = 0.0;
+  for (int j = 1; j <= n; j++)
+    for (int i = 1; i <= (m < j ? m : j); i++) {
+      const double sum = fabs(a[(i - 1) + (size_t)(j - 1) * lda]);
+      if (value < sum || sum != sum) value = sum;
+    }
+  return value;
+}
+
+/* ---- DGESVX: SRC/dgesvx.f:350-597.  FACT 'N' / 'E' / 'F', optional
+ * equilibration, DGETRF, the reciprocal pivot growth (returned in
+ * work[0]), DGECON, DGETRS, DGERFS, unscaling; INFO = N+1 when RCOND < eps.
+ * *equed is in/out.  work: 4n doubles, iwork: n ints. */
+void or_dgesvx(char fact, char trans, int n, int nrhs, double *a, int lda, double *af, int ldaf, int *ipiv,
+               char *equed, double *r, double *c, double *b, int ldb, double *x, int ldx, double *rcond, double *ferr,
+               double *berr, double *work, int *iwork, int *info) {
+  *info = 0;
+  const int nofact = (fact == 'N' || fact == 'n'), equil = (fact == 'E' || fact == 'e');
+  const int notran = (trans == 'N' || trans == 'n');
+  int rowequ = 0, colequ = 0;
+  double smlnum = 0.0, bignum = 0.0, rowcnd = 1.0, colcnd = 1.0, amax = 0.0;
+  if (nofact || equil) {
+    *equed = 'N';
+  } else {
+    rowequ = (*equed == 'R' || *equed == 'r' || *equed == 'B' || *equed == 'b');
+    colequ = (*equed == 'C' || *equed == 'c' || *equed == 'B' || *equed == 'b');
+    smlnum = or_dlamch('S');
+    bignum = 1.0 / smlnum;
+  }
+  if (!nofact && !equil && fact != 'F' && fact != 'f') *info = -1;
+  else if (!notran && trans != 'T' && trans != 't' && trans != 'C' && trans != 'c') *info = -2;
+  else if (n < 0) *info = -3;
+  else if (nrhs < 0) *info = -4;
+  else if (lda < (n > 1 ? n : 1)) *info = -6;
+  else if (ldaf < (n > 1 ? n : 1)) *info = -8;
+  else if ((fact == 'F' || fact == 'f') && !(rowequ || colequ || *equed == 'N' || *equed == 'n')) *info = -10;
+  else {
+    if (rowequ) {
+      double rcmin = bignum, rcmax = 0.0;
+      for (int j = 0; j < n; j++) { rcmin = fmin(rcmin, r[j]); rcmax = fmax(rcmax, r[j]); }
+      if (rcmin <= 0.0) *info = -11;
+      else if (n > 0) rowcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+      else rowcnd = 1.0;
+    }
+    if (colequ && *info == 0) {
+      double rcmin = bignum, rcmax = 0.0;
+      for (int j = 0; j < n; j++) { rcmin = fmin(rcmin, c[j]); rcmax = fmax(rcmax, c[j]); }
+      if (rcmin <= 0.0) *info = -12;
+      else if (n > 0) colcnd = fmax(rcmin, smlnum) / fmin(rcmax, bignum);
+      else colcnd = 1.0;
+    }
+    if (*info == 0) {
+      if (ldb < (n > 1 ? n : 1)) *info = -14;
+      else if (ldx < (n > 1 ? n : 1)) *info = -16;
+    }
+  }
+  if (*info != 0) { or_xerbla("DGESVX", -*info); return; }
+  if (equil) {
+    int infequ = 0;
+    or_dgeequ(n, n, a, lda, r, c, &rowcnd, &colcnd, &amax, &infequ);
+    if (infequ == 0) {
+      *equed = or_dlaqge(n, n, a, lda, r, c, rowcnd, colcnd, amax);
+      rowequ = (*equed == 'R' || *equed == 'B');
+      colequ = (*equed == 'C' || *equed == 'B');
+    }
+  }
+  if (notran) {
+    if (rowequ)
+      for (int j = 0; j < nrhs; j++)
+        for (int i = 0; i < n; i++) b[i + (size_t)j * ldb] = r[i] * b[i + (size_t)j * ldb];
+  } else if (colequ) {
+    for (int j = 0; j < nrhs; j++)
+      for (int i = 0; i < n; i++) b[i + (size_t)j * ldb] = c[i] * b[i + (size_t)j * ldb];
+  }
+  if (nofact || equil) {
+    or_dlacpy(n, n, a, lda, af, ldaf);
+    or_dgetrf(n, n, af, ldaf, ipiv, info);
+    if (*info > 0) {
+      double rpvgrw = or_dlantr_mun(*info, *info, af, ldaf);
+      if (rpvgrw == 0.0) rpvgrw = 1.0;
+      else rpvgrw = or_dlange('M', n, *info, a, lda, work) / rpvgrw;
+      work[0] = rpvgrw;
+      *rcond = 0.0;
+      return;
+    }
+  }
+  const char norm = notran ? '1' : 'I';
+  const double anorm = or_dlange(norm, n, n, a, lda, work);
+  double rpvgrw = or_dlantr_mun(n, n, af, ldaf);
+  if (rpvgrw == 0.0) rpvgrw = 1.0;
+  else rpvgrw = or_dlange('M', n, n, a, lda, work) / rpvgrw;
+  or_dgecon(norm, n, af, ldaf, anorm, rcond, work, iwork, info);
+  or_dlacpy(n, nrhs, b, ldb, x, ldx);
+  or_dgetrs(trans, n, nrhs, af, ldaf, ipiv, x, ldx, info);
+  or_dgerfs(trans, n, nrhs, a, lda, af, ldaf, ipiv, b, ldb, x, ldx, ferr, berr, work, iwork, info);
+  if (notran) {
+    if (colequ) {
+      for (int j = 0; j < nrhs; j++)
+        for (int i = 0; i < n; i++) x[i + (size_t)j * ldx] = c[i] * x[i + (size_t)j * ldx];
+      for (int j = 0; j < nrhs; j++) ferr[j] = ferr[j] / colcnd;
+    }
+  } else if (rowequ) {
+    for (int j = 0; j < nrhs; j++)
+      for (int i = 0; i < n; i++) x[i + (size_t)j * ldx] = r[i] * x[i + (size_t)j * ldx];
+    for (int j = 0; j < nrhs; j++) ferr[j] = ferr[j] / rowcnd;
+  }
+  work[0] = rpvgrw;
+  if (*rcond < or_dlamch('E')) *info = n + 1;
+}
+
 /* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
  * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */
 void or_dlarnv(int idist, int iseed[4], long long n, double *x) {

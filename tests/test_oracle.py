@@ -2,6 +2,7 @@
 reference's own pins: the DLARUV multiplier table read from SRC/dlaruv.f,
 the TESTING/LIN test ratios over the TESTING/dtest.in and dstest.in grids,
 the error-exit tables, and an independent LU (OpenBLAS via scipy)."""
+import ctypes
 import json
 import os
 
@@ -161,6 +162,112 @@ def test_dlatrs_careful_path(uplo, trans, diag):
     assert np.abs(r).max() <= 1e3 * n * ck.EPS64 * np.abs(tt).max() * 1.0
 
 
+def _svx_systems(n, imat, seed):
+    """The DCHKGE test matrix and row / column scaled copies of it, so that
+    DGEEQU + DLAQGE choose EQUED = 'N', 'R', 'C' and 'B'."""
+    a, izero = oracle.ge_test_matrix(n, n, imat, seed)
+    out = [(a, izero)]
+    if n >= 2 and izero == 0:
+        g = np.random.default_rng(seed)
+        dr = 10.0 ** g.uniform(-6, 6, n)
+        dc = 10.0 ** g.uniform(-6, 6, n)
+        out += [(dr[:, None] * a, 0), (a * dc[None, :], 0), (dr[:, None] * a * dc[None, :], 0)]
+    return out
+
+
+@pytest.mark.parametrize("imat", range(1, 12))
+@pytest.mark.parametrize("fact,trans", [("N", "N"), ("E", "N"), ("E", "T"), ("N", "T")])
+def test_dgesvx_ddrvge_ratios(imat, fact, trans):
+    """DDRVGE's DGESVX checks (TESTING/LIN/ddrvge.f:518-628): INFO = IZERO
+    with RCOND = 0 for the zero-column types; otherwise DGET01 on the
+    (equilibrated) factors, DGET02 and DGET07 on the original system,
+    DGET04 against the original condition number, DGET06 against the
+    condition number of the matrix actually factored, the reciprocal pivot
+    growth recomputed from A and AF (RESULT(7)), and INFO = N+1 exactly when
+    RCOND < eps."""
+    for n in INPUTS["dtest"]["n"]:
+        if n == 0 or (5 <= imat <= 7 and n < imat - 4):
+            continue
+        for a, izero in _svx_systems(n, imat, 1991 + 3 * n + imat):
+            xact = oracle.random_matrix(n, 2, 7 + n, idist=2)[0]
+            op = a if trans == "N" else a.T
+            b = op @ xact
+            o = oracle.gesvx(a, b, fact, trans)
+            if izero:
+                assert o["info"] == izero and o["rcond"] == 0.0
+                continue
+            assert o["info"] in (0, n + 1)
+            assert (o["info"] == n + 1) == (o["rcond"] < ck.EPS64)
+            ae, af = o["a"], o["af"]
+            assert ck.dget01(ae, af, o["ipiv"]) < THRESH
+            rp = oracle.lib().or_dlantr_mun
+            rp.restype = ctypes.c_double
+            rp.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+            afc = np.asfortranarray(af)
+            u = rp(n, n, afc.ctypes.data_as(ctypes.c_void_p), n)
+            rpv = 1.0 if u == 0 else np.abs(ae).max() / u
+            assert abs(rpv - o["rpvgrw"]) / max(rpv, o["rpvgrw"]) / ck.EPS64 < THRESH
+            tr = "N" if trans == "N" else "T"
+            assert ck.dget02(a, o["x"], b, tr) < THRESH
+            p = 1 if trans == "N" else np.inf
+            rc_orig = 1.0 / np.linalg.cond(a, p)
+            assert ck.dget04(o["x"], xact, rc_orig) < THRESH
+            r1, r2 = ck.dget07(a, b, o["x"], xact, o["ferr"], o["berr"], tr)
+            assert r1 < THRESH and r2 < THRESH, (n, imat, o["equed"], r1, r2)
+            rc_eq = 1.0 / np.linalg.cond(ae, p)
+            assert ck.dget06(o["rcond"], rc_eq) < THRESH
+            # FACT = 'F' with the returned factors, scalings and the original B:
+            # the same X, BERR and RCOND bit for bit; FERR is divided by a
+            # ROWCND / COLCND that FACT = 'F' recomputes from the reciprocal
+            # scalings (dgesvx.f:395-420), equal up to rounding
+            if fact == "E":
+                f = oracle.gesvx(o["a"], b, "F", trans, af=o["af"], ipiv=o["ipiv"], equed=o["equed"], r=o["r"],
+                                 c=o["c"])
+                assert f["info"] == o["info"] and f["rcond"] == o["rcond"]
+                assert f["x"].tobytes() == o["x"].tobytes() and f["berr"].tobytes() == o["berr"].tobytes()
+                np.testing.assert_allclose(f["ferr"], o["ferr"], rtol=8 * ck.EPS64)
+
+
+EQUED_CASES = {   # 2 x 2 systems for which DGEEQU + DLAQGE pick each EQUED
+    "N": [[2.0, 1.0], [1.0, 3.0]],
+    "R": [[1e8, 2e8], [1.0, 3.0]],
+    "C": [[1.0, 1e-8], [1.0, 2e-8]],
+    "B": [[1e8, 1.0], [1.0, 2e-8]],
+}
+
+
+@pytest.mark.parametrize("equed", "NRCB")
+@pytest.mark.parametrize("trans", "NT")
+def test_dgesvx_equed_cases(equed, trans):
+    a = np.array(EQUED_CASES[equed])
+    xact = np.array([[1.0, -2.0], [3.0, 0.5]])
+    b = (a if trans == "N" else a.T) @ xact
+    o = oracle.gesvx(a, b, "E", trans)
+    assert o["equed"] == equed and o["info"] == 0
+    assert np.allclose(o["x"], xact, rtol=1e-6)
+    r1, r2 = ck.dget07(a, b, o["x"], xact, o["ferr"], o["berr"], trans)
+    assert r1 < THRESH and r2 < THRESH
+
+
+def test_dgeequ_reference_rules():
+    """DGEEQU (SRC/dgeequ.f): R and C are reciprocals of the clamped row /
+    column maxima, ROWCND / COLCND their ratios, INFO names the first zero
+    row (i) or column (M + j)."""
+    a = np.array([[4.0, 0.0, 1.0], [0.0, 0.5, 0.0], [2.0, 0.0, 8.0]])
+    r, c, rowcnd, colcnd, amax, info = oracle.geequ(a)
+    assert info == 0 and amax == 8.0
+    assert np.array_equal(r, 1.0 / np.array([4.0, 0.5, 8.0]))
+    assert np.array_equal(c, 1.0 / np.array([1.0, 1.0, 1.0]))
+    assert rowcnd == 0.5 / 8.0 and colcnd == 1.0
+    z = a.copy()
+    z[1, :] = 0.0
+    assert oracle.geequ(z)[5] == 2
+    z = a.copy()
+    z[:, 2] = 0.0
+    z[1, 1] = 1.0
+    assert oracle.geequ(z)[5] == 3 + 3
+
+
 def test_oracle_ipiv_matches_openblas():
     scipy_linalg = pytest.importorskip("scipy.linalg")
     for n, seed in ((64, 1), (200, 2), (513, 3)):
@@ -199,6 +306,7 @@ ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), -1), (("N", -1, 0, 1, 1, 1, 1), -2), (("N
              (("N", 2, 1, 1, 2, 2, 2), -5), (("N", 2, 1, 2, 1, 2, 2), -7), (("N", 2, 1, 2, 2, 1, 2), -10),
              (("N", 2, 1, 2, 2, 2, 1), -12)]                                 # TESTING/LIN/derrge.f:186-216
 ERR_GECON = [(("/", 0, 1), -1), (("1", -1, 1), -2), (("1", 2, 1), -4)]     # TESTING/LIN/derrge.f:218-229
+ERR_GEEQU = [((-1, 0, 1), -1), ((0, -1, 1), -2), ((2, 2, 1), -4)]          # TESTING/LIN/derrge.f:231-242
 
 
 def _oracle_err(fn, *args):
@@ -236,3 +344,6 @@ def test_oracle_error_exits():
     for (nm, n, lda), code in ERR_GECON:
         name, inf = _oracle_err(L.or_dgecon, nm.encode(), n, p(a), lda, 1.0, p(rc), p(w), p(iw), p(info))
         assert (name, inf) == ("DGECON", -code)
+    for (m, n, lda), code in ERR_GEEQU:
+        name, inf = _oracle_err(L.or_dgeequ, m, n, p(a), lda, p(w), p(w), p(w), p(w), p(w), p(info))
+        assert (name, inf) == ("DGEEQU", -code)
