@@ -88,6 +88,14 @@ void dgecon_(const char* norm, const lapack_int* n, const double* a, const lapac
 void dlatrs_(const char* uplo, const char* trans, const char* diag, const char* normin, const lapack_int* n,
              const double* a, const lapack_int* lda, double* x, double* scale, double* cnorm, lapack_int* info,
              size_t uplo_len, size_t trans_len, size_t diag_len, size_t normin_len);
+/* Expert driver: optional equilibration, LU, condition estimate, solve,
+ * refinement with error bounds.  Replaces SRC/dgesvx.f:344 (lapack.h:4118-4139).  WORK(1) receives the reciprocal pivot growth; IWORK
+ * is accepted and unused. */
+void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lapack_int* nrhs, double* a,
+             const lapack_int* lda, double* af, const lapack_int* ldaf, lapack_int* ipiv, char* equed, double* r,
+             double* c, double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* rcond,
+             double* ferr, double* berr, double* work, lapack_int* iwork, lapack_int* info, size_t fact_len,
+             size_t trans_len, size_t equed_len);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -214,6 +222,13 @@ int gb300_dgecon_dev(char norm, int n, const double* dA, int lda, double anorm, 
  * (n) are device arrays; *scale is a host output. */
 int gb300_dlatrs_dev(char uplo, char trans, char diag, char normin, int n, const double* dA, int lda, double* dX,
                      double* scale, double* dCnorm, void* stream);
+/* DGESVX on device memory (SRC/dgesvx.f:344): dA, dAF (n x n), dB, dX
+ * (n x nrhs), dIpiv, dR, dC (n), dFerr, dBerr (nrhs) are device arrays;
+ * *equed (in for FACT = 'F', out otherwise), *rcond, *rpvgrw (the
+ * reference's WORK(1)) and *info are host values. */
+int gb300_dgesvx_dev(char fact, char trans, int n, int nrhs, double* dA, int lda, double* dAF, int ldaf, int* dIpiv,
+                     char* equed, double* dR, double* dC, double* dB, int ldb, double* dX, int ldx, double* rcond,
+                     double* dFerr, double* dBerr, double* rpvgrw, int* info, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

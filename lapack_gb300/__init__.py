@@ -22,7 +22,7 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _sz = ctypes.c_size_t
 
 FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
-                   "dsgesv_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
+                   "dsgesv_", "dgesvx_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
                    "slamch_", "xerbla_"]
 
 
@@ -227,6 +227,34 @@ def latrs(t, x, uplo, trans, diag, cnorm=None):
     if info.value != 0:
         raise RuntimeError(f"dlatrs failed with INFO = {info.value}")
     return x, scale.value, cn[:n]
+
+
+def gesvx(a, b, fact="N", trans="N", af=None, ipiv=None, equed="N", r=None, c=None):
+    """DGESVX (SRC/dgesvx.f).  Returns a dict: a (equilibrated when
+    EQUED != 'N'), af, ipiv, equed, r, c, b (scaled as the reference leaves
+    it), x, rcond, ferr, berr, rpvgrw (WORK(1)), info."""
+    a = _fortran(a, np.float64)
+    b2 = _fortran(_as2d(b), np.float64)
+    n, nrhs = b2.shape
+    ld = max(1, n)
+    af = np.zeros((n, n), order="F") if af is None else _fortran(af, np.float64)
+    ipiv = np.zeros(ld, dtype=np.int32) if ipiv is None else np.array(ipiv, dtype=np.int32)
+    r = np.zeros(ld) if r is None else np.array(r, dtype=np.float64)
+    c = np.zeros(ld) if c is None else np.array(c, dtype=np.float64)
+    eq = ctypes.create_string_buffer(equed.encode(), 2)
+    x = np.zeros((n, nrhs), order="F")
+    rcond = ctypes.c_double(0.0)
+    ferr = np.zeros(max(nrhs, 1))
+    berr = np.zeros(max(nrhs, 1))
+    work = np.zeros(4 * ld)
+    iwork = np.zeros(ld, dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().dgesvx_(ctypes.c_char_p(fact.encode()), ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(a),
+                  _ref(ld), _ptr(af), _ref(ld), _ptr(ipiv), eq, _ptr(r), _ptr(c), _ptr(b2), _ref(ld), _ptr(x),
+                  _ref(ld), ctypes.byref(rcond), _ptr(ferr), _ptr(berr), _ptr(work), _ptr(iwork), ctypes.byref(info),
+                  _sz(1), _sz(1), _sz(1))
+    return dict(a=a, af=af, ipiv=ipiv[:n], equed=eq.value.decode(), r=r[:n], c=c[:n], b=b2, x=x,
+                rcond=rcond.value, ferr=ferr[:nrhs], berr=berr[:nrhs], rpvgrw=float(work[0]), info=info.value)
 
 
 def laswp(a, k1, k2, ipiv, incx=1):

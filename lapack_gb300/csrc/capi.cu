@@ -3,6 +3,7 @@
 // device-pointer entry points.
 #include "../../include/lapack_gb300.h"
 #include "driver.h"
+#include "latrs_seq.h"
 
 #include <algorithm>
 #include <cmath>
@@ -417,6 +418,97 @@ void dlatrs_(const char* uplo, const char* trans, const char* diag, const char* 
   if (rc) device_failure("DLATRS", rc, info);
 }
 
+namespace {
+// DGESVX argument checks (SRC/dgesvx.f:375-430); for FACT = 'F' also the
+// condition numbers of the given scalings.  Returns INFO (0 or negative).
+int gesvx_args(char fact, char trans, int n, int nrhs, int lda, int ldaf, char equed, const double* r,
+               const double* c, int ldb, int ldx, bool host_scalings, double* rowcnd, double* colcnd,
+               cudaStream_t s, int* err) {
+  const bool nofact = lsame(fact, 'N'), equil = lsame(fact, 'E');
+  bool rowequ = false, colequ = false;
+  if (!nofact && !equil) {
+    rowequ = lsame(equed, 'R') || lsame(equed, 'B');
+    colequ = lsame(equed, 'C') || lsame(equed, 'B');
+  }
+  *err = 0;
+  if (!nofact && !equil && !lsame(fact, 'F')) return -1;
+  if (!lsame(trans, 'N') && !lsame(trans, 'T') && !lsame(trans, 'C')) return -2;
+  if (n < 0) return -3;
+  if (nrhs < 0) return -4;
+  if (lda < std::max(1, n)) return -6;
+  if (ldaf < std::max(1, n)) return -8;
+  if (lsame(fact, 'F') && !(rowequ || colequ || lsame(equed, 'N'))) return -10;
+  if (rowequ) {
+    const int bad = host_scalings ? gb::scalings_cnd_seq(n, r, rowcnd) : gb::scalings_cnd_dev(n, r, rowcnd, s, err);
+    if (*err) return 0;
+    if (bad) return -11;
+  }
+  if (colequ) {
+    const int bad = host_scalings ? gb::scalings_cnd_seq(n, c, colcnd) : gb::scalings_cnd_dev(n, c, colcnd, s, err);
+    if (*err) return 0;
+    if (bad) return -12;
+  }
+  if (ldb < std::max(1, n)) return -14;
+  if (ldx < std::max(1, n)) return -16;
+  return 0;
+}
+}  // namespace
+
+void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lapack_int* nrhs, double* a,
+             const lapack_int* lda, double* af, const lapack_int* ldaf, lapack_int* ipiv, char* equed, double* r,
+             double* c, double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* rcond,
+             double* ferr, double* berr, double* work, lapack_int*, lapack_int* info, size_t, size_t, size_t) {
+  double rowcnd = 1.0, colcnd = 1.0;
+  int err = 0;
+  *info = gesvx_args(*fact, *trans, *n, *nrhs, *lda, *ldaf, *equed, r, c, *ldb, *ldx, true, &rowcnd, &colcnd,
+                     nullptr, &err);
+  if (*info != 0) { call_xerbla("DGESVX", -*info); return; }
+  const bool factored = lsame(*fact, 'F'), equil = lsame(*fact, 'E');
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  cudaStream_t s = thread_stream();
+  const size_t nn = (size_t)ld * std::max(N, 1), nr = (size_t)ld * std::max(R, 1);
+  DevScratch dA(sizeof(double) * nn, s), dAF(sizeof(double) * nn, s), dB(sizeof(double) * nr, s),
+      dX(sizeof(double) * nr, s), dV(sizeof(double) * (2 * (size_t)std::max(N, 1) + 2 * (size_t)std::max(R, 1)), s),
+      dP(sizeof(int) * std::max(N, 1), s);
+  if (!dA.p || !dAF.p || !dB.p || !dX.p || !dV.p || !dP.p) {
+    device_failure("DGESVX", (int)cudaErrorMemoryAllocation, info);
+    return;
+  }
+  double* dR = dV.as<double>();
+  double* dC = dR + std::max(N, 1);
+  double* dF = dC + std::max(N, 1);
+  double* dBe = dF + std::max(R, 1);
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  if (!rc && N > 0) rc = (int)cudaMemcpyAsync(dR, r, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+  if (!rc && N > 0) rc = (int)cudaMemcpyAsync(dC, c, sizeof(double) * N, cudaMemcpyHostToDevice, s);
+  if (!rc && factored) rc = h2d(dAF.as<double>(), ld, af, *ldaf, N, N, s);
+  if (!rc && factored && N > 0) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  char eq = factored ? *equed : 'N';
+  double rcnd = 0.0, rpv = 1.0;
+  int inf = 0;
+  if (!rc) rc = gb::dgesvx_dev(*fact, lsame(*trans, 'N') ? 'N' : 'T', N, R, dA.as<double>(), ld, dAF.as<double>(),
+                               ld, dP.as<int>(), &eq, dR, dC, dB.as<double>(), ld, dX.as<double>(), ld, rowcnd,
+                               colcnd, &rcnd, dF, dBe, &rpv, &inf, s);
+  if (!rc) rc = finish(s);
+  if (!rc && equil) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
+  if (!rc && !factored) rc = d2h(af, *ldaf, dAF.as<double>(), ld, N, N, s);
+  if (!rc && !factored && N > 0) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc && equil && N > 0) rc = (int)cudaMemcpyAsync(r, dR, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc && equil && N > 0) rc = (int)cudaMemcpyAsync(c, dC, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  const bool solved = inf == 0 || inf == N + 1;
+  if (!rc && solved) rc = d2h(b, *ldb, dB.as<double>(), ld, N, R, s);
+  if (!rc && solved) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
+  if (!rc && solved && R > 0) rc = (int)cudaMemcpyAsync(ferr, dF, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
+  if (!rc && solved && R > 0) rc = (int)cudaMemcpyAsync(berr, dBe, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DGESVX", rc, info); return; }
+  if (!factored) *equed = eq;
+  *rcond = rcnd;
+  work[0] = rpv;
+  *info = inf;
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -612,6 +704,27 @@ int gb300_dlatrs_dev(char uplo, char trans, char diag, char normin, int n, const
                           &sc, dCnorm, s);
   if (!rc) rc = finish(s);
   if (scale) *scale = sc;
+  return rc;
+}
+
+int gb300_dgesvx_dev(char fact, char trans, int n, int nrhs, double* dA, int lda, double* dAF, int ldaf, int* dIpiv,
+                     char* equed, double* dR, double* dC, double* dB, int ldb, double* dX, int ldx, double* rcond,
+                     double* dFerr, double* dBerr, double* rpvgrw, int* info, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  double rowcnd = 1.0, colcnd = 1.0;
+  int err = 0;
+  const int bad = gesvx_args(fact, trans, n, nrhs, lda, ldaf, *equed, dR, dC, ldb, ldx, false, &rowcnd, &colcnd, s,
+                             &err);
+  if (err) return err;
+  if (bad) return bad;
+  double rc_ = 0.0, rp = 1.0;
+  int inf = 0;
+  int rc = gb::dgesvx_dev(fact, lsame(trans, 'N') ? 'N' : 'T', n, nrhs, dA, lda, dAF, ldaf, dIpiv, equed, dR, dC, dB,
+                          ldb, dX, ldx, rowcnd, colcnd, &rc_, dFerr, dBerr, &rp, &inf, s);
+  if (!rc) rc = finish(s);
+  if (rcond) *rcond = rc_;
+  if (rpvgrw) *rpvgrw = rp;
+  if (info) *info = inf;
   return rc;
 }
 

@@ -66,3 +66,93 @@ gecon_rescale_kernel(int n, double* __restrict__ x, const LatrsPlan* __restrict_
 }
 
 }  // namespace gb
+
+namespace gb {
+
+// ------------------------------------------------------------- DGESVX
+// DGEEQU (SRC/dgeequ.f): row maxima R(i) = MAX_j |A(i,j)| (one thread per
+// row, columns in order), column maxima C(j) = MAX_i |A(i,j)|*R(i) (one
+// warp per column); maxima are order-free, so these equal the reference's.
+__global__ void geequ_rowmax_kernel(const double* __restrict__ A, int lda, int m, int n, double* __restrict__ r) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  double v = 0.0;
+  for (int j = 0; j < n; ++j) v = fmax(v, fabs(A[(size_t)i + (size_t)j * lda]));
+  r[i] = v;
+}
+
+__global__ void __launch_bounds__(256)
+geequ_colmax_kernel(const double* __restrict__ A, int lda, int m, int n, const double* __restrict__ r,
+                    double* __restrict__ c) {
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (j >= n) return;
+  const double* col = A + (size_t)j * lda;
+  double v = 0.0;
+  for (int i = lane; i < m; i += 32) v = fmax(v, __dmul_rn(fabs(col[i]), r[i]));
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+  if (lane == 0) c[j] = v;
+}
+
+// What DGEEQU / the FACT = 'F' check report back: condition numbers of the
+// scalings, AMAX and INFO.
+struct EquStat {
+  double rowcnd, colcnd, amax;
+  int info;
+};
+
+// DGEEQU's two finishing steps on one thread (the R step, then, when it
+// found no zero row, the C maxima must already be in c).  step 0: rows;
+// step 1: columns.
+__global__ void __launch_bounds__(1) equ_finish_kernel(int step, int m, int n, double* __restrict__ s,
+                                                       EquStat* __restrict__ st) {
+  double smax = 0.0;
+  if (step == 0) {
+    st->info = equ_finish_seq(m, s, 0, &st->rowcnd, &smax);
+    st->amax = smax;
+  } else {
+    st->info = equ_finish_seq(n, s, m, &st->colcnd, &smax);
+  }
+}
+
+// FACT = 'F': MIN(s) <= 0 check and the condition number of given R or C.
+__global__ void __launch_bounds__(1) scalings_cnd_kernel(int n, const double* __restrict__ s, double* __restrict__ cnd,
+                                                         int* __restrict__ bad) {
+  *bad = scalings_cnd_seq(n, s, cnd);
+}
+
+// A(i,j) := C(j)*A(i,j), R(i)*A(i,j) or (C(j)*R(i))*A(i,j) (DLAQGE,
+// SRC/dlaqge.f:159-186; also the right-hand-side scalings of DGESVX and
+// the unscaling of X, with c = NULL).
+__global__ void scale_rows_cols_kernel(double* __restrict__ A, int lda, int m, int n, const double* __restrict__ r,
+                                       const double* __restrict__ c) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
+  double* p = A + (size_t)i + (size_t)j * lda;
+  if (c && r) *p = __dmul_rn(__dmul_rn(c[j], r[i]), *p);
+  else if (c) *p = __dmul_rn(c[j], *p);
+  else *p = __dmul_rn(r[i], *p);
+}
+
+// max |A(i,j)| over i <= min(m-1, j) (DLANTR('M','U','N'), SRC/dlantr.f:173-182)
+// or over the whole m x n block (DLANGE('M')), NaN propagating: a NaN sets
+// *nanflag, otherwise the bit patterns of |a| are maximised.
+__global__ void max_abs_tri_kernel(const double* __restrict__ A, int lda, int m, int n, int upper,
+                                   unsigned long long* __restrict__ bits, int* __restrict__ nanflag) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * n) return;
+  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
+  if (upper && i > j) return;
+  const double v = A[(size_t)i + (size_t)j * lda];
+  if (v != v) { *nanflag = 1; return; }
+  atomicMax(bits, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+// FERR(j) := FERR(j) / cnd (dgesvx.f:566-585).
+__global__ void div_by_kernel(double* __restrict__ v, int n, double cnd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = __ddiv_rn(v[i], cnd);
+}
+
+}  // namespace gb

@@ -85,6 +85,14 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
                int* iter, int* info, cudaStream_t s);
 // DGECON on device memory: *rcond and *info are host outputs.
 int dgecon_dev(char norm, int n, const double* LU, int lda, double anorm, double* rcond, int* info, cudaStream_t s);
+// DGESVX on device memory after its argument checks (for FACT = 'F' the
+// caller passes ROWCND / COLCND of the given scalings).  *equed, *rcond,
+// *rpvgrw (WORK(1)) and *info are host values; R, C, FERR, BERR device arrays.
+int dgesvx_dev(char fact, char trans, int n, int nrhs, double* A, int lda, double* AF, int ldaf, int* ipiv,
+               char* equed, double* R, double* C, double* B, int ldb, double* X, int ldx, double rowcnd,
+               double colcnd, double* rcond, double* ferr, double* berr, double* rpvgrw, int* info, cudaStream_t s);
+// MIN(s) <= 0 test (returns 1) and MAX(min,SMLNUM)/MIN(max,BIGNUM) of device scalings.
+int scalings_cnd_dev(int n, const double* s_dev, double* cnd, cudaStream_t s, int* err);
 // DGERFS on device memory; FERR/BERR are device arrays of nrhs doubles.
 int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const double* AF, int ldaf, const int* ipiv,
                const double* B, int ldb, double* X, int ldx, double* ferr, double* berr, cudaStream_t s);

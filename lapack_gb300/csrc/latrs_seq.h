@@ -347,4 +347,41 @@ GB_HD inline int gecon_rescale_seq(int n, double* x, double sl, double su) {
   return 0;
 }
 
+// DGEEQU's finishing step for one set of scalings (SRC/dgeequ.f:166-189
+// for R, :203-225 for C): the smallest and largest of the maxima s[0..m),
+// INFO = info_base + (first zero) when one is zero, else s(i) =
+// 1/MIN(MAX(s(i), SMLNUM), BIGNUM) and *cnd = MAX(min, SMLNUM)/MIN(max,
+// BIGNUM).  *smax receives the largest maximum (AMAX for the rows).
+GB_HD inline int equ_finish_seq(int m, double* s, int info_base, double* cnd, double* smax) {
+  const double smlnum = kSafeMin, bignum = rn_div(1.0, smlnum);
+  double rcmin = bignum, rcmax = 0.0;
+  for (int i = 0; i < m; ++i) {
+    rcmax = fmax(rcmax, s[i]);
+    rcmin = fmin(rcmin, s[i]);
+  }
+  *smax = rcmax;
+  if (rcmin == 0.0) {
+    for (int i = 0; i < m; ++i)
+      if (s[i] == 0.0) return info_base + i + 1;
+  }
+  for (int i = 0; i < m; ++i) s[i] = rn_div(1.0, fmin(fmax(s[i], smlnum), bignum));
+  *cnd = rn_div(fmax(rcmin, smlnum), fmin(rcmax, bignum));
+  return 0;
+}
+
+// DGESVX's check of given scalings (FACT = 'F', SRC/dgesvx.f:395-420):
+// returns 1 when min s(i) <= 0, else 0 with *cnd = MAX(min, SMLNUM) /
+// MIN(max, BIGNUM) (1 for m = 0).
+GB_HD inline int scalings_cnd_seq(int m, const double* s, double* cnd) {
+  const double smlnum = kSafeMin, bignum = rn_div(1.0, smlnum);
+  double rcmin = bignum, rcmax = 0.0;
+  for (int i = 0; i < m; ++i) {
+    rcmin = fmin(rcmin, s[i]);
+    rcmax = fmax(rcmax, s[i]);
+  }
+  if (rcmin <= 0.0) return 1;
+  *cnd = m > 0 ? rn_div(fmax(rcmin, smlnum), fmin(rcmax, bignum)) : 1.0;
+  return 0;
+}
+
 }  // namespace gb

@@ -23,6 +23,8 @@
 #include "condest_kernels.cuh"
 
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace gb {
@@ -300,6 +302,174 @@ int dlatrs_dev(bool upper, bool trans, bool unit, bool normin_y, int n, const do
   GB_CUDA_TRY(cudaStreamSynchronize(s));
   *scale = hp.scale;
   return 0;
+}
+
+namespace {
+
+// max |A| over the upper triangle (upper) or the whole m x n block, NaN
+// propagating, into a host double.
+int max_abs_dev(const double* A, int lda, int m, int n, bool upper, double* out, cudaStream_t s) {
+  *out = 0.0;
+  if (m <= 0 || n <= 0) return 0;
+  DevScratch w(16, s);
+  if (!w.p) return (int)cudaErrorMemoryAllocation;
+  GB_CUDA_TRY(cudaMemsetAsync(w.p, 0, 16, s));
+  unsigned long long* bits = w.as<unsigned long long>();
+  int* nanflag = reinterpret_cast<int*>(w.as<char>() + 8);
+  const size_t tot = (size_t)m * n;
+  GB_LAUNCH(max_abs_tri_kernel<<<blocks256(tot), 256, 0, s>>>(A, lda, m, n, upper ? 1 : 0, bits, nanflag));
+  unsigned long long hb = 0;
+  int hn = 0;
+  GB_CUDA_TRY(cudaMemcpyAsync(&hb, bits, 8, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaMemcpyAsync(&hn, nanflag, 4, cudaMemcpyDeviceToHost, s));
+  GB_CUDA_TRY(cudaStreamSynchronize(s));
+  double v;
+  memcpy(&v, &hb, 8);
+  *out = hn ? NAN : v;
+  return 0;
+}
+
+// RPVGRW of SRC/dgesvx.f:520-545: max|A(:, 1:k)| / max|U(1:k, 1:k)|, 1 when
+// the latter is zero.
+int rpvgrw_dev(int n, int k, const double* A, int lda, const double* AF, int ldaf, double* out, cudaStream_t s) {
+  double u = 0.0, a = 0.0;
+  int rc = max_abs_dev(AF, ldaf, k, k, true, &u, s);
+  if (rc) return rc;
+  if (u == 0.0) {
+    *out = 1.0;
+    return 0;
+  }
+  if ((rc = max_abs_dev(A, lda, n, k, false, &a, s))) return rc;
+  *out = a / u;
+  return 0;
+}
+
+}  // namespace
+
+int dgesvx_dev(char fact, char trans, int n, int nrhs, double* A, int lda, double* AF, int ldaf, int* ipiv,
+               char* equed, double* R, double* C, double* B, int ldb, double* X, int ldx, double rowcnd,
+               double colcnd, double* rcond, double* ferr, double* berr, double* rpvgrw, int* info, cudaStream_t s) {
+  // SRC/dgesvx.f:350-597 after the argument checks
+  const bool nofact = (fact == 'N' || fact == 'n'), equil = (fact == 'E' || fact == 'e');
+  const bool notran = (trans == 'N' || trans == 'n');
+  bool rowequ = false, colequ = false;
+  if (nofact || equil) {
+    *equed = 'N';
+  } else {
+    rowequ = (*equed == 'R' || *equed == 'r' || *equed == 'B' || *equed == 'b');
+    colequ = (*equed == 'C' || *equed == 'c' || *equed == 'B' || *equed == 'b');
+  }
+  *info = 0;
+  *rcond = 0.0;
+  *rpvgrw = 1.0;
+  int rc;
+  if (n == 0) {
+    if (nrhs > 0) {
+      GB_CUDA_TRY(cudaMemsetAsync(ferr, 0, sizeof(double) * nrhs, s));
+      GB_CUDA_TRY(cudaMemsetAsync(berr, 0, sizeof(double) * nrhs, s));
+    }
+    *rcond = 1.0;   // DGECON's N = 0 answer; RCOND >= eps, so INFO stays 0
+    return 0;
+  }
+  if (equil) {
+    // DGEEQU, then DLAQGE's choice (THRESH = 0.1, SMALL = SMLNUM/PREC)
+    DevScratch eb(sizeof(EquStat), s);
+    if (!eb.p) return (int)cudaErrorMemoryAllocation;
+    EquStat* st = eb.as<EquStat>();
+    GB_LAUNCH(geequ_rowmax_kernel<<<blocks256(n), 256, 0, s>>>(A, lda, n, n, R));
+    GB_LAUNCH(equ_finish_kernel<<<1, 1, 0, s>>>(0, n, n, R, st));
+    EquStat hs;
+    GB_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hs.info == 0) {
+      GB_LAUNCH(geequ_colmax_kernel<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(A, lda, n, n, R, C));
+      GB_LAUNCH(equ_finish_kernel<<<1, 1, 0, s>>>(1, n, n, C, st));
+      GB_CUDA_TRY(cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s));
+      GB_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (hs.info == 0) {
+      rowcnd = hs.rowcnd;
+      colcnd = hs.colcnd;
+      const double thresh = 0.1, small = kSafeMin / kPrec, large = 1.0 / small;
+      const size_t tot = (size_t)n * n;
+      if (hs.rowcnd >= thresh && hs.amax >= small && hs.amax <= large) {
+        if (hs.colcnd >= thresh) {
+          *equed = 'N';
+        } else {
+          GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(tot), 256, 0, s>>>(A, lda, n, n, nullptr, C));
+          *equed = 'C';
+        }
+      } else if (hs.colcnd >= thresh) {
+        GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(tot), 256, 0, s>>>(A, lda, n, n, R, nullptr));
+        *equed = 'R';
+      } else {
+        GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(tot), 256, 0, s>>>(A, lda, n, n, R, C));
+        *equed = 'B';
+      }
+      rowequ = (*equed == 'R' || *equed == 'B');
+      colequ = (*equed == 'C' || *equed == 'B');
+    }
+  }
+  const size_t rhs = (size_t)n * nrhs;
+  if (nrhs > 0) {
+    if (notran && rowequ) GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(rhs), 256, 0, s>>>(B, ldb, n, nrhs, R, nullptr));
+    else if (!notran && colequ)
+      GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(rhs), 256, 0, s>>>(B, ldb, n, nrhs, C, nullptr));
+  }
+  if (nofact || equil) {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(AF, sizeof(double) * (size_t)ldaf, A, sizeof(double) * (size_t)lda,
+                                  sizeof(double) * (size_t)n, n, cudaMemcpyDeviceToDevice, s));
+    DevScratch ib(sizeof(int), s);
+    if (!ib.p) return (int)cudaErrorMemoryAllocation;
+    if ((rc = getrf_dev<double>(n, n, AF, ldaf, ipiv, ib.as<int>(), s, 0, options().nb_f64))) return rc;
+    int hinfo = 0;
+    GB_CUDA_TRY(cudaMemcpyAsync(&hinfo, ib.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hinfo > 0) {   // dgesvx.f:505-517: singular U, the pivot growth of the leading columns
+      *info = hinfo;
+      if ((rc = rpvgrw_dev(n, hinfo, A, lda, AF, ldaf, rpvgrw, s))) return rc;
+      *rcond = 0.0;
+      return 0;
+    }
+  }
+  double anorm = 0.0;
+  if ((rc = dlange_dev(notran ? 1 : 2, n, n, A, lda, &anorm, s))) return rc;
+  if ((rc = rpvgrw_dev(n, n, A, lda, AF, ldaf, rpvgrw, s))) return rc;
+  int cinfo = 0;
+  if ((rc = dgecon_dev(notran ? '1' : 'I', n, AF, ldaf, anorm, rcond, &cinfo, s))) return rc;
+  if (nrhs > 0) {
+    GB_CUDA_TRY(cudaMemcpy2DAsync(X, sizeof(double) * (size_t)ldx, B, sizeof(double) * (size_t)ldb,
+                                  sizeof(double) * (size_t)n, nrhs, cudaMemcpyDeviceToDevice, s));
+    if ((rc = getrs_dev<double>(notran ? 'N' : 'T', n, nrhs, AF, ldaf, ipiv, nullptr, X, ldx, s))) return rc;
+    if ((rc = dgerfs_dev(notran ? 'N' : 'T', n, nrhs, A, lda, AF, ldaf, ipiv, B, ldb, X, ldx, ferr, berr, s)))
+      return rc;
+    if (notran && colequ) {
+      GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(rhs), 256, 0, s>>>(X, ldx, n, nrhs, C, nullptr));
+      GB_LAUNCH(div_by_kernel<<<blocks256(nrhs), 256, 0, s>>>(ferr, nrhs, colcnd));
+    } else if (!notran && rowequ) {
+      GB_LAUNCH(scale_rows_cols_kernel<<<blocks256(rhs), 256, 0, s>>>(X, ldx, n, nrhs, R, nullptr));
+      GB_LAUNCH(div_by_kernel<<<blocks256(nrhs), 256, 0, s>>>(ferr, nrhs, rowcnd));
+    }
+  }
+  if (*rcond < 1.1102230246251565e-16) *info = n + 1;   // RCOND < DLAMCH('Epsilon')
+  return (int)cudaGetLastError();
+}
+
+// FACT = 'F' on device scalings: the MIN <= 0 check and the condition
+// number of R (which = 0) or C (which = 1); returns 1 when MIN <= 0.
+int scalings_cnd_dev(int n, const double* s_dev, double* cnd, cudaStream_t s, int* err) {
+  *err = 0;
+  *cnd = 1.0;
+  DevScratch b(sizeof(double) + sizeof(int), s);
+  if (!b.p) { *err = (int)cudaErrorMemoryAllocation; return 0; }
+  double* dc = b.as<double>();
+  int* bad = reinterpret_cast<int*>(b.as<char>() + sizeof(double));
+  GB_LAUNCH(scalings_cnd_kernel<<<1, 1, 0, s>>>(n, s_dev, dc, bad));
+  int hb = 0;
+  cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaMemcpyAsync(cnd, dc, sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) *err = (int)cudaGetLastError();
+  return hb;
 }
 
 }  // namespace gb

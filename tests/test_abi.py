@@ -51,6 +51,12 @@ ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), 1), (("N", -1, 0, 1, 1, 1, 1), 2), (("N",
 ERR_LATRS = [(("/", "N", "N", "N", 0, 1), 1), (("U", "/", "N", "N", 0, 1), 2), (("U", "N", "/", "N", 0, 1), 3),
              (("U", "N", "N", "/", 0, 1), 4), (("U", "N", "N", "N", -1, 1), 5),
              (("U", "N", "N", "N", 2, 1), 7)]       # TESTING/LIN/derrtr.f:228-247
+ERR_GESVX = [(("/", "N", 0, 0, 1, 1, "N", 1, 1), 1), (("N", "/", 0, 0, 1, 1, "N", 1, 1), 2),
+             (("N", "N", -1, 0, 1, 1, "N", 1, 1), 3), (("N", "N", 0, -1, 1, 1, "N", 1, 1), 4),
+             (("N", "N", 2, 1, 1, 2, "N", 2, 2), 6), (("N", "N", 2, 1, 2, 1, "N", 2, 2), 8),
+             (("F", "N", 0, 0, 1, 1, "/", 1, 1), 10), (("F", "N", 1, 0, 1, 1, "R", 1, 1), 11),
+             (("F", "N", 1, 0, 1, 1, "C", 1, 1), 12), (("N", "N", 2, 1, 2, 2, "N", 1, 2), 14),
+             (("N", "N", 2, 1, 2, 2, "N", 2, 1), 16)]   # TESTING/LIN/derrvx.f:151-200
 ERR_GECON = [(("/", 0, 1, 1.0), 1), (("1", -1, 1, 1.0), 2), (("1", 2, 1, 1.0), 4),
              (("1", 2, 2, -1.0), 5)]                # derrge.f:218-229, and ANORM < 0
 
@@ -95,6 +101,13 @@ def test_fortran_abi_error_exits(lib):
             lib.dlatrs_(c(ul), c(tr), c(dg), c(nm), _i(n), p(a), _i(lda), p(w), ctypes.byref(rc), p(w),
                         ctypes.byref(info), *([ctypes.c_size_t(1)] * 4))
             assert info.value == -code and g.xerbla_last() == ("DLATRS", code)
+        zero = np.zeros(4)                           # R, C with a non-positive entry
+        for (fa, tr, n, nrhs, lda, ldaf, eq, ldb, ldx), code in ERR_GESVX:
+            c = lambda ch: ctypes.c_char_p(ch.encode())
+            lib.dgesvx_(c(fa), c(tr), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldaf), p(ip), c(eq), p(zero),
+                        p(zero), p(a), _i(ldb), p(a), _i(ldx), ctypes.byref(rc), p(w), p(w), p(w), p(ip),
+                        ctypes.byref(info), *([ctypes.c_size_t(1)] * 3))
+            assert info.value == -code and g.xerbla_last() == ("DGESVX", code)
         for (nm, n, lda, anorm), code in ERR_GECON:
             lib.dgecon_(ctypes.c_char_p(nm.encode()), _i(n), p(a), _i(lda), ctypes.byref(ctypes.c_double(anorm)),
                         ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
