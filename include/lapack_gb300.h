@@ -181,6 +181,26 @@ lapack_int LAPACKE_dlag2s_work(int matrix_layout, lapack_int m, lapack_int n, co
                                float* sa, lapack_int ldsa);
 lapack_int LAPACKE_slag2d(int matrix_layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa,
                           double* a, lapack_int lda);
+/* LAPACKE/include/lapacke.h:469, 844, 1051 (dgecon, dgerfs, dgesvx) and their _work forms */
+lapack_int LAPACKE_dgecon(int matrix_layout, char norm, lapack_int n, const double* a, lapack_int lda, double anorm,
+                          double* rcond);
+lapack_int LAPACKE_dgecon_work(int matrix_layout, char norm, lapack_int n, const double* a, lapack_int lda,
+                               double anorm, double* rcond, double* work, lapack_int* iwork);
+lapack_int LAPACKE_dgerfs(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const double* a,
+                          lapack_int lda, const double* af, lapack_int ldaf, const lapack_int* ipiv, const double* b,
+                          lapack_int ldb, double* x, lapack_int ldx, double* ferr, double* berr);
+lapack_int LAPACKE_dgerfs_work(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const double* a,
+                               lapack_int lda, const double* af, lapack_int ldaf, const lapack_int* ipiv,
+                               const double* b, lapack_int ldb, double* x, lapack_int ldx, double* ferr,
+                               double* berr, double* work, lapack_int* iwork);
+lapack_int LAPACKE_dgesvx(int matrix_layout, char fact, char trans, lapack_int n, lapack_int nrhs, double* a,
+                          lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
+                          double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
+                          double* ferr, double* berr, double* rpivot);
+lapack_int LAPACKE_dgesvx_work(int matrix_layout, char fact, char trans, lapack_int n, lapack_int nrhs, double* a,
+                               lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
+                               double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
+                               double* ferr, double* berr, double* work, lapack_int* iwork);
 lapack_int LAPACKE_slag2d_work(int matrix_layout, lapack_int m, lapack_int n, const float* sa, lapack_int ldsa,
                                double* a, lapack_int lda);
 /* LAPACKE/src/lapacke_nancheck.c:97-115 */

@@ -411,4 +411,208 @@ lapack_int LAPACKE_slag2d(int layout, lapack_int m, lapack_int n, const float* s
   return LAPACKE_slag2d_work(layout, m, n, sa, ldsa, a, lda);
 }
 
+// ---------------------------------------------------------------- GECON
+// LAPACKE/src/lapacke_dgecon.c, lapacke_dgecon_work.c: NaN checks of A (-4)
+// and ANORM (-6); row-major A transposed into scratch (LDA < N: -5).
+lapack_int LAPACKE_dgecon_work(int layout, char norm, lapack_int n, const double* a, lapack_int lda, double anorm,
+                               double* rcond, double* work, lapack_int* iwork) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dgecon_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dgecon_(&norm, &n, a, &lda, &anorm, rcond, work, iwork, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  dgecon_(&norm, &n, a_t, &lda_t, &anorm, rcond, work, iwork, &info, 1);
+  if (info < 0) info -= 1;
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dgecon(int layout, char norm, lapack_int n, const double* a, lapack_int lda, double anorm,
+                          double* rcond) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgecon", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -4;
+    if (anorm != anorm) return -6;
+  }
+  lapack_int* iwork = alloc<lapack_int>((size_t)std::max(1, n));
+  double* work = iwork ? alloc<double>((size_t)std::max(1, 4 * n)) : nullptr;
+  if (!work) {
+    if (iwork) LAPACKE_free_proxy(iwork);
+    LAPACKE_xerbla("LAPACKE_dgecon", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_dgecon_work(layout, norm, n, a, lda, anorm, rcond, work, iwork);
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(iwork);
+  return info;
+}
+
+// ---------------------------------------------------------------- GERFS
+// LAPACKE/src/lapacke_dgerfs.c, lapacke_dgerfs_work.c: NaN checks of A (-5),
+// AF (-7), B (-10), X (-12); row-major: LDA, LDAF < N give -6, -8, LDB,
+// LDX < NRHS give -11, -13; only X is transposed back.
+lapack_int LAPACKE_dgerfs_work(int layout, char trans, lapack_int n, lapack_int nrhs, const double* a,
+                               lapack_int lda, const double* af, lapack_int ldaf, const lapack_int* ipiv,
+                               const double* b, lapack_int ldb, double* x, lapack_int ldx, double* ferr,
+                               double* berr, double* work, lapack_int* iwork) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dgerfs_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dgerfs_(&trans, &n, &nrhs, a, &lda, af, &ldaf, ipiv, b, &ldb, x, &ldx, ferr, berr, work, iwork, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldaf_t = std::max(1, n), ldb_t = std::max(1, n), ldx_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -6); return -6; }
+  if (ldaf < n) { LAPACKE_xerbla(nm, -8); return -8; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -11); return -11; }
+  if (ldx < nrhs) { LAPACKE_xerbla(nm, -13); return -13; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  double* af_t = a_t ? alloc<double>((size_t)ldaf_t * std::max(1, n)) : nullptr;
+  double* b_t = af_t ? alloc<double>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  double* x_t = b_t ? alloc<double>((size_t)ldx_t * std::max(1, nrhs)) : nullptr;
+  if (!x_t) {
+    if (b_t) LAPACKE_free_proxy(b_t);
+    if (af_t) LAPACKE_free_proxy(af_t);
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, n, af, ldaf, af_t, ldaf_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  ge_trans(layout, n, nrhs, x, ldx, x_t, ldx_t);
+  dgerfs_(&trans, &n, &nrhs, a_t, &lda_t, af_t, &ldaf_t, ipiv, b_t, &ldb_t, x_t, &ldx_t, ferr, berr, work, iwork,
+          &info, 1);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, x_t, ldx_t, x, ldx);
+  LAPACKE_free_proxy(x_t);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(af_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dgerfs(int layout, char trans, lapack_int n, lapack_int nrhs, const double* a, lapack_int lda,
+                          const double* af, lapack_int ldaf, const lapack_int* ipiv, const double* b, lapack_int ldb,
+                          double* x, lapack_int ldx, double* ferr, double* berr) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgerfs", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, n, af, ldaf)) return -7;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -10;
+    if (ge_has_nan(layout, n, nrhs, x, ldx)) return -12;
+  }
+  lapack_int* iwork = alloc<lapack_int>((size_t)std::max(1, n));
+  double* work = iwork ? alloc<double>((size_t)std::max(1, 3 * n)) : nullptr;
+  if (!work) {
+    if (iwork) LAPACKE_free_proxy(iwork);
+    LAPACKE_xerbla("LAPACKE_dgerfs", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_dgerfs_work(layout, trans, n, nrhs, a, lda, af, ldaf, ipiv, b, ldb, x, ldx, ferr, berr,
+                                        work, iwork);
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(iwork);
+  return info;
+}
+
+// ---------------------------------------------------------------- GESVX
+// LAPACKE/src/lapacke_dgesvx.c, lapacke_dgesvx_work.c.  NaN checks: A (-6),
+// AF when FACT = 'F' (-8), B (-14), C (-13) when FACT = 'F' and EQUED is
+// 'B' or 'C', R (-12) when FACT = 'F' and EQUED is 'B' or 'R'.  Row major:
+// LDA, LDAF < N give -7, -9, LDB, LDX < NRHS give -15, -17; AF is
+// transposed in only for FACT = 'F'; written back are A when FACT = 'E'
+// and EQUED != 'N', AF when FACT is 'E' or 'N', B when FACT = 'F' and
+// EQUED != 'N', and X.  WORK(1) (the reciprocal pivot growth) is returned
+// in *rpivot.
+namespace {
+bool lsame_c(char a, char b) { return (a | 0x20) == (b | 0x20); }
+bool vec_has_nan(lapack_int n, const double* x) {
+  for (lapack_int i = 0; i < n; ++i)
+    if (x[i] != x[i]) return true;
+  return false;
+}
+}  // namespace
+
+lapack_int LAPACKE_dgesvx_work(int layout, char fact, char trans, lapack_int n, lapack_int nrhs, double* a,
+                               lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
+                               double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
+                               double* ferr, double* berr, double* work, lapack_int* iwork) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dgesvx_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dgesvx_(&fact, &trans, &n, &nrhs, a, &lda, af, &ldaf, ipiv, equed, r, c, b, &ldb, x, &ldx, rcond, ferr, berr,
+            work, iwork, &info, 1, 1, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldaf_t = std::max(1, n), ldb_t = std::max(1, n), ldx_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -7); return -7; }
+  if (ldaf < n) { LAPACKE_xerbla(nm, -9); return -9; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -15); return -15; }
+  if (ldx < nrhs) { LAPACKE_xerbla(nm, -17); return -17; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  double* af_t = a_t ? alloc<double>((size_t)ldaf_t * std::max(1, n)) : nullptr;
+  double* b_t = af_t ? alloc<double>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  double* x_t = b_t ? alloc<double>((size_t)ldx_t * std::max(1, nrhs)) : nullptr;
+  if (!x_t) {
+    if (b_t) LAPACKE_free_proxy(b_t);
+    if (af_t) LAPACKE_free_proxy(af_t);
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  if (lsame_c(fact, 'f')) ge_trans(layout, n, n, af, ldaf, af_t, ldaf_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  dgesvx_(&fact, &trans, &n, &nrhs, a_t, &lda_t, af_t, &ldaf_t, ipiv, equed, r, c, b_t, &ldb_t, x_t, &ldx_t, rcond,
+          ferr, berr, work, iwork, &info, 1, 1, 1);
+  if (info < 0) info -= 1;
+  const bool scaled = lsame_c(*equed, 'b') || lsame_c(*equed, 'c') || lsame_c(*equed, 'r');
+  if (lsame_c(fact, 'e') && scaled) ge_trans(LAPACK_COL_MAJOR, n, n, a_t, lda_t, a, lda);
+  if (lsame_c(fact, 'e') || lsame_c(fact, 'n')) ge_trans(LAPACK_COL_MAJOR, n, n, af_t, ldaf_t, af, ldaf);
+  if (lsame_c(fact, 'f') && scaled) ge_trans(LAPACK_COL_MAJOR, n, nrhs, b_t, ldb_t, b, ldb);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, x_t, ldx_t, x, ldx);
+  LAPACKE_free_proxy(x_t);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(af_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dgesvx(int layout, char fact, char trans, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                          double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r, double* c, double* b,
+                          lapack_int ldb, double* x, lapack_int ldx, double* rcond, double* ferr, double* berr,
+                          double* rpivot) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgesvx", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, a, lda)) return -6;
+    if (lsame_c(fact, 'f') && ge_has_nan(layout, n, n, af, ldaf)) return -8;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -14;
+    if (lsame_c(fact, 'f') && (lsame_c(*equed, 'b') || lsame_c(*equed, 'c')) && vec_has_nan(n, c)) return -13;
+    if (lsame_c(fact, 'f') && (lsame_c(*equed, 'b') || lsame_c(*equed, 'r')) && vec_has_nan(n, r)) return -12;
+  }
+  lapack_int* iwork = alloc<lapack_int>((size_t)std::max(1, n));
+  double* work = iwork ? alloc<double>((size_t)std::max(1, 4 * n)) : nullptr;
+  if (!work) {
+    if (iwork) LAPACKE_free_proxy(iwork);
+    LAPACKE_xerbla("LAPACKE_dgesvx", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_dgesvx_work(layout, fact, trans, n, nrhs, a, lda, af, ldaf, ipiv, equed, r, c, b, ldb, x,
+                                        ldx, rcond, ferr, berr, work, iwork);
+  *rpivot = work[0];
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(iwork);
+  return info;
+}
+
 }  // extern "C"

@@ -19,6 +19,11 @@ void or_slaswp(int, float *, int, int, int, const int *, int);
 void or_dlag2s(int, int, const double *, int, float *, int, int *);
 void or_slag2d(int, int, const float *, int, double *, int, int *);
 void or_dsgesv(int, int, double *, int, int *, const double *, int, double *, int, double *, float *, int *, int *);
+void or_dgecon(char, int, const double *, int, double, double *, double *, int *, int *);
+void or_dgerfs(char, int, int, const double *, int, const double *, int, const int *, const double *, int, double *,
+               int, double *, double *, double *, int *, int *);
+void or_dgesvx(char, char, int, int, double *, int, double *, int, int *, char *, double *, double *, double *, int,
+               double *, int, double *, double *, double *, double *, int *, int *);
 
 void dgesv_(const int *n, const int *nrhs, double *a, const int *lda, int *ipiv, double *b, const int *ldb, int *info) {
   or_dgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
@@ -63,6 +68,27 @@ void slag2d_(const int *m, const int *n, const float *sa, const int *ldsa, doubl
 void dsgesv_(const int *n, const int *nrhs, double *a, const int *lda, int *ipiv, const double *b, const int *ldb,
              double *x, const int *ldx, double *work, float *swork, int *iter, int *info) {
   or_dsgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, work, swork, iter, info);
+}
+void dgecon_(const char *norm, const int *n, const double *a, const int *lda, const double *anorm, double *rcond,
+             double *work, int *iwork, int *info, size_t norm_len) {
+  (void)norm_len;
+  or_dgecon(*norm, *n, a, *lda, *anorm, rcond, work, iwork, info);
+}
+void dgerfs_(const char *trans, const int *n, const int *nrhs, const double *a, const int *lda, const double *af,
+             const int *ldaf, const int *ipiv, const double *b, const int *ldb, double *x, const int *ldx,
+             double *ferr, double *berr, double *work, int *iwork, int *info, size_t trans_len) {
+  (void)trans_len;
+  or_dgerfs(*trans, *n, *nrhs, a, *lda, af, *ldaf, ipiv, b, *ldb, x, *ldx, ferr, berr, work, iwork, info);
+}
+void dgesvx_(const char *fact, const char *trans, const int *n, const int *nrhs, double *a, const int *lda,
+             double *af, const int *ldaf, int *ipiv, char *equed, double *r, double *c, double *b, const int *ldb,
+             double *x, const int *ldx, double *rcond, double *ferr, double *berr, double *work, int *iwork,
+             int *info, size_t fact_len, size_t trans_len, size_t equed_len) {
+  (void)fact_len;
+  (void)trans_len;
+  (void)equed_len;
+  or_dgesvx(*fact, *trans, *n, *nrhs, a, *lda, af, *ldaf, ipiv, equed, r, c, b, *ldb, x, *ldx, rcond, ferr, berr,
+            work, iwork, info);
 }
 
 /* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */

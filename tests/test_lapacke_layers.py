@@ -146,3 +146,101 @@ def test_laswp(libs, capfd, layout, incx):
         ip = np.array([1, 3, 2, 9, 5, 5], dtype=np.int32)   # IPIV(K1..K2) = IPIV(2..6) is read
         return (layout, 4, p(a), lda, 2, 6, p(ip), incx), (a,)
     _both(libs, "LAPACKE_dlaswp", laswp, capfd)
+
+
+WIDE_CASES = [(layout, n, nrhs, extra) for layout in (101, 102) for n in (0, 1, 6, 13) for nrhs in (0, 2)
+              for extra in (0, 3)]
+
+
+def _factored(libs, n, layout, extra, seed):
+    """A, its LU (through the oracle's DGETRF) and IPIV in the given layout."""
+    import oracle
+    a, lda = _mat(n, n, seed, layout, extra)
+    lu = a.copy()
+    ip = np.zeros(max(n, 1), dtype=np.int32)
+    if n:
+        if layout == 102:
+            f = np.asfortranarray(lu[:n, :n].T)
+        else:
+            f = np.asfortranarray(lu[:n, :n])
+        lu_f, ipv, _ = oracle.getrf(f)
+        if layout == 102:
+            lu[:n, :n] = lu_f.T
+        else:
+            lu[:n, :n] = lu_f
+        ip[:n] = ipv
+    return a, lda, lu, ip
+
+
+@pytest.mark.parametrize("layout,n,nrhs,extra", WIDE_CASES)
+def test_gecon_gerfs_gesvx(libs, capfd, layout, n, nrhs, extra):
+    """LAPACKE_dgecon / dgerfs / dgesvx (and _work via them): same return
+    codes, outputs and messages as the reference wrappers."""
+    def gecon():
+        a, lda, lu, ip = _factored(libs, n, layout, extra, 40 + n)
+        rc = np.zeros(1)
+        return (layout, ctypes.c_char(b"1"), n, p(lu), lda, ctypes.c_double(3.5), p(rc)), (rc,)
+    _both(libs, "LAPACKE_dgecon", gecon, capfd)
+
+    def gerfs():
+        a, lda, lu, ip = _factored(libs, n, layout, extra, 50 + n)
+        b, ldb = _mat(n, nrhs, 51 + n, layout, extra)
+        x = b.copy()
+        fe = np.zeros(max(nrhs, 1))
+        be = np.zeros(max(nrhs, 1))
+        return ((layout, ctypes.c_char(b"N"), n, nrhs, p(a), lda, p(lu), lda, p(ip), p(b), ldb, p(x), ldb, p(fe),
+                 p(be)), (x, fe, be))
+    _both(libs, "LAPACKE_dgerfs", gerfs, capfd)
+
+    for fact in (b"N", b"E"):
+        for trans in (b"N", b"T"):
+            def gesvx():
+                a, lda = _mat(n, n, 60 + n, layout, extra)
+                if n:
+                    a[0, :] *= 1e7                     # badly scaled, so EQUED != 'N' with FACT = 'E'
+                af = np.zeros_like(a)
+                ip = np.zeros(max(n, 1), dtype=np.int32)
+                eq = ctypes.create_string_buffer(b"N", 2)
+                r = np.zeros(max(n, 1))
+                c = np.zeros(max(n, 1))
+                b, ldb = _mat(n, nrhs, 61 + n, layout, extra)
+                x = np.zeros_like(b)
+                rc = np.zeros(1)
+                fe = np.zeros(max(nrhs, 1))
+                be = np.zeros(max(nrhs, 1))
+                rp = np.zeros(1)
+                eqa = np.frombuffer(eq, dtype=np.uint8)
+                return ((layout, ctypes.c_char(fact), ctypes.c_char(trans), n, nrhs, p(a), lda, p(af), lda, p(ip),
+                         eq, p(r), p(c), p(b), ldb, p(x), ldb, p(rc), p(fe), p(be), p(rp)),
+                        (a, af, ip, eqa, r, c, b, x, rc, fe, be, rp))
+            _both(libs, "LAPACKE_dgesvx", gesvx, capfd)
+
+
+def test_gesvx_nan_and_ld_codes(libs, capfd):
+    """The NaN-check and row-major leading-dimension codes of the three
+    wrappers (including the FACT = 'F' checks of AF, R and C)."""
+    n, nrhs = 3, 1
+    for layout in (101, 102):
+        def call(fact, equed, nan_in, lda_off=0, ldb_off=0):
+            def build():
+                a, lda = _mat(n, n, 3, layout)
+                af = a.copy()
+                ip = np.array([1, 2, 3], dtype=np.int32)
+                r = np.ones(n)
+                c = np.ones(n)
+                b, ldb = _mat(n, nrhs, 4, layout)
+                x = np.zeros_like(b)
+                {"a": a, "af": af, "b": b, "r": r, "c": c}.get(nan_in, np.zeros(1))[0] = np.nan
+                eq = ctypes.create_string_buffer(equed, 2)
+                return ((layout, ctypes.c_char(fact), ctypes.c_char(b"N"), n, nrhs, p(a), lda - lda_off, p(af),
+                         lda, p(ip), eq, p(r), p(c), p(b), ldb - ldb_off, p(x), ldb, p(np.zeros(1)),
+                         p(np.zeros(1)), p(np.zeros(1)), p(np.zeros(1))), (x,))
+            return _both(libs, "LAPACKE_dgesvx", build, capfd)
+        assert call(b"N", b"N", "a") == -6
+        assert call(b"F", b"N", "af") == -8
+        assert call(b"N", b"N", "b") == -14
+        assert call(b"F", b"C", "c") == -13
+        assert call(b"F", b"R", "r") == -12
+        if layout == 101:
+            assert call(b"N", b"N", None, lda_off=1) == -7
+            assert call(b"N", b"N", None, ldb_off=1) == -15
