@@ -57,6 +57,7 @@ def lib():
         L.or_dgesvx.argtypes = [_c, _c, _i, _i, _p, _i, _p, _i, _p, _p, _p, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p,
                                 _p]
         L.or_dgeequ.argtypes = [_i, _i, _p, _i, _p, _p, _p, _p, _p, _p]
+        L.or_dgetri.argtypes = [_i, _p, _i, _p, _p, _i, _i, _p]
         L.or_dlatrs.argtypes = [_c, _c, _c, _c, _i, _p, _i, _p, _p, _p, _p]
         L.or_dtrsv.argtypes = [_c, _c, _c, _i, _p, _i, _p]
         L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
@@ -207,6 +208,19 @@ def geequ(a):
     lib().or_dgeequ(m, n, _ptr(a), max(1, m), _ptr(r), _ptr(c), _ptr(sc[0:]), _ptr(sc[1:]), _ptr(sc[2:]),
                     _ptr(info))
     return r[:m], c[:n], float(sc[0]), float(sc[1]), float(sc[2]), int(info[0])
+
+
+def getri(lu, ipiv, nb=64, lwork=None):
+    """DGETRI (SRC/dgetri.f) on a copy of the factors with block size nb;
+    returns (ainv, info, work0)."""
+    a = _colmajor(lu, np.float64).copy(order="F")
+    n = a.shape[0]
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    lw = max(1, n * max(nb, 1)) if lwork is None else lwork
+    work = np.zeros(max(1, lw, n * max(nb, 1)))
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dgetri(n, _ptr(a), max(1, n), _ptr(ipiv), _ptr(work), lw, nb, _ptr(info))
+    return a, int(info[0]), float(work[0])
 
 
 def gesv(a, b):

@@ -176,6 +176,25 @@ def dget06(rcond, rcondc, eps=None):
         return rcondc / eps
     return 0.0
 
+def dget03(a, ainv, eps=None):
+    """TESTING/LIN/dget03.f:128-157: ||I - AINV*A||_1 * RCOND / (eps * n),
+    RCOND = 1/(||A||_1 ||AINV||_1); returns (resid, rcond)."""
+    a = np.asarray(a, dtype=np.float64)
+    ainv = np.asarray(ainv, dtype=np.float64)
+    n = a.shape[0]
+    eps = EPS64 if eps is None else eps
+    if n <= 0:
+        return 0.0, 1.0
+    anorm = np.abs(a).sum(axis=0).max()
+    ainvnm = np.abs(ainv).sum(axis=0).max()
+    if anorm <= 0 or ainvnm <= 0:
+        return 1.0 / eps, 0.0
+    rcond = (1.0 / anorm) / ainvnm
+    w = -(ainv @ a)
+    w[np.diag_indices(n)] += 1.0
+    resid = np.abs(w).sum(axis=0).max()
+    return ((resid * rcond) / eps) / n, rcond
+
 def scaled_residual(a, x, b):
     """||b - A x||_inf / (||A||_inf ||x||_inf n eps): the parity measure the
     GPU result must meet (at or below the oracle's own value)."""

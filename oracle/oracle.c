@@ -1015,6 +1015,150 @@ void or_dgesvx(char fact, char trans, int n, int nrhs, double *a, int lda, doubl
   if (*rcond < or_dlamch('E')) *info = n + 1;
 }
 
+/* ---- DGETRI and the routines it calls, in the reference loop order
+ * (BLAS/SRC/dtrmv.f:226-235, dtrmm.f:271-283, dtrsm.f:333-367,
+ * SRC/dtrti2.f:128-160, dtrtri.f:149-196, dgetri.f:169-262).  NB is a
+ * parameter (ILAENV's 64 by default; the test suite varies it). */
+#define A_(i, j) a[(size_t)(i) + (size_t)(j) * lda]
+static void or_dtrmv_un(int nounit, int n, const double *a, int lda, double *x) {
+  for (int j = 0; j < n; j++) {
+    const double temp = x[j];
+    for (int i = 0; i < j; i++) x[i] = x[i] + temp * A_(i, j);
+    if (nounit) x[j] = x[j] * A_(j, j);
+  }
+}
+/* B := alpha*A*B, A upper (m x m), B m x n */
+static void or_dtrmm_lun(int nounit, int m, int n, double alpha, const double *a, int lda, double *b, int ldb) {
+  for (int j = 0; j < n; j++)
+    for (int k = 0; k < m; k++) {
+      double temp = alpha * b[k + (size_t)j * ldb];
+      for (int i = 0; i < k; i++) b[i + (size_t)j * ldb] = b[i + (size_t)j * ldb] + temp * A_(i, k);
+      if (nounit) temp = temp * A_(k, k);
+      b[k + (size_t)j * ldb] = temp;
+    }
+}
+/* B := alpha*B*inv(A), A upper (n x n) or lower, B m x n */
+static void or_dtrsm_rn(int upper, int nounit, int m, int n, double alpha, const double *a, int lda, double *b,
+                        int ldb) {
+  if (upper) {
+    for (int j = 0; j < n; j++) {
+      for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = alpha * b[i + (size_t)j * ldb];
+      for (int k = 0; k < j; k++)
+        for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = b[i + (size_t)j * ldb] - A_(k, j) * b[i + (size_t)k * ldb];
+      if (nounit)
+        for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = b[i + (size_t)j * ldb] / A_(j, j);
+    }
+  } else {
+    for (int j = n - 1; j >= 0; j--) {
+      for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = alpha * b[i + (size_t)j * ldb];
+      for (int k = j + 1; k < n; k++)
+        for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = b[i + (size_t)j * ldb] - A_(k, j) * b[i + (size_t)k * ldb];
+      if (nounit)
+        for (int i = 0; i < m; i++) b[i + (size_t)j * ldb] = b[i + (size_t)j * ldb] / A_(j, j);
+    }
+  }
+}
+/* DTRTI2 upper */
+static void or_dtrti2_u(int nounit, int n, double *a, int lda) {
+  for (int j = 0; j < n; j++) {
+    double ajj;
+    if (nounit) {
+      A_(j, j) = 1.0 / A_(j, j);
+      ajj = -A_(j, j);
+    } else {
+      ajj = -1.0;
+    }
+    or_dtrmv_un(nounit, j, a, lda, &A_(0, j));
+    or_dscal(j, ajj, &A_(0, j), 1);
+  }
+}
+/* DTRTRI('U', diag): INFO = first zero diagonal (non-unit) */
+void or_dtrtri_u(char diag, int n, double *a, int lda, int nb, int *info) {
+  const int nounit = (diag == 'N' || diag == 'n');
+  *info = 0;
+  if (n == 0) return;
+  if (nounit)
+    for (int i = 0; i < n; i++)
+      if (A_(i, i) == 0.0) { *info = i + 1; return; }
+  if (nb <= 1 || nb >= n) {
+    or_dtrti2_u(nounit, n, a, lda);
+    return;
+  }
+  for (int j = 0; j < n; j += nb) {
+    const int jb = (nb < n - j) ? nb : n - j;
+    or_dtrmm_lun(nounit, j, jb, 1.0, a, lda, &A_(0, j), lda);
+    or_dtrsm_rn(1, nounit, j, jb, -1.0, &A_(j, j), lda, &A_(0, j), lda);
+    or_dtrti2_u(nounit, jb, &A_(j, j), lda);
+  }
+}
+/* DGETRI; lwork = -1 is the workspace query (work[0] = max(1, n*nb)) */
+void or_dgetri(int n, double *a, int lda, const int *ipiv, double *work, int lwork, int nb, int *info) {
+  *info = 0;
+  const int lwkopt = (n * nb > 1) ? n * nb : 1;
+  work[0] = (double)lwkopt;
+  const int lquery = (lwork == -1);
+  if (n < 0) *info = -1;
+  else if (lda < (n > 1 ? n : 1)) *info = -3;
+  else if (lwork < (n > 1 ? n : 1) && !lquery) *info = -6;
+  if (*info != 0) { or_xerbla("DGETRI", -*info); return; }
+  if (lquery) return;
+  if (n == 0) return;
+  or_dtrtri_u('N', n, a, lda, nb, info);
+  if (*info > 0) return;
+  int nbmin = 2;
+  const int ldwork = n;
+  int iws;
+  if (nb > 1 && nb < n) {
+    iws = (ldwork * nb > 1) ? ldwork * nb : 1;
+    if (lwork < iws) {
+      nb = lwork / ldwork;
+      nbmin = 2;   /* ILAENV(2, 'DGETRI') */
+    }
+  } else {
+    iws = n;
+  }
+  if (nb < nbmin || nb >= n) {
+    for (int j = n - 1; j >= 0; j--) {
+      for (int i = j + 1; i < n; i++) {
+        work[i] = A_(i, j);
+        A_(i, j) = 0.0;
+      }
+      if (j < n - 1) {
+        /* DGEMV('N', N, N-J, -1, A(1,J+1), LDA, WORK(J+1), 1, 1, A(1,J), 1) */
+        for (int jj = j + 1; jj < n; jj++) {
+          const double temp = -1.0 * work[jj];
+          for (int i = 0; i < n; i++) A_(i, j) = A_(i, j) + temp * A_(i, jj);
+        }
+      }
+    }
+  } else {
+    const int nn = ((n - 1) / nb) * nb;
+    for (int j = nn; j >= 0; j -= nb) {
+      const int jb = (nb < n - j) ? nb : n - j;
+      for (int jj = j; jj < j + jb; jj++)
+        for (int i = jj + 1; i < n; i++) {
+          work[i + (size_t)(jj - j) * ldwork] = A_(i, jj);
+          A_(i, jj) = 0.0;
+        }
+      if (j + jb < n)
+        or_dgemm('N', 'N', n, jb, n - j - jb, -1.0, &A_(0, j + jb), lda, work + j + jb, ldwork, 1.0, &A_(0, j),
+                 lda);
+      or_dtrsm_rn(0, 0, n, jb, 1.0, work + j, ldwork, &A_(0, j), lda);
+    }
+  }
+  for (int j = n - 2; j >= 0; j--) {
+    const int jp = ipiv[j] - 1;
+    if (jp != j)
+      for (int i = 0; i < n; i++) {
+        const double t = A_(i, j);
+        A_(i, j) = A_(i, jp);
+        A_(i, jp) = t;
+      }
+  }
+  work[0] = (double)iws;
+}
+#undef A_
+
 /* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
  * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */
 void or_dlarnv(int idist, int iseed[4], long long n, double *x) {

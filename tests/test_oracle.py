@@ -268,6 +268,44 @@ def test_dgeequ_reference_rules():
     assert oracle.geequ(z)[5] == 3 + 3
 
 
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_dgetri_dchkge_ratio(imat):
+    """DCHKGE test 2 (TESTING/LIN/dchkge.f:383-420): DGET03 < THRESH for the
+    inverse from the factors, for every square N and every NB of dtest.in
+    (NB = 1 and NB >= N take the unblocked loop); INFO = i for the first
+    zero pivot of the zero-column types."""
+    for n in INPUTS["dtest"]["n"]:
+        if 5 <= imat <= 7 and n < imat - 4:
+            continue
+        a, izero = oracle.ge_test_matrix(n, n, imat, 1988 + 7 * n + n)
+        lu, ipiv, info = oracle.getrf(a)
+        for nb in sorted(set(INPUTS["dtest"]["nb"])) + [64]:
+            ainv, info, _ = oracle.getri(lu, ipiv, nb=nb)
+            if izero:
+                assert info > 0 and lu[info - 1, info - 1] == 0.0
+                continue
+            assert info == 0
+            if n:
+                assert ck.dget03(a, ainv)[0] < THRESH, (n, imat, nb)
+
+
+def test_dgetri_workspace_rules():
+    """LWORK = -1 returns N*NB in WORK(1) and does nothing else; a workspace
+    below N*NB shrinks the block size (dgetri.f:200-216) with the same
+    result up to rounding; LWORK < N is argument 6."""
+    a = oracle.random_matrix(40, 40, 3, idist=3)[0]
+    lu, ipiv, _ = oracle.getrf(a)
+    _, info, w0 = oracle.getri(lu, ipiv, nb=16, lwork=-1)
+    assert info == 0 and w0 == 40 * 16
+    x1, _, _ = oracle.getri(lu, ipiv, nb=16)
+    x2, info, w0 = oracle.getri(lu, ipiv, nb=16, lwork=40 * 5)
+    assert info == 0 and w0 == 40 * 16
+    np.testing.assert_allclose(x2, x1, rtol=1e-9, atol=1e-12)
+    oracle.xerbla_reset()
+    _, info, _ = oracle.getri(lu, ipiv, nb=16, lwork=39)
+    assert info == -6 and oracle.xerbla_last() == ("DGETRI", 6)
+
+
 def test_oracle_ipiv_matches_openblas():
     scipy_linalg = pytest.importorskip("scipy.linalg")
     for n, seed in ((64, 1), (200, 2), (513, 3)):
@@ -306,6 +344,7 @@ ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), -1), (("N", -1, 0, 1, 1, 1, 1), -2), (("N
              (("N", 2, 1, 1, 2, 2, 2), -5), (("N", 2, 1, 2, 1, 2, 2), -7), (("N", 2, 1, 2, 2, 1, 2), -10),
              (("N", 2, 1, 2, 2, 2, 1), -12)]                                 # TESTING/LIN/derrge.f:186-216
 ERR_GECON = [(("/", 0, 1), -1), (("1", -1, 1), -2), (("1", 2, 1), -4)]     # TESTING/LIN/derrge.f:218-229
+ERR_GETRI = [((-1, 1, 64), -1), ((2, 1, 64), -3)]                          # TESTING/LIN/derrge.f:157-165
 ERR_GEEQU = [((-1, 0, 1), -1), ((0, -1, 1), -2), ((2, 2, 1), -4)]          # TESTING/LIN/derrge.f:231-242
 
 
@@ -344,6 +383,10 @@ def test_oracle_error_exits():
     for (nm, n, lda), code in ERR_GECON:
         name, inf = _oracle_err(L.or_dgecon, nm.encode(), n, p(a), lda, 1.0, p(rc), p(w), p(iw), p(info))
         assert (name, inf) == ("DGECON", -code)
+    wk = np.zeros(256)
+    for (n, lda, lw), code in ERR_GETRI:
+        name, inf = _oracle_err(L.or_dgetri, n, p(a), lda, p(ip), p(wk), lw, 64, p(info))
+        assert (name, inf) == ("DGETRI", -code)
     for (m, n, lda), code in ERR_GEEQU:
         name, inf = _oracle_err(L.or_dgeequ, m, n, p(a), lda, p(w), p(w), p(w), p(w), p(w), p(info))
         assert (name, inf) == ("DGEEQU", -code)
