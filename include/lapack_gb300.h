@@ -96,6 +96,11 @@ void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lap
              double* c, double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* rcond,
              double* ferr, double* berr, double* work, lapack_int* iwork, lapack_int* info, size_t fact_len,
              size_t trans_len, size_t equed_len);
+/* Inverse from the LU factors.  Replaces SRC/dgetri.f:111
+ * (lapack.h:4398-4404).  LWORK = -1 is the workspace query (WORK(1) = N*NB);
+ * a smaller LWORK shrinks the block size as the reference does. */
+void dgetri_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* ipiv, double* work,
+             const lapack_int* lwork, lapack_int* info);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -197,6 +202,10 @@ lapack_int LAPACKE_dgesvx(int matrix_layout, char fact, char trans, lapack_int n
                           lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
                           double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
                           double* ferr, double* berr, double* rpivot);
+/* LAPACKE/include/lapacke.h:1153 (dgetri) and its _work form */
+lapack_int LAPACKE_dgetri(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv);
+lapack_int LAPACKE_dgetri_work(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv,
+                               double* work, lapack_int lwork);
 lapack_int LAPACKE_dgesvx_work(int matrix_layout, char fact, char trans, lapack_int n, lapack_int nrhs, double* a,
                                lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
                                double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
@@ -249,6 +258,10 @@ int gb300_dlatrs_dev(char uplo, char trans, char diag, char normin, int n, const
 int gb300_dgesvx_dev(char fact, char trans, int n, int nrhs, double* dA, int lda, double* dAF, int ldaf, int* dIpiv,
                      char* equed, double* dR, double* dC, double* dB, int ldb, double* dX, int ldx, double* rcond,
                      double* dFerr, double* dBerr, double* rpvgrw, int* info, void* stream);
+/* DGETRI on device memory (SRC/dgetri.f:111): dA holds the LU factors
+ * and receives inv(A); dIpiv on the device; *info host.  No workspace
+ * argument: the library's scratch is stream ordered. */
+int gb300_dgetri_dev(int n, double* dA, int lda, const int* dIpiv, int* info, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

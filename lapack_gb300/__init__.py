@@ -22,7 +22,7 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _sz = ctypes.c_size_t
 
 FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
-                   "dsgesv_", "dgesvx_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
+                   "dsgesv_", "dgesvx_", "dgetri_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
                    "slamch_", "xerbla_"]
 
 
@@ -57,6 +57,7 @@ def lib():
         L.gb300_dgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
         L.gb300_dsgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _ip, _ip, _p]
         L.gb300_dgecon_dev.argtypes = [ctypes.c_char, _i, _p, _i, ctypes.c_double, _p, _ip, _p]
+        L.gb300_dgetri_dev.argtypes = [_i, _p, _i, _p, _ip, _p]
         L.gb300_dgerfs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p]
         _LIB = L
     return _LIB
@@ -255,6 +256,20 @@ def gesvx(a, b, fact="N", trans="N", af=None, ipiv=None, equed="N", r=None, c=No
                   _sz(1), _sz(1), _sz(1))
     return dict(a=a, af=af, ipiv=ipiv[:n], equed=eq.value.decode(), r=r[:n], c=c[:n], b=b2, x=x,
                 rcond=rcond.value, ferr=ferr[:nrhs], berr=berr[:nrhs], rpvgrw=float(work[0]), info=info.value)
+
+
+def getri(lu, ipiv, lwork=None):
+    """DGETRI (SRC/dgetri.f) on a copy of the factors; returns (ainv, info,
+    work0).  lwork = -1 is the workspace query."""
+    a = _fortran(lu, np.float64)
+    n = a.shape[0]
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    nb = max(1, get_option("nb64"))
+    lw = max(1, n * nb) if lwork is None else lwork
+    work = np.zeros(max(1, lw, n * nb))
+    info = ctypes.c_int(0)
+    lib().dgetri_(_ref(n), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(work), _ref(lw), ctypes.byref(info))
+    return a, info.value, float(work[0])
 
 
 def laswp(a, k1, k2, ipiv, incx=1):

@@ -509,6 +509,41 @@ void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lap
   *info = inf;
 }
 
+void dgetri_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* ipiv, double* work,
+             const lapack_int* lwork, lapack_int* info) {
+  // SRC/dgetri.f:169-197: workspace query and argument checks; NB is the
+  // library's FP64 block size (64 by default, ILAENV's value)
+  *info = 0;
+  int nb = options().nb_f64;
+  const int N = *n;
+  work[0] = (double)std::max(1, N * nb);
+  const bool lquery = (*lwork == -1);
+  if (N < 0) *info = -1;
+  else if (*lda < std::max(1, N)) *info = -3;
+  else if (*lwork < std::max(1, N) && !lquery) *info = -6;
+  if (*info != 0) { call_xerbla("DGETRI", -*info); return; }
+  if (lquery || N == 0) return;
+  int iws = N;
+  if (nb > 1 && nb < N) {
+    iws = std::max(N * nb, 1);
+    if (*lwork < iws) nb = *lwork / N;   // dgetri.f:203-210 (NBMIN = 2 below)
+  }
+  const int nb_run = (nb < 2) ? 1 : nb;
+  cudaStream_t s = thread_stream();
+  const int ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dP.p) { device_failure("DGETRI", (int)cudaErrorMemoryAllocation, info); return; }
+  int inf = 0;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::dgetri_dev(N, dA.as<double>(), ld, dP.as<int>(), nb_run, &inf, s);
+  if (!rc && inf == 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DGETRI", rc, info); return; }
+  *info = inf;
+  if (inf == 0) work[0] = (double)iws;
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -724,6 +759,17 @@ int gb300_dgesvx_dev(char fact, char trans, int n, int nrhs, double* dA, int lda
   if (!rc) rc = finish(s);
   if (rcond) *rcond = rc_;
   if (rpvgrw) *rpvgrw = rp;
+  if (info) *info = inf;
+  return rc;
+}
+
+int gb300_dgetri_dev(int n, double* dA, int lda, const int* dIpiv, int* info, void* stream) {
+  if (n < 0) return -1;
+  if (lda < std::max(1, n)) return -3;
+  cudaStream_t s = (cudaStream_t)stream;
+  int inf = 0;
+  int rc = gb::dgetri_dev(n, dA, lda, dIpiv, options().nb_f64, &inf, s);
+  if (!rc) rc = finish(s);
   if (info) *info = inf;
   return rc;
 }

@@ -156,3 +156,62 @@ __global__ void div_by_kernel(double* __restrict__ v, int n, double cnd) {
 }
 
 }  // namespace gb
+
+#include "getri_seq.h"
+
+namespace gb {
+
+// ------------------------------------------------------------- DGETRI
+// First zero on the diagonal (DTRTRI's INFO, SRC/dtrtri.f:134-139): the
+// smallest such index, 1-based, by an order-free atomicMin.
+__global__ void first_zero_diag_kernel(const double* __restrict__ A, int lda, int n, int* __restrict__ first) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && A[(size_t)i + (size_t)i * lda] == 0.0) atomicMin(first, i + 1);
+}
+
+// B := A*B (DTRMM left, upper, non-unit, ALPHA = 1) from the copy B0.
+__global__ void trmm_lun_kernel(int m, int ncols, const double* __restrict__ A, int lda, const double* __restrict__ B0,
+                                int ldb0, double* __restrict__ B, int ldb) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * ncols) return;
+  const int c = (int)(e / m), i = (int)(e - (size_t)c * m);
+  B[(size_t)i + (size_t)c * ldb] = trmm_lun_elem(i, c, m, A, lda, B0, ldb0);
+}
+
+// B := ALPHA*B*inv(T), one thread per row of B.
+__global__ void trsm_rn_kernel(int m, int upper, int nounit, int n, double alpha, const double* __restrict__ T,
+                               int ldt, double* __restrict__ B, int ldb) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) trsm_rn_row(i, upper, nounit, n, alpha, T, ldt, B, ldb);
+}
+
+// DTRTI2 of one diagonal block (at most the block size), on one thread.
+__global__ void __launch_bounds__(1) trti2_upper_kernel(int n, double* __restrict__ A, int lda) {
+  trti2_upper_seq(n, A, lda);
+}
+
+// WORK(:, c) = the strictly lower part of column j0 + c, which is then zeroed
+// (dgetri.f:222-226, 236-241); rows <= j0 + c of WORK are left as they are.
+__global__ void getri_take_l_kernel(int n, int j0, int jb, double* __restrict__ A, int lda, double* __restrict__ W,
+                                    int ldw) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)n * jb) return;
+  const int c = (int)(e / n), i = (int)(e - (size_t)c * n);
+  const int jj = j0 + c;
+  if (i <= jj) return;
+  double* a = A + (size_t)i + (size_t)jj * lda;
+  W[(size_t)i + (size_t)c * ldw] = *a;
+  *a = 0.0;
+}
+
+__global__ void getri_gemv_kernel(int n, int j, double* __restrict__ A, int lda, const double* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) getri_gemv_row(i, j, n, A, lda, w);
+}
+
+__global__ void getri_swap_kernel(int n, double* __restrict__ A, int lda, const int* __restrict__ ipiv) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) getri_swap_row(i, n, A, lda, ipiv);
+}
+
+}  // namespace gb

@@ -615,4 +615,50 @@ lapack_int LAPACKE_dgesvx(int layout, char fact, char trans, lapack_int n, lapac
   return info;
 }
 
+// ---------------------------------------------------------------- GETRI
+// LAPACKE/src/lapacke_dgetri.c, lapacke_dgetri_work.c: NaN check of A (-3);
+// the workspace is sized by a query; row major: LDA < N gives -4, the query
+// passes LDA_T, A is transposed in and out.
+lapack_int LAPACKE_dgetri_work(int layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv,
+                               double* work, lapack_int lwork) {
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dgetri_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dgetri_(&n, a, &lda, ipiv, work, &lwork, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -4); return -4; }
+  if (lwork == -1) {
+    dgetri_(&n, a, &lda_t, ipiv, work, &lwork, &info);
+    return (info < 0) ? (info - 1) : info;
+  }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  ge_trans(layout, n, n, a, lda, a_t, lda_t);
+  dgetri_(&n, a_t, &lda_t, ipiv, work, &lwork, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, n, a_t, lda_t, a, lda);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dgetri(int layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dgetri", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, n, n, a, lda)) return -3;
+  double query = 0.0;
+  lapack_int info = LAPACKE_dgetri_work(layout, n, a, lda, ipiv, &query, -1);
+  if (info != 0) return info;
+  const lapack_int lwork = (lapack_int)query;
+  double* work = static_cast<double*>(LAPACKE_malloc_proxy(sizeof(double) * (size_t)lwork));
+  if (!work) {
+    LAPACKE_xerbla("LAPACKE_dgetri", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  info = LAPACKE_dgetri_work(layout, n, a, lda, ipiv, work, lwork);
+  LAPACKE_free_proxy(work);
+  return info;
+}
+
 }  // extern "C"

@@ -472,4 +472,78 @@ int scalings_cnd_dev(int n, const double* s_dev, double* cnd, cudaStream_t s, in
   return hb;
 }
 
+// DGETRI on device memory (SRC/dgetri.f:169-262) with block size nb (the
+// reference's ILAENV value is 64): DTRTRI of U by block columns (DTRMM with
+// the inverse so far, DTRSM with the diagonal block, DTRTI2 of the diagonal
+// block), then inv(A) from inv(U) and L by block columns right to left
+// (DGEMM through the library's update kernel, DTRSM with the unit lower
+// block), then the column interchanges.  *info: 0, or the first zero
+// pivot of U (A untouched then, as DTRTRI returns before any work).
+int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cudaStream_t s) {
+  *info = 0;
+  if (n <= 0) return 0;
+  {
+    DevScratch fz(sizeof(int), s);
+    if (!fz.p) return (int)cudaErrorMemoryAllocation;
+    const int big = 0x7fffffff;
+    GB_CUDA_TRY(cudaMemcpyAsync(fz.p, &big, sizeof(int), cudaMemcpyHostToDevice, s));
+    GB_LAUNCH(first_zero_diag_kernel<<<blocks256(n), 256, 0, s>>>(A, lda, n, fz.as<int>()));
+    int h = big;
+    GB_CUDA_TRY(cudaMemcpyAsync(&h, fz.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (h != big) {
+      *info = h;
+      return 0;
+    }
+  }
+  const int nbe = std::max(1, nb);
+  // ---- DTRTRI('U', 'N')
+  if (nbe <= 1 || nbe >= n) {
+    GB_LAUNCH(trti2_upper_kernel<<<1, 1, 0, s>>>(n, A, lda));
+  } else {
+    DevScratch cp(sizeof(double) * (size_t)n * nbe, s);
+    if (!cp.p) return (int)cudaErrorMemoryAllocation;
+    for (int j = 0; j < n; j += nbe) {
+      const int jb = std::min(nbe, n - j);
+      double* Bj = A + (size_t)j * lda;   // rows 0..j-1 of block column j
+      if (j > 0) {
+        GB_CUDA_TRY(cudaMemcpy2DAsync(cp.p, sizeof(double) * (size_t)j, Bj, sizeof(double) * (size_t)lda,
+                                      sizeof(double) * (size_t)j, jb, cudaMemcpyDeviceToDevice, s));
+        GB_LAUNCH(trmm_lun_kernel<<<blocks256((size_t)j * jb), 256, 0, s>>>(j, jb, A, lda, cp.as<double>(), j, Bj,
+                                                                             lda));
+        GB_LAUNCH(trsm_rn_kernel<<<blocks256(j), 256, 0, s>>>(j, 1, 1, jb, -1.0, A + j + (size_t)j * lda, lda, Bj,
+                                                              lda));
+      }
+      GB_LAUNCH(trti2_upper_kernel<<<1, 1, 0, s>>>(jb, A + j + (size_t)j * lda, lda));
+    }
+  }
+  // ---- inv(A) * L = inv(U)
+  const int ldw = n;
+  DevScratch wb(sizeof(double) * (size_t)ldw * nbe, s);
+  if (!wb.p) return (int)cudaErrorMemoryAllocation;
+  double* W = wb.as<double>();
+  int rc;
+  if (nbe < 2 || nbe >= n) {
+    for (int j = n - 1; j >= 0; --j) {
+      GB_LAUNCH(getri_take_l_kernel<<<blocks256(n), 256, 0, s>>>(n, j, 1, A, lda, W, ldw));
+      if (j < n - 1) GB_LAUNCH(getri_gemv_kernel<<<blocks256(n), 256, 0, s>>>(n, j, A, lda, W));
+    }
+  } else {
+    const int nn = ((n - 1) / nbe) * nbe;
+    for (int j = nn; j >= 0; j -= nbe) {
+      const int jb = std::min(nbe, n - j);
+      GB_LAUNCH(getri_take_l_kernel<<<blocks256((size_t)n * jb), 256, 0, s>>>(n, j, jb, A, lda, W, ldw));
+      if (j + jb < n) {
+        // A(:, j:j+jb) -= A(:, j+jb:n) * WORK(j+jb:n, 0:jb)   (DGEMM, alpha = -1, beta = 1)
+        if ((rc = gemm_update_dev<double>(n, jb, n - j - jb, A + (size_t)(j + jb) * lda, lda, W + j + jb, ldw,
+                                          A + (size_t)j * lda, lda, s, 0)))
+          return rc;
+      }
+      GB_LAUNCH(trsm_rn_kernel<<<blocks256(n), 256, 0, s>>>(n, 0, 0, jb, 1.0, W + j, ldw, A + (size_t)j * lda, lda));
+    }
+  }
+  GB_LAUNCH(getri_swap_kernel<<<blocks256(n), 256, 0, s>>>(n, A, lda, ipiv));
+  return (int)cudaGetLastError();
+}
+
 }  // namespace gb

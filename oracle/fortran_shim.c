@@ -20,6 +20,7 @@ void or_dlag2s(int, int, const double *, int, float *, int, int *);
 void or_slag2d(int, int, const float *, int, double *, int, int *);
 void or_dsgesv(int, int, double *, int, int *, const double *, int, double *, int, double *, float *, int *, int *);
 void or_dgecon(char, int, const double *, int, double, double *, double *, int *, int *);
+void or_dgetri(int, double *, int, const int *, double *, int, int, int *);
 void or_dgerfs(char, int, int, const double *, int, const double *, int, const int *, const double *, int, double *,
                int, double *, double *, double *, int *, int *);
 void or_dgesvx(char, char, int, int, double *, int, double *, int, int *, char *, double *, double *, double *, int,
@@ -89,6 +90,9 @@ void dgesvx_(const char *fact, const char *trans, const int *n, const int *nrhs,
   (void)equed_len;
   or_dgesvx(*fact, *trans, *n, *nrhs, a, *lda, af, *ldaf, ipiv, equed, r, c, b, *ldb, x, *ldx, rcond, ferr, berr,
             work, iwork, info);
+}
+void dgetri_(const int *n, double *a, const int *lda, const int *ipiv, double *work, const int *lwork, int *info) {
+  or_dgetri(*n, a, *lda, ipiv, work, *lwork, 64, info);   /* NB = ILAENV(1, 'DGETRI') = 64 */
 }
 
 /* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */

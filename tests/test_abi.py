@@ -57,6 +57,7 @@ ERR_GESVX = [(("/", "N", 0, 0, 1, 1, "N", 1, 1), 1), (("N", "/", 0, 0, 1, 1, "N"
              (("F", "N", 0, 0, 1, 1, "/", 1, 1), 10), (("F", "N", 1, 0, 1, 1, "R", 1, 1), 11),
              (("F", "N", 1, 0, 1, 1, "C", 1, 1), 12), (("N", "N", 2, 1, 2, 2, "N", 1, 2), 14),
              (("N", "N", 2, 1, 2, 2, "N", 2, 1), 16)]   # TESTING/LIN/derrvx.f:151-200
+ERR_GETRI = [((-1, 1, 1), 1), ((2, 1, 4), 3), ((2, 2, 1), 6)]   # TESTING/LIN/derrge.f:157-165, and LWORK < N
 ERR_GECON = [(("/", 0, 1, 1.0), 1), (("1", -1, 1, 1.0), 2), (("1", 2, 1, 1.0), 4),
              (("1", 2, 2, -1.0), 5)]                # derrge.f:218-229, and ANORM < 0
 
@@ -108,6 +109,12 @@ def test_fortran_abi_error_exits(lib):
                         p(zero), p(a), _i(ldb), p(a), _i(ldx), ctypes.byref(rc), p(w), p(w), p(w), p(ip),
                         ctypes.byref(info), *([ctypes.c_size_t(1)] * 3))
             assert info.value == -code and g.xerbla_last() == ("DGESVX", code)
+        for (n, lda, lw), code in ERR_GETRI:
+            lib.dgetri_(_i(n), p(a), _i(lda), p(ip), p(w), _i(lw), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("DGETRI", code)
+        wq = np.zeros(2)
+        lib.dgetri_(_i(10), p(a), _i(10), p(ip), p(wq), _i(-1), ctypes.byref(info))   # workspace query: no GPU work
+        assert info.value == 0 and wq[0] == 10 * g.get_option("nb64")
         for (nm, n, lda, anorm), code in ERR_GECON:
             lib.dgecon_(ctypes.c_char_p(nm.encode()), _i(n), p(a), _i(lda), ctypes.byref(ctypes.c_double(anorm)),
                         ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))

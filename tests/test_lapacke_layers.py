@@ -244,3 +244,17 @@ def test_gesvx_nan_and_ld_codes(libs, capfd):
         if layout == 101:
             assert call(b"N", b"N", None, lda_off=1) == -7
             assert call(b"N", b"N", None, ldb_off=1) == -15
+
+
+@pytest.mark.parametrize("layout,n,extra", [(l, n, e) for l in (101, 102) for n in (0, 1, 6, 13, 70) for e in (0, 3)])
+def test_getri(libs, capfd, layout, n, extra):
+    """LAPACKE_dgetri (workspace query, then the inverse) and its error codes."""
+    def getri():
+        a, lda, lu, ip = _factored(libs, n, layout, extra, 80 + n)
+        return (layout, n, p(lu), lda, p(ip)), (lu,)
+    _both(libs, "LAPACKE_dgetri", getri, capfd)
+
+    def bad_ld():
+        a, lda, lu, ip = _factored(libs, max(n, 2), layout, 0, 81)
+        return (layout, max(n, 2), p(lu), lda - 1, p(ip)), (lu,)
+    _both(libs, "LAPACKE_dgetri", bad_ld, capfd)

@@ -1,12 +1,15 @@
-"""The sequential DLATRS plan / careful solve and DGECON rescaling step
-(lapack_gb300/csrc/latrs_seq.h, run on the GPU as one-thread kernels)
-compiled with g++ from the same header and composed into DLATRS and DGECON
-exactly as the library composes them (CNORM by sequential column sums, the
-plain solve by DTRSV in the reference loop order, DLACN2 for the estimate),
-then checked bit for bit against the oracle's or_dlatrs / or_dgecon
-(SRC/dlatrs.f, SRC/dgecon.f): x, SCALE and CNORM for every UPLO / TRANS /
-DIAG on well-scaled, badly scaled and overflowing triangles, and RCOND on
-the DCHKGE matrix types and on factors with tiny pivots."""
+"""Host/device code checked on the CPU.  The sequential DLATRS plan, careful
+solve and DGECON rescaling step (lapack_gb300/csrc/latrs_seq.h, run on the
+GPU as one-thread kernels) and the element steps of DGETRI
+(lapack_gb300/csrc/getri_seq.h, one GPU thread each) are compiled with g++
+from the same headers and composed exactly as the library composes them
+(CNORM by sequential column sums, the plain solve by DTRSV in the reference
+loop order, DLACN2 for the estimate; DGEMM for DGETRI's update), then
+checked bit for bit against the oracle (SRC/dlatrs.f, SRC/dgecon.f,
+SRC/dgetri.f): x, SCALE and CNORM for every UPLO / TRANS / DIAG on
+well-scaled, badly scaled and overflowing triangles; RCOND on the DCHKGE
+matrix types and on factors with tiny pivots; the inverse for blocked and
+unblocked block sizes."""
 import ctypes
 import os
 import shutil
@@ -23,9 +26,62 @@ ORACLE_DIR = os.path.join(HERE, "..", "oracle")
 
 HARNESS = r"""
 #include <cstddef>
+#include <vector>
 #include "latrs_seq.h"
+#include "getri_seq.h"
 extern "C" {
 void or_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x);
+void or_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *a, int lda, const double *b, int ldb,
+              double beta, double *c, int ldc);
+
+// DGETRI as the library's GPU driver runs it: each kernel's per-thread
+// function applied to every thread index, the update through DGEMM.
+int seq_dgetri(int n, double *a, int lda, const int *ipiv, int nb) {
+  for (int i = 0; i < n; ++i)
+    if (a[(size_t)i + (size_t)i * lda] == 0.0) return i + 1;
+  if (nb <= 1 || nb >= n) {
+    gb::trti2_upper_seq(n, a, lda);
+  } else {
+    std::vector<double> cp((size_t)n * nb);
+    for (int j = 0; j < n; j += nb) {
+      const int jb = nb < n - j ? nb : n - j;
+      double *bj = a + (size_t)j * lda;
+      if (j > 0) {
+        for (int c = 0; c < jb; ++c)
+          for (int i = 0; i < j; ++i) cp[(size_t)i + (size_t)c * j] = bj[(size_t)i + (size_t)c * lda];
+        for (int c = 0; c < jb; ++c)
+          for (int i = 0; i < j; ++i) bj[(size_t)i + (size_t)c * lda] = gb::trmm_lun_elem(i, c, j, a, lda, cp.data(), j);
+        for (int i = 0; i < j; ++i) gb::trsm_rn_row(i, 1, 1, jb, -1.0, a + j + (size_t)j * lda, lda, bj, lda);
+      }
+      gb::trti2_upper_seq(jb, a + j + (size_t)j * lda, lda);
+    }
+  }
+  const int ldw = n;
+  std::vector<double> w((size_t)ldw * (nb > 1 ? nb : 1));
+  if (nb < 2 || nb >= n) {
+    for (int j = n - 1; j >= 0; --j) {
+      for (int i = j + 1; i < n; ++i) { w[i] = a[(size_t)i + (size_t)j * lda]; a[(size_t)i + (size_t)j * lda] = 0.0; }
+      if (j < n - 1)
+        for (int i = 0; i < n; ++i) gb::getri_gemv_row(i, j, n, a, lda, w.data());
+    }
+  } else {
+    const int nn = ((n - 1) / nb) * nb;
+    for (int j = nn; j >= 0; j -= nb) {
+      const int jb = nb < n - j ? nb : n - j;
+      for (int c = 0; c < jb; ++c)
+        for (int i = j + c + 1; i < n; ++i) {
+          w[(size_t)i + (size_t)c * ldw] = a[(size_t)i + (size_t)(j + c) * lda];
+          a[(size_t)i + (size_t)(j + c) * lda] = 0.0;
+        }
+      if (j + jb < n)
+        or_dgemm('N', 'N', n, jb, n - j - jb, -1.0, a + (size_t)(j + jb) * lda, lda, w.data() + j + jb, ldw, 1.0,
+                 a + (size_t)j * lda, lda);
+      for (int i = 0; i < n; ++i) gb::trsm_rn_row(i, 0, 0, jb, 1.0, w.data() + j, ldw, a + (size_t)j * lda, lda);
+    }
+  }
+  for (int i = 0; i < n; ++i) gb::getri_swap_row(i, n, a, lda, ipiv);
+  return 0;
+}
 void or_dlacn2(int n, double *v, double *x, int *isgn, double *est, int *kase, int isave[3]);
 
 // DLATRS as the library runs it: CNORM (NORMIN = 'N'), plan, then the
@@ -95,6 +151,7 @@ def seq(tmp_path_factory):
     L.seq_dlatrs.argtypes = [ctypes.c_int] * 5 + [p, ctypes.c_int, p, p, p]
     L.seq_dgecon.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, ctypes.c_double, p, p]
     L.seq_dgecon.restype = ctypes.c_double
+    L.seq_dgetri.argtypes = [ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
     return L
 
 
@@ -194,3 +251,23 @@ def test_dgecon_seq_tiny_pivots(seq, tiny):
         iwork = np.zeros(n, dtype=np.int32)
         r_seq = seq.seq_dgecon(int(norm == "1"), n, _ptr(luf), n, 3.0, _ptr(work), _ptr(iwork))
         assert np.float64(r_seq).tobytes() == np.float64(r_ref).tobytes(), (tiny, norm, r_seq, r_ref)
+
+
+@pytest.mark.parametrize("nb", [1, 3, 20, 64, 200])
+def test_dgetri_seq_bitwise_vs_oracle(seq, nb):
+    """The DGETRI element steps composed as the GPU driver composes them
+    give the oracle's DGETRI bit for bit, blocked and unblocked, over the
+    DCHKGE types; the zero-pivot INFO matches."""
+    for n in (1, 2, 7, 65, 130):
+        for imat in (1, 4, 6, 9):
+            if imat == 6 and n < 2:
+                continue
+            a, izero = oracle.ge_test_matrix(n, n, imat, 11 + n + imat)
+            lu, ipiv, info = oracle.getrf(a)
+            ref, rinfo, _ = oracle.getri(lu, ipiv, nb=nb)
+            got = np.asfortranarray(lu.copy())
+            ip = np.ascontiguousarray(ipiv, dtype=np.int32)
+            ginfo = seq.seq_dgetri(n, _ptr(got), n, _ptr(ip), nb)
+            assert ginfo == rinfo, (n, imat, nb)
+            if rinfo == 0:
+                assert got.tobytes() == np.asfortranarray(ref).tobytes(), (n, imat, nb)
