@@ -1,15 +1,16 @@
 """Host/device code checked on the CPU.  The sequential DLATRS plan, careful
 solve and DGECON rescaling step (lapack_gb300/csrc/latrs_seq.h, run on the
-GPU as one-thread kernels) and the element steps of DGETRI
-(lapack_gb300/csrc/getri_seq.h, one GPU thread each) are compiled with g++
+GPU as one-thread kernels), DGEEQU's finishing steps and the element steps
+of DGETRI (lapack_gb300/csrc/getri_seq.h, one GPU thread each) are compiled
+with g++
 from the same headers and composed exactly as the library composes them
 (CNORM by sequential column sums, the plain solve by DTRSV in the reference
 loop order, DLACN2 for the estimate; DGEMM for DGETRI's update), then
 checked bit for bit against the oracle (SRC/dlatrs.f, SRC/dgecon.f,
 SRC/dgetri.f): x, SCALE and CNORM for every UPLO / TRANS / DIAG on
 well-scaled, badly scaled and overflowing triangles; RCOND on the DCHKGE
-matrix types and on factors with tiny pivots; the inverse for blocked and
-unblocked block sizes."""
+matrix types and on factors with tiny pivots; R, C and the condition
+numbers of DGEEQU; the inverse for blocked and unblocked block sizes."""
 import ctypes
 import os
 import shutil
@@ -33,6 +34,27 @@ extern "C" {
 void or_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x);
 void or_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *a, int lda, const double *b, int ldb,
               double beta, double *c, int ldc);
+
+// DGEEQU as the library's GPU kernels compute it: row maxima (one thread
+// per row), the row finishing step, column maxima of |A|*R (any order: a
+// maximum), the column finishing step.
+int seq_dgeequ(int m, int n, const double *a, int lda, double *r, double *c, double *rowcnd, double *colcnd,
+               double *amax) {
+  for (int i = 0; i < m; ++i) {
+    double v = 0.0;
+    for (int j = 0; j < n; ++j) v = fmax(v, fabs(a[(size_t)i + (size_t)j * lda]));
+    r[i] = v;
+  }
+  int info = gb::equ_finish_seq(m, r, 0, rowcnd, amax);
+  if (info) return info;
+  for (int j = 0; j < n; ++j) {
+    double v = 0.0;
+    for (int i = m - 1; i >= 0; --i) v = fmax(v, fabs(a[(size_t)i + (size_t)j * lda]) * r[i]);
+    c[j] = v;
+  }
+  double cmax;
+  return gb::equ_finish_seq(n, c, m, colcnd, &cmax);
+}
 
 // DGETRI as the library's GPU driver runs it: each kernel's per-thread
 // function applied to every thread index, the update through DGEMM.
@@ -152,6 +174,7 @@ def seq(tmp_path_factory):
     L.seq_dgecon.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, ctypes.c_double, p, p]
     L.seq_dgecon.restype = ctypes.c_double
     L.seq_dgetri.argtypes = [ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
+    L.seq_dgeequ.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, p, p, p]
     return L
 
 
@@ -271,3 +294,38 @@ def test_dgetri_seq_bitwise_vs_oracle(seq, nb):
             assert ginfo == rinfo, (n, imat, nb)
             if rinfo == 0:
                 assert got.tobytes() == np.asfortranarray(ref).tobytes(), (n, imat, nb)
+
+
+def test_dgeequ_seq_bitwise_vs_oracle(seq):
+    """DGEEQU as the GPU kernels compute it (maxima in another order, the
+    finishing steps of latrs_seq.h) equals the oracle's DGEEQU bit for bit:
+    R, C, ROWCND, COLCND, AMAX and INFO, on random, badly scaled,
+    zero-row, zero-column and extreme-range matrices."""
+    rng = np.random.default_rng(4)
+    cases = []
+    for m, n in ((1, 1), (5, 5), (40, 33), (70, 70)):
+        a = rng.standard_normal((m, n))
+        cases.append(a)
+        cases.append(a * 10.0 ** rng.uniform(-200, 200, (m, 1)) * 10.0 ** rng.uniform(-100, 100, (1, n)))
+        if m > 2:
+            z = a.copy()
+            z[2, :] = 0.0
+            cases.append(z)
+            z = a.copy()
+            z[:, n - 1] = 0.0
+            cases.append(z)
+    cases.append(np.array([[1e-320, 1.0], [3.0, 1e308]]))
+    for a in cases:
+        m, n = a.shape
+        rr, cr, rowr, colr, amr, infr = oracle.geequ(a)
+        af = np.asfortranarray(a)
+        r = np.zeros(m)
+        c = np.zeros(n)
+        sc = np.zeros(3)
+        info = seq.seq_dgeequ(m, n, _ptr(af), m, _ptr(r), _ptr(c), _ptr(sc[0:]), _ptr(sc[1:]), _ptr(sc[2:]))
+        assert info == infr
+        assert r.tobytes() == rr.tobytes() and sc[2] == amr
+        if infr == 0:
+            assert c.tobytes() == cr.tobytes() and sc[0] == rowr and sc[1] == colr
+        elif infr > m:
+            assert sc[0] == rowr
