@@ -58,6 +58,12 @@ def lib():
                                 _p]
         L.or_dgeequ.argtypes = [_i, _i, _p, _i, _p, _p, _p, _p, _p, _p]
         L.or_dgetri.argtypes = [_i, _p, _i, _p, _p, _i, _i, _p]
+        for pre in "ds":
+            getattr(L, f"or_{pre}potrf_nb").argtypes = [_c, _i, _p, _i, _p, _i]
+            getattr(L, f"or_{pre}potrs").argtypes = [_c, _i, _i, _p, _i, _p, _i, _p]
+        L.or_dsposv.argtypes = [_c, _i, _i, _p, _i, _p, _i, _p, _i, _p, _p, _p, _p]
+        L.or_dlansy.argtypes = [_c, _c, _i, _p, _i, _p]
+        L.or_dlansy.restype = ctypes.c_double
         L.or_dlatrs.argtypes = [_c, _c, _c, _c, _i, _p, _i, _p, _p, _p, _p]
         L.or_dtrsv.argtypes = [_c, _c, _c, _i, _p, _i, _p]
         L.or_dlag2s.argtypes = [_i, _i, _p, _i, _p, _i, _p]
@@ -221,6 +227,68 @@ def getri(lu, ipiv, nb=64, lwork=None):
     info = np.zeros(1, dtype=np.int32)
     lib().or_dgetri(n, _ptr(a), max(1, n), _ptr(ipiv), _ptr(work), lw, nb, _ptr(info))
     return a, int(info[0]), float(work[0])
+
+
+def spd_matrix(n, cond, seed, uplo="L", junk=1e300, dtype=np.float64):
+    """A symmetric positive definite test matrix Q diag(d) Q^T with d
+    geometric from 1 to 1/cond (Q from the QR of a seeded N(0,1) matrix);
+    only the `uplo` triangle is meaningful, the other holds `junk` so that a
+    routine reading it is caught."""
+    if n == 0:
+        return np.zeros((0, 0), dtype=dtype)
+    g = random_matrix(n, n, seed, idist=3)[0]
+    q, _ = np.linalg.qr(g)
+    d = cond ** (-np.arange(n) / max(n - 1, 1))
+    a = (q * d) @ q.T
+    a = (a + a.T) / 2
+    full = a.astype(dtype)
+    out = np.tril(full) if uplo == "L" else np.triu(full)
+    mask = np.triu(np.ones((n, n), bool), 1) if uplo == "L" else np.tril(np.ones((n, n), bool), -1)
+    out[mask] = junk
+    return out
+
+
+def potrf(a, uplo="L", nb=64):
+    """xPOTRF (SRC/dpotrf.f) with block size nb: returns (factor, info)."""
+    dt = np.dtype(a.dtype if a.dtype in (np.float32, np.float64) else np.float64)
+    a = _colmajor(a, dt).copy(order="F")
+    n = a.shape[0]
+    info = np.zeros(1, dtype=np.int32)
+    getattr(lib(), f"or_{_pre(a)}potrf_nb")(uplo.encode(), n, _ptr(a), max(1, n), _ptr(info), nb)
+    return a, int(info[0])
+
+
+def potrs(f, b, uplo="L"):
+    """xPOTRS (SRC/dpotrs.f): returns (x, info)."""
+    dt = f.dtype
+    f = _colmajor(f, dt)
+    b2 = _colmajor(_as2d(b), dt).copy(order="F")
+    n, nrhs = b2.shape
+    info = np.zeros(1, dtype=np.int32)
+    getattr(lib(), f"or_{_pre(f)}potrs")(uplo.encode(), n, nrhs, _ptr(f), max(1, n), _ptr(b2), max(1, n),
+                                          _ptr(info))
+    return b2.reshape(np.asarray(b).shape), int(info[0])
+
+
+def dsposv(a, b, uplo="L"):
+    """DSPOSV (SRC/dsposv.f): returns (a_out, x, iter, info)."""
+    a = _colmajor(a, np.float64).copy(order="F")
+    b2 = _colmajor(_as2d(b), np.float64)
+    n, nrhs = b2.shape
+    x = np.zeros((n, nrhs), order="F")
+    work = np.zeros(max(1, n * nrhs))
+    swork = np.zeros(max(1, n * (n + nrhs)), dtype=np.float32)
+    it = np.zeros(1, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_dsposv(uplo.encode(), n, nrhs, _ptr(a), max(1, n), _ptr(b2), max(1, n), _ptr(x), max(1, n),
+                    _ptr(work), _ptr(swork), _ptr(it), _ptr(info))
+    return a, x.reshape(np.asarray(b).shape), int(it[0]), int(info[0])
+
+
+def dlansy(norm, uplo, a):
+    a = _colmajor(a, np.float64)
+    n = a.shape[0]
+    return lib().or_dlansy(norm.encode(), uplo.encode(), n, _ptr(a), max(1, n), _ptr(np.zeros(max(1, n))))
 
 
 def gesv(a, b):

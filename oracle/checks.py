@@ -195,6 +195,78 @@ def dget03(a, ainv, eps=None):
     resid = np.abs(w).sum(axis=0).max()
     return ((resid * rcond) / eps) / n, rcond
 
+def _sym_full(a, uplo):
+    a = np.asarray(a, dtype=np.float64)
+    t = np.tril(a) if uplo == "L" else np.triu(a)
+    return t + t.T - np.diag(np.diag(t))
+
+
+def dpot01(a, f, uplo="L", eps=None):
+    """TESTING/LIN/dpot01.f: ||L L^T - A||_1 / (n ||A||_1 eps) (or U^T U),
+    reading only the `uplo` triangles of A and of the factor."""
+    n = a.shape[0]
+    if n <= 0:
+        return 0.0
+    eps = EPS64 if eps is None else eps
+    af = _sym_full(a, uplo)
+    anorm = np.abs(af).sum(axis=0).max()
+    if anorm <= 0:
+        return 1.0 / eps
+    f = np.asarray(f, dtype=np.float64)
+    t = np.tril(f) if uplo == "L" else np.triu(f)
+    prod = t @ t.T if uplo == "L" else t.T @ t
+    return ((np.abs(prod - af).sum(axis=0).max() / n) / anorm) / eps
+
+
+def dpot02(a, x, b, uplo="L", eps=None):
+    """TESTING/LIN/dpot02.f: max_j ||b_j - A x_j||_1 / (||A||_1 ||x_j||_1 eps)."""
+    af = _sym_full(a, uplo)
+    n = af.shape[0]
+    eps = EPS64 if eps is None else eps
+    x = np.asarray(x, dtype=np.float64).reshape(n, -1)
+    b = np.asarray(b, dtype=np.float64).reshape(n, -1)
+    if n <= 0:
+        return 0.0
+    anorm = np.abs(af).sum(axis=0).max()
+    if anorm <= 0:
+        return 1.0 / eps
+    r = b - af @ x
+    out = 0.0
+    for j in range(x.shape[1]):
+        xn = np.abs(x[:, j]).sum()
+        if xn <= 0:
+            return 1.0 / eps
+        out = max(out, ((np.abs(r[:, j]).sum() / anorm) / xn) / eps)
+    return out
+
+
+def dpot06(a, x, b, uplo="L", eps=None):
+    """TESTING/LIN/dpot06.f: max_j ||b_j - A x_j||_inf / (||A||_inf ||x_j||_inf
+    eps), the residual by the oracle's restatement of DSYMM (the call DPOT06
+    makes) and ||A|| by DLANSY('I'), so the ratio is the reference test's."""
+    import ctypes
+    import oracle
+    a = np.asfortranarray(np.asarray(a, dtype=np.float64))
+    n = a.shape[0]
+    eps = EPS64 if eps is None else eps
+    x = np.asfortranarray(np.asarray(x, dtype=np.float64).reshape(n, -1))
+    r = np.asfortranarray(np.array(b, dtype=np.float64).reshape(n, -1))
+    if n <= 0:
+        return 0.0
+    anorm = oracle.dlansy("I", uplo, a)
+    if anorm <= 0:
+        return 1.0 / eps
+    L = oracle.lib()
+    L.or_dsymm_l.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_double] + \
+        [ctypes.c_void_p, ctypes.c_int] * 3
+    pp = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    L.or_dsymm_l(uplo.encode(), n, x.shape[1], -1.0, pp(a), n, pp(x), n, pp(r), n)
+    out = 0.0
+    for j in range(x.shape[1]):
+        xn = np.abs(x[:, j]).max()
+        out = max(out, ((np.abs(r[:, j]).max() / anorm) / xn) / eps)
+    return out
+
 def scaled_residual(a, x, b):
     """||b - A x||_inf / (||A||_inf ||x||_inf n eps): the parity measure the
     GPU result must meet (at or below the oracle's own value)."""

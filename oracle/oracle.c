@@ -76,6 +76,7 @@ float or_slamch(char c) {
 #define ABS_T fabs
 #define SFMIN_T DBL_MIN
 #include "oracle_lu.inc"
+#include "oracle_chol.inc"
 #undef T
 #undef P
 #undef PNAME
@@ -88,6 +89,7 @@ float or_slamch(char c) {
 #define ABS_T fabsf
 #define SFMIN_T FLT_MIN
 #include "oracle_lu.inc"
+#include "oracle_chol.inc"
 #undef T
 #undef P
 #undef PNAME
@@ -1158,6 +1160,155 @@ void or_dgetri(int n, double *a, int lda, const int *ipiv, double *work, int lwo
   work[0] = (double)iws;
 }
 #undef A_
+
+/* ---- DLANSY ('M', 'I' / '1' / 'O'): SRC/dlansy.f:144-200.  work: n. */
+double or_dlansy(char norm, char uplo, int n, const double *a, int lda, double *work) {
+  const int upper = (uplo == 'U' || uplo == 'u');
+  double value = 0.0;
+  if (n == 0) return 0.0;
+  if (norm == 'M' || norm == 'm') {
+    for (int j = 0; j < n; j++) {
+      const int i0 = upper ? 0 : j, i1 = upper ? j : n - 1;
+      for (int i = i0; i <= i1; i++) {
+        const double sum = fabs(a[i + (size_t)j * lda]);
+        if (value < sum || sum != sum) value = sum;
+      }
+    }
+  } else if (upper) {
+    for (int j = 0; j < n; j++) {
+      double sum = 0.0;
+      for (int i = 0; i < j; i++) {
+        const double absa = fabs(a[i + (size_t)j * lda]);
+        sum = sum + absa;
+        work[i] = work[i] + absa;
+      }
+      work[j] = sum + fabs(a[j + (size_t)j * lda]);
+    }
+    for (int i = 0; i < n; i++) {
+      const double sum = work[i];
+      if (value < sum || sum != sum) value = sum;
+    }
+  } else {
+    for (int i = 0; i < n; i++) work[i] = 0.0;
+    for (int j = 0; j < n; j++) {
+      double sum = work[j] + fabs(a[j + (size_t)j * lda]);
+      for (int i = j + 1; i < n; i++) {
+        const double absa = fabs(a[i + (size_t)j * lda]);
+        sum = sum + absa;
+        work[i] = work[i] + absa;
+      }
+      if (value < sum || sum != sum) value = sum;
+    }
+  }
+  return value;
+}
+
+/* ---- DLAT2S: SRC/dlat2s.f:128-158.  Stops with INFO = 1 at the first
+ * element of the triangle (column order) outside [-RMAX, RMAX]. */
+void or_dlat2s(char uplo, int n, const double *a, int lda, float *sa, int ldsa, int *info) {
+  const double rmax = (double)or_slamch('O');
+  const int upper = (uplo == 'U' || uplo == 'u');
+  *info = 0;
+  for (int j = 0; j < n; j++) {
+    const int i0 = upper ? 0 : j, i1 = upper ? j : n - 1;
+    for (int i = i0; i <= i1; i++) {
+      const double v = a[i + (size_t)j * lda];
+      if (v < -rmax || v > rmax) { *info = 1; return; }
+      sa[i + (size_t)j * ldsa] = (float)v;
+    }
+  }
+}
+
+/* ---- DSYMM('L', uplo), C := alpha*A*B + C (BETA = 1): BLAS/SRC/dsymm.f:289-323. */
+void or_dsymm_l(char uplo, int m, int n, double alpha, const double *a, int lda, const double *b, int ldb, double *c,
+                int ldc) {
+  const int upper = (uplo == 'U' || uplo == 'u');
+  if (m == 0 || n == 0 || alpha == 0.0) return;
+  for (int j = 0; j < n; j++) {
+    if (upper) {
+      for (int i = 0; i < m; i++) {
+        const double temp1 = alpha * b[i + (size_t)j * ldb];
+        double temp2 = 0.0;
+        for (int k = 0; k < i; k++) {
+          c[k + (size_t)j * ldc] = c[k + (size_t)j * ldc] + temp1 * a[k + (size_t)i * lda];
+          temp2 = temp2 + b[k + (size_t)j * ldb] * a[k + (size_t)i * lda];
+        }
+        c[i + (size_t)j * ldc] = c[i + (size_t)j * ldc] + temp1 * a[i + (size_t)i * lda] + alpha * temp2;
+      }
+    } else {
+      for (int i = m - 1; i >= 0; i--) {
+        const double temp1 = alpha * b[i + (size_t)j * ldb];
+        double temp2 = 0.0;
+        for (int k = i + 1; k < m; k++) {
+          c[k + (size_t)j * ldc] = c[k + (size_t)j * ldc] + temp1 * a[k + (size_t)i * lda];
+          temp2 = temp2 + b[k + (size_t)j * ldb] * a[k + (size_t)i * lda];
+        }
+        c[i + (size_t)j * ldc] = c[i + (size_t)j * ldc] + temp1 * a[i + (size_t)i * lda] + alpha * temp2;
+      }
+    }
+  }
+}
+
+/* ---- DSPOSV: SRC/dsposv.f:237-420 (ITERMAX = 30, BWDMAX = 1).
+ * work: n*nrhs doubles, swork: n*(n+nrhs) floats. */
+void or_dsposv(char uplo, int n, int nrhs, double *a, int lda, const double *b, int ldb, double *x, int ldx,
+               double *work, float *swork, int *iter, int *info) {
+  const int itermax = 30;
+  const double bwdmax = 1.0;
+  *info = 0;
+  *iter = 0;
+  if (uplo != 'U' && uplo != 'u' && uplo != 'L' && uplo != 'l') *info = -1;
+  else if (n < 0) *info = -2;
+  else if (nrhs < 0) *info = -3;
+  else if (lda < (n > 1 ? n : 1)) *info = -5;
+  else if (ldb < (n > 1 ? n : 1)) *info = -7;
+  else if (ldx < (n > 1 ? n : 1)) *info = -9;
+  if (*info != 0) { or_xerbla("DSPOSV", -*info); return; }
+  if (n == 0) return;
+  const double anrm = or_dlansy('I', uplo, n, a, lda, work);
+  const double eps = or_dlamch('E');
+  const double cte = anrm * eps * sqrt((double)n) * bwdmax;
+  float *sa = swork;
+  float *sx = swork + (size_t)n * n;
+  int i;
+  or_dlag2s(n, nrhs, b, ldb, sx, n, info);
+  if (*info != 0) { *iter = -2; goto fallback; }
+  or_dlat2s(uplo, n, a, lda, sa, n, info);
+  if (*info != 0) { *iter = -2; goto fallback; }
+  or_spotrf(uplo, n, sa, n, info);
+  if (*info != 0) { *iter = -3; goto fallback; }
+  or_spotrs(uplo, n, nrhs, sa, n, sx, n, info);
+  or_slag2d(n, nrhs, sx, n, x, ldx, info);
+  or_dlacpy(n, nrhs, b, ldb, work, n);
+  or_dsymm_l(uplo, n, nrhs, -1.0, a, lda, x, ldx, work, n);
+  for (i = 0; i < nrhs; i++) {
+    const double xnrm = fabs(x[(size_t)(or_diamax(n, x + (size_t)i * ldx, 1) - 1) + (size_t)i * ldx]);
+    const double rnrm = fabs(work[(size_t)(or_diamax(n, work + (size_t)i * n, 1) - 1) + (size_t)i * n]);
+    if (rnrm > xnrm * cte) break;
+  }
+  if (i == nrhs) { *iter = 0; return; }
+  for (int iiter = 1; iiter <= itermax; iiter++) {
+    or_dlag2s(n, nrhs, work, n, sx, n, info);
+    if (*info != 0) { *iter = -2; goto fallback; }
+    or_spotrs(uplo, n, nrhs, sa, n, sx, n, info);
+    or_slag2d(n, nrhs, sx, n, work, n, info);
+    for (int k = 0; k < nrhs; k++) or_daxpy(n, 1.0, work + (size_t)k * n, 1, x + (size_t)k * ldx, 1);
+    or_dlacpy(n, nrhs, b, ldb, work, n);
+    or_dsymm_l(uplo, n, nrhs, -1.0, a, lda, x, ldx, work, n);
+    for (i = 0; i < nrhs; i++) {
+      const double xnrm = fabs(x[(size_t)(or_diamax(n, x + (size_t)i * ldx, 1) - 1) + (size_t)i * ldx]);
+      const double rnrm = fabs(work[(size_t)(or_diamax(n, work + (size_t)i * n, 1) - 1) + (size_t)i * n]);
+      if (rnrm > xnrm * cte) break;
+    }
+    if (i == nrhs) { *iter = iiter; return; }
+  }
+  *iter = -itermax - 1;
+fallback:
+  or_dpotrf(uplo, n, a, lda, info);
+  if (*info != 0) return;
+  or_dlacpy(n, nrhs, b, ldb, x, ldx);
+  or_dpotrs(uplo, n, nrhs, a, lda, x, ldx, info);
+}
 
 /* ---- DLARNV: SRC/dlarnv.f:94-174.  Chunks of 64 outputs; IDIST 1 U(0,1),
  * 2 U(-1,1), 3 N(0,1) by Box-Muller on consecutive pairs. */

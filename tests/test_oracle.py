@@ -306,6 +306,59 @@ def test_dgetri_workspace_rules():
     assert info == -6 and oracle.xerbla_last() == ("DGETRI", 6)
 
 
+@pytest.mark.parametrize("uplo", "LU")
+@pytest.mark.parametrize("cond", [2.0, 1e4, 1e8])
+def test_dpotrf_dchkpo_ratios(uplo, cond):
+    """DCHKPO tests 1 and 3 (TESTING/LIN/dchkpo.f): DPOT01 and DPOT02 below
+    THRESH on every N, NB and NRHS of dtest.in, reading only the UPLO
+    triangle (the other triangle holds 1e300); blocked and unblocked
+    factors agree on INFO for a matrix that is not positive definite."""
+    for n in INPUTS["dtest"]["n"]:
+        a = oracle.spd_matrix(n, cond, 31 + n, uplo)
+        for nb in sorted(set(INPUTS["dtest"]["nb"])) + [64]:
+            f, info = oracle.potrf(a, uplo, nb=nb)
+            assert info == 0
+            if n:
+                assert ck.dpot01(a, f, uplo) < THRESH, (n, nb)
+        for nrhs in INPUTS["dtest"]["nrhs"]:
+            xact = oracle.random_matrix(n, nrhs, 7 + n, idist=2)[0]
+            b = ck._sym_full(a, uplo) @ xact
+            x, info = oracle.potrs(f, b, uplo)
+            assert info == 0
+            if n:
+                assert ck.dpot02(a, x, b, uplo) < THRESH
+        if n >= 3:
+            bad = a.copy()
+            bad[n // 2, n // 2] = -1.0
+            infos = {oracle.potrf(bad, uplo, nb=nb)[1] for nb in (1, 2, 3, 64)}
+            assert len(infos) == 1 and infos.pop() > 0
+
+
+@pytest.mark.parametrize("uplo", "LU")
+@pytest.mark.parametrize("nrhs", INPUTS["dstest"]["nrhs"])
+def test_dsposv_ddrvac_ratios(uplo, nrhs):
+    """DDRVAC (TESTING/LIN/ddrvac.f): for ITER >= 0 the DPOT06 ratio is below
+    sqrt(N) and A is returned unchanged; an ill-conditioned matrix drives
+    the FP64 fallback (ITER < 0) with DPOT06 below THRESH."""
+    for n in INPUTS["dstest"]["n"]:
+        for cond in (2.0, 1e3, 1e10):
+            a = oracle.spd_matrix(n, cond, 91 + n, uplo)
+            xact = oracle.random_matrix(n, nrhs, 5 + n, idist=2)[0]
+            b = ck._sym_full(a, uplo) @ xact if n else np.zeros((0, nrhs))
+            ao, x, it, info = oracle.dsposv(a, b, uplo)
+            assert info == 0
+            if n == 0:
+                continue
+            r = ck.dpot06(a, x, b, uplo)
+            if it >= 0:
+                assert r < np.sqrt(n) or r < 1.0, (n, cond, it, r)
+                assert np.array_equal(ao, a)
+            else:
+                assert r < THRESH, (n, cond, it, r)
+            if cond >= 1e10 and n >= 10:
+                assert it < 0
+
+
 def test_oracle_ipiv_matches_openblas():
     scipy_linalg = pytest.importorskip("scipy.linalg")
     for n, seed in ((64, 1), (200, 2), (513, 3)):
@@ -345,6 +398,12 @@ ERR_GERFS = [(("/", 0, 0, 1, 1, 1, 1), -1), (("N", -1, 0, 1, 1, 1, 1), -2), (("N
              (("N", 2, 1, 2, 2, 2, 1), -12)]                                 # TESTING/LIN/derrge.f:186-216
 ERR_GECON = [(("/", 0, 1), -1), (("1", -1, 1), -2), (("1", 2, 1), -4)]     # TESTING/LIN/derrge.f:218-229
 ERR_GETRI = [((-1, 1, 64), -1), ((2, 1, 64), -3)]                          # TESTING/LIN/derrge.f:157-165
+ERR_POTRF = [(("/", 0, 1), -1), (("U", -1, 1), -2), (("U", 2, 1), -4)]     # TESTING/LIN/derrpo.f:133-142
+ERR_POTRS = [(("/", 0, 0, 1, 1), -1), (("U", -1, 0, 1, 1), -2), (("U", 0, -1, 1, 1), -3),
+             (("U", 2, 1, 1, 2), -5), (("U", 2, 1, 2, 1), -7)]                # derrpo.f:172-187
+ERR_DSPOSV = [(("/", 0, 0, 1, 1, 1), -1), (("U", -1, 0, 1, 1, 1), -2), (("U", 0, -1, 1, 1, 1), -3),
+              (("U", 2, 1, 1, 2, 2), -5), (("U", 2, 1, 2, 1, 2), -7),
+              (("U", 2, 1, 2, 2, 1), -9)]                                      # TESTING/LIN/derrac.f:110-128
 ERR_GEEQU = [((-1, 0, 1), -1), ((0, -1, 1), -2), ((2, 2, 1), -4)]          # TESTING/LIN/derrge.f:231-242
 
 
@@ -387,6 +446,16 @@ def test_oracle_error_exits():
     for (n, lda, lw), code in ERR_GETRI:
         name, inf = _oracle_err(L.or_dgetri, n, p(a), lda, p(ip), p(wk), lw, 64, p(info))
         assert (name, inf) == ("DGETRI", -code)
+    for (ul, n, lda), code in ERR_POTRF:
+        name, inf = _oracle_err(L.or_dpotrf_nb, ul.encode(), n, p(a), lda, p(info), 64)
+        assert (name, inf) == ("DPOTRF", -code)
+    for (ul, n, nrhs, lda, ldb), code in ERR_POTRS:
+        name, inf = _oracle_err(L.or_dpotrs, ul.encode(), n, nrhs, p(a), lda, p(a), ldb, p(info))
+        assert (name, inf) == ("DPOTRS", -code)
+    for (ul, n, nrhs, lda, ldb, ldx), code in ERR_DSPOSV:
+        name, inf = _oracle_err(L.or_dsposv, ul.encode(), n, nrhs, p(a), lda, p(a), ldb, p(a), ldx, p(wk), p(wk),
+                                p(info), p(info))
+        assert (name, inf) == ("DSPOSV", -code)
     for (m, n, lda), code in ERR_GEEQU:
         name, inf = _oracle_err(L.or_dgeequ, m, n, p(a), lda, p(w), p(w), p(w), p(w), p(w), p(info))
         assert (name, inf) == ("DGEEQU", -code)
