@@ -35,11 +35,23 @@ GB_HD inline double rn_add(double a, double b) { return __dadd_rn(a, b); }
 GB_HD inline double rn_sub(double a, double b) { return __dsub_rn(a, b); }
 GB_HD inline double rn_mul(double a, double b) { return __dmul_rn(a, b); }
 GB_HD inline double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+GB_HD inline double rn_sqrt(double a) { return __dsqrt_rn(a); }
+GB_HD inline float rn_add(float a, float b) { return __fadd_rn(a, b); }
+GB_HD inline float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+GB_HD inline float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+GB_HD inline float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+GB_HD inline float rn_sqrt(float a) { return __fsqrt_rn(a); }
 #else
 GB_HD inline double rn_add(double a, double b) { return a + b; }
 GB_HD inline double rn_sub(double a, double b) { return a - b; }
 GB_HD inline double rn_mul(double a, double b) { return a * b; }
 GB_HD inline double rn_div(double a, double b) { return a / b; }
+GB_HD inline double rn_sqrt(double a) { return std::sqrt(a); }
+GB_HD inline float rn_add(float a, float b) { return a + b; }
+GB_HD inline float rn_sub(float a, float b) { return a - b; }
+GB_HD inline float rn_mul(float a, float b) { return a * b; }
+GB_HD inline float rn_div(float a, float b) { return a / b; }
+GB_HD inline float rn_sqrt(float a) { return std::sqrt(a); }
 #endif
 
 // IDAMAX (BLAS/SRC/idamax.f:93-123), 1-based, 0 for n < 1.

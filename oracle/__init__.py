@@ -244,7 +244,7 @@ def spd_matrix(n, cond, seed, uplo="L", junk=1e300, dtype=np.float64):
     full = a.astype(dtype)
     out = np.tril(full) if uplo == "L" else np.triu(full)
     mask = np.triu(np.ones((n, n), bool), 1) if uplo == "L" else np.tril(np.ones((n, n), bool), -1)
-    out[mask] = junk
+    out[mask] = min(junk, float(np.finfo(dtype).max) / 16)
     return out
 
 

@@ -1,8 +1,8 @@
 """Host/device code checked on the CPU.  The sequential DLATRS plan, careful
 solve and DGECON rescaling step (lapack_gb300/csrc/latrs_seq.h, run on the
 GPU as one-thread kernels), DGEEQU's finishing steps and the element steps
-of DGETRI (lapack_gb300/csrc/getri_seq.h, one GPU thread each) are compiled
-with g++
+of DGETRI (lapack_gb300/csrc/getri_seq.h, one GPU thread each) and the
+Cholesky steps (lapack_gb300/csrc/potrf_seq.h) are compiled with g++
 from the same headers and composed exactly as the library composes them
 (CNORM by sequential column sums, the plain solve by DTRSV in the reference
 loop order, DLACN2 for the estimate; DGEMM for DGETRI's update), then
@@ -10,7 +10,9 @@ checked bit for bit against the oracle (SRC/dlatrs.f, SRC/dgecon.f,
 SRC/dgetri.f): x, SCALE and CNORM for every UPLO / TRANS / DIAG on
 well-scaled, badly scaled and overflowing triangles; RCOND on the DCHKGE
 matrix types and on factors with tiny pivots; R, C and the condition
-numbers of DGEEQU; the inverse for blocked and unblocked block sizes."""
+numbers of DGEEQU; the inverse for blocked and unblocked block sizes; the
+Cholesky factor (D and S, both triangles, blocked and unblocked), DLANSY and
+DSYMM as the Cholesky kernels compute them."""
 import ctypes
 import os
 import shutil
@@ -30,7 +32,59 @@ HARNESS = r"""
 #include <vector>
 #include "latrs_seq.h"
 #include "getri_seq.h"
+#include "potrf_seq.h"
+// xPOTRF as the library's GPU driver runs it (per-element DSYRK and DGEMM,
+// per-row / per-column DTRSM, one-thread DPOTRF2 of each diagonal block).
+template <typename T>
+int seq_potrf_t(int upper, int n, T *a, int lda, int nb) {
+  if (n == 0) return 0;
+  if (nb <= 1 || nb >= n) return gb::potrf2_seq(upper, n, a, lda);
+  for (int j = 0; j < n; j += nb) {
+    const int jb = nb < n - j ? nb : n - j;
+    T *d = a + j + (size_t)j * lda;
+    if (j > 0) {
+      const T *aop = upper ? a + (size_t)j * lda : a + j;
+      for (int jj = 0; jj < jb; ++jj)
+        for (int i = upper ? 0 : jj; i < (upper ? jj + 1 : jb); ++i) gb::syrk_elem(upper, i, jj, j, T(-1), aop, lda, d, lda);
+    }
+    const int info = gb::potrf2_seq(upper, jb, d, lda);
+    if (info) return info + j;
+    const int rest = n - j - jb;
+    if (rest > 0) {
+      if (!upper) {
+        T *c = a + (j + jb) + (size_t)j * lda;
+        if (j > 0)
+          for (int jj = 0; jj < jb; ++jj)
+            for (int i = 0; i < rest; ++i) gb::gemm_chol_elem(0, i, jj, j, T(-1), a + j + jb, lda, a + j, lda, c, lda);
+        for (int i = 0; i < rest; ++i) gb::trsm_rltn_row(i, jb, d, lda, c, lda);
+      } else {
+        T *c = a + j + (size_t)(j + jb) * lda;
+        if (j > 0)
+          for (int jj = 0; jj < rest; ++jj)
+            for (int i = 0; i < jb; ++i)
+              gb::gemm_chol_elem(1, i, jj, j, T(-1), a + (size_t)j * lda, lda, a + (size_t)(j + jb) * lda, lda, c, lda);
+        for (int jj = 0; jj < rest; ++jj) gb::trsm_lutn_col(jj, jb, d, lda, c, lda);
+      }
+    }
+  }
+  return 0;
+}
 extern "C" {
+int seq_dpotrf(int upper, int n, double *a, int lda, int nb) { return seq_potrf_t<double>(upper, n, a, lda, nb); }
+int seq_spotrf(int upper, int n, float *a, int lda, int nb) { return seq_potrf_t<float>(upper, n, a, lda, nb); }
+double seq_dlansy_i(int upper, int n, const double *a, int lda) {
+  double v = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double s = gb::lansy_row_sum(upper, i, n, a, lda);
+    if (v < s || s != s) v = s;
+  }
+  return v;
+}
+void seq_dsymm_l(int upper, int m, int n, double alpha, const double *a, int lda, const double *b, int ldb, double *c,
+                 int ldc, double *out) {
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) out[(size_t)i + (size_t)j * m] = gb::symm_l_elem(upper, i, j, m, alpha, a, lda, b, ldb, c, ldc);
+}
 void or_dtrsv(char uplo, char trans, char diag, int n, const double *a, int lda, double *x);
 void or_dgemm(char ta, char tb, int m, int n, int k, double alpha, const double *a, int lda, const double *b, int ldb,
               double beta, double *c, int ldc);
@@ -175,6 +229,12 @@ def seq(tmp_path_factory):
     L.seq_dgecon.restype = ctypes.c_double
     L.seq_dgetri.argtypes = [ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
     L.seq_dgeequ.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, p, p, p]
+    L.seq_dpotrf.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, ctypes.c_int]
+    L.seq_spotrf.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, ctypes.c_int]
+    L.seq_dlansy_i.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int]
+    L.seq_dlansy_i.restype = ctypes.c_double
+    L.seq_dsymm_l.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, p, ctypes.c_int, p,
+                              ctypes.c_int, p, ctypes.c_int, p]
     return L
 
 
@@ -329,3 +389,39 @@ def test_dgeequ_seq_bitwise_vs_oracle(seq):
             assert c.tobytes() == cr.tobytes() and sc[0] == rowr and sc[1] == colr
         elif infr > m:
             assert sc[0] == rowr
+
+
+@pytest.mark.parametrize("uplo", "LU")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_potrf_seq_bitwise_vs_oracle(seq, uplo, dtype):
+    """xPOTRF as the GPU driver composes its per-thread steps equals the
+    oracle's xPOTRF bit for bit (blocked and unblocked, D and S), INFO
+    included for a matrix that is not positive definite."""
+    fn = seq.seq_dpotrf if dtype == np.float64 else seq.seq_spotrf
+    for n in (1, 2, 7, 33, 70, 130):
+        for nb in (1, 3, 20, 64, 200):
+            a = oracle.spd_matrix(n, 1e3, 17 + n, uplo, dtype=dtype)
+            if n > 4 and nb == 3:
+                a[n // 2, n // 2] = -1.0
+            ref, rinfo = oracle.potrf(a, uplo, nb=nb)
+            got = np.asfortranarray(a.copy())
+            ginfo = fn(int(uplo == "U"), n, _ptr(got), n, nb)
+            assert ginfo == rinfo, (n, nb)
+            assert got.tobytes() == ref.tobytes(), (n, nb)
+
+
+@pytest.mark.parametrize("uplo", "LU")
+def test_lansy_symm_seq_bitwise_vs_oracle(seq, uplo):
+    for n in (1, 5, 40, 97):
+        a = np.asfortranarray(oracle.spd_matrix(n, 1e2, 3 + n, uplo))
+        assert seq.seq_dlansy_i(int(uplo == "U"), n, _ptr(a), n) == oracle.dlansy("I", uplo, a)
+        x = np.asfortranarray(oracle.random_matrix(n, 3, 5, idist=3)[0])
+        c = np.asfortranarray(oracle.random_matrix(n, 3, 6, idist=3)[0])
+        out = np.zeros((n, 3), order="F")
+        seq.seq_dsymm_l(int(uplo == "U"), n, 3, -1.0, _ptr(a), n, _ptr(x), n, _ptr(c), n, _ptr(out))
+        L = oracle.lib()
+        L.or_dsymm_l.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_double] + \
+            [ctypes.c_void_p, ctypes.c_int] * 3
+        ref = c.copy(order="F")
+        L.or_dsymm_l(uplo.encode(), n, 3, -1.0, _ptr(a), n, _ptr(x), n, _ptr(ref), n)
+        assert out.tobytes() == ref.tobytes()
