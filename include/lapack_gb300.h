@@ -101,6 +101,25 @@ void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lap
  * a smaller LWORK shrinks the block size as the reference does. */
 void dgetri_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* ipiv, double* work,
              const lapack_int* lwork, lapack_int* info);
+/* Cholesky factorization, solve and driver of a symmetric positive
+ * definite matrix (one triangle referenced).  Replace SRC/dpotrf.f:104,
+ * SRC/spotrf.f, SRC/dpotrs.f:107, SRC/spotrs.f, SRC/dposv.f:127 (the
+ * LAPACK_dpotrf, _spotrf, _dpotrs, _spotrs, _dposv prototypes of lapack.h). */
+void dpotrf_(const char* uplo, const lapack_int* n, double* a, const lapack_int* lda, lapack_int* info,
+             size_t uplo_len);
+void spotrf_(const char* uplo, const lapack_int* n, float* a, const lapack_int* lda, lapack_int* info,
+             size_t uplo_len);
+void dpotrs_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, const double* a, const lapack_int* lda,
+             double* b, const lapack_int* ldb, lapack_int* info, size_t uplo_len);
+void spotrs_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, const float* a, const lapack_int* lda,
+             float* b, const lapack_int* ldb, lapack_int* info, size_t uplo_len);
+void dposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+            double* b, const lapack_int* ldb, lapack_int* info, size_t uplo_len);
+/* Mixed-precision Cholesky refinement.  Replaces SRC/dsposv.f:195 (lapack.h
+ * LAPACK_dsposv).  WORK and SWORK are accepted and unused. */
+void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+             const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* work, float* swork,
+             lapack_int* iter, lapack_int* info, size_t uplo_len);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -262,6 +281,12 @@ int gb300_dgesvx_dev(char fact, char trans, int n, int nrhs, double* dA, int lda
  * and receives inv(A); dIpiv on the device; *info host.  No workspace
  * argument: the library's scratch is stream ordered. */
 int gb300_dgetri_dev(int n, double* dA, int lda, const int* dIpiv, int* info, void* stream);
+/* Cholesky on device memory: DPOTRF (one triangle of dA, in place; *info
+ * host), DPOTRS with those factors, DSPOSV (*iter, *info host). */
+int gb300_dpotrf_dev(char uplo, int n, double* dA, int lda, int* info, void* stream);
+int gb300_dpotrs_dev(char uplo, int n, int nrhs, const double* dA, int lda, double* dB, int ldb, void* stream);
+int gb300_dsposv_dev(char uplo, int n, int nrhs, double* dA, int lda, const double* dB, int ldb, double* dX, int ldx,
+                     int* iter, int* info, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

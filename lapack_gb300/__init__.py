@@ -22,7 +22,8 @@ _ip = ctypes.POINTER(ctypes.c_int)
 _sz = ctypes.c_size_t
 
 FORTRAN_SYMBOLS = ["dgetrf_", "sgetrf_", "dgetrf2_", "sgetrf2_", "dgetrs_", "sgetrs_", "dgesv_", "sgesv_",
-                   "dsgesv_", "dgesvx_", "dgetri_", "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
+                   "dsgesv_", "dgesvx_", "dgetri_", "dpotrf_", "spotrf_", "dpotrs_", "spotrs_", "dposv_", "dsposv_",
+                   "dgerfs_", "dgecon_", "dlatrs_", "dlaswp_", "slaswp_", "dlag2s_", "slag2d_", "dlange_", "dlamch_",
                    "slamch_", "xerbla_"]
 
 
@@ -270,6 +271,54 @@ def getri(lu, ipiv, lwork=None):
     info = ctypes.c_int(0)
     lib().dgetri_(_ref(n), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(work), _ref(lw), ctypes.byref(info))
     return a, info.value, float(work[0])
+
+
+def potrf(a, uplo="L", dtype=None):
+    """xPOTRF (SRC/dpotrf.f): returns (factor, info) for a copy of ``a``."""
+    dtype = np.dtype(dtype or (a.dtype if a.dtype in (np.float32, np.float64) else np.float64))
+    a = _fortran(a, dtype)
+    n = a.shape[0]
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}potrf_")(ctypes.c_char_p(uplo.encode()), _ref(n), _ptr(a), _ref(max(1, n)),
+                                           ctypes.byref(info), _sz(1))
+    return a, info.value
+
+
+def potrs(f, b, uplo="L"):
+    """xPOTRS (SRC/dpotrs.f): returns (x, info)."""
+    dtype = f.dtype
+    f = _fortran(f, dtype)
+    b2 = _fortran(_as2d(b), dtype)
+    n, nrhs = b2.shape
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_pre(dtype)}potrs_")(ctypes.c_char_p(uplo.encode()), _ref(n), _ref(nrhs), _ptr(f),
+                                           _ref(max(1, n)), _ptr(b2), _ref(max(1, n)), ctypes.byref(info), _sz(1))
+    return b2.reshape(np.asarray(b).shape), info.value
+
+
+def posv(a, b, uplo="L"):
+    """DPOSV (SRC/dposv.f): returns (factor, x, info)."""
+    a = _fortran(a, np.float64)
+    b2 = _fortran(_as2d(b), np.float64)
+    n, nrhs = b2.shape
+    info = ctypes.c_int(0)
+    lib().dposv_(ctypes.c_char_p(uplo.encode()), _ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(b2),
+                 _ref(max(1, n)), ctypes.byref(info), _sz(1))
+    return a, b2.reshape(np.asarray(b).shape), info.value
+
+
+def dsposv(a, b, uplo="L"):
+    """DSPOSV (SRC/dsposv.f): returns (a_out, x, iter, info)."""
+    a = _fortran(a, np.float64)
+    b2 = _fortran(_as2d(b), np.float64)
+    n, nrhs = b2.shape
+    x = np.zeros((n, nrhs), order="F")
+    it = ctypes.c_int(0)
+    info = ctypes.c_int(0)
+    lib().dsposv_(ctypes.c_char_p(uplo.encode()), _ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(b2),
+                  _ref(max(1, n)), _ptr(x), _ref(max(1, n)), _ptr(np.zeros(1)), _ptr(np.zeros(1, np.float32)),
+                  ctypes.byref(it), ctypes.byref(info), _sz(1))
+    return a, x.reshape(np.asarray(b).shape), it.value, info.value
 
 
 def laswp(a, k1, k2, ipiv, incx=1):

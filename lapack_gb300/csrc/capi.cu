@@ -199,6 +199,57 @@ void laswp_host(const lapack_int* n, T* a, const lapack_int* lda, const lapack_i
 
 }  // namespace
 
+namespace {
+// ------------------------------------------------------------ POTRF / POTRS / POSV
+template <typename T>
+void potrf_host(const char* name, const char* uplo, const lapack_int* n, T* a, const lapack_int* lda,
+                lapack_int* info) {
+  // SRC/dpotrf.f:131-145
+  *info = 0;
+  const bool upper = lsame(*uplo, 'U');
+  if (!upper && !lsame(*uplo, 'L')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, ld = ld_dev(N);
+  DevScratch dA(sizeof(T) * (size_t)ld * N, s);
+  if (!dA.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  int inf = 0;
+  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = gb::potrf_dev<T>(upper, N, dA.as<T>(), ld, 64, &inf, s);
+  if (!rc) rc = d2h(a, *lda, dA.as<T>(), ld, N, N, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure(name, rc, info); return; }
+  *info = inf;
+}
+template <typename T>
+void potrs_host(const char* name, const char* uplo, const lapack_int* n, const lapack_int* nrhs, const T* a,
+                const lapack_int* lda, T* b, const lapack_int* ldb, lapack_int* info) {
+  // SRC/dpotrs.f:146-165
+  *info = 0;
+  const bool upper = lsame(*uplo, 'U');
+  if (!upper && !lsame(*uplo, 'L')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0 || *nrhs == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dB(sizeof(T) * (size_t)ld * R, s);
+  if (!dA.p || !dB.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<T>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::potrs_dev<T>(upper, N, R, dA.as<T>(), ld, dB.as<T>(), ld, s);
+  if (!rc) rc = d2h(b, *ldb, dB.as<T>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure(name, rc, info);
+}
+}  // namespace
+
 extern "C" {
 
 __attribute__((weak)) void xerbla_(const char* srname, const lapack_int* info, size_t len) {
@@ -544,6 +595,82 @@ void dgetri_(const lapack_int* n, double* a, const lapack_int* lda, const lapack
   if (inf == 0) work[0] = (double)iws;
 }
 
+void dpotrf_(const char* uplo, const lapack_int* n, double* a, const lapack_int* lda, lapack_int* info, size_t) {
+  potrf_host<double>("DPOTRF", uplo, n, a, lda, info);
+}
+void spotrf_(const char* uplo, const lapack_int* n, float* a, const lapack_int* lda, lapack_int* info, size_t) {
+  potrf_host<float>("SPOTRF", uplo, n, a, lda, info);
+}
+void dpotrs_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, const double* a, const lapack_int* lda,
+             double* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  potrs_host<double>("DPOTRS", uplo, n, nrhs, a, lda, b, ldb, info);
+}
+void spotrs_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, const float* a, const lapack_int* lda,
+             float* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  potrs_host<float>("SPOTRS", uplo, n, nrhs, a, lda, b, ldb, info);
+}
+void dposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+            double* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  // SRC/dposv.f:130-165
+  *info = 0;
+  const bool upper = lsame(*uplo, 'U');
+  if (!upper && !lsame(*uplo, 'L')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  if (*info != 0) { call_xerbla("DPOSV ", -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dB(sizeof(double) * (size_t)ld * std::max(R, 1), s);
+  if (!dA.p || !dB.p) { device_failure("DPOSV", (int)cudaErrorMemoryAllocation, info); return; }
+  int inf = 0;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::potrf_dev<double>(upper, N, dA.as<double>(), ld, 64, &inf, s);
+  if (!rc && inf == 0) rc = gb::potrs_dev<double>(upper, N, R, dA.as<double>(), ld, dB.as<double>(), ld, s);
+  if (!rc) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
+  if (!rc && inf == 0) rc = d2h(b, *ldb, dB.as<double>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DPOSV", rc, info); return; }
+  *info = inf;
+}
+void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
+             const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double*, float*,
+             lapack_int* iter, lapack_int* info, size_t) {
+  // SRC/dsposv.f:209-232
+  *info = 0;
+  *iter = 0;
+  const bool upper = lsame(*uplo, 'U');
+  if (!upper && !lsame(*uplo, 'L')) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  else if (*ldx < std::max(1, *n)) *info = -9;
+  if (*info != 0) { call_xerbla("DSPOSV", -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dB(sizeof(double) * (size_t)ld * std::max(R, 1), s),
+      dX(sizeof(double) * (size_t)ld * std::max(R, 1), s);
+  if (!dA.p || !dB.p || !dX.p) { device_failure("DSPOSV", (int)cudaErrorMemoryAllocation, info); return; }
+  int it = 0, inf = 0;
+  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::dsposv_dev(upper, N, R, dA.as<double>(), ld, dB.as<double>(), ld, dX.as<double>(), ld, &it, &inf,
+                               s);
+  if (!rc) rc = finish(s);
+  // A holds the FP64 factor when the refinement fell back (ITER < 0)
+  if (!rc && it < 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
+  if (!rc && inf == 0) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("DSPOSV", rc, info); return; }
+  *iter = it;
+  *info = inf;
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -770,6 +897,45 @@ int gb300_dgetri_dev(int n, double* dA, int lda, const int* dIpiv, int* info, vo
   int inf = 0;
   int rc = gb::dgetri_dev(n, dA, lda, dIpiv, options().nb_f64, &inf, s);
   if (!rc) rc = finish(s);
+  if (info) *info = inf;
+  return rc;
+}
+
+int gb300_dpotrf_dev(char uplo, int n, double* dA, int lda, int* info, void* stream) {
+  if (!lsame(uplo, 'U') && !lsame(uplo, 'L')) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  cudaStream_t s = (cudaStream_t)stream;
+  int inf = 0;
+  int rc = gb::potrf_dev<double>(lsame(uplo, 'U'), n, dA, lda, 64, &inf, s);
+  if (!rc) rc = finish(s);
+  if (info) *info = inf;
+  return rc;
+}
+int gb300_dpotrs_dev(char uplo, int n, int nrhs, const double* dA, int lda, double* dB, int ldb, void* stream) {
+  if (!lsame(uplo, 'U') && !lsame(uplo, 'L')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, n)) return -7;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::potrs_dev<double>(lsame(uplo, 'U'), n, nrhs, dA, lda, dB, ldb, s);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+int gb300_dsposv_dev(char uplo, int n, int nrhs, double* dA, int lda, const double* dB, int ldb, double* dX, int ldx,
+                     int* iter, int* info, void* stream) {
+  if (!lsame(uplo, 'U') && !lsame(uplo, 'L')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, n)) return -7;
+  if (ldx < std::max(1, n)) return -9;
+  cudaStream_t s = (cudaStream_t)stream;
+  int it = 0, inf = 0;
+  int rc = gb::dsposv_dev(lsame(uplo, 'U'), n, nrhs, dA, lda, dB, ldb, dX, ldx, &it, &inf, s);
+  if (!rc) rc = finish(s);
+  if (iter) *iter = it;
   if (info) *info = inf;
   return rc;
 }

@@ -58,6 +58,18 @@ int unit_lower_inverse_dev(int k, const T* L, int ldl, T* X, int ldx, cudaStream
 template <typename T>
 int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int lda, long long sA, T* dX, int ldx,
                      long long sX, int nbatch, cudaStream_t s, bool dtrsv_order = false);
+// op(T) X = B, T a triangle of dA (any UPLO / TRANS / DIAG), nrhs columns.
+template <typename T>
+int trsm_left_dev(bool upper, bool trans, bool unit, int n, int nrhs, const T* dA, int lda, T* dB, int ldb,
+                  cudaStream_t s);
+// Cholesky on device memory (SRC/dpotrf.f with block size nb); *info host.
+template <typename T>
+int potrf_dev(bool upper, int n, T* dA, int lda, int nb, int* info, cudaStream_t s);
+template <typename T>
+int potrs_dev(bool upper, int n, int nrhs, const T* dA, int lda, T* dB, int ldb, cudaStream_t s);
+// DSPOSV on device memory; *iter and *info are host outputs.
+int dsposv_dev(bool upper, int n, int nrhs, double* dA, int lda, const double* dB, int ldb, double* dX, int ldx,
+               int* iter, int* info, cudaStream_t s);
 // DTRSV on one device vector (X has n elements, unit stride).
 int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int lda, double* dX, cudaStream_t s);
 // DLATRS (SRC/dlatrs.f) on one device vector: *scale (host) receives SCALE;

@@ -886,6 +886,31 @@ int trsv_batched_dev(bool lower, bool trans, int n, int nrhs, const T* dA, int l
 template int trsv_batched_dev<double>(bool, bool, int, int, const double*, int, long long, double*, int, long long,
                                       int, cudaStream_t, bool);
 
+// op(T) X = B for nrhs right-hand sides with any UPLO / TRANS / DIAG of the
+// triangle T (DTRSM('L', ...), BLAS/SRC/dtrsm.f:272-329): exact mode in the
+// DTRSM loop order, otherwise the streaming solve.
+template <typename T>
+int trsm_left_dev(bool upper, bool trans, bool unit, int n, int nrhs, const T* dA, int lda, T* dB, int ldb,
+                  cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return 0;
+  const bool ex = options().exact;
+#define GB_TRSM(FWD, UN, TR)                                                                           \
+  return ex ? launch_trsv<T, true, FWD, UN, TR>(dA, lda, n, dB, ldb, nrhs, s, false)                   \
+            : launch_trsv<T, false, FWD, UN, TR>(dA, lda, n, dB, ldb, nrhs, s, false)
+  // solve order: forward for L and for U^T, backward for U and for L^T
+  if (!trans) {
+    if (!upper) { if (unit) GB_TRSM(true, true, false); else GB_TRSM(true, false, false); }
+    if (unit) GB_TRSM(false, true, false);
+    GB_TRSM(false, false, false);
+  }
+  if (upper) { if (unit) GB_TRSM(true, true, true); else GB_TRSM(true, false, true); }
+  if (unit) GB_TRSM(false, true, true);
+  GB_TRSM(false, false, true);
+#undef GB_TRSM
+}
+template int trsm_left_dev<double>(bool, bool, bool, int, int, const double*, int, double*, int, cudaStream_t);
+template int trsm_left_dev<float>(bool, bool, bool, int, int, const float*, int, float*, int, cudaStream_t);
+
 // DTRSV (BLAS/SRC/dtrsv.f, INCX = 1) on one device vector for any UPLO,
 // TRANS, DIAG, in every mode with the reference's operations: each element's
 // sum in the DTRSV loop order and a true division by the diagonal.  DLATRS

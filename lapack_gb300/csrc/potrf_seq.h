@@ -78,32 +78,50 @@ GB_HD inline void trsm_lutn_col(int j, int m, const T* A, int lda, T* B, int ldb
 }
 
 // DPOTRF2 (SRC/dpotrf2.f:168-205) of an n x n block on one thread; returns
-// INFO (the order of the first leading minor that is not positive).
+// INFO (the order of the first leading minor that is not positive).  The
+// reference recursion (factor A11 of order N/2, DTRSM, DSYRK, factor A22)
+// runs as a loop over an explicit stack of blocks, so the device code needs
+// no call stack for it.
 template <typename T>
 GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
   if (n == 0) return 0;
-  if (n == 1) {
-    const T a = elc(A, lda, 0, 0);
-    if (a <= T(0) || a != a) return 1;
-    el(A, lda, 0, 0) = rn_sqrt(a);
-    return 0;
+  struct Blk { int off, n, phase; };
+  Blk st[40];                          // depth <= log2(n) + 1
+  int top = 0;
+  st[top++] = Blk{0, n, 0};
+  while (top > 0) {
+    Blk& b = st[top - 1];
+    T* a11 = A + b.off + (size_t)b.off * lda;
+    if (b.n == 1) {
+      const T a = a11[0];
+      if (a <= T(0) || a != a) return b.off + 1;
+      a11[0] = rn_sqrt(a);
+      --top;
+      continue;
+    }
+    const int n1 = b.n / 2, n2 = b.n - n1;
+    if (b.phase == 0) {
+      b.phase = 1;
+      st[top++] = Blk{b.off, n1, 0};
+    } else if (b.phase == 1) {
+      T* a12 = upper ? a11 + (size_t)n1 * lda : a11 + n1;   // A(1, N1+1) or A(N1+1, 1) of the block
+      T* a22 = a11 + n1 + (size_t)n1 * lda;
+      if (upper) {
+        for (int j = 0; j < n2; ++j) trsm_lutn_col(j, n1, a11, lda, a12, lda);
+        for (int j = 0; j < n2; ++j)
+          for (int i = 0; i <= j; ++i) syrk_elem(1, i, j, n1, T(-1), a12, lda, a22, lda);
+      } else {
+        for (int i = 0; i < n2; ++i) trsm_rltn_row(i, n1, a11, lda, a12, lda);
+        for (int j = 0; j < n2; ++j)
+          for (int i = j; i < n2; ++i) syrk_elem(0, i, j, n1, T(-1), a12, lda, a22, lda);
+      }
+      b.phase = 2;
+      st[top++] = Blk{b.off + n1, n2, 0};
+    } else {
+      --top;
+    }
   }
-  const int n1 = n / 2, n2 = n - n1;
-  int info = potrf2_seq(upper, n1, A, lda);
-  if (info) return info;
-  T* A12 = upper ? A + (size_t)n1 * lda : A + n1;   // A(1, N1+1) or A(N1+1, 1)
-  T* A22 = A + n1 + (size_t)n1 * lda;
-  if (upper) {
-    for (int j = 0; j < n2; ++j) trsm_lutn_col(j, n1, A, lda, A12, lda);
-    for (int j = 0; j < n2; ++j)
-      for (int i = 0; i <= j; ++i) syrk_elem(1, i, j, n1, T(-1), A12, lda, A22, lda);
-  } else {
-    for (int i = 0; i < n2; ++i) trsm_rltn_row(i, n1, A, lda, A12, lda);
-    for (int j = 0; j < n2; ++j)
-      for (int i = j; i < n2; ++i) syrk_elem(0, i, j, n1, T(-1), A12, lda, A22, lda);
-  }
-  info = potrf2_seq(upper, n2, A22, lda);
-  return info ? info + n1 : 0;
+  return 0;
 }
 
 // Row sum i of DLANSY('I') (SRC/dlansy.f:159-186) in the order the reference

@@ -58,6 +58,11 @@ ERR_GESVX = [(("/", "N", 0, 0, 1, 1, "N", 1, 1), 1), (("N", "/", 0, 0, 1, 1, "N"
              (("F", "N", 1, 0, 1, 1, "C", 1, 1), 12), (("N", "N", 2, 1, 2, 2, "N", 1, 2), 14),
              (("N", "N", 2, 1, 2, 2, "N", 2, 1), 16)]   # TESTING/LIN/derrvx.f:151-200
 ERR_GETRI = [((-1, 1, 1), 1), ((2, 1, 4), 3), ((2, 2, 1), 6)]   # TESTING/LIN/derrge.f:157-165, and LWORK < N
+ERR_POTRF = [(("/", 0, 1), 1), (("U", -1, 1), 2), (("U", 2, 1), 4)]      # TESTING/LIN/derrpo.f:133-142
+ERR_POTRS = [(("/", 0, 0, 1, 1), 1), (("U", -1, 0, 1, 1), 2), (("U", 0, -1, 1, 1), 3),
+             (("U", 2, 1, 1, 2), 5), (("U", 2, 1, 2, 1), 7)]                 # derrpo.f:172-187
+ERR_SPOSV = [(("/", 0, 0, 1, 1, 1), 1), (("U", -1, 0, 1, 1, 1), 2), (("U", 0, -1, 1, 1, 1), 3),
+             (("U", 2, 1, 1, 2, 2), 5), (("U", 2, 1, 2, 1, 2), 7), (("U", 2, 1, 2, 2, 1), 9)]   # derrac.f:110-128
 ERR_GECON = [(("/", 0, 1, 1.0), 1), (("1", -1, 1, 1.0), 2), (("1", 2, 1, 1.0), 4),
              (("1", 2, 2, -1.0), 5)]                # derrge.f:218-229, and ANORM < 0
 
@@ -115,6 +120,21 @@ def test_fortran_abi_error_exits(lib):
         wq = np.zeros(2)
         lib.dgetri_(_i(10), p(a), _i(10), p(ip), p(wq), _i(-1), ctypes.byref(info))   # workspace query: no GPU work
         assert info.value == 0 and wq[0] == 10 * g.get_option("nb64")
+        cc = lambda ch: ctypes.c_char_p(ch.encode())
+        for (ul, n, lda), code in ERR_POTRF:
+            for pre in "ds":
+                getattr(lib, pre + "potrf_")(cc(ul), _i(n), p(a), _i(lda), ctypes.byref(info), ctypes.c_size_t(1))
+                assert info.value == -code and g.xerbla_last() == (pre.upper() + "POTRF", code)
+        for (ul, n, nrhs, lda, ldb), code in ERR_POTRS:
+            lib.dpotrs_(cc(ul), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldb), ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DPOTRS", code)
+            lib.dposv_(cc(ul), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldb), ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DPOSV", code)
+        itr = ctypes.c_int(0)
+        for (ul, n, nrhs, lda, ldb, ldx), code in ERR_SPOSV:
+            lib.dsposv_(cc(ul), _i(n), _i(nrhs), p(a), _i(lda), p(a), _i(ldb), p(a), _i(ldx), p(w), p(w),
+                        ctypes.byref(itr), ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("DSPOSV", code)
         for (nm, n, lda, anorm), code in ERR_GECON:
             lib.dgecon_(ctypes.c_char_p(nm.encode()), _i(n), p(a), _i(lda), ctypes.byref(ctypes.c_double(anorm)),
                         ctypes.byref(rc), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))
