@@ -221,6 +221,28 @@ lapack_int LAPACKE_dgesvx(int matrix_layout, char fact, char trans, lapack_int n
                           lapack_int lda, double* af, lapack_int ldaf, lapack_int* ipiv, char* equed, double* r,
                           double* c, double* b, lapack_int ldb, double* x, lapack_int ldx, double* rcond,
                           double* ferr, double* berr, double* rpivot);
+/* LAPACKE/include/lapacke.h:3030-3145, 8600 (dposv, dsposv, s/dpotrf, s/dpotrs) and their _work forms */
+lapack_int LAPACKE_dpotrf(int matrix_layout, char uplo, lapack_int n, double* a, lapack_int lda);
+lapack_int LAPACKE_dpotrf_work(int matrix_layout, char uplo, lapack_int n, double* a, lapack_int lda);
+lapack_int LAPACKE_spotrf(int matrix_layout, char uplo, lapack_int n, float* a, lapack_int lda);
+lapack_int LAPACKE_spotrf_work(int matrix_layout, char uplo, lapack_int n, float* a, lapack_int lda);
+lapack_int LAPACKE_dpotrs(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, const double* a,
+                          lapack_int lda, double* b, lapack_int ldb);
+lapack_int LAPACKE_dpotrs_work(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, const double* a,
+                               lapack_int lda, double* b, lapack_int ldb);
+lapack_int LAPACKE_spotrs(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, const float* a, lapack_int lda,
+                          float* b, lapack_int ldb);
+lapack_int LAPACKE_spotrs_work(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, const float* a,
+                               lapack_int lda, float* b, lapack_int ldb);
+lapack_int LAPACKE_dposv(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                         double* b, lapack_int ldb);
+lapack_int LAPACKE_dposv_work(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                              double* b, lapack_int ldb);
+lapack_int LAPACKE_dsposv(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                          const double* b, lapack_int ldb, double* x, lapack_int ldx, lapack_int* iter);
+lapack_int LAPACKE_dsposv_work(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                               const double* b, lapack_int ldb, double* x, lapack_int ldx, double* work,
+                               float* swork, lapack_int* iter);
 /* LAPACKE/include/lapacke.h:1153 (dgetri) and its _work form */
 lapack_int LAPACKE_dgetri(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv);
 lapack_int LAPACKE_dgetri_work(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv,

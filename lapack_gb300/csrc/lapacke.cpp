@@ -155,6 +155,97 @@ lapack_int laswp_work(const char* nm, F fort, int layout, lapack_int n, T* a, la
   return 0;
 }
 
+
+// NaN check of the UPLO triangle (LAPACKE/utils/lapacke_dtr_nancheck.c with
+// DIAG = 'N', as LAPACKE_dpo_nancheck calls it): the triangle of the stored
+// matrix in the given layout, clipped by LDA.
+template <typename T>
+bool tr_has_nan(int layout, char uplo, lapack_int n, const T* a, lapack_int lda) {
+  if (!a) return false;
+  const bool colmaj = layout == LAPACK_COL_MAJOR, lower = (uplo | 0x20) == 'l';
+  if ((!colmaj && layout != LAPACK_ROW_MAJOR) || (!lower && (uplo | 0x20) != 'u')) return false;
+  if (colmaj != lower) {   // column-major upper or row-major lower
+    for (lapack_int j = 0; j < n; ++j)
+      for (lapack_int i = 0; i < std::min(j + 1, lda); ++i)
+        if (a[i + (size_t)j * lda] != a[i + (size_t)j * lda]) return true;
+  } else {
+    for (lapack_int j = 0; j < n; ++j)
+      for (lapack_int i = j; i < std::min(n, lda); ++i)
+        if (a[i + (size_t)j * lda] != a[i + (size_t)j * lda]) return true;
+  }
+  return false;
+}
+
+// Layout change of the UPLO triangle (LAPACKE/utils/lapacke_dtr_trans.c with
+// DIAG = 'N'): out(j, i) = in(i, j) over the triangle, clipped by both
+// leading dimensions; the other triangle of `out` is not written.
+template <typename T>
+void tr_trans(int layout, char uplo, lapack_int n, const T* in, lapack_int ldin, T* out, lapack_int ldout) {
+  if (!in || !out) return;
+  const bool colmaj = layout == LAPACK_COL_MAJOR, lower = (uplo | 0x20) == 'l';
+  if ((!colmaj && layout != LAPACK_ROW_MAJOR) || (!lower && (uplo | 0x20) != 'u')) return;
+  if (colmaj != lower) {
+    for (lapack_int j = 0; j < std::min(n, ldout); ++j)
+      for (lapack_int i = 0; i < std::min(j + 1, ldin); ++i) out[j + (size_t)i * ldout] = in[i + (size_t)j * ldin];
+  } else {
+    for (lapack_int j = 0; j < std::min(n, ldout); ++j)
+      for (lapack_int i = j; i < std::min(n, ldin); ++i) out[j + (size_t)i * ldout] = in[i + (size_t)j * ldin];
+  }
+}
+
+// ---- POTRF / POTRS / POSV (LAPACKE/src/lapacke_dpotrf*.c, dpotrs*.c, dposv*.c)
+template <typename T, typename F>
+lapack_int potrf_work(const char* nm, F fort, int layout, char uplo, lapack_int n, T* a, lapack_int lda) {
+  lapack_int info = 0;
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&uplo, &n, a, &lda, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  if (!a_t) { LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR); return LAPACK_TRANSPOSE_MEMORY_ERROR; }
+  tr_trans(layout, uplo, n, a, lda, a_t, lda_t);
+  fort(&uplo, &n, a_t, &lda_t, &info, 1);
+  if (info < 0) info -= 1;
+  tr_trans(LAPACK_COL_MAJOR, uplo, n, a_t, lda_t, a, lda);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+// potrs (solve only, A not written back) and posv (factor written back)
+template <typename T, typename F>
+lapack_int potrs_posv_work(const char* nm, F fort, bool write_a, int layout, char uplo, lapack_int n, lapack_int nrhs,
+                           T* a, lapack_int lda, T* b, lapack_int ldb) {
+  lapack_int info = 0;
+  if (layout == LAPACK_COL_MAJOR) {
+    fort(&uplo, &n, &nrhs, a, &lda, b, &ldb, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -6); return -6; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -8); return -8; }
+  T* a_t = alloc<T>((size_t)lda_t * std::max(1, n));
+  T* b_t = a_t ? alloc<T>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  if (!b_t) {
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  tr_trans(layout, uplo, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  fort(&uplo, &n, &nrhs, a_t, &lda_t, b_t, &ldb_t, &info, 1);
+  if (info < 0) info -= 1;
+  if (write_a) tr_trans(LAPACK_COL_MAJOR, uplo, n, a_t, lda_t, a, lda);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, b_t, ldb_t, b, ldb);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+
 }  // namespace
 
 extern "C" {
@@ -658,6 +749,127 @@ lapack_int LAPACKE_dgetri(int layout, lapack_int n, double* a, lapack_int lda, c
   }
   info = LAPACKE_dgetri_work(layout, n, a, lda, ipiv, work, lwork);
   LAPACKE_free_proxy(work);
+  return info;
+}
+
+// ---------------------------------------------------------------- POTRF / POTRS / POSV / SPOSV
+lapack_int LAPACKE_dpotrf_work(int layout, char uplo, lapack_int n, double* a, lapack_int lda) {
+  return potrf_work<double>("LAPACKE_dpotrf_work", dpotrf_, layout, uplo, n, a, lda);
+}
+lapack_int LAPACKE_spotrf_work(int layout, char uplo, lapack_int n, float* a, lapack_int lda) {
+  return potrf_work<float>("LAPACKE_spotrf_work", spotrf_, layout, uplo, n, a, lda);
+}
+lapack_int LAPACKE_dpotrf(int layout, char uplo, lapack_int n, double* a, lapack_int lda) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dpotrf", -1); return -1; }
+  if (nancheck() && tr_has_nan(layout, uplo, n, a, lda)) return -4;
+  return LAPACKE_dpotrf_work(layout, uplo, n, a, lda);
+}
+lapack_int LAPACKE_spotrf(int layout, char uplo, lapack_int n, float* a, lapack_int lda) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_spotrf", -1); return -1; }
+  if (nancheck() && tr_has_nan(layout, uplo, n, a, lda)) return -4;
+  return LAPACKE_spotrf_work(layout, uplo, n, a, lda);
+}
+lapack_int LAPACKE_dpotrs_work(int layout, char uplo, lapack_int n, lapack_int nrhs, const double* a, lapack_int lda,
+                               double* b, lapack_int ldb) {
+  return potrs_posv_work<double>("LAPACKE_dpotrs_work",
+                                 [](const char* u, const lapack_int* nn, const lapack_int* nr, double* aa,
+                                    const lapack_int* la, double* bb, const lapack_int* lb, lapack_int* inf,
+                                    size_t len) { dpotrs_(u, nn, nr, aa, la, bb, lb, inf, len); },
+                                 false, layout, uplo, n, nrhs, const_cast<double*>(a), lda, b, ldb);
+}
+lapack_int LAPACKE_spotrs_work(int layout, char uplo, lapack_int n, lapack_int nrhs, const float* a, lapack_int lda,
+                               float* b, lapack_int ldb) {
+  return potrs_posv_work<float>("LAPACKE_spotrs_work",
+                                [](const char* u, const lapack_int* nn, const lapack_int* nr, float* aa,
+                                   const lapack_int* la, float* bb, const lapack_int* lb, lapack_int* inf,
+                                   size_t len) { spotrs_(u, nn, nr, aa, la, bb, lb, inf, len); },
+                                false, layout, uplo, n, nrhs, const_cast<float*>(a), lda, b, ldb);
+}
+lapack_int LAPACKE_dpotrs(int layout, char uplo, lapack_int n, lapack_int nrhs, const double* a, lapack_int lda,
+                          double* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dpotrs", -1); return -1; }
+  if (nancheck()) {
+    if (tr_has_nan(layout, uplo, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  return LAPACKE_dpotrs_work(layout, uplo, n, nrhs, a, lda, b, ldb);
+}
+lapack_int LAPACKE_spotrs(int layout, char uplo, lapack_int n, lapack_int nrhs, const float* a, lapack_int lda,
+                          float* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_spotrs", -1); return -1; }
+  if (nancheck()) {
+    if (tr_has_nan(layout, uplo, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  return LAPACKE_spotrs_work(layout, uplo, n, nrhs, a, lda, b, ldb);
+}
+lapack_int LAPACKE_dposv_work(int layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                              double* b, lapack_int ldb) {
+  return potrs_posv_work<double>("LAPACKE_dposv_work", dposv_, true, layout, uplo, n, nrhs, a, lda, b, ldb);
+}
+lapack_int LAPACKE_dposv(int layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda, double* b,
+                         lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dposv", -1); return -1; }
+  if (nancheck()) {
+    if (tr_has_nan(layout, uplo, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  return LAPACKE_dposv_work(layout, uplo, n, nrhs, a, lda, b, ldb);
+}
+lapack_int LAPACKE_dsposv_work(int layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                               const double* b, lapack_int ldb, double* x, lapack_int ldx, double* work, float* swork,
+                               lapack_int* iter) {
+  // LAPACKE/src/lapacke_dsposv_work.c: row major LDA < N -6, LDB < NRHS -8,
+  // LDX < NRHS -10; A (the triangle) and X written back
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_dsposv_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    dsposv_(&uplo, &n, &nrhs, a, &lda, b, &ldb, x, &ldx, work, swork, iter, &info, 1);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n), ldx_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -6); return -6; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -8); return -8; }
+  if (ldx < nrhs) { LAPACKE_xerbla(nm, -10); return -10; }
+  double* a_t = alloc<double>((size_t)lda_t * std::max(1, n));
+  double* b_t = a_t ? alloc<double>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  double* x_t = b_t ? alloc<double>((size_t)ldx_t * std::max(1, nrhs)) : nullptr;
+  if (!x_t) {
+    if (b_t) LAPACKE_free_proxy(b_t);
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  tr_trans(layout, uplo, n, a, lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, b, ldb, b_t, ldb_t);
+  dsposv_(&uplo, &n, &nrhs, a_t, &lda_t, b_t, &ldb_t, x_t, &ldx_t, work, swork, iter, &info, 1);
+  if (info < 0) info -= 1;
+  tr_trans(LAPACK_COL_MAJOR, uplo, n, a_t, lda_t, a, lda);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, x_t, ldx_t, x, ldx);
+  LAPACKE_free_proxy(x_t);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_dsposv(int layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
+                          const double* b, lapack_int ldb, double* x, lapack_int ldx, lapack_int* iter) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_dsposv", -1); return -1; }
+  if (nancheck()) {
+    if (tr_has_nan(layout, uplo, n, a, lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, b, ldb)) return -7;
+  }
+  float* swork = alloc<float>((size_t)std::max(1, n) * std::max(1, n + nrhs));
+  double* work = swork ? alloc<double>((size_t)std::max(1, n) * std::max(1, nrhs)) : nullptr;
+  if (!work) {
+    if (swork) LAPACKE_free_proxy(swork);
+    LAPACKE_xerbla("LAPACKE_dsposv", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_dsposv_work(layout, uplo, n, nrhs, a, lda, b, ldb, x, ldx, work, swork, iter);
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(swork);
   return info;
 }
 

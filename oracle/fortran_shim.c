@@ -21,6 +21,12 @@ void or_slag2d(int, int, const float *, int, double *, int, int *);
 void or_dsgesv(int, int, double *, int, int *, const double *, int, double *, int, double *, float *, int *, int *);
 void or_dgecon(char, int, const double *, int, double, double *, double *, int *, int *);
 void or_dgetri(int, double *, int, const int *, double *, int, int, int *);
+void or_dpotrf(char, int, double *, int, int *);
+void or_spotrf(char, int, float *, int, int *);
+void or_dpotrs(char, int, int, const double *, int, double *, int, int *);
+void or_spotrs(char, int, int, const float *, int, float *, int, int *);
+void or_dposv(char, int, int, double *, int, double *, int, int *);
+void or_dsposv(char, int, int, double *, int, const double *, int, double *, int, double *, float *, int *, int *);
 void or_dgerfs(char, int, int, const double *, int, const double *, int, const int *, const double *, int, double *,
                int, double *, double *, double *, int *, int *);
 void or_dgesvx(char, char, int, int, double *, int, double *, int, int *, char *, double *, double *, double *, int,
@@ -93,6 +99,34 @@ void dgesvx_(const char *fact, const char *trans, const int *n, const int *nrhs,
 }
 void dgetri_(const int *n, double *a, const int *lda, const int *ipiv, double *work, const int *lwork, int *info) {
   or_dgetri(*n, a, *lda, ipiv, work, *lwork, 64, info);   /* NB = ILAENV(1, 'DGETRI') = 64 */
+}
+void dpotrf_(const char *uplo, const int *n, double *a, const int *lda, int *info, size_t l) {
+  (void)l;
+  or_dpotrf(*uplo, *n, a, *lda, info);
+}
+void spotrf_(const char *uplo, const int *n, float *a, const int *lda, int *info, size_t l) {
+  (void)l;
+  or_spotrf(*uplo, *n, a, *lda, info);
+}
+void dpotrs_(const char *uplo, const int *n, const int *nrhs, const double *a, const int *lda, double *b,
+             const int *ldb, int *info, size_t l) {
+  (void)l;
+  or_dpotrs(*uplo, *n, *nrhs, a, *lda, b, *ldb, info);
+}
+void spotrs_(const char *uplo, const int *n, const int *nrhs, const float *a, const int *lda, float *b,
+             const int *ldb, int *info, size_t l) {
+  (void)l;
+  or_spotrs(*uplo, *n, *nrhs, a, *lda, b, *ldb, info);
+}
+void dposv_(const char *uplo, const int *n, const int *nrhs, double *a, const int *lda, double *b, const int *ldb,
+            int *info, size_t l) {
+  (void)l;
+  or_dposv(*uplo, *n, *nrhs, a, *lda, b, *ldb, info);
+}
+void dsposv_(const char *uplo, const int *n, const int *nrhs, double *a, const int *lda, const double *b,
+             const int *ldb, double *x, const int *ldx, double *work, float *swork, int *iter, int *info, size_t l) {
+  (void)l;
+  or_dsposv(*uplo, *n, *nrhs, a, *lda, b, *ldb, x, *ldx, work, swork, iter, info);
 }
 
 /* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */

@@ -258,3 +258,106 @@ def test_getri(libs, capfd, layout, n, extra):
         a, lda, lu, ip = _factored(libs, max(n, 2), layout, 0, 81)
         return (layout, max(n, 2), p(lu), lda - 1, p(ip)), (lu,)
     _both(libs, "LAPACKE_dgetri", bad_ld, capfd)
+
+
+def _spd(n, seed, layout, extra, dtype=np.float64, shift=1.0):
+    """A symmetric positive definite n x n matrix M M^T / n + shift * I in
+    the layout's storage (padding 7.25); `shift` < 0 makes it indefinite."""
+    rng = np.random.default_rng(seed)
+    m = rng.standard_normal((n, n))
+    a = m @ m.T / max(n, 1) + shift * np.eye(n)
+    ld = max(1, n + extra)
+    buf = np.full((max(n, 1), ld), 7.25)
+    buf[:n, :n] = a            # symmetric: the same bytes in either layout
+    return buf.astype(dtype), ld
+
+
+CHOL_CASES = [(layout, uplo, n, nrhs, extra) for layout in (101, 102) for uplo in (b"U", b"L")
+              for n in (0, 1, 5, 17, 70) for nrhs in (0, 2) for extra in (0, 3)]
+
+
+@pytest.mark.parametrize("layout,uplo,n,nrhs,extra", CHOL_CASES)
+def test_potrf_potrs_posv_dsposv(libs, capfd, layout, uplo, n, nrhs, extra):
+    """LAPACKE_{d,s}potrf, {d,s}potrs, dposv and dsposv (and their _work
+    forms through them): the stored triangle transposed for row-major, the
+    other triangle untouched, the same INFO and ITER as the reference
+    wrappers (LAPACKE/src/lapacke_dpotrf.c, dpotrs.c, dposv.c, dsposv.c)."""
+    u = ctypes.c_char(uplo)
+    for fn, dt in (("LAPACKE_dpotrf", np.float64), ("LAPACKE_spotrf", np.float32)):
+        def potrf():
+            a, lda = _spd(n, 90 + n, layout, extra, dt)
+            return (layout, u, n, p(a), lda), (a,)
+        _both(libs, fn, potrf, capfd)
+
+    for fn, dt in (("LAPACKE_dpotrs", np.float64), ("LAPACKE_spotrs", np.float32)):
+        def potrs():
+            a, lda = _spd(n, 91 + n, layout, extra, dt, shift=4.0)   # used as a factor as it stands
+            b, ldb = _mat(n, nrhs, 92 + n, layout, extra)
+            b = b.astype(dt)
+            return (layout, u, n, nrhs, p(a), lda, p(b), ldb), (a, b)
+        _both(libs, fn, potrs, capfd)
+
+    def posv():
+        a, lda = _spd(n, 93 + n, layout, extra)
+        b, ldb = _mat(n, nrhs, 94 + n, layout, extra)
+        return (layout, u, n, nrhs, p(a), lda, p(b), ldb), (a, b)
+    _both(libs, "LAPACKE_dposv", posv, capfd)
+
+    for shift in (1.0, -0.5):                  # -0.5: not positive definite, ITER = -3, FP64 fallback INFO > 0
+        def dsposv():
+            a, lda = _spd(n, 95 + n, layout, extra, shift=shift)
+            b, ldb = _mat(n, nrhs, 96 + n, layout, extra)
+            x, ldx = _mat(n, nrhs, 97 + n, layout, extra)
+            it = np.zeros(1, dtype=np.int32)
+            # INFO > 0 leaves X unset; row-major then copies back the
+            # wrapper's uninitialised X buffer, so X is compared only on success
+            outs = (a, x, it) if shift > 0 or layout == 102 else (a, it)
+            return (layout, u, n, nrhs, p(a), lda, p(b), ldb, p(x), ldx, p(it)), outs
+        _both(libs, "LAPACKE_dsposv", dsposv, capfd)
+
+
+@pytest.mark.parametrize("layout", [101, 102])
+def test_chol_error_and_nan_codes(libs, capfd, layout):
+    """Bad layout (-1), bad UPLO (Fortran -1, LAPACKE -2), row-major leading
+    dimensions (-5 / -6 / -8 / -10), NaN inside the stored triangle (-4 / -5 /
+    -7) and outside it (not checked), an indefinite matrix (INFO > 0)."""
+    def call(fn, uplo=b"U", n=6, nrhs=2, lda_off=0, ldb_off=0, ldx_off=0, nan_at=None, shift=1.0, lay=layout):
+        def build():
+            a, lda = _spd(n, 7, layout, 0, shift=shift)
+            if nan_at is not None:
+                a[nan_at] = np.nan
+            b, ldb = _mat(n, nrhs, 8, layout)
+            x, ldx = _mat(n, nrhs, 9, layout)
+            it = np.zeros(1, dtype=np.int32)
+            u = ctypes.c_char(uplo)
+            if fn == "LAPACKE_dpotrf":
+                return (lay, u, n, p(a), lda - lda_off), (a,)
+            if fn in ("LAPACKE_dpotrs", "LAPACKE_dposv"):
+                return (lay, u, n, nrhs, p(a), lda - lda_off, p(b), ldb - ldb_off), (a, b)
+            # INFO != 0 leaves X unset, and row-major copies back the
+            # wrapper's uninitialised X buffer: X is compared column-major only
+            outs = (a, x, it) if layout == 102 else (a, it)
+            return ((lay, u, n, nrhs, p(a), lda - lda_off, p(b), ldb - ldb_off, p(x), ldx - ldx_off, p(it)),
+                    outs)
+        return _both(libs, fn, build, capfd)
+
+    for fn in ("LAPACKE_dpotrf", "LAPACKE_dpotrs", "LAPACKE_dposv", "LAPACKE_dsposv"):
+        assert call(fn, lay=7) == -1
+        assert call(fn, uplo=b"X") == -2
+        # NaN in row 0, column 3: upper triangle in column-major storage
+        # (buf[col, row]) is buf[3, 0]; row-major upper is buf[0, 3]
+        upper_nan = (3, 0) if layout == 102 else (0, 3)
+        lower_nan = upper_nan[::-1]
+        code = -4 if fn == "LAPACKE_dpotrf" else -5
+        assert call(fn, uplo=b"U", nan_at=upper_nan) == code
+        assert call(fn, uplo=b"L", nan_at=lower_nan) == code
+        call(fn, uplo=b"U", nan_at=lower_nan)       # outside the stored triangle: no NaN code
+        call(fn, uplo=b"L", nan_at=upper_nan)
+        if fn != "LAPACKE_dpotrs":
+            assert call(fn, shift=-0.5) > 0
+        if layout == 101:
+            assert call(fn, lda_off=1) == (-5 if fn == "LAPACKE_dpotrf" else -6)
+            if fn != "LAPACKE_dpotrf":
+                assert call(fn, ldb_off=1) == -8
+            if fn == "LAPACKE_dsposv":
+                assert call(fn, ldx_off=1) == -10
