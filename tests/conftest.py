@@ -37,5 +37,10 @@ _AFTER_SOLVE_PATH = {"test_gpu_refine.py": 1, "test_gpu_condest.py": 2, "test_gp
                      "test_gpu_chol.py": 5}
 
 
+# The allocation-free entry point's test file comes after everything else,
+# so a run stopped at its failure has already run every other test.
+_LAST = "test_zz_no_alloc.py"
+
+
 def pytest_collection_modifyitems(session, config, items):
-    items.sort(key=lambda it: _AFTER_SOLVE_PATH.get(it.fspath.basename, 0))
+    items.sort(key=lambda it: (it.fspath.basename == _LAST, _AFTER_SOLVE_PATH.get(it.fspath.basename, 0)))
