@@ -174,7 +174,6 @@ int dsposv_dev(bool upper, int n, int nrhs, double* dA, int lda, const double* d
   *iter = 0;
   *info = 0;
   if (n == 0) return 0;
-  const Options& opt = options();
   const int up = upper ? 1 : 0;
   const size_t nn = (size_t)n * n, nr = (size_t)n * nrhs;
   size_t bytes = 0;
@@ -241,8 +240,9 @@ int dsposv_dev(bool upper, int n, int nrhs, double* dA, int lda, const double* d
   }
   *iter = -itermax - 1;
 fallback:
-  // FP64 DPOTRF on A in place, X = B, DPOTRS (SRC/dsposv.f:405-418)
-  if ((rc = potrf_dev<double>(upper, n, dA, lda, opt.nb_f64, info, s))) return rc;
+  // FP64 DPOTRF on A in place (ILAENV's block size, as DPOTRF uses), X = B,
+  // DPOTRS (SRC/dsposv.f:405-418)
+  if ((rc = potrf_dev<double>(upper, n, dA, lda, kCholNb, info, s))) return rc;
   if (*info != 0) return 0;
   if (nr > 0) GB_LAUNCH(copy_cols_kernel<double><<<nblocks(nr), 256, 0, s>>>(dB, ldb, dX, ldx, n, nrhs));
   return potrs_dev<double>(upper, n, nrhs, dA, lda, dX, ldx, s);
