@@ -34,7 +34,7 @@ def lib():
     global _LIB
     if _LIB is None:
         path = os.path.join(_HERE, "liboracle.so")
-        src = [os.path.join(_HERE, f) for f in ("oracle.c", "oracle_lu.inc")]
+        src = [os.path.join(_HERE, f) for f in ("oracle.c", "oracle_lu.inc", "oracle_chol.inc", "oracle_z.inc")]
         if not os.path.exists(path) or any(os.path.getmtime(s) > os.path.getmtime(path) for s in src):
             build()
         L = ctypes.CDLL(path)
@@ -73,6 +73,11 @@ def lib():
         L.or_dlaruv_power.argtypes = [_i, _p]
         L.or_seed_from_int.argtypes = [ctypes.c_longlong, _p]
         L.or_xerbla_last.argtypes = [_p, _i]
+        L.or_zgetrf_nb.argtypes = [_i, _i, _p, _i, _p, _p, _i]
+        L.or_zgetrf2.argtypes = [_i, _i, _p, _i, _p, _p]
+        L.or_zgetrs.argtypes = [_c, _i, _i, _p, _i, _p, _p, _i, _p]
+        L.or_zgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p]
+        L.or_izamax.argtypes = [_i, _p]
         L.or_dlamch.argtypes = [_c]
         L.or_dlamch.restype = _d
         L.or_slamch.argtypes = [_c]
@@ -465,3 +470,61 @@ def ge_test_matrix(m, n, imat, seed):
         else:
             a[:, izero - 1:] = 0.0
     return np.asfortranarray(a), izero
+
+
+# ---------------------------------------------------------------- complex LU
+def zgetrf(a, nb=64):
+    """ZGETRF (SRC/zgetrf.f) on a complex128 copy of ``a`` with block size
+    ``nb`` (nb <= 1 or >= min(m, n): ZGETRF2 alone): returns (lu, ipiv, info)."""
+    a = _colmajor(a, np.complex128)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_zgetrf_nb(m, n, _ptr(a), max(1, m), _ptr(ipiv), _ptr(info), nb)
+    return a, ipiv[: min(m, n)], int(info[0])
+
+
+def zgetrs(lu, ipiv, b, trans="N"):
+    """ZGETRS (SRC/zgetrs.f), TRANS = 'N', 'T' or 'C': returns (x, info)."""
+    lu = _colmajor(lu, np.complex128)
+    b2 = _colmajor(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_zgetrs(trans.encode(), n, nrhs, _ptr(lu), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(info))
+    return b2.reshape(np.asarray(b).shape), int(info[0])
+
+
+def zgesv(a, b):
+    """ZGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
+    a = _colmajor(a, np.complex128)
+    b2 = _colmajor(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_zgesv(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(info))
+    return a, ipiv[:n], b2.reshape(np.asarray(b).shape), int(info[0])
+
+
+def izamax(x):
+    """IZAMAX (BLAS/SRC/izamax.f90), 1-based."""
+    x = np.ascontiguousarray(x, dtype=np.complex128)
+    return lib().or_izamax(x.size, _ptr(x))
+
+
+def random_zmatrix(m, n, seed):
+    """Complex test matrix: real and imaginary parts iid N(0,1), each from
+    the DLARNV(3) stream of its own seed (seed and seed + 7919)."""
+    re = random_matrix(m, n, seed, idist=3)[0]
+    im = random_matrix(m, n, seed + 7919, idist=3)[0]
+    return np.asfortranarray(re + 1j * im)
+
+
+def zge_test_matrix(m, n, imat, seed):
+    """Complex analogue of ``ge_test_matrix``: real and imaginary parts are
+    two matrices of the same GE type (from seeds seed and seed + 1), so the
+    zero columns of types 5-7, the triangles of types 2-3 and the scalings of
+    types 10-11 carry over.  Returns (A, izero)."""
+    re, izero = ge_test_matrix(m, n, imat, seed)
+    im, _ = ge_test_matrix(m, n, imat, seed + 1)
+    return np.asfortranarray(re + 1j * im), izero

@@ -287,3 +287,42 @@ def lu_rel_diff(lu_a, lu_b, a):
     n = a.shape[0]
     scale = max(np.abs(a).max(), 1e-300) * max(n, 1) * _eps(lu_a.dtype)
     return float(np.abs(np.asarray(lu_a, np.float64) - np.asarray(lu_b, np.float64)).max() / scale)
+
+
+def zget01(a, lu, ipiv):
+    """||P L U - A||_1 / (N ||A||_1 eps) for complex factors, ZLANGE('1') on
+    moduli (TESTING/LIN/zget01.f)."""
+    a = np.asarray(a, dtype=np.complex128)
+    m, n = a.shape
+    if m == 0 or n == 0:
+        return 0.0
+    perm, L, U = unpack_lu(np.asarray(lu, dtype=np.complex128), ipiv)
+    anorm = np.abs(a).sum(axis=0).max()
+    resid = np.abs(L @ U - a[perm, :]).sum(axis=0).max()
+    if anorm <= 0:
+        return 0.0 if resid == 0 else 1.0 / EPS64
+    return ((resid / n) / anorm) / EPS64
+
+
+def zget02(a, x, b, trans="N"):
+    """max_j DZASUM(b_j - op(A) x_j) / (||op(A)||_1 DZASUM(x_j) eps)
+    (TESTING/LIN/zget02.f): ZLANGE('1') for TRANS = 'N', ZLANGE('I')
+    otherwise; DZASUM sums |re| + |im|."""
+    a = np.asarray(a, dtype=np.complex128)
+    x = np.asarray(x, dtype=np.complex128).reshape(a.shape[0], -1)
+    b = np.asarray(b, dtype=np.complex128).reshape(a.shape[0], -1)
+    if a.size == 0 or x.shape[1] == 0:
+        return 0.0
+    anorm = np.abs(a).sum(axis=0).max() if trans == "N" else np.abs(a).sum(axis=1).max()
+    if anorm <= 0:
+        return 1.0 / EPS64
+    op = a if trans == "N" else (a.T if trans == "T" else a.conj().T)
+    r = b - op @ x
+    dzasum = lambda v: np.abs(v.real).sum() + np.abs(v.imag).sum()
+    resid = 0.0
+    for j in range(x.shape[1]):
+        xn = dzasum(x[:, j])
+        if xn <= 0:
+            return 1.0 / EPS64
+        resid = max(resid, ((dzasum(r[:, j]) / anorm) / xn) / EPS64)
+    return resid

@@ -96,6 +96,8 @@ float or_slamch(char c) {
 #undef ABS_T
 #undef SFMIN_T
 
+#include "oracle_z.inc"
+
 /* ---- DLAG2S: SRC/dlag2s.f:135-146.  INFO=1 (and stop converting) at the
  * first |a| > SLAMCH('O'); a NaN passes the test and converts to NaN. */
 void or_dlag2s(int m, int n, const double *a, int lda, float *sa, int ldsa, int *info) {

@@ -459,3 +459,82 @@ def test_oracle_error_exits():
     for (m, n, lda), code in ERR_GEEQU:
         name, inf = _oracle_err(L.or_dgeequ, m, n, p(a), lda, p(w), p(w), p(w), p(w), p(w), p(info))
         assert (name, inf) == ("DGEEQU", -code)
+
+
+# ------------------------------------------------------------------ complex LU
+@pytest.mark.parametrize("imat", range(1, 12))
+@pytest.mark.parametrize("nb", sorted(set(INPUTS["dtest"]["nb"])))
+def test_zgetrf_zchkge_ratios(imat, nb):
+    """ZCHKGE tests 1 and 3 (TESTING/LIN/zchkge.f, the complex twin of
+    DCHKGE) on every M x N of dtest.in: INFO = IZERO for the zero-column
+    types, ZGET01 < THRESH, and ZGET02 < THRESH for TRANS = N, T, C."""
+    for m in INPUTS["dtest"]["m"]:
+        for n in INPUTS["dtest"]["n"]:
+            if 5 <= imat <= 7 and n < imat - 4:
+                continue
+            a, izero = oracle.zge_test_matrix(m, n, imat, 2011 + 7 * m + n)
+            lu, ipiv, info = oracle.zgetrf(a, nb=nb)
+            assert info == izero, (m, n, imat, info, izero)
+            if m and n:
+                assert ck.zget01(a, lu, ipiv) < THRESH, (m, n, imat)
+            if m == n and n > 0 and izero == 0:
+                for nrhs in INPUTS["dtest"]["nrhs"]:
+                    xact = oracle.random_zmatrix(n, nrhs, 5 + n + nrhs)
+                    for trans in "NTC":
+                        op = a if trans == "N" else (a.T if trans == "T" else a.conj().T)
+                        b = op @ xact
+                        x, info = oracle.zgetrs(lu, ipiv, b, trans)
+                        assert info == 0
+                        assert ck.zget02(a, x, b, trans) < THRESH, (n, imat, trans)
+
+
+def test_zgetrf_blocked_equals_recursive_and_ipiv_matches_openblas():
+    """ZGETRF with NB = 64 and ZGETRF2 alone apply each element's updates in
+    the same order: identical bits.  OpenBLAS's zgetrf (through scipy, an
+    independent implementation) picks the same pivots on random matrices."""
+    import scipy.linalg as sl
+    for n, seed in ((150, 3), (200, 4), (257, 5)):
+        a = oracle.random_zmatrix(n, n, seed)
+        lu, ip, info = oracle.zgetrf(a, nb=64)
+        lu2, ip2, _ = oracle.zgetrf(a, nb=1)
+        assert info == 0 and np.array_equal(ip, ip2)
+        assert lu.tobytes() == lu2.tobytes()
+        _, piv = sl.lu_factor(a)
+        assert np.array_equal(ip, piv + 1)
+
+
+def test_izamax_rules():
+    """IZAMAX (BLAS/SRC/izamax.f90): first maximum of |re| + |im|; the first
+    NaN wins outright; an infinite part wins unless a NaN follows; the
+    0.25-scaled comparison once |re| + |im| overflows."""
+    z = lambda *v: np.array(v, dtype=np.complex128)
+    assert oracle.izamax(z()) == 0
+    assert oracle.izamax(z(5 + 5j)) == 1
+    assert oracle.izamax(z(1 + 1j, -2 + 0j, 0 + 2j)) == 1       # ties: the first
+    assert oracle.izamax(z(1 + 1j, -2.5 + 0j, 0 + 2j)) == 2
+    assert oracle.izamax(z(1, complex(np.nan, 0), 1e300)) == 2
+    assert oracle.izamax(z(1, complex(np.inf, 0), 3, complex(0, np.nan))) == 4
+    assert oracle.izamax(z(1, complex(0, -np.inf), 3)) == 2
+    big = 1.5e308
+    assert oracle.izamax(z(1, complex(big, big), complex(big, 0.9 * big), complex(big, 1.1 * big))) == 4
+
+
+ERR_ZGETRF = [((-1, 0, 1), -1), ((0, -1, 1), -2), ((2, 1, 1), -4)]          # TESTING/LIN/zerrge.f:135-144
+ERR_ZGETRS = [(("/", 0, 0, 1, 1), -1), (("N", -1, 0, 1, 1), -2), (("N", 0, -1, 1, 1), -3),
+              (("N", 2, 1, 1, 2), -5), (("N", 2, 1, 2, 1), -8)]              # zerrge.f:174-190
+ERR_ZGESV = [((-1, 0, 1, 1), -1), ((0, -1, 1, 1), -2), ((2, 1, 1, 2), -4), ((2, 1, 2, 1), -7)]  # zerrvx.f:142-154
+
+
+def test_oracle_complex_error_exits():
+    L = oracle.lib()
+    a = np.zeros(16, dtype=np.complex128)
+    ip = np.zeros(4, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    for (m, n, lda), code in ERR_ZGETRF:
+        assert _oracle_err(L.or_zgetrf_nb, m, n, p(a), lda, p(ip), p(info), 64) == ("ZGETRF", -code)
+    for (tr, n, nrhs, lda, ldb), code in ERR_ZGETRS:
+        assert _oracle_err(L.or_zgetrs, tr.encode(), n, nrhs, p(a), lda, p(ip), p(a), ldb, p(info)) == ("ZGETRS", -code)
+    for (n, nrhs, lda, ldb), code in ERR_ZGESV:
+        name, inf = _oracle_err(L.or_zgesv, n, nrhs, p(a), lda, p(ip), p(a), ldb, p(info))
+        assert (name.strip(), inf) == ("ZGESV", -code)
