@@ -120,6 +120,17 @@ void dposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, doubl
 void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, double* a, const lapack_int* lda,
              const double* b, const lapack_int* ldb, double* x, const lapack_int* ldx, double* work, float* swork,
              lapack_int* iter, lapack_int* info, size_t uplo_len);
+/* Complex LU factorization, solve and driver.  Replace SRC/zgetrf.f:105,
+ * SRC/zgetrs.f:118 and SRC/zgesv.f:121 (the LAPACK_zgetrf, _zgetrs, _zgesv
+ * prototypes of lapack.h).  COMPLEX*16 arrays are (re, im) pairs of doubles;
+ * any lapack_complex_double* (C double _Complex, C++ std::complex<double>)
+ * converts to the void* parameters. */
+void zgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info);
+void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
+             const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t trans_len);
+void zgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
+            const lapack_int* ldb, lapack_int* info);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -309,6 +320,14 @@ int gb300_dpotrf_dev(char uplo, int n, double* dA, int lda, int* info, void* str
 int gb300_dpotrs_dev(char uplo, int n, int nrhs, const double* dA, int lda, double* dB, int ldb, void* stream);
 int gb300_dsposv_dev(char uplo, int n, int nrhs, double* dA, int lda, const double* dB, int ldb, double* dX, int ldx,
                      int* iter, int* info, void* stream);
+/* ZGETRF / ZGETRS / ZGESV on device memory (SRC/zgetrf.f:105,
+ * SRC/zgetrs.f:118, SRC/zgesv.f:121): dA, dB hold (re, im) double pairs,
+ * dIpiv is a device int array; INFO goes to the host int *info; the return
+ * value is 0, the negative index of an illegal argument, or a CUDA status. */
+int gb300_zgetrf_dev(int m, int n, void* dA, int lda, int* dIpiv, int* info, void* stream);
+int gb300_zgetrs_dev(char trans, int n, int nrhs, const void* dA, int lda, const int* dIpiv, void* dB, int ldb,
+                     void* stream);
+int gb300_zgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, void* dB, int ldb, int* info, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

@@ -60,6 +60,9 @@ def lib():
         L.gb300_dgecon_dev.argtypes = [ctypes.c_char, _i, _p, _i, ctypes.c_double, _p, _ip, _p]
         L.gb300_dgetri_dev.argtypes = [_i, _p, _i, _p, _ip, _p]
         L.gb300_dgerfs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p]
+        L.gb300_zgetrf_dev.argtypes = [_i, _i, _p, _i, _p, _ip, _p]
+        L.gb300_zgetrs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _p, _i, _p]
+        L.gb300_zgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
         _LIB = L
     return _LIB
 
@@ -319,6 +322,40 @@ def dsposv(a, b, uplo="L"):
                   _ref(max(1, n)), _ptr(x), _ref(max(1, n)), _ptr(np.zeros(1)), _ptr(np.zeros(1, np.float32)),
                   ctypes.byref(it), ctypes.byref(info), _sz(1))
     return a, x.reshape(np.asarray(b).shape), it.value, info.value
+
+
+def zgetrf(a):
+    """ZGETRF (SRC/zgetrf.f) on a complex128 copy of ``a``: returns (lu, ipiv, info)."""
+    a = _fortran(a, np.complex128)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().zgetrf_(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv), ctypes.byref(info))
+    return a, ipiv[: min(m, n)], info.value
+
+
+def zgetrs(lu, ipiv, b, trans="N"):
+    """ZGETRS (SRC/zgetrs.f), TRANS = 'N', 'T' or 'C': returns (x, info)."""
+    lu = _fortran(lu, np.complex128)
+    b2 = _fortran(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().zgetrs_(ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(lu), _ref(max(1, n)), _ptr(ipiv),
+                  _ptr(b2), _ref(max(1, n)), ctypes.byref(info), _sz(1))
+    return b2.reshape(np.asarray(b).shape), info.value
+
+
+def zgesv(a, b):
+    """ZGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
+    a = _fortran(a, np.complex128)
+    b2 = _fortran(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    info = ctypes.c_int(0)
+    lib().zgesv_(_ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)),
+                 ctypes.byref(info))
+    return a, ipiv[:n], b2.reshape(np.asarray(b).shape), info.value
 
 
 def laswp(a, k1, k2, ipiv, incx=1):

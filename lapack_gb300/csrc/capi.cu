@@ -4,6 +4,7 @@
 #include "../../include/lapack_gb300.h"
 #include "driver.h"
 #include "latrs_seq.h"
+#include "zlu_seq.h"
 
 #include <algorithm>
 #include <cmath>
@@ -671,6 +672,92 @@ void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, doub
   *info = inf;
 }
 
+// ---------------------------------------------------------------- complex LU
+// COMPLEX*16 arrays are (re, im) pairs of doubles; ZGETRF uses ILAENV's
+// block size 64, as the reference does.
+void zgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info) {
+  // SRC/zgetrf.f:144-157
+  *info = 0;
+  if (*m < 0) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*lda < std::max(1, *m)) *info = -4;
+  if (*info != 0) { call_xerbla("ZGETRF", -*info); return; }
+  if (*m == 0 || *n == 0) return;
+  using gb::zdc;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M), mn = std::min(M, N);
+  DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dP(sizeof(int) * mn, s);
+  if (!dA.p || !dP.p) { device_failure("ZGETRF", (int)cudaErrorMemoryAllocation, info); return; }
+  zdc* ha = static_cast<zdc*>(a);
+  int inf = 0;
+  int rc = h2d(dA.as<zdc>(), ld, ha, *lda, M, N, s);
+  if (!rc) rc = gb::zgetrf_dev(M, N, dA.as<zdc>(), ld, dP.as<int>(), 64, &inf, s);
+  if (!rc) rc = d2h(ha, *lda, dA.as<zdc>(), ld, M, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("ZGETRF", rc, info); return; }
+  *info = inf;
+}
+
+void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
+             const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  // SRC/zgetrs.f:157-177
+  *info = 0;
+  const bool notran = lsame(*trans, 'N'), tr = lsame(*trans, 'T'), cj = lsame(*trans, 'C');
+  if (!notran && !tr && !cj) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -8;
+  if (*info != 0) { call_xerbla("ZGETRS", -*info); return; }
+  if (*n == 0 || *nrhs == 0) return;
+  using gb::zdc;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dB(sizeof(zdc) * (size_t)ld * R, s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure("ZGETRS", (int)cudaErrorMemoryAllocation, info); return; }
+  zdc* hb = static_cast<zdc*>(b);
+  int rc = h2d(dA.as<zdc>(), ld, static_cast<const zdc*>(a), *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<zdc>(), ld, static_cast<const zdc*>(hb), *ldb, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::zgetrs_dev(notran ? 0 : (tr ? 1 : 2), N, R, dA.as<zdc>(), ld, dP.as<int>(), dB.as<zdc>(), ld, s);
+  if (!rc) rc = d2h(hb, *ldb, dB.as<zdc>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure("ZGETRS", rc, info);
+}
+
+void zgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
+            const lapack_int* ldb, lapack_int* info) {
+  // SRC/zgesv.f:148-177: the solve only when the factorization succeeded
+  *info = 0;
+  if (*n < 0) *info = -1;
+  else if (*nrhs < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  if (*info != 0) { call_xerbla("ZGESV ", -*info); return; }
+  if (*n == 0) return;
+  using gb::zdc;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dB(sizeof(zdc) * (size_t)ld * std::max(R, 1), s),
+      dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure("ZGESV", (int)cudaErrorMemoryAllocation, info); return; }
+  zdc* ha = static_cast<zdc*>(a);
+  zdc* hb = static_cast<zdc*>(b);
+  int inf = 0;
+  int rc = h2d(dA.as<zdc>(), ld, ha, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<zdc>(), ld, static_cast<const zdc*>(hb), *ldb, N, R, s);
+  if (!rc) rc = gb::zgetrf_dev(N, N, dA.as<zdc>(), ld, dP.as<int>(), 64, &inf, s);
+  if (!rc && inf == 0) rc = gb::zgetrs_dev(0, N, R, dA.as<zdc>(), ld, dP.as<int>(), dB.as<zdc>(), ld, s);
+  if (!rc) rc = d2h(ha, *lda, dA.as<zdc>(), ld, N, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc && inf == 0) rc = d2h(hb, *ldb, dB.as<zdc>(), ld, N, R, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure("ZGESV", rc, info); return; }
+  *info = inf;
+}
+
 void dlag2s_(const lapack_int* m, const lapack_int* n, const double* a, const lapack_int* lda, float* sa,
              const lapack_int* ldsa, lapack_int* info) {
   // SRC/dlag2s.f:135-146: no argument checks; conversion in column order
@@ -936,6 +1023,46 @@ int gb300_dsposv_dev(char uplo, int n, int nrhs, double* dA, int lda, const doub
   int rc = gb::dsposv_dev(lsame(uplo, 'U'), n, nrhs, dA, lda, dB, ldb, dX, ldx, &it, &inf, s);
   if (!rc) rc = finish(s);
   if (iter) *iter = it;
+  if (info) *info = inf;
+  return rc;
+}
+
+int gb300_zgetrf_dev(int m, int n, void* dA, int lda, int* dIpiv, int* info, void* stream) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, m)) return -4;
+  cudaStream_t s = (cudaStream_t)stream;
+  int inf = 0;
+  int rc = gb::zgetrf_dev(m, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
+  if (!rc) rc = finish(s);
+  if (info) *info = inf;
+  return rc;
+}
+int gb300_zgetrs_dev(char trans, int n, int nrhs, const void* dA, int lda, const int* dIpiv, void* dB, int ldb,
+                     void* stream) {
+  const bool notran = lsame(trans, 'N'), tr = lsame(trans, 'T');
+  if (!notran && !tr && !lsame(trans, 'C')) return -1;
+  if (n < 0) return -2;
+  if (nrhs < 0) return -3;
+  if (lda < std::max(1, n)) return -5;
+  if (ldb < std::max(1, n)) return -8;
+  cudaStream_t s = (cudaStream_t)stream;
+  int rc = gb::zgetrs_dev(notran ? 0 : (tr ? 1 : 2), n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv,
+                          static_cast<gb::zdc*>(dB), ldb, s);
+  if (!rc) rc = finish(s);
+  return rc;
+}
+int gb300_zgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, void* dB, int ldb, int* info, void* stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  if (ldb < std::max(1, n)) return -7;
+  cudaStream_t s = (cudaStream_t)stream;
+  int inf = 0;
+  int rc = gb::zgetrf_dev(n, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
+  if (!rc && inf == 0) rc = gb::zgetrs_dev(0, n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv,
+                                           static_cast<gb::zdc*>(dB), ldb, s);
+  if (!rc) rc = finish(s);
   if (info) *info = inf;
   return rc;
 }

@@ -129,6 +129,21 @@ void dsposv_(const char *uplo, const int *n, const int *nrhs, double *a, const i
   or_dsposv(*uplo, *n, *nrhs, a, *lda, b, *ldb, x, *ldx, work, swork, iter, info);
 }
 
+void or_zgetrf(int, int, void *, int, int *, int *);
+void or_zgetrs(char, int, int, const void *, int, const int *, void *, int, int *);
+void or_zgesv(int, int, void *, int, int *, void *, int, int *);
+void zgetrf_(const int *m, const int *n, void *a, const int *lda, int *ipiv, int *info) {
+  or_zgetrf(*m, *n, a, *lda, ipiv, info);
+}
+void zgetrs_(const char *trans, const int *n, const int *nrhs, const void *a, const int *lda, const int *ipiv,
+             void *b, const int *ldb, int *info, size_t l) {
+  (void)l;
+  or_zgetrs(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void zgesv_(const int *n, const int *nrhs, void *a, const int *lda, int *ipiv, void *b, const int *ldb, int *info) {
+  or_zgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+
 /* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */
 int lsame_(const char *ca, const char *cb, size_t la, size_t lb) {
   (void)la;

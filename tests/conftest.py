@@ -30,11 +30,11 @@ def exact_mode(gpu):
 
 
 # Routines beyond the solve path itself (refinement with error bounds,
-# condition estimation, the expert driver, the inverse, Cholesky) run after
+# condition estimation, the expert driver, the inverse, Cholesky, complex LU) run after
 # the solve-path tests, so that a run
 # stopped at its first failure (-x) still reports the solve path in full.
 _AFTER_SOLVE_PATH = {"test_gpu_refine.py": 1, "test_gpu_condest.py": 2, "test_gpu_svx.py": 3, "test_gpu_getri.py": 4,
-                     "test_gpu_chol.py": 5}
+                     "test_gpu_chol.py": 5, "test_gpu_zlu.py": 6}
 
 
 # The allocation-free entry point's test file comes after everything else,

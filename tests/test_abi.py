@@ -149,6 +149,19 @@ def test_fortran_abi_error_exits(lib):
         assert np.isnan(rc.value) and info.value == -5
         lib.dgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
         assert info.value == 0
+        # complex LU: TESTING/LIN/zerrge.f:135-190, zerrvx.f:142-154
+        for (m, n, lda), code in ERR_GETRF:
+            lib.zgetrf_(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("ZGETRF", code)
+        for (tr, n, nrhs, lda, ldb), code in ERR_GETRS:
+            lib.zgetrs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb),
+                        ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("ZGETRS", code)
+        for (n, nrhs, lda, ldb), code in ERR_GESV:
+            lib.zgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("ZGESV", code)
+        lib.zgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
+        assert info.value == 0
         fb = np.full(4, 7.0)
         lib.dgerfs_(ctypes.c_char_p(b"T"), _i(0), _i(2), p(a), _i(1), p(a), _i(1), p(ip), p(a), _i(1), p(a), _i(1),
                     p(fb), p(fb[2:]), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))

@@ -1,0 +1,142 @@
+"""Complex LU on the GPU (SRC/zgetrf.f, SRC/zgetrf2.f, SRC/zgetrs.f,
+SRC/zgesv.f) against the oracle's restatement.
+
+The GPU runs the reference's block loop and panel recursion with every
+element's operations in the reference order, so factors, IPIV, INFO and
+solutions are compared bit for bit with the oracle (NaN results counted
+equal whatever their sign or payload).  The ZCHKGE ratios (ZGET01, ZGET02
+below THRESH for TRANS = N, T, C) and the device entry points are checked
+too."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+import oracle.checks as ck
+
+pytestmark = pytest.mark.gpu
+THRESH = 30.0
+
+
+def _same_bits(x, y):
+    """Bitwise equality with every NaN counted equal to every NaN (IEEE 754
+    leaves the sign and payload of a NaN result open)."""
+    x = np.asfortranarray(x).ravel(order="F").view(np.float64)
+    y = np.asfortranarray(y).ravel(order="F").view(np.float64)
+    nx, ny = np.isnan(x), np.isnan(y)
+    return x.shape == y.shape and np.array_equal(nx, ny) and x[~nx].tobytes() == y[~ny].tobytes()
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (5, 1), (1, 5), (7, 7), (65, 65), (130, 97), (97, 130), (200, 200),
+                                 (300, 300)])
+def test_zgetrf_bitwise(gpu, m, n):
+    a = oracle.random_zmatrix(m, n, 17 * m + n)
+    lu_r, ip_r, info_r = oracle.zgetrf(a)
+    lu_g, ip_g, info_g = gpu.zgetrf(a)
+    assert info_g == info_r == 0
+    assert np.array_equal(ip_g, ip_r)
+    assert _same_bits(lu_g, lu_r)
+
+
+@pytest.mark.parametrize("kind", ["zero_cols", "tiny", "signed_zeros", "inf"])
+def test_zgetrf_edge_cases_bitwise(gpu, kind):
+    """Zero columns (INFO = the first), pivots below the safe minimum (the
+    division branch of ZGETRF2), signed zeros (ZTRSM's ALPHA*B and ZGEMM's
+    ALPHA*B(L,J) products decide their signs), an infinite entry."""
+    for m, n in ((40, 40), (130, 100)):
+        a = oracle.random_zmatrix(m, n, 3 * m + n)
+        if kind == "zero_cols":
+            a[:, n // 3] = 0
+            a[:, (2 * n) // 3] = 0
+        elif kind == "tiny":
+            a = a * 1e-306
+        elif kind == "signed_zeros":
+            rng = np.random.default_rng(m + n)
+            re = np.where(rng.random((m, n)) < 0.3, np.where(rng.random((m, n)) < 0.5, 0.0, -0.0), a.real)
+            im = np.where(rng.random((m, n)) < 0.3, -0.0, a.imag)
+            a = re + 1j * im
+        elif kind == "inf":
+            a[m // 2, n // 2] = complex(np.inf, 1.0)
+        lu_r, ip_r, info_r = oracle.zgetrf(a)
+        lu_g, ip_g, info_g = gpu.zgetrf(a)
+        assert info_g == info_r, (kind, m, n)
+        assert np.array_equal(ip_g, ip_r)
+        assert _same_bits(lu_g, lu_r)
+        if kind == "zero_cols":
+            assert info_g == n // 3 + 1
+
+
+@pytest.mark.parametrize("trans", "NTC")
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (5, 3), (64, 2), (130, 4), (257, 1)])
+def test_zgetrs_bitwise(gpu, trans, n, nrhs):
+    a = oracle.random_zmatrix(n, n, 100 + n)
+    lu, ip, info = oracle.zgetrf(a)
+    assert info == 0
+    b = oracle.random_zmatrix(n, nrhs, 200 + n)
+    x_r, _ = oracle.zgetrs(lu, ip, b, trans)
+    x_g, info = gpu.zgetrs(lu, ip, b, trans)
+    assert info == 0
+    assert _same_bits(x_g, x_r)
+
+
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_zgesv_zchkge_ratios(gpu, imat):
+    """ZCHKGE tests 1 and 3 on the GPU: INFO = IZERO for the zero-column
+    types, ZGET01 < THRESH, ZGET02 < THRESH for TRANS = N, T, C; ZGESV's
+    solution equal to the oracle's."""
+    for n in (3, 10, 50, 200):
+        if 5 <= imat <= 7 and n < imat - 4:
+            continue
+        a, izero = oracle.zge_test_matrix(n, n, imat, 2011 + 9 * n)
+        lu, ipiv, info = gpu.zgetrf(a)
+        assert info == izero, (n, imat, info, izero)
+        assert ck.zget01(a, lu, ipiv) < THRESH, (n, imat)
+        if izero:
+            continue
+        xact = oracle.random_zmatrix(n, 2, 5 + n)
+        for trans in "NTC":
+            op = a if trans == "N" else (a.T if trans == "T" else a.conj().T)
+            b = op @ xact
+            x, info = gpu.zgetrs(lu, ipiv, b, trans)
+            assert info == 0 and ck.zget02(a, x, b, trans) < THRESH, (n, imat, trans)
+        b = a @ xact
+        _, ip_g, x_g, info_g = gpu.zgesv(a, b)
+        _, ip_r, x_r, info_r = oracle.zgesv(a, b)
+        assert info_g == info_r == 0 and np.array_equal(ip_g, ip_r)
+        assert _same_bits(x_g, x_r)
+
+
+def test_zgesv_singular_leaves_b(gpu):
+    """ZGESV with a zero column: INFO > 0, the factorization completed, B
+    not solved (SRC/zgesv.f:165-172)."""
+    n = 20
+    a = oracle.random_zmatrix(n, n, 4)
+    a[:, 7] = 0
+    b = oracle.random_zmatrix(n, 2, 5)
+    lu_g, ip_g, x_g, info_g = gpu.zgesv(a, b)
+    lu_r, ip_r, x_r, info_r = oracle.zgesv(a, b)
+    assert info_g == info_r == 8
+    assert _same_bits(lu_g, lu_r) and np.array_equal(ip_g, ip_r)
+    assert np.asfortranarray(x_g).tobytes() == np.asfortranarray(b).tobytes()
+
+
+def test_zgesv_device_api_matches_host_abi(gpu):
+    import torch
+    n, nrhs = 150, 3
+    a = oracle.random_zmatrix(n, n, 77)
+    b = oracle.random_zmatrix(n, nrhs, 78)
+    lu_h, ip_h, x_h, info_h = gpu.zgesv(a, b)
+    A = gpu.to_colmajor(a)
+    B = gpu.to_colmajor(b)
+    ip = torch.zeros(n, dtype=torch.int32, device="cuda")
+    inf = ctypes.c_int(-7)
+    lda, pa = gpu._colmajor_view(A)
+    ldb, pb = gpu._colmajor_view(B)
+    rc = gpu.lib().gb300_zgesv_dev(n, nrhs, ctypes.c_void_p(pa), lda, ctypes.c_void_p(ip.data_ptr()),
+                                   ctypes.c_void_p(pb), ldb, ctypes.byref(inf), gpu._stream_ptr(None))
+    torch.cuda.synchronize()
+    assert rc == 0 and inf.value == 0 == info_h
+    assert np.array_equal(ip.cpu().numpy(), ip_h)
+    assert _same_bits(A.cpu().numpy(), lu_h)
+    assert _same_bits(B.cpu().numpy(), x_h)
