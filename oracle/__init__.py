@@ -73,11 +73,15 @@ def lib():
         L.or_dlaruv_power.argtypes = [_i, _p]
         L.or_seed_from_int.argtypes = [ctypes.c_longlong, _p]
         L.or_xerbla_last.argtypes = [_p, _i]
-        L.or_zgetrf_nb.argtypes = [_i, _i, _p, _i, _p, _p, _i]
-        L.or_zgetrf2.argtypes = [_i, _i, _p, _i, _p, _p]
-        L.or_zgetrs.argtypes = [_c, _i, _i, _p, _i, _p, _p, _i, _p]
-        L.or_zgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p]
-        L.or_izamax.argtypes = [_i, _p]
+        for pre in "zc":
+            getattr(L, f"or_{pre}getrf_nb").argtypes = [_i, _i, _p, _i, _p, _p, _i]
+            getattr(L, f"or_{pre}getrf2").argtypes = [_i, _i, _p, _i, _p, _p]
+            getattr(L, f"or_{pre}getrs").argtypes = [_c, _i, _i, _p, _i, _p, _p, _i, _p]
+            getattr(L, f"or_{pre}gesv").argtypes = [_i, _i, _p, _i, _p, _p, _i, _p]
+            getattr(L, f"or_{pre}iamax").argtypes = [_i, _p]
+        L.or_zcgesv.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _p, _p, _p, _p, _p]
+        L.or_zlange_inf.argtypes = [_i, _i, _p, _i, _p]
+        L.or_zlange_inf.restype = _d
         L.or_dlamch.argtypes = [_c]
         L.or_dlamch.restype = _d
         L.or_slamch.argtypes = [_c]
@@ -473,43 +477,72 @@ def ge_test_matrix(m, n, imat, seed):
 
 
 # ---------------------------------------------------------------- complex LU
-def zgetrf(a, nb=64):
-    """ZGETRF (SRC/zgetrf.f) on a complex128 copy of ``a`` with block size
-    ``nb`` (nb <= 1 or >= min(m, n): ZGETRF2 alone): returns (lu, ipiv, info)."""
-    a = _colmajor(a, np.complex128)
+def _zpre(dtype):
+    return "c" if np.dtype(dtype) == np.complex64 else "z"
+
+
+def zgetrf(a, nb=64, dtype=np.complex128):
+    """ZGETRF (SRC/zgetrf.f; CGETRF for dtype complex64) on a copy of ``a``
+    with block size ``nb`` (nb <= 1 or >= min(m, n): xGETRF2 alone): returns
+    (lu, ipiv, info)."""
+    a = _colmajor(a, dtype)
     m, n = a.shape
     ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
     info = np.zeros(1, dtype=np.int32)
-    lib().or_zgetrf_nb(m, n, _ptr(a), max(1, m), _ptr(ipiv), _ptr(info), nb)
+    getattr(lib(), f"or_{_zpre(dtype)}getrf_nb")(m, n, _ptr(a), max(1, m), _ptr(ipiv), _ptr(info), nb)
     return a, ipiv[: min(m, n)], int(info[0])
 
 
 def zgetrs(lu, ipiv, b, trans="N"):
-    """ZGETRS (SRC/zgetrs.f), TRANS = 'N', 'T' or 'C': returns (x, info)."""
-    lu = _colmajor(lu, np.complex128)
-    b2 = _colmajor(_as2d(b), np.complex128)
+    """ZGETRS / CGETRS (SRC/zgetrs.f), TRANS = 'N', 'T' or 'C', in the
+    precision of ``lu``: returns (x, info)."""
+    dtype = np.complex64 if np.asarray(lu).dtype == np.complex64 else np.complex128
+    lu = _colmajor(lu, dtype)
+    b2 = _colmajor(_as2d(b), dtype)
     n, nrhs = b2.shape
     ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
     info = np.zeros(1, dtype=np.int32)
-    lib().or_zgetrs(trans.encode(), n, nrhs, _ptr(lu), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(info))
+    getattr(lib(), f"or_{_zpre(dtype)}getrs")(trans.encode(), n, nrhs, _ptr(lu), max(1, n), _ptr(ipiv), _ptr(b2),
+                                              max(1, n), _ptr(info))
     return b2.reshape(np.asarray(b).shape), int(info[0])
 
 
-def zgesv(a, b):
-    """ZGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
-    a = _colmajor(a, np.complex128)
-    b2 = _colmajor(_as2d(b), np.complex128)
+def zgesv(a, b, dtype=np.complex128):
+    """ZGESV / CGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
+    a = _colmajor(a, dtype)
+    b2 = _colmajor(_as2d(b), dtype)
     n, nrhs = b2.shape
     ipiv = np.zeros(max(1, n), dtype=np.int32)
     info = np.zeros(1, dtype=np.int32)
-    lib().or_zgesv(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(info))
+    getattr(lib(), f"or_{_zpre(dtype)}gesv")(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n),
+                                             _ptr(info))
     return a, ipiv[:n], b2.reshape(np.asarray(b).shape), int(info[0])
 
 
+def zcgesv(a, b):
+    """ZCGESV (SRC/zcgesv.f): returns (a_out, ipiv, x, iter, info); a_out
+    holds the COMPLEX*16 factors when the refinement fell back (ITER < 0)."""
+    a = _colmajor(a, np.complex128)
+    b2 = _colmajor(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    x = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    work = np.zeros(max(1, n * nrhs), dtype=np.complex128)
+    swork = np.zeros(max(1, n * (n + nrhs)), dtype=np.complex64)
+    rwork = np.zeros(max(1, n))
+    it = np.zeros(1, dtype=np.int32)
+    info = np.zeros(1, dtype=np.int32)
+    lib().or_zcgesv(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b2), max(1, n), _ptr(x), max(1, n), _ptr(work),
+                    _ptr(swork), _ptr(rwork), _ptr(it), _ptr(info))
+    return a, ipiv[:n], x.reshape(np.asarray(b).shape), int(it[0]), int(info[0])
+
+
 def izamax(x):
-    """IZAMAX (BLAS/SRC/izamax.f90), 1-based."""
-    x = np.ascontiguousarray(x, dtype=np.complex128)
-    return lib().or_izamax(x.size, _ptr(x))
+    """IZAMAX (BLAS/SRC/izamax.f90), 1-based; ICAMAX for complex64 input."""
+    x = np.asarray(x)
+    dtype = np.complex64 if x.dtype == np.complex64 else np.complex128
+    x = np.ascontiguousarray(x, dtype=dtype)
+    return getattr(lib(), f"or_{_zpre(dtype)}iamax")(x.size, _ptr(x))
 
 
 def random_zmatrix(m, n, seed):

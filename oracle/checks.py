@@ -326,3 +326,50 @@ def zget02(a, x, b, trans="N"):
             return 1.0 / EPS64
         resid = max(resid, ((dzasum(r[:, j]) / anorm) / xn) / EPS64)
     return resid
+
+
+def _ref_zresidual(a, x, b):
+    """B - A X with the oracle's restatement of the reference ZGEMM
+    (BLAS/SRC/zgemm.f), the call ZGET08 makes."""
+    import ctypes
+    import oracle
+
+    class Z(ctypes.Structure):
+        _fields_ = [("re", ctypes.c_double), ("im", ctypes.c_double)]
+
+    a = np.asfortranarray(a, dtype=np.complex128)
+    x = np.asfortranarray(x, dtype=np.complex128)
+    r = np.asfortranarray(np.array(b, dtype=np.complex128, copy=True))
+    m, k = a.shape
+    if m == 0 or r.shape[1] == 0:
+        return r
+    p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
+    f = oracle.lib().or_zgemm_nn
+    f.argtypes = [ctypes.c_int] * 3 + [Z, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_void_p, ctypes.c_int]
+    f(m, r.shape[1], k, Z(-1.0, 0.0), p(a), max(1, m), p(x), max(1, k), p(r), max(1, m))
+    return r
+
+
+def zget08(a, x, b):
+    """max_j CABS1(r(IZAMAX r)) / (||A||_inf CABS1(x(IZAMAX x)) eps), r =
+    b_j - A x_j (TESTING/LIN/zget08.f), ||A||_inf = ZLANGE('I') on moduli."""
+    import oracle
+    a = np.asarray(a, dtype=np.complex128)
+    x = np.asarray(x, dtype=np.complex128).reshape(a.shape[1], -1)
+    b = np.asarray(b, dtype=np.complex128).reshape(a.shape[0], -1)
+    if a.size == 0 or x.shape[1] == 0:
+        return 0.0
+    anorm = np.abs(a).sum(axis=1).max()
+    if anorm <= 0:
+        return 1.0 / EPS64
+    r = _ref_zresidual(a, x, b)
+    cabs1 = lambda z: abs(z.real) + abs(z.imag)
+    resid = 0.0
+    for j in range(x.shape[1]):
+        xn = cabs1(x[oracle.izamax(x[:, j]) - 1, j])
+        if xn <= 0:
+            return 1.0 / EPS64
+        rn = cabs1(r[oracle.izamax(np.ascontiguousarray(r[:, j])) - 1, j])
+        resid = max(resid, ((rn / anorm) / xn) / EPS64)
+    return resid

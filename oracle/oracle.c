@@ -96,7 +96,155 @@ float or_slamch(char c) {
 #undef ABS_T
 #undef SFMIN_T
 
+/* Complex LU: COMPLEX*16 (or_z...) and COMPLEX (or_c...) from one source. */
+#define ZT double
+#define ZC zcd
+#define ZH(x) zcd_##x
+#define ZFN(x) or_z##x
+#define ZNAME "Z"
+#define ZABS fabs
+#define ZHYPOT hypot
+#define ZHUGE DBL_MAX
+#define ZSFMIN DBL_MIN
 #include "oracle_z.inc"
+#undef ZT
+#undef ZC
+#undef ZH
+#undef ZFN
+#undef ZNAME
+#undef ZABS
+#undef ZHYPOT
+#undef ZHUGE
+#undef ZSFMIN
+#define ZT float
+#define ZC zcf
+#define ZH(x) zcf_##x
+#define ZFN(x) or_c##x
+#define ZNAME "C"
+#define ZABS fabsf
+#define ZHYPOT hypotf
+#define ZHUGE FLT_MAX
+#define ZSFMIN FLT_MIN
+#include "oracle_z.inc"
+#undef ZT
+#undef ZC
+#undef ZH
+#undef ZFN
+#undef ZNAME
+#undef ZABS
+#undef ZHYPOT
+#undef ZHUGE
+#undef ZSFMIN
+
+/* ---- ZCGESV (SRC/zcgesv.f:259-448): COMPLEX factorization and solves,
+ * COMPLEX*16 residual, convergence test and update, ITERMAX = 30,
+ * BWDMAX = 1, the ZGETRF / ZGETRS fallback. */
+
+/* ZLAG2C (SRC/zlag2c.f:134-153): INFO = 1 at the first part outside
+ * [-RMAX, RMAX] (RMAX = SLAMCH('O')), in column order, stopping there; a
+ * NaN passes and converts to NaN. */
+void or_zlag2c(int m, int n, const zcd *a, int lda, zcf *sa, int ldsa, int *info) {
+  const double rmax = FLT_MAX;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) {
+      const zcd v = a[(size_t)i + (size_t)j * lda];
+      if (v.re < -rmax || v.re > rmax || v.im < -rmax || v.im > rmax) { *info = 1; return; }
+      sa[(size_t)i + (size_t)j * ldsa].re = (float)v.re;
+      sa[(size_t)i + (size_t)j * ldsa].im = (float)v.im;
+    }
+  *info = 0;
+}
+
+/* CLAG2Z (SRC/clag2z.f:120-132): exact widening. */
+void or_clag2z(int m, int n, const zcf *sa, int ldsa, zcd *a, int lda, int *info) {
+  *info = 0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) {
+      a[(size_t)i + (size_t)j * lda].re = sa[(size_t)i + (size_t)j * ldsa].re;
+      a[(size_t)i + (size_t)j * lda].im = sa[(size_t)i + (size_t)j * ldsa].im;
+    }
+}
+
+/* ZLANGE('I') (SRC/zlange.f:175-190): row sums of moduli accumulated column
+ * by column, the maximum taken with NaN propagation. */
+double or_zlange_inf(int m, int n, const zcd *a, int lda, double *work) {
+  for (int i = 0; i < m; ++i) work[i] = 0.0;
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < m; ++i) work[i] = work[i] + hypot(a[(size_t)i + (size_t)j * lda].re, a[(size_t)i + (size_t)j * lda].im);
+  double value = 0.0;
+  for (int i = 0; i < m; ++i)
+    if (value < work[i] || work[i] != work[i]) value = work[i];
+  return value;
+}
+
+static double zcd_cabs1(zcd z) { return fabs(z.re) + fabs(z.im); }
+
+/* Convergence test of SRC/zcgesv.f:350-357: 1 when some column has
+ * CABS1(R(IZAMAX(R))) > CABS1(X(IZAMAX(X)))*CTE. */
+static int zcgesv_notconv(int n, int nrhs, const zcd *x, int ldx, const zcd *r, int ldr, double cte) {
+  for (int j = 0; j < nrhs; ++j) {
+    const zcd *xc = x + (size_t)j * ldx, *rc = r + (size_t)j * ldr;
+    const double xnrm = zcd_cabs1(xc[or_ziamax(n, xc) - 1]);
+    const double rnrm = zcd_cabs1(rc[or_ziamax(n, rc) - 1]);
+    if (rnrm > xnrm * cte) return 1;
+  }
+  return 0;
+}
+
+void or_zcgesv(int n, int nrhs, zcd *a, int lda, int *ipiv, const zcd *b, int ldb, zcd *x, int ldx, zcd *work,
+               zcf *swork, double *rwork, int *iter, int *info) {
+  const int itermax = 30;
+  const double bwdmax = 1.0;
+  const zcd one = {1.0, 0.0}, negone = {-1.0, 0.0};
+  *info = 0;
+  *iter = 0;
+  if (n < 0) *info = -1;
+  else if (nrhs < 0) *info = -2;
+  else if (lda < (n > 1 ? n : 1)) *info = -4;
+  else if (ldb < (n > 1 ? n : 1)) *info = -7;
+  else if (ldx < (n > 1 ? n : 1)) *info = -9;
+  if (*info != 0) { or_xerbla("ZCGESV", -*info); return; }
+  if (n == 0) return;
+  const double anrm = or_zlange_inf(n, n, a, lda, rwork);
+  const double eps = DBL_EPSILON * 0.5;
+  const double cte = anrm * eps * sqrt((double)n) * bwdmax;
+  zcf *sa = swork, *sx = swork + (size_t)n * n;
+  int inf2;
+  or_zlag2c(n, nrhs, b, ldb, sx, n, &inf2);
+  if (inf2 != 0) { *iter = -2; goto fallback; }
+  or_zlag2c(n, n, a, lda, sa, n, &inf2);
+  if (inf2 != 0) { *iter = -2; goto fallback; }
+  or_cgetrf(n, n, sa, n, ipiv, &inf2);
+  if (inf2 != 0) { *iter = -3; goto fallback; }
+  or_cgetrs('N', n, nrhs, sa, n, ipiv, sx, n, &inf2);
+  or_clag2z(n, nrhs, sx, n, x, ldx, &inf2);
+  for (int j = 0; j < nrhs; ++j)
+    for (int i = 0; i < n; ++i) work[(size_t)i + (size_t)j * n] = b[(size_t)i + (size_t)j * ldb];
+  or_zgemm_nn(n, nrhs, n, negone, a, lda, x, ldx, work, n);
+  if (!zcgesv_notconv(n, nrhs, x, ldx, work, n, cte)) { *iter = 0; return; }
+  for (int it = 1; it <= itermax; ++it) {
+    or_zlag2c(n, nrhs, work, n, sx, n, &inf2);
+    if (inf2 != 0) { *iter = -2; goto fallback; }
+    or_cgetrs('N', n, nrhs, sa, n, ipiv, sx, n, &inf2);
+    or_clag2z(n, nrhs, sx, n, work, n, &inf2);
+    for (int j = 0; j < nrhs; ++j)   /* ZAXPY (BLAS/SRC/zaxpy.f:114-122) with ZA = ONE */
+      for (int i = 0; i < n; ++i) {
+        zcd *y = &x[(size_t)i + (size_t)j * ldx];
+        *y = zcd_add(*y, zcd_mul(one, work[(size_t)i + (size_t)j * n]));
+      }
+    for (int j = 0; j < nrhs; ++j)
+      for (int i = 0; i < n; ++i) work[(size_t)i + (size_t)j * n] = b[(size_t)i + (size_t)j * ldb];
+    or_zgemm_nn(n, nrhs, n, negone, a, lda, x, ldx, work, n);
+    if (!zcgesv_notconv(n, nrhs, x, ldx, work, n, cte)) { *iter = it; return; }
+  }
+  *iter = -itermax - 1;
+fallback:
+  or_zgetrf(n, n, a, lda, ipiv, info);
+  if (*info != 0) return;
+  for (int j = 0; j < nrhs; ++j)
+    for (int i = 0; i < n; ++i) x[(size_t)i + (size_t)j * ldx] = b[(size_t)i + (size_t)j * ldb];
+  or_zgetrs('N', n, nrhs, a, lda, ipiv, x, ldx, info);
+}
 
 /* ---- DLAG2S: SRC/dlag2s.f:135-146.  INFO=1 (and stop converting) at the
  * first |a| > SLAMCH('O'); a NaN passes the test and converts to NaN. */

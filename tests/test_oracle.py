@@ -533,8 +533,57 @@ def test_oracle_complex_error_exits():
     p = lambda v: v.ctypes.data_as(ctypes.c_void_p)
     for (m, n, lda), code in ERR_ZGETRF:
         assert _oracle_err(L.or_zgetrf_nb, m, n, p(a), lda, p(ip), p(info), 64) == ("ZGETRF", -code)
+        assert _oracle_err(L.or_cgetrf_nb, m, n, p(a), lda, p(ip), p(info), 64) == ("CGETRF", -code)
     for (tr, n, nrhs, lda, ldb), code in ERR_ZGETRS:
         assert _oracle_err(L.or_zgetrs, tr.encode(), n, nrhs, p(a), lda, p(ip), p(a), ldb, p(info)) == ("ZGETRS", -code)
     for (n, nrhs, lda, ldb), code in ERR_ZGESV:
         name, inf = _oracle_err(L.or_zgesv, n, nrhs, p(a), lda, p(ip), p(a), ldb, p(info))
         assert (name.strip(), inf) == ("ZGESV", -code)
+
+
+@pytest.mark.parametrize("nrhs", INPUTS["dstest"]["nrhs"])
+def test_zcgesv_zdrvab_ratios(nrhs):
+    """ZDRVAB (TESTING/LIN/zdrvab.f:315-366) on the dstest.in sizes and the
+    ZCHKGE matrix types: INFO = IZERO; ZGET08 < sqrt(N) when ITER >= 0,
+    < THRESH when the refinement fell back (ITER < 0); A unchanged when
+    ITER >= 0, and ITER < 0 for the ill-conditioned types."""
+    for n in INPUTS["dstest"]["n"]:
+        for imat in range(1, 12):
+            if 5 <= imat <= 7 and n < imat - 4:
+                continue
+            a, izero = oracle.zge_test_matrix(n, n, imat, 1988 + 3 * n + imat)
+            xact = oracle.random_zmatrix(n, nrhs, 7 + n)
+            b = a @ xact
+            ao, ipiv, x, it, info = oracle.zcgesv(a, b)
+            assert info == izero, (n, imat, info, izero)
+            if info or n == 0:
+                continue
+            r = ck.zget08(a, x, b)
+            if it >= 0:
+                assert r < np.sqrt(n), (n, imat, it, r)
+                assert ao.tobytes() == np.asfortranarray(a).tobytes()
+            else:
+                assert r < THRESH, (n, imat, it, r)
+
+
+def test_zcgesv_fallback_and_exit_codes():
+    """ITER = -31 with the COMPLEX*16 solution for a system too ill
+    conditioned for COMPLEX refinement; ITER = -2 when B does not fit
+    COMPLEX (ZLAG2C overflow); ITER = -3 when CGETRF finds a zero pivot that
+    ZGETRF does not (an entry that rounds to 0 in single precision)."""
+    n = 60
+    u, _ = np.linalg.qr(oracle.random_zmatrix(n, n, 1))
+    v, _ = np.linalg.qr(oracle.random_zmatrix(n, n, 2))
+    a = (u * 1e12 ** (-np.arange(n) / (n - 1))) @ v.conj().T
+    xt = oracle.random_zmatrix(n, 1, 3)
+    b = a @ xt
+    ao, ip, x, it, info = oracle.zcgesv(a, b)
+    assert it == -31 and info == 0 and ck.zget08(a, x, b) < THRESH
+    lu, ip2, _ = oracle.zgetrf(a)
+    assert ao.tobytes() == lu.tobytes() and np.array_equal(ip, ip2)
+    big = b.copy()
+    big[3, 0] = complex(1.0, 1e39)
+    assert oracle.zcgesv(a, big)[3] == -2
+    d = np.diag([1.0, 1e-50, 1.0]).astype(np.complex128)
+    _, _, x, it, info = oracle.zcgesv(d, np.ones((3, 1), dtype=np.complex128))
+    assert it == -3 and info == 0 and abs(x[1, 0] - 1e50) < 1e36
