@@ -23,25 +23,33 @@ ORACLE_DIR = os.path.join(HERE, "..", "oracle")
 
 HARNESS = r"""
 #include <climits>
+#include <cstring>
+#include <vector>
 #include "zlu_seq.h"
+using gb::cpx;
 using gb::zdc;
+using gb::cfc;
 // Every step of the schedules as a loop over its threads' work, in any
 // order: the GPU threads of one step touch disjoint data.
 struct CpuOps {
-  int info = INT_MAX;
-  int col(int m, zdc *a, int *ipiv, int gcol) {
+  int info = INT_MAX, ovf = 0, nc = 0;
+  int info_reset() { info = INT_MAX; return 0; }
+  int info_read(int *out) { *out = info == INT_MAX ? 0 : info; return 0; }
+  template <typename R> int col(int m, cpx<R> *a, int *ipiv, int gcol) {
     if (gb::zgetrf2_col(m, a, ipiv) && gcol < info) info = gcol;
     return 0;
   }
-  int laswp(int ncols, zdc *A, int lda, int k1, int k2, const int *ipiv, int incx) {
+  template <typename R> int laswp(int ncols, cpx<R> *A, int lda, int k1, int k2, const int *ipiv, int incx) {
     for (int j = ncols - 1; j >= 0; --j) gb::zlaswp_col(A + (size_t)j * lda, k1, k2, ipiv, incx);
     return 0;
   }
-  int trsm(int upper, int trans, int unit, int m, int ncols, const zdc *A, int lda, zdc *B, int ldb) {
+  template <typename R>
+  int trsm(int upper, int trans, int unit, int m, int ncols, const cpx<R> *A, int lda, cpx<R> *B, int ldb) {
     for (int j = ncols - 1; j >= 0; --j) gb::ztrsm_left_col(upper, trans, unit, m, A, lda, B + (size_t)j * ldb);
     return 0;
   }
-  int gemm(int m, int n, int k, const zdc *A, int lda, const zdc *B, int ldb, zdc *C, int ldc) {
+  template <typename R>
+  int gemm(int m, int n, int k, const cpx<R> *A, int lda, const cpx<R> *B, int ldb, cpx<R> *C, int ldc) {
     for (int j = n - 1; j >= 0; --j)
       for (int i = m - 1; i >= 0; --i) gb::zgemm_nn_elem(i, j, k, A, lda, B, ldb, C, ldc);
     return 0;
@@ -50,18 +58,67 @@ struct CpuOps {
     for (int i = 0; i < cnt; ++i) ipiv[i] += off;
     return 0;
   }
+  int lange_inf(int n, const zdc *A, int lda, double *anrm) {
+    std::vector<double> rows(n);
+    for (int i = n - 1; i >= 0; --i) rows[i] = gb::zlange_row(i, n, A, lda);
+    *anrm = gb::zlange_max(n, rows.data());
+    return 0;
+  }
+  int flags_reset() { ovf = nc = 0; return 0; }
+  int flags_read(int *o, int *c) { *o = ovf; *c = nc; return 0; }
+  int lag2c(int m, int ncols, const zdc *A, int lda, cfc *S, int lds) {
+    for (int j = 0; j < ncols; ++j)
+      for (int i = 0; i < m; ++i)
+        if (!gb::zlag2c_elem(A[(size_t)i + (size_t)j * lda], S + (size_t)i + (size_t)j * lds)) ovf = 1;
+    return 0;
+  }
+  int lag2z(int m, int ncols, const cfc *S, int lds, zdc *X, int ldx, bool add) {
+    for (int j = 0; j < ncols; ++j)
+      for (int i = 0; i < m; ++i) gb::zlag2z_elem(S[(size_t)i + (size_t)j * lds], X + (size_t)i + (size_t)j * ldx, add);
+    return 0;
+  }
+  int copy(int m, int ncols, const zdc *B, int ldb, zdc *R, int ldr) {
+    for (int j = 0; j < ncols; ++j) memcpy(R + (size_t)j * ldr, B + (size_t)j * ldb, sizeof(zdc) * m);
+    return 0;
+  }
+  int check(int n, int nrhs, const zdc *X, int ldx, const zdc *R, int ldr, double cte) {
+    for (int j = nrhs - 1; j >= 0; --j)
+      if (gb::zcgesv_col_notconv(n, X + (size_t)j * ldx, R + (size_t)j * ldr, cte)) nc = 1;
+    return 0;
+  }
 };
-extern "C" {
-int seq_zgetrf(int m, int n, double *a, int lda, int *ipiv, int nb) {
+template <typename R> int getrf_t(int m, int n, R *a, int lda, int *ipiv, int nb) {
   CpuOps ops;
-  gb::zgetrf_sched(ops, m, n, reinterpret_cast<zdc *>(a), lda, ipiv, nb);
-  return ops.info == INT_MAX ? 0 : ops.info;
+  int info = 0;
+  gb::zgetrf_full(ops, m, n, reinterpret_cast<cpx<R> *>(a), lda, ipiv, nb, &info);
+  return info;
 }
-void seq_zgetrs(int trans, int n, int nrhs, const double *a, int lda, const int *ipiv, double *b, int ldb) {
+template <typename R> void getrs_t(int trans, int n, int nrhs, const R *a, int lda, const int *ipiv, R *b, int ldb) {
   CpuOps ops;
-  gb::zgetrs_sched(ops, trans, n, nrhs, reinterpret_cast<const zdc *>(a), lda, ipiv, reinterpret_cast<zdc *>(b), ldb);
+  gb::zgetrs_sched(ops, trans, n, nrhs, reinterpret_cast<const cpx<R> *>(a), lda, ipiv, reinterpret_cast<cpx<R> *>(b),
+                   ldb);
+}
+extern "C" {
+int seq_zgetrf(int m, int n, double *a, int lda, int *ipiv, int nb) { return getrf_t(m, n, a, lda, ipiv, nb); }
+int seq_cgetrf(int m, int n, float *a, int lda, int *ipiv, int nb) { return getrf_t(m, n, a, lda, ipiv, nb); }
+void seq_zgetrs(int trans, int n, int nrhs, const double *a, int lda, const int *ipiv, double *b, int ldb) {
+  getrs_t(trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+void seq_cgetrs(int trans, int n, int nrhs, const float *a, int lda, const int *ipiv, float *b, int ldb) {
+  getrs_t(trans, n, nrhs, a, lda, ipiv, b, ldb);
 }
 int seq_izamax(int n, const double *x) { return gb::izamax_seq(n, reinterpret_cast<const zdc *>(x)); }
+int seq_icamax(int n, const float *x) { return gb::izamax_seq(n, reinterpret_cast<const cfc *>(x)); }
+int seq_zcgesv(int n, int nrhs, double *a, int lda, int *ipiv, const double *b, int ldb, double *x, int ldx,
+               int *iter) {
+  CpuOps ops;
+  std::vector<cfc> sa((size_t)n * n + 1), sx((size_t)n * nrhs + 1);
+  std::vector<zdc> r((size_t)n * nrhs + 1);
+  int info = 0;
+  gb::zcgesv_sched(ops, n, nrhs, reinterpret_cast<zdc *>(a), lda, ipiv, reinterpret_cast<const zdc *>(b), ldb,
+                   reinterpret_cast<zdc *>(x), ldx, sa.data(), sx.data(), r.data(), iter, &info);
+  return info;
+}
 }
 """
 
@@ -82,6 +139,10 @@ def seq(tmp_path_factory):
     L.seq_zgetrf.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
     L.seq_zgetrs.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int]
     L.seq_izamax.argtypes = [ctypes.c_int, p]
+    L.seq_icamax.argtypes = [ctypes.c_int, p]
+    L.seq_cgetrf.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
+    L.seq_cgetrs.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int]
+    L.seq_zcgesv.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int, p, ctypes.c_int, p]
     return L
 
 
@@ -99,19 +160,22 @@ def _same_bits(x, y):
     return x.shape == y.shape and np.array_equal(nx, ny) and x[~nx].tobytes() == y[~ny].tobytes()
 
 
-def _seq_getrf(L, a, nb):
-    a = np.asfortranarray(np.array(a, dtype=np.complex128, copy=True))
+def _seq_getrf(L, a, nb, dtype=np.complex128):
+    a = np.asfortranarray(np.array(a, dtype=dtype, copy=True))
     m, n = a.shape
     ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
-    info = L.seq_zgetrf(m, n, _ptr(a), max(1, m), _ptr(ipiv), nb)
+    fn = L.seq_cgetrf if dtype == np.complex64 else L.seq_zgetrf
+    info = fn(m, n, _ptr(a), max(1, m), _ptr(ipiv), nb)
     return a, ipiv[: min(m, n)], info
 
 
 def _seq_getrs(L, lu, ipiv, b, trans):
-    b = np.asfortranarray(np.array(b, dtype=np.complex128, copy=True))
+    dtype = lu.dtype
+    b = np.asfortranarray(np.array(b, dtype=dtype, copy=True))
     n, nrhs = b.shape
-    L.seq_zgetrs("NTC".index(trans), n, nrhs, _ptr(np.asfortranarray(lu)), max(1, n),
-                 _ptr(np.ascontiguousarray(ipiv, dtype=np.int32)), _ptr(b), max(1, n))
+    fn = L.seq_cgetrs if dtype == np.complex64 else L.seq_zgetrs
+    fn("NTC".index(trans), n, nrhs, _ptr(np.asfortranarray(lu)), max(1, n),
+       _ptr(np.ascontiguousarray(ipiv, dtype=np.int32)), _ptr(b), max(1, n))
     return b
 
 
@@ -185,3 +249,63 @@ def test_izamax_seq_matches_oracle(seq):
     for x in cases:
         x = np.ascontiguousarray(x, dtype=np.complex128)
         assert seq.seq_izamax(x.size, _ptr(x)) == oracle.izamax(x)
+
+
+@pytest.mark.parametrize("nb", [1, 20, 64])
+@pytest.mark.parametrize("m,n", [(1, 1), (7, 7), (33, 20), (20, 33), (130, 130)])
+def test_cgetrf_cgetrs_schedule_bitwise(seq, nb, m, n):
+    """The COMPLEX twins (CGETRF, CGETRF2, CGETRS) through the same
+    templates, against the oracle's single-precision restatement."""
+    a = oracle.random_zmatrix(m, n, 5 * m + n).astype(np.complex64)
+    lu_r, ip_r, info_r = oracle.zgetrf(a, nb=nb, dtype=np.complex64)
+    lu_g, ip_g, info_g = _seq_getrf(seq, a, nb, np.complex64)
+    assert info_g == info_r and np.array_equal(ip_g, ip_r)
+    assert lu_g.tobytes() == lu_r.tobytes()
+    if m == n:
+        b = oracle.random_zmatrix(n, 2, 9).astype(np.complex64)
+        for trans in "NTC":
+            x_r, _ = oracle.zgetrs(lu_r, ip_r, b, trans)
+            assert _seq_getrs(seq, lu_r, ip_r, b, trans).tobytes() == np.asfortranarray(x_r).tobytes()
+
+
+def _seq_zcgesv(L, a, b):
+    a = np.asfortranarray(np.array(a, dtype=np.complex128, copy=True))
+    b = np.asfortranarray(np.array(b, dtype=np.complex128, copy=True)).reshape(a.shape[0], -1)
+    n, nrhs = b.shape
+    x = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    it = np.zeros(1, dtype=np.int32)
+    info = L.seq_zcgesv(n, nrhs, _ptr(a), max(1, n), _ptr(ipiv), _ptr(b), max(1, n), _ptr(x), max(1, n), _ptr(it))
+    return a, ipiv[:n], x, int(it[0]), info
+
+
+@pytest.mark.parametrize("kappa", [1e1, 1e4, 1e7, 1e12])
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (13, 2), (70, 1), (130, 3)])
+def test_zcgesv_schedule_bitwise(seq, kappa, n, nrhs):
+    """ZCGESV's schedule (ITER, X, IPIV, and A after a fallback) equal to the
+    oracle's, from converged refinement to the ITER = -31 fallback."""
+    u, _ = np.linalg.qr(oracle.random_zmatrix(n, n, 1 + n))
+    v, _ = np.linalg.qr(oracle.random_zmatrix(n, n, 2 + n))
+    a = np.asfortranarray((u * kappa ** (-np.arange(n) / max(n - 1, 1))) @ v.conj().T)
+    b = a @ oracle.random_zmatrix(n, nrhs, 3 + n)
+    ao_r, ip_r, x_r, it_r, info_r = oracle.zcgesv(a, b)
+    ao_g, ip_g, x_g, it_g, info_g = _seq_zcgesv(seq, a, b)
+    assert (it_g, info_g) == (it_r, info_r)
+    assert np.array_equal(ip_g, ip_r)
+    assert x_g.tobytes() == np.asfortranarray(x_r.reshape(n, nrhs)).tobytes()
+    assert ao_g.tobytes() == ao_r.tobytes()
+
+
+def test_zcgesv_schedule_exits(seq):
+    """ITER = -2 (B does not fit COMPLEX) and -3 (CGETRF meets a zero pivot
+    that ZGETRF does not) as the oracle."""
+    n = 30
+    a = oracle.random_zmatrix(n, n, 8)
+    b = a @ oracle.random_zmatrix(n, 1, 9)
+    b[4, 0] = complex(1e39, 0.0)
+    for aa, bb in ((a, b), (np.diag([1.0, 1e-50, 1.0]).astype(np.complex128), np.ones((3, 1), np.complex128))):
+        ao_r, ip_r, x_r, it_r, info_r = oracle.zcgesv(aa, bb)
+        ao_g, ip_g, x_g, it_g, info_g = _seq_zcgesv(seq, aa, bb)
+        assert (it_g, info_g) == (it_r, info_r) and it_r in (-2, -3)
+        assert x_g.tobytes() == np.asfortranarray(x_r.reshape(x_g.shape)).tobytes()
+        assert ao_g.tobytes() == ao_r.tobytes() and np.array_equal(ip_g, ip_r)
