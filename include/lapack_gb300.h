@@ -131,6 +131,20 @@ void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, con
              const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t trans_len);
 void zgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
             const lapack_int* ldb, lapack_int* info);
+/* The COMPLEX twins.  Replace SRC/cgetrf.f:105, SRC/cgetrs.f:118,
+ * SRC/cgesv.f:121 (lapack.h LAPACK_cgetrf, _cgetrs, _cgesv); arrays are
+ * (re, im) pairs of floats. */
+void cgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info);
+void cgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
+             const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t trans_len);
+void cgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
+            const lapack_int* ldb, lapack_int* info);
+/* Mixed-precision complex solve with refinement.  Replaces SRC/zcgesv.f:197
+ * (lapack.h LAPACK_zcgesv).  WORK, SWORK and RWORK are accepted and unused. */
+void zcgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv,
+             const void* b, const lapack_int* ldb, void* x, const lapack_int* ldx, void* work, void* swork,
+             double* rwork, lapack_int* iter, lapack_int* info);
 /* Row interchanges.  Replaces SRC/dlaswp.f:112 (lapack.h:11326-11332). */
 void dlaswp_(const lapack_int* n, double* a, const lapack_int* lda, const lapack_int* k1,
              const lapack_int* k2, const lapack_int* ipiv, const lapack_int* incx);
@@ -328,6 +342,9 @@ int gb300_zgetrf_dev(int m, int n, void* dA, int lda, int* dIpiv, int* info, voi
 int gb300_zgetrs_dev(char trans, int n, int nrhs, const void* dA, int lda, const int* dIpiv, void* dB, int ldb,
                      void* stream);
 int gb300_zgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, void* dB, int ldb, int* info, void* stream);
+/* ZCGESV on device memory (SRC/zcgesv.f:197): ITER and INFO go to host ints. */
+int gb300_zcgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, const void* dB, int ldb, void* dX, int ldx,
+                     int* iter, int* info, void* stream);
 /* DGERFS on device memory (SRC/dgerfs.f:181): dA, dAF (n x n), dB, dX
  * (n x nrhs), dIpiv (n) and dFerr, dBerr (nrhs) are device arrays; the
  * return value is 0, the negative index of an illegal argument as DGERFS

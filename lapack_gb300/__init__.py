@@ -63,6 +63,7 @@ def lib():
         L.gb300_zgetrf_dev.argtypes = [_i, _i, _p, _i, _p, _ip, _p]
         L.gb300_zgetrs_dev.argtypes = [ctypes.c_char, _i, _i, _p, _i, _p, _p, _i, _p]
         L.gb300_zgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _ip, _p]
+        L.gb300_zcgesv_dev.argtypes = [_i, _i, _p, _i, _p, _p, _i, _p, _i, _ip, _ip, _p]
         _LIB = L
     return _LIB
 
@@ -324,38 +325,64 @@ def dsposv(a, b, uplo="L"):
     return a, x.reshape(np.asarray(b).shape), it.value, info.value
 
 
-def zgetrf(a):
-    """ZGETRF (SRC/zgetrf.f) on a complex128 copy of ``a``: returns (lu, ipiv, info)."""
-    a = _fortran(a, np.complex128)
+def _zpre(dtype):
+    return "c" if np.dtype(dtype) == np.complex64 else "z"
+
+
+def zgetrf(a, dtype=np.complex128):
+    """ZGETRF (SRC/zgetrf.f), or CGETRF for dtype complex64, on a copy of
+    ``a``: returns (lu, ipiv, info)."""
+    a = _fortran(a, dtype)
     m, n = a.shape
     ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
     info = ctypes.c_int(0)
-    lib().zgetrf_(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv), ctypes.byref(info))
+    getattr(lib(), f"{_zpre(dtype)}getrf_")(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv), ctypes.byref(info))
     return a, ipiv[: min(m, n)], info.value
 
 
 def zgetrs(lu, ipiv, b, trans="N"):
-    """ZGETRS (SRC/zgetrs.f), TRANS = 'N', 'T' or 'C': returns (x, info)."""
-    lu = _fortran(lu, np.complex128)
-    b2 = _fortran(_as2d(b), np.complex128)
+    """ZGETRS / CGETRS (SRC/zgetrs.f) in the precision of ``lu``, TRANS =
+    'N', 'T' or 'C': returns (x, info)."""
+    dtype = np.complex64 if np.asarray(lu).dtype == np.complex64 else np.complex128
+    lu = _fortran(lu, dtype)
+    b2 = _fortran(_as2d(b), dtype)
     n, nrhs = b2.shape
     ipiv = np.ascontiguousarray(ipiv, dtype=np.int32)
     info = ctypes.c_int(0)
-    lib().zgetrs_(ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(lu), _ref(max(1, n)), _ptr(ipiv),
-                  _ptr(b2), _ref(max(1, n)), ctypes.byref(info), _sz(1))
+    getattr(lib(), f"{_zpre(dtype)}getrs_")(ctypes.c_char_p(trans.encode()), _ref(n), _ref(nrhs), _ptr(lu),
+                                            _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)),
+                                            ctypes.byref(info), _sz(1))
     return b2.reshape(np.asarray(b).shape), info.value
 
 
-def zgesv(a, b):
-    """ZGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
-    a = _fortran(a, np.complex128)
-    b2 = _fortran(_as2d(b), np.complex128)
+def zgesv(a, b, dtype=np.complex128):
+    """ZGESV / CGESV (SRC/zgesv.f): returns (lu, ipiv, x, info)."""
+    a = _fortran(a, dtype)
+    b2 = _fortran(_as2d(b), dtype)
     n, nrhs = b2.shape
     ipiv = np.zeros(max(1, n), dtype=np.int32)
     info = ctypes.c_int(0)
-    lib().zgesv_(_ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)),
-                 ctypes.byref(info))
+    getattr(lib(), f"{_zpre(dtype)}gesv_")(_ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(b2),
+                                           _ref(max(1, n)), ctypes.byref(info))
     return a, ipiv[:n], b2.reshape(np.asarray(b).shape), info.value
+
+
+def zcgesv(a, b):
+    """ZCGESV (SRC/zcgesv.f): returns (a_out, ipiv, x, iter, info); a_out
+    holds the COMPLEX*16 factors when the refinement fell back (ITER < 0)."""
+    a = _fortran(a, np.complex128)
+    b2 = _fortran(_as2d(b), np.complex128)
+    n, nrhs = b2.shape
+    x = np.zeros((n, nrhs), dtype=np.complex128, order="F")
+    ipiv = np.zeros(max(1, n), dtype=np.int32)
+    it = ctypes.c_int(0)
+    info = ctypes.c_int(0)
+    work = np.zeros(max(1, n * nrhs), dtype=np.complex128)
+    swork = np.zeros(max(1, n * (n + nrhs)), dtype=np.complex64)
+    rwork = np.zeros(max(1, n))
+    lib().zcgesv_(_ref(n), _ref(nrhs), _ptr(a), _ref(max(1, n)), _ptr(ipiv), _ptr(b2), _ref(max(1, n)), _ptr(x),
+                  _ref(max(1, n)), _ptr(work), _ptr(swork), _ptr(rwork), ctypes.byref(it), ctypes.byref(info))
+    return a, ipiv[:n], x.reshape(np.asarray(b).shape), it.value, info.value
 
 
 def laswp(a, k1, k2, ipiv, incx=1):

@@ -251,6 +251,95 @@ void potrs_host(const char* name, const char* uplo, const lapack_int* n, const l
 }
 }  // namespace
 
+// ------------------------------------------------------------ complex LU
+// COMPLEX*16 / COMPLEX arrays are (re, im) pairs; xGETRF uses ILAENV's block
+// size 64, as the reference does.
+template <typename R>
+void zgetrf_host(const char* name, const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda,
+                 lapack_int* ipiv, lapack_int* info) {
+  // SRC/zgetrf.f:144-157
+  using C = gb::cpx<R>;
+  *info = 0;
+  if (*m < 0) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*lda < std::max(1, *m)) *info = -4;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*m == 0 || *n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int M = *m, N = *n, ld = ld_dev(M), mn = std::min(M, N);
+  DevScratch dA(sizeof(C) * (size_t)ld * N, s), dP(sizeof(int) * mn, s);
+  if (!dA.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  C* ha = static_cast<C*>(a);
+  int inf = 0;
+  int rc = h2d(dA.as<C>(), ld, ha, *lda, M, N, s);
+  if (!rc) rc = gb::zgetrf_dev<R>(M, N, dA.as<C>(), ld, dP.as<int>(), 64, &inf, s);
+  if (!rc) rc = d2h(ha, *lda, dA.as<C>(), ld, M, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure(name, rc, info); return; }
+  *info = inf;
+}
+
+template <typename R>
+void zgetrs_host(const char* name, const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a,
+                 const lapack_int* lda, const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info) {
+  // SRC/zgetrs.f:157-177
+  using C = gb::cpx<R>;
+  *info = 0;
+  const bool notran = lsame(*trans, 'N'), tr = lsame(*trans, 'T'), cj = lsame(*trans, 'C');
+  if (!notran && !tr && !cj) *info = -1;
+  else if (*n < 0) *info = -2;
+  else if (*nrhs < 0) *info = -3;
+  else if (*lda < std::max(1, *n)) *info = -5;
+  else if (*ldb < std::max(1, *n)) *info = -8;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0 || *nrhs == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R_ = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(C) * (size_t)ld * N, s), dB(sizeof(C) * (size_t)ld * R_, s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  C* hb = static_cast<C*>(b);
+  int rc = h2d(dA.as<C>(), ld, static_cast<const C*>(a), *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<C>(), ld, static_cast<const C*>(hb), *ldb, N, R_, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::zgetrs_dev<R>(notran ? 0 : (tr ? 1 : 2), N, R_, dA.as<C>(), ld, dP.as<int>(), dB.as<C>(), ld, s);
+  if (!rc) rc = d2h(hb, *ldb, dB.as<C>(), ld, N, R_, s);
+  if (!rc) rc = finish(s);
+  if (rc) device_failure(name, rc, info);
+}
+
+template <typename R>
+void zgesv_host(const char* name, const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda,
+                lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info) {
+  // SRC/zgesv.f:148-177: the solve only when the factorization succeeded
+  using C = gb::cpx<R>;
+  *info = 0;
+  if (*n < 0) *info = -1;
+  else if (*nrhs < 0) *info = -2;
+  else if (*lda < std::max(1, *n)) *info = -4;
+  else if (*ldb < std::max(1, *n)) *info = -7;
+  if (*info != 0) { call_xerbla(name, -*info); return; }
+  if (*n == 0) return;
+  cudaStream_t s = thread_stream();
+  const int N = *n, R_ = *nrhs, ld = ld_dev(N);
+  DevScratch dA(sizeof(C) * (size_t)ld * N, s), dB(sizeof(C) * (size_t)ld * std::max(R_, 1), s),
+      dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  C* ha = static_cast<C*>(a);
+  C* hb = static_cast<C*>(b);
+  int inf = 0;
+  int rc = h2d(dA.as<C>(), ld, ha, *lda, N, N, s);
+  if (!rc) rc = h2d(dB.as<C>(), ld, static_cast<const C*>(hb), *ldb, N, R_, s);
+  if (!rc) rc = gb::zgetrf_dev<R>(N, N, dA.as<C>(), ld, dP.as<int>(), 64, &inf, s);
+  if (!rc && inf == 0) rc = gb::zgetrs_dev<R>(0, N, R_, dA.as<C>(), ld, dP.as<int>(), dB.as<C>(), ld, s);
+  if (!rc) rc = d2h(ha, *lda, dA.as<C>(), ld, N, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc && inf == 0) rc = d2h(hb, *ldb, dB.as<C>(), ld, N, R_, s);
+  if (!rc) rc = finish(s);
+  if (rc) { device_failure(name, rc, info); return; }
+  *info = inf;
+}
+
 extern "C" {
 
 __attribute__((weak)) void xerbla_(const char* srname, const lapack_int* info, size_t len) {
@@ -673,88 +762,61 @@ void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, doub
 }
 
 // ---------------------------------------------------------------- complex LU
-// COMPLEX*16 arrays are (re, im) pairs of doubles; ZGETRF uses ILAENV's
-// block size 64, as the reference does.
 void zgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
              lapack_int* info) {
-  // SRC/zgetrf.f:144-157
-  *info = 0;
-  if (*m < 0) *info = -1;
-  else if (*n < 0) *info = -2;
-  else if (*lda < std::max(1, *m)) *info = -4;
-  if (*info != 0) { call_xerbla("ZGETRF", -*info); return; }
-  if (*m == 0 || *n == 0) return;
-  using gb::zdc;
-  cudaStream_t s = thread_stream();
-  const int M = *m, N = *n, ld = ld_dev(M), mn = std::min(M, N);
-  DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dP(sizeof(int) * mn, s);
-  if (!dA.p || !dP.p) { device_failure("ZGETRF", (int)cudaErrorMemoryAllocation, info); return; }
-  zdc* ha = static_cast<zdc*>(a);
-  int inf = 0;
-  int rc = h2d(dA.as<zdc>(), ld, ha, *lda, M, N, s);
-  if (!rc) rc = gb::zgetrf_dev(M, N, dA.as<zdc>(), ld, dP.as<int>(), 64, &inf, s);
-  if (!rc) rc = d2h(ha, *lda, dA.as<zdc>(), ld, M, N, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
-  if (!rc) rc = finish(s);
-  if (rc) { device_failure("ZGETRF", rc, info); return; }
-  *info = inf;
+  zgetrf_host<double>("ZGETRF", m, n, a, lda, ipiv, info);
 }
-
+void cgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+             lapack_int* info) {
+  zgetrf_host<float>("CGETRF", m, n, a, lda, ipiv, info);
+}
 void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
              const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t) {
-  // SRC/zgetrs.f:157-177
-  *info = 0;
-  const bool notran = lsame(*trans, 'N'), tr = lsame(*trans, 'T'), cj = lsame(*trans, 'C');
-  if (!notran && !tr && !cj) *info = -1;
-  else if (*n < 0) *info = -2;
-  else if (*nrhs < 0) *info = -3;
-  else if (*lda < std::max(1, *n)) *info = -5;
-  else if (*ldb < std::max(1, *n)) *info = -8;
-  if (*info != 0) { call_xerbla("ZGETRS", -*info); return; }
-  if (*n == 0 || *nrhs == 0) return;
-  using gb::zdc;
-  cudaStream_t s = thread_stream();
-  const int N = *n, R = *nrhs, ld = ld_dev(N);
-  DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dB(sizeof(zdc) * (size_t)ld * R, s), dP(sizeof(int) * N, s);
-  if (!dA.p || !dB.p || !dP.p) { device_failure("ZGETRS", (int)cudaErrorMemoryAllocation, info); return; }
-  zdc* hb = static_cast<zdc*>(b);
-  int rc = h2d(dA.as<zdc>(), ld, static_cast<const zdc*>(a), *lda, N, N, s);
-  if (!rc) rc = h2d(dB.as<zdc>(), ld, static_cast<const zdc*>(hb), *ldb, N, R, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
-  if (!rc) rc = gb::zgetrs_dev(notran ? 0 : (tr ? 1 : 2), N, R, dA.as<zdc>(), ld, dP.as<int>(), dB.as<zdc>(), ld, s);
-  if (!rc) rc = d2h(hb, *ldb, dB.as<zdc>(), ld, N, R, s);
-  if (!rc) rc = finish(s);
-  if (rc) device_failure("ZGETRS", rc, info);
+  zgetrs_host<double>("ZGETRS", trans, n, nrhs, a, lda, ipiv, b, ldb, info);
 }
-
+void cgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
+             const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t) {
+  zgetrs_host<float>("CGETRS", trans, n, nrhs, a, lda, ipiv, b, ldb, info);
+}
 void zgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
             const lapack_int* ldb, lapack_int* info) {
-  // SRC/zgesv.f:148-177: the solve only when the factorization succeeded
+  zgesv_host<double>("ZGESV ", n, nrhs, a, lda, ipiv, b, ldb, info);
+}
+void cgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,
+            const lapack_int* ldb, lapack_int* info) {
+  zgesv_host<float>("CGESV ", n, nrhs, a, lda, ipiv, b, ldb, info);
+}
+void zcgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv,
+             const void* b, const lapack_int* ldb, void* x, const lapack_int* ldx, void*, void*, double*,
+             lapack_int* iter, lapack_int* info) {
+  // SRC/zcgesv.f:259-292
+  using gb::zdc;
   *info = 0;
+  *iter = 0;
   if (*n < 0) *info = -1;
   else if (*nrhs < 0) *info = -2;
   else if (*lda < std::max(1, *n)) *info = -4;
   else if (*ldb < std::max(1, *n)) *info = -7;
-  if (*info != 0) { call_xerbla("ZGESV ", -*info); return; }
+  else if (*ldx < std::max(1, *n)) *info = -9;
+  if (*info != 0) { call_xerbla("ZCGESV", -*info); return; }
   if (*n == 0) return;
-  using gb::zdc;
   cudaStream_t s = thread_stream();
   const int N = *n, R = *nrhs, ld = ld_dev(N);
   DevScratch dA(sizeof(zdc) * (size_t)ld * N, s), dB(sizeof(zdc) * (size_t)ld * std::max(R, 1), s),
-      dP(sizeof(int) * N, s);
-  if (!dA.p || !dB.p || !dP.p) { device_failure("ZGESV", (int)cudaErrorMemoryAllocation, info); return; }
+      dX(sizeof(zdc) * (size_t)ld * std::max(R, 1), s), dP(sizeof(int) * N, s);
+  if (!dA.p || !dB.p || !dX.p || !dP.p) { device_failure("ZCGESV", (int)cudaErrorMemoryAllocation, info); return; }
   zdc* ha = static_cast<zdc*>(a);
-  zdc* hb = static_cast<zdc*>(b);
-  int inf = 0;
+  int it = 0, inf = 0;
   int rc = h2d(dA.as<zdc>(), ld, ha, *lda, N, N, s);
-  if (!rc) rc = h2d(dB.as<zdc>(), ld, static_cast<const zdc*>(hb), *ldb, N, R, s);
-  if (!rc) rc = gb::zgetrf_dev(N, N, dA.as<zdc>(), ld, dP.as<int>(), 64, &inf, s);
-  if (!rc && inf == 0) rc = gb::zgetrs_dev(0, N, R, dA.as<zdc>(), ld, dP.as<int>(), dB.as<zdc>(), ld, s);
-  if (!rc) rc = d2h(ha, *lda, dA.as<zdc>(), ld, N, N, s);
+  if (!rc) rc = h2d(dB.as<zdc>(), ld, static_cast<const zdc*>(b), *ldb, N, R, s);
+  if (!rc) rc = gb::zcgesv_dev(N, R, dA.as<zdc>(), ld, dP.as<int>(), dB.as<zdc>(), ld, dX.as<zdc>(), ld, &it, &inf, s);
+  // A holds the COMPLEX*16 factors when the refinement fell back (ITER < 0)
+  if (!rc && it < 0) rc = d2h(ha, *lda, dA.as<zdc>(), ld, N, N, s);
   if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
-  if (!rc && inf == 0) rc = d2h(hb, *ldb, dB.as<zdc>(), ld, N, R, s);
+  if (!rc && inf == 0) rc = d2h(static_cast<zdc*>(x), *ldx, dX.as<zdc>(), ld, N, R, s);
   if (!rc) rc = finish(s);
-  if (rc) { device_failure("ZGESV", rc, info); return; }
+  if (rc) { device_failure("ZCGESV", rc, info); return; }
+  *iter = it;
   *info = inf;
 }
 
@@ -1033,7 +1095,7 @@ int gb300_zgetrf_dev(int m, int n, void* dA, int lda, int* dIpiv, int* info, voi
   if (lda < std::max(1, m)) return -4;
   cudaStream_t s = (cudaStream_t)stream;
   int inf = 0;
-  int rc = gb::zgetrf_dev(m, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
+  int rc = gb::zgetrf_dev<double>(m, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
   if (!rc) rc = finish(s);
   if (info) *info = inf;
   return rc;
@@ -1047,8 +1109,8 @@ int gb300_zgetrs_dev(char trans, int n, int nrhs, const void* dA, int lda, const
   if (lda < std::max(1, n)) return -5;
   if (ldb < std::max(1, n)) return -8;
   cudaStream_t s = (cudaStream_t)stream;
-  int rc = gb::zgetrs_dev(notran ? 0 : (tr ? 1 : 2), n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv,
-                          static_cast<gb::zdc*>(dB), ldb, s);
+  int rc = gb::zgetrs_dev<double>(notran ? 0 : (tr ? 1 : 2), n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv,
+                                  static_cast<gb::zdc*>(dB), ldb, s);
   if (!rc) rc = finish(s);
   return rc;
 }
@@ -1059,10 +1121,27 @@ int gb300_zgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, void* dB, in
   if (ldb < std::max(1, n)) return -7;
   cudaStream_t s = (cudaStream_t)stream;
   int inf = 0;
-  int rc = gb::zgetrf_dev(n, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
-  if (!rc && inf == 0) rc = gb::zgetrs_dev(0, n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv,
-                                           static_cast<gb::zdc*>(dB), ldb, s);
+  int rc = gb::zgetrf_dev<double>(n, n, static_cast<gb::zdc*>(dA), lda, dIpiv, 64, &inf, s);
+  if (!rc && inf == 0)
+    rc = gb::zgetrs_dev<double>(0, n, nrhs, static_cast<const gb::zdc*>(dA), lda, dIpiv, static_cast<gb::zdc*>(dB),
+                                ldb, s);
   if (!rc) rc = finish(s);
+  if (info) *info = inf;
+  return rc;
+}
+int gb300_zcgesv_dev(int n, int nrhs, void* dA, int lda, int* dIpiv, const void* dB, int ldb, void* dX, int ldx,
+                     int* iter, int* info, void* stream) {
+  if (n < 0) return -1;
+  if (nrhs < 0) return -2;
+  if (lda < std::max(1, n)) return -4;
+  if (ldb < std::max(1, n)) return -7;
+  if (ldx < std::max(1, n)) return -9;
+  cudaStream_t s = (cudaStream_t)stream;
+  int it = 0, inf = 0;
+  int rc = gb::zcgesv_dev(n, nrhs, static_cast<gb::zdc*>(dA), lda, dIpiv, static_cast<const gb::zdc*>(dB), ldb,
+                          static_cast<gb::zdc*>(dX), ldx, &it, &inf, s);
+  if (!rc) rc = finish(s);
+  if (iter) *iter = it;
   if (info) *info = inf;
   return rc;
 }

@@ -70,13 +70,18 @@ int potrs_dev(bool upper, int n, int nrhs, const T* dA, int lda, T* dB, int ldb,
 // DSPOSV on device memory; *iter and *info are host outputs.
 int dsposv_dev(bool upper, int n, int nrhs, double* dA, int lda, const double* dB, int ldb, double* dX, int ldx,
                int* iter, int* info, cudaStream_t s);
-// Complex LU (ZGETRF with block size nb, ZGETRF2 panels) and ZGETRS
-// (trans 0 = 'N', 1 = 'T', 2 = 'C') on device memory; COMPLEX*16 elements
-// are (re, im) double pairs.  *info is a host output.
-struct zdc;
-int zgetrf_dev(int m, int n, zdc* dA, int lda, int* dIpiv, int nb, int* info, cudaStream_t s);
-int zgetrs_dev(int trans, int n, int nrhs, const zdc* dA, int lda, const int* dIpiv, zdc* dB, int ldb,
+// Complex LU (xGETRF with block size nb, xGETRF2 panels) and xGETRS
+// (trans 0 = 'N', 1 = 'T', 2 = 'C') on device memory, for COMPLEX*16
+// (R = double) and COMPLEX (R = float); elements are (re, im) pairs.  ZCGESV
+// on device memory.  *info and *iter are host outputs.
+template <typename R> struct cpx;
+template <typename R>
+int zgetrf_dev(int m, int n, cpx<R>* dA, int lda, int* dIpiv, int nb, int* info, cudaStream_t s);
+template <typename R>
+int zgetrs_dev(int trans, int n, int nrhs, const cpx<R>* dA, int lda, const int* dIpiv, cpx<R>* dB, int ldb,
                cudaStream_t s);
+int zcgesv_dev(int n, int nrhs, cpx<double>* dA, int lda, int* dIpiv, const cpx<double>* dB, int ldb,
+               cpx<double>* dX, int ldx, int* iter, int* info, cudaStream_t s);
 // DTRSV on one device vector (X has n elements, unit stride).
 int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int lda, double* dX, cudaStream_t s);
 // DLATRS (SRC/dlatrs.f) on one device vector: *scale (host) receives SCALE;

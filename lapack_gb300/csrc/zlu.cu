@@ -1,16 +1,20 @@
-// Complex LU on the GPU: ZGETRF (SRC/zgetrf.f:144-225) with the recursive
-// panel ZGETRF2 (SRC/zgetrf2.f:154-272), ZGETRS (SRC/zgetrs.f:157-223).
+// Complex LU on the GPU: ZGETRF / CGETRF (SRC/zgetrf.f:144-225) with the
+// recursive panel xGETRF2 (SRC/zgetrf2.f:154-272), ZGETRS / CGETRS
+// (SRC/zgetrs.f:157-223), and the mixed-precision ZCGESV
+// (SRC/zcgesv.f:259-448).
 //
-// The schedules (block loop, panel recursion, solve sequence) are the
-// host-side templates of zlu_seq.h; here each of their steps is one kernel
-// launch on the caller's stream: ZLASWP and ZTRSM with one thread per column,
-// the ZGEMM update with one thread per element, the pivot step of a panel
-// column on one thread.  Every thread runs the shared per-thread function
-// in the reference loop order with separately rounded operations, so the
-// factors, IPIV, INFO and solutions equal the reference's bit for bit (the
-// CPU tests run the same schedules and functions against the oracle).  This
-// is the correctness-first form of the complex path: no tiling and no
-// tensor cores yet.
+// The schedules (block loop, panel recursion, solve sequence, refinement
+// loop) are the host-side templates of zlu_seq.h; here each of their steps
+// is one kernel launch on the caller's stream: ZLASWP and ZTRSM with one
+// thread per column, the ZGEMM update and the conversions with one thread
+// per element, ZLANGE with one thread per row, the pivot step of a panel
+// column and ZLANGE's maximum on one thread, the convergence test with one
+// thread per right-hand side.  Every thread runs the shared per-thread
+// function in the reference loop order with separately rounded operations,
+// so the results equal the reference's bit for bit (the CPU tests run the
+// same schedules and functions against the oracle).  This is the
+// correctness-first form of the complex path: no tiling and no tensor cores
+// yet.
 #include "common.cuh"
 #include "driver.h"
 #include "zlu_seq.h"
@@ -23,25 +27,29 @@ namespace {
 
 unsigned zblocks(size_t n, int per = 128) { return (unsigned)((n + per - 1) / per); }
 
-__global__ void __launch_bounds__(1) zcol_kernel(int m, zdc* __restrict__ a, int* __restrict__ ipiv, int gcol,
+template <typename R>
+__global__ void __launch_bounds__(1) zcol_kernel(int m, cpx<R>* __restrict__ a, int* __restrict__ ipiv, int gcol,
                                                  int* __restrict__ info) {
   if (zgetrf2_col(m, a, ipiv)) atomicMin(info, gcol);
 }
 
-__global__ void zlaswp_kernel(int ncols, zdc* __restrict__ A, int lda, int k1, int k2, const int* __restrict__ ipiv,
+template <typename R>
+__global__ void zlaswp_kernel(int ncols, cpx<R>* __restrict__ A, int lda, int k1, int k2, const int* __restrict__ ipiv,
                               int incx) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < ncols) zlaswp_col(A + (size_t)j * lda, k1, k2, ipiv, incx);
 }
 
-__global__ void ztrsm_kernel(int upper, int trans, int unit, int m, int ncols, const zdc* __restrict__ A, int lda,
-                             zdc* __restrict__ B, int ldb) {
+template <typename R>
+__global__ void ztrsm_kernel(int upper, int trans, int unit, int m, int ncols, const cpx<R>* __restrict__ A, int lda,
+                             cpx<R>* __restrict__ B, int ldb) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < ncols) ztrsm_left_col(upper, trans, unit, m, A, lda, B + (size_t)j * ldb);
 }
 
-__global__ void zgemm_kernel(int m, int n, int k, const zdc* __restrict__ A, int lda, const zdc* __restrict__ B,
-                             int ldb, zdc* __restrict__ C, int ldc) {
+template <typename R>
+__global__ void zgemm_kernel(int m, int n, int k, const cpx<R>* __restrict__ A, int lda, const cpx<R>* __restrict__ B,
+                             int ldb, cpx<R>* __restrict__ C, int ldc) {
   const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (size_t)m * n) return;
   const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
@@ -53,28 +61,83 @@ __global__ void zipiv_add_kernel(int* __restrict__ ipiv, int cnt, int off) {
   if (i < cnt) ipiv[i] += off;
 }
 
-// The backend of the zlu_seq.h schedules: one launch per step.  `info` is a
-// device int holding INT_MAX until a zero pivot records its global column.
+__global__ void zlange_rows_kernel(int n, const zdc* __restrict__ A, int lda, double* __restrict__ rows) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rows[i] = zlange_row(i, n, A, lda);
+}
+
+__global__ void __launch_bounds__(1) zlange_max_kernel(int n, const double* __restrict__ rows,
+                                                       double* __restrict__ out) {
+  *out = zlange_max(n, rows);
+}
+
+__global__ void zlag2c_kernel(int m, int ncols, const zdc* __restrict__ A, int lda, cfc* __restrict__ S, int lds,
+                              int* __restrict__ overflow) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * ncols) return;
+  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
+  if (!zlag2c_elem(A[(size_t)i + (size_t)j * lda], S + (size_t)i + (size_t)j * lds)) *overflow = 1;
+}
+
+__global__ void zlag2z_kernel(int m, int ncols, const cfc* __restrict__ S, int lds, zdc* __restrict__ X, int ldx,
+                              int add) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (size_t)m * ncols) return;
+  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
+  zlag2z_elem(S[(size_t)i + (size_t)j * lds], X + (size_t)i + (size_t)j * ldx, add != 0);
+}
+
+__global__ void zcheck_kernel(int n, int nrhs, const zdc* __restrict__ X, int ldx, const zdc* __restrict__ R, int ldr,
+                              double cte, int* __restrict__ notconv) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nrhs && zcgesv_col_notconv(n, X + (size_t)j * ldx, R + (size_t)j * ldr, cte)) *notconv = 1;
+}
+
+// Device words the backend keeps: [0] INFO (INT_MAX until a zero pivot),
+// [1] conversion overflow, [2] not converged; then ANRM and the row sums.
+struct ZWords {
+  int* info;
+  int* flags;       // flags[0] overflow, flags[1] notconv
+  double* anrm;
+  double* rows;     // n row sums (ZCGESV only)
+};
+
+// The backend of the zlu_seq.h schedules: one launch per step.
 struct GpuZOps {
   cudaStream_t s;
-  int* info;
-  int col(int m, zdc* a, int* ipiv, int gcol) {
-    GB_LAUNCH(zcol_kernel<<<1, 1, 0, s>>>(m, a, ipiv, gcol, info));
+  ZWords w;
+  int info_reset() {
+    const int none = INT_MAX;
+    return (int)cudaMemcpyAsync(w.info, &none, sizeof(int), cudaMemcpyHostToDevice, s);
+  }
+  int info_read(int* out) {
+    int h = INT_MAX;
+    GB_CUDA_TRY(cudaMemcpyAsync(&h, w.info, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = (h == INT_MAX) ? 0 : h;
+    return 0;
+  }
+  template <typename R>
+  int col(int m, cpx<R>* a, int* ipiv, int gcol) {
+    GB_LAUNCH(zcol_kernel<R><<<1, 1, 0, s>>>(m, a, ipiv, gcol, w.info));
     return (int)cudaGetLastError();
   }
-  int laswp(int ncols, zdc* A, int lda, int k1, int k2, const int* ipiv, int incx) {
+  template <typename R>
+  int laswp(int ncols, cpx<R>* A, int lda, int k1, int k2, const int* ipiv, int incx) {
     if (ncols <= 0 || k2 < k1) return 0;
-    GB_LAUNCH(zlaswp_kernel<<<zblocks(ncols), 128, 0, s>>>(ncols, A, lda, k1, k2, ipiv, incx));
+    GB_LAUNCH(zlaswp_kernel<R><<<zblocks(ncols), 128, 0, s>>>(ncols, A, lda, k1, k2, ipiv, incx));
     return (int)cudaGetLastError();
   }
-  int trsm(int upper, int trans, int unit, int m, int ncols, const zdc* A, int lda, zdc* B, int ldb) {
+  template <typename R>
+  int trsm(int upper, int trans, int unit, int m, int ncols, const cpx<R>* A, int lda, cpx<R>* B, int ldb) {
     if (m <= 0 || ncols <= 0) return 0;
-    GB_LAUNCH(ztrsm_kernel<<<zblocks(ncols), 128, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
+    GB_LAUNCH(ztrsm_kernel<R><<<zblocks(ncols), 128, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
     return (int)cudaGetLastError();
   }
-  int gemm(int m, int n, int k, const zdc* A, int lda, const zdc* B, int ldb, zdc* C, int ldc) {
+  template <typename R>
+  int gemm(int m, int n, int k, const cpx<R>* A, int lda, const cpx<R>* B, int ldb, cpx<R>* C, int ldc) {
     if (m <= 0 || n <= 0 || k <= 0) return 0;   // ZGEMM's quick return (BETA = ONE)
-    GB_LAUNCH(zgemm_kernel<<<zblocks((size_t)m * n, 256), 256, 0, s>>>(m, n, k, A, lda, B, ldb, C, ldc));
+    GB_LAUNCH(zgemm_kernel<R><<<zblocks((size_t)m * n, 256), 256, 0, s>>>(m, n, k, A, lda, B, ldb, C, ldc));
     return (int)cudaGetLastError();
   }
   int ipiv_add(int* ipiv, int cnt, int off) {
@@ -82,31 +145,86 @@ struct GpuZOps {
     GB_LAUNCH(zipiv_add_kernel<<<zblocks(cnt), 128, 0, s>>>(ipiv, cnt, off));
     return (int)cudaGetLastError();
   }
+  int lange_inf(int n, const zdc* A, int lda, double* anrm) {
+    GB_LAUNCH(zlange_rows_kernel<<<zblocks(n), 128, 0, s>>>(n, A, lda, w.rows));
+    GB_LAUNCH(zlange_max_kernel<<<1, 1, 0, s>>>(n, w.rows, w.anrm));
+    GB_CUDA_TRY(cudaMemcpyAsync(anrm, w.anrm, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    return 0;
+  }
+  int flags_reset() { return (int)cudaMemsetAsync(w.flags, 0, 2 * sizeof(int), s); }
+  int flags_read(int* ovf, int* nc) {
+    int h[2] = {0, 0};
+    GB_CUDA_TRY(cudaMemcpyAsync(h, w.flags, sizeof(h), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    *ovf = h[0];
+    *nc = h[1];
+    return 0;
+  }
+  int lag2c(int m, int ncols, const zdc* A, int lda, cfc* S, int lds) {
+    if (m <= 0 || ncols <= 0) return 0;
+    GB_LAUNCH(zlag2c_kernel<<<zblocks((size_t)m * ncols, 256), 256, 0, s>>>(m, ncols, A, lda, S, lds, w.flags));
+    return (int)cudaGetLastError();
+  }
+  int lag2z(int m, int ncols, const cfc* S, int lds, zdc* X, int ldx, bool add) {
+    if (m <= 0 || ncols <= 0) return 0;
+    GB_LAUNCH(zlag2z_kernel<<<zblocks((size_t)m * ncols, 256), 256, 0, s>>>(m, ncols, S, lds, X, ldx, add ? 1 : 0));
+    return (int)cudaGetLastError();
+  }
+  int copy(int m, int ncols, const zdc* B, int ldb, zdc* R, int ldr) {
+    if (m <= 0 || ncols <= 0) return 0;
+    return (int)cudaMemcpy2DAsync(R, sizeof(zdc) * (size_t)ldr, B, sizeof(zdc) * (size_t)ldb, sizeof(zdc) * (size_t)m,
+                                  ncols, cudaMemcpyDeviceToDevice, s);
+  }
+  int check(int n, int nrhs, const zdc* X, int ldx, const zdc* R, int ldr, double cte) {
+    if (nrhs <= 0) return 0;
+    GB_LAUNCH(zcheck_kernel<<<zblocks(nrhs), 128, 0, s>>>(n, nrhs, X, ldx, R, ldr, cte, w.flags + 1));
+    return (int)cudaGetLastError();
+  }
 };
 
 }  // namespace
 
-int zgetrf_dev(int m, int n, zdc* dA, int lda, int* dIpiv, int nb, int* info, cudaStream_t s) {
+template <typename R>
+int zgetrf_dev(int m, int n, cpx<R>* dA, int lda, int* dIpiv, int nb, int* info, cudaStream_t s) {
   *info = 0;
   if (m <= 0 || n <= 0) return 0;
   DevScratch ib(sizeof(int), s);
   if (!ib.p) return (int)cudaErrorMemoryAllocation;
-  const int none = INT_MAX;
-  GB_CUDA_TRY(cudaMemcpyAsync(ib.p, &none, sizeof(int), cudaMemcpyHostToDevice, s));
-  GpuZOps ops{s, ib.as<int>()};
-  int rc = zgetrf_sched(ops, m, n, dA, lda, dIpiv, nb);
-  if (rc) return rc;
-  int h = none;
-  GB_CUDA_TRY(cudaMemcpyAsync(&h, ib.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GB_CUDA_TRY(cudaStreamSynchronize(s));
-  *info = (h == none) ? 0 : h;
-  return 0;
+  GpuZOps ops{s, ZWords{ib.as<int>(), nullptr, nullptr, nullptr}};
+  return zgetrf_full(ops, m, n, dA, lda, dIpiv, nb, info);
 }
+template int zgetrf_dev<double>(int, int, zdc*, int, int*, int, int*, cudaStream_t);
+template int zgetrf_dev<float>(int, int, cfc*, int, int*, int, int*, cudaStream_t);
 
-int zgetrs_dev(int trans, int n, int nrhs, const zdc* dA, int lda, const int* dIpiv, zdc* dB, int ldb,
+template <typename R>
+int zgetrs_dev(int trans, int n, int nrhs, const cpx<R>* dA, int lda, const int* dIpiv, cpx<R>* dB, int ldb,
                cudaStream_t s) {
-  GpuZOps ops{s, nullptr};
+  GpuZOps ops{s, ZWords{nullptr, nullptr, nullptr, nullptr}};
   return zgetrs_sched(ops, trans, n, nrhs, dA, lda, dIpiv, dB, ldb);
+}
+template int zgetrs_dev<double>(int, int, int, const zdc*, int, const int*, zdc*, int, cudaStream_t);
+template int zgetrs_dev<float>(int, int, int, const cfc*, int, const int*, cfc*, int, cudaStream_t);
+
+int zcgesv_dev(int n, int nrhs, zdc* dA, int lda, int* dIpiv, const zdc* dB, int ldb, zdc* dX, int ldx, int* iter,
+               int* info, cudaStream_t s) {
+  *iter = 0;
+  *info = 0;
+  if (n <= 0) return 0;
+  size_t bytes = 0;
+  auto carve = [&](size_t b) { size_t off = bytes; bytes += (b + 255) / 256 * 256; return off; };
+  const size_t nn = (size_t)n * n, nr = (size_t)n * (size_t)(nrhs > 0 ? nrhs : 1);
+  const size_t o_sa = carve(sizeof(cfc) * nn), o_sx = carve(sizeof(cfc) * nr), o_r = carve(sizeof(zdc) * nr),
+               o_rows = carve(sizeof(double) * (size_t)n), o_anrm = carve(sizeof(double)),
+               o_words = carve(sizeof(int) * 4);
+  DevScratch ws(bytes, s);
+  if (!ws.p) return (int)cudaErrorMemoryAllocation;
+  char* base = ws.as<char>();
+  int* words = reinterpret_cast<int*>(base + o_words);
+  GpuZOps ops{s, ZWords{words, words + 1, reinterpret_cast<double*>(base + o_anrm),
+                        reinterpret_cast<double*>(base + o_rows)}};
+  return zcgesv_sched(ops, n, nrhs, dA, lda, dIpiv, dB, ldb, dX, ldx, reinterpret_cast<cfc*>(base + o_sa),
+                      reinterpret_cast<cfc*>(base + o_sx), reinterpret_cast<zdc*>(base + o_r), iter, info);
 }
 
 }  // namespace gb

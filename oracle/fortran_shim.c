@@ -143,6 +143,25 @@ void zgetrs_(const char *trans, const int *n, const int *nrhs, const void *a, co
 void zgesv_(const int *n, const int *nrhs, void *a, const int *lda, int *ipiv, void *b, const int *ldb, int *info) {
   or_zgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
 }
+void or_cgetrf(int, int, void *, int, int *, int *);
+void or_cgetrs(char, int, int, const void *, int, const int *, void *, int, int *);
+void or_cgesv(int, int, void *, int, int *, void *, int, int *);
+void or_zcgesv(int, int, void *, int, int *, const void *, int, void *, int, void *, void *, double *, int *, int *);
+void cgetrf_(const int *m, const int *n, void *a, const int *lda, int *ipiv, int *info) {
+  or_cgetrf(*m, *n, a, *lda, ipiv, info);
+}
+void cgetrs_(const char *trans, const int *n, const int *nrhs, const void *a, const int *lda, const int *ipiv,
+             void *b, const int *ldb, int *info, size_t l) {
+  (void)l;
+  or_cgetrs(*trans, *n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void cgesv_(const int *n, const int *nrhs, void *a, const int *lda, int *ipiv, void *b, const int *ldb, int *info) {
+  or_cgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, info);
+}
+void zcgesv_(const int *n, const int *nrhs, void *a, const int *lda, int *ipiv, const void *b, const int *ldb,
+             void *x, const int *ldx, void *work, void *swork, double *rwork, int *iter, int *info) {
+  or_zcgesv(*n, *nrhs, a, *lda, ipiv, b, *ldb, x, *ldx, work, swork, rwork, iter, info);
+}
 
 /* LSAME (INSTALL/lsame.f): case-insensitive comparison of one character. */
 int lsame_(const char *ca, const char *cb, size_t la, size_t lb) {

@@ -160,8 +160,25 @@ def test_fortran_abi_error_exits(lib):
         for (n, nrhs, lda, ldb), code in ERR_GESV:
             lib.zgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), ctypes.byref(info))
             assert info.value == -code and g.xerbla_last() == ("ZGESV", code)
+        for (m, n, lda), code in ERR_GETRF:
+            lib.cgetrf_(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("CGETRF", code)
+        for (tr, n, nrhs, lda, ldb), code in ERR_GETRS:
+            lib.cgetrs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb),
+                        ctypes.byref(info), ctypes.c_size_t(1))
+            assert info.value == -code and g.xerbla_last() == ("CGETRS", code)
+        for (n, nrhs, lda, ldb), code in ERR_GESV:
+            lib.cgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("CGESV", code)
+        for (n, nrhs, lda, ldb, ldx), code in ERR_DSGESV:      # TESTING/LIN/zerrab.f: the same table
+            lib.zcgesv_(_i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb), p(a), _i(ldx), p(a), p(a), p(w),
+                        ctypes.byref(it), ctypes.byref(info))
+            assert info.value == -code and g.xerbla_last() == ("ZCGESV", code)
         lib.zgetrf_(_i(0), _i(5), p(a), _i(1), p(ip), ctypes.byref(info))
         assert info.value == 0
+        lib.zcgesv_(_i(0), _i(1), p(a), _i(1), p(ip), p(a), _i(1), p(a), _i(1), p(a), p(a), p(w),
+                    ctypes.byref(it), ctypes.byref(info))
+        assert info.value == 0 and it.value == 0
         fb = np.full(4, 7.0)
         lib.dgerfs_(ctypes.c_char_p(b"T"), _i(0), _i(2), p(a), _i(1), p(a), _i(1), p(ip), p(a), _i(1), p(a), _i(1),
                     p(fb), p(fb[2:]), p(w), p(ip), ctypes.byref(info), ctypes.c_size_t(1))

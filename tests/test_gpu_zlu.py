@@ -140,3 +140,67 @@ def test_zgesv_device_api_matches_host_abi(gpu):
     assert np.array_equal(ip.cpu().numpy(), ip_h)
     assert _same_bits(A.cpu().numpy(), lu_h)
     assert _same_bits(B.cpu().numpy(), x_h)
+
+
+@pytest.mark.parametrize("m,n", [(1, 1), (7, 7), (130, 97), (200, 200)])
+def test_cgetrf_cgetrs_bitwise(gpu, m, n):
+    """The COMPLEX twins (CGETRF, CGETRS, CGESV) against the oracle's
+    single-precision restatement."""
+    a = oracle.random_zmatrix(m, n, 41 * m + n).astype(np.complex64)
+    lu_r, ip_r, info_r = oracle.zgetrf(a, dtype=np.complex64)
+    lu_g, ip_g, info_g = gpu.zgetrf(a, dtype=np.complex64)
+    assert info_g == info_r == 0 and np.array_equal(ip_g, ip_r)
+    assert _same_bits(lu_g, lu_r)
+    if m == n:
+        b = oracle.random_zmatrix(n, 2, 43 + n).astype(np.complex64)
+        for trans in "NTC":
+            x_r, _ = oracle.zgetrs(lu_r, ip_r, b, trans)
+            x_g, info = gpu.zgetrs(lu_g, ip_g, b, trans)
+            assert info == 0 and _same_bits(x_g, x_r)
+        _, _, x_g, info = gpu.zgesv(a, b, dtype=np.complex64)
+        _, _, x_r, _ = oracle.zgesv(a, b, dtype=np.complex64)
+        assert info == 0 and _same_bits(x_g, x_r)
+
+
+def _conditioned(n, kappa, seed):
+    u, _ = np.linalg.qr(oracle.random_zmatrix(n, n, seed))
+    v, _ = np.linalg.qr(oracle.random_zmatrix(n, n, seed + 1))
+    return np.asfortranarray((u * kappa ** (-np.arange(n) / max(n - 1, 1))) @ v.conj().T)
+
+
+@pytest.mark.parametrize("kappa", [1e1, 1e5, 1e12])
+@pytest.mark.parametrize("n,nrhs", [(1, 1), (13, 2), (130, 1), (300, 3)])
+def test_zcgesv_matches_oracle(gpu, kappa, n, nrhs):
+    """ZCGESV: ITER, INFO, IPIV, X and (after a fallback) A equal to the
+    oracle's; ZDRVAB's check (ZGET08 < sqrt(N) when ITER >= 0, < THRESH
+    after the fallback).  ZLANGE's moduli come from the GPU's hypot, which
+    can differ from the host's in the last bit; that moves CTE by an ulp and
+    could change ITER only for a residual on the threshold itself."""
+    a = _conditioned(n, kappa, 3 + n)
+    b = a @ oracle.random_zmatrix(n, nrhs, 5 + n)
+    ao_r, ip_r, x_r, it_r, info_r = oracle.zcgesv(a, b)
+    ao_g, ip_g, x_g, it_g, info_g = gpu.zcgesv(a, b)
+    assert (it_g, info_g) == (it_r, info_r)
+    assert np.array_equal(ip_g, ip_r)
+    assert _same_bits(x_g, x_r) and _same_bits(ao_g, ao_r)
+    r = ck.zget08(a, x_g, b)
+    assert r < (np.sqrt(n) if it_g >= 0 else THRESH) or (n == 1 and r < 1.0)
+    if it_g >= 0:
+        assert np.asfortranarray(ao_g).tobytes() == np.asfortranarray(a).tobytes()
+    if kappa >= 1e12 and n >= 13:
+        assert it_g == -31
+
+
+def test_zcgesv_exit_codes(gpu):
+    """ITER = -2 (B does not fit COMPLEX) and -3 (CGETRF meets a zero pivot
+    that ZGETRF does not), with the COMPLEX*16 fallback's answer."""
+    n = 30
+    a = oracle.random_zmatrix(n, n, 8)
+    b = a @ oracle.random_zmatrix(n, 1, 9)
+    b[4, 0] = complex(1e39, 0.0)
+    d = np.diag([1.0, 1e-50, 1.0]).astype(np.complex128)
+    for aa, bb, want in ((a, b, -2), (d, np.ones((3, 1), np.complex128), -3)):
+        ao_r, ip_r, x_r, it_r, info_r = oracle.zcgesv(aa, bb)
+        ao_g, ip_g, x_g, it_g, info_g = gpu.zcgesv(aa, bb)
+        assert it_g == it_r == want and info_g == info_r == 0
+        assert _same_bits(x_g, x_r) and _same_bits(ao_g, ao_r) and np.array_equal(ip_g, ip_r)
