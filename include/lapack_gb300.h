@@ -268,6 +268,36 @@ lapack_int LAPACKE_dsposv(int matrix_layout, char uplo, lapack_int n, lapack_int
 lapack_int LAPACKE_dsposv_work(int matrix_layout, char uplo, lapack_int n, lapack_int nrhs, double* a, lapack_int lda,
                                const double* b, lapack_int ldb, double* x, lapack_int ldx, double* work,
                                float* swork, lapack_int* iter);
+/* LAPACKE/include/lapacke.h (zgetrf, cgetrf, zgetrs, cgetrs, zgesv, cgesv,
+ * zcgesv) and their _work forms; complex arrays as void*, so any
+ * lapack_complex_double* / lapack_complex_float* passes. */
+lapack_int LAPACKE_zgetrf(int matrix_layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv);
+lapack_int LAPACKE_zgetrf_work(int matrix_layout, lapack_int m, lapack_int n, void* a, lapack_int lda,
+                               lapack_int* ipiv);
+lapack_int LAPACKE_cgetrf(int matrix_layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv);
+lapack_int LAPACKE_cgetrf_work(int matrix_layout, lapack_int m, lapack_int n, void* a, lapack_int lda,
+                               lapack_int* ipiv);
+lapack_int LAPACKE_zgetrs(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                          const lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_zgetrs_work(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const void* a,
+                               lapack_int lda, const lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_cgetrs(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                          const lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_cgetrs_work(int matrix_layout, char trans, lapack_int n, lapack_int nrhs, const void* a,
+                               lapack_int lda, const lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_zgesv(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                         void* b, lapack_int ldb);
+lapack_int LAPACKE_zgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda,
+                              lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_cgesv(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                         void* b, lapack_int ldb);
+lapack_int LAPACKE_cgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda,
+                              lapack_int* ipiv, void* b, lapack_int ldb);
+lapack_int LAPACKE_zcgesv(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                          const void* b, lapack_int ldb, void* x, lapack_int ldx, lapack_int* iter);
+lapack_int LAPACKE_zcgesv_work(int matrix_layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda,
+                               lapack_int* ipiv, const void* b, lapack_int ldb, void* x, lapack_int ldx, void* work,
+                               void* swork, double* rwork, lapack_int* iter);
 /* LAPACKE/include/lapacke.h:1153 (dgetri) and its _work form */
 lapack_int LAPACKE_dgetri(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv);
 lapack_int LAPACKE_dgetri_work(int matrix_layout, lapack_int n, double* a, lapack_int lda, const lapack_int* ipiv,

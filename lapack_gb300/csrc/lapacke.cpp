@@ -246,6 +246,18 @@ lapack_int potrs_posv_work(const char* nm, F fort, bool write_a, int layout, cha
   return info;
 }
 
+// COMPLEX*16 / COMPLEX elements for the generic wrappers above: x != x
+// holds when either part is a NaN (LAPACKE/utils/lapacke_zge_nancheck.c
+// through LAPACKE_zisnan).
+struct zc_t {
+  double re, im;
+  bool operator!=(const zc_t& o) const { return re != o.re || im != o.im; }
+};
+struct cc_t {
+  float re, im;
+  bool operator!=(const cc_t& o) const { return re != o.re || im != o.im; }
+};
+
 }  // namespace
 
 extern "C" {
@@ -870,6 +882,142 @@ lapack_int LAPACKE_dsposv(int layout, char uplo, lapack_int n, lapack_int nrhs, 
   lapack_int info = LAPACKE_dsposv_work(layout, uplo, n, nrhs, a, lda, b, ldb, x, ldx, work, swork, iter);
   LAPACKE_free_proxy(work);
   LAPACKE_free_proxy(swork);
+  return info;
+}
+
+
+// ---------------------------------------------------------------- complex LU
+// LAPACKE/src/lapacke_{z,c}getrf*.c, {z,c}getrs*.c, {z,c}gesv*.c, zcgesv*.c
+lapack_int LAPACKE_zgetrf_work(int layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv) {
+  return getrf_work<zc_t>("LAPACKE_zgetrf_work", zgetrf_, layout, m, n, static_cast<zc_t*>(a), lda, ipiv);
+}
+lapack_int LAPACKE_cgetrf_work(int layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv) {
+  return getrf_work<cc_t>("LAPACKE_cgetrf_work", cgetrf_, layout, m, n, static_cast<cc_t*>(a), lda, ipiv);
+}
+lapack_int LAPACKE_zgetrf(int layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_zgetrf", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, static_cast<const zc_t*>(a), lda)) return -4;
+  return LAPACKE_zgetrf_work(layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_cgetrf(int layout, lapack_int m, lapack_int n, void* a, lapack_int lda, lapack_int* ipiv) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_cgetrf", -1); return -1; }
+  if (nancheck() && ge_has_nan(layout, m, n, static_cast<const cc_t*>(a), lda)) return -4;
+  return LAPACKE_cgetrf_work(layout, m, n, a, lda, ipiv);
+}
+lapack_int LAPACKE_zgetrs_work(int layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                               const lapack_int* ipiv, void* b, lapack_int ldb) {
+  return getrs_work<zc_t>("LAPACKE_zgetrs_work", zgetrs_, layout, trans, n, nrhs, static_cast<const zc_t*>(a), lda,
+                          ipiv, static_cast<zc_t*>(b), ldb);
+}
+lapack_int LAPACKE_cgetrs_work(int layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                               const lapack_int* ipiv, void* b, lapack_int ldb) {
+  return getrs_work<cc_t>("LAPACKE_cgetrs_work", cgetrs_, layout, trans, n, nrhs, static_cast<const cc_t*>(a), lda,
+                          ipiv, static_cast<cc_t*>(b), ldb);
+}
+lapack_int LAPACKE_zgetrs(int layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                          const lapack_int* ipiv, void* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_zgetrs", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, static_cast<const zc_t*>(a), lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, static_cast<const zc_t*>(b), ldb)) return -8;
+  }
+  return LAPACKE_zgetrs_work(layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_cgetrs(int layout, char trans, lapack_int n, lapack_int nrhs, const void* a, lapack_int lda,
+                          const lapack_int* ipiv, void* b, lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_cgetrs", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, static_cast<const cc_t*>(a), lda)) return -5;
+    if (ge_has_nan(layout, n, nrhs, static_cast<const cc_t*>(b), ldb)) return -8;
+  }
+  return LAPACKE_cgetrs_work(layout, trans, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_zgesv_work(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                              void* b, lapack_int ldb) {
+  return gesv_work<zc_t>("LAPACKE_zgesv_work", zgesv_, layout, n, nrhs, static_cast<zc_t*>(a), lda, ipiv,
+                         static_cast<zc_t*>(b), ldb);
+}
+lapack_int LAPACKE_cgesv_work(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                              void* b, lapack_int ldb) {
+  return gesv_work<cc_t>("LAPACKE_cgesv_work", cgesv_, layout, n, nrhs, static_cast<cc_t*>(a), lda, ipiv,
+                         static_cast<cc_t*>(b), ldb);
+}
+lapack_int LAPACKE_zgesv(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv, void* b,
+                         lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_zgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, static_cast<const zc_t*>(a), lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, static_cast<const zc_t*>(b), ldb)) return -7;
+  }
+  return LAPACKE_zgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_cgesv(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv, void* b,
+                         lapack_int ldb) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_cgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, static_cast<const cc_t*>(a), lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, static_cast<const cc_t*>(b), ldb)) return -7;
+  }
+  return LAPACKE_cgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb);
+}
+lapack_int LAPACKE_zcgesv_work(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                               const void* b, lapack_int ldb, void* x, lapack_int ldx, void* work, void* swork,
+                               double* rwork, lapack_int* iter) {
+  // LAPACKE/src/lapacke_zcgesv_work.c: row major LDA < N -5, LDB < NRHS -8,
+  // LDX < NRHS -10; A and X written back
+  lapack_int info = 0;
+  const char* nm = "LAPACKE_zcgesv_work";
+  if (layout == LAPACK_COL_MAJOR) {
+    zcgesv_(&n, &nrhs, a, &lda, ipiv, b, &ldb, x, &ldx, work, swork, rwork, iter, &info);
+    if (info < 0) info -= 1;
+    return info;
+  }
+  if (layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla(nm, -1); return -1; }
+  lapack_int lda_t = std::max(1, n), ldb_t = std::max(1, n), ldx_t = std::max(1, n);
+  if (lda < n) { LAPACKE_xerbla(nm, -5); return -5; }
+  if (ldb < nrhs) { LAPACKE_xerbla(nm, -8); return -8; }
+  if (ldx < nrhs) { LAPACKE_xerbla(nm, -10); return -10; }
+  zc_t* a_t = alloc<zc_t>((size_t)lda_t * std::max(1, n));
+  zc_t* b_t = a_t ? alloc<zc_t>((size_t)ldb_t * std::max(1, nrhs)) : nullptr;
+  zc_t* x_t = b_t ? alloc<zc_t>((size_t)ldx_t * std::max(1, nrhs)) : nullptr;
+  if (!x_t) {
+    if (b_t) LAPACKE_free_proxy(b_t);
+    if (a_t) LAPACKE_free_proxy(a_t);
+    LAPACKE_xerbla(nm, LAPACK_TRANSPOSE_MEMORY_ERROR);
+    return LAPACK_TRANSPOSE_MEMORY_ERROR;
+  }
+  ge_trans(layout, n, n, static_cast<const zc_t*>(a), lda, a_t, lda_t);
+  ge_trans(layout, n, nrhs, static_cast<const zc_t*>(b), ldb, b_t, ldb_t);
+  zcgesv_(&n, &nrhs, a_t, &lda_t, ipiv, b_t, &ldb_t, x_t, &ldx_t, work, swork, rwork, iter, &info);
+  if (info < 0) info -= 1;
+  ge_trans(LAPACK_COL_MAJOR, n, n, a_t, lda_t, static_cast<zc_t*>(a), lda);
+  ge_trans(LAPACK_COL_MAJOR, n, nrhs, x_t, ldx_t, static_cast<zc_t*>(x), ldx);
+  LAPACKE_free_proxy(x_t);
+  LAPACKE_free_proxy(b_t);
+  LAPACKE_free_proxy(a_t);
+  return info;
+}
+lapack_int LAPACKE_zcgesv(int layout, lapack_int n, lapack_int nrhs, void* a, lapack_int lda, lapack_int* ipiv,
+                          const void* b, lapack_int ldb, void* x, lapack_int ldx, lapack_int* iter) {
+  if (layout != LAPACK_COL_MAJOR && layout != LAPACK_ROW_MAJOR) { LAPACKE_xerbla("LAPACKE_zcgesv", -1); return -1; }
+  if (nancheck()) {
+    if (ge_has_nan(layout, n, n, static_cast<const zc_t*>(a), lda)) return -4;
+    if (ge_has_nan(layout, n, nrhs, static_cast<const zc_t*>(b), ldb)) return -7;
+  }
+  // RWORK, SWORK, WORK as LAPACKE_zcgesv allocates them
+  double* rwork = alloc<double>((size_t)std::max(1, n));
+  cc_t* swork = rwork ? alloc<cc_t>((size_t)std::max(1, n) * std::max(1, n + nrhs)) : nullptr;
+  zc_t* work = swork ? alloc<zc_t>((size_t)std::max(1, n) * std::max(1, nrhs)) : nullptr;
+  if (!work) {
+    if (swork) LAPACKE_free_proxy(swork);
+    if (rwork) LAPACKE_free_proxy(rwork);
+    LAPACKE_xerbla("LAPACKE_zcgesv", LAPACK_WORK_MEMORY_ERROR);
+    return LAPACK_WORK_MEMORY_ERROR;
+  }
+  lapack_int info = LAPACKE_zcgesv_work(layout, n, nrhs, a, lda, ipiv, b, ldb, x, ldx, work, swork, rwork, iter);
+  LAPACKE_free_proxy(work);
+  LAPACKE_free_proxy(swork);
+  LAPACKE_free_proxy(rwork);
   return info;
 }
 

@@ -361,3 +361,95 @@ def test_chol_error_and_nan_codes(libs, capfd, layout):
                 assert call(fn, ldb_off=1) == -8
             if fn == "LAPACKE_dsposv":
                 assert call(fn, ldx_off=1) == -10
+
+
+def _zmat(m, n, seed, layout, ld_extra=0, dtype=np.complex128):
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))
+    if layout == 102:
+        ld = max(1, m + ld_extra)
+        buf = np.full((max(n, 1), ld), 7.25 - 3.5j)
+        buf[:n, :m] = a.T
+    else:
+        ld = max(1, n + ld_extra)
+        buf = np.full((max(m, 1), ld), 7.25 - 3.5j)
+        buf[:m, :n] = a
+    return buf.astype(dtype), ld
+
+
+@pytest.mark.parametrize("pre,dtype", [("z", np.complex128), ("c", np.complex64)])
+@pytest.mark.parametrize("layout,n,nrhs,extra", CASES)
+def test_complex_getrf_getrs_gesv(libs, capfd, pre, dtype, layout, n, nrhs, extra):
+    """LAPACKE_{z,c}gesv, {z,c}getrf, {z,c}getrs (TRANS N, T, C) against the
+    reference wrappers (LAPACKE/src/lapacke_zgesv.c ...)."""
+    def gesv():
+        a, lda = _zmat(n, n, 1 + n, layout, extra, dtype)
+        b, ldb = _zmat(n, nrhs, 2 + n, layout, extra, dtype)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        return (layout, n, nrhs, p(a), lda, p(ip), p(b), ldb), (a, b, ip)
+    _both(libs, f"LAPACKE_{pre}gesv", gesv, capfd)
+
+    def getrf():
+        a, lda = _zmat(n, n + 2, 3 + n, layout, extra, dtype)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        return (layout, n, n + 2, p(a), lda, p(ip)), (a, ip)
+    _both(libs, f"LAPACKE_{pre}getrf", getrf, capfd)
+
+    for tr in (b"N", b"T", b"C"):
+        def getrs():
+            a, lda = _zmat(n, n, 4 + n, layout, extra, dtype)
+            a[np.arange(min(a.shape)), np.arange(min(a.shape))] += 4.0
+            b, ldb = _zmat(n, nrhs, 5 + n, layout, extra, dtype)
+            ip = np.maximum(np.arange(1, max(n, 1) + 1, dtype=np.int32)[::-1].copy(),
+                            np.arange(1, max(n, 1) + 1, dtype=np.int32))
+            return (layout, ctypes.c_char(tr), n, nrhs, p(a), lda, p(ip), p(b), ldb), (b,)
+        _both(libs, f"LAPACKE_{pre}getrs", getrs, capfd)
+
+
+@pytest.mark.parametrize("layout,n,nrhs,extra", CASES)
+def test_zcgesv(libs, capfd, layout, n, nrhs, extra):
+    """LAPACKE_zcgesv (and _work through it): ITER, A, X, IPIV as the
+    reference wrapper (LAPACKE/src/lapacke_zcgesv.c)."""
+    def zcgesv():
+        a, lda = _zmat(n, n, 6 + n, layout, extra)
+        a[np.arange(min(a.shape)), np.arange(min(a.shape))] += 3.0
+        b, ldb = _zmat(n, nrhs, 7 + n, layout, extra)
+        x, ldx = _zmat(n, nrhs, 8 + n, layout, extra)
+        ip = np.zeros(max(n, 1), dtype=np.int32)
+        it = np.zeros(1, dtype=np.int32)
+        return (layout, n, nrhs, p(a), lda, p(ip), p(b), ldb, p(x), ldx, p(it)), (a, x, ip, it)
+    _both(libs, "LAPACKE_zcgesv", zcgesv, capfd)
+
+
+@pytest.mark.parametrize("layout", [101, 102])
+def test_complex_error_and_nan_codes(libs, capfd, layout):
+    """Bad layout (-1); a NaN in either part of A or B (-4 / -7, -5 / -8 for
+    xGETRS); row-major leading dimensions too small; INFO > 0 for a zero
+    column."""
+    def gesv(lay=layout, nan=None, lda_off=0, ldb_off=0, zero_col=False):
+        def build():
+            a, lda = _zmat(4, 4, 1, layout)
+            b, ldb = _zmat(4, 2, 2, layout)
+            if nan == "a_re":
+                a.flat[1] = complex(np.nan, 1.0)
+            elif nan == "a_im":
+                a.flat[2] = complex(1.0, np.nan)
+            elif nan == "b":
+                b.flat[0] = complex(0.0, np.nan)
+            if zero_col:
+                if layout == 102:
+                    a[2, :4] = 0
+                else:
+                    a[:4, 2] = 0
+            ip = np.zeros(4, dtype=np.int32)
+            return (lay, 4, 2, p(a), lda - lda_off, p(ip), p(b), ldb - ldb_off), (a, b, ip)
+        return build
+    for fn in ("LAPACKE_zgesv",):
+        assert _both(libs, fn, gesv(lay=9), capfd) == -1
+        assert _both(libs, fn, gesv(nan="a_re"), capfd) == -4
+        assert _both(libs, fn, gesv(nan="a_im"), capfd) == -4
+        assert _both(libs, fn, gesv(nan="b"), capfd) == -7
+        assert _both(libs, fn, gesv(zero_col=True), capfd) == 3
+        if layout == 101:
+            assert _both(libs, fn, gesv(lda_off=1), capfd) == -5
+            assert _both(libs, fn, gesv(ldb_off=1), capfd) == -8
