@@ -185,7 +185,7 @@ def _special(kind, m, n, seed):
         a[:, n // 3] = 0
         a[:, (2 * n) // 3] = 0
     elif kind == "tiny":
-        a = a * 1e-306            # pivots below the safe minimum: ZGETRF2 divides
+        a = a * 1e-309            # subnormal pivots, below the safe minimum: ZGETRF2 divides
     elif kind == "signed_zeros":
         z = np.array([0.0, -0.0])
         mask = np.random.default_rng(seed).random((m, n)) < 0.3
