@@ -440,12 +440,14 @@ def run_gpu(args, rank, world):
     return result
 
 
-def run_batched(args):
+def run_batched(args, rank=0, world=1):
     """20000 independent systems, n uniform in [8, 512] (seeded), nrhs in
     {1, 2, 4}, entries N(0,1) with n*I added to every other system, solved in
     one persistent launch captured in a CUDA graph.  One step = one graph
     replay over the whole batch (inputs restored between steps, outside the
-    timed region)."""
+    timed region).  Under torchrun the batch is partitioned over the ranks by
+    LU cost (lapack_gb300.shard), each rank solving its share with no
+    collective on the data path; the step time is the maximum over ranks."""
     import torch
     import lapack_gb300 as g
     from lapack_gb300 import autotune
@@ -458,6 +460,12 @@ def run_batched(args):
     rng = np.random.default_rng(args.seed)
     ns = rng.integers(8, 513, args.batch).astype(np.int64)
     nrhs = rng.choice([1, 2, 4], args.batch).astype(np.int64)
+    glob = np.arange(args.batch)                   # global system index of each local system
+    if world > 1:
+        from lapack_gb300 import shard
+        glob = shard.partition_by_cost(ns, nrhs, world)[rank]
+        ns, nrhs = ns[glob], nrhs[glob]
+    batch = len(ns)
     aoff = np.concatenate([[0], np.cumsum(ns * ns)])
     boff = np.concatenate([[0], np.cumsum(ns * nrhs)])
     poff = np.concatenate([[0], np.cumsum(ns)])
@@ -465,12 +473,13 @@ def run_batched(args):
     A = torch.randn(int(aoff[-1]), dtype=dtype, device=dev, generator=gen)
     B = torch.randn(int(boff[-1]), dtype=dtype, device=dev, generator=gen)
     # n*I on every other system's diagonal
-    diag = np.concatenate([aoff[i] + np.arange(ns[i]) * (ns[i] + 1) for i in range(0, args.batch, 2)])
-    vals = np.concatenate([np.full(ns[i], float(ns[i])) for i in range(0, args.batch, 2)])
+    shifted = [i for i in range(batch) if glob[i] % 2 == 0]
+    diag = np.concatenate([aoff[i] + np.arange(ns[i]) * (ns[i] + 1) for i in shifted])
+    vals = np.concatenate([np.full(ns[i], float(ns[i])) for i in shifted])
     A.index_add_(0, torch.from_numpy(diag).to(dev), torch.from_numpy(vals).to(dev, dtype))
     A0, B0 = A.clone(), B.clone()
     ipiv = torch.zeros(int(poff[-1]), dtype=torch.int32, device=dev)
-    info = torch.zeros(args.batch, dtype=torch.int32, device=dev)
+    info = torch.zeros(batch, dtype=torch.int32, device=dev)
     d_n = torch.from_numpy(ns.astype(np.int32)).to(dev)
     d_r = torch.from_numpy(nrhs.astype(np.int32)).to(dev)
     Ap = torch.from_numpy((A.data_ptr() + aoff[:-1] * es).astype(np.int64)).to(dev)
@@ -480,7 +489,7 @@ def run_batched(args):
     vp = lambda t: ctypes.c_void_p(t.data_ptr())
 
     def launch(stream):
-        rc = fn(args.batch, vp(d_n), vp(d_r), vp(Ap), vp(d_n), vp(Pp), vp(Bp), vp(d_n), vp(info),
+        rc = fn(batch, vp(d_n), vp(d_r), vp(Ap), vp(d_n), vp(Pp), vp(Bp), vp(d_n), vp(info),
                 ctypes.c_void_p(stream.cuda_stream))
         if rc:
             raise RuntimeError(f"batched solve status {rc}")
@@ -505,6 +514,9 @@ def run_batched(args):
         A.copy_(A0)
         B.copy_(B0)
         torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -517,6 +529,14 @@ def run_batched(args):
     ms = sum(times) / len(times)
     flops = float(np.sum(2.0 / 3.0 * ns.astype(np.float64) ** 3 + 2.0 * ns ** 2 * nrhs))
     bytes_ = float(np.sum(es * (2.0 * ns * ns + 2.0 * ns * nrhs) + 4.0 * ns))
+    info_nonzero = int((info != 0).sum().item())
+    if world > 1:
+        # whole-job figures: the slowest rank's time, the work of all ranks
+        red = torch.tensor([ms, 0.0, 0.0, 0.0], dtype=torch.float64, device=dev)
+        tot = torch.tensor([0.0, flops, bytes_, float(info_nonzero)], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(red, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
+        ms, flops, bytes_, info_nonzero = float(red[0]), float(tot[1]), float(tot[2]), int(tot[3])
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     L.gb300_probe_peak.restype = ctypes.c_double
@@ -526,7 +546,7 @@ def run_batched(args):
     hA, hB = A0.cpu().numpy(), B0.cpu().numpy()
     X = B.cpu().numpy()
     worst = 0.0
-    for i in list(range(0, args.batch, max(1, args.batch // 8))):
+    for i in list(range(0, batch, max(1, batch // 8))):
         n, r = int(ns[i]), int(nrhs[i])
         a = hA[aoff[i]:aoff[i + 1]].reshape(n, n).T.astype(np.float64)
         b = hB[boff[i]:boff[i + 1]].reshape(r, n).T.astype(np.float64)
@@ -535,14 +555,17 @@ def run_batched(args):
         worst = max(worst, res)
     return {
         "metric": f"batched uneven {'D' if args.dtype == 'd' else 'S'}GESV: {args.batch} systems, n in [8,512], nrhs in {{1,2,4}}, one persistent launch",
-        "value": ms * 1e-3, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": False, "dtype": "f64" if args.dtype == "d" else "f32", "data": "synthetic",
+        "value": ms * 1e-3, "unit": "s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": False, "scaling": "strong", "dtype": "f64" if args.dtype == "d" else "f32",
+        "data": "synthetic",
         "config": {"workload": "batched uneven solves in one CUDA-graph-captured persistent launch", "batch": args.batch,
+                   "parallelism": (f"systems partitioned by LU cost over {world} ranks, no collective"
+                                   if world > 1 else "single GPU"),
                    "nb_table": g.vbatched_nb(0 if args.dtype == "d" else 1),
                    "l2": f"inputs {bytes_ / 2e9:.1f} GB >> L2"},
-        "gflops": flops / ms / 1e6, "fma_peak_tflops": fma_peak, "frac_of_fma_peak": flops / ms / 1e9 / fma_peak,
-        "hbm_gbs": bytes_ / ms / 1e6, "frac_of_hbm": bytes_ / ms / 1e6 / hbm, "algorithmic_bytes": bytes_,
-        "algorithmic_flops": flops, "info_nonzero": int((info != 0).sum().item()), "worst_scaled_residual": worst,
+        "gflops": flops / ms / 1e6, "fma_peak_tflops": fma_peak, "frac_of_fma_peak": flops / ms / 1e9 / (fma_peak * world),
+        "hbm_gbs": bytes_ / ms / 1e6, "frac_of_hbm": bytes_ / ms / 1e6 / (hbm * world), "algorithmic_bytes": bytes_,
+        "algorithmic_flops": flops, "info_nonzero": info_nonzero, "worst_scaled_residual": worst,
         "gpu_launches": (L.gb300_launch_count() - launches0) // max(1, args.steps + args.warmup), "clocks": clk,
     }
 
@@ -620,7 +643,7 @@ def run_adjoint(args):
             "ms_per_step": ms, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "adjoint batch 64 x n=2048 x nrhs=8, factors resident", "forward_s": t_fwd},
             "kernels": parts, "algorithmic_bytes": bytes_, "hbm_gbs": bytes_ / ms / 1e6,
-            "frac_of_hbm": bytes_ / ms / 1e6 / hbm,
+            "frac_of_hbm": bytes_ / ms / 1e6 / (hbm * world),
             "roofline": {"bound": "fp64-fma", "achieved": tf, "peak": dfma, "unit": "TFLOP/s", "frac": tf / dfma,
                          "peak_source": "gb300_probe_peak FP64 FMA loop measured in this run",
                          "work": "4*n^2*nrhs flop per system"}}
@@ -629,7 +652,17 @@ def run_adjoint(args):
 def main():
     args = parse()
     if args.workload == "batched" and args.impl == "gb300":
-        print(json.dumps(run_batched(args)))
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        rank = int(os.environ.get("RANK", "0"))
+        if world > 1:
+            import torch
+            torch.distributed.init_process_group("nccl")
+        result = run_batched(args, rank, world)
+        if rank == 0:
+            print(json.dumps(result))
+        if world > 1:
+            torch.distributed.barrier()
+            torch.distributed.destroy_process_group()
         return
     if args.workload == "adjoint" and args.impl == "gb300":
         print(json.dumps(run_adjoint(args)))
