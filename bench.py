@@ -643,7 +643,7 @@ def run_adjoint(args):
             "ms_per_step": ms, "higher_is_better": False, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "adjoint batch 64 x n=2048 x nrhs=8, factors resident", "forward_s": t_fwd},
             "kernels": parts, "algorithmic_bytes": bytes_, "hbm_gbs": bytes_ / ms / 1e6,
-            "frac_of_hbm": bytes_ / ms / 1e6 / (hbm * world),
+            "frac_of_hbm": bytes_ / ms / 1e6 / hbm,
             "roofline": {"bound": "fp64-fma", "achieved": tf, "peak": dfma, "unit": "TFLOP/s", "frac": tf / dfma,
                          "peak_source": "gb300_probe_peak FP64 FMA loop measured in this run",
                          "work": "4*n^2*nrhs flop per system"}}
