@@ -127,6 +127,12 @@ void dsposv_(const char* uplo, const lapack_int* n, const lapack_int* nrhs, doub
  * converts to the void* parameters. */
 void zgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
              lapack_int* info);
+/* The recursive panel factorization alone.  Replaces SRC/zgetrf2.f:112 and
+ * SRC/cgetrf2.f:112 (lapack.h LAPACK_zgetrf2, LAPACK_cgetrf2). */
+void zgetrf2_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info);
+void cgetrf2_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info);
 void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
              const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t trans_len);
 void zgesv_(const lapack_int* n, const lapack_int* nrhs, void* a, const lapack_int* lda, lapack_int* ipiv, void* b,

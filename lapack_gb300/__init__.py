@@ -340,6 +340,17 @@ def zgetrf(a, dtype=np.complex128):
     return a, ipiv[: min(m, n)], info.value
 
 
+def zgetrf2(a, dtype=np.complex128):
+    """ZGETRF2 / CGETRF2 (SRC/zgetrf2.f): the recursive factorization alone."""
+    a = _fortran(a, dtype)
+    m, n = a.shape
+    ipiv = np.zeros(max(1, min(m, n)), dtype=np.int32)
+    info = ctypes.c_int(0)
+    getattr(lib(), f"{_zpre(dtype)}getrf2_")(_ref(m), _ref(n), _ptr(a), _ref(max(1, m)), _ptr(ipiv),
+                                             ctypes.byref(info))
+    return a, ipiv[: min(m, n)], info.value
+
+
 def zgetrs(lu, ipiv, b, trans="N"):
     """ZGETRS / CGETRS (SRC/zgetrs.f) in the precision of ``lu``, TRANS =
     'N', 'T' or 'C': returns (x, info)."""

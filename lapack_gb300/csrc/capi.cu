@@ -256,8 +256,8 @@ void potrs_host(const char* name, const char* uplo, const lapack_int* n, const l
 // size 64, as the reference does.
 template <typename R>
 void zgetrf_host(const char* name, const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda,
-                 lapack_int* ipiv, lapack_int* info) {
-  // SRC/zgetrf.f:144-157
+                 lapack_int* ipiv, lapack_int* info, int nb = 64) {
+  // SRC/zgetrf.f:144-157 (nb = 1: xGETRF2 alone, SRC/zgetrf2.f:154-170)
   using C = gb::cpx<R>;
   *info = 0;
   if (*m < 0) *info = -1;
@@ -272,7 +272,7 @@ void zgetrf_host(const char* name, const lapack_int* m, const lapack_int* n, voi
   C* ha = static_cast<C*>(a);
   int inf = 0;
   int rc = h2d(dA.as<C>(), ld, ha, *lda, M, N, s);
-  if (!rc) rc = gb::zgetrf_dev<R>(M, N, dA.as<C>(), ld, dP.as<int>(), 64, &inf, s);
+  if (!rc) rc = gb::zgetrf_dev<R>(M, N, dA.as<C>(), ld, dP.as<int>(), nb, &inf, s);
   if (!rc) rc = d2h(ha, *lda, dA.as<C>(), ld, M, N, s);
   if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
   if (!rc) rc = finish(s);
@@ -769,6 +769,14 @@ void zgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int
 void cgetrf_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
              lapack_int* info) {
   zgetrf_host<float>("CGETRF", m, n, a, lda, ipiv, info);
+}
+void zgetrf2_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info) {
+  zgetrf_host<double>("ZGETRF2", m, n, a, lda, ipiv, info, 1);
+}
+void cgetrf2_(const lapack_int* m, const lapack_int* n, void* a, const lapack_int* lda, lapack_int* ipiv,
+              lapack_int* info) {
+  zgetrf_host<float>("CGETRF2", m, n, a, lda, ipiv, info, 1);
 }
 void zgetrs_(const char* trans, const lapack_int* n, const lapack_int* nrhs, const void* a, const lapack_int* lda,
              const lapack_int* ipiv, void* b, const lapack_int* ldb, lapack_int* info, size_t) {

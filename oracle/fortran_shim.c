@@ -150,6 +150,14 @@ void or_zcgesv(int, int, void *, int, int *, const void *, int, void *, int, voi
 void cgetrf_(const int *m, const int *n, void *a, const int *lda, int *ipiv, int *info) {
   or_cgetrf(*m, *n, a, *lda, ipiv, info);
 }
+void or_zgetrf2(int, int, void *, int, int *, int *);
+void or_cgetrf2(int, int, void *, int, int *, int *);
+void zgetrf2_(const int *m, const int *n, void *a, const int *lda, int *ipiv, int *info) {
+  or_zgetrf2(*m, *n, a, *lda, ipiv, info);
+}
+void cgetrf2_(const int *m, const int *n, void *a, const int *lda, int *ipiv, int *info) {
+  or_cgetrf2(*m, *n, a, *lda, ipiv, info);
+}
 void cgetrs_(const char *trans, const int *n, const int *nrhs, const void *a, const int *lda, const int *ipiv,
              void *b, const int *ldb, int *info, size_t l) {
   (void)l;

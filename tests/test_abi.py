@@ -163,6 +163,9 @@ def test_fortran_abi_error_exits(lib):
         for (m, n, lda), code in ERR_GETRF:
             lib.cgetrf_(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
             assert info.value == -code and g.xerbla_last() == ("CGETRF", code)
+            for pre in "zc":
+                getattr(lib, pre + "getrf2_")(_i(m), _i(n), p(a), _i(lda), p(ip), ctypes.byref(info))
+                assert info.value == -code and g.xerbla_last() == (pre.upper() + "GETRF2", code)
         for (tr, n, nrhs, lda, ldb), code in ERR_GETRS:
             lib.cgetrs_(ctypes.c_char_p(tr.encode()), _i(n), _i(nrhs), p(a), _i(lda), p(ip), p(a), _i(ldb),
                         ctypes.byref(info), ctypes.c_size_t(1))

@@ -204,3 +204,15 @@ def test_zcgesv_exit_codes(gpu):
         ao_g, ip_g, x_g, it_g, info_g = gpu.zcgesv(aa, bb)
         assert it_g == it_r == want and info_g == info_r == 0
         assert _same_bits(x_g, x_r) and _same_bits(ao_g, ao_r) and np.array_equal(ip_g, ip_r)
+
+
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64])
+def test_zgetrf2_recursive_alone_bitwise(gpu, dtype):
+    """xGETRF2 as its own entry point: the whole matrix by the recursion, as
+    the oracle's ZGETRF with block size 1."""
+    for m, n in ((90, 90), (120, 70), (70, 120)):
+        a = oracle.random_zmatrix(m, n, 13 * m + n).astype(dtype)
+        lu_r, ip_r, info_r = oracle.zgetrf(a, nb=1, dtype=dtype)
+        lu_g, ip_g, info_g = gpu.zgetrf2(a, dtype=dtype)
+        assert info_g == info_r == 0 and np.array_equal(ip_g, ip_r)
+        assert _same_bits(lu_g, lu_r)
