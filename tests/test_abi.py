@@ -220,3 +220,32 @@ def test_lapacke_argument_codes(lib, capfd):
         assert "Wrong parameter 5 in LAPACKE_dgesv_work" in out
     finally:
         g.xerbla_capture(False)
+
+
+def test_header_accepts_c_complex_arrays(tmp_path):
+    """A C caller's double _Complex / float _Complex arrays (LAPACKE's
+    lapack_complex_double / _float in C) pass to the complex entry points
+    without casts, and the header compiles as C99 and as C++."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("needs gcc")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <complex.h>\n#include "lapack_gb300.h"\n'
+        "void use(double _Complex *a, double _Complex *b, float _Complex *c, lapack_int *ip) {\n"
+        "  lapack_int n = 2, nrhs = 1, info = 0, it = 0;\n"
+        "  zgesv_(&n, &nrhs, a, &n, ip, b, &n, &info);\n"
+        "  cgetrf_(&n, &n, c, &n, ip, &info);\n"
+        "  (void)LAPACKE_zgesv(LAPACK_COL_MAJOR, n, nrhs, a, n, ip, b, n);\n"
+        "  (void)LAPACKE_zcgesv(LAPACK_COL_MAJOR, n, nrhs, a, n, ip, b, n, b, n, &it);\n"
+        "}\n")
+    inc = os.path.join(ROOT, "include")
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-c", str(src), "-I", inc, "-o",
+                        str(tmp_path / "caller.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    cpp = tmp_path / "caller.cpp"
+    cpp.write_text('#include "lapack_gb300.h"\nint main() { return 0; }\n')
+    r = subprocess.run(["g++", "-std=c++11", "-Wall", "-Werror", "-c", str(cpp), "-I", inc, "-o",
+                        str(tmp_path / "caller2.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
