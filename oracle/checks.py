@@ -291,7 +291,9 @@ def lu_rel_diff(lu_a, lu_b, a):
 
 def zget01(a, lu, ipiv):
     """||P L U - A||_1 / (N ||A||_1 eps) for complex factors, ZLANGE('1') on
-    moduli (TESTING/LIN/zget01.f)."""
+    moduli (TESTING/LIN/zget01.f; CGET01 with the COMPLEX eps for complex64
+    factors)."""
+    eps = EPS32 if np.asarray(lu).dtype == np.complex64 else EPS64
     a = np.asarray(a, dtype=np.complex128)
     m, n = a.shape
     if m == 0 or n == 0:
@@ -300,14 +302,17 @@ def zget01(a, lu, ipiv):
     anorm = np.abs(a).sum(axis=0).max()
     resid = np.abs(L @ U - a[perm, :]).sum(axis=0).max()
     if anorm <= 0:
-        return 0.0 if resid == 0 else 1.0 / EPS64
-    return ((resid / n) / anorm) / EPS64
+        return 0.0 if resid == 0 else 1.0 / eps
+    return ((resid / n) / anorm) / eps
 
 
-def zget02(a, x, b, trans="N"):
+def zget02(a, x, b, trans="N", eps=None):
     """max_j DZASUM(b_j - op(A) x_j) / (||op(A)||_1 DZASUM(x_j) eps)
     (TESTING/LIN/zget02.f): ZLANGE('1') for TRANS = 'N', ZLANGE('I')
-    otherwise; DZASUM sums |re| + |im|."""
+    otherwise; DZASUM sums |re| + |im|.  eps defaults to the COMPLEX*16 one,
+    or the COMPLEX one for a complex64 solution."""
+    if eps is None:
+        eps = EPS32 if np.asarray(x).dtype == np.complex64 else EPS64
     a = np.asarray(a, dtype=np.complex128)
     x = np.asarray(x, dtype=np.complex128).reshape(a.shape[0], -1)
     b = np.asarray(b, dtype=np.complex128).reshape(a.shape[0], -1)
@@ -315,7 +320,7 @@ def zget02(a, x, b, trans="N"):
         return 0.0
     anorm = np.abs(a).sum(axis=0).max() if trans == "N" else np.abs(a).sum(axis=1).max()
     if anorm <= 0:
-        return 1.0 / EPS64
+        return 1.0 / eps
     op = a if trans == "N" else (a.T if trans == "T" else a.conj().T)
     r = b - op @ x
     dzasum = lambda v: np.abs(v.real).sum() + np.abs(v.imag).sum()
@@ -323,8 +328,8 @@ def zget02(a, x, b, trans="N"):
     for j in range(x.shape[1]):
         xn = dzasum(x[:, j])
         if xn <= 0:
-            return 1.0 / EPS64
-        resid = max(resid, ((dzasum(r[:, j]) / anorm) / xn) / EPS64)
+            return 1.0 / eps
+        resid = max(resid, ((dzasum(r[:, j]) / anorm) / xn) / eps)
     return resid
 
 

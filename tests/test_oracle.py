@@ -587,3 +587,29 @@ def test_zcgesv_fallback_and_exit_codes():
     d = np.diag([1.0, 1e-50, 1.0]).astype(np.complex128)
     _, _, x, it, info = oracle.zcgesv(d, np.ones((3, 1), dtype=np.complex128))
     assert it == -3 and info == 0 and abs(x[1, 0] - 1e50) < 1e36
+
+
+@pytest.mark.parametrize("imat", range(1, 12))
+def test_cgetrf_cchkge_ratios(imat):
+    """CCHKGE tests 1 and 3 (the COMPLEX twin of ZCHKGE) with the COMPLEX eps:
+    INFO = IZERO, CGET01 < THRESH, CGET02 < THRESH for TRANS = N, T, C; the
+    ill-conditioned types 8 and 9 are skipped for the solve as single
+    precision cannot reach them."""
+    for n in INPUTS["dtest"]["n"]:
+        if 5 <= imat <= 7 and n < imat - 4:
+            continue
+        a, izero = oracle.zge_test_matrix(n, n, imat, 2011 + 7 * n)
+        if imat >= 10:
+            a = a * (1e-30 / 1e-290 if imat == 10 else 1e30 / 1e290)   # scalings inside COMPLEX's range
+        a = a.astype(np.complex64)
+        lu, ipiv, info = oracle.zgetrf(a, dtype=np.complex64)
+        assert info == izero, (n, imat, info, izero)
+        if n:
+            assert ck.zget01(a, lu, ipiv) < THRESH, (n, imat)
+        if n and izero == 0 and imat not in (8, 9):
+            xact = oracle.random_zmatrix(n, 2, 5 + n).astype(np.complex64)
+            for trans in "NTC":
+                op = a if trans == "N" else (a.T if trans == "T" else a.conj().T)
+                b = (op.astype(np.complex128) @ xact).astype(np.complex64)
+                x, info = oracle.zgetrs(lu, ipiv, b, trans)
+                assert info == 0 and ck.zget02(a, x, b, trans) < THRESH, (n, imat, trans)
