@@ -13,69 +13,16 @@ with the oracle bit for bit.  This checks the kernels' index arithmetic,
 launch geometry and the backend that drives the shared schedules."""
 import ctypes
 import os
-import re
 import shutil
-import subprocess
 
 import numpy as np
 import pytest
 
+import cuda_emu
 import oracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "..", "lapack_gb300", "csrc")
-
-EMU = r"""
-#pragma once
-// CPU stand-in for the CUDA runtime calls and kernel launches of zlu.cu.
-#include <cstddef>
-#include <cstdlib>
-#include <cstring>
-#include <cstdio>
-#define __global__
-#define __launch_bounds__(...)
-struct dim3 { unsigned x, y, z; };
-static thread_local dim3 blockIdx, threadIdx, blockDim;
-typedef void* cudaStream_t;
-typedef int cudaError_t;
-enum { cudaSuccess = 0, cudaErrorMemoryAllocation = 2 };
-enum cudaMemcpyKind { cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
-static inline int atomicMin(int* p, int v) { int o = *p; if (v < o) *p = v; return o; }
-static inline cudaError_t cudaMemcpyAsync(void* d, const void* s, size_t n, cudaMemcpyKind, cudaStream_t) {
-  memmove(d, s, n); return cudaSuccess; }
-static inline cudaError_t cudaMemcpy2DAsync(void* d, size_t dp, const void* s, size_t sp, size_t w, size_t h,
-                                            cudaMemcpyKind, cudaStream_t) {
-  for (size_t r = 0; r < h; ++r) memmove((char*)d + r * dp, (const char*)s + r * sp, w);
-  return cudaSuccess; }
-static inline cudaError_t cudaMemsetAsync(void* d, int v, size_t n, cudaStream_t) { memset(d, v, n); return cudaSuccess; }
-static inline cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
-static inline cudaError_t cudaGetLastError() { return cudaSuccess; }
-static inline const char* cudaGetErrorString(cudaError_t) { return "emulated"; }
-#define GB_LAUNCH(...) do { __VA_ARGS__; } while (0)
-#define GB_CUDA_TRY(expr) do { cudaError_t _e = (expr); if (_e != cudaSuccess) return (int)_e; } while (0)
-namespace emu {
-template <typename K, typename... A>
-void launch(K kernel, unsigned grid, unsigned block, int, cudaStream_t, A... args) {
-  blockDim = dim3{block, 1, 1};
-  for (unsigned b = 0; b < grid; ++b)
-    for (unsigned t = 0; t < block; ++t) {
-      blockIdx = dim3{b, 0, 0};
-      threadIdx = dim3{t, 0, 0};
-      kernel(args...);
-    }
-}
-}  // namespace emu
-namespace gb {
-struct DevScratch {
-  void* p = nullptr;
-  DevScratch(size_t bytes, cudaStream_t) { p = calloc(1, bytes ? bytes : 1); }
-  ~DevScratch() { free(p); }
-  DevScratch(const DevScratch&) = delete;
-  DevScratch& operator=(const DevScratch&) = delete;
-  template <typename T> T* as() const { return static_cast<T*>(p); }
-};
-}  // namespace gb
-"""
 
 ENTRY = r"""
 extern "C" {
@@ -104,31 +51,14 @@ int emu_zcgesv(int n, int nrhs, double* a, int lda, int* ipiv, const double* b, 
 """
 
 
-def _translate(src):
-    """zlu.cu with its launches made sequential and its CUDA headers replaced."""
-    src = src.replace('#include "common.cuh"\n', '#include "emu_cuda.h"\n')
-    src = src.replace('#include "driver.h"\n', "")
-    launch = re.compile(r"(\w+(?:<\w+>)?)<<<(.*?)>>>\(")
-    out, n = launch.subn(lambda m: f"emu::launch({m.group(1)}, {m.group(2)}, ", src)
-    assert n >= 10, n          # every kernel launch of the file was rewritten
-    assert "<<<" not in out
-    return out
-
-
 @pytest.fixture(scope="module")
 def emu(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("needs g++")
-    d = tmp_path_factory.mktemp("zluemu")
-    (d / "emu_cuda.h").write_text(EMU)
-    src = _translate(open(os.path.join(CSRC, "zlu.cu")).read())
-    (d / "zlu_emu.cpp").write_text(src + ENTRY)
-    so = d / "libzluemu.so"
-    cmd = ["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", str(d), "-I", CSRC,
-           str(d / "zlu_emu.cpp"), "-o", str(so)]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    assert r.returncode == 0, r.stderr[-4000:]
-    L = ctypes.CDLL(str(so))
+    d = str(tmp_path_factory.mktemp("zluemu"))
+    src = cuda_emu.translate(open(os.path.join(CSRC, "zlu.cu")).read(), min_launches=10)
+    so = cuda_emu.build(d, "zluemu", src + ENTRY, [CSRC])
+    L = ctypes.CDLL(so)
     p, i = ctypes.c_void_p, ctypes.c_int
     L.emu_zgetrf.argtypes = [i, i, p, i, p, i]
     L.emu_cgetrf.argtypes = [i, i, p, i, p, i]
