@@ -637,8 +637,11 @@ void dgesvx_(const char* fact, const char* trans, const lapack_int* n, const lap
   if (!rc && !factored && N > 0) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
   if (!rc && equil && N > 0) rc = (int)cudaMemcpyAsync(r, dR, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
   if (!rc && equil && N > 0) rc = (int)cudaMemcpyAsync(c, dC, sizeof(double) * N, cudaMemcpyDeviceToHost, s);
+  // B comes back in every case: it is scaled before the factorization
+  // (SRC/dgesvx.f:492-508, before DGETRF at :515), so a singular U leaves it
+  // scaled as well
   const bool solved = inf == 0 || inf == N + 1;
-  if (!rc && solved) rc = d2h(b, *ldb, dB.as<double>(), ld, N, R, s);
+  if (!rc) rc = d2h(b, *ldb, dB.as<double>(), ld, N, R, s);
   if (!rc && solved) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
   if (!rc && solved && R > 0) rc = (int)cudaMemcpyAsync(ferr, dF, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
   if (!rc && solved && R > 0) rc = (int)cudaMemcpyAsync(berr, dBe, sizeof(double) * R, cudaMemcpyDeviceToHost, s);
