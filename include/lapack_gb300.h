@@ -397,8 +397,11 @@ int gb300_dgerfs_dev(char trans, int n, int nrhs, const double* dA, int lda, con
  * it accepts n <= 16384 and n*nrhs <= 131072 and returns -100 for larger
  * problems.  The first call on a device looks up that array's address and
  * should come before any stream capture.  All calls share the array: calls
- * that overlap on the GPU race, so issue them one after another.  Same
- * arguments, results and return codes as gb300_dgetrs_dev otherwise. */
+ * that overlap on the GPU race, so issue them one after another.  Each call
+ * waits for its stream before it returns.  Same arguments and return codes
+ * as gb300_dgetrs_dev otherwise; the solution agrees with that routine's to
+ * rounding (this variant always runs the default FMA-form solve and does not
+ * follow the exact-mode option). */
 int gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double* dA, int lda, const int* dIpiv, double* dB,
                          int ldb, void* stream);
 
@@ -482,7 +485,9 @@ int gb300_prof_enable(int on);
 unsigned gb300_prof_mask(unsigned mask);
 void gb300_prof_reset(void);
 int gb300_prof_read(int kind, double* ms, double* flops, double* bytes, long long* launches);
-/* Measured FMA throughput of the current GPU in TFLOP/s (0: FP64, 1: FP32). */
+/* Measured arithmetic throughput of the current GPU in TFLOP/s: 0 FP64 FMA,
+ * 1 FP32 FMA, 2 FP64 tensor core (mma.sync m8n8k4), 3 FP64 tensor core
+ * (mma.sync m16n8k16); -1 for another value.  No reference counterpart. */
 double gb300_probe_peak(int which);
 
 #ifdef __cplusplus

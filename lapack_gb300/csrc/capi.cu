@@ -4,6 +4,7 @@
 #include "../../include/lapack_gb300.h"
 #include "driver.h"
 #include "latrs_seq.h"
+#include "prof.h"
 #include "zlu_seq.h"
 
 #include <algorithm>
@@ -435,15 +436,19 @@ void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapac
       dX(sizeof(double) * (size_t)ld * std::max(R, 1), s), dP(sizeof(int) * N, s);
   if (!dA.p || !dB.p || !dX.p || !dP.p) { device_failure("DSGESV", (int)cudaErrorMemoryAllocation, info); return; }
   int it = 0, inf = 0;
+  gb::prof_begin(gb::kProfCopyH2D, s);
   int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
   if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  gb::prof_end(gb::kProfCopyH2D, s, 0.0, 8.0 * (double)N * (N + R));
   if (!rc) rc = gb::dsgesv_dev(N, R, dA.as<double>(), ld, dP.as<int>(), dB.as<double>(), ld, dX.as<double>(), ld,
                                &it, &inf, s);
   if (!rc) rc = finish(s);
   // A is returned unchanged when ITER >= 0 and holds the FP64 LU otherwise
+  gb::prof_begin(gb::kProfCopyD2H, s);
   if (!rc && it < 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
   if (!rc && inf == 0) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
   if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  gb::prof_end(gb::kProfCopyD2H, s, 0.0, 8.0 * (double)N * ((it < 0 ? N : 0) + R) + 4.0 * N);
   if (!rc) rc = finish(s);
   if (rc) { device_failure("DSGESV", rc, info); return; }
   *iter = it;
@@ -680,7 +685,7 @@ void dgetri_(const lapack_int* n, double* a, const lapack_int* lda, const lapack
   int inf = 0;
   int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
   if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
-  if (!rc) rc = gb::dgetri_dev(N, dA.as<double>(), ld, dP.as<int>(), nb_run, &inf, s);
+  if (!rc) rc = gb::dgetri_dev(N, dA.as<double>(), ld, dP.as<int>(), options().nb_f64, nb_run, &inf, s);
   if (!rc && inf == 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
   if (!rc) rc = finish(s);
   if (rc) { device_failure("DGETRI", rc, info); return; }
@@ -1055,7 +1060,7 @@ int gb300_dgetri_dev(int n, double* dA, int lda, const int* dIpiv, int* info, vo
   if (lda < std::max(1, n)) return -3;
   cudaStream_t s = (cudaStream_t)stream;
   int inf = 0;
-  int rc = gb::dgetri_dev(n, dA, lda, dIpiv, options().nb_f64, &inf, s);
+  int rc = gb::dgetri_dev(n, dA, lda, dIpiv, options().nb_f64, options().nb_f64, &inf, s);
   if (!rc) rc = finish(s);
   if (info) *info = inf;
   return rc;

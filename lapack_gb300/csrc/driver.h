@@ -117,8 +117,9 @@ int dgesvx_dev(char fact, char trans, int n, int nrhs, double* A, int lda, doubl
                double colcnd, double* rcond, double* ferr, double* berr, double* rpvgrw, int* info, cudaStream_t s);
 // MIN(s) <= 0 test (returns 1) and MAX(min,SMLNUM)/MIN(max,BIGNUM) of device scalings.
 int scalings_cnd_dev(int n, const double* s_dev, double* cnd, cudaStream_t s, int* err);
-// DGETRI on device memory with block size nb; *info is a host output.
-int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cudaStream_t s);
+// DGETRI on device memory: DTRTRI in blocks of nb_trtri, the inv(A)*L loop
+// in blocks of nb (the workspace-limited value); *info is a host output.
+int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb_trtri, int nb, int* info, cudaStream_t s);
 // DGERFS on device memory; FERR/BERR are device arrays of nrhs doubles.
 int dgerfs_dev(char trans, int n, int nrhs, const double* A, int lda, const double* AF, int ldaf, const int* ipiv,
                const double* B, int ldb, double* X, int ldx, double* ferr, double* berr, cudaStream_t s);

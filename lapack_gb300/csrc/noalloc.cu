@@ -23,7 +23,13 @@
 // On the first call on a device the library looks up the array's device
 // address (cudaGetSymbolAddress) with that device current and sets the
 // shared-memory attributes of the kernels it launches; make that first call
-// before any stream capture.  No cudaMalloc, cudaFree or allocating library routine is called.
+// before any stream capture.  Every call reads the kernels' status word back
+// and waits for its stream before it returns.  No cudaMalloc, cudaFree or
+// allocating library routine is called.
+//
+// The solution agrees with gb300_dgetrs_dev's to rounding: both solve with
+// the same factors, but this variant always uses the blocked solve kernel in
+// its default (FMA) form and does not follow the exact-mode option.
 #include "../../include/lapack_gb300.h"
 #include "common.cuh"
 #include "prof.h"
@@ -81,12 +87,13 @@ int setup_device(unsigned char** base) {
 }
 
 template <bool FORWARD, bool UNIT, bool TRANS>
-void launch_solve(const double* A, int lda, int n, double* W, int nrhs, int* flags, int* status, cudaStream_t s) {
+int launch_solve(const double* A, int lda, int n, double* W, int nrhs, int* flags, int* status, cudaStream_t s) {
   const int nblk = (n + kSolveBS - 1) / kSolveBS;
   unsigned* ticket = reinterpret_cast<unsigned*>(flags + nblk);
-  cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), s);
-  GB_LAUNCH(trsv_blocked_kernel<double, false, FORWARD, UNIT, TRANS><<<nblk, 256, kTrsvSmem<double>, s>>>(A, lda, n, W, n, nrhs, flags,
-                                                                                        ticket, status));
+  GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * (size_t)(nblk + 1), s));
+  GB_LAUNCH(trsv_blocked_kernel<double, false, FORWARD, UNIT, TRANS>
+            <<<nblk, 256, kTrsvSmem<double>, s>>>(A, lda, n, W, n, nrhs, flags, ticket, status));
+  return 0;
 }
 
 }  // namespace
@@ -118,13 +125,13 @@ extern "C" int gb300_dgetrs_noalloc(char trans, int n, int nrhs, const double* d
   const unsigned blocks = (unsigned)((tot + 255) / 256);
   if (t == 'n') {
     GB_LAUNCH(perm_rows_kernel<double, false><<<blocks, 256, 0, s>>>(dB, ldb, W, n, perm, 0, n, nrhs));
-    launch_solve<true, true, false>(dA, lda, n, W, nrhs, flags, status, s);
-    launch_solve<false, false, false>(dA, lda, n, W, nrhs, flags, status, s);
+    if ((rc = launch_solve<true, true, false>(dA, lda, n, W, nrhs, flags, status, s))) return rc;
+    if ((rc = launch_solve<false, false, false>(dA, lda, n, W, nrhs, flags, status, s))) return rc;
     GB_LAUNCH(copy_cols_kernel<double><<<blocks, 256, 0, s>>>(W, n, dB, ldb, n, nrhs));
   } else {
     GB_LAUNCH(copy_cols_kernel<double><<<blocks, 256, 0, s>>>(dB, ldb, W, n, n, nrhs));
-    launch_solve<true, false, true>(dA, lda, n, W, nrhs, flags, status, s);
-    launch_solve<false, true, true>(dA, lda, n, W, nrhs, flags, status, s);
+    if ((rc = launch_solve<true, false, true>(dA, lda, n, W, nrhs, flags, status, s))) return rc;
+    if ((rc = launch_solve<false, true, true>(dA, lda, n, W, nrhs, flags, status, s))) return rc;
     GB_LAUNCH(perm_rows_kernel<double, true><<<blocks, 256, 0, s>>>(W, n, dB, ldb, perm, 0, n, nrhs));
   }
   int hstatus = 0;

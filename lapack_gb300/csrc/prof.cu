@@ -59,6 +59,43 @@ __global__ void probe_fma_kernel(T* out, int iters, T a, T b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// FP64 tensor-core (DMMA) probes: each warp keeps four independent
+// accumulator tiles and issues mma.sync back to back.  SHAPE 0 is
+// m8n8k4 (512 flop per instruction), SHAPE 1 is m16n8k16 (4096 flop).
+template <int SHAPE>
+__global__ void probe_dmma_kernel(double* out, int iters) {
+  const double a0 = 1.0 + 1e-9 * threadIdx.x, b0 = 1.0 - 1e-9 * threadIdx.x;
+  if constexpr (SHAPE == 0) {
+    double c[4][2] = {};
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(c[t][0]), "+d"(c[t][1])
+                     : "d"(a0), "d"(b0));
+    }
+    double acc = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc += c[t][0] + c[t][1];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+  } else {
+    double c[4][4] = {};
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int t = 0; t < 4; ++t)
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+                     "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
+                     : "+d"(c[t][0]), "+d"(c[t][1]), "+d"(c[t][2]), "+d"(c[t][3])
+                     : "d"(a0), "d"(a0), "d"(a0), "d"(a0), "d"(a0), "d"(a0), "d"(a0), "d"(a0), "d"(b0), "d"(b0),
+                       "d"(b0), "d"(b0));
+    }
+    double acc = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc += c[t][0] + c[t][1] + c[t][2] + c[t][3];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+  }
+}
+
 }  // namespace gb
 
 extern "C" {
@@ -101,14 +138,16 @@ int gb300_prof_read(int kind, double* ms, double* flops, double* bytes, long lon
   return 0;
 }
 
-// Measured FMA throughput of this GPU in TFLOP/s: which = 0 FP64 (DFMA),
-// 1 FP32 (FFMA).  A few tens of milliseconds of work.
+// Measured arithmetic throughput of this GPU in TFLOP/s: which = 0 FP64
+// FMA (DFMA), 1 FP32 FMA (FFMA), 2 FP64 tensor core mma.sync m8n8k4,
+// 3 FP64 tensor core mma.sync m16n8k16.  A few tens of milliseconds of work.
 double gb300_probe_peak(int which) {
+  if (which < 0 || which > 3) return -1.0;
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = nsm * 4, threads = 256;
-  const int iters = which == 0 ? 2000 : 20000;
+  const int iters = which == 0 ? 2000 : which == 1 ? 20000 : which == 2 ? 1000 : 200;
   void* out = nullptr;
   if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1.0;
   cudaEvent_t e0, e1;
@@ -118,7 +157,9 @@ double gb300_probe_peak(int which) {
   for (int rep = 0; rep < 3; ++rep) {
     cudaEventRecord(e0);
     if (which == 0) gb::probe_fma_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.999999, 1e-7);
-    else gb::probe_fma_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
+    else if (which == 1) gb::probe_fma_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.999999f, 1e-7f);
+    else if (which == 2) gb::probe_dmma_kernel<0><<<blocks, threads>>>((double*)out, iters);
+    else gb::probe_dmma_kernel<1><<<blocks, threads>>>((double*)out, iters);
     cudaEventRecord(e1);
     cudaEventSynchronize(e1);
     float ms = 0;
@@ -128,7 +169,9 @@ double gb300_probe_peak(int which) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(out);
-  double flops = 2.0 * 64.0 * iters * (double)blocks * threads;
+  double flops;
+  if (which <= 1) flops = 2.0 * 64.0 * iters * (double)blocks * threads;
+  else flops = (which == 2 ? 512.0 : 4096.0) * 4.0 * iters * (double)blocks * (threads / 32);
   return flops / (best * 1e-3) / 1e12;
 }
 

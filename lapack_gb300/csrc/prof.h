@@ -14,7 +14,9 @@ enum ProfKind : int {
   kProfTrsv = 6,        // blocked triangular solves (GETRS)
   kProfResidual = 7,    // FP64 residual of the refinement
   kProfOther = 8,
-  kProfKinds = 9,
+  kProfCopyH2D = 9,     // host-to-device operand copies of the host-pointer routines
+  kProfCopyD2H = 10,    // device-to-host result copies of the host-pointer routines
+  kProfKinds = 11,
 };
 
 // Counts one kernel launch of this library.

@@ -472,14 +472,17 @@ int scalings_cnd_dev(int n, const double* s_dev, double* cnd, cudaStream_t s, in
   return hb;
 }
 
-// DGETRI on device memory (SRC/dgetri.f:169-262) with block size nb (the
-// reference's ILAENV value is 64): DTRTRI of U by block columns (DTRMM with
-// the inverse so far, DTRSM with the diagonal block, DTRTI2 of the diagonal
-// block), then inv(A) from inv(U) and L by block columns right to left
-// (DGEMM through the library's update kernel, DTRSM with the unit lower
-// block), then the column interchanges.  *info: 0, or the first zero
-// pivot of U (A untouched then, as DTRTRI returns before any work).
-int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cudaStream_t s) {
+// DGETRI on device memory (SRC/dgetri.f:169-262): DTRTRI of U by block
+// columns of nb_trtri (DTRMM with the inverse so far, DTRSM with the diagonal
+// block, DTRTI2 of the diagonal block), then inv(A) from inv(U) and L by block
+// columns of nb right to left (DGEMM through the library's update kernel,
+// DTRSM with the unit lower block), then the column interchanges.  The two
+// block sizes differ as in the reference: DTRTRI always takes its own ILAENV
+// value (SRC/dtrtri.f:180, called at SRC/dgetri.f:180), while DGETRI's nb is
+// cut to LWORK/N when the workspace is short (SRC/dgetri.f:184-190) and
+// nb < 2 selects the unblocked loop.  *info: 0, or the first zero pivot of
+// U (A untouched then, as DTRTRI returns before any work).
+int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb_trtri, int nb, int* info, cudaStream_t s) {
   *info = 0;
   if (n <= 0) return 0;
   {
@@ -496,15 +499,15 @@ int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cu
       return 0;
     }
   }
-  const int nbe = std::max(1, nb);
+  const int nbt = std::max(1, nb_trtri);
   // ---- DTRTRI('U', 'N')
-  if (nbe <= 1 || nbe >= n) {
+  if (nbt <= 1 || nbt >= n) {
     GB_LAUNCH(trti2_upper_kernel<<<1, 1, 0, s>>>(n, A, lda));
   } else {
-    DevScratch cp(sizeof(double) * (size_t)n * nbe, s);
+    DevScratch cp(sizeof(double) * (size_t)n * nbt, s);
     if (!cp.p) return (int)cudaErrorMemoryAllocation;
-    for (int j = 0; j < n; j += nbe) {
-      const int jb = std::min(nbe, n - j);
+    for (int j = 0; j < n; j += nbt) {
+      const int jb = std::min(nbt, n - j);
       double* Bj = A + (size_t)j * lda;   // rows 0..j-1 of block column j
       if (j > 0) {
         GB_CUDA_TRY(cudaMemcpy2DAsync(cp.p, sizeof(double) * (size_t)j, Bj, sizeof(double) * (size_t)lda,
@@ -518,6 +521,7 @@ int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cu
     }
   }
   // ---- inv(A) * L = inv(U)
+  const int nbe = std::max(1, nb);
   const int ldw = n;
   DevScratch wb(sizeof(double) * (size_t)ldw * nbe, s);
   if (!wb.p) return (int)cudaErrorMemoryAllocation;

@@ -46,7 +46,9 @@ def test_inputs(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("LAPACK_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("usage: make_golden.py <reference tree>  (or set LAPACK_REFERENCE_DIR)")
     with open(os.path.join(HERE, "dlaruv_mm.json"), "w") as f:
         json.dump({"source": "SRC/dlaruv.f DATA MM(128,4)", "mm": dlaruv_table(ref)}, f)
     with open(os.path.join(HERE, "test_inputs.json"), "w") as f:

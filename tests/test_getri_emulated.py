@@ -42,9 +42,9 @@ int gemm_update_dev(int m, int n, int k, const T* A, int lda, const T* B, int ld
 
 ENTRY = r"""
 }  // namespace gb
-extern "C" int emu_dgetri(int n, double* a, int lda, const int* ipiv, int nb) {
+extern "C" int emu_dgetri(int n, double* a, int lda, const int* ipiv, int nb_trtri, int nb) {
   int info = 0;
-  gb::dgetri_dev(n, a, lda, ipiv, nb, &info, nullptr);
+  gb::dgetri_dev(n, a, lda, ipiv, nb_trtri, nb, &info, nullptr);
   return info;
 }
 """
@@ -63,14 +63,15 @@ def emu(tmp_path_factory):
     kern = open(os.path.join(CSRC, "condest_kernels.cuh")).read()
     kern = _slice(kern, "// ------------------------------------------------------------- DGETRI", "}  // namespace gb")
     drv = open(os.path.join(CSRC, "refine.cu")).read()
-    drv = _slice(drv, "int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb, int* info, cudaStream_t s) {",
+    drv = _slice(drv, "int dgetri_dev(int n, double* A, int lda, const int* ipiv, int nb_trtri, int nb, int* info,",
                  "\n}  // namespace gb") + "\n"
     src = cuda_emu.translate(PRELUDE + kern + drv + ENTRY, drop_includes=(), min_launches=7)
     oracle.lib()
     so = cuda_emu.build(str(tmp_path_factory.mktemp("getriemu")), "getriemu", src, [CSRC])
     ctypes.CDLL(os.path.join(ORACLE_DIR, "liboracle.so"), mode=ctypes.RTLD_GLOBAL)
     L = ctypes.CDLL(so)
-    L.emu_dgetri.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.emu_dgetri.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                             ctypes.c_int]
     return L
 
 
@@ -82,9 +83,25 @@ def test_getri_cu_bitwise(emu, nb, n, imat):
     ref, rinfo, _ = oracle.getri(lu, ipiv, nb=nb)
     got = np.asfortranarray(lu.copy())
     ginfo = emu.emu_dgetri(n, got.ctypes.data_as(ctypes.c_void_p), n,
-                           np.ascontiguousarray(ipiv, dtype=np.int32).ctypes.data_as(ctypes.c_void_p), nb)
+                           np.ascontiguousarray(ipiv, dtype=np.int32).ctypes.data_as(ctypes.c_void_p), nb, nb)
     assert ginfo == rinfo
     if rinfo == 0:
         assert got.tobytes(order="F") == np.asfortranarray(ref).tobytes(order="F")
     else:
         assert got.tobytes(order="F") == np.asfortranarray(lu).tobytes(order="F")   # untouched, as DTRTRI returns
+
+
+@pytest.mark.parametrize("n,lwork_cols", [(200, 5), (200, 1), (130, 2), (300, 63)])
+def test_getri_cu_short_workspace_bitwise(emu, n, lwork_cols):
+    """A workspace shorter than N*NB: DTRTRI keeps its block size of 64
+    (SRC/dtrtri.f:180) while the inv(A)*L loop runs with LWORK/N columns
+    (SRC/dgetri.f:184-190), or unblocked below NBMIN = 2."""
+    a, _ = oracle.ge_test_matrix(n, n, 1, 41 + n)
+    lu, ipiv, _ = oracle.getrf(a)
+    ref, rinfo, _ = oracle.getri(lu, ipiv, nb=64, lwork=n * lwork_cols)
+    assert rinfo == 0
+    nb_loop = lwork_cols if lwork_cols >= 2 else 1
+    got = np.asfortranarray(lu.copy())
+    emu.emu_dgetri(n, got.ctypes.data_as(ctypes.c_void_p), n,
+                   np.ascontiguousarray(ipiv, dtype=np.int32).ctypes.data_as(ctypes.c_void_p), 64, nb_loop)
+    assert got.tobytes(order="F") == np.asfortranarray(ref).tobytes(order="F")

@@ -58,6 +58,45 @@ def test_noalloc_matches_allocating_getrs(gpu, trans, n, nrhs):
         assert np.abs(x - x_ref).max() <= tol
 
 
+@pytest.mark.parametrize("trans,n,nrhs,pad", [("C", 8192, 16, 3), ("N", 4096, 32, 5), ("T", 16384, 8, 0)])
+def test_noalloc_at_scratch_limit_with_padded_ldb(gpu, trans, n, nrhs, pad):
+    """n*nrhs exactly at the 131072-element limit, ldb > n, TRANS = 'C':
+    the fixed offsets inside the scratch array at their largest extent.
+    Checked against the allocating entry point and, through the residual,
+    against the system itself."""
+    import torch
+    L = gpu.lib()
+    L.gb300_dgetrs_noalloc.argtypes = [ctypes.c_char, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+    a, b, dA, dIp = _setup(gpu, n, nrhs, 70 + n)
+    ldb = n + pad
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def padded():
+        buf = torch.zeros((nrhs, ldb), dtype=torch.float64, device="cuda")
+        buf[:, :n] = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+        return buf
+
+    def run(fn, buf):
+        return fn(ctypes.c_char(trans.encode()), n, nrhs, ctypes.c_void_p(dA.data_ptr()), dA.stride(1),
+                  ctypes.c_void_p(dIp.data_ptr()), ctypes.c_void_p(buf.data_ptr()), ldb, s)
+
+    ref = padded()
+    assert run(L.gb300_dgetrs_dev, ref) == 0
+    x_ref = ref[:, :n].cpu().numpy().T
+    for _ in range(2):
+        buf = padded()
+        assert run(L.gb300_dgetrs_noalloc, buf) == 0
+        got = buf.cpu().numpy()
+        assert np.all(got[:, n:] == 0.0)                   # the padding rows are not written
+        x = got[:, :n].T
+        tol = np.abs(x_ref).max() * n * np.finfo(np.float64).eps * 1e3
+        assert np.abs(x - x_ref).max() <= tol
+        op = a if trans == "N" else a.T
+        r = np.abs(b - op @ x).max() / (np.abs(op).sum(axis=1).max() * np.abs(x).max() * n * np.finfo(float).eps)
+        assert r < 30.0
+
+
 def test_noalloc_rejects_sizes_beyond_scratch(gpu):
     import torch
     L = gpu.lib()
