@@ -109,6 +109,20 @@ def backward_errors(A, X, B, n):
     return out, out / n
 
 
+def load_peaks():
+    """Roofline denominators: the measured copy bandwidth and BF16 GEMM
+    throughput of this machine's GPUs when MEASURED_PEAKS.json is present, else
+    the fallback figures of an earlier GB300 measurement (6.8 TB/s, 1.9
+    PFLOP/s BF16 burst), labelled as such."""
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        with open(pk_path) as f:
+            peaks = json.load(f)
+        if "hbm_gbs" in peaks and "bf16_tflops" in peaks:
+            return peaks, "of measured (MEASURED_PEAKS.json)"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "of fallback (no MEASURED_PEAKS.json)"
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -237,7 +251,11 @@ def run_gpu(args, rank, world):
     L.gb300_prof_enable(0)
     breakdown = read_prof(1)
     L.gb300_prof_reset()
-    dom_name = max(breakdown, key=lambda k: breakdown[k]["ms_per_step"]) if breakdown else None
+    # the roofline is reported for the BF16x3 trailing update, the dominant
+    # arithmetic kernel; the class that takes most device time (the panel
+    # on the look-ahead stream, latency-bound) is named beside it
+    top_class = max(breakdown, key=lambda k: breakdown[k]["ms_per_step"]) if breakdown else None
+    dom_name = "gemm_bf16x3" if "gemm_bf16x3" in breakdown else top_class
 
     if world > 1:
         torch.distributed.barrier()
@@ -276,14 +294,13 @@ def run_gpu(args, rank, world):
     bwd, scaled = backward_errors(A, X, B, n)
     fwd = ((X - xt).abs().max() / xt.abs().max()).item()
 
-    peaks = {}
-    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk_path):
-        with open(pk_path) as f:
-            peaks = json.load(f)
+    peaks, peak_label = load_peaks()
     L.gb300_probe_peak.restype = ctypes.c_double
     dfma_peak = L.gb300_probe_peak(0)
     ffma_peak = L.gb300_probe_peak(1)
+    # FP64 tensor-core (DMMA) throughput beside DFMA: the FP64 update runs on
+    # whichever of the two is faster on this part
+    dmma_peaks = {"m8n8k4": L.gb300_probe_peak(2), "m16n8k16": L.gb300_probe_peak(3)}
 
     # dominant kernel of the step and its roofline
     dom = (dom_name, timed.get(dom_name, breakdown.get(dom_name))) if dom_name else (None, None)
@@ -296,8 +313,8 @@ def run_gpu(args, rank, world):
             # C read+written, 192 flop/B, below the BF16/HBM ridge (~286
             # flop/B), so the update is HBM-bound; the tensor fraction is
             # reported beside it.
-            tpeak = float(peaks.get("bf16_tflops", 1900.0))
-            hbm = float(peaks.get("hbm_gbs", 6800.0))
+            tpeak = float(peaks["bf16_tflops"])
+            hbm = float(peaks["hbm_gbs"])
             secs = d["ms_per_step"] * 1e-3
             tens = 3.0 * d["flops"] / secs / 1e12
             intensity = 3.0 * d["flops"] / d["bytes"]
@@ -305,11 +322,11 @@ def run_gpu(args, rank, world):
             if intensity < ridge:
                 achieved = d["bytes"] / secs / 1e9
                 roof = {"bound": "hbm", "kernel": nm, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                        "frac": achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured"}
+                        "frac": achieved / hbm, "peak_source": f"hbm_gbs, {peak_label}"}
             else:
                 achieved = tens
                 roof = {"bound": "tensor", "kernel": nm, "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
-                        "frac": achieved / tpeak, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst), of measured"}
+                        "frac": achieved / tpeak, "peak_source": f"bf16_tflops (burst), {peak_label}"}
             roof.update({"work": "per trailing update: 4*(M*K + K*N + 2*M*N) bytes (fp32 A, B read; C read "
                                  "and written), 3 BF16 products x 2*M*N*K flop",
                          "intensity_flop_per_byte": intensity, "ridge_flop_per_byte": ridge,
@@ -321,10 +338,10 @@ def run_gpu(args, rank, world):
                     "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                     "peak_source": "gb300_probe_peak FMA loop measured in this run"}
         else:
-            hbm = float(peaks.get("hbm_gbs", 6800.0))
+            hbm = float(peaks["hbm_gbs"])
             achieved = d["bytes"] / (d["ms_per_step"] * 1e-3) / 1e9
             roof = {"bound": "hbm", "kernel": nm, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                    "frac": achieved / hbm, "peak_source": "MEASURED_PEAKS.json hbm_gbs, of measured"}
+                    "frac": achieved / hbm, "peak_source": f"hbm_gbs, {peak_label}"}
         roof["per_launch_ms"] = per_launch_ms
         roof["traffic"] = None
         if nm in TRAFFIC_RATIO and d["bytes"]:
@@ -351,8 +368,12 @@ def run_gpu(args, rank, world):
         "kernel_ms_per_step": {k: v["ms_per_step"] for k, v in breakdown.items()},
         "kernel_launches_per_step": {k: v["launches_per_step"] for k, v in breakdown.items()},
         "roofline": roof, "gpu_launches": launches,
+        "top_device_time_class": top_class,
+        "panel_us_per_column": (breakdown["panel"]["ms_per_step"] * 1e3 / n) if "panel" in breakdown else None,
         "clocks": clk, "peaks_measured": {"dfma_tflops": dfma_peak, "ffma_tflops": ffma_peak,
-                                          "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops")},
+                                          "dmma_tflops": dmma_peaks,
+                                          "hbm_gbs": peaks.get("hbm_gbs"), "bf16_tflops": peaks.get("bf16_tflops"),
+                                          "hbm_and_bf16_source": peak_label},
     }
 
     if not args.no_e2e:
@@ -396,6 +417,19 @@ def run_gpu(args, rank, world):
             split[nm + "_gbs"] = by.value / max(t_ms.value * 1e-3, 1e-12) / 1e9
         split["total_s"] = t_split
         split["device_and_host_rest_s"] = t_split - split["h2d_s"] - split["d2h_s"]
+        # the host->device rate of the same pinned bytes by a plain copy, three
+        # times: the link's rate at the moment, which varies between calls
+        rates = []
+        dst = torch.empty_like(M)
+        for _ in range(3):
+            c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            c0.record(stream)
+            dst.copy_(hA, non_blocking=True)
+            c1.record(stream)
+            torch.cuda.synchronize()
+            rates.append(8.0 * n * n / (c0.elapsed_time(c1) * 1e-3) / 1e9)
+        del dst
+        split["plain_copy_rates_gbs"] = rates
         L.gb300_prof_reset()
         L.gb300_prof_mask(0xFFFFFFFF)
         result["e2e"] = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
@@ -468,14 +502,24 @@ def run_gpu(args, rank, world):
             torch.cuda.empty_cache()
             M, A, B, xt = make_system(n, kap, args.seed, nrhs, dev)
             per[f"{kap:g}"] = solve_once_both(L, g, M, A, B, xt, n, nrhs, ipiv, dev, stream, sp)
+            if per[f"{kap:g}"]["iter"] > 0 and not per[f"{kap:g}"]["forward_error_vs_x_true"] < 1.0:
+                # the refinement overflowed and DSGESV's stopping test passed
+                # the NaN residual (SRC/dsgesv.f:384-389); the same system with
+                # the library's NaN guard, which sends it to the FP64 solve
+                old_guard = g.set_option("ir_nan_guard", 1)
+                try:
+                    per[f"{kap:g}"]["with_ir_nan_guard"] = solve_once_both(L, g, M, A, B, xt, n, nrhs, ipiv, dev,
+                                                                           stream, sp, fp64=False)
+                finally:
+                    g.set_option("ir_nan_guard", old_guard)
         result["per_kappa"] = per
     return result
 
 
-def solve_once_both(L, g, M, A, B, xt, n, nrhs, ipiv, dev, stream, sp):
-    """One mixed DSGESV and one plain FP64 DGESV of the same system, each on
-    its own copy of A, timed with CUDA events on the launching stream, with
-    their accuracy measures."""
+def solve_once_both(L, g, M, A, B, xt, n, nrhs, ipiv, dev, stream, sp, fp64=True):
+    """One mixed DSGESV and (fp64=True) one plain FP64 DGESV of the same
+    system, each on its own copy of A, timed with CUDA events on the
+    launching stream, with their accuracy measures."""
     import torch
     it, info = ctypes.c_int(0), ctypes.c_int(0)
     X = torch.empty((nrhs, n), dtype=torch.float64, device=dev).t()
@@ -491,6 +535,14 @@ def solve_once_both(L, g, M, A, B, xt, n, nrhs, ipiv, dev, stream, sp):
     t_mixed = e0.elapsed_time(e1) * 1e-3
     iter_mixed, info_mixed = it.value, info.value
     bw, sc = backward_errors(A, X, B, n)
+    if not fp64:
+        out = {"mixed_seconds": t_mixed, "status": rc, "iter": iter_mixed, "info": info_mixed,
+               "backward_error_dget08": bw, "scaled_residual": sc,
+               "forward_error_vs_x_true": ((X - xt).abs().max() / xt.abs().max()).item(),
+               "dsgesv_stopping_test_met": bool(bw < n ** 0.5)}
+        del Aw, X
+        torch.cuda.empty_cache()
+        return out
     Aw.copy_(M)
     Xd = torch.empty((nrhs, n), dtype=torch.float64, device=dev).t()
     Xd.copy_(B)
@@ -614,11 +666,10 @@ def run_batched(args, rank=0, world=1):
         torch.distributed.all_reduce(red, op=torch.distributed.ReduceOp.MAX)
         torch.distributed.all_reduce(tot, op=torch.distributed.ReduceOp.SUM)
         ms, flops, bytes_, info_nonzero = float(red[0]), float(tot[1]), float(tot[2]), int(tot[3])
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peaks, peak_label = load_peaks()
     L.gb300_probe_peak.restype = ctypes.c_double
     fma_peak = L.gb300_probe_peak(0 if args.dtype == "d" else 1)
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    hbm = float(peaks["hbm_gbs"])
     # residual spot check of a few systems
     hA, hB = A0.cpu().numpy(), B0.cpu().numpy()
     X = B.cpu().numpy()
@@ -704,9 +755,8 @@ def run_adjoint(args):
         if cnt.value:
             parts[nm] = {"ms_per_step": t_ms.value / args.steps, "gbs": by.value / max(t_ms.value, 1e-9) / 1e6}
     L.gb300_prof_reset()
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    peaks, peak_label = load_peaks()
+    hbm = float(peaks["hbm_gbs"])
     bytes_ = batch * (8.0 * n * n * 2 + 8.0 * n * nrhs * 4)     # LU read by the solves + gA written + vectors
     # both halves do 2*n^2*nrhs flop per system (the two triangular solves
     # together, and gA = -gB X^T): 2 flop per byte of LU read or gA written,

@@ -455,7 +455,17 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * FP32 factorization factors block column k+1 on a second, high-priority
  * stream while the trailing update of block column k runs; 0: one stream),
  * "trsv_inv" (1: DSGESV's FP32 correction solves apply each 64 x 64
- * diagonal block as its inverse, formed in the solve; 0: substitution).
+ * diagonal block as its inverse, formed in the solve; 0: substitution),
+ * "gemm_ws" (1: the BF16x3 trailing update runs as a warp-specialised
+ * multi-tile kernel; 0: one 128 x 128 tile per CTA), "gemm_tiles" (tiles
+ * each CTA of the warp-specialised update takes, 4 by default; 0: one CTA
+ * per SM),
+ * "ir_nan_guard" (0, the default, keeps DSGESV's stopping test exactly:
+ * a residual of NaNs passes it, because RNRM.GT.XNRM*CTE is false for a
+ * NaN (SRC/dsgesv.f:384-389), so a refinement that overflowed returns its
+ * iterate with ITER > 0; 1 treats a NaN or infinity in the iterate or the
+ * residual as DLAG2S treats an overflow: ITER = -2 and the FP64
+ * factorization).
  * Returns the previous value, or -1 for an unknown name.  Not thread-safe:
  * set at start-up. */
 int gb300_set_option(const char* name, int value);

@@ -92,7 +92,10 @@ def _pre(dtype):
 # ------------------------------------------------------------------ options
 def set_option(name, value):
     """Library options: 'exact' (0/1), 'nb64', 'nb32', 'mixed' (0 BF16x3
-    tensor cores, 1 FP32 CUDA cores), 'sgetrf'.  Returns the old value."""
+    tensor cores, 1 FP32 CUDA cores), 'sgetrf', 'lookahead', 'gemm_ws' (1
+    warp-specialised multi-tile BF16x3 update, 0 one tile per CTA),
+    'gemm_tiles' (tiles per CTA of that update, 0: one CTA per SM) and the
+    others gb300_set_option names.  Returns the old value."""
     return lib().gb300_set_option(name.encode(), int(value))
 
 

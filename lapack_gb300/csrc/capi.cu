@@ -81,6 +81,55 @@ int d2h(T* h, int ldh, const T* d, int ldd, int m, int n, cudaStream_t s) {
 
 inline int ld_dev(int m) { return std::max(1, (m + 31) / 32 * 32); }
 
+// Device copies of the operands of the host-pointer solve routines live in
+// one buffer per host thread and device, grown on demand and kept for the
+// next call (freed when the thread exits).  Keeping it matters beyond the
+// cost of allocating: a host->device copy into device memory the GPU has
+// not touched before runs several times slower than into memory it has.
+struct HostWorkspace {
+  char* p[64] = {};
+  size_t bytes[64] = {};
+  ~HostWorkspace() {
+    for (int d = 0; d < 64; ++d)
+      if (p[d] && cudaSetDevice(d) == cudaSuccess) cudaFree(p[d]);
+  }
+};
+
+char* host_workspace(size_t bytes, cudaStream_t s) {
+  thread_local HostWorkspace w;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (w.bytes[dev] < bytes) {
+    if (w.p[dev]) {
+      cudaStreamSynchronize(s);
+      cudaFree(w.p[dev]);
+      w.p[dev] = nullptr;
+      w.bytes[dev] = 0;
+    }
+    void* q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    w.p[dev] = static_cast<char*>(q);
+    w.bytes[dev] = bytes;
+  }
+  return w.p[dev];
+}
+
+// Consecutive 256-byte aligned pieces of one buffer.
+struct Carve {
+  size_t off = 0;
+  char* base = nullptr;
+  size_t add(size_t b) {
+    size_t o = off;
+    off += (b + 255) / 256 * 256;
+    return o;
+  }
+  template <typename T>
+  T* at(size_t o) const { return reinterpret_cast<T*>(base + o); }
+};
+
 // ------------------------------------------------------------ GETRF
 template <typename T>
 void getrf_host(const char* name, const lapack_int* m, const lapack_int* n, T* a, const lapack_int* lda,
@@ -93,13 +142,17 @@ void getrf_host(const char* name, const lapack_int* m, const lapack_int* n, T* a
   if (*m == 0 || *n == 0) return;
   cudaStream_t s = thread_stream();
   const int M = *m, N = *n, ld = ld_dev(M), mn = std::min(M, N);
-  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dP(sizeof(int) * (mn + 1), s);
-  if (!dA.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
-  int* dInfo = dP.as<int>() + mn;
-  int rc = h2d(dA.as<T>(), ld, a, *lda, M, N, s);
-  if (!rc) rc = gb::getrf_dev<T>(M, N, dA.as<T>(), ld, dP.as<int>(), dInfo, s, gemm_mode, nb);
-  if (!rc) rc = d2h(a, *lda, dA.as<T>(), ld, M, N, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.as<int>(), sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
+  Carve cv;
+  const size_t oA = cv.add(sizeof(T) * (size_t)ld * N), oP = cv.add(sizeof(int) * (mn + 1));
+  cv.base = host_workspace(cv.off, s);
+  if (!cv.base) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  T* dA = cv.at<T>(oA);
+  int* dP = cv.at<int>(oP);
+  int* dInfo = dP + mn;
+  int rc = h2d(dA, ld, a, *lda, M, N, s);
+  if (!rc) rc = gb::getrf_dev<T>(M, N, dA, ld, dP, dInfo, s, gemm_mode, nb);
+  if (!rc) rc = d2h(a, *lda, dA, ld, M, N, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP, sizeof(int) * mn, cudaMemcpyDeviceToHost, s);
   int hinfo = 0;
   if (!rc) rc = (int)cudaMemcpyAsync(&hinfo, dInfo, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (!rc) rc = finish(s);
@@ -122,13 +175,19 @@ void getrs_host(const char* name, const char* trans, const lapack_int* n, const 
   if (*n == 0 || *nrhs == 0) return;
   cudaStream_t s = thread_stream();
   const int N = *n, R = *nrhs, ld = ld_dev(N);
-  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dB(sizeof(T) * (size_t)ld * R, s), dP(sizeof(int) * N, s);
-  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
-  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
-  if (!rc) rc = h2d(dB.as<T>(), ld, b, *ldb, N, R, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(dP.p, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
-  if (!rc) rc = gb::getrs_dev<T>(notran ? 'N' : 'T', N, R, dA.as<T>(), ld, dP.as<int>(), nullptr, dB.as<T>(), ld, s);
-  if (!rc) rc = d2h(b, *ldb, dB.as<T>(), ld, N, R, s);
+  Carve cv;
+  const size_t oA = cv.add(sizeof(T) * (size_t)ld * N), oB = cv.add(sizeof(T) * (size_t)ld * R),
+               oP = cv.add(sizeof(int) * N);
+  cv.base = host_workspace(cv.off, s);
+  if (!cv.base) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  T* dA = cv.at<T>(oA);
+  T* dB = cv.at<T>(oB);
+  int* dP = cv.at<int>(oP);
+  int rc = h2d(dA, ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB, ld, b, *ldb, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(dP, ipiv, sizeof(int) * N, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = gb::getrs_dev<T>(notran ? 'N' : 'T', N, R, dA, ld, dP, nullptr, dB, ld, s);
+  if (!rc) rc = d2h(b, *ldb, dB, ld, N, R, s);
   if (!rc) rc = finish(s);
   if (rc) device_failure(name, rc, info);
 }
@@ -146,21 +205,26 @@ void gesv_host(const char* name, const lapack_int* n, const lapack_int* nrhs, T*
   if (*n == 0) return;
   cudaStream_t s = thread_stream();
   const int N = *n, R = *nrhs, ld = ld_dev(N);
-  DevScratch dA(sizeof(T) * (size_t)ld * N, s), dB(sizeof(T) * (size_t)ld * std::max(R, 1), s),
-      dP(sizeof(int) * (N + 1), s);
-  if (!dA.p || !dB.p || !dP.p) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
-  int* dInfo = dP.as<int>() + N;
+  Carve cv;
+  const size_t oA = cv.add(sizeof(T) * (size_t)ld * N), oB = cv.add(sizeof(T) * (size_t)ld * std::max(R, 1)),
+               oP = cv.add(sizeof(int) * (N + 1));
+  cv.base = host_workspace(cv.off, s);
+  if (!cv.base) { device_failure(name, (int)cudaErrorMemoryAllocation, info); return; }
+  T* dA = cv.at<T>(oA);
+  T* dB = cv.at<T>(oB);
+  int* dP = cv.at<int>(oP);
+  int* dInfo = dP + N;
   int hinfo = 0;
-  int rc = h2d(dA.as<T>(), ld, a, *lda, N, N, s);
-  if (!rc) rc = h2d(dB.as<T>(), ld, b, *ldb, N, R, s);
-  if (!rc) rc = gb::getrf_dev<T>(N, N, dA.as<T>(), ld, dP.as<int>(), dInfo, s, gemm_mode, nb);
+  int rc = h2d(dA, ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB, ld, b, *ldb, N, R, s);
+  if (!rc) rc = gb::getrf_dev<T>(N, N, dA, ld, dP, dInfo, s, gemm_mode, nb);
   if (!rc) rc = (int)cudaMemcpyAsync(&hinfo, dInfo, sizeof(int), cudaMemcpyDeviceToHost, s);
   if (!rc) rc = finish(s);
   if (!rc && hinfo == 0 && R > 0)   // SRC/dgesv.f:166: solve only for a nonsingular U
-    rc = gb::getrs_dev<T>('N', N, R, dA.as<T>(), ld, dP.as<int>(), nullptr, dB.as<T>(), ld, s);
-  if (!rc) rc = d2h(a, *lda, dA.as<T>(), ld, N, N, s);
-  if (!rc && hinfo == 0) rc = d2h(b, *ldb, dB.as<T>(), ld, N, R, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+    rc = gb::getrs_dev<T>('N', N, R, dA, ld, dP, nullptr, dB, ld, s);
+  if (!rc) rc = d2h(a, *lda, dA, ld, N, N, s);
+  if (!rc && hinfo == 0) rc = d2h(b, *ldb, dB, ld, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
   if (!rc) rc = finish(s);
   if (rc) { device_failure(name, rc, info); return; }
   *info = hinfo;
@@ -432,22 +496,27 @@ void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapac
   if (*n == 0) return;
   cudaStream_t s = thread_stream();
   const int N = *n, R = *nrhs, ld = ld_dev(N);
-  DevScratch dA(sizeof(double) * (size_t)ld * N, s), dB(sizeof(double) * (size_t)ld * std::max(R, 1), s),
-      dX(sizeof(double) * (size_t)ld * std::max(R, 1), s), dP(sizeof(int) * N, s);
-  if (!dA.p || !dB.p || !dX.p || !dP.p) { device_failure("DSGESV", (int)cudaErrorMemoryAllocation, info); return; }
+  Carve cv;
+  const size_t oA = cv.add(sizeof(double) * (size_t)ld * N), oB = cv.add(sizeof(double) * (size_t)ld * std::max(R, 1)),
+               oX = cv.add(sizeof(double) * (size_t)ld * std::max(R, 1)), oP = cv.add(sizeof(int) * N);
+  cv.base = host_workspace(cv.off, s);
+  if (!cv.base) { device_failure("DSGESV", (int)cudaErrorMemoryAllocation, info); return; }
+  double* dA = cv.at<double>(oA);
+  double* dB = cv.at<double>(oB);
+  double* dX = cv.at<double>(oX);
+  int* dP = cv.at<int>(oP);
   int it = 0, inf = 0;
   gb::prof_begin(gb::kProfCopyH2D, s);
-  int rc = h2d(dA.as<double>(), ld, a, *lda, N, N, s);
-  if (!rc) rc = h2d(dB.as<double>(), ld, b, *ldb, N, R, s);
+  int rc = h2d(dA, ld, a, *lda, N, N, s);
+  if (!rc) rc = h2d(dB, ld, b, *ldb, N, R, s);
   gb::prof_end(gb::kProfCopyH2D, s, 0.0, 8.0 * (double)N * (N + R));
-  if (!rc) rc = gb::dsgesv_dev(N, R, dA.as<double>(), ld, dP.as<int>(), dB.as<double>(), ld, dX.as<double>(), ld,
-                               &it, &inf, s);
+  if (!rc) rc = gb::dsgesv_dev(N, R, dA, ld, dP, dB, ld, dX, ld, &it, &inf, s);
   if (!rc) rc = finish(s);
   // A is returned unchanged when ITER >= 0 and holds the FP64 LU otherwise
   gb::prof_begin(gb::kProfCopyD2H, s);
-  if (!rc && it < 0) rc = d2h(a, *lda, dA.as<double>(), ld, N, N, s);
-  if (!rc && inf == 0) rc = d2h(x, *ldx, dX.as<double>(), ld, N, R, s);
-  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP.p, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
+  if (!rc && it < 0) rc = d2h(a, *lda, dA, ld, N, N, s);
+  if (!rc && inf == 0) rc = d2h(x, *ldx, dX, ld, N, R, s);
+  if (!rc) rc = (int)cudaMemcpyAsync(ipiv, dP, sizeof(int) * N, cudaMemcpyDeviceToHost, s);
   gb::prof_end(gb::kProfCopyD2H, s, 0.0, 8.0 * (double)N * ((it < 0 ? N : 0) + R) + 4.0 * N);
   if (!rc) rc = finish(s);
   if (rc) { device_failure("DSGESV", rc, info); return; }
@@ -1220,6 +1289,9 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "cluster_panel")) { old = o.cluster_panel; o.cluster_panel = value; }
   else if (!strcmp(name, "lookahead")) { old = o.lookahead; o.lookahead = value; }
   else if (!strcmp(name, "trsv_inv")) { old = o.trsv_inv; o.trsv_inv = value; }
+  else if (!strcmp(name, "gemm_ws")) { old = o.gemm_ws; o.gemm_ws = value; }
+  else if (!strcmp(name, "gemm_tiles")) { old = o.gemm_tiles; o.gemm_tiles = std::max(0, value); }
+  else if (!strcmp(name, "ir_nan_guard")) { old = o.ir_nan_guard; o.ir_nan_guard = value != 0; }
   else return -1;
   return old;
 }
@@ -1235,6 +1307,9 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "cluster_panel")) return o.cluster_panel;
   if (!strcmp(name, "lookahead")) return o.lookahead;
   if (!strcmp(name, "trsv_inv")) return o.trsv_inv;
+  if (!strcmp(name, "gemm_ws")) return o.gemm_ws;
+  if (!strcmp(name, "gemm_tiles")) return o.gemm_tiles;
+  if (!strcmp(name, "ir_nan_guard")) return o.ir_nan_guard;
   return -1;
 }
 int gb300_status(int clear) {

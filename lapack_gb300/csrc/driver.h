@@ -22,6 +22,9 @@ struct Options {
   int cluster_panel = 2;          // FP32 leaves on one thread-block cluster: 2 shared-memory kernel, 1 register kernel, 0 off
   int lookahead = 1;              // FP32 cluster path: factor the next block column beside the trailing update
   int trsv_inv = 1;               // DSGESV's FP32 solves: diagonal blocks applied as their inverses
+  int gemm_ws = 1;                // BF16x3 update: 1 warp-specialised multi-tile kernel, 0 one tile per CTA
+  int gemm_tiles = 4;             // tiles per CTA of the warp-specialised update (0: one CTA per SM)
+  int ir_nan_guard = 0;           // DSGESV: a non-finite iterate or residual ends the refinement (ITER = -2)
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 

@@ -29,6 +29,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <mutex>
 
 namespace gb {
@@ -240,6 +241,304 @@ gemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_const
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-specialised form of the same update, several tiles per CTA.
+//
+// One CTA per SM (224 KB of shared memory) walks tiles t = blockIdx.x +
+// i * gridDim.x.  Roles:
+//   warp 0  operand producer: TMA loads of ah, al, bh, bl per 64-wide K block
+//           into a two-stage ring (64 KB per stage);
+//   warp 1  MMA issuer: twelve tcgen05.mma per K block into one of two
+//           128-column TMEM accumulators (tile i uses accumulator i & 1), so
+//           the next tile's products run while the epilogue drains this one;
+//   warp 6  C producer: TMA loads of the C tile in two 128 x 64 halves into a
+//           ring of three 32 KB buffers, issued as soon as a buffer is free,
+//           so C streams from HBM ahead of the epilogue;
+//   warps 2-5 epilogue: warp w owns TMEM lanes 32(w%4)..+31 (tile rows) and
+//           the matching 32-row quadrant of each C buffer; it reads the
+//           accumulator with tcgen05.ld, forms C - acc in shared memory and
+//           writes its quadrant back with a TMA store.
+// Every mbarrier wait is bounded.  A wait that runs out records the status
+// and raises a CTA-wide abort flag; every role then leaves its loop, the
+// producers wait (bounded) for their copies in flight, and TMEM is freed.
+constexpr int kWsStages = 2;
+constexpr int kWsCBufs = 3;
+constexpr int kWsCHalfCols = 64;
+constexpr int kWsCHalfBytes = kTcBM * kWsCHalfCols * 4;    // 32 KB
+constexpr int kWsCQuadBytes = 32 * kWsCHalfCols * 4;        // 8 KB: 32 rows x 64 columns
+constexpr int kWsThreads = 224;
+constexpr int kWsSmem = kWsStages * kStageBytes + kWsCBufs * kWsCHalfBytes + 1024;
+constexpr uint32_t kWsTmemCols = 256;
+
+struct WsBars {
+  uint64_t full[kWsStages], empty[kWsStages];
+  uint64_t acc_full[2], acc_empty[2];
+  uint64_t c_full[kWsCBufs], c_empty[kWsCBufs];
+  uint64_t mma_done;
+};
+
+// Bounded wait that also gives up when another role has raised the abort
+// flag; returns false then (and sets the flag itself on a timeout).
+__device__ __forceinline__ bool ws_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag, int* status) {
+  const uint32_t a = smem_u32(bar);
+  for (unsigned spins = 0; spins < kSpinLimit; ++spins) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if ((spins & 255u) == 255u && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  atomicCAS(status, kStatusOk, kStatusFlagTimeout);
+  return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
+      " [%0], [%1, {%2, %3}], [%4], %5;"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d_hint(const CUtensorMap* map, int x, int y, const void* src,
+                                                  uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group.L2::cache_hint [%0, {%1, %2}], [%3], %4;"
+      ::"l"(map), "r"(x), "r"(y), "r"(smem_u32(src)), "l"(policy)
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kWsThreads, 1)
+gemm_bf16x3_ws_kernel(const __grid_constant__ CUtensorMap tm_ah, const __grid_constant__ CUtensorMap tm_al,
+                      const __grid_constant__ CUtensorMap tm_bh, const __grid_constant__ CUtensorMap tm_bl,
+                      const __grid_constant__ CUtensorMap tm_c, int M, int N, int tiles_m, int ntiles,
+                      int tiles_per_cta, int nkb, int* __restrict__ status, int overwrite) {
+  extern __shared__ unsigned char ws_smem_raw[];
+  __shared__ WsBars bars;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int abort_s;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t raw = smem_u32(ws_smem_raw);
+  unsigned char* base = ws_smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  unsigned char* stage0 = base;                                          // kWsStages x [ah | al | bh | bl]
+  float* cbuf0 = reinterpret_cast<float*>(base + kWsStages * kStageBytes);  // kWsCBufs x 4 quadrants
+
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(kWsTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < kWsStages; ++i) {
+      mbar_init(&bars.full[i], 1);
+      mbar_init(&bars.empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&bars.acc_full[i], 1);
+      mbar_init(&bars.acc_empty[i], 4);     // lane 0 of each epilogue warp
+    }
+    for (int i = 0; i < kWsCBufs; ++i) {
+      mbar_init(&bars.c_full[i], 1);
+      mbar_init(&bars.c_empty[i], 4);       // each epilogue warp after its store has read the buffer
+    }
+    mbar_init(&bars.mma_done, 1);
+    abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  int* st = status;
+
+  if (warp == 0) {
+    // ---------------------------------------------------- operand producer
+    if (lane == 0) {
+      uint64_t keep;
+      asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(keep));
+      uint32_t it = 0;
+      bool ok = true;
+      for (int i = 0; i < tiles_per_cta && ok; ++i) {
+        const int t = blockIdx.x + i * gridDim.x;
+        if (t >= ntiles) break;
+        const int m0 = (t % tiles_m) * kTcBM, n0 = (t / tiles_m) * kTcBN;
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = (int)(it % kWsStages);
+          const uint32_t u = it / kWsStages;
+          if (!ws_wait(&bars.empty[s], (u & 1u) ^ 1u, &abort_s, st)) { ok = false; break; }
+          unsigned char* sb = stage0 + (size_t)s * kStageBytes;
+          mbar_expect_tx(&bars.full[s], kStageBytes);
+          tma_load_2d_hint(sb, &tm_ah, kb * kTcBK, m0, &bars.full[s], keep);
+          tma_load_2d_hint(sb + kTileBytesA, &tm_al, kb * kTcBK, m0, &bars.full[s], keep);
+          tma_load_2d_hint(sb + 2 * kTileBytesA, &tm_bh, kb * kTcBK, n0, &bars.full[s], keep);
+          tma_load_2d_hint(sb + 2 * kTileBytesA + kTileBytesB, &tm_bl, kb * kTcBK, n0, &bars.full[s], keep);
+        }
+      }
+      if (!ok) {
+        // copies in flight land before the CTA may exit
+        for (uint32_t j = (it > (uint32_t)kWsStages ? it - kWsStages : 0u); j < it; ++j) {
+          volatile int never = 0;
+          ws_wait(&bars.full[j % kWsStages], (j / kWsStages) & 1u, &never, st);
+        }
+      }
+    }
+  } else if (warp == 6) {
+    // ------------------------------------------------------------ C producer
+    if (lane == 0) {
+      uint64_t stream_pol;
+      asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(stream_pol));
+      uint32_t cit = 0;
+      bool ok = true;
+      for (int i = 0; i < tiles_per_cta && ok; ++i) {
+        const int t = blockIdx.x + i * gridDim.x;
+        if (t >= ntiles) break;
+        const int m0 = (t % tiles_m) * kTcBM, n0 = (t / tiles_m) * kTcBN;
+        for (int h = 0; h < 2; ++h, ++cit) {
+          const int b = (int)(cit % kWsCBufs);
+          const uint32_t u = cit / kWsCBufs;
+          if (!ws_wait(&bars.c_empty[b], (u & 1u) ^ 1u, &abort_s, st)) { ok = false; break; }
+          if (overwrite) {
+            mbar_arrive(&bars.c_full[b]);
+          } else {
+            float* cb = cbuf0 + (size_t)b * (kWsCHalfBytes / 4);
+            mbar_expect_tx(&bars.c_full[b], kWsCHalfBytes);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              tma_load_2d_hint(cb + q * (kWsCQuadBytes / 4), &tm_c, m0 + 32 * q, n0 + h * kWsCHalfCols,
+                               &bars.c_full[b], stream_pol);
+          }
+        }
+      }
+      if (!ok && !overwrite) {
+        for (uint32_t j = (cit > (uint32_t)kWsCBufs ? cit - kWsCBufs : 0u); j < cit; ++j) {
+          volatile int never = 0;
+          ws_wait(&bars.c_full[j % kWsCBufs], (j / kWsCBufs) & 1u, &never, st);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(kTcBM, kTcBN);
+      uint32_t it = 0, tl = 0;
+      bool ok = true;
+      for (int i = 0; i < tiles_per_cta && ok; ++i, ++tl) {
+        const int t = blockIdx.x + i * gridDim.x;
+        if (t >= ntiles) break;
+        const int a = (int)(tl & 1u);
+        const uint32_t ua = tl >> 1;
+        if (!ws_wait(&bars.acc_empty[a], (ua & 1u) ^ 1u, &abort_s, st)) { ok = false; break; }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t acc = tmem + (uint32_t)(a * kTcBN);
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = (int)(it % kWsStages);
+          const uint32_t u = it / kWsStages;
+          if (!ws_wait(&bars.full[s], u & 1u, &abort_s, st)) { ok = false; break; }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sb = smem_u32(stage0 + (size_t)s * kStageBytes);
+          const uint32_t a_hi = sb, a_lo = sb + kTileBytesA, b_hi = sb + 2 * kTileBytesA,
+                         b_lo = sb + 2 * kTileBytesA + kTileBytesB;
+#pragma unroll
+          for (int kk = 0; kk < kTcBK / 16; ++kk) {
+            const uint32_t off = kk * 32;
+            const uint64_t dah = smem_desc_sw128(a_hi + off), dal = smem_desc_sw128(a_lo + off);
+            const uint64_t dbh = smem_desc_sw128(b_hi + off), dbl = smem_desc_sw128(b_lo + off);
+            const uint32_t acc0 = (kb > 0 || kk > 0) ? 1u : 0u;
+            mma_bf16(acc, dal, dbh, idesc, acc0);   // small terms first
+            mma_bf16(acc, dah, dbl, idesc, 1u);
+            mma_bf16(acc, dah, dbh, idesc, 1u);
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_u32(&bars.empty[s]))
+                       : "memory");
+        }
+        if (!ok) break;
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(&bars.acc_full[a]))
+                     : "memory");
+      }
+      // every MMA issued has completed before TMEM is freed
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(&bars.mma_done))
+                   : "memory");
+      volatile int never = 0;
+      ws_wait(&bars.mma_done, 0, &never, st);
+    }
+  } else {
+    // -------------------------------------------------------------- epilogue
+    const int q = warp & 3;                      // TMEM lane quadrant = tile rows 32q..32q+31
+    uint64_t stream_pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(stream_pol));
+    uint32_t cit = 0, tl = 0;
+    for (int i = 0; i < tiles_per_cta; ++i, ++tl) {
+      const int t = blockIdx.x + i * gridDim.x;
+      if (t >= ntiles) break;
+      const int m0 = (t % tiles_m) * kTcBM, n0 = (t / tiles_m) * kTcBN;
+      const int a = (int)(tl & 1u);
+      const uint32_t ua = tl >> 1;
+      bool ok = ws_wait(&bars.acc_full[a], ua & 1u, &abort_s, st);
+      if (!__all_sync(0xffffffffu, ok)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * kTcBN);
+      bool fail = false;
+      for (int h = 0; h < 2; ++h, ++cit) {
+        const int b = (int)(cit % kWsCBufs);
+        const uint32_t u = cit / kWsCBufs;
+        ok = ws_wait(&bars.c_full[b], u & 1u, &abort_s, st);
+        if (!__all_sync(0xffffffffu, ok)) { fail = true; break; }
+        float* cq = cbuf0 + (size_t)b * (kWsCHalfBytes / 4) + q * (kWsCQuadBytes / 4);   // [64 cols][32 rows]
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          float v[32];
+          tmem_ld_32cols(lane_base + (uint32_t)(h * kWsCHalfCols + j * 32), v);
+#pragma unroll
+          for (int c = 0; c < 32; ++c) {
+            float* p = cq + (j * 32 + c) * 32 + lane;
+            *p = overwrite ? v[c] : *p - v[c];
+          }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) {
+          // quadrants wholly outside C are not stored (the loads there only
+          // filled zeros); partial ones are clipped by the tensor map
+          if (m0 + 32 * q < M && n0 + h * kWsCHalfCols < N) {
+            tma_store_2d_hint(&tm_c, m0 + 32 * q, n0 + h * kWsCHalfCols, cq, stream_pol);
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          }
+          mbar_arrive(&bars.c_empty[b]);
+        }
+        __syncwarp();
+      }
+      if (fail) break;
+      // this warp's reads of accumulator a are complete
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&bars.acc_empty[a]);
+    }
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    __syncwarp();
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kWsTmemCols));
+  }
+}
+
 // A (M x K, column-major) -> ah/al [M][Kp] row-major bf16 (K contiguous),
 // through a 32 x 32 shared-memory transpose; zero for k >= K.
 __global__ void __launch_bounds__(256)
@@ -306,6 +605,21 @@ bool make_map(CUtensorMap* map, const void* base, int rows, int Kp, int box_rows
   return r == CUDA_SUCCESS;
 }
 
+// 2D map over a column-major fp32 matrix (rows contiguous), box 32 rows x 64
+// columns: one epilogue warp's quadrant of a C half-tile.
+bool make_map_c(CUtensorMap* map, const float* base, int M, int N, int ldc) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[2] = {(cuuint64_t)M, (cuuint64_t)N};
+  cuuint64_t strides[1] = {(cuuint64_t)ldc * 4};
+  cuuint32_t box[2] = {32u, (cuuint32_t)kWsCHalfCols};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
 }  // namespace
 
 
@@ -334,14 +648,39 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
   if (!make_map(&m_ah, ah, M, Kp, kTcBM) || !make_map(&m_al, al, M, Kp, kTcBM) ||
       !make_map(&m_bh, bh, N, Kp, kTcBN) || !make_map(&m_bl, bl, N, Kp, kTcBN))
     return (int)cudaErrorInvalidValue;
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-    attr = true;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  static bool attr[64] = {false};
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+    GB_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16x3_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWsSmem));
+    attr[dev] = true;
   }
-  dim3 grid((M + kTcBM - 1) / kTcBM, (N + kTcBN - 1) / kTcBN);
-  GB_LAUNCH(gemm_bf16x3_kernel<<<grid, kTcThreads, kTcSmem, s>>>(m_ah, m_al, m_bh, m_bl, C, ldc, M, N, Kp / kTcBK,
-                                                                 device_status_word(), overwrite ? 1 : 0));
+  const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + kTcBN - 1) / kTcBN;
+  // the warp-specialised kernel stores C by TMA: C and its column stride
+  // must be 16-byte aligned, and so must the end of each column (a TMA
+  // store clips the box at the matrix edge in 16-byte units: with M not a
+  // multiple of 4 it would also write the rows after M in the last unit)
+  CUtensorMap m_c;
+  const bool use_ws = options().gemm_ws != 0 && ((uintptr_t)C % 16) == 0 && ((size_t)ldc * 4) % 16 == 0 &&
+                      M % 4 == 0 && make_map_c(&m_c, C, M, N, ldc);
+  if (use_ws) {
+    const int ntiles = tiles_m * tiles_n;
+    int tpc = options().gemm_tiles, grid;
+    if (tpc <= 0) {
+      grid = std::min(ntiles, device_sm_count());
+      tpc = (ntiles + grid - 1) / grid;
+    } else {
+      grid = (ntiles + tpc - 1) / tpc;
+    }
+    GB_LAUNCH(gemm_bf16x3_ws_kernel<<<grid, kWsThreads, kWsSmem, s>>>(m_ah, m_al, m_bh, m_bl, m_c, M, N, tiles_m,
+                                                                      ntiles, tpc, Kp / kTcBK, device_status_word(),
+                                                                      overwrite ? 1 : 0));
+  } else {
+    dim3 grid(tiles_m, tiles_n);
+    GB_LAUNCH(gemm_bf16x3_kernel<<<grid, kTcThreads, kTcSmem, s>>>(m_ah, m_al, m_bh, m_bl, C, ldc, M, N, Kp / kTcBK,
+                                                                   device_status_word(), overwrite ? 1 : 0));
+  }
   prof_end(kProfGemmBf16x3, s, 2.0 * M * N * (double)K,
            4.0 * ((double)M * K + (double)K * N + (overwrite ? 1.0 : 2.0) * M * N));
   return (int)cudaGetLastError();

@@ -37,6 +37,9 @@ Options& options() {
     x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
     x.lookahead = env_int("LAPACK_GB300_LOOKAHEAD", 1);
     x.trsv_inv = env_int("LAPACK_GB300_TRSV_INV", 1);
+    x.gemm_ws = env_int("LAPACK_GB300_GEMM_WS", 1);
+    x.gemm_tiles = std::max(0, env_int("LAPACK_GB300_GEMM_TILES", 4));
+    x.ir_nan_guard = env_int("LAPACK_GB300_IR_NAN_GUARD", 0);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;

@@ -211,9 +211,13 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s, opt.trsv_inv != 0))) return rc;
   GB_LAUNCH(slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
   if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
-  GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
+  // the NaN guard (option ir_nan_guard) reports a non-finite X or R in
+  // flags[0], the overflow flag, so it ends the refinement as DLAG2S would
+  GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr,
+                                                 opt.ir_nan_guard ? flags : nullptr));
   GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
   GB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (hflags[0]) { *iter = -2; goto fallback; }
   if (hflags[1] == 0) { *iter = 0; return 0; }
   for (int it = 1; it <= itermax; ++it) {
     GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 2, s));
@@ -221,7 +225,8 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
     if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s, opt.trsv_inv != 0))) return rc;
     GB_LAUNCH(lag2d_axpy_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));
     if ((rc = residual(n, nrhs, dA, lda, dX, ldx, dB, ldb, R, n, s))) return rc;
-    GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr));
+    GB_LAUNCH(ir_check_kernel<<<nrhs, 256, 0, s>>>(dX, ldx, R, n, n, anrm, flags + 1, nullptr,
+                                                   opt.ir_nan_guard ? flags : nullptr));
     GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
     if (hflags[0]) { *iter = -2; goto fallback; }

@@ -513,19 +513,26 @@ __global__ void residual_reduce_kernel(const double* __restrict__ partial, int n
 // Convergence test of SRC/dsgesv.f:337-342 for every right-hand side:
 // XNRM = |X(IDAMAX(X(:,j)),j)|, RNRM likewise, not converged when
 // RNRM > XNRM*CTE with CTE = ||A||_inf * eps * sqrt(n).  One CTA per
-// right-hand side; `notconv` counts the failing ones.
+// right-hand side; `notconv` counts the failing ones.  With `nonfinite`
+// (the library's NaN guard, off by default) a NaN or infinity in X or R
+// sets *nonfinite instead of letting the NaN pass the test.
 static __global__ void __launch_bounds__(256)
 ir_check_kernel(const double* __restrict__ X, int ldx, const double* __restrict__ R, int ldr, int n,
-                const double* __restrict__ anrm, int* __restrict__ notconv, double* __restrict__ norms_out) {
+                const double* __restrict__ anrm, int* __restrict__ notconv, double* __restrict__ norms_out,
+                int* __restrict__ nonfinite = nullptr) {
   __shared__ Cand<double> red[2][8];
   const int j = blockIdx.x, tid = threadIdx.x;
   Cand<double> bx{0, -1, -1}, br{0, -1, -1};
+  bool bad = false;
   for (int i = tid; i < n; i += 256) {
-    Cand<double> cx = make_cand(X[(size_t)i + (size_t)j * ldx], i, 0);
-    Cand<double> cr = make_cand(R[(size_t)i + (size_t)j * ldr], i, 0);
+    const double xv = X[(size_t)i + (size_t)j * ldx], rv = R[(size_t)i + (size_t)j * ldr];
+    Cand<double> cx = make_cand(xv, i, 0);
+    Cand<double> cr = make_cand(rv, i, 0);
     if (cand_better(cx, bx)) bx = cx;
     if (cand_better(cr, br)) br = cr;
+    bad |= !isfinite(xv) || !isfinite(rv);
   }
+  if (nonfinite && __syncthreads_or(bad) && tid == 0) *nonfinite = 1;
   bx = warp_best(bx);
   br = warp_best(br);
   if ((tid & 31) == 0) { red[0][tid >> 5] = bx; red[1][tid >> 5] = br; }
