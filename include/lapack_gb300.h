@@ -450,8 +450,11 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32
  * factorization), "sgetrf" (same choice for SGETRF itself),
  * "panel_ctas64" / "panel_ctas32" (CTAs of the grid-wide panel kernel, 0:
- * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 2
- * shared-memory kernel, 1 register kernel, 0 off), "lookahead" (1: the
+ * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 3,
+ * the default, shared-memory kernel whose per-column exchange is pushed to
+ * every CTA by remote asynchronous stores; 2 the same kernel exchanging
+ * through cluster barriers and remote loads; 1 register kernel; 0 off),
+ * "lookahead" (1: the
  * FP32 factorization factors block column k+1 on a second, high-priority
  * stream while the trailing update of block column k runs; 0: one stream),
  * "trsv_inv" (1: DSGESV's FP32 correction solves apply each 64 x 64
@@ -499,6 +502,13 @@ int gb300_prof_read(int kind, double* ms, double* flops, double* bytes, long lon
  * 1 FP32 FMA, 2 FP64 tensor core (mma.sync m8n8k4), 3 FP64 tensor core
  * (mma.sync m16n8k16); -1 for another value.  No reference counterpart. */
 double gb300_probe_peak(int which);
+/* Microseconds per iteration of the skeleton of one cluster-panel column
+ * (two CTA barriers around a cluster-wide exchange of 16-byte messages) on
+ * one cluster of `ctas` CTAs: mode 0 the pushed exchange (st.async counted
+ * on the receivers' mbarriers), 1 a cluster barrier.  Negative on an error.
+ * No reference counterpart: a measurement of the latency floor of the
+ * FP32 panel leaf. */
+double gb300_probe_cluster_exchange(int ctas, int mode, int iters);
 
 #ifdef __cplusplus
 }

@@ -10,7 +10,10 @@
 // Two steps per call:
 //  1. split kernels write ah/al and bh/bl as K-major bf16 arrays (row r holds
 //     K contiguous values, K padded with zeros to a multiple of 64);
-//  2. the MMA kernel: one CTA per 128 x 128 tile of C.  Per 64-wide K block
+//  2. an MMA kernel: by default the warp-specialised multi-tile kernel
+//     described before gemm_bf16x3_ws_kernel below; where C cannot be moved
+//     by TMA (C or its column stride not 16-byte aligned, M not a multiple
+//     of 4) the one-tile kernel: one CTA per 128 x 128 tile of C.  Per 64-wide K block
 //     one thread issues the four TMA loads (128B-swizzled tiles) on an
 //     mbarrier, then twelve tcgen05.mma (M=128, N=128, K=16, three products x
 //     four K steps) into a 128-column TMEM accumulator, and commits them to a

@@ -34,7 +34,7 @@ Options& options() {
     x.nb_f32 = std::max(1, env_int("LAPACK_GB300_NB32", 256));
     x.panel_ctas_f64 = env_int("LAPACK_GB300_PANEL_CTAS64", 0);
     x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
-    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
+    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 3);
     x.lookahead = env_int("LAPACK_GB300_LOOKAHEAD", 1);
     x.trsv_inv = env_int("LAPACK_GB300_TRSV_INV", 1);
     x.gemm_ws = env_int("LAPACK_GB300_GEMM_WS", 1);
@@ -251,7 +251,7 @@ struct ClusterCaps {
   int dyn_cap = 0;
 };
 
-template <bool EXACT>
+template <bool EXACT, bool PUSH = false>
 static ClusterCaps cluster_caps() {
   static ClusterCaps caps[64];
   static bool done[64] = {false};
@@ -259,7 +259,7 @@ static ClusterCaps cluster_caps() {
   cudaGetDevice(&dev);
   if (!done[dev]) {
     done[dev] = true;
-    auto kern = leaf_panel_cluster_kernel<EXACT, 64>;
+    auto kern = PUSH ? leaf_panel_cluster_push_kernel<EXACT, 64> : leaf_panel_cluster_kernel<EXACT, 64>;
     cudaFuncAttributes fa;
     int optin = 0;
     if (cudaFuncGetAttributes(&fa, (const void*)kern) == cudaSuccess &&
@@ -299,9 +299,12 @@ template <typename T>
 static int cluster_leaf_width(int M, int* kind) {
   *kind = 0;
   if (sizeof(T) != 4 || options().cluster_panel == 0) return 0;
-  ClusterCaps c = options().exact ? cluster_caps<true>() : cluster_caps<false>();
+  const bool push = options().cluster_panel == 3;
+  ClusterCaps c = options().exact ? (push ? cluster_caps<true, true>() : cluster_caps<true>())
+                                  : (push ? cluster_caps<false, true>() : cluster_caps<false>());
   if (!c.ok) return 0;
-  const long long R = (M + kClusterCtas - 1) / kClusterCtas;
+  long long R = (M + kClusterCtas - 1) / kClusterCtas;
+  if (push) R = leaf_push_rows((int)R);
   if (options().cluster_panel == 1) {
     if (R <= 2 * kClusterThreads) { *kind = 1; return 32; }
     if (R <= 4 * kClusterThreads) { *kind = 1; return 16; }
@@ -347,17 +350,16 @@ static int launch_leaf_cluster_reg(float* P, int lda, int M, int jb, int row0, i
   return rc;
 }
 
-template <bool EXACT, int JBT>
+template <bool EXACT, int JBT, bool PUSH>
 static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t smem, int row0, int* ipiv, int* info,
                                  PanelCtx<float>& cx, cudaStream_t s, int dyn_cap) {
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
+  auto kern = PUSH ? leaf_panel_cluster_push_kernel<EXACT, JBT> : leaf_panel_cluster_kernel<EXACT, JBT>;
   if (!attr[dev]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(leaf_panel_cluster_kernel<EXACT, JBT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     dyn_cap));
-    GB_CUDA_TRY(cudaFuncSetAttribute(leaf_panel_cluster_kernel<EXACT, JBT>,
-                                     cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap));
+    GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
     attr[dev] = true;
   }
   cudaLaunchConfig_t cfg = {};
@@ -381,27 +383,39 @@ static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t
     b0 = row0 + JB;
     b1 = cx.imm_hi;
   }
-  return (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT, JBT>, P, lda, M, JB, R, row0, ipiv, info,
-                                 cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status, a0, a1, b0, b1);
+  return (int)cudaLaunchKernelEx(&cfg, kern, P, lda, M, JB, R, row0, ipiv, info, cx.ps.pair_dst, cx.ps.pair_src,
+                                 cx.ps.pair_count, cx.status, a0, a1, b0, b1);
 }
 
-template <bool EXACT>
-static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
-                               PanelCtx<float>& cx, cudaStream_t s) {
-  ClusterCaps c = cluster_caps<EXACT>();
+template <bool EXACT, bool PUSH>
+static int launch_leaf_cluster_p(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
+                                 PanelCtx<float>& cx, cudaStream_t s) {
+  ClusterCaps c = cluster_caps<EXACT, PUSH>();
   const int R = (M + kClusterCtas - 1) / kClusterCtas;
-  size_t smem = (size_t)JB * R * 4 + (size_t)R * 4 + 16;
+  const int Rs = PUSH ? leaf_push_rows(R) : R;      // the push kernel pads its rows
+  size_t smem = (size_t)JB * Rs * 4 + (size_t)Rs * 4 + 16;
   if (!c.ok || (long long)smem > c.dyn_cap || JB > 64) return 1000 + kStatusCapacity;
   GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
   prof_begin(kProfPanel, s);
   int rc;
-  if (JB <= 8) rc = launch_leaf_cluster_w<EXACT, 8>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
-  else if (JB <= 16) rc = launch_leaf_cluster_w<EXACT, 16>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
-  else if (JB <= 32) rc = launch_leaf_cluster_w<EXACT, 32>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
-  else rc = launch_leaf_cluster_w<EXACT, 64>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  if (JB <= 8) rc = launch_leaf_cluster_w<EXACT, 8, PUSH>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else if (JB <= 16)
+    rc = launch_leaf_cluster_w<EXACT, 16, PUSH>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else if (JB <= 32)
+    rc = launch_leaf_cluster_w<EXACT, 32, PUSH>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
+  else rc = launch_leaf_cluster_w<EXACT, 64, PUSH>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
   count_launch();
   prof_end(kProfPanel, s, (double)M * JB * JB, 2.0 * 4.0 * (double)M * JB);
   return rc;
+}
+
+// The shared-memory cluster leaf: the push exchange (option cluster_panel
+// 3) or the cluster-barrier exchange (2).
+template <bool EXACT>
+static int launch_leaf_cluster(float* P, int lda, int M, int JB, int row0, int* ipiv, int* info,
+                               PanelCtx<float>& cx, cudaStream_t s) {
+  if (options().cluster_panel == 3) return launch_leaf_cluster_p<EXACT, true>(P, lda, M, JB, row0, ipiv, info, cx, s);
+  return launch_leaf_cluster_p<EXACT, false>(P, lda, M, JB, row0, ipiv, info, cx, s);
 }
 
 // Left width of a recursion split of w > leaf columns: halves above 64

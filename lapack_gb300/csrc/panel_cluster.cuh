@@ -309,6 +309,350 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Push form of the cluster leaf: the same factorization as
+// leaf_panel_cluster_kernel, with the per-column exchange done by remote
+// asynchronous stores instead of a cluster barrier and remote loads.  For
+// column k every CTA sends its candidate (key, label and the candidate row,
+// brought up to date) into a receive slot of every CTA of the cluster with
+// st.async, which also counts the bytes on the receiver's mbarrier; the CTA
+// holding row k sends that row the same way.  Each CTA then waits on its own
+// mbarrier for the G + 1 messages of the column and picks the winner from
+// the G keys itself (all CTAs reach the same winner).  One remote store
+// latency per column replaces the barrier and the two dependent remote
+// round trips.  Receive slots alternate by column parity: a CTA sends the
+// messages of column k+2 only after it has received every CTA's message of
+// column k+1, and each CTA sends that only after it has read its slots of
+// column k, so a slot is never overwritten while it is being read; each
+// CTA re-arms the barrier of a parity as soon as it has read that column.
+template <int JBT>
+struct PushMsg {
+  unsigned long long key;
+  int label;
+  int pad;
+  float row[JBT];
+};
+
+__device__ __forceinline__ uint32_t cl_smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ uint32_t cl_mapa(uint32_t addr, int rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cl_st_async_v4(uint32_t raddr, uint4 v, uint32_t rbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
+               ::"r"(raddr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w), "r"(rbar)
+               : "memory");
+}
+__device__ __forceinline__ void cl_arm(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(cl_smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// Bounded wait (acquire at cluster scope: the remote stores are released by
+// their complete-tx); returns false when it ran out.
+__device__ __forceinline__ bool cl_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = cl_smem_u32(bar);
+  for (unsigned spins = 0; spins < kSpinLimit; ++spins) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__host__ __device__ constexpr int leaf_push_rows(int R) {
+  return ((R + 3) / 4 % 2 == 0) ? (R + 3) / 4 * 4 + 4 : (R + 3) / 4 * 4;
+}
+
+template <bool EXACT, int JBT>
+__global__ void __launch_bounds__(kClusterThreads, 1)
+leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, int R, int row0, int* __restrict__ ipiv,
+                               int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
+                               int* __restrict__ pair_count, int* __restrict__ status, int swap_a0, int swap_a1,
+                               int swap_b0, int swap_b1) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  using Msg = PushMsg<JBT>;
+  constexpr int kMsgVecs = (int)sizeof(Msg) / 16;
+  static_assert(sizeof(Msg) % 16 == 0, "message of whole 16-byte vectors");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // rows of the tile padded to a multiple of four (the update works on
+  // groups of four rows with 16-byte shared-memory accesses) and to an odd
+  // number of such groups, so that the lanes of a warp reading one row
+  // across the columns spread over eight banks instead of one
+  const int Rp = leaf_push_rows(R);
+  float* tile = reinterpret_cast<float*>(smem_raw);                        // [JB][Rp]
+  int* label = reinterpret_cast<int*>(tile + (size_t)JB * Rp);             // [Rp]
+  __shared__ __align__(16) Msg recv[2][kClusterCtas];                      // candidates of column k, by parity
+  __shared__ __align__(16) Msg recv_k[2];                                  // row k of column k, by parity
+  __shared__ __align__(16) Msg out_s;                                      // this CTA's candidate message
+  __shared__ __align__(16) Msg outk_s;                                     // row k, when this CTA holds it
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ __align__(16) float urow[kLeafMax];
+  __shared__ __align__(16) float rowk_s[kLeafMax];
+  __shared__ unsigned long long wbest[kClusterThreads / 32];
+  __shared__ float pv_s;
+  __shared__ int win_label_s, rowk_label_s, prow_s;
+  __shared__ __align__(16) float uh[kDefer][kLeafMax];
+
+  const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int rbeg = b * R;
+  const int nrows = max(0, min(M, rbeg + R) - rbeg);
+  const uint32_t tx_per_col = (uint32_t)((G + 1) * sizeof(Msg));
+
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cl_smem_u32(&full[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cl_smem_u32(&full[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    cl_arm(&full[0], tx_per_col);
+    if (JB > 1) cl_arm(&full[1], tx_per_col);
+  }
+  for (int c = 0; c < JB; ++c)
+    for (int r = tid; r < nrows; r += kClusterThreads)
+      cp_async_elem(tile + c * Rp + r, P + (size_t)(rbeg + r) + (size_t)c * lda);
+  cp_async_commit();
+  for (int r = tid; r < nrows; r += kClusterThreads) label[r] = rbeg + r;
+  cp_async_wait<0>();
+  // every CTA's barriers are initialised and armed before any message flies
+  cluster.sync();
+  unsigned long long mykey = 0;
+  for (int r = tid; r < nrows; r += kClusterThreads) {
+    unsigned long long kk = pack_key(tile[r], rbeg + r, 0);
+    mykey = kk > mykey ? kk : mykey;
+  }
+  bool timed_out = false;
+
+  for (int k = 0; k < JB; ++k) {
+    const int par = k & 1;
+    const int s_slot = k % kDefer, kfirst = k - s_slot;
+    const int k_cta = k / R;
+    // 1. this CTA's best candidate for column k
+    mykey = warp_max_u64(mykey);
+    if (lane == 0) wbest[warp] = mykey;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long kk = lane < kClusterThreads / 32 ? wbest[lane] : 0ull;
+      kk = warp_max_u64(kk);
+      // 2. the message: key, label and the candidate row up to date (its
+      //    columns after k get the pending updates, in column order)
+      if (lane == 0) out_s.key = kk;
+      if (kk != 0ull) {
+        const int lr = (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) - rbeg;
+        for (int c = lane; c < JBT; c += 32) {
+          float v = 0.0f;
+          if (c < JB) {
+            v = tile[c * Rp + lr];
+            if (c > k)
+              for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * Rp + lr], uh[d][c], v);
+          }
+          out_s.row[c] = v;
+        }
+        if (lane == 0) out_s.label = label[lr];
+      }
+      const bool holds_k = (b == k_cta);
+      if (holds_k) {
+        for (int c = lane; c < JBT; c += 32) outk_s.row[c] = c < JB ? tile[c * Rp + (k - rbeg)] : 0.0f;
+        if (lane == 0) {
+          outk_s.label = label[k - rbeg];
+          outk_s.key = 0ull;
+        }
+      }
+      __syncwarp();
+      // 3. push it to every CTA of the cluster (slot b of the receiver)
+      const uint32_t bar_l = cl_smem_u32(&full[par]);
+      const uint4* src = reinterpret_cast<const uint4*>(&out_s);
+      const uint32_t slot_l = cl_smem_u32(&recv[par][b]);
+      for (int i = lane; i < G * kMsgVecs; i += 32) {
+        const int d = i / kMsgVecs, v = i - d * kMsgVecs;
+        cl_st_async_v4(cl_mapa(slot_l + 16u * v, d), src[v], cl_mapa(bar_l, d));
+      }
+      if (holds_k) {
+        const uint4* srck = reinterpret_cast<const uint4*>(&outk_s);
+        const uint32_t slotk_l = cl_smem_u32(&recv_k[par]);
+        for (int i = lane; i < G * kMsgVecs; i += 32) {
+          const int d = i / kMsgVecs, v = i - d * kMsgVecs;
+          cl_st_async_v4(cl_mapa(slotk_l + 16u * v, d), srck[v], cl_mapa(bar_l, d));
+        }
+      }
+      // 4. wait for the G candidates and row k of this column (every lane
+      //    of the warp acquires the remote stores it is about to read)
+      // After one wait has run out the CTA waits no more: it finishes the
+      // leaf on whatever it holds (the status word tells the host).
+      const bool ok = timed_out ? false : __all_sync(0xffffffffu, cl_wait(&full[par], (uint32_t)((k >> 1) & 1)));
+      if (!ok && !timed_out) {
+        timed_out = true;
+        if (lane == 0) atomicCAS(status, kStatusOk, kStatusFlagTimeout);
+      }
+      unsigned long long ck = lane < G ? recv[par][lane].key : 0ull;
+      const unsigned long long wk = warp_max_u64(ck);
+      const int wc = __ffsll(__ballot_sync(0xffffffffu, ck == wk && lane < G)) - 1;
+      const int prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
+      const Msg& wm = recv[par][wc < 0 ? 0 : wc];
+      for (int c = lane; c < JB; c += 32) urow[c] = wm.row[c];
+      const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
+      if (own_p && prow != k) {
+        for (int c = lane; c < JB; c += 32) rowk_s[c] = recv_k[par].row[c];
+      }
+      __syncwarp();
+      if (lane == 0) {
+        win_label_s = wm.label;
+        if (own_p && prow != k) rowk_label_s = recv_k[par].label;
+        prow_s = prow;
+        pv_s = urow[k];
+        if (b == 0) {
+          ipiv[k] = row0 + prow + 1;
+          if (urow[k] == 0.0f && *info == 0) *info = row0 + k + 1;
+        }
+        // the slots of this parity are read: re-arm for column k + 2
+        if (k + 2 < JB) cl_arm(&full[par], tx_per_col);
+      }
+      __syncwarp();
+      if (k >= rbeg && k < rbeg + nrows) {
+        const int lk = k - rbeg;
+        for (int c = lane; c < JB; c += 32) tile[c * Rp + lk] = urow[c];
+        if (lane == 0 && prow != k) label[lk] = win_label_s;
+      }
+      if (prow != k && own_p) {
+        const int lp = prow - rbeg;
+        for (int c = lane; c < JB; c += 32) tile[c * Rp + lp] = rowk_s[c];
+        if (lane == 0) label[lp] = rowk_label_s;
+      }
+      for (int c = lane; c < JB; c += 32) uh[s_slot][c] = urow[c];
+    }
+    __syncthreads();
+    // 5. scale column k, update column k+1 (the next candidates) and, every
+    //    kDefer columns, the later columns, in the order of
+    //    leaf_panel_cluster_kernel, on groups of four rows (one 16-byte
+    //    access per column); rows at or above k and the padding rows after
+    //    the CTA's last row keep their values
+    const float pv = pv_s;
+    const bool scale = pv != 0.0f;
+    const bool recip = fabsf(pv) >= Lim<float>::sfmin();
+    const float rp = 1.0f / pv;
+    const bool flush = s_slot == kDefer - 1;
+    float* __restrict__ tl = tile;
+    mykey = 0;
+    const int r_lo = k + 1 - rbeg;       // first local row below the diagonal
+    const int nq = (nrows + 3) >> 2;
+    for (int q = max(0, r_lo) / 4 + tid; q < nq; q += kClusterThreads) {
+      const int r0 = 4 * q;
+      bool act[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) act[e] = (r0 + e >= r_lo) && (r0 + e < nrows);
+      float4 v = *reinterpret_cast<const float4*>(tl + (size_t)k * Rp + r0);
+      float l[4] = {v.x, v.y, v.z, v.w};
+      if (scale) {
+        if (recip) {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] * rp : l[e];
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] / pv : l[e];
+        }
+        *reinterpret_cast<float4*>(tl + (size_t)k * Rp + r0) = make_float4(l[0], l[1], l[2], l[3]);
+      }
+      float ld[kDefer][4];
+#pragma unroll
+      for (int d = 0; d < kDefer; ++d) {
+        if (d < s_slot) {
+          const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(kfirst + d) * Rp + r0);
+          ld[d][0] = w.x; ld[d][1] = w.y; ld[d][2] = w.z; ld[d][3] = w.w;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) ld[d][e] = d == s_slot ? l[e] : 0.0f;
+        }
+      }
+      if (k + 1 < JB) {
+        const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(k + 1) * Rp + r0);
+        float t[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int d = 0; d < kDefer; ++d) {
+          if (d <= s_slot) {
+            const float u = uh[d][k + 1];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
+          }
+        }
+        *reinterpret_cast<float4*>(tl + (size_t)(k + 1) * Rp + r0) = make_float4(t[0], t[1], t[2], t[3]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          if (act[e]) {
+            const unsigned long long kk = pack_key(t[e], rbeg + r0 + e, k + 1);
+            mykey = kk > mykey ? kk : mykey;
+          }
+        }
+      }
+      if (flush) {
+        for (int c = k + 2; c < JB; ++c) {
+          float* pc = tl + (size_t)c * Rp + r0;
+          const float4 w = *reinterpret_cast<const float4*>(pc);
+          float t[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+          for (int d = 0; d < kDefer; ++d) {
+            const float u = uh[d][c];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
+          }
+          *reinterpret_cast<float4*>(pc) = make_float4(t[0], t[1], t[2], t[3]);
+        }
+      }
+    }
+  }
+  // the columns left over after the last flush (JB not a multiple of kDefer)
+  // were finished column by column above; no CTA leaves while another may
+  // still read it in the interchange step below
+  cluster.sync();
+  for (int c = 0; c < JB; ++c)
+    for (int r = tid; r < nrows; r += kClusterThreads) P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * Rp + r];
+  for (int r = tid; r < nrows; r += kClusterThreads) {
+    int g = rbeg + r;
+    if (g < JB) {
+      pair_dst[g] = row0 + g;
+      pair_src[g] = row0 + label[r];
+    } else if (label[r] != g) {
+      int sl = JB + atomicAdd(pair_count, 1);
+      if (sl < 2 * kLeafMax) {
+        pair_dst[sl] = row0 + g;
+        pair_src[sl] = row0 + label[r];
+      } else {
+        atomicCAS(status, kStatusOk, kStatusCapacity);
+      }
+    }
+  }
+  const int na = max(0, swap_a1 - swap_a0), nb = max(0, swap_b1 - swap_b0);
+  if (na + nb > 0) {
+    __threadfence();
+    cluster.sync();
+    float* Am = P - (size_t)row0 - (size_t)row0 * lda;
+    const int np = min(JB + *(volatile int*)pair_count, 2 * kLeafMax);
+    constexpr int kPer = (2 * kLeafMax + 31) / 32;
+    for (int idx = b * (kClusterThreads / 32) + warp; idx < na + nb; idx += G * (kClusterThreads / 32)) {
+      const int col = idx < na ? swap_a0 + idx : swap_b0 + (idx - na);
+      float* Ac = Am + (size_t)col * lda;
+      float v[kPer];
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        const int i = lane + 32 * q;
+        if (i < np) v[q] = Ac[__ldcg(pair_src + i)];
+      }
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < kPer; ++q) {
+        const int i = lane + 32 * q;
+        if (i < np) Ac[__ldcg(pair_dst + i)] = v[q];
+      }
+    }
+  }
+}
+
 }  // namespace gb
 
 namespace gb {

@@ -1,7 +1,10 @@
 // Launch counter, per-kernel-class event timing, and the FP64/FP32
 // arithmetic peak probes used as roofline denominators.
+#include "common.cuh"
 #include "prof.h"
 #include "../../include/lapack_gb300.h"
+
+#include <cooperative_groups.h>
 
 #include <atomic>
 #include <mutex>
@@ -96,6 +99,83 @@ __global__ void probe_dmma_kernel(double* out, int iters) {
   }
 }
 
+// Cluster exchange probe: every iteration is the skeleton of one column of
+// the cluster panel leaf without its arithmetic: a CTA-wide barrier, warp 0
+// of every CTA pushes a 16-byte message into every CTA of the cluster with
+// st.async (counted on the receiver's mbarrier), waits for the G messages
+// of the iteration, then a second CTA-wide barrier.  mode 1 replaces the
+// push and wait by one cluster barrier.  Waits are bounded; on a timeout
+// *bad is set and the probe stops waiting.
+__global__ void __launch_bounds__(512, 1) probe_cluster_kernel(int iters, int mode, int* bad) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ __align__(16) uint4 slots[2][16];
+  __shared__ __align__(8) uint64_t full[2];
+  __shared__ int sink;
+  const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31;
+  const uint32_t tx = (uint32_t)(G * 16);
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&full[i])));
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+                       (uint32_t)__cvta_generic_to_shared(&full[i])),
+                   "r"(tx)
+                   : "memory");
+    sink = 0;
+  }
+  cluster.sync();
+  bool timed_out = false;
+  for (int it = 0; it < iters; ++it) {
+    const int par = it & 1;
+    __syncthreads();
+    if (mode == 1) {
+      cluster.sync();
+    } else if (tid < 32) {
+      const uint32_t bar_l = (uint32_t)__cvta_generic_to_shared(&full[par]);
+      const uint32_t slot_l = (uint32_t)__cvta_generic_to_shared(&slots[par][b]);
+      if (lane < G) {
+        uint32_t ra, rb;
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(slot_l), "r"(lane));
+        asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(rb) : "r"(bar_l), "r"(lane));
+        asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v4.b32 [%0], {%1, %2, %3, %4}, [%5];"
+                     ::"r"(ra), "r"(it), "r"(b), "r"(0), "r"(0), "r"(rb)
+                     : "memory");
+      }
+      bool ok = true;
+      if (!timed_out) {
+        ok = false;
+        for (unsigned spins = 0; spins < kSpinLimit && !ok; ++spins) {
+          uint32_t done;
+          asm volatile(
+              "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+              " selp.u32 %0, 1, 0, p;\n}\n"
+              : "=r"(done)
+              : "r"(bar_l), "r"((uint32_t)((it >> 1) & 1))
+              : "memory");
+          ok = done != 0;
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok && !timed_out) {
+        timed_out = true;
+        if (lane == 0) atomicExch(bad, 1);
+      }
+      if (lane == 0) {
+        sink += (int)slots[par][(b + 1) % G].x;
+        if (it + 2 < iters)
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_l), "r"(tx) : "memory");
+      }
+    }
+    __syncthreads();
+  }
+  cluster.sync();
+  if (tid == 0 && sink == -1) atomicExch(bad, 2);
+}
+
 }  // namespace gb
 
 extern "C" {
@@ -173,6 +253,51 @@ double gb300_probe_peak(int which) {
   if (which <= 1) flops = 2.0 * 64.0 * iters * (double)blocks * threads;
   else flops = (which == 2 ? 512.0 : 4096.0) * 4.0 * iters * (double)blocks * (threads / 32);
   return flops / (best * 1e-3) / 1e12;
+}
+
+// Microseconds per iteration of the cluster exchange probe (see
+// probe_cluster_kernel): mode 0 pushed messages, 1 cluster barrier; ctas is
+// the cluster size (2 to 16).  Negative on an error or a timed-out wait.
+double gb300_probe_cluster_exchange(int ctas, int mode, int iters) {
+  if (ctas < 1 || ctas > 16 || iters < 1) return -1.0;
+  int* bad = nullptr;
+  if (cudaMalloc(&bad, sizeof(int)) != cudaSuccess) return -1.0;
+  cudaMemset(bad, 0, sizeof(int));
+  if (cudaFuncSetAttribute(gb::probe_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess) {
+    cudaFree(bad);
+    return -1.0;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = ctas;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(ctas);
+  cfg.blockDim = dim3(512);
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 1e30;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    cudaLaunchKernelEx(&cfg, gb::probe_cluster_kernel, iters, mode, bad);
+    cudaEventRecord(e1);
+    if (cudaEventSynchronize(e1) != cudaSuccess) { best = -1.0; break; }
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  int hbad = 0;
+  cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(bad);
+  if (hbad || best < 0) return -1.0;
+  return best * 1e3 / iters;
 }
 
 }  // extern "C"

@@ -87,8 +87,10 @@ def test_lookahead_dsgesv_identical(gpu):
     assert x0.tobytes() == x1.tobytes()
 
 
-@pytest.mark.parametrize("cluster_panel", [0, 1, 2])      # grid-wide leaf / register cluster leaf / shared-memory cluster leaf
-@pytest.mark.parametrize("m,n,nb", [(700, 700, 64), (1500, 1500, 256), (2100, 900, 128)])
+# grid-wide leaf / register cluster leaf / shared-memory cluster leaf (barrier exchange / pushed exchange)
+@pytest.mark.parametrize("cluster_panel", [0, 1, 2, 3])
+@pytest.mark.parametrize("m,n,nb", [(700, 700, 64), (1500, 1500, 256), (2100, 900, 128), (16384, 200, 64),
+                                    (9000, 300, 256), (40, 37, 16)])
 def test_panel_variants_exact_bitwise(gpu, exact_mode, cluster_panel, m, n, nb):
     """Every FP32 leaf kernel applies the DGETRF2 pivot and update rules in
     the reference order (SRC/dgetrf2.f:170-265): LU, IPIV and INFO match the
