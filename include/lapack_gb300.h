@@ -432,6 +432,16 @@ int gb300_dgetrf_vbatched_dev(int batch, const int* d_n, double* const* dA_array
  * 1 float), as chosen by the autotuner (lapack_gb300.autotune_batched). */
 int gb300_vbatched_set_nb(int dtype, const int* table);
 int gb300_vbatched_get_nb(int dtype, int* table);
+/* Instrumentation of the batched kernel, no reference counterpart: with
+ * gb300_vbatched_profile(1) every later batched launch sums, per phase of
+ * the per-system work, the SM cycles its CTAs spend (clock64 differences
+ * of thread 0): [0] queue, [1] panel staging, [2] panel factorization,
+ * [3] write-back and interchanges, [4] triangular solve of the U block row,
+ * [5] trailing update, [6] the solve of the right-hand sides.
+ * gb300_vbatched_profile_read copies the seven sums and clears them.
+ * Returns the previous switch / 0, or -1 on a device error. */
+int gb300_vbatched_profile(int on);
+int gb300_vbatched_profile_read(unsigned long long* cycles);
 
 /* Adjoint of X = A^{-1} B from the stored factors (no reference counterpart;
  * the building blocks are DGETRS('T'), SRC/dgetrs.f:199-217, and

@@ -14,6 +14,21 @@ namespace gb {
 namespace {
 
 std::mutex g_tab_mu;
+// optional per-phase cycle counters of the batched kernel (one per device)
+bool g_phase_on = false;
+unsigned long long* g_phase[64] = {nullptr};
+
+unsigned long long* phase_buffer() {
+  int dev = 0;
+  if (!g_phase_on || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!g_phase[dev]) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, sizeof(unsigned long long) * kBatPhases) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, sizeof(unsigned long long) * kBatPhases);
+    g_phase[dev] = static_cast<unsigned long long*>(p);
+  }
+  return g_phase[dev];
+}
 int g_nb_table[2][kBatBuckets] = {
     {16, 32, 32, 32, 32, 32, 32, 32},   // double (capacity 32)
     {16, 32, 32, 32, 64, 64, 64, 64},   // float (capacity 64)
@@ -32,11 +47,11 @@ int launch_batched(BatchArgs<T> a, cudaStream_t s) {
     attr[dev] = true;
   }
   int occ = 0;
-  GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_gesv_kernel<T, EXACT>, kBatThreads, smem));
+  GB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batched_gesv_kernel<T, EXACT>, bat_threads<T>(), smem));
   const int grid = std::max(1, std::min(a.batch, device_sm_count() * std::max(1, occ)));
   a.cap = cap;
   prof_begin(kProfOther, s);
-  GB_LAUNCH(batched_gesv_kernel<T, EXACT><<<grid, kBatThreads, smem, s>>>(a));
+  GB_LAUNCH(batched_gesv_kernel<T, EXACT><<<grid, bat_threads<T>(), smem, s>>>(a));
   prof_end(kProfOther, s, 0.0, 0.0);
   return (int)cudaGetLastError();
 }
@@ -76,7 +91,7 @@ int gesv_vbatched_dev(int batch, const int* d_n, const int* d_nrhs, T* const* dA
   GB_LAUNCH(batched_set_table_kernel<<<1, kBatBuckets, 0, s>>>(tab, BucketTable{{htab[0], htab[1], htab[2], htab[3],
                                                                                    htab[4], htab[5], htab[6], htab[7]}}));
   GB_CUDA_TRY(cudaMemsetAsync(queue, 0, sizeof(unsigned), s));
-  BatchArgs<T> a{batch, d_n, d_nrhs, dA, d_lda, dIpiv, dB, d_ldb, d_info, order, queue, tab, 0, solve};
+  BatchArgs<T> a{batch, d_n, d_nrhs, dA, d_lda, dIpiv, dB, d_ldb, d_info, order, queue, tab, 0, solve, phase_buffer()};
   return options().exact ? launch_batched<T, true>(a, s) : launch_batched<T, false>(a, s);
 }
 template int gesv_vbatched_dev<double>(int, const int*, const int*, double* const*, const int*, int* const*,
@@ -121,6 +136,22 @@ int gb300_dgetrf_vbatched_dev(int batch, const int* d_n, double* const* dA_array
 int gb300_vbatched_set_nb(int dtype, const int* table) {
   if (dtype != 0 && dtype != 1) return -1;
   gb::set_batched_table(dtype, table);
+  return 0;
+}
+int gb300_vbatched_profile(int on) {
+  const int old = gb::g_phase_on;
+  gb::g_phase_on = on != 0;
+  return old;
+}
+int gb300_vbatched_profile_read(unsigned long long* cycles) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  for (int i = 0; i < gb::kBatPhases; ++i) cycles[i] = 0;
+  if (!gb::g_phase[dev]) return 0;
+  if (cudaMemcpy(cycles, gb::g_phase[dev], sizeof(unsigned long long) * gb::kBatPhases, cudaMemcpyDeviceToHost) !=
+      cudaSuccess)
+    return -1;
+  cudaMemset(gb::g_phase[dev], 0, sizeof(unsigned long long) * gb::kBatPhases);
   return 0;
 }
 int gb300_vbatched_get_nb(int dtype, int* table) {

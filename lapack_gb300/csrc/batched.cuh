@@ -24,17 +24,22 @@
 
 namespace gb {
 
-constexpr int kBatThreads = 256;
+// threads per CTA: 512 for FP32 (more warps to hide the latency of the
+// per-column steps), 256 for FP64 (whose tiles need more registers)
+template <typename T>
+constexpr int bat_threads() { return sizeof(T) == 4 ? 512 : 256; }
 constexpr int kBatMaxN = 512;
 constexpr int kBatMaxNb = 64;               // panel width cap (FP64 is limited to 32 by shared memory)
 constexpr int kBatMaxRhs = 4;
 constexpr int kBatBuckets = kBatMaxN / 64;   // size buckets of 64 rows
 constexpr int kBatUChunk = 64;               // U12 columns staged per chunk
+constexpr int kBatUStride = kBatUChunk + 8;  // row stride of the staged chunk (spreads the solve's lanes over the banks)
+constexpr int kBatDefer = 4;                 // panel columns whose rank-1 updates are applied together
 
-// panel [cap][512] + U12 chunk [cap][kBatUChunk] + B [4][512] + labels and pairs
+// panel [cap][512] + U12 chunk [cap][kBatUStride] + B [4][512] + labels and pairs
 template <typename T>
 constexpr size_t batched_smem_bytes(int cap) {
-  return sizeof(T) * ((size_t)cap * kBatMaxN + (size_t)cap * kBatUChunk + (size_t)kBatMaxN * kBatMaxRhs) +
+  return sizeof(T) * ((size_t)cap * kBatMaxN + (size_t)cap * kBatUStride + (size_t)kBatMaxN * kBatMaxRhs) +
          sizeof(int) * (4 * kBatMaxNb + kBatMaxN) + 64;
 }
 template <typename T>
@@ -56,34 +61,40 @@ struct BatchArgs {
   const int* nb_table;     // panel width per 64-row size bucket (each <= cap)
   int cap;                 // panel width the shared memory is laid out for (32 or 64)
   int solve;               // 0: factor only (DGETRF), 1: factor + solve (DGESV)
+  unsigned long long* phase;   // per-phase SM cycles summed over CTAs (kBatPhases), or null
 };
 
-// Block-wide IDAMAX over x[0..len) of a shared-memory column: returns the
-// index (first maximum, NaN only when first) to every thread.
-template <typename T>
-__device__ __forceinline__ int block_iamax(const T* x, int len, Cand<T>* red) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  Cand<T> best;
-  best.absval = 0; best.row = -1; best.cls = -1;
-  for (int i = tid; i < len; i += kBatThreads) {
-    Cand<T> c = make_cand(x[i], i, 0);
-    if (cand_better(c, best)) best = c;
+// Phases of the per-system work whose cycles the optional instrumentation
+// sums (thread 0 of every CTA, clock64 differences).
+enum : int { kBatPhQueue = 0, kBatPhStage, kBatPhPanel, kBatPhSwap, kBatPhTrsm, kBatPhUpdate, kBatPhSolve, kBatPhases };
+struct BatPhaseClock {
+  unsigned long long* out;
+  long long t0;
+  __device__ __forceinline__ explicit BatPhaseClock(unsigned long long* o) : out(threadIdx.x == 0 ? o : nullptr) {
+    t0 = out ? clock64() : 0;
   }
-  best = warp_best(best);
-  if (lane == 0) red[warp] = best;
-  __syncthreads();
-  if (warp == 0) {
-    Cand<T> c = lane < kBatThreads / 32 ? red[lane] : Cand<T>{0, -1, -1};
-    c = warp_best(c);
-    if (lane == 0) red[kBatThreads / 32] = c;
+  __device__ __forceinline__ void mark(int ph) {
+    if (out) {
+      const long long now = clock64();
+      atomicAdd(out + ph, (unsigned long long)(now - t0));
+      t0 = now;
+    }
   }
-  __syncthreads();
-  const int r = red[kBatThreads / 32].row;
-  return r < 0 ? 0 : r;
-}
+};
+
+// 16-byte shared-memory vector of T and its unpacking.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> {
+  using type = float4;
+  __device__ __forceinline__ static void unpack(const float4& v, float* o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <> struct Vec16<double> {
+  using type = double2;
+  __device__ __forceinline__ static void unpack(const double2& v, double* o) { o[0] = v.x; o[1] = v.y; }
+};
 
 // Shared-memory layout, sized for the widest panel `cap`:
-// [panel cap x 512][U12 chunk cap x 64][B 4 x 512][labels 512][pairs 2 x 128]
+// [panel cap x 512][U12 chunk cap x kBatUStride][B 4 x 512][labels 512][pairs 2 x 128]
 template <typename T>
 __device__ __forceinline__ T* bat_panel(unsigned char* smem) { return reinterpret_cast<T*>(smem); }
 template <typename T>
@@ -92,7 +103,7 @@ __device__ __forceinline__ T* bat_uchunk(unsigned char* smem, int cap) {
 }
 template <typename T>
 __device__ __forceinline__ T* bat_rhs(unsigned char* smem, int cap) {
-  return bat_uchunk<T>(smem, cap) + (size_t)cap * kBatUChunk;
+  return bat_uchunk<T>(smem, cap) + (size_t)cap * kBatUStride;
 }
 template <typename T>
 __device__ __forceinline__ int* bat_labels(unsigned char* smem, int cap) {
@@ -101,127 +112,226 @@ __device__ __forceinline__ int* bat_labels(unsigned char* smem, int cap) {
 
 template <typename T, bool EXACT>
 __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __restrict__ ipiv, int* __restrict__ info,
-                                  int nb, int cap, unsigned char* smem) {
+                                  int nb, int cap, unsigned char* smem, BatPhaseClock& clk) {
+  constexpr int kBatThreads = bat_threads<T>();
   const int tid = threadIdx.x;
   T* P = bat_panel<T>(smem);                                // panel [nb][M]
-  T* U = bat_uchunk<T>(smem, cap);                          // U12 chunk [nb][kBatUChunk]
+  T* U = bat_uchunk<T>(smem, cap);                          // U12 chunk [nb][kBatUStride]
   int* lab = bat_labels<T>(smem, cap);                      // [kBatMaxN]
   int* pd = lab + kBatMaxN;                                 // pair dst [2nb]
   int* ps = pd + 2 * kBatMaxNb;                             // pair src [2nb]
   __shared__ Cand<T> red[kBatThreads / 32 + 1];
   __shared__ int npairs_s;
+  // pivot rows of the columns whose updates are still pending (slot k % kBatDefer)
+  __shared__ T uh[kBatDefer * kBatMaxNb];
   int first_zero = 0;
   for (int j = 0; j < n; j += nb) {
     const int jb = min(nb, n - j);
     const int M = n - j;
+    const int Mp = (M + 3) & ~3;          // panel column stride: 16-byte aligned columns
     // 1. stage the panel and factor it column by column
     batched_copy<8, kBatThreads, T>(
         jb * M, tid, [&](int e) { const int c = e / M, r = e - c * M; return A[(size_t)(j + r) + (size_t)(j + c) * lda]; },
-        [&](int e, T v) { const int c = e / M, r = e - c * M; P[c * M + r] = v; });
+        [&](int e, T v) { const int c = e / M, r = e - c * M; P[c * Mp + r] = v; });
     for (int r = tid; r < M; r += kBatThreads) lab[r] = r;
     __syncthreads();
+    clk.mark(kBatPhStage);
+    // Column by column, with the rank-1 updates of a group of kBatDefer
+    // columns deferred: column k+1 receives the group's pending updates at
+    // once (its values are the next pivot candidates, searched during that
+    // update), the columns after it receive them every kBatDefer columns in
+    // one pass.  Every element still receives its updates in increasing k
+    // (the order of SRC/dgetrf2.f), so the factors are those of the
+    // column-by-column loop.  Per column: one CTA-wide reduction of the
+    // candidates, one barrier after the interchange.
+    Cand<T> mine{0, -1, -1};
+    for (int r = tid; r < M; r += kBatThreads) {
+      const Cand<T> c = make_cand(P[r], r, 0);
+      if (cand_better(c, mine)) mine = c;
+    }
     for (int k = 0; k < jb; ++k) {
-      const int p = k + block_iamax<T>(P + k * M + k, M - k, red);
-      const T pv = P[k * M + p];
-      if (tid == 0) {
-        ipiv[j + k] = j + p + 1;
-        if (pv == T(0) && first_zero == 0) first_zero = j + k + 1;
-      }
-      if (pv == T(0) && first_zero == 0) first_zero = j + k + 1;
-      if (p != k) {
-        for (int c = tid; c < jb; c += kBatThreads) {
-          const T t = P[c * M + k];
-          P[c * M + k] = P[c * M + p];
-          P[c * M + p] = t;
+      const int s_slot = k % kBatDefer, kfirst = k - s_slot;
+      // 1. the pivot: warp winners, then every thread reduces the warps'
+      mine = warp_best(mine);
+      if ((tid & 31) == 0) red[tid >> 5] = mine;
+      __syncthreads();
+      Cand<T> best = red[0];
+#pragma unroll
+      for (int w = 1; w < kBatThreads / 32; ++w)
+        if (cand_better(red[w], best)) best = red[w];
+      const int p = best.row < 0 ? k : best.row;
+      // 2. the pivot row brought up to date (the group's pending updates on
+      //    its columns after k+1) becomes row k of U and the pending-update
+      //    row of this column; the old row k moves to p as it stands (its
+      //    multipliers and pending updates travel with it)
+      //    (threads 0..63, one column each: every read of the two rows
+      //    before any write, separated by a barrier of those 64 threads)
+      if (tid < kBatMaxNb) {
+        const int c = tid;
+        T v = T(0), old_k = T(0);
+        if (c < jb) {
+          v = P[c * Mp + p];
+          if (c > k)
+            for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(P[(kfirst + d) * Mp + p], uh[d * kBatMaxNb + c], v);
+          old_k = P[c * Mp + k];
         }
-        if (tid == 0) { const int t = lab[k]; lab[k] = lab[p]; lab[p] = t; }
+        asm volatile("bar.sync 1, %0;" ::"n"(kBatMaxNb) : "memory");
+        if (c < jb) {
+          uh[s_slot * kBatMaxNb + c] = v;
+          if (p != k) P[c * Mp + p] = old_k;
+          P[c * Mp + k] = v;
+        }
+        if (c == 0 && p != k) { const int t = lab[k]; lab[k] = lab[p]; lab[p] = t; }
       }
       __syncthreads();
+      const T pv = P[k * Mp + k];
+      if (tid == 0) ipiv[j + k] = j + p + 1;
+      if (pv == T(0) && first_zero == 0) first_zero = j + k + 1;
+      // 3. scale column k, update column k+1 (and search it), flush the
+      //    group's updates into the later columns every kBatDefer columns
       const bool scale = pv != T(0);
       const bool recip = (pv < 0 ? -pv : pv) >= Lim<T>::sfmin();
       const T rp = T(1) / pv;
+      const bool flush = s_slot == kBatDefer - 1;
+      mine = Cand<T>{0, -1, -1};
       for (int r = k + 1 + tid; r < M; r += kBatThreads) {
-        const T v = P[k * M + r];
-        const T l = scale ? (recip ? v * rp : v / pv) : v;
-        P[k * M + r] = l;
-        for (int c = k + 1; c < jb; ++c) P[c * M + r] = fnmadd<EXACT>(l, P[c * M + k], P[c * M + r]);
+        const T v = P[k * Mp + r];
+        T l = v;
+        if (scale) l = recip ? v * rp : v / pv;
+        P[k * Mp + r] = l;
+        T ld[kBatDefer];
+#pragma unroll
+        for (int d = 0; d < kBatDefer; ++d) ld[d] = d < s_slot ? P[(kfirst + d) * Mp + r] : (d == s_slot ? l : T(0));
+        if (k + 1 < jb) {
+          T t = P[(k + 1) * Mp + r];
+#pragma unroll
+          for (int d = 0; d < kBatDefer; ++d)
+            if (d <= s_slot) t = fnmadd<EXACT>(ld[d], uh[d * kBatMaxNb + k + 1], t);
+          P[(k + 1) * Mp + r] = t;
+          const Cand<T> c = make_cand(t, r, k + 1);
+          if (cand_better(c, mine)) mine = c;
+        }
+        if (flush) {
+          for (int c = k + 2; c < jb; ++c) {
+            T t = P[c * Mp + r];
+#pragma unroll
+            for (int d = 0; d < kBatDefer; ++d) t = fnmadd<EXACT>(ld[d], uh[d * kBatMaxNb + c], t);
+            P[c * Mp + r] = t;
+          }
+        }
       }
-      __syncthreads();
     }
+    // (no update is left pending: the last column's k+1 step covers the
+    // panel's final column)
+    __syncthreads();
+    clk.mark(kBatPhPanel);
     // write the factored panel back
     for (int e = tid; e < jb * M; e += kBatThreads) {
       const int c = e / M, r = e - c * M;
-      A[(size_t)(j + r) + (size_t)(j + c) * lda] = P[c * M + r];
+      A[(size_t)(j + r) + (size_t)(j + c) * lda] = P[c * Mp + r];
     }
     // 2. interchanges of the other columns as a gather over the moved rows
-    if (tid == 0) {
-      int np = 0;
-      for (int r = 0; r < M && np < 2 * kBatMaxNb; ++r)
-        if (lab[r] != r) { pd[np] = j + r; ps[np] = j + lab[r]; ++np; }
-      npairs_s = np;
-    }
+    // (at most 2 jb rows moved; their order in the list does not matter:
+    // every source is read before any destination is written)
+    if (tid == 0) npairs_s = 0;
     __syncthreads();
-    const int np = npairs_s;
-    if (np > 0) {
-      for (int c = tid; c < n; c += kBatThreads) {
-        if (c >= j && c < j + jb) continue;
-        T v[2 * kBatMaxNb];
-#pragma unroll 8
-        for (int i = 0; i < np; ++i) v[i] = A[(size_t)ps[i] + (size_t)c * lda];
-#pragma unroll 8
-        for (int i = 0; i < np; ++i) A[(size_t)pd[i] + (size_t)c * lda] = v[i];
-      }
-    }
-    __syncthreads();
-    const int ncol = n - j - jb;
-    if (ncol <= 0) continue;
-    // 3. U12 = L11^{-1} A12 (L11 = top jb rows of the panel), per column in registers
-    for (int c = tid; c < ncol; c += kBatThreads) {
-      T x[kBatMaxNb];
-      T* col = A + (size_t)j + (size_t)(j + jb + c) * lda;
-#pragma unroll
-      for (int i = 0; i < kBatMaxNb; ++i) x[i] = i < jb ? col[i] : T(0);
-#pragma unroll
-      for (int kk = 0; kk < kBatMaxNb - 1; ++kk) {
-        if (kk < jb - 1) {
-#pragma unroll
-          for (int i = kk + 1; i < kBatMaxNb; ++i)
-            if (i < jb) x[i] = fnmadd<EXACT>(x[kk], P[kk * M + i], x[i]);
+    for (int r = tid; r < M; r += kBatThreads) {
+      if (lab[r] != r) {
+        const int slot = atomicAdd(&npairs_s, 1);
+        if (slot < 2 * kBatMaxNb) {
+          pd[slot] = j + r;
+          ps[slot] = j + lab[r];
         }
       }
-#pragma unroll
-      for (int i = 0; i < kBatMaxNb; ++i)
-        if (i < jb) col[i] = x[i];
     }
     __syncthreads();
-    // 4. A22 -= A21 * U12 in chunks of kBatUChunk columns; A21 = panel rows jb..M-1
-    const int mrows = M - jb;
+    const int np = min(npairs_s, 2 * kBatMaxNb);
+    if (np > 0) {
+      // one warp per column, the lanes over the moved rows (np <= 128)
+      const int warp = tid >> 5, lane = tid & 31;
+      constexpr int kPer = 2 * kBatMaxNb / 32;
+      for (int c = warp; c < n; c += kBatThreads / 32) {
+        if (c >= j && c < j + jb) continue;
+        T* Ac = A + (size_t)c * lda;
+        T v[kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+          const int i = lane + 32 * q;
+          if (i < np) v[q] = Ac[ps[i]];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+          const int i = lane + 32 * q;
+          if (i < np) Ac[pd[i]] = v[q];
+        }
+      }
+    }
+    __syncthreads();
+    clk.mark(kBatPhSwap);
+    const int ncol = n - j - jb;
+    if (ncol <= 0) continue;
+    // 3 + 4. per chunk of kBatUChunk columns of the block row: stage A12 in
+    //    shared memory, U12 = L11^{-1} A12 there (SRC/dgetrf.f:204), write
+    //    U12 back, then A22 -= A21 * U12 (SRC/dgetrf.f:212-216) with U12 read
+    //    from shared memory.  The triangular solve: warp w takes columns
+    //    8w..8w+7, the four lane groups of eight the rows of one residue mod
+    //    4, one step per column kk of L11 (every element gets its updates in
+    //    increasing kk, the order of BLAS/SRC/dtrsm.f:290-300).
     for (int cb = 0; cb < ncol; cb += kBatUChunk) {
       const int cw = min(kBatUChunk, ncol - cb);
       batched_copy<8, kBatThreads, T>(
           jb * cw, tid,
           [&](int e) { const int c = e / jb, r = e - c * jb; return A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda]; },
-          [&](int e, T v) { const int c = e / jb, r = e - c * jb; U[r * kBatUChunk + c] = v; });
+          [&](int e, T v) { const int c = e / jb, r = e - c * jb; U[r * kBatUStride + c] = v; });
       __syncthreads();
-      // each thread: 4 rows x 4 columns of the chunk per pass
-      const int tiles_r = (mrows + 3) / 4, tiles_c = (cw + 3) / 4;
+      {
+        const int lane = tid & 31, c = 8 * (tid >> 5) + (lane & 7), q = lane >> 3;
+        const bool live = c < cw;
+        for (int kk = 0; kk + 1 < jb; ++kk) {
+          if (live) {
+            const T xk = U[kk * kBatUStride + c];
+            const int i0 = kk + 1 + ((q - (kk + 1)) & 3);
+            for (int i = i0; i < jb; i += 4)
+              U[i * kBatUStride + c] = fnmadd<EXACT>(xk, P[kk * Mp + i], U[i * kBatUStride + c]);
+          }
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+      for (int e = tid; e < jb * cw; e += kBatThreads) {
+        const int c = e / jb, r = e - c * jb;
+        A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] = U[r * kBatUStride + c];
+      }
+      clk.mark(kBatPhTrsm);
+      // each thread: a 4 x 4 tile of the chunk per pass, its operands read
+      // from shared memory with 16-byte loads.  Tile rows start at the
+      // aligned row jb & ~3 of the panel; rows above jb (part of U) and
+      // columns past the chunk are computed but not stored.
+      constexpr int VE = 16 / (int)sizeof(T);               // elements per 16-byte load
+      using V = typename Vec16<T>::type;
+      const int rb = jb & ~3;
+      const int tiles_r = (M - rb + 3) / 4, tiles_c = (cw + 3) / 4;
       for (int t = tid; t < tiles_r * tiles_c; t += kBatThreads) {
         const int tr = t % tiles_r, tc = t / tiles_r;
-        const int r0 = tr * 4, c0 = tc * 4;
+        const int r0 = rb + tr * 4, c0 = tc * 4;          // panel row, chunk column
         T acc[4][4];
 #pragma unroll
         for (int a = 0; a < 4; ++a)
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int r = r0 + a, c = c0 + b;
-            acc[a][b] = (r < mrows && c < cw) ? A[(size_t)(j + jb + r) + (size_t)(j + jb + cb + c) * lda] : T(0);
+            acc[a][b] = (r >= jb && r < M && c < cw) ? A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] : T(0);
           }
         for (int kk = 0; kk < jb; ++kk) {
           T av[4], bv[4];
+          const V* pa = reinterpret_cast<const V*>(P + (size_t)kk * Mp + r0);
+          const V* pb = reinterpret_cast<const V*>(U + (size_t)kk * kBatUStride + c0);
 #pragma unroll
-          for (int a = 0; a < 4; ++a) av[a] = (r0 + a < mrows) ? P[kk * M + jb + r0 + a] : T(0);
-#pragma unroll
-          for (int b = 0; b < 4; ++b) bv[b] = U[kk * kBatUChunk + c0 + b];
+          for (int qv = 0; qv < 4 / VE; ++qv) {
+            Vec16<T>::unpack(pa[qv], av + qv * VE);
+            Vec16<T>::unpack(pb[qv], bv + qv * VE);
+          }
 #pragma unroll
           for (int a = 0; a < 4; ++a)
 #pragma unroll
@@ -232,11 +342,12 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
 #pragma unroll
           for (int b = 0; b < 4; ++b) {
             const int r = r0 + a, c = c0 + b;
-            if (r < mrows && c < cw) A[(size_t)(j + jb + r) + (size_t)(j + jb + cb + c) * lda] = acc[a][b];
+            if (r >= jb && r < M && c < cw) A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] = acc[a][b];
           }
       }
       __syncthreads();
     }
+    clk.mark(kBatPhUpdate);
   }
   if (tid == 0) *info = first_zero;
   __syncthreads();
@@ -252,6 +363,7 @@ constexpr int kBatSolveChunk = 32;
 template <typename T, bool EXACT>
 __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int lda, const int* __restrict__ ipiv,
                                   T* __restrict__ B, int ldb, unsigned char* smem, int cap) {
+  constexpr int kBatThreads = bat_threads<T>();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   T* Lc = bat_panel<T>(smem);                               // [kBatSolveChunk][n] chunk of factors (cap >= 32)
   T* Bs = bat_rhs<T>(smem, cap);                            // [nrhs][kBatMaxN]
@@ -315,10 +427,11 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
 }
 
 template <typename T, bool EXACT>
-__global__ void __launch_bounds__(kBatThreads)
+__global__ void __launch_bounds__(bat_threads<T>())
 batched_gesv_kernel(BatchArgs<T> a) {
   extern __shared__ __align__(16) unsigned char bat_smem[];
   __shared__ int sys_s;
+  BatPhaseClock clk(a.phase);
   for (;;) {
     if (threadIdx.x == 0) {
       const unsigned t = atomicAdd(a.queue, 1u);
@@ -334,11 +447,13 @@ batched_gesv_kernel(BatchArgs<T> a) {
       continue;
     }
     const int nb = min(max(a.nb_table[(n - 1) / 64], 1), a.cap);
-    batched_getrf_one<T, EXACT>(n, a.A[s], a.lda[s], a.ipiv[s], a.info + s, nb, a.cap, bat_smem);
+    clk.mark(kBatPhQueue);
+    batched_getrf_one<T, EXACT>(n, a.A[s], a.lda[s], a.ipiv[s], a.info + s, nb, a.cap, bat_smem, clk);
     __syncthreads();
     if (a.solve && a.info[s] == 0 && a.nrhs[s] > 0)
       batched_getrs_one<T, EXACT>(n, min(a.nrhs[s], kBatMaxRhs), a.A[s], a.lda[s], a.ipiv[s], a.B[s], a.ldb[s],
                                   bat_smem, a.cap);
+    clk.mark(kBatPhSolve);
   }
 }
 

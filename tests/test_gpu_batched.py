@@ -99,3 +99,27 @@ def test_batched_graph_capture(gpu):
         for i in range(len(As)):
             assert np.array_equal(got[1][i], ref[1][i])
             assert np.array_equal(got[2][i], ref[2][i])
+
+
+@pytest.mark.parametrize("dt", ["d", "s"])
+@pytest.mark.parametrize("nb", [1, 3, 5, 8, 13, 32])
+def test_batched_exact_bitwise_panel_widths(gpu, exact_mode, dt, nb):
+    """Panel widths that are not multiples of the four columns whose
+    updates the panel defers (and the single-column panel): the factors and
+    solutions stay bitwise the oracle's."""
+    import torch
+    dtype = np.float64 if dt == "d" else np.float32
+    code = 0 if dt == "d" else 1
+    old = gpu.vbatched_nb(code)
+    gpu.set_vbatched_nb(code, [nb] * 8)
+    try:
+        As, Bs = make_batch(10, 29 + nb, nmax=300, dtype=dtype)
+        lus, ips, xs, info = gpu.gesv_vbatched(As, Bs, torch.float64 if dt == "d" else torch.float32)
+    finally:
+        gpu.set_vbatched_nb(code, old)
+    for i, (a, b) in enumerate(zip(As, Bs)):
+        lu_r, ip_r, x_r, info_r = oracle.gesv(a, b)
+        assert info[i] == info_r
+        np.testing.assert_array_equal(ips[i], ip_r)
+        assert lus[i].tobytes() == np.asfortranarray(lu_r).tobytes(), f"system {i} n={a.shape[0]}"
+        assert xs[i].tobytes() == np.asfortranarray(x_r).tobytes(), f"system {i} n={a.shape[0]}"
