@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-sweep", action="store_true", help="skip the per-kappa records (1e2, 1e6, 1e10)")
+    p.add_argument("--no-sub", action="store_true", help="skip the batched and adjoint records of the default run")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
     p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint"],
                    help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
@@ -392,50 +393,56 @@ def run_gpu(args, rank, world):
                       ctypes.c_void_p(hB.data_ptr()), ci(n), ctypes.c_void_p(hX.data_ptr()), ci(n),
                       work.ctypes.data_as(ctypes.c_void_p), swork.ctypes.data_as(ctypes.c_void_p),
                       ctypes.byref(it), ctypes.byref(info))
+        def plain_copy_rates(k):
+            # the host->device rate of the same pinned bytes by a plain copy:
+            # the link's rate at that moment, which varies with the host
+            rates = []
+            for _ in range(k):
+                c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                c0.record(stream)
+                dst.copy_(hA, non_blocking=True)
+                c1.record(stream)
+                torch.cuda.synchronize()
+                rates.append(8.0 * n * n / (c0.elapsed_time(c1) * 1e-3) / 1e9)
+            return rates
+
+        dst = torch.empty_like(M)
         e2e_step()
         torch.cuda.synchronize()
-        t_steps = []
+        before = plain_copy_rates(3)
+        # each call with its copies bracketed by events: the split of the
+        # end-to-end time into host->device copy, device work and device->host
+        t_steps, splits = [], []
+        L.gb300_prof_mask((1 << 9) | (1 << 10))
         for _ in range(max(3, min(args.steps, 5))):
+            L.gb300_prof_reset()
+            L.gb300_prof_enable(1)
             t0 = time.perf_counter()
             e2e_step()
             t_steps.append(time.perf_counter() - t0)
-        t_e2e = statistics.median(t_steps)
-        # one more call with the copies bracketed by events: the split of the
-        # end-to-end time into host->device copy, device work and device->host
-        L.gb300_prof_reset()
-        L.gb300_prof_mask((1 << 9) | (1 << 10))
-        L.gb300_prof_enable(1)
-        t0 = time.perf_counter()
-        e2e_step()
-        t_split = time.perf_counter() - t0
-        L.gb300_prof_enable(0)
-        split = {}
-        for k, nm in ((9, "h2d"), (10, "d2h")):
-            t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
-            L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
-            split[nm + "_s"] = t_ms.value * 1e-3
-            split[nm + "_gbs"] = by.value / max(t_ms.value * 1e-3, 1e-12) / 1e9
-        split["total_s"] = t_split
-        split["device_and_host_rest_s"] = t_split - split["h2d_s"] - split["d2h_s"]
-        # the host->device rate of the same pinned bytes by a plain copy, three
-        # times: the link's rate at the moment, which varies between calls
-        rates = []
-        dst = torch.empty_like(M)
-        for _ in range(3):
-            c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            c0.record(stream)
-            dst.copy_(hA, non_blocking=True)
-            c1.record(stream)
-            torch.cuda.synchronize()
-            rates.append(8.0 * n * n / (c0.elapsed_time(c1) * 1e-3) / 1e9)
-        del dst
-        split["plain_copy_rates_gbs"] = rates
+            L.gb300_prof_enable(0)
+            sp_ = {}
+            for k, nm in ((9, "h2d"), (10, "d2h")):
+                t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+                L.gb300_prof_read(k, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
+                sp_[nm + "_s"] = t_ms.value * 1e-3
+                sp_[nm + "_gbs"] = by.value / max(t_ms.value * 1e-3, 1e-12) / 1e9
+            sp_["rest_s"] = t_steps[-1] - sp_["h2d_s"] - sp_["d2h_s"]
+            splits.append(sp_)
         L.gb300_prof_reset()
         L.gb300_prof_mask(0xFFFFFFFF)
+        after = plain_copy_rates(3)
+        del dst
+        t_e2e = statistics.median(t_steps)
+        mid = t_steps.index(sorted(t_steps)[len(t_steps) // 2])
+        split = dict(splits[mid])
+        split["per_call"] = splits
+        split["plain_copy_rates_gbs_before"] = before
+        split["plain_copy_rates_gbs_after"] = after
         result["e2e"] = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": 8 * n * n + 8 * n * nrhs,
                          "d2h_bytes_per_step": 8 * n * nrhs + 4 * n,
                          "path": "dsgesv_ (LAPACK Fortran ABI) on pinned host buffers, copies inside the call",
-                         "steps_s": t_steps, "statistic": "median", "split_one_call": split}
+                         "steps_s": t_steps, "statistic": "median", "split_median_call": split}
         del hA, hB, hX
     # ---- plain FP64 GPU DGESV on the same system (the comparison arm)
     if not args.no_fp64:
@@ -824,6 +831,21 @@ def main():
     if world > 1:
         torch.distributed.init_process_group("nccl")
     result = run_gpu(args, rank, world)
+    if not args.no_sub and world == 1:
+        # the other configurations of the path, one record each beside the
+        # headline: the batched uneven solves (FP32 and FP64) and the adjoint
+        import torch
+        torch.cuda.empty_cache()
+        subs = {}
+        for dt in ("s", "d"):
+            a2 = argparse.Namespace(**vars(args))
+            a2.dtype, a2.steps, a2.warmup = dt, 3, 2
+            subs["batched_f32" if dt == "s" else "batched_f64"] = run_batched(a2, 0, 1)
+            torch.cuda.empty_cache()
+        a3 = argparse.Namespace(**vars(args))
+        a3.steps, a3.warmup = 5, 2
+        subs["adjoint"] = run_adjoint(a3)
+        result["sub_workloads"] = subs
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline(args.n, args.cpu_n, args.kappa, args.seed)
     if rank == 0:

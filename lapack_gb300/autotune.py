@@ -4,9 +4,10 @@ Batched: for every 64-row size bucket (n in 1..64, 65..128, ..., 449..512)
 and every candidate panel width, a synthetic batch of systems of that bucket
 is solved in one launch and timed with CUDA events; the fastest width per
 bucket becomes the table the persistent kernel reads
-(gb300_vbatched_set_nb).  Blocked LU: the outer block size of the FP64 and
-FP32 factorizations (NB in 128..512 for the FP32 path, 32..256 for FP64) at
-a given n.
+(gb300_vbatched_set_nb).  Blocked LU: the outer block size of the FP32
+factorization in DSGESV's mode (BF16x3 updates; NB in 128..512 at
+n = 16384) and of the FP64 one (NB 64 and 128..512 at n = 16384, the FP64
+DGESV configuration's size).
 
 Results are written to autotune.json next to this file; `load()` installs
 them (import of the package does this when the file exists).
@@ -75,6 +76,9 @@ def tune_getrf_nb(dtype_code, n, candidates):
     import lapack_gb300 as g
     dtype = torch.float64 if dtype_code == 0 else torch.float32
     key = "nb64" if dtype_code == 0 else "nb32"
+    # the FP32 block size serves DSGESV's factorization: tune it in that
+    # factorization's mode (BF16x3 trailing updates)
+    old_mode = g.set_option("sgetrf", 0) if dtype_code == 1 else None
     A0 = g.colmajor_empty(n, n, dtype)
     A0.copy_(torch.rand(n, n, dtype=dtype, device="cuda") * 2 - 1)
     ip = torch.empty(n, dtype=torch.int32, device="cuda")
@@ -94,6 +98,8 @@ def tune_getrf_nb(dtype_code, n, candidates):
         res[nb] = e0.elapsed_time(e1)
     best = min(res, key=res.get)
     g.set_option(key, best)
+    if old_mode is not None:
+        g.set_option("sgetrf", old_mode)
     return best, res
 
 
@@ -127,8 +133,8 @@ def main():
     if not args.quick:
         best, res = tune_getrf_nb(1, 16384, [128, 256, 384, 512])
         out["getrf"]["nb32"] = {"n": 16384, "best": best, "ms": res}
-        best, res = tune_getrf_nb(0, 8192, [32, 64, 128, 256])
-        out["getrf"]["nb64"] = {"n": 8192, "best": best, "ms": res}
+        best, res = tune_getrf_nb(0, 16384, [64, 128, 256, 384, 512])
+        out["getrf"]["nb64"] = {"n": 16384, "best": best, "ms": res}
         print("getrf", out["getrf"], flush=True)
     with open(args.out, "w") as f:
         json.dump(out, f, indent=1)

@@ -794,7 +794,7 @@ static int launch_trsv(const T* A, int lda, int n, T* X, int ldx, int nrhs, cuda
     }
     prof_begin(kProfTrsv, s);
     GB_LAUNCH(kern<<<(unsigned)nblk * (unsigned)nbatch, kTsThreads, smem, s>>>(A, lda, n, X, ldx, nrhs, pub, ticket,
-                                                                             device_status_word(), sA, sX));
+                                                                             device_status_word(), sA, sX, nbatch));
     prof_end(kProfTrsv, s, (double)nbatch * n * n * nrhs,
              (double)nbatch * sizeof(T) * (0.5 * n * (double)n + 2.0 * n * nrhs));
     return (int)cudaGetLastError();

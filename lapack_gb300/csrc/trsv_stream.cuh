@@ -140,7 +140,7 @@ __device__ __forceinline__ bool ts_poll(T (&v)[NV], const T* const (&p)[NV], con
 template <typename T, bool FORWARD, bool UNIT, bool TRANS, bool INV>
 __global__ void __launch_bounds__(kTsThreads)
 trsv_stream_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, int ldx, int nrhs, T* __restrict__ pub,
-                   unsigned* __restrict__ ticket, int* __restrict__ status, long long sA, long long sX) {
+                   unsigned* __restrict__ ticket, int* __restrict__ status, long long sA, long long sX, int nbatch) {
   extern __shared__ __align__(16) unsigned char ts_smem[];
   T* D = reinterpret_cast<T*>(ts_smem);                 // [64][65] op(T) diagonal block, row-major
   T* Lt = D + kTsBS * kTsLd;                            // [64][65] op(T) link tile, row-major
@@ -156,10 +156,13 @@ trsv_stream_kernel(const T* __restrict__ A, int lda, int n, T* __restrict__ X, i
   const int nblk = (n + kTsBS - 1) / kTsBS;
   if (tid == 0) { t_s = atomicAdd(ticket, 1u); ok_s = 1; }
   __syncthreads();
-  // a batch of independent systems shares the ticket counter: ticket ->
-  // (system, block in solve order); a block waits only on smaller tickets
-  const int sys = (int)(t_s / (unsigned)nblk);
-  const int t = (int)(t_s - (unsigned)sys * (unsigned)nblk);
+  // a batch of independent systems shares the ticket counter, block-major:
+  // ticket -> (block t in solve order, system), so the resident CTAs work on
+  // the first blocks of every system at once and each system's chain of
+  // blocks overlaps the others'; a block waits only on smaller tickets (the
+  // earlier blocks of its own system)
+  const int sys = (int)(t_s % (unsigned)nbatch);
+  const int t = (int)(t_s / (unsigned)nbatch);
   A += sys * sA;
   X += sys * sX;
   pub += (size_t)sys * n * nrhs;
