@@ -442,6 +442,15 @@ int gb300_vbatched_get_nb(int dtype, int* table);
  * Returns the previous switch / 0, or -1 on a device error. */
 int gb300_vbatched_profile(int on);
 int gb300_vbatched_profile_read(unsigned long long* cycles);
+/* Instrumentation of the FP32 cluster panel leaf (pushed exchange), no
+ * reference counterpart: with gb300_leaf_profile(1) every later leaf adds
+ * the SM cycles that CTA 0 spends in each step of its columns: [0] the
+ * CTA's candidate reduction, [1] building and pushing its message, [2] the
+ * wait for the cluster's messages, [3] the interchange, [4] the barrier
+ * after it, [5] the update.  gb300_leaf_profile_read copies the six sums
+ * and clears them.  Returns the previous switch / 0, or -1. */
+int gb300_leaf_profile(int on);
+int gb300_leaf_profile_read(unsigned long long* cycles);
 
 /* Adjoint of X = A^{-1} B from the stored factors (no reference counterpart;
  * the building blocks are DGETRS('T'), SRC/dgetrs.f:199-217, and

@@ -246,6 +246,22 @@ static int laswp_log(T* A, int lda, int a0, int a1, int b0, int b1, const PanelC
 }
 
 // ---- cluster leaf (FP32): availability, width and launch
+
+// Optional cycle counters of the push leaf's column steps (one buffer per
+// device, null while off).
+static bool g_leaf_phase_on = false;
+static unsigned long long* g_leaf_phase[64] = {nullptr};
+static unsigned long long* leaf_phase_buffer() {
+  int dev = 0;
+  if (!g_leaf_phase_on || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!g_leaf_phase[dev]) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, 8 * sizeof(unsigned long long)) != cudaSuccess) return nullptr;
+    cudaMemset(p, 0, 8 * sizeof(unsigned long long));
+    g_leaf_phase[dev] = static_cast<unsigned long long*>(p);
+  }
+  return g_leaf_phase[dev];
+}
 struct ClusterCaps {
   bool ok = false;
   int dyn_cap = 0;
@@ -259,7 +275,8 @@ static ClusterCaps cluster_caps() {
   cudaGetDevice(&dev);
   if (!done[dev]) {
     done[dev] = true;
-    auto kern = PUSH ? leaf_panel_cluster_push_kernel<EXACT, 64> : leaf_panel_cluster_kernel<EXACT, 64>;
+    const void* kern = PUSH ? (const void*)leaf_panel_cluster_push_kernel<EXACT, 64>
+                            : (const void*)leaf_panel_cluster_kernel<EXACT, 64>;
     cudaFuncAttributes fa;
     int optin = 0;
     if (cudaFuncGetAttributes(&fa, (const void*)kern) == cudaSuccess &&
@@ -356,7 +373,8 @@ static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
-  auto kern = PUSH ? leaf_panel_cluster_push_kernel<EXACT, JBT> : leaf_panel_cluster_kernel<EXACT, JBT>;
+  const void* kern = PUSH ? (const void*)leaf_panel_cluster_push_kernel<EXACT, JBT>
+                          : (const void*)leaf_panel_cluster_kernel<EXACT, JBT>;
   if (!attr[dev]) {
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn_cap));
     GB_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
@@ -383,8 +401,13 @@ static int launch_leaf_cluster_w(float* P, int lda, int M, int JB, int R, size_t
     b0 = row0 + JB;
     b1 = cx.imm_hi;
   }
-  return (int)cudaLaunchKernelEx(&cfg, kern, P, lda, M, JB, R, row0, ipiv, info, cx.ps.pair_dst, cx.ps.pair_src,
-                                 cx.ps.pair_count, cx.status, a0, a1, b0, b1);
+  if constexpr (PUSH)
+    return (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_push_kernel<EXACT, JBT>, P, lda, M, JB, R, row0, ipiv,
+                                   info, cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status, a0, a1, b0, b1,
+                                   leaf_phase_buffer());
+  else
+    return (int)cudaLaunchKernelEx(&cfg, leaf_panel_cluster_kernel<EXACT, JBT>, P, lda, M, JB, R, row0, ipiv, info,
+                                   cx.ps.pair_dst, cx.ps.pair_src, cx.ps.pair_count, cx.status, a0, a1, b0, b1);
 }
 
 template <bool EXACT, bool PUSH>
@@ -951,3 +974,21 @@ int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int ld
 }
 
 }  // namespace gb
+
+extern "C" {
+int gb300_leaf_profile(int on) {
+  const int old = gb::g_leaf_phase_on;
+  gb::g_leaf_phase_on = on != 0;
+  return old;
+}
+int gb300_leaf_profile_read(unsigned long long* cycles) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  for (int i = 0; i < 6; ++i) cycles[i] = 0;
+  if (!gb::g_leaf_phase[dev]) return 0;
+  if (cudaMemcpy(cycles, gb::g_leaf_phase[dev], 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return -1;
+  cudaMemset(gb::g_leaf_phase[dev], 0, 8 * sizeof(unsigned long long));
+  return 0;
+}
+}  // extern "C"

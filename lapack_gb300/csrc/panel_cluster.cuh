@@ -376,11 +376,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1)
 leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, int R, int row0, int* __restrict__ ipiv,
                                int* __restrict__ info, int* __restrict__ pair_dst, int* __restrict__ pair_src,
                                int* __restrict__ pair_count, int* __restrict__ status, int swap_a0, int swap_a1,
-                               int swap_b0, int swap_b1) {
+                               int swap_b0, int swap_b1, unsigned long long* __restrict__ phase) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   using Msg = PushMsg<JBT>;
-  constexpr int kMsgVecs = (int)sizeof(Msg) / 16;
   static_assert(sizeof(Msg) % 16 == 0, "message of whole 16-byte vectors");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // rows of the tile padded to a multiple of four (the update works on
@@ -395,18 +394,20 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
   __shared__ __align__(16) Msg out_s;                                      // this CTA's candidate message
   __shared__ __align__(16) Msg outk_s;                                     // row k, when this CTA holds it
   __shared__ __align__(8) uint64_t full[2];
-  __shared__ __align__(16) float urow[kLeafMax];
-  __shared__ __align__(16) float rowk_s[kLeafMax];
   __shared__ unsigned long long wbest[kClusterThreads / 32];
   __shared__ float pv_s;
-  __shared__ int win_label_s, rowk_label_s, prow_s;
   __shared__ __align__(16) float uh[kDefer][kLeafMax];
 
   const int b = (int)cluster.block_rank(), G = (int)cluster.num_blocks();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int rbeg = b * R;
   const int nrows = max(0, min(M, rbeg + R) - rbeg);
-  const uint32_t tx_per_col = (uint32_t)((G + 1) * sizeof(Msg));
+  // a message is its 16-byte header and the row's JB values, whole vectors
+  const int nvec = 1 + (JB + 3) / 4;
+  const uint32_t tx_per_col = (uint32_t)((G + 1) * nvec * 16);
+  // this lane's first vector of the push (destination d0, vector v0) and
+  // the step of 32 vectors in destinations and vectors
+  const int d0 = lane / nvec, v0 = lane - d0 * nvec, q32 = 32 / nvec, r32 = 32 - q32 * nvec;
 
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(cl_smem_u32(&full[0])));
@@ -429,6 +430,19 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
     mykey = kk > mykey ? kk : mykey;
   }
   bool timed_out = false;
+  // optional cycle counts of the column steps (CTA 0, thread 0): [0] the
+  // CTA reduction, [1] the message and its push, [2] the wait, [3] the
+  // interchange, [4] the barrier after it, [5] the update
+  const bool timing = phase != nullptr && b == 0 && tid == 0;
+  long long ph[6] = {0, 0, 0, 0, 0, 0};
+  long long tc = timing ? clock64() : 0;
+  auto mark = [&](int i) {
+    if (timing) {
+      const long long now = clock64();
+      ph[i] += now - tc;
+      tc = now;
+    }
+  };
 
   for (int k = 0; k < JB; ++k) {
     const int par = k & 1;
@@ -438,50 +452,56 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
     mykey = warp_max_u64(mykey);
     if (lane == 0) wbest[warp] = mykey;
     __syncthreads();
+    mark(0);
     if (warp == 0) {
       unsigned long long kk = lane < kClusterThreads / 32 ? wbest[lane] : 0ull;
       kk = warp_max_u64(kk);
-      // 2. the message: key, label and the candidate row up to date (its
-      //    columns after k get the pending updates, in column order)
+      // 2 + 3. the message: key, label and the candidate row with the
+      //    group's pending updates applied to its columns after k, staged
+      //    in shared memory, then pushed to every CTA of the cluster with
+      //    consecutive lanes covering one destination's vectors (few
+      //    destinations per store instruction); the CTA holding row k
+      //    sends that row as it stands
       if (lane == 0) out_s.key = kk;
       if (kk != 0ull) {
         const int lr = (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) - rbeg;
-        for (int c = lane; c < JBT; c += 32) {
-          float v = 0.0f;
-          if (c < JB) {
-            v = tile[c * Rp + lr];
-            if (c > k)
-              for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * Rp + lr], uh[d][c], v);
-          }
+        for (int c = lane; c < JB; c += 32) {
+          float v = tile[c * Rp + lr];
+          if (c > k)
+            for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * Rp + lr], uh[d][c], v);
           out_s.row[c] = v;
         }
         if (lane == 0) out_s.label = label[lr];
       }
       const bool holds_k = (b == k_cta);
+      const int lk0 = k - rbeg;
       if (holds_k) {
-        for (int c = lane; c < JBT; c += 32) outk_s.row[c] = c < JB ? tile[c * Rp + (k - rbeg)] : 0.0f;
-        if (lane == 0) {
-          outk_s.label = label[k - rbeg];
-          outk_s.key = 0ull;
-        }
+        for (int c = lane; c < JB; c += 32) outk_s.row[c] = tile[c * Rp + lk0];
+        if (lane == 0) outk_s.label = label[lk0];
       }
       __syncwarp();
-      // 3. push it to every CTA of the cluster (slot b of the receiver)
-      const uint32_t bar_l = cl_smem_u32(&full[par]);
-      const uint4* src = reinterpret_cast<const uint4*>(&out_s);
-      const uint32_t slot_l = cl_smem_u32(&recv[par][b]);
-      for (int i = lane; i < G * kMsgVecs; i += 32) {
-        const int d = i / kMsgVecs, v = i - d * kMsgVecs;
-        cl_st_async_v4(cl_mapa(slot_l + 16u * v, d), src[v], cl_mapa(bar_l, d));
-      }
-      if (holds_k) {
-        const uint4* srck = reinterpret_cast<const uint4*>(&outk_s);
-        const uint32_t slotk_l = cl_smem_u32(&recv_k[par]);
-        for (int i = lane; i < G * kMsgVecs; i += 32) {
-          const int d = i / kMsgVecs, v = i - d * kMsgVecs;
-          cl_st_async_v4(cl_mapa(slotk_l + 16u * v, d), srck[v], cl_mapa(bar_l, d));
+      {
+        const uint32_t bar_l = cl_smem_u32(&full[par]);
+        const uint4* src = reinterpret_cast<const uint4*>(&out_s);
+        const uint32_t slot_l = cl_smem_u32(&recv[par][b]);
+        // vector i = lane + 32 j of the G * nvec is vector v of CTA d; (d, v)
+        // stepped without a division
+        for (int d = d0, v = v0; d < G; d += q32, v += r32) {
+          if (v >= nvec) { v -= nvec; ++d; }
+          if (d >= G) break;
+          cl_st_async_v4(cl_mapa(slot_l + 16u * v, d), src[v], cl_mapa(bar_l, d));
+        }
+        if (holds_k) {
+          const uint4* srck = reinterpret_cast<const uint4*>(&outk_s);
+          const uint32_t slotk_l = cl_smem_u32(&recv_k[par]);
+          for (int d = d0, v = v0; d < G; d += q32, v += r32) {
+            if (v >= nvec) { v -= nvec; ++d; }
+            if (d >= G) break;
+            cl_st_async_v4(cl_mapa(slotk_l + 16u * v, d), srck[v], cl_mapa(bar_l, d));
+          }
         }
       }
+      mark(1);
       // 4. wait for the G candidates and row k of this column (every lane
       //    of the warp acquires the remote stores it is about to read)
       // After one wait has run out the CTA waits no more: it finishes the
@@ -491,43 +511,40 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
         timed_out = true;
         if (lane == 0) atomicCAS(status, kStatusOk, kStatusFlagTimeout);
       }
+      mark(2);
+      // the winner (every CTA reaches the same), its row into the pending
+      // pivot rows and, where this CTA holds them, into row k; the old row
+      // k into the pivot's place
       unsigned long long ck = lane < G ? recv[par][lane].key : 0ull;
       const unsigned long long wk = warp_max_u64(ck);
       const int wc = __ffsll(__ballot_sync(0xffffffffu, ck == wk && lane < G)) - 1;
       const int prow = (int)(0xFFFFFFFFu - (unsigned)(wk & 0xFFFFFFFFull));
       const Msg& wm = recv[par][wc < 0 ? 0 : wc];
-      for (int c = lane; c < JB; c += 32) urow[c] = wm.row[c];
-      const bool own_p = (prow >= rbeg && prow < rbeg + nrows);
-      if (own_p && prow != k) {
-        for (int c = lane; c < JB; c += 32) rowk_s[c] = recv_k[par].row[c];
+      const bool own_p = (prow >= rbeg && prow < rbeg + nrows) && prow != k;
+      const bool own_k = (k >= rbeg && k < rbeg + nrows);
+      const int lp = prow - rbeg;
+      for (int c = lane; c < JB; c += 32) {
+        const float u = wm.row[c];
+        uh[s_slot][c] = u;
+        if (own_k) tile[c * Rp + lk0] = u;
+        if (own_p) tile[c * Rp + lp] = recv_k[par].row[c];
       }
-      __syncwarp();
       if (lane == 0) {
-        win_label_s = wm.label;
-        if (own_p && prow != k) rowk_label_s = recv_k[par].label;
-        prow_s = prow;
-        pv_s = urow[k];
+        const float pv = wm.row[k];
+        if (own_k && prow != k) label[lk0] = wm.label;
+        if (own_p) label[lp] = recv_k[par].label;
+        pv_s = pv;
         if (b == 0) {
           ipiv[k] = row0 + prow + 1;
-          if (urow[k] == 0.0f && *info == 0) *info = row0 + k + 1;
+          if (pv == 0.0f && *info == 0) *info = row0 + k + 1;
         }
         // the slots of this parity are read: re-arm for column k + 2
         if (k + 2 < JB) cl_arm(&full[par], tx_per_col);
       }
-      __syncwarp();
-      if (k >= rbeg && k < rbeg + nrows) {
-        const int lk = k - rbeg;
-        for (int c = lane; c < JB; c += 32) tile[c * Rp + lk] = urow[c];
-        if (lane == 0 && prow != k) label[lk] = win_label_s;
-      }
-      if (prow != k && own_p) {
-        const int lp = prow - rbeg;
-        for (int c = lane; c < JB; c += 32) tile[c * Rp + lp] = rowk_s[c];
-        if (lane == 0) label[lp] = rowk_label_s;
-      }
-      for (int c = lane; c < JB; c += 32) uh[s_slot][c] = urow[c];
+      mark(3);
     }
     __syncthreads();
+    mark(4);
     // 5. scale column k, update column k+1 (the next candidates) and, every
     //    kDefer columns, the later columns, in the order of
     //    leaf_panel_cluster_kernel, on groups of four rows (one 16-byte
@@ -591,6 +608,7 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
         }
       }
       if (flush) {
+#pragma unroll 4
         for (int c = k + 2; c < JB; ++c) {
           float* pc = tl + (size_t)c * Rp + r0;
           const float4 w = *reinterpret_cast<const float4*>(pc);
@@ -605,7 +623,10 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
         }
       }
     }
+    mark(5);
   }
+  if (timing)
+    for (int i = 0; i < 6; ++i) atomicAdd(phase + i, (unsigned long long)ph[i]);
   // the columns left over after the last flush (JB not a multiple of kDefer)
   // were finished column by column above; no CTA leaves while another may
   // still read it in the interchange step below
