@@ -469,10 +469,12 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * "mixed" (0: BF16x3 tensor cores, 1: FP32 CUDA cores for DSGESV's FP32
  * factorization), "sgetrf" (same choice for SGETRF itself),
  * "panel_ctas64" / "panel_ctas32" (CTAs of the grid-wide panel kernel, 0:
- * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 3,
- * the default, shared-memory kernel whose per-column exchange is pushed to
- * every CTA by remote asynchronous stores; 2 the same kernel exchanging
- * through cluster barriers and remote loads; 1 register kernel; 0 off),
+ * all SMs), "cluster_panel" (FP32 leaves on one thread-block cluster: 2,
+ * the default, shared-memory kernel exchanging each column's candidates
+ * through a cluster barrier and remote loads; 3 the same kernel with the
+ * exchange pushed to every CTA by remote asynchronous stores, faster alone
+ * but slower beside the concurrent trailing update; 1 register kernel; 0
+ * off),
  * "lookahead" (1: the
  * FP32 factorization factors block column k+1 on a second, high-priority
  * stream while the trailing update of block column k runs; 0: one stream),

@@ -19,8 +19,8 @@ struct Options {
   int sgetrf_mode = kMixedFp32;   // sgetrf_ itself: plain FP32 by default
   int panel_ctas_f64 = 0;         // CTAs of the cooperative panel (0: all SMs)
   int panel_ctas_f32 = 0;
-  int cluster_panel = 3;          // FP32 leaves on one thread-block cluster: 3 shared-memory kernel with pushed
-                                  // exchange, 2 shared-memory kernel with cluster barriers, 1 register kernel, 0 off
+  int cluster_panel = 2;          // FP32 leaves on one thread-block cluster: 2 shared-memory kernel with cluster
+                                  // barriers, 3 the same with a pushed exchange, 1 register kernel, 0 off
   int lookahead = 1;              // FP32 cluster path: factor the next block column beside the trailing update
   int trsv_inv = 1;               // DSGESV's FP32 solves: diagonal blocks applied as their inverses
   int gemm_ws = 1;                // BF16x3 update: 1 warp-specialised multi-tile kernel, 0 one tile per CTA

@@ -34,7 +34,7 @@ Options& options() {
     x.nb_f32 = std::max(1, env_int("LAPACK_GB300_NB32", 256));
     x.panel_ctas_f64 = env_int("LAPACK_GB300_PANEL_CTAS64", 0);
     x.panel_ctas_f32 = env_int("LAPACK_GB300_PANEL_CTAS32", 0);
-    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 3);
+    x.cluster_panel = env_int("LAPACK_GB300_CLUSTER_PANEL", 2);
     x.lookahead = env_int("LAPACK_GB300_LOOKAHEAD", 1);
     x.trsv_inv = env_int("LAPACK_GB300_TRSV_INV", 1);
     x.gemm_ws = env_int("LAPACK_GB300_GEMM_WS", 1);
@@ -321,7 +321,7 @@ static int cluster_leaf_width(int M, int* kind) {
                                   : (push ? cluster_caps<false, true>() : cluster_caps<false>());
   if (!c.ok) return 0;
   long long R = (M + kClusterCtas - 1) / kClusterCtas;
-  if (push) R = leaf_push_rows((int)R);
+  if (options().cluster_panel >= 2) R = leaf_push_rows((int)R);
   if (options().cluster_panel == 1) {
     if (R <= 2 * kClusterThreads) { *kind = 1; return 32; }
     if (R <= 4 * kClusterThreads) { *kind = 1; return 16; }
@@ -415,7 +415,7 @@ static int launch_leaf_cluster_p(float* P, int lda, int M, int JB, int row0, int
                                  PanelCtx<float>& cx, cudaStream_t s) {
   ClusterCaps c = cluster_caps<EXACT, PUSH>();
   const int R = (M + kClusterCtas - 1) / kClusterCtas;
-  const int Rs = PUSH ? leaf_push_rows(R) : R;      // the push kernel pads its rows
+  const int Rs = leaf_push_rows(R);      // both shared-memory leaves pad their rows
   size_t smem = (size_t)JB * Rs * 4 + (size_t)Rs * 4 + 16;
   if (!c.ok || (long long)smem > c.dyn_cap || JB > 64) return 1000 + kStatusCapacity;
   GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));

@@ -48,6 +48,97 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return ((unsigned long long)mhi << 32) | mlo;
 }
 
+// Step 5 of a leaf column on the CTA's tile (stride Rp, a multiple of four):
+// scale column k below the pivot, bring column k+1 up to date (the next
+// pivot candidates, whose best key is returned) and, every kDefer columns,
+// apply the group's kDefer pending updates to the later columns; in the
+// order of DGETRF2's right-looking rank-1 updates per element
+// (SRC/dgetrf2.f:217-265).  Groups of four rows with 16-byte accesses; rows
+// at or above k and the padding rows after the CTA's last row keep their
+// values.
+template <bool EXACT>
+__device__ __forceinline__ unsigned long long leaf_update_quads(float* __restrict__ tl, int Rp, int k, int JB,
+                                                              int rbeg, int nrows, int kfirst, int s_slot,
+                                                              const float (*uh)[kLeafMax], float pv) {
+  const int tid = threadIdx.x;
+  const bool scale = pv != 0.0f;
+  const bool recip = fabsf(pv) >= Lim<float>::sfmin();
+  const float rp = 1.0f / pv;
+  const bool flush = s_slot == kDefer - 1;
+  unsigned long long mykey = 0;
+  const int r_lo = k + 1 - rbeg;       // first local row below the diagonal
+  const int nq = (nrows + 3) >> 2;
+  for (int q = max(0, r_lo) / 4 + tid; q < nq; q += kClusterThreads) {
+    const int r0 = 4 * q;
+    bool act[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) act[e] = (r0 + e >= r_lo) && (r0 + e < nrows);
+    float4 v = *reinterpret_cast<const float4*>(tl + (size_t)k * Rp + r0);
+    float l[4] = {v.x, v.y, v.z, v.w};
+    if (scale) {
+      if (recip) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] * rp : l[e];
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] / pv : l[e];
+      }
+      *reinterpret_cast<float4*>(tl + (size_t)k * Rp + r0) = make_float4(l[0], l[1], l[2], l[3]);
+    }
+    float ld[kDefer][4];
+#pragma unroll
+    for (int d = 0; d < kDefer; ++d) {
+      if (d < s_slot) {
+        const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(kfirst + d) * Rp + r0);
+        ld[d][0] = w.x; ld[d][1] = w.y; ld[d][2] = w.z; ld[d][3] = w.w;
+      } else {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) ld[d][e] = d == s_slot ? l[e] : 0.0f;
+      }
+    }
+    if (k + 1 < JB) {
+      const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(k + 1) * Rp + r0);
+      float t[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+      for (int d = 0; d < kDefer; ++d) {
+        if (d <= s_slot) {
+          const float u = uh[d][k + 1];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
+        }
+      }
+      *reinterpret_cast<float4*>(tl + (size_t)(k + 1) * Rp + r0) = make_float4(t[0], t[1], t[2], t[3]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (act[e]) {
+          const unsigned long long kk = pack_key(t[e], rbeg + r0 + e, k + 1);
+          mykey = kk > mykey ? kk : mykey;
+        }
+      }
+    }
+    if (flush) {
+#pragma unroll 4
+      for (int c = k + 2; c < JB; ++c) {
+        float* pc = tl + (size_t)c * Rp + r0;
+        const float4 w = *reinterpret_cast<const float4*>(pc);
+        float t[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int d = 0; d < kDefer; ++d) {
+          const float u = uh[d][c];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
+        }
+        *reinterpret_cast<float4*>(pc) = make_float4(t[0], t[1], t[2], t[3]);
+      }
+    }
+  }
+  return mykey;
+}
+
+__host__ __device__ constexpr int leaf_push_rows(int R) {
+  return ((R + 3) / 4 % 2 == 0) ? (R + 3) / 4 * 4 + 4 : (R + 3) / 4 * 4;
+}
+
 // JBT: the leaf-width capacity (8, 16, 32 or 64), so the rank-1 update's
 // column loop is unrolled; JB <= JBT is the actual width.
 template <bool EXACT, int JBT>
@@ -59,8 +150,9 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  float* tile = reinterpret_cast<float*>(smem_raw);                        // [JB][R]
-  int* label = reinterpret_cast<int*>(tile + (size_t)JB * R);              // [R]
+  const int Rp = leaf_push_rows(R);                                        // padded row stride
+  float* tile = reinterpret_cast<float*>(smem_raw);                        // [JB][Rp]
+  int* label = reinterpret_cast<int*>(tile + (size_t)JB * Rp);             // [Rp]
   __shared__ ClusterSlot slot[2];
   __shared__ __align__(16) float urow[kLeafMax];
   __shared__ __align__(16) float rowk_s[kLeafMax];
@@ -79,7 +171,7 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
   // at once (the panel streams from L2/HBM at the SM's bandwidth)
   for (int c = 0; c < JB; ++c)
     for (int r = tid; r < nrows; r += kClusterThreads)
-      cp_async_elem(tile + c * R + r, P + (size_t)(rbeg + r) + (size_t)c * lda);
+      cp_async_elem(tile + c * Rp + r, P + (size_t)(rbeg + r) + (size_t)c * lda);
   cp_async_commit();
   for (int r = tid; r < nrows; r += kClusterThreads) label[r] = rbeg + r;
   cp_async_wait<0>();
@@ -110,15 +202,15 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
         // the pending updates, in column order (it may become row k of U)
         const int lr = (int)(0xFFFFFFFFu - (unsigned)(kk & 0xFFFFFFFFull)) - rbeg;
         for (int c = lane; c < JB; c += 32) {
-          float v = tile[c * R + lr];
+          float v = tile[c * Rp + lr];
           if (c > k)
-            for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * R + lr], uh[d][c], v);
+            for (int d = 0; d < s_slot; ++d) v = fnmadd<EXACT>(tile[(kfirst + d) * Rp + lr], uh[d][c], v);
           sl.row[c] = v;
         }
         if (lane == 0) sl.label = label[lr];
       }
       if (k >= rbeg && k < rbeg + nrows) {
-        for (int c = lane; c < JB; c += 32) sl.row_k[c] = tile[c * R + (k - rbeg)];
+        for (int c = lane; c < JB; c += 32) sl.row_k[c] = tile[c * Rp + (k - rbeg)];
         if (lane == 0) sl.row_k_label = label[k - rbeg];
       }
     }
@@ -209,12 +301,12 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
       // updates, which step 6 applies at its new place
       if (k >= rbeg && k < rbeg + nrows) {
         const int lk = k - rbeg;
-        for (int c = lane; c < JB; c += 32) tile[c * R + lk] = urow[c];
+        for (int c = lane; c < JB; c += 32) tile[c * Rp + lk] = urow[c];
         if (lane == 0 && prow != k) label[lk] = win_label_s;
       }
       if (prow != k && own_p) {
         const int lp = prow - rbeg;
-        for (int c = lane; c < JB; c += 32) tile[c * R + lp] = rowk_s[c];
+        for (int c = lane; c < JB; c += 32) tile[c * Rp + lp] = rowk_s[c];
         if (lane == 0) label[lp] = rowk_label_s;
       }
       for (int c = lane; c < JB; c += 32) uh[s_slot][c] = urow[c];
@@ -223,46 +315,13 @@ leaf_panel_cluster_kernel(float* __restrict__ P, int lda, int M, int JB, int R, 
     // 6. scale column k below the pivot; column k+1 receives the pending
     //    updates and this column's at once (its values are the next pivot
     //    candidates); every kDefer columns the later columns receive the
-    //    group's kDefer updates in one pass (one read-modify-write of shared
-    //    memory per element per group instead of per column).  Every element
-    //    still receives its updates in column order.
-    const float pv = pv_s;
-    const bool scale = pv != 0.0f;
-    const bool recip = fabsf(pv) >= Lim<float>::sfmin();
-    const float rp = 1.0f / pv;
-    const bool flush = s_slot == kDefer - 1;
-    float* __restrict__ tl = tile;
-    mykey = 0;
-    for (int r = max(0, k + 1 - rbeg) + tid; r < nrows; r += kClusterThreads) {
-      const float v = tl[k * R + r];
-      const float l = scale ? (recip ? v * rp : v / pv) : v;
-      tl[k * R + r] = l;
-      float ld[kDefer];
-#pragma unroll
-      for (int d = 0; d < kDefer; ++d) ld[d] = d < s_slot ? tl[(kfirst + d) * R + r] : (d == s_slot ? l : 0.0f);
-      if (k + 1 < JB) {
-        float t = tl[(k + 1) * R + r];
-#pragma unroll
-        for (int d = 0; d < kDefer; ++d)
-          if (d <= s_slot) t = fnmadd<EXACT>(ld[d], uh[d][k + 1], t);
-        tl[(k + 1) * R + r] = t;
-        unsigned long long kk = pack_key(t, rbeg + r, k + 1);
-        mykey = kk > mykey ? kk : mykey;
-      }
-      if (flush) {
-        for (int c = k + 2; c < JB; ++c) {
-          float t = tl[c * R + r];
-#pragma unroll
-          for (int d = 0; d < kDefer; ++d) t = fnmadd<EXACT>(ld[d], uh[d][c], t);
-          tl[c * R + r] = t;
-        }
-      }
-    }
+    //    group's kDefer updates in one pass
+    mykey = leaf_update_quads<EXACT>(tile, Rp, k, JB, rbeg, nrows, kfirst, s_slot, uh, pv_s);
   }
   // no CTA may exit while others can still read its shared memory
   cluster.sync();
   for (int c = 0; c < JB; ++c)
-    for (int r = tid; r < nrows; r += kClusterThreads) P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * R + r];
+    for (int r = tid; r < nrows; r += kClusterThreads) P[(size_t)(rbeg + r) + (size_t)c * lda] = tile[c * Rp + r];
   for (int r = tid; r < nrows; r += kClusterThreads) {
     int g = rbeg + r;
     if (g < JB) {
@@ -365,10 +424,6 @@ __device__ __forceinline__ bool cl_wait(uint64_t* bar, uint32_t parity) {
     if (done) return true;
   }
   return false;
-}
-
-__host__ __device__ constexpr int leaf_push_rows(int R) {
-  return ((R + 3) / 4 % 2 == 0) ? (R + 3) / 4 * 4 + 4 : (R + 3) / 4 * 4;
 }
 
 template <bool EXACT, int JBT>
@@ -546,83 +601,8 @@ leaf_panel_cluster_push_kernel(float* __restrict__ P, int lda, int M, int JB, in
     __syncthreads();
     mark(4);
     // 5. scale column k, update column k+1 (the next candidates) and, every
-    //    kDefer columns, the later columns, in the order of
-    //    leaf_panel_cluster_kernel, on groups of four rows (one 16-byte
-    //    access per column); rows at or above k and the padding rows after
-    //    the CTA's last row keep their values
-    const float pv = pv_s;
-    const bool scale = pv != 0.0f;
-    const bool recip = fabsf(pv) >= Lim<float>::sfmin();
-    const float rp = 1.0f / pv;
-    const bool flush = s_slot == kDefer - 1;
-    float* __restrict__ tl = tile;
-    mykey = 0;
-    const int r_lo = k + 1 - rbeg;       // first local row below the diagonal
-    const int nq = (nrows + 3) >> 2;
-    for (int q = max(0, r_lo) / 4 + tid; q < nq; q += kClusterThreads) {
-      const int r0 = 4 * q;
-      bool act[4];
-#pragma unroll
-      for (int e = 0; e < 4; ++e) act[e] = (r0 + e >= r_lo) && (r0 + e < nrows);
-      float4 v = *reinterpret_cast<const float4*>(tl + (size_t)k * Rp + r0);
-      float l[4] = {v.x, v.y, v.z, v.w};
-      if (scale) {
-        if (recip) {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] * rp : l[e];
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) l[e] = act[e] ? l[e] / pv : l[e];
-        }
-        *reinterpret_cast<float4*>(tl + (size_t)k * Rp + r0) = make_float4(l[0], l[1], l[2], l[3]);
-      }
-      float ld[kDefer][4];
-#pragma unroll
-      for (int d = 0; d < kDefer; ++d) {
-        if (d < s_slot) {
-          const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(kfirst + d) * Rp + r0);
-          ld[d][0] = w.x; ld[d][1] = w.y; ld[d][2] = w.z; ld[d][3] = w.w;
-        } else {
-#pragma unroll
-          for (int e = 0; e < 4; ++e) ld[d][e] = d == s_slot ? l[e] : 0.0f;
-        }
-      }
-      if (k + 1 < JB) {
-        const float4 w = *reinterpret_cast<const float4*>(tl + (size_t)(k + 1) * Rp + r0);
-        float t[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-        for (int d = 0; d < kDefer; ++d) {
-          if (d <= s_slot) {
-            const float u = uh[d][k + 1];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
-          }
-        }
-        *reinterpret_cast<float4*>(tl + (size_t)(k + 1) * Rp + r0) = make_float4(t[0], t[1], t[2], t[3]);
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          if (act[e]) {
-            const unsigned long long kk = pack_key(t[e], rbeg + r0 + e, k + 1);
-            mykey = kk > mykey ? kk : mykey;
-          }
-        }
-      }
-      if (flush) {
-#pragma unroll 4
-        for (int c = k + 2; c < JB; ++c) {
-          float* pc = tl + (size_t)c * Rp + r0;
-          const float4 w = *reinterpret_cast<const float4*>(pc);
-          float t[4] = {w.x, w.y, w.z, w.w};
-#pragma unroll
-          for (int d = 0; d < kDefer; ++d) {
-            const float u = uh[d][c];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) t[e] = act[e] ? fnmadd<EXACT>(ld[d][e], u, t[e]) : t[e];
-          }
-          *reinterpret_cast<float4*>(pc) = make_float4(t[0], t[1], t[2], t[3]);
-        }
-      }
-    }
+    //    kDefer columns, the later columns
+    mykey = leaf_update_quads<EXACT>(tile, Rp, k, JB, rbeg, nrows, kfirst, s_slot, uh, pv_s);
     mark(5);
   }
   if (timing)
