@@ -16,6 +16,7 @@ pinned host buffers, the host<->device copies inside the timed region.
 Inputs are synthetic, drawn from numpy's PCG64 with a fixed seed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+    python bench.py --workload batched|adjoint|update|leaf ...   (one configuration or kernel class alone)
 """
 import argparse
 import ctypes
@@ -63,10 +64,13 @@ def parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the per-kappa records (1e2, 1e6, 1e10)")
     p.add_argument("--no-sub", action="store_true", help="skip the batched and adjoint records of the default run")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
-    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint"],
+    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint", "update", "leaf"],
                    help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
     p.add_argument("--dtype", default="d", choices=["d", "s"], help="precision of the batched workload")
     p.add_argument("--batch", type=int, default=20000)
+    p.add_argument("--fixed-n", type=int, default=0, help="batched: every system of this size (0: uniform 8..512)")
+    p.add_argument("--m", type=int, default=8192, help="update / leaf: rows (update: M = N)")
+    p.add_argument("--k", type=int, default=256, help="update: K; leaf: panel width")
     return p.parse_args()
 
 
@@ -595,6 +599,8 @@ def run_batched(args, rank=0, world=1):
     es = 8 if args.dtype == "d" else 4
     rng = np.random.default_rng(args.seed)
     ns = rng.integers(8, 513, args.batch).astype(np.int64)
+    if args.fixed_n > 0:
+        ns[:] = args.fixed_n
     nrhs = rng.choice([1, 2, 4], args.batch).astype(np.int64)
     glob = np.arange(args.batch)                   # global system index of each local system
     if world > 1:
@@ -783,8 +789,91 @@ def run_adjoint(args):
                          "work": "4*n^2*nrhs flop per system"}}
 
 
+def run_kernel_case(args):
+    """One kernel class alone, for timing and profiling: 'update' is the
+    BF16x3 trailing update C -= A B of an M x M matrix with K = k
+    (gb300_sgemm_update_dev, mode 0); 'leaf' is the FP32 LU of one m x k
+    panel (gb300_sgetrf_dev on the panel: one cluster leaf for k up to the
+    leaf width).  Four untimed calls, then `steps` calls timed with CUDA
+    events on the launching stream."""
+    import torch
+    import lapack_gb300 as g
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    s = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    m, k = args.m, args.k
+    if args.workload == "update":
+        A = g.colmajor_empty(m, k, torch.float32)
+        A.copy_(torch.randn(m, k, device=dev, generator=gen))
+        B = g.colmajor_empty(k, m, torch.float32)
+        B.copy_(torch.randn(k, m, device=dev, generator=gen))
+        C = g.colmajor_empty(m, m, torch.float32)
+        C.copy_(torch.randn(m, m, device=dev, generator=gen))
+
+        def call():
+            rc = L.gb300_sgemm_update_dev(0, m, m, k, ctypes.c_void_p(A.data_ptr()), m, ctypes.c_void_p(B.data_ptr()),
+                                          k, ctypes.c_void_p(C.data_ptr()), m, sp)
+            if rc:
+                raise RuntimeError(f"update status {rc}")
+        work = {"bytes": 4.0 * (m * k + k * m + 2.0 * m * m), "flops": 2.0 * m * m * k}
+    else:
+        P0 = g.colmajor_empty(m, k, torch.float32)
+        P0.copy_(torch.rand(m, k, device=dev, generator=gen) * 2 - 1)
+        P = P0.clone()
+        ip = torch.empty(k, dtype=torch.int32, device=dev)
+
+        def call():
+            P.copy_(P0)
+            g.getrf_dev(P, ip)
+        work = {"bytes": 2.0 * 4.0 * m * k, "flops": float(m) * k * k}
+    for _ in range(4):
+        call()
+    torch.cuda.synchronize()
+    # the panel class (the leaf kernel alone) carries events in the leaf case
+    if args.workload == "leaf":
+        L.gb300_prof_reset()
+        L.gb300_prof_mask(1 << 3)
+        L.gb300_prof_enable(1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        call()
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if args.workload == "leaf":
+        L.gb300_prof_enable(0)
+        t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
+        L.gb300_prof_read(3, ctypes.byref(t_ms), ctypes.byref(fl), ctypes.byref(by), ctypes.byref(cnt))
+        L.gb300_prof_reset()
+        L.gb300_prof_mask(0xFFFFFFFF)
+        ms = t_ms.value / max(cnt.value, 1)
+    out = {"workload": args.workload, "m": m, "k": k,
+           "ms_per_call" if args.workload == "update" else "ms_per_leaf_kernel": ms,
+           "algorithmic_gbs": work["bytes"] / ms / 1e6, "tflops": work["flops"] / ms / 1e9,
+           "options": {o: g.get_option(o) for o in ("gemm_ws", "gemm_tiles", "cluster_panel")}}
+    if args.workload == "update":
+        out["tensor_tflops_3_products"] = 3.0 * work["flops"] / ms / 1e9
+    else:
+        # the latency floor of one leaf column: the skeleton of its exchange
+        # (two CTA barriers around a cluster-wide exchange) on one cluster
+        L.gb300_probe_cluster_exchange.restype = ctypes.c_double
+        L.gb300_probe_cluster_exchange.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        out["cluster_exchange_us_per_column"] = {
+            f"{mode}_{ctas}": L.gb300_probe_cluster_exchange(ctas, 0 if mode == "push" else 1, 20000)
+            for mode in ("push", "barrier") for ctas in (16, 8)}
+        out["us_per_column"] = ms * 1e3 / k
+    return out
+
+
 def main():
     args = parse()
+    if args.workload in ("update", "leaf"):
+        print(json.dumps(run_kernel_case(args)))
+        return
     if args.workload == "batched" and args.impl == "gb300":
         world = int(os.environ.get("WORLD_SIZE", "1"))
         rank = int(os.environ.get("RANK", "0"))
