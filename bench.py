@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the per-kappa records (1e2, 1e6, 1e10)")
     p.add_argument("--no-sub", action="store_true", help="skip the batched and adjoint records of the default run")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
-    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint", "update", "leaf"],
+    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint", "update", "leaf", "dgetrf"],
                    help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
     p.add_argument("--dtype", default="d", choices=["d", "s"], help="precision of the batched workload")
     p.add_argument("--batch", type=int, default=20000)
@@ -819,6 +819,16 @@ def run_kernel_case(args):
             if rc:
                 raise RuntimeError(f"update status {rc}")
         work = {"bytes": 4.0 * (m * k + k * m + 2.0 * m * m), "flops": 2.0 * m * m * k}
+    elif args.workload == "dgetrf":
+        A0 = g.colmajor_empty(m, m, torch.float64)
+        A0.copy_(torch.rand(m, m, dtype=torch.float64, device=dev, generator=gen) * 2 - 1)
+        A = A0.clone()
+        ip = torch.empty(m, dtype=torch.int32, device=dev)
+
+        def call():
+            A.copy_(A0)
+            g.getrf_dev(A, ip)
+        work = {"bytes": 2.0 * 8.0 * m * m, "flops": 2.0 / 3.0 * m ** 3}
     else:
         P0 = g.colmajor_empty(m, k, torch.float32)
         P0.copy_(torch.rand(m, k, device=dev, generator=gen) * 2 - 1)
@@ -852,12 +862,12 @@ def run_kernel_case(args):
         L.gb300_prof_mask(0xFFFFFFFF)
         ms = t_ms.value / max(cnt.value, 1)
     out = {"workload": args.workload, "m": m, "k": k,
-           "ms_per_call" if args.workload == "update" else "ms_per_leaf_kernel": ms,
+           ("ms_per_leaf_kernel" if args.workload == "leaf" else "ms_per_call"): ms,
            "algorithmic_gbs": work["bytes"] / ms / 1e6, "tflops": work["flops"] / ms / 1e9,
            "options": {o: g.get_option(o) for o in ("gemm_ws", "gemm_tiles", "cluster_panel")}}
     if args.workload == "update":
         out["tensor_tflops_3_products"] = 3.0 * work["flops"] / ms / 1e9
-    else:
+    elif args.workload == "leaf":
         # the latency floor of one leaf column: the skeleton of its exchange
         # (two CTA barriers around a cluster-wide exchange) on one cluster
         L.gb300_probe_cluster_exchange.restype = ctypes.c_double
@@ -871,7 +881,7 @@ def run_kernel_case(args):
 
 def main():
     args = parse()
-    if args.workload in ("update", "leaf"):
+    if args.workload in ("update", "leaf", "dgetrf"):
         print(json.dumps(run_kernel_case(args)))
         return
     if args.workload == "batched" and args.impl == "gb300":

@@ -104,9 +104,22 @@ template <typename T>
 int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode,
                   bool one_launch = true);   // false: leaf kernel + GEMM only (small shared memory)
 
-// BF16x3 tensor-core update C -= A*B for FP32 operands (tcgen05).
+// The BF16 hi/lo split of an update's A operand (M x Kp bf16 each, K-major),
+// made once by bf16x3_split_a_dev and passed to several updates that share A.
+struct Bf16SplitA {
+  const void* hi = nullptr;
+  const void* lo = nullptr;
+  int M = 0, Kp = 0;
+};
+// Bytes one split of an M x K operand takes (hi and lo, 256-byte aligned).
+size_t bf16x3_split_bytes(int M, int K);
+// Splits A (M x K, column-major) into buf (bf16x3_split_bytes(M, K) bytes).
+int bf16x3_split_a_dev(int M, int K, const float* A, int lda, void* buf, Bf16SplitA* out, cudaStream_t s);
+// BF16x3 tensor-core update C -= A*B for FP32 operands (tcgen05); with
+// a_pre the A operand's split is taken from there instead of made here.
 int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                    cudaStream_t s, bool overwrite = false);   // overwrite: C = A*B
+                    cudaStream_t s, bool overwrite = false,   // overwrite: C = A*B
+                    const Bf16SplitA* a_pre = nullptr);
 
 // DSGESV on device memory.  *iter and *info are host outputs.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,

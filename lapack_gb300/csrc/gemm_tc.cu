@@ -627,25 +627,56 @@ bool make_map_c(CUtensorMap* map, const float* base, int M, int N, int ldc) {
 
 
 
+size_t bf16x3_split_bytes(int M, int K) {
+  const int Kp = (K + kTcBK - 1) / kTcBK * kTcBK;
+  return 2 * (((size_t)M * Kp * 2 + 255) / 256 * 256);
+}
+
+int bf16x3_split_a_dev(int M, int K, const float* A, int lda, void* buf, Bf16SplitA* out, cudaStream_t s) {
+  const int Kp = (K + kTcBK - 1) / kTcBK * kTcBK;
+  const size_t half = ((size_t)M * Kp * 2 + 255) / 256 * 256;
+  __nv_bfloat16* ah = static_cast<__nv_bfloat16*>(buf);
+  __nv_bfloat16* al = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(buf) + half);
+  out->hi = ah;
+  out->lo = al;
+  out->M = M;
+  out->Kp = Kp;
+  if (M <= 0 || K <= 0) return 0;
+  prof_begin(kProfOther, s);
+  dim3 ga((M + 31) / 32, (Kp + 31) / 32);
+  GB_LAUNCH(split_a_kernel<<<ga, 256, 0, s>>>(A, lda, M, K, Kp, ah, al));
+  prof_end(kProfOther, s, 0.0, 4.0 * (double)M * K + 4.0 * (double)M * Kp);
+  return (int)cudaGetLastError();
+}
+
 int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B, int ldb, float* C, int ldc,
-                    cudaStream_t s, bool overwrite) {
+                    cudaStream_t s, bool overwrite, const Bf16SplitA* a_pre) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   const int Kp = (K + kTcBK - 1) / kTcBK * kTcBK;
-  const size_t bytes_a = (size_t)M * Kp * 2, bytes_b = (size_t)N * Kp * 2;
+  if (a_pre && (a_pre->M != M || a_pre->Kp != Kp)) return (int)cudaErrorInvalidValue;
+  const size_t bytes_a = a_pre ? 0 : (size_t)M * Kp * 2, bytes_b = (size_t)N * Kp * 2;
   auto up = [](size_t b) { return (b + 255) / 256 * 256; };
   DevScratch ws(2 * up(bytes_a) + 2 * up(bytes_b), s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
   char* base = ws.as<char>();
-  __nv_bfloat16* ah = reinterpret_cast<__nv_bfloat16*>(base);
-  __nv_bfloat16* al = reinterpret_cast<__nv_bfloat16*>(base + up(bytes_a));
+  const __nv_bfloat16* ah = a_pre ? static_cast<const __nv_bfloat16*>(a_pre->hi) : reinterpret_cast<__nv_bfloat16*>(base);
+  const __nv_bfloat16* al =
+      a_pre ? static_cast<const __nv_bfloat16*>(a_pre->lo) : reinterpret_cast<__nv_bfloat16*>(base + up(bytes_a));
   __nv_bfloat16* bh = reinterpret_cast<__nv_bfloat16*>(base + 2 * up(bytes_a));
   __nv_bfloat16* bl = reinterpret_cast<__nv_bfloat16*>(base + 2 * up(bytes_a) + up(bytes_b));
 
-  prof_begin(kProfGemmBf16x3, s);
-  dim3 ga((M + 31) / 32, (Kp + 31) / 32);
-  GB_LAUNCH(split_a_kernel<<<ga, 256, 0, s>>>(A, lda, M, K, Kp, ah, al));
+  // the operand splits are their own class; the update class brackets the
+  // tensor-core kernel alone (the roofline's per-launch time)
+  prof_begin(kProfOther, s);
+  if (!a_pre) {
+    dim3 ga((M + 31) / 32, (Kp + 31) / 32);
+    GB_LAUNCH(split_a_kernel<<<ga, 256, 0, s>>>(A, lda, M, K, Kp, const_cast<__nv_bfloat16*>(ah),
+                                                const_cast<__nv_bfloat16*>(al)));
+  }
   size_t nb = (size_t)N * Kp;
   GB_LAUNCH(split_b_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, s>>>(B, ldb, K, N, Kp, bh, bl));
+  prof_end(kProfOther, s, 0.0, (a_pre ? 0.0 : 4.0 * (double)M * K + 4.0 * (double)M * Kp) +
+                                   4.0 * (double)N * K + 4.0 * (double)N * Kp);
 
   CUtensorMap m_ah, m_al, m_bh, m_bl;
   if (!make_map(&m_ah, ah, M, Kp, kTcBM) || !make_map(&m_al, al, M, Kp, kTcBM) ||
@@ -659,6 +690,7 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
     GB_CUDA_TRY(cudaFuncSetAttribute(gemm_bf16x3_ws_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kWsSmem));
     attr[dev] = true;
   }
+  prof_begin(kProfGemmBf16x3, s);
   const int tiles_m = (M + kTcBM - 1) / kTcBM, tiles_n = (N + kTcBN - 1) / kTcBN;
   // the warp-specialised kernel stores C by TMA: C and its column stride
   // must be 16-byte aligned, and so must the end of each column (a TMA

@@ -663,6 +663,10 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     cudaStream_t sp = lr->sp;
     int* logs = reinterpret_cast<int*>(base + o_log);
     int* lcnt = reinterpret_cast<int*>(base + o_lcnt);
+    // room for the BF16 hi/lo split of the largest A21 (m rows, nb columns)
+    const bool split_a21 = sizeof(T) == 4 && gemm_mode == kMixedBf16x3;
+    DevScratch a21buf(split_a21 ? bf16x3_split_bytes(m, nb) : 0, s);
+    if (split_a21 && !a21buf.p) return (int)cudaErrorMemoryAllocation;
     GB_CUDA_TRY(cudaEventRecord(lr->fork, s));
     GB_CUDA_TRY(cudaStreamWaitEvent(sp, lr->fork, 0));
     int k = 0;
@@ -687,13 +691,28 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       T* Ajj = dA + j + (size_t)j * lda;
       rc = form_linv<T>(dA, lda, j, jb, linv, s);
       if (rc) return rc;
+      // the BF16 split of A21, made once for both updates of this block column
+      // (stream s orders it after the previous column's updates that read the buffer)
+      const bool presplit = a21buf.p && j2 < m;
+      Bf16SplitA a21;
+      if (presplit) {
+        if constexpr (sizeof(T) == 4) rc = bf16x3_split_a_dev(m - j2, jb, Ajj + jb, lda, a21buf.p, &a21, s);
+        if (rc) return rc;
+      }
+      auto update = [&](int ncols, int coff) -> int {
+        if constexpr (sizeof(T) == 4) {
+          if (presplit)
+            return gemm_bf16x3_dev(m - j2, ncols, jb, Ajj + jb, lda, Ajj + (size_t)coff * lda, lda,
+                                   Ajj + jb + (size_t)coff * lda, lda, s, false, &a21);
+        }
+        return gemm_update_dev<T>(m - j2, ncols, jb, Ajj + jb, lda, Ajj + (size_t)coff * lda, lda,
+                                  Ajj + jb + (size_t)coff * lda, lda, s, gemm_mode);
+      };
       // next block column first
       if (nb2 > 0) {
         rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
         if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, linv, s, gemm_mode);
-        if (!rc && j2 < m)
-          rc = gemm_update_dev<T>(m - j2, nb2, jb, Ajj + jb, lda, Ajj + (size_t)jb * lda, lda,
-                                  Ajj + jb + (size_t)jb * lda, lda, s, gemm_mode);
+        if (!rc && j2 < m) rc = update(nb2, jb);
         if (rc) return rc;
       }
       GB_CUDA_TRY(cudaEventRecord(lr->L[b], s));
@@ -702,9 +721,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       rc = laswp_log<T>(dA, lda, 0, j, c2, n, cx, cx.perm, s);
       if (!rc && c2 < n) {
         rc = block_row_u<T>(dA, lda, j, jb, c2, n, linv, s, gemm_mode);
-        if (!rc && j2 < m)
-          rc = gemm_update_dev<T>(m - j2, n - c2, jb, Ajj + jb, lda, Ajj + (size_t)(c2 - j) * lda, lda,
-                                  Ajj + jb + (size_t)(c2 - j) * lda, lda, s, gemm_mode);
+        if (!rc && j2 < m) rc = update(n - c2, c2 - j);
       }
       if (rc) return rc;
     }
