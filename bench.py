@@ -854,6 +854,7 @@ def run_kernel_case(args):
     e1.record(s)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
+    ms_call = ms
     if args.workload == "leaf":
         L.gb300_prof_enable(0)
         t_ms, fl, by, cnt = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_longlong()
@@ -876,6 +877,8 @@ def run_kernel_case(args):
             f"{mode}_{ctas}": L.gb300_probe_cluster_exchange(ctas, 0 if mode == "push" else 1, 20000)
             for mode in ("push", "barrier") for ctas in (16, 8)}
         out["us_per_column"] = ms * 1e3 / k
+        # the whole panel call: its leaves, the solves and updates between them
+        out["ms_per_panel_call"] = ms_call
     return out
 
 

@@ -1290,6 +1290,7 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "lookahead")) { old = o.lookahead; o.lookahead = value; }
   else if (!strcmp(name, "trsv_inv")) { old = o.trsv_inv; o.trsv_inv = value; }
   else if (!strcmp(name, "gemm_ws")) { old = o.gemm_ws; o.gemm_ws = value; }
+  else if (!strcmp(name, "panel_fuse")) { old = o.panel_fuse; o.panel_fuse = value; }
   else if (!strcmp(name, "gemm_tiles")) { old = o.gemm_tiles; o.gemm_tiles = std::max(0, value); }
   else if (!strcmp(name, "ir_nan_guard")) { old = o.ir_nan_guard; o.ir_nan_guard = value != 0; }
   else return -1;
@@ -1308,6 +1309,7 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "lookahead")) return o.lookahead;
   if (!strcmp(name, "trsv_inv")) return o.trsv_inv;
   if (!strcmp(name, "gemm_ws")) return o.gemm_ws;
+  if (!strcmp(name, "panel_fuse")) return o.panel_fuse;
   if (!strcmp(name, "gemm_tiles")) return o.gemm_tiles;
   if (!strcmp(name, "ir_nan_guard")) return o.ir_nan_guard;
   return -1;

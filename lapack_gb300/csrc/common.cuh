@@ -181,9 +181,35 @@ __device__ __forceinline__ void cp_async_elem(T* smem_dst, const T* gsrc) {
   else
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(gsrc) : "memory");
 }
+// The same with zero fill: `valid` false writes zeros and reads nothing
+// (gsrc must still be a mapped address).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem_zfill(T* smem_dst, const T* gsrc, bool valid) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  const int n = valid ? (int)sizeof(T) : 0;
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(d), "l"(gsrc), "r"(n) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(gsrc), "r"(n) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Stages a rows x cols column-major block (leading dimension ld) into shared
+// memory at dst[c * ldd + r] with cp.async: warp w takes columns w, w + NT/32,
+// ..., its lanes consecutive rows (coalesced reads, no index division).
+// The caller commits and waits.
+template <typename T, int NT>
+__device__ __forceinline__ void stage_cols_async(const T* __restrict__ src, int ld, int rows, int cols,
+                                                 T* __restrict__ dst, int ldd, int tid) {
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int c = warp; c < cols; c += NT / 32) {
+    const T* s = src + (size_t)c * ld;
+    T* d = dst + (size_t)c * ldd;
+    for (int r = lane; r < rows; r += 32) cp_async_elem(d + r, s + r);
+  }
+}
 
 
 }  // namespace gb

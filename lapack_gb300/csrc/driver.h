@@ -26,6 +26,7 @@ struct Options {
   int gemm_ws = 1;                // BF16x3 update: 1 warp-specialised multi-tile kernel, 0 one tile per CTA
   int gemm_tiles = 4;             // tiles per CTA of the warp-specialised update (0: one CTA per SM)
   int ir_nan_guard = 0;           // DSGESV: a non-finite iterate or residual ends the refinement (ITER = -2)
+  int panel_fuse = 1;             // panel recursion: a node with halves <= 64 columns as one fused launch
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 
@@ -100,6 +101,11 @@ int laswp_dev(int ncols, T* dA, int lda, int k1, int k2, const int* dIpiv, int i
 template <typename T>
 int gemm_update_dev(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                     cudaStream_t s, int gemm_mode);
+// One node of the panel recursion in one launch (k, nc <= 64): U12 =
+// L11^{-1} A12 and A22 -= A21 U12, bitwise as trsm_llnu_dev + the FFMA / DFMA
+// update.  *node_count: a zeroed device int, left zeroed.
+template <typename T>
+int panel_node_dev(T* A11, int lda, int M, int k, int nc, int* node_count, cudaStream_t s);
 template <typename T>
 int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode,
                   bool one_launch = true);   // false: leaf kernel + GEMM only (small shared memory)

@@ -40,6 +40,7 @@ Options& options() {
     x.gemm_ws = env_int("LAPACK_GB300_GEMM_WS", 1);
     x.gemm_tiles = std::max(0, env_int("LAPACK_GB300_GEMM_TILES", 4));
     x.ir_nan_guard = env_int("LAPACK_GB300_IR_NAN_GUARD", 0);
+    x.panel_fuse = env_int("LAPACK_GB300_PANEL_FUSE", 1);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -165,6 +166,7 @@ struct PanelCtx {
   int* log_src = nullptr;
   int* log_cnt = nullptr;   // [kMaxLogSlots], zeroed before the block column
   PairLogArgs log{};
+  int* node_count = nullptr;   // arrival counter of the fused panel-node kernel (zero between launches)
 };
 
 template <typename T, bool EXACT>
@@ -346,7 +348,9 @@ static int launch_leaf_cluster_reg(float* P, int lda, int M, int jb, int row0, i
   }
   const int R = (M + kClusterCtas - 1) / kClusterCtas;
   if (R > (64 / JB) * kClusterThreads || jb > JB) return 1000 + kStatusCapacity;
-  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
+  // with the interchange log the pair count is this leaf's slot of the
+  // block column's counters, zeroed with them before the block column
+  if (!cx.logging) GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
   cudaLaunchConfig_t cfg = {};
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -418,7 +422,9 @@ static int launch_leaf_cluster_p(float* P, int lda, int M, int JB, int row0, int
   const int Rs = leaf_push_rows(R);      // both shared-memory leaves pad their rows
   size_t smem = (size_t)JB * Rs * 4 + (size_t)Rs * 4 + 16;
   if (!c.ok || (long long)smem > c.dyn_cap || JB > 64) return 1000 + kStatusCapacity;
-  GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
+  // with the interchange log the pair count is this leaf's slot of the
+  // block column's counters, zeroed with them before the block column
+  if (!cx.logging) GB_CUDA_TRY(cudaMemsetAsync(cx.ps.pair_count, 0, sizeof(int), s));
   prof_begin(kProfPanel, s);
   int rc;
   if (JB <= 8) rc = launch_leaf_cluster_w<EXACT, 8, PUSH>(P, lda, M, JB, R, smem, row0, ipiv, info, cx, s, c.dyn_cap);
@@ -510,10 +516,15 @@ static int getrf_rec(T* A, int lda, int m, int n, int c0, int w, int* ipiv, int*
   // FMA kernel: one launch, no operand split, K <= 64 would be padded to a
   // full BF16 K block anyway
   const int gm = (gemm_mode == kMixedBf16x3 && w - n1 <= 64) ? kMixedFp32 : gemm_mode;
-  rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gm, false);
-  if (rc) return rc;
-  rc = gemm_update_dev<T>(m - c0 - n1, w - n1, n1, A11 + n1, lda, A11 + (size_t)n1 * lda, lda,
-                          A11 + n1 + (size_t)n1 * lda, lda, s, gm);
+  if (options().panel_fuse && n1 <= 64 && w - n1 <= 64 && (sizeof(T) == 8 || gm == kMixedFp32)) {
+    // the solve and the narrow update of this node in one launch (same arithmetic)
+    rc = panel_node_dev<T>(A11, lda, m - c0, n1, w - n1, cx.node_count, s);
+  } else {
+    rc = trsm_llnu_dev<T>(n1, w - n1, A11, lda, A11 + (size_t)n1 * lda, lda, s, gm, false);
+    if (rc) return rc;
+    rc = gemm_update_dev<T>(m - c0 - n1, w - n1, n1, A11 + n1, lda, A11 + (size_t)n1 * lda, lda,
+                            A11 + n1 + (size_t)n1 * lda, lda, s, gm);
+  }
   if (rc) return rc;
   return getrf_rec<T>(A, lda, m, n, c0 + n1, w - n1, ipiv, info, cx, s, gemm_mode);
 }
@@ -616,6 +627,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   size_t o_log = carve(sizeof(int) * 4 * log_ints);
   size_t o_lcnt = carve(sizeof(int) * 2 * kMaxLogSlots);
   size_t o_linv = carve(sizeof(T) * 256 * 256);
+  size_t o_node = carve(sizeof(int));
   DevScratch ws(bytes, s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
   char* base = ws.as<char>();
@@ -634,6 +646,8 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   cx.status = device_status_word();
   cx.max_optin = optin;
   if (!cx.status) return (int)cudaErrorMemoryAllocation;
+  cx.node_count = reinterpret_cast<int*>(base + o_node);
+  GB_CUDA_TRY(cudaMemsetAsync(cx.node_count, 0, sizeof(int), s));
 
   const int mn = std::min(m, n);
   if (nb < 1) nb = 1;

@@ -385,71 +385,135 @@ laswp_log_kernel(T* __restrict__ A, int lda, int a0, int a1, int b0, int b1, con
   }
 }
 
-// B := L^{-1} B for a unit lower triangular L (k x k, k <= 64) and B of k
-// rows.  Four lanes per column of B: lane s of a group holds rows s, s+4,
-// s+8, ... of that column in registers; at step kk the lane holding row kk
-// broadcasts it with a shuffle and every lane updates its rows below kk --
-// forward substitution in the reference order (BLAS/SRC/dtrsm.f:290-300:
-// for each k, rows below k get B(i,j) - B(k,j)*A(i,k)) with no block
-// barriers inside the solve.  L is staged in shared memory (padded rows).
-constexpr int kTrsmThreads = 256;
-constexpr int kTrsmCols = kTrsmThreads / 4;
-
-template <typename T, int KMAX>
-constexpr int trsm_leaf_smem() {
-  return (KMAX * (KMAX + 1) + KMAX * (kTrsmCols + 1)) * (int)sizeof(T);
+// Forward substitution X := L^{-1} X for a unit lower triangular L (k x k)
+// and nc columns of X kept column-major in shared memory (element (i, c) at
+// X[c * ldx + i], ldx a multiple of 16 bytes, rows allocated up to k
+// rounded up to 8), LPC adjacent lanes per column, in blocks of 8 rows.
+// Lane `sub` of a column owns the row blocks I with I % LPC == sub; at step
+// J the owner of block J solves its 8 x 8 diagonal block in registers, and
+// after a warp barrier every lane subtracts L(I, J) x_J from each of its
+// blocks I > J.  Blocks of X and columns of L (Lt[j * ldt + i] = L(i, j),
+// ldt a multiple of 8) move in 16-byte vectors.  The loops over the blocks
+// are real loops: their unrolled bodies are a few hundred instructions
+// that stay in the instruction cache (a fully unrolled 64-row solve is
+// thousands of straight-line instructions fetched once per launch, which
+// cost more than the arithmetic).  Per element the updates run in
+// increasing j, x_i := x_i - x_j * L(i, j), the order of
+// BLAS/SRC/dtrsm.f:290-300.  Rows i >= k of the padded blocks hold whatever
+// shared memory holds and are never stored.  Every thread of the block
+// calls this (tid < LPC * ncolumns-per-block); lanes of columns >= nc only
+// keep the warp barriers.
+template <typename T>
+__device__ __forceinline__ void ld8_shared(const T* __restrict__ p, T (&v)[8]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0], b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const double2 q = reinterpret_cast<const double2*>(p)[u];
+      v[2 * u] = q.x;
+      v[2 * u + 1] = q.y;
+    }
+  }
+}
+template <typename T>
+__device__ __forceinline__ void st8_shared(T* __restrict__ p, const T (&v)[8]) {
+  if constexpr (sizeof(T) == 4) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(v[0], v[1], v[2], v[3]);
+    reinterpret_cast<float4*>(p)[1] = make_float4(v[4], v[5], v[6], v[7]);
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) reinterpret_cast<double2*>(p)[u] = make_double2(v[2 * u], v[2 * u + 1]);
+  }
 }
 
-template <typename T, bool EXACT, int KMAX>
-__global__ void __launch_bounds__(kTrsmThreads)
-trsm_llnu_leaf_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int ldb, int k, int ncols) {
-  constexpr int RPL = KMAX / 4;                              // rows per lane
-  extern __shared__ __align__(16) unsigned char trsm_smem[];
-  T* Ls = reinterpret_cast<T*>(trsm_smem);                  // Ls[i * (KMAX+1) + j] = L(i, j)
-  T* Bs = Ls + KMAX * (KMAX + 1);                           // [KMAX][kTrsmCols + 1]
-  const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * kTrsmCols;
-  const int nc = min(kTrsmCols, ncols - c0);
-  // stage L (k x k) and this CTA's columns of B, loads batched per thread
-  batched_copy<8, kTrsmThreads, T>(
-      k * k, tid, [&](int e) { const int c = e / k, r = e - c * k; return L[(size_t)r + (size_t)c * ldl]; },
-      [&](int e, T v) { const int c = e / k, r = e - c * k; Ls[r * (KMAX + 1) + c] = v; });
-  batched_copy<8, kTrsmThreads, T>(
-      k * nc, tid, [&](int e) { const int c = e / k, r = e - c * k; return B[(size_t)r + (size_t)(c0 + c) * ldb]; },
-      [&](int e, T v) { const int c = e / k, r = e - c * k; Bs[r * (kTrsmCols + 1) + c] = v; });
-  __syncthreads();
-  const int col = tid >> 2, sub = tid & 3;
-  const unsigned gmask = 0xFu << ((tid & 31) & ~3);
-  T x[RPL];
+template <typename T, bool EXACT, int LPC>
+__device__ __forceinline__ void solve_unit_lower_cols(const T* __restrict__ Lt, int ldt, T* __restrict__ X, int ldx,
+                                                      int k, int nc, int tid) {
+  static_assert(LPC == 4 || LPC == 8 || LPC == 16, "lanes per column: 4, 8 or 16");
+  const int col = tid / LPC, sub = tid % LPC;
+  const bool act = col < nc;
+  const int nblk = (k + 7) / 8;
+  T* xc = X + (size_t)(act ? col : 0) * ldx;
+  for (int J = 0; J < nblk; ++J) {
+    const int j0 = 8 * J;
+    T xj[8];
+    if (act && J % LPC == sub) {
+      // the diagonal block
+      ld8_shared<T>(xc + j0, xj);
 #pragma unroll
-  for (int t = 0; t < RPL; ++t) {
-    const int i = sub + 4 * t;
-    x[t] = (col < nc && i < k) ? Bs[i * (kTrsmCols + 1) + col] : T(0);
-  }
+      for (int jj = 0; jj < 7; ++jj) {
+        T l[8];
+        ld8_shared<T>(Lt + (size_t)(j0 + jj) * ldt + j0, l);
 #pragma unroll
-  for (int kk = 0; kk < KMAX - 1; ++kk) {
-    if (kk < k - 1) {
-      const T xk = __shfl_sync(0xffffffffu, x[kk / 4], ((tid & 31) & ~3) | (kk & 3));
-      (void)gmask;
+        for (int ii = jj + 1; ii < 8; ++ii) xj[ii] = fnmadd<EXACT>(xj[jj], l[ii], xj[ii]);
+      }
+      st8_shared<T>(xc + j0, xj);
+    }
+    __syncwarp();
+    if (act) {
+      ld8_shared<T>(xc + j0, xj);
+      // this lane's blocks below J: the first I > J with I % LPC == sub
+      for (int I = J + 1 + ((sub - J - 1) & (LPC - 1)); I < nblk; I += LPC) {
+        const int i0 = 8 * I;
+        T xi[8];
+        ld8_shared<T>(xc + i0, xi);
 #pragma unroll
-      for (int t = 0; t < RPL; ++t) {
-        const int i = sub + 4 * t;
-        if (i > kk && i < k) x[t] = fnmadd<EXACT>(xk, Ls[i * (KMAX + 1) + kk], x[t]);
+        for (int jj = 0; jj < 8; ++jj) {
+          T l[8];
+          ld8_shared<T>(Lt + (size_t)(j0 + jj) * ldt + i0, l);
+#pragma unroll
+          for (int ii = 0; ii < 8; ++ii) xi[ii] = fnmadd<EXACT>(xj[jj], l[ii], xi[ii]);
+        }
+        st8_shared<T>(xc + i0, xi);
       }
     }
+    __syncwarp();
   }
-  if (col < nc) {
-#pragma unroll
-    for (int t = 0; t < RPL; ++t) {
-      const int i = sub + 4 * t;
-      if (i < k) Bs[i * (kTrsmCols + 1) + col] = x[t];
-    }
-  }
+}
+
+// Leading dimensions of the staged blocks: L by columns (k rounded up to
+// 8) and the columns of X, padded by 16 bytes so that neighbouring columns
+// start in different banks.
+__host__ __device__ constexpr int trsm_ldt(int k) { return (k + 7) / 8 * 8; }
+template <typename T>
+__host__ __device__ constexpr int trsm_ldx(int k) { return trsm_ldt(k) + 16 / (int)sizeof(T); }
+
+// B := L^{-1} B for a unit lower triangular L (k x k, k <= kTrsmLeafMax)
+// and B of k rows (the panel's U12 = L11^{-1} A12, SRC/dgetrf2.f:240): L
+// and this CTA's 256 / LPC columns of B are staged in shared memory by
+// cp.async, then solved LPC lanes per column (solve_unit_lower_cols).
+// More lanes per column for taller L: more warps share the k-step chain.
+constexpr int kTrsmThreads = 256;
+constexpr int kTrsmLeafMax = 128;
+
+template <typename T>
+__host__ __device__ constexpr int trsm_leaf_smem(int k, int lpc) {
+  return (trsm_ldt(k) * trsm_ldt(k) + trsm_ldx<T>(k) * (kTrsmThreads / lpc)) * (int)sizeof(T);
+}
+
+template <typename T, bool EXACT, int LPC>
+__global__ void __launch_bounds__(kTrsmThreads)
+trsm_llnu_leaf_kernel(const T* __restrict__ L, int ldl, T* __restrict__ B, int ldb, int k, int ncols) {
+  constexpr int CPB = kTrsmThreads / LPC;                   // columns per CTA
+  extern __shared__ __align__(16) unsigned char trsm_smem[];
+  const int ldt = trsm_ldt(k), ldx = trsm_ldx<T>(k);
+  T* Lt = reinterpret_cast<T*>(trsm_smem);                  // Lt[j * ldt + i] = L(i, j)
+  T* Bs = Lt + ldt * ldt;                                   // Bs[c * ldx + i] = B(i, c0 + c)
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * CPB;
+  const int nc = min(CPB, ncols - c0);
+  stage_cols_async<T, kTrsmThreads>(L, ldl, k, k, Lt, ldt, tid);
+  stage_cols_async<T, kTrsmThreads>(B + (size_t)c0 * ldb, ldb, k, nc, Bs, ldx, tid);
+  cp_async_commit();
+  cp_async_wait<0>();
   __syncthreads();
-  for (int e = tid; e < k * nc; e += kTrsmThreads) {
-    const int c = e / k, r = e - c * k;
-    B[(size_t)r + (size_t)(c0 + c) * ldb] = Bs[r * (kTrsmCols + 1) + c];
-  }
+  solve_unit_lower_cols<T, EXACT, LPC>(Lt, ldt, Bs, ldx, k, nc, tid);
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int c = warp; c < nc; c += kTrsmThreads / 32)
+    for (int r = lane; r < k; r += 32) B[(size_t)r + (size_t)(c0 + c) * ldb] = Bs[c * ldx + r];
 }
 
 // The same solve for k up to KMAX = 128 or 256 in one launch (the block

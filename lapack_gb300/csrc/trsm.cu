@@ -10,30 +10,30 @@
 namespace gb {
 
 // ------------------------------------------------------------------- TRSM
-template <typename T, bool EXACT, int KMAX>
-static int launch_trsm_leaf_k(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
+template <typename T, bool EXACT, int LPC>
+static int launch_trsm_leaf_l(const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
   static bool attr[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
   if (!attr[dev]) {
-    GB_CUDA_TRY(cudaFuncSetAttribute(trsm_llnu_leaf_kernel<T, EXACT, KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     trsm_leaf_smem<T, KMAX>()));
+    GB_CUDA_TRY(cudaFuncSetAttribute(trsm_llnu_leaf_kernel<T, EXACT, LPC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     trsm_leaf_smem<T>(kTrsmLeafMax, LPC)));
     attr[dev] = true;
   }
-  GB_LAUNCH(trsm_llnu_leaf_kernel<T, EXACT, KMAX><<<grid, kTrsmThreads, trsm_leaf_smem<T, KMAX>(), s>>>(L, ldl, B, ldb,
+  constexpr int cpb = kTrsmThreads / LPC;
+  const int grid = (ncols + cpb - 1) / cpb;
+  GB_LAUNCH(trsm_llnu_leaf_kernel<T, EXACT, LPC><<<grid, kTrsmThreads, trsm_leaf_smem<T>(k, LPC), s>>>(L, ldl, B, ldb,
                                                                                                      k, ncols));
   return 0;
 }
 
-// the unrolled solve is sized to the leaf: 16, 32 or 64 rows
+// lanes per column follow the height of L: one 8-row block per lane and step
 template <typename T, bool EXACT>
-static int launch_trsm_leaf(int grid, const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
+static int launch_trsm_leaf(const T* L, int ldl, T* B, int ldb, int k, int ncols, cudaStream_t s) {
   prof_begin(kProfTrsm, s);
-  int rc;
-  if (k <= 16) rc = launch_trsm_leaf_k<T, EXACT, 16>(grid, L, ldl, B, ldb, k, ncols, s);
-  else if (k <= 32) rc = launch_trsm_leaf_k<T, EXACT, 32>(grid, L, ldl, B, ldb, k, ncols, s);
-  else rc = launch_trsm_leaf_k<T, EXACT, 64>(grid, L, ldl, B, ldb, k, ncols, s);
-  return rc;
+  if (k > 64) return launch_trsm_leaf_l<T, EXACT, 16>(L, ldl, B, ldb, k, ncols, s);
+  if (k > 32) return launch_trsm_leaf_l<T, EXACT, 8>(L, ldl, B, ldb, k, ncols, s);
+  return launch_trsm_leaf_l<T, EXACT, 4>(L, ldl, B, ldb, k, ncols, s);
 }
 
 // One-launch solve for 64 < k <= KMAX: LPC lanes per column, 16 when the
@@ -67,10 +67,12 @@ static int launch_trsm_tri(const T* L, int ldl, T* B, int ldb, int k, int ncols,
   return rc;
 }
 
-// B := L^{-1} B, L unit lower k x k: leaves of at most 64 rows, one launch
-// up to 256 rows (FP32) or 128 rows (FP64), GEMM for the coupling beyond.
-// one_launch = false keeps to the leaf kernel and the GEMM (small shared
-// memory footprint: the panel's solves run beside the trailing update).
+// B := L^{-1} B, L unit lower k x k: one leaf launch up to 128 rows (4 to
+// 16 lanes per column, 8-row blocks); with one_launch, the packed-triangle
+// kernel for 64 < k <= 256 (FP32) or 128 (FP64), whose several lanes per
+// column suit the wide block row of U; GEMM for the coupling beyond.
+// one_launch = false keeps to the leaf kernel and the GEMM (the panel's
+// solves, which run beside the trailing update).
 template <typename T>
 int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStream_t s, int gemm_mode,
                   bool one_launch) {
@@ -88,15 +90,14 @@ int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStre
     if (rc) return rc;
     return (int)cudaGetLastError();
   }
-  if (k <= kLeafMax) {
-    int grid = (ncols + kTrsmCols - 1) / kTrsmCols;
-    int rc = options().exact ? launch_trsm_leaf<T, true>(grid, L, ldl, B, ldb, k, ncols, s)
-                             : launch_trsm_leaf<T, false>(grid, L, ldl, B, ldb, k, ncols, s);
+  if (k <= kTrsmLeafMax) {
+    int rc = options().exact ? launch_trsm_leaf<T, true>(L, ldl, B, ldb, k, ncols, s)
+                             : launch_trsm_leaf<T, false>(L, ldl, B, ldb, k, ncols, s);
     if (rc) return rc;
     prof_end(kProfTrsm, s, (double)k * k * ncols, sizeof(T) * ((double)k * k + 2.0 * k * ncols));
     return (int)cudaGetLastError();
   }
-  const int kone = (one_launch ? (sizeof(T) == 4 ? 256 : 128) : kLeafMax);   // largest single solve
+  const int kone = (one_launch ? (sizeof(T) == 4 ? 256 : 128) : kTrsmLeafMax);   // largest single solve
   int k1 = ((k / 2) + kLeafMax - 1) / kLeafMax * kLeafMax;
   if (k1 > kone) k1 = kone;
   if (k1 >= k) k1 = kLeafMax;
@@ -108,6 +109,7 @@ int trsm_llnu_dev(int k, int ncols, const T* L, int ldl, T* B, int ldb, cudaStre
 }
 template int trsm_llnu_dev<double>(int, int, const double*, int, double*, int, cudaStream_t, int, bool);
 template int trsm_llnu_dev<float>(int, int, const float*, int, float*, int, cudaStream_t, int, bool);
+
 
 }  // namespace gb
 
