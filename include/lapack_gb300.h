@@ -450,6 +450,16 @@ int gb300_vbatched_profile_read(unsigned long long* cycles);
  * after it, [5] the update.  gb300_leaf_profile_read copies the six sums
  * and clears them.  Returns the previous switch / 0, or -1. */
 int gb300_leaf_profile(int on);
+/* Timeline of the host-pointer DSGESV's fed factorization (test and bench
+ * hook, no reference counterpart): with gb300_feed_trace(1) later calls
+ * record, on the device, the start of the copies (kind 3), each chunk
+ * landed and converted (kind 2, idx = chunk), each chunk taken into the
+ * factorization (kind 1, idx = chunk, aux = the block-column step it
+ * joined at) and each step's end (kind 0, idx = step, aux = columns taken
+ * in); gb300_feed_trace_read returns up to cap records with their times in
+ * ms after the first (waits for the last), or -1. */
+int gb300_feed_trace(int on);
+int gb300_feed_trace_read(int* kind, int* idx, int* aux, double* ms, int cap);
 int gb300_leaf_profile_read(unsigned long long* cycles);
 
 /* Adjoint of X = A^{-1} B from the stored factors (no reference counterpart;
@@ -484,6 +494,17 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * multi-tile kernel; 0: one 128 x 128 tile per CTA), "gemm_tiles" (tiles
  * each CTA of the warp-specialised update takes, 4 by default; 0: one CTA
  * per SM),
+ * "panel_fuse" (1: a node of the panel recursion whose halves are at most
+ * 64 columns, U12 = L11^-1 A12 and A22 -= A21 U12, runs as one launch; 0:
+ * two; bitwise the same), "feed" (1: the host-pointer dsgesv_ copies A in
+ * column chunks on a second stream while the FP32 factorization takes each
+ * chunk in as it lands; 0: the whole copy first; bitwise the same),
+ * "feed_lazy" (1: a landed chunk is taken in only when the factorization
+ * needs it, which brings it up to date block column by block column; a
+ * test setting), "pool_keep" (1: the device's stream-ordered memory pool,
+ * which this library's scratch comes from, keeps the memory it has grown to
+ * for the rest of the process instead of returning it at every
+ * synchronisation; read when the library first allocates on a device),
  * "ir_nan_guard" (0, the default, keeps DSGESV's stopping test exactly:
  * a residual of NaNs passes it, because RNRM.GT.XNRM*CTE is false for a
  * NaN (SRC/dsgesv.f:384-389), so a refinement that overflowed returns its

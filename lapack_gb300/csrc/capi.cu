@@ -506,11 +506,19 @@ void dsgesv_(const lapack_int* n, const lapack_int* nrhs, double* a, const lapac
   double* dX = cv.at<double>(oX);
   int* dP = cv.at<int>(oP);
   int it = 0, inf = 0;
-  gb::prof_begin(gb::kProfCopyH2D, s);
-  int rc = h2d(dA, ld, a, *lda, N, N, s);
-  if (!rc) rc = h2d(dB, ld, b, *ldb, N, R, s);
-  gb::prof_end(gb::kProfCopyH2D, s, 0.0, 8.0 * (double)N * (N + R));
-  if (!rc) rc = gb::dsgesv_dev(N, R, dA, ld, dP, dB, ld, dX, ld, &it, &inf, s);
+  int rc;
+  if (gb::options().feed) {
+    // A and B are copied inside: A in column chunks that the FP32
+    // factorization takes in as they land
+    const gb::HostOperands host{a, *lda, b, *ldb};
+    rc = gb::dsgesv_dev(N, R, dA, ld, dP, dB, ld, dX, ld, &it, &inf, s, &host);
+  } else {
+    gb::prof_begin(gb::kProfCopyH2D, s);
+    rc = h2d(dA, ld, a, *lda, N, N, s);
+    if (!rc) rc = h2d(dB, ld, b, *ldb, N, R, s);
+    gb::prof_end(gb::kProfCopyH2D, s, 0.0, 8.0 * (double)N * (N + R));
+    if (!rc) rc = gb::dsgesv_dev(N, R, dA, ld, dP, dB, ld, dX, ld, &it, &inf, s);
+  }
   if (!rc) rc = finish(s);
   // A is returned unchanged when ITER >= 0 and holds the FP64 LU otherwise
   gb::prof_begin(gb::kProfCopyD2H, s);
@@ -1291,6 +1299,9 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "trsv_inv")) { old = o.trsv_inv; o.trsv_inv = value; }
   else if (!strcmp(name, "gemm_ws")) { old = o.gemm_ws; o.gemm_ws = value; }
   else if (!strcmp(name, "panel_fuse")) { old = o.panel_fuse; o.panel_fuse = value; }
+  else if (!strcmp(name, "feed")) { old = o.feed; o.feed = value; }
+  else if (!strcmp(name, "feed_lazy")) { old = o.feed_lazy; o.feed_lazy = value; }
+  else if (!strcmp(name, "pool_keep")) { old = o.pool_keep; o.pool_keep = value; }
   else if (!strcmp(name, "gemm_tiles")) { old = o.gemm_tiles; o.gemm_tiles = std::max(0, value); }
   else if (!strcmp(name, "ir_nan_guard")) { old = o.ir_nan_guard; o.ir_nan_guard = value != 0; }
   else return -1;
@@ -1310,6 +1321,9 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "trsv_inv")) return o.trsv_inv;
   if (!strcmp(name, "gemm_ws")) return o.gemm_ws;
   if (!strcmp(name, "panel_fuse")) return o.panel_fuse;
+  if (!strcmp(name, "feed")) return o.feed;
+  if (!strcmp(name, "feed_lazy")) return o.feed_lazy;
+  if (!strcmp(name, "pool_keep")) return o.pool_keep;
   if (!strcmp(name, "gemm_tiles")) return o.gemm_tiles;
   if (!strcmp(name, "ir_nan_guard")) return o.ir_nan_guard;
   return -1;

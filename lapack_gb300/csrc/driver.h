@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstddef>
+#include <functional>
 
 namespace gb {
 
@@ -27,6 +28,9 @@ struct Options {
   int gemm_tiles = 4;             // tiles per CTA of the warp-specialised update (0: one CTA per SM)
   int ir_nan_guard = 0;           // DSGESV: a non-finite iterate or residual ends the refinement (ITER = -2)
   int panel_fuse = 1;             // panel recursion: a node with halves <= 64 columns as one fused launch
+  int feed = 1;                   // host-pointer DSGESV: copy A in column chunks beside the FP32 factorization
+  int feed_lazy = 0;              // take a landed chunk in only when the factorization needs it (more catch-up)
+  int pool_keep = 1;              // the stream-ordered pool keeps its memory between calls (set at first use)
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 
@@ -44,12 +48,34 @@ struct DevScratch {
   template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Columns of the matrix that reach the device while it is being factored
+// (the host-pointer DSGESV copies A in column chunks beside the FP32
+// factorization).  Chunk q covers columns [cols[q], cols[q+1]) and is in
+// the matrix, in the original row order, once event ready[q] has
+// completed.  When the factorization takes chunk q in, it calls
+// admit(q, dPerm, s), which queues on s the reordering of the chunk's rows
+// by the gather permutation of the interchanges so far, and then
+// rejected(q), which may block until the chunk's data are known and
+// returns true when they cannot be factored (DSGESV: an entry overflows
+// FP32); the factorization then returns kFeedStop.
+struct ColumnFeed {
+  int nchunks = 0;
+  const int* cols = nullptr;             // nchunks + 1 column boundaries
+  const cudaEvent_t* ready = nullptr;    // nchunks events
+  std::function<int(int, const int*, cudaStream_t)> admit;
+  std::function<bool(int)> rejected;
+};
+constexpr int kFeedStop = 2000;
+// A timing mark for the optional timeline of fed factorizations (no-op unless on).
+void feed_trace_mark(int kind, int idx, int aux, cudaStream_t s);
+
 // Device-pointer routines.  Return 0 or a CUDA / status error code; the
 // LAPACK INFO goes to the device int *dInfo.  All work is queued on `s`.
 // dPerm (optional, m ints): receives the gather permutation of P*A.
+// feed (FP32, needs dPerm): columns arriving during the factorization.
 template <typename T>
 int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb,
-              int* dPerm = nullptr);
+              int* dPerm = nullptr, const ColumnFeed* feed = nullptr);
 template <typename T>
 int getrs_dev(char trans, int n, int nrhs, const T* dA, int lda, const int* dIpiv, const int* dPerm,
               T* dB, int ldb, cudaStream_t s, bool inv_diag = false);   // inv_diag: diagonal blocks by their inverses
@@ -127,9 +153,19 @@ int gemm_bf16x3_dev(int M, int N, int K, const float* A, int lda, const float* B
                     cudaStream_t s, bool overwrite = false,   // overwrite: C = A*B
                     const Bf16SplitA* a_pre = nullptr);
 
-// DSGESV on device memory.  *iter and *info are host outputs.
+// Host operands of the host-pointer DSGESV: dsgesv_dev copies them into
+// dA / dB itself, A in column chunks on a second stream while the FP32
+// factorization takes the chunks in as they land.
+struct HostOperands {
+  const double* a;
+  int lda;
+  const double* b;
+  int ldb;
+};
+// DSGESV on device memory.  *iter and *info are host outputs.  With host,
+// dA and dB are filled from host->a and host->b first.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
-               int* iter, int* info, cudaStream_t s);
+               int* iter, int* info, cudaStream_t s, const HostOperands* host = nullptr);
 // DGECON on device memory: *rcond and *info are host outputs.
 int dgecon_dev(char norm, int n, const double* LU, int lda, double anorm, double* rcond, int* info, cudaStream_t s);
 // DGESVX on device memory after its argument checks (for FACT = 'F' the

@@ -5,6 +5,8 @@
 // recursion whose leaves of width <= 64 are the cooperative panel kernel),
 // apply its interchanges to the other columns, form the block row of U with
 // a triangular solve, then update the trailing matrix with one GEMM.
+#include <vector>
+
 #include "driver.h"
 #include "prof.h"
 #include "gemm_simt.cuh"
@@ -41,6 +43,9 @@ Options& options() {
     x.gemm_tiles = std::max(0, env_int("LAPACK_GB300_GEMM_TILES", 4));
     x.ir_nan_guard = env_int("LAPACK_GB300_IR_NAN_GUARD", 0);
     x.panel_fuse = env_int("LAPACK_GB300_PANEL_FUSE", 1);
+    x.feed = env_int("LAPACK_GB300_FEED", 1);
+    x.feed_lazy = env_int("LAPACK_GB300_FEED_LAZY", 0);
+    x.pool_keep = env_int("LAPACK_GB300_POOL_KEEP", 1);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -62,7 +67,28 @@ int device_sm_count() {
   return n;
 }
 
+// The scratch comes from the device's default stream-ordered pool.  By
+// default the pool hands its memory back to the driver at every
+// synchronisation, so each call would map its gigabytes again (and a pool
+// growing while host->device copies run waits for them); with option
+// pool_keep the pool keeps what it has grown to for the process (a
+// property of this process's pool, nothing on the device).
+static void keep_pool_memory() {
+  static bool done[64] = {false};
+  int dev = 0;
+  if (!options().pool_keep || cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64 || done[dev]) return;
+  done[dev] = true;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  unsigned long long keep = ~0ull;
+  if (cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) cudaGetLastError();
+}
+
 DevScratch::DevScratch(size_t bytes, cudaStream_t st) : s(st) {
+  keep_pool_memory();
   if (bytes && cudaMallocAsync(&p, bytes, st) != cudaSuccess) p = nullptr;
 }
 DevScratch::~DevScratch() {
@@ -600,11 +626,62 @@ static __global__ void iota_kernel(int* p, int n) {
   if (i < n) p[i] = i;
 }
 
+// Host events marking the end of each look-ahead step while columns are
+// fed in: the host keeps at most two steps ahead of the device, so that
+// the chunks it finds arrived are taken in as early as the device can use
+// them (a chunk taken in late is first brought up to date column block by
+// column block).
+struct StepEvents {
+  cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+  bool ok = true;
+  StepEvents() {
+    for (auto& x : e) ok = ok && cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess;
+  }
+  ~StepEvents() {
+    for (auto& x : e)
+      if (x) cudaEventDestroy(x);
+  }
+};
+
+// Optional timeline of the fed factorization (gb300_feed_trace): timing
+// events on the factorization's stream at each step's end (kind 0) and
+// after each chunk is taken in and brought up to date (kind 1, with the
+// step it joined at), read back as milliseconds after the first.
+struct FeedTrace {
+  bool on = false;
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> kind, idx, aux;
+  void add(int k, int i, int a, cudaStream_t s) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, s);
+    ev.push_back(e);
+    kind.push_back(k);
+    idx.push_back(i);
+    aux.push_back(a);
+  }
+  void clear() {
+    for (auto e : ev) cudaEventDestroy(e);
+    ev.clear();
+    kind.clear();
+    idx.clear();
+    aux.clear();
+  }
+};
+static FeedTrace g_feed_trace;
+
+void feed_trace_mark(int kind, int idx, int aux, cudaStream_t s) {
+  if (g_feed_trace.on) g_feed_trace.add(kind, idx, aux, s);
+}
+
 template <typename T>
 int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t s, int gemm_mode, int nb,
-              int* dPerm) {
+              int* dPerm, const ColumnFeed* feed) {
   GB_CUDA_TRY(cudaMemsetAsync(dInfo, 0, sizeof(int), s));
   if (m <= 0 || n <= 0) return 0;
+  if (feed && (!dPerm || sizeof(T) != 4 || feed->nchunks < 1 || feed->cols[0] != 0 ||
+               feed->cols[feed->nchunks] != n))
+    return (int)cudaErrorInvalidValue;
   if (dPerm) GB_LAUNCH(iota_kernel<<<(m + 255) / 256, 256, 0, s>>>(dPerm, m));
   const int nsm = device_sm_count();
   int dev = 0;
@@ -672,6 +749,55 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
                 ? reinterpret_cast<T*>(base + o_linv)
                 : nullptr;
   LookaheadRes* lr = la ? lookahead_res() : nullptr;
+  // Fed columns: [0, win) are in the matrix and current; chunk nq is next.
+  // A chunk taken in after block columns 0..kdone-1 were factored gets their
+  // interchanges (by the gather in admit) and then, block column by block
+  // column in order, their U rows and trailing updates: the operations, in
+  // the order, the right-looking loop applies to every column it covers,
+  // so the result does not depend on when the chunk arrived.
+  int win = feed ? 0 : n, nq = 0;
+  // fed columns with the look-ahead: every block column's L11^{-1}, for the catch-up
+  DevScratch linv_keep((feed && lr && linv) ? sizeof(T) * (size_t)((mn + nb - 1) / nb) * nb * nb : 0, s);
+  T* linv_hist = linv_keep.as<T>();
+  if (feed && lr && linv && !linv_hist) return (int)cudaErrorMemoryAllocation;
+  // takes chunks [nq, qend) in after block columns 0..kdone-1: their row
+  // reordering, then one catch-up over the chunks together
+  auto admit_upto = [&](int qend, int kdone) -> int {
+    if (qend <= nq) return 0;
+    for (int q = nq; q < qend; ++q) {
+      GB_CUDA_TRY(cudaStreamWaitEvent(s, feed->ready[q], 0));
+      const int rc = feed->admit(q, kdone > 0 ? dPerm : nullptr, s);
+      if (rc) return rc;
+      if (feed->rejected(q)) return kFeedStop;
+    }
+    const int c0 = feed->cols[nq], c1 = feed->cols[qend];
+    for (int kk = 0, jj = 0; kk < kdone; ++kk, jj += nb) {
+      const int jjb = std::min(nb, std::min(m, n) - jj), jj2 = jj + jjb;
+      const T* lv = linv_hist ? linv_hist + (size_t)kk * nb * nb : nullptr;
+      T* Ajj = dA + jj + (size_t)jj * lda;
+      int rc = block_row_u<T>(dA, lda, jj, jjb, c0, c1, lv, s, gemm_mode);
+      if (!rc && jj2 < m)
+        rc = gemm_update_dev<T>(m - jj2, c1 - c0, jjb, Ajj + jjb, lda, dA + jj + (size_t)c0 * lda, lda,
+                                dA + jj2 + (size_t)c0 * lda, lda, s, gemm_mode);
+      if (rc) return rc;
+    }
+    win = c1;
+    for (int q = nq; q < qend; ++q)
+      if (g_feed_trace.on) g_feed_trace.add(1, q, kdone, s);
+    nq = qend;
+    return 0;
+  };
+  // the first chunk index whose columns reach `col`
+  auto chunk_reaching = [&](int col) {
+    int q = nq;
+    while (q < feed->nchunks && feed->cols[q] < col) ++q;
+    return q;
+  };
+  if (feed && !lr) {
+    // no look-ahead schedule: take every chunk in before the factorization
+    const int rc = admit_upto(feed->nchunks, 0);
+    if (rc) return rc;
+  }
   if (lr) {
     std::lock_guard<std::mutex> lk(lr->mu);
     cudaStream_t sp = lr->sp;
@@ -681,12 +807,20 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     const bool split_a21 = sizeof(T) == 4 && gemm_mode == kMixedBf16x3;
     DevScratch a21buf(split_a21 ? bf16x3_split_bytes(m, nb) : 0, s);
     if (split_a21 && !a21buf.p) return (int)cudaErrorMemoryAllocation;
+    StepEvents steps;
+    if (feed) {
+      if (!steps.ok) return (int)cudaErrorMemoryAllocation;
+      // the first two block columns before anything starts
+      const int rc = admit_upto(chunk_reaching(std::min(n, 2 * nb)), 0);
+      if (rc) return rc;
+    }
     GB_CUDA_TRY(cudaEventRecord(lr->fork, s));
     GB_CUDA_TRY(cudaStreamWaitEvent(sp, lr->fork, 0));
     int k = 0;
     for (int j = 0; j < mn; j += nb, ++k) {
       const int jb = std::min(nb, mn - j);
       const int b = k & 1;
+      if (feed && k >= 2) GB_CUDA_TRY(cudaEventSynchronize(steps.e[(k - 2) & 3]));
       if (k > 0) GB_CUDA_TRY(cudaStreamWaitEvent(sp, lr->L[b ^ 1], 0));
       cx.logging = true;
       cx.imm_lo = j;
@@ -703,7 +837,8 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       const int j2 = j + jb;
       const int nb2 = j2 < mn ? std::min(nb, mn - j2) : 0;   // next block column
       T* Ajj = dA + j + (size_t)j * lda;
-      rc = form_linv<T>(dA, lda, j, jb, linv, s);
+      T* lv = linv_hist ? linv_hist + (size_t)k * nb * nb : linv;
+      rc = form_linv<T>(dA, lda, j, jb, lv, s);
       if (rc) return rc;
       // the BF16 split of A21, made once for both updates of this block column
       // (stream s orders it after the previous column's updates that read the buffer)
@@ -725,18 +860,39 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       // next block column first
       if (nb2 > 0) {
         rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
-        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, linv, s, gemm_mode);
+        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, lv, s, gemm_mode);
         if (!rc && j2 < m) rc = update(nb2, jb);
         if (rc) return rc;
       }
       GB_CUDA_TRY(cudaEventRecord(lr->L[b], s));
-      // then the columns left of the block column and the rest of the trailing matrix
       const int c2 = j2 + nb2;
-      rc = laswp_log<T>(dA, lda, 0, j, c2, n, cx, cx.perm, s);
-      if (!rc && c2 < n) {
-        rc = block_row_u<T>(dA, lda, j, jb, c2, n, linv, s, gemm_mode);
-        if (!rc && j2 < m) rc = update(n - c2, c2 - j);
+      if (feed) {
+        // chunks that have arrived, then those the next step needs (the
+        // block column after the next one), brought up to date with block
+        // columns 0..k-1 before this block column's interchanges reach them
+        int qend = chunk_reaching(std::min(n, c2 + nb));
+        if (!options().feed_lazy) {
+          int ql = nq;
+          while (ql < feed->nchunks && cudaEventQuery(feed->ready[ql]) == cudaSuccess) ++ql;
+          cudaGetLastError();   // (a not-ready query leaves no error behind)
+          qend = std::max(qend, ql);
+        }
+        rc = admit_upto(qend, k);
+        if (rc) return rc;
       }
+      // then the columns left of the block column and the rest of the trailing matrix
+      rc = laswp_log<T>(dA, lda, 0, j, c2, win, cx, cx.perm, s);
+      if (!rc && c2 < win) {
+        rc = block_row_u<T>(dA, lda, j, jb, c2, win, lv, s, gemm_mode);
+        if (!rc && j2 < m) rc = update(win - c2, c2 - j);
+      }
+      if (rc) return rc;
+      if (feed) GB_CUDA_TRY(cudaEventRecord(steps.e[k & 3], s));
+      if (feed && g_feed_trace.on) g_feed_trace.add(0, k, win, s);
+    }
+    // columns right of min(m, n) still outside (wide matrices)
+    if (feed) {
+      const int rc = admit_upto(feed->nchunks, k);
       if (rc) return rc;
     }
     return (int)cudaGetLastError();
@@ -763,8 +919,8 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   }
   return (int)cudaGetLastError();
 }
-template int getrf_dev<double>(int, int, double*, int, int*, int*, cudaStream_t, int, int, int*);
-template int getrf_dev<float>(int, int, float*, int, int*, int*, cudaStream_t, int, int, int*);
+template int getrf_dev<double>(int, int, double*, int, int*, int*, cudaStream_t, int, int, int*, const ColumnFeed*);
+template int getrf_dev<float>(int, int, float*, int, int*, int*, cudaStream_t, int, int, int*, const ColumnFeed*);
 
 // ------------------------------------------------------------- permutation
 int ipiv_perm_dev(const int* dIpiv, int k1, int k2, int incx, int lo, int span, int* dPerm, cudaStream_t s) {
@@ -1007,6 +1163,31 @@ int dtrsv_dev(bool upper, bool trans, bool unit, int n, const double* dA, int ld
 }  // namespace gb
 
 extern "C" {
+int gb300_feed_trace(int on) {
+  const int old = gb::g_feed_trace.on;
+  gb::g_feed_trace.clear();
+  gb::g_feed_trace.on = on != 0;
+  return old;
+}
+// Up to cap records of the last fed factorizations: kind (0 step end, 1
+// chunk taken in, 2 chunk landed and converted, 3 start of the copies),
+// index (step or chunk), aux (columns in the window, or the step a chunk
+// joined at), milliseconds after the first record.
+int gb300_feed_trace_read(int* kind, int* idx, int* aux, double* ms, int cap) {
+  auto& t = gb::g_feed_trace;
+  if (t.ev.empty()) return 0;
+  if (cudaEventSynchronize(t.ev.back()) != cudaSuccess) return -1;
+  const int n = std::min<int>(cap, (int)t.ev.size());
+  for (int i = 0; i < n; ++i) {
+    float f = 0;
+    cudaEventElapsedTime(&f, t.ev[0], t.ev[i]);
+    kind[i] = t.kind[i];
+    idx[i] = t.idx[i];
+    aux[i] = t.aux[i];
+    ms[i] = f;
+  }
+  return n;
+}
 int gb300_leaf_profile(int on) {
   const int old = gb::g_leaf_phase_on;
   gb::g_leaf_phase_on = on != 0;

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 namespace gb {
 
@@ -149,8 +150,158 @@ int dlange_dev(int which, int m, int n, const double* dA, int lda, double* out, 
 }
 
 
+// Streams of the host-pointer DSGESV, per host thread and device: one for
+// the host->device copies, one for the conversions of the landed chunks;
+// and a pinned word per chunk receiving the overflow flag after its
+// conversion.
+struct FeedStreams {
+  cudaStream_t copy[64] = {};
+  cudaStream_t conv[64] = {};
+  int* flag_words = nullptr;
+  int nwords = 0;
+  ~FeedStreams() {
+    if (flag_words) cudaFreeHost(flag_words);
+  }
+};
+
+static FeedStreams* feed_streams(int nchunks) {
+  thread_local FeedStreams fs;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!fs.copy[dev] && cudaStreamCreateWithFlags(&fs.copy[dev], cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  if (!fs.conv[dev] && cudaStreamCreateWithFlags(&fs.conv[dev], cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+  if (fs.nwords < nchunks) {
+    if (fs.flag_words) cudaFreeHost(fs.flag_words);
+    fs.flag_words = nullptr;
+    fs.nwords = 0;
+    if (cudaHostAlloc(&fs.flag_words, sizeof(int) * (size_t)nchunks, cudaHostAllocMapped) != cudaSuccess) return nullptr;
+    fs.nwords = nchunks;
+  }
+  return &fs;
+}
+
+// dst(i, c) = src(perm[i], c) (perm null: src(i, c)): the rows of a landed
+// chunk in the order of the interchanges made before it was taken in, and
+// the copy back.  Kernels rather than device-to-device memcpy: a memcpy
+// would queue on the copy engines behind the host->device chunks.
+static __global__ void gather_rows_kernel(const float* __restrict__ src, int lds, const int* __restrict__ perm, int m,
+                                          float* __restrict__ dst, int ldd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[(size_t)i + (size_t)blockIdx.y * ldd] = src[(size_t)(perm ? perm[i] : i) + (size_t)blockIdx.y * lds];
+}
+
+// *word = *flag, word in mapped host memory (the chunk's overflow verdict,
+// read by the host after the conversion's event; no copy engine involved)
+static __global__ void flag_to_host_kernel(const int* __restrict__ flag, volatile int* word) { *word = *flag; }
+
+// Events of one host-pointer call, destroyed with it (a pending event is
+// released once it completes).
+struct EventSet {
+  std::vector<cudaEvent_t> e;
+  bool ok = true;
+  explicit EventSet(int k) : e(k, nullptr) {
+    for (auto& x : e) ok = ok && cudaEventCreateWithFlags(&x, cudaEventDisableTiming) == cudaSuccess;
+  }
+  ~EventSet() {
+    for (auto& x : e)
+      if (x) cudaEventDestroy(x);
+  }
+};
+
+// The host-pointer DSGESV up to the FP32 factorization.  B, then A in
+// column chunks go to the device on the copy stream; each landed chunk is
+// converted on the conversion stream (DLAG2S and its DLANGE row sums: the
+// chunks are the row-sum split, so the folded norm is that of one pass, or
+// in exact mode 2048-column chunks continuing one running sum per row); the
+// FP32 factorization on s takes every chunk in as it is converted.  Returns
+// 0 (SA factored, its INFO in flags[2]), 1 (an entry overflows FP32: ITER =
+// -2) or a CUDA error; on return s is ordered after every copy and
+// conversion.
+static int fed_sgetrf(int n, int nrhs, double* dA, int lda, double* dB, int ldb, const HostOperands& h, float* SA,
+                      float* SX, double* part, double* rows, double* anrm, int nsplit, int chunk, int* flags,
+                      int* dIpiv, int* perm, cudaStream_t s) {
+  const Options& opt = options();
+  const int cw = opt.exact ? std::min(n, 2048) : chunk;
+  std::vector<int> cols;
+  for (int c0 = 0; c0 < n; c0 += cw) cols.push_back(c0);
+  cols.push_back(n);
+  const int Q = (int)cols.size() - 1;
+  FeedStreams* fs = feed_streams(Q);
+  if (!fs) return (int)cudaErrorMemoryAllocation;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaStream_t cp = fs->copy[dev], cv = fs->conv[dev];
+  int* words = fs->flag_words;
+  int* words_dev = nullptr;
+  GB_CUDA_TRY(cudaHostGetDevicePointer(reinterpret_cast<void**>(&words_dev), words, 0));
+  // events: [0, Q) chunk converted, Q start, Q+1 B landed; evl: chunk landed
+  EventSet ev(Q + 2), evl(Q);
+  if (!ev.ok || !evl.ok) return (int)cudaErrorMemoryAllocation;
+  DevScratch tmp(sizeof(float) * (size_t)n * cw, s);
+  if (!tmp.p) return (int)cudaErrorMemoryAllocation;
+  {
+    // grow the pool now by what the catch-ups' operand splits take (A21
+    // and a slab of U rows in BF16 hi/lo), not while the copies run
+    DevScratch pre(2 * bf16x3_split_bytes(n, opt.nb_f32), s);
+    if (!pre.p) return (int)cudaErrorMemoryAllocation;
+  }
+  for (int q = 0; q < Q; ++q) words[q] = 0;
+  // the copies follow whatever s queued before (the buffers, the flags reset)
+  feed_trace_mark(3, 0, 0, s);
+  GB_CUDA_TRY(cudaEventRecord(ev.e[Q], s));
+  GB_CUDA_TRY(cudaStreamWaitEvent(cp, ev.e[Q], 0));
+  GB_CUDA_TRY(cudaStreamWaitEvent(cv, ev.e[Q], 0));
+  prof_begin(kProfCopyH2D, cp);
+  GB_CUDA_TRY(cudaMemcpy2DAsync(dB, sizeof(double) * ldb, h.b, sizeof(double) * h.ldb, sizeof(double) * n, nrhs,
+                                cudaMemcpyHostToDevice, cp));
+  GB_CUDA_TRY(cudaEventRecord(ev.e[Q + 1], cp));
+  for (int q = 0; q < Q; ++q) {
+    const int c0 = cols[q], c1 = cols[q + 1];
+    GB_CUDA_TRY(cudaMemcpy2DAsync(dA + (size_t)c0 * lda, sizeof(double) * lda, h.a + (size_t)c0 * h.lda,
+                                  sizeof(double) * h.lda, sizeof(double) * n, c1 - c0, cudaMemcpyHostToDevice, cp));
+    GB_CUDA_TRY(cudaEventRecord(evl.e[q], cp));
+    GB_CUDA_TRY(cudaStreamWaitEvent(cv, evl.e[q], 0));
+    dim3 g((n + 127) / 128, 1);
+    GB_LAUNCH(dlag2s_rowsum_kernel<<<g, 128, 0, cv>>>(dA + (size_t)c0 * lda, lda, n, c1 - c0, c1 - c0,
+                                                      SA + (size_t)c0 * n, n, opt.exact ? part : part + (size_t)q * n,
+                                                      flags, opt.exact && q > 0));
+    GB_LAUNCH(flag_to_host_kernel<<<1, 1, 0, cv>>>(flags, words_dev + q));
+    GB_CUDA_TRY(cudaEventRecord(ev.e[q], cv));
+    feed_trace_mark(2, q, 0, cv);
+  }
+  prof_end(kProfCopyH2D, cp, 0.0, 8.0 * (double)n * (n + nrhs));
+  // SX = DLAG2S(B) once B has landed
+  GB_CUDA_TRY(cudaStreamWaitEvent(s, ev.e[Q + 1], 0));
+  GB_LAUNCH(dlag2s_kernel<<<blocks_for((size_t)n * nrhs), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
+  ColumnFeed feed;
+  feed.nchunks = Q;
+  feed.cols = cols.data();
+  feed.ready = ev.e.data();
+  feed.admit = [&](int q, const int* pm, cudaStream_t st) -> int {
+    if (!pm) return 0;   // no interchanges yet
+    const int c0 = cols[q], nc = cols[q + 1] - c0;
+    dim3 g((n + 255) / 256, nc);
+    GB_LAUNCH(gather_rows_kernel<<<g, 256, 0, st>>>(SA + (size_t)c0 * n, n, pm, n, tmp.as<float>(), n));
+    GB_LAUNCH(gather_rows_kernel<<<g, 256, 0, st>>>(tmp.as<float>(), n, nullptr, n, SA + (size_t)c0 * n, n));
+    return (int)cudaGetLastError();
+  };
+  feed.rejected = [&](int q) -> bool {
+    if (cudaEventSynchronize(ev.e[q]) != cudaSuccess) return true;
+    return words[q] != 0;
+  };
+  int rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32, perm, &feed);
+  // s after every chunk's conversion (and so every copy)
+  const cudaError_t jrc = cudaStreamWaitEvent(s, ev.e[Q - 1], 0);
+  if (rc == kFeedStop) return 1;
+  if (rc) return rc;
+  if (jrc != cudaSuccess) return (int)jrc;
+  GB_LAUNCH(fold_partials_kernel<<<(n + 255) / 256, 256, 0, s>>>(part, nsplit, n, rows));
+  GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, n, anrm));
+  return (int)cudaGetLastError();
+}
+
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,
-               int* iter, int* info, cudaStream_t s) {
+               int* iter, int* info, cudaStream_t s, const HostOperands* host) {
   const int itermax = 30;
   *iter = 0;
   *info = 0;
@@ -178,35 +329,47 @@ int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* d
   int* flags = reinterpret_cast<int*>(base + o_flags);
   int hflags[4];
   int rc;
+  // row sums of DLANGE('I'): exact mode one running sum per row in column
+  // order, otherwise column chunks folded in fixed order
+  const int nsplit = opt.exact ? 1 : std::max(1, std::min(16, n / 512));
+  const int chunk = (n + nsplit - 1) / nsplit;
+  DevScratch buf(sizeof(double) * (size_t)n * (nsplit + 1), s);
+  if (!buf.p) return (int)cudaErrorMemoryAllocation;
+  double* part = buf.as<double>();
+  double* rows = part + (size_t)n * nsplit;
 
   GB_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int) * 4, s));
-  // SX = DLAG2S(B)
-  GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
-  // ANRM = DLANGE('I') (kept on the device for the convergence test) and
-  // SA = DLAG2S(A), in one pass over A; exact mode sums each row in column
-  // order, otherwise column chunks are folded in fixed order
-  {
-    const int nsplit = opt.exact ? 1 : std::max(1, std::min(16, n / 512));
-    const int chunk = (n + nsplit - 1) / nsplit;
-    DevScratch buf(sizeof(double) * (size_t)n * (nsplit + 1), s);
-    if (!buf.p) return (int)cudaErrorMemoryAllocation;
-    double* part = buf.as<double>();
-    double* rows = part + (size_t)n * nsplit;
+  if (host) {
+    // copies, conversion and SGETRF overlapped; the overflow test of
+    // DLAG2S(B) and DLAG2S(A) and the SGETRF INFO are read after
+    rc = fed_sgetrf(n, nrhs, dA, lda, const_cast<double*>(dB), ldb, *host, SA, SX, part, rows, anrm, nsplit,
+                    chunk, flags, dIpiv, perm, s);
+    if (rc > 1) return rc;
+    GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int) * 3, cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (rc == 1 || hflags[0]) { *iter = -2; goto fallback; }
+    if (hflags[2] != 0) { *iter = -3; goto fallback; }
+  } else {
+    // SX = DLAG2S(B)
+    GB_LAUNCH(dlag2s_kernel<<<blocks_for(nr), 256, 0, s>>>(dB, ldb, SX, n, n, nrhs, flags));
+    // ANRM = DLANGE('I') (kept on the device for the convergence test) and
+    // SA = DLAG2S(A), in one pass over A; exact mode sums each row in column
+    // order, otherwise column chunks are folded in fixed order
     dim3 g((n + 127) / 128, nsplit);
     GB_LAUNCH(dlag2s_rowsum_kernel<<<g, 128, 0, s>>>(dA, lda, n, n, chunk, SA, n, part, flags));
     GB_LAUNCH(fold_partials_kernel<<<(n + 255) / 256, 256, 0, s>>>(part, nsplit, n, rows));
     GB_LAUNCH(max_nan_kernel<double><<<1, 1024, 0, s>>>(rows, n, anrm));
+    GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hflags[0]) { *iter = -2; goto fallback; }
+    // SGETRF(SA)
+    // the factorization also returns the gather permutation the solves reuse
+    rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32, perm);
+    if (rc) return rc;
+    GB_CUDA_TRY(cudaMemcpyAsync(hflags + 2, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hflags[2] != 0) { *iter = -3; goto fallback; }
   }
-  GB_CUDA_TRY(cudaMemcpyAsync(hflags, flags, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GB_CUDA_TRY(cudaStreamSynchronize(s));
-  if (hflags[0]) { *iter = -2; goto fallback; }
-  // SGETRF(SA)
-  // the factorization also returns the gather permutation the solves reuse
-  rc = getrf_dev<float>(n, n, SA, n, dIpiv, flags + 2, s, opt.mixed_mode, opt.nb_f32, perm);
-  if (rc) return rc;
-  GB_CUDA_TRY(cudaMemcpyAsync(hflags + 2, flags + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
-  GB_CUDA_TRY(cudaStreamSynchronize(s));
-  if (hflags[2] != 0) { *iter = -3; goto fallback; }
   // SX = SA^{-1} SX, X = SLAG2D(SX), R = B - A X
   if ((rc = getrs_dev<float>('N', n, nrhs, SA, n, dIpiv, perm, SX, n, s, opt.trsv_inv != 0))) return rc;
   GB_LAUNCH(slag2d_kernel<<<blocks_for(nr), 256, 0, s>>>(SX, n, dX, ldx, n, nrhs));

@@ -352,7 +352,7 @@ static __global__ void dlag2s_kernel(const double* __restrict__ A, int lda, floa
 // of 16 columns are issued together.
 static __global__ void __launch_bounds__(128)
 dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int chunk, float* __restrict__ S, int lds,
-                     double* __restrict__ part, int* __restrict__ overflow) {
+                     double* __restrict__ part, int* __restrict__ overflow, bool accumulate = false) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const int l0 = blockIdx.y * chunk, l1 = min(n, l0 + chunk);
@@ -364,7 +364,9 @@ dlag2s_rowsum_kernel(const double* __restrict__ A, int lda, int m, int n, int ch
   constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
   const double* p = A + i;
   float* q = S + i;
-  double s = 0;
+  // accumulate: continue the row sums of the columns before (one running
+  // sum per row in column order, the columns arriving in chunks)
+  double s = accumulate ? part[(size_t)blockIdx.y * m + i] : 0.0;
   bool ovf = false;
   int j = l0;
   for (; j + 16 <= l1; j += 16) {
