@@ -499,9 +499,11 @@ int gb300_dgesv_adjoint_batched_dev(int batch, int n, int nrhs, const double* dL
  * two; bitwise the same), "feed" (1: the host-pointer dsgesv_ copies A in
  * column chunks on a second stream while the FP32 factorization takes each
  * chunk in as it lands; 0: the whole copy first; bitwise the same),
- * "feed_lazy" (1: a landed chunk is taken in only when the factorization
- * needs it, which brings it up to date block column by block column; a
- * test setting), "pool_keep" (1: the device's stream-ordered memory pool,
+ * "feed_lazy" (test settings: 1, a landed chunk is taken in only when the
+ * factorization needs it, which brings it up to date block column by block
+ * column at once; 2, the next chunk is taken in at every step whether
+ * landed or not, which exercises the catch-up spread over steps), "feed_catchup" (block columns of catch-up a landed chunk
+ * taken in early gets per step, 8 by default; 0: all at once), "pool_keep" (1: the device's stream-ordered memory pool,
  * which this library's scratch comes from, keeps the memory it has grown to
  * for the rest of the process instead of returning it at every
  * synchronisation; read when the library first allocates on a device),

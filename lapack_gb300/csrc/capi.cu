@@ -1302,6 +1302,7 @@ int gb300_set_option(const char* name, int value) {
   else if (!strcmp(name, "feed")) { old = o.feed; o.feed = value; }
   else if (!strcmp(name, "feed_lazy")) { old = o.feed_lazy; o.feed_lazy = value; }
   else if (!strcmp(name, "pool_keep")) { old = o.pool_keep; o.pool_keep = value; }
+  else if (!strcmp(name, "feed_catchup")) { old = o.feed_catchup; o.feed_catchup = std::max(0, value); }
   else if (!strcmp(name, "gemm_tiles")) { old = o.gemm_tiles; o.gemm_tiles = std::max(0, value); }
   else if (!strcmp(name, "ir_nan_guard")) { old = o.ir_nan_guard; o.ir_nan_guard = value != 0; }
   else return -1;
@@ -1324,6 +1325,7 @@ int gb300_get_option(const char* name) {
   if (!strcmp(name, "feed")) return o.feed;
   if (!strcmp(name, "feed_lazy")) return o.feed_lazy;
   if (!strcmp(name, "pool_keep")) return o.pool_keep;
+  if (!strcmp(name, "feed_catchup")) return o.feed_catchup;
   if (!strcmp(name, "gemm_tiles")) return o.gemm_tiles;
   if (!strcmp(name, "ir_nan_guard")) return o.ir_nan_guard;
   return -1;

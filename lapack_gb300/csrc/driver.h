@@ -29,8 +29,9 @@ struct Options {
   int ir_nan_guard = 0;           // DSGESV: a non-finite iterate or residual ends the refinement (ITER = -2)
   int panel_fuse = 1;             // panel recursion: a node with halves <= 64 columns as one fused launch
   int feed = 1;                   // host-pointer DSGESV: copy A in column chunks beside the FP32 factorization
-  int feed_lazy = 0;              // take a landed chunk in only when the factorization needs it (more catch-up)
+  int feed_lazy = 0;              // test settings: 1 take a chunk in only when needed, 2 one chunk every step
   int pool_keep = 1;              // the stream-ordered pool keeps its memory between calls (set at first use)
+  int feed_catchup = 8;           // block columns of catch-up a pending chunk gets per step
 };
 Options& options();          // process-wide; initialised from LAPACK_GB300_* environment variables
 

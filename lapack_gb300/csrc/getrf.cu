@@ -46,6 +46,7 @@ Options& options() {
     x.feed = env_int("LAPACK_GB300_FEED", 1);
     x.feed_lazy = env_int("LAPACK_GB300_FEED_LAZY", 0);
     x.pool_keep = env_int("LAPACK_GB300_POOL_KEEP", 1);
+    x.feed_catchup = env_int("LAPACK_GB300_FEED_CATCHUP", 8);
     const char* mm = getenv("LAPACK_GB300_MIXED");
     if (mm && strcmp(mm, "fp32") == 0) x.mixed_mode = kMixedFp32;
     if (mm && strcmp(mm, "bf16x3") == 0) x.mixed_mode = kMixedBf16x3;
@@ -750,28 +751,43 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
                 : nullptr;
   LookaheadRes* lr = la ? lookahead_res() : nullptr;
   // Fed columns: [0, win) are in the matrix and current; chunk nq is next.
-  // A chunk taken in after block columns 0..kdone-1 were factored gets their
-  // interchanges (by the gather in admit) and then, block column by block
-  // column in order, their U rows and trailing updates: the operations, in
-  // the order, the right-looking loop applies to every column it covers,
-  // so the result does not depend on when the chunk arrived.
+  // Chunks taken in together form the pending slab [win, pend_end): their
+  // rows are reordered at once by the interchanges made so far (the gather
+  // in admit), every later step's interchanges reach them with the rest of
+  // the matrix, and block column by block column, in order, they get the U
+  // rows and trailing updates of the block columns already factored -- a
+  // few block columns per step, so the catch-up runs beside the panels
+  // instead of holding them up -- until they are current and join the
+  // window.  Per element these are the operations of the right-looking
+  // loop in its order (an interchange of a later block column moves whole
+  // rows of L and of the slab alike), so the result does not depend on
+  // when a chunk arrived.
   int win = feed ? 0 : n, nq = 0;
+  int pend_end = win, pend_k = 0;   // pending slab, brought up to date through block column pend_k - 1
   // fed columns with the look-ahead: every block column's L11^{-1}, for the catch-up
   DevScratch linv_keep((feed && lr && linv) ? sizeof(T) * (size_t)((mn + nb - 1) / nb) * nb * nb : 0, s);
   T* linv_hist = linv_keep.as<T>();
   if (feed && lr && linv && !linv_hist) return (int)cudaErrorMemoryAllocation;
-  // takes chunks [nq, qend) in after block columns 0..kdone-1: their row
-  // reordering, then one catch-up over the chunks together
-  auto admit_upto = [&](int qend, int kdone) -> int {
-    if (qend <= nq) return 0;
+  // chunks [nq, qend) become the pending slab (none pending), after the
+  // interchanges of block columns 0..kdone-1
+  auto take_in = [&](int qend, int kdone) -> int {
+    if (qend <= nq || pend_end > win) return 0;
     for (int q = nq; q < qend; ++q) {
       GB_CUDA_TRY(cudaStreamWaitEvent(s, feed->ready[q], 0));
       const int rc = feed->admit(q, kdone > 0 ? dPerm : nullptr, s);
       if (rc) return rc;
       if (feed->rejected(q)) return kFeedStop;
     }
-    const int c0 = feed->cols[nq], c1 = feed->cols[qend];
-    for (int kk = 0, jj = 0; kk < kdone; ++kk, jj += nb) {
+    pend_end = feed->cols[qend];
+    pend_k = 0;
+    nq = qend;
+    return 0;
+  };
+  // block columns pend_k..kto-1 on the pending slab; it joins the window once current at step k_now
+  auto catch_up = [&](int kto, int k_now) -> int {
+    if (pend_end <= win) return 0;
+    const int c0 = win, c1 = pend_end;
+    for (int kk = pend_k, jj = pend_k * nb; kk < kto; ++kk, jj += nb) {
       const int jjb = std::min(nb, std::min(m, n) - jj), jj2 = jj + jjb;
       const T* lv = linv_hist ? linv_hist + (size_t)kk * nb * nb : nullptr;
       T* Ajj = dA + jj + (size_t)jj * lda;
@@ -781,10 +797,13 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
                                 dA + jj2 + (size_t)c0 * lda, lda, s, gemm_mode);
       if (rc) return rc;
     }
-    win = c1;
-    for (int q = nq; q < qend; ++q)
-      if (g_feed_trace.on) g_feed_trace.add(1, q, kdone, s);
-    nq = qend;
+    pend_k = std::max(pend_k, kto);
+    if (pend_k >= k_now) {
+      if (g_feed_trace.on)
+        for (int q = 0; q < feed->nchunks; ++q)
+          if (feed->cols[q] >= c0 && feed->cols[q] < c1) g_feed_trace.add(1, q, k_now, s);
+      win = pend_end;
+    }
     return 0;
   };
   // the first chunk index whose columns reach `col`
@@ -793,9 +812,30 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     while (q < feed->nchunks && feed->cols[q] < col) ++q;
     return q;
   };
+  // chunks landed so far, from nq on
+  auto chunks_landed = [&]() {
+    int q = nq;
+    while (q < feed->nchunks && cudaEventQuery(feed->ready[q]) == cudaSuccess) ++q;
+    cudaGetLastError();   // (a not-ready query leaves no error behind)
+    return q;
+  };
+  // everything the step after the next needs, and (eagerly) whatever landed
+  auto take_in_now = [&](int need, int k_now) -> int {
+    int rc = 0;
+    if (win < need) {
+      rc = catch_up(k_now, k_now);
+      if (!rc && win < need) {
+        int qend = chunk_reaching(need);
+        if (options().feed_lazy == 0) qend = std::max(qend, chunks_landed());
+        rc = take_in(qend, k_now);
+        if (!rc) rc = catch_up(k_now, k_now);
+      }
+    }
+    return rc;
+  };
   if (feed && !lr) {
     // no look-ahead schedule: take every chunk in before the factorization
-    const int rc = admit_upto(feed->nchunks, 0);
+    const int rc = take_in_now(n, 0);
     if (rc) return rc;
   }
   if (lr) {
@@ -811,7 +851,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     if (feed) {
       if (!steps.ok) return (int)cudaErrorMemoryAllocation;
       // the first two block columns before anything starts
-      const int rc = admit_upto(chunk_reaching(std::min(n, 2 * nb)), 0);
+      const int rc = take_in_now(std::min(n, 2 * nb), 0);
       if (rc) return rc;
     }
     GB_CUDA_TRY(cudaEventRecord(lr->fork, s));
@@ -867,21 +907,22 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       GB_CUDA_TRY(cudaEventRecord(lr->L[b], s));
       const int c2 = j2 + nb2;
       if (feed) {
-        // chunks that have arrived, then those the next step needs (the
-        // block column after the next one), brought up to date with block
-        // columns 0..k-1 before this block column's interchanges reach them
-        int qend = chunk_reaching(std::min(n, c2 + nb));
-        if (!options().feed_lazy) {
-          int ql = nq;
-          while (ql < feed->nchunks && cudaEventQuery(feed->ready[ql]) == cudaSuccess) ++ql;
-          cudaGetLastError();   // (a not-ready query leaves no error behind)
-          qend = std::max(qend, ql);
+        // the columns the next step needs (the block column after the next
+        // one), current before this block column's interchanges reach them;
+        // then landed chunks, a few block columns of catch-up per step
+        rc = take_in_now(std::min(n, c2 + nb), k);
+        if (!rc && options().feed_lazy != 1) {
+          // feed_lazy 2 (a test setting) takes the next chunk in every step, landed or not
+          if (pend_end <= win)
+            rc = take_in(options().feed_lazy == 2 ? std::min(feed->nchunks, nq + 1) : chunks_landed(), k);
+          const int budget = options().feed_catchup;   // block columns per step, 0: all at once
+          if (!rc) rc = catch_up(budget > 0 ? std::min(k, pend_k + budget) : k, k);
         }
-        rc = admit_upto(qend, k);
         if (rc) return rc;
       }
-      // then the columns left of the block column and the rest of the trailing matrix
-      rc = laswp_log<T>(dA, lda, 0, j, c2, win, cx, cx.perm, s);
+      // then the columns left of the block column and the rest of the
+      // trailing matrix (the pending slab takes the interchanges too)
+      rc = laswp_log<T>(dA, lda, 0, j, c2, std::max(win, pend_end), cx, cx.perm, s);
       if (!rc && c2 < win) {
         rc = block_row_u<T>(dA, lda, j, jb, c2, win, lv, s, gemm_mode);
         if (!rc && j2 < m) rc = update(win - c2, c2 - j);
@@ -892,7 +933,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
     }
     // columns right of min(m, n) still outside (wide matrices)
     if (feed) {
-      const int rc = admit_upto(feed->nchunks, k);
+      const int rc = take_in_now(n, k);
       if (rc) return rc;
     }
     return (int)cudaGetLastError();

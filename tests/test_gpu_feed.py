@@ -59,7 +59,7 @@ def _both(gpu, a, b, **kv):
 
 
 @pytest.mark.parametrize("n,nrhs", [(600, 1), (3000, 1), (5000, 3), (8192, 2)])
-@pytest.mark.parametrize("lazy", [0, 1])
+@pytest.mark.parametrize("lazy", [0, 1, 2])
 @pytest.mark.parametrize("mixed", [0, 1])          # BF16x3 tensor cores / FP32 CUDA cores
 def test_fed_dsgesv_matches_whole_copy(gpu, n, nrhs, lazy, mixed):
     a, b = _system(n, nrhs, 3 + n)
@@ -68,8 +68,21 @@ def test_fed_dsgesv_matches_whole_copy(gpu, n, nrhs, lazy, mixed):
     assert r1[3] >= 0 and r1[4] == 0
 
 
+@pytest.mark.parametrize("catchup", [0, 1, 3, 8])
+@pytest.mark.parametrize("mixed", [0, 1])
+def test_fed_dsgesv_spread_catchup(gpu, catchup, mixed):
+    """A chunk taken in at every step (feed_lazy 2) while the ones before
+    are still catching up a few block columns per step (catchup; 0: all at
+    once): the pending columns take every later interchange with the rest
+    of the matrix and join when current -- same bits."""
+    n = 9000                                      # 16 chunks of 563 columns, 36 block columns
+    a, b = _system(n, 1, 7)
+    r0, r1 = _both(gpu, a, b, feed_lazy=2, feed_catchup=catchup, mixed=mixed)
+    _same(r0, r1)
+
+
 @pytest.mark.parametrize("n", [2500, 4500])
-@pytest.mark.parametrize("lazy", [0, 1])
+@pytest.mark.parametrize("lazy", [0, 1, 2])
 def test_fed_dsgesv_exact_matches_whole_copy_and_oracle(gpu, exact_mode, n, lazy):
     """Exact mode with the FP32 CUDA-core factorization (the SGETRF
     arithmetic): 2048-column chunks continue one running row sum; the result
