@@ -31,7 +31,7 @@ unsigned long long* phase_buffer() {
 }
 int g_nb_table[2][kBatBuckets] = {
     {16, 32, 32, 32, 32, 32, 32, 32},   // double (capacity 32)
-    {16, 32, 32, 32, 64, 64, 64, 64},   // float (capacity 64)
+    {16, 32, 32, 32, 32, 32, 32, 32},   // float (capacity 32)
 };
 
 template <typename T, bool EXACT>

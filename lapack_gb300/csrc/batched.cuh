@@ -24,10 +24,13 @@
 
 namespace gb {
 
-// threads per CTA: 512 for FP32 (more warps to hide the latency of the
-// per-column steps), 256 for FP64 (whose tiles need more registers)
+// threads per CTA: 256 (eight warps: the block-row solve takes eight
+// columns per warp over a 64-column chunk).  FP32 fits two CTAs per SM
+// (128 registers, 83 KB of shared memory with a 32-column panel), so two
+// systems' per-column latencies overlap on every SM; one 512-thread CTA per
+// SM with a 64-column panel was 1.6x slower over the uneven batch.
 template <typename T>
-constexpr int bat_threads() { return sizeof(T) == 4 ? 512 : 256; }
+constexpr int bat_threads() { return 256; }
 constexpr int kBatMaxN = 512;
 constexpr int kBatMaxNb = 64;               // panel width cap (FP64 is limited to 32 by shared memory)
 constexpr int kBatMaxRhs = 4;
@@ -35,6 +38,10 @@ constexpr int kBatBuckets = kBatMaxN / 64;   // size buckets of 64 rows
 constexpr int kBatUChunk = 64;               // U12 columns staged per chunk
 constexpr int kBatUStride = kBatUChunk + 8;  // row stride of the staged chunk (spreads the solve's lanes over the banks)
 constexpr int kBatDefer = 4;                 // panel columns whose rank-1 updates are applied together
+static_assert(bat_threads<float>() / 32 * 8 >= kBatUChunk && bat_threads<double>() / 32 * 8 >= kBatUChunk,
+              "the block-row solve takes eight columns per warp");
+static_assert(bat_threads<float>() >= kBatMaxNb && bat_threads<double>() >= kBatMaxNb,
+              "the pivot-row step takes one thread per panel column");
 
 // panel [cap][512] + U12 chunk [cap][kBatUStride] + B [4][512] + labels and pairs
 template <typename T>
@@ -43,7 +50,7 @@ constexpr size_t batched_smem_bytes(int cap) {
          sizeof(int) * (4 * kBatMaxNb + kBatMaxN) + 64;
 }
 template <typename T>
-constexpr int batched_cap() { return sizeof(T) == 8 ? 32 : 64; }
+constexpr int batched_cap() { return 32; }
 
 template <typename T>
 struct BatchArgs {
@@ -365,7 +372,8 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
                                   T* __restrict__ B, int ldb, unsigned char* smem, int cap) {
   constexpr int kBatThreads = bat_threads<T>();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  T* Lc = bat_panel<T>(smem);                               // [kBatSolveChunk][n] chunk of factors (cap >= 32)
+  T* Lc = bat_panel<T>(smem);                               // [sc][n] chunk of factors, sc <= cap
+  const int sc = min(kBatSolveChunk, cap);
   T* Bs = bat_rhs<T>(smem, cap);                            // [nrhs][kBatMaxN]
   for (int e = tid; e < n * nrhs; e += kBatThreads) {
     const int q = e / n, r = e - q * n;
@@ -381,8 +389,8 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
   }
   __syncthreads();
   // L (unit lower): columns k0..k0+31 staged, rows k0..n-1
-  for (int k0 = 0; k0 < n; k0 += kBatSolveChunk) {
-    const int kw = min(kBatSolveChunk, n - k0), rows = n - k0;
+  for (int k0 = 0; k0 < n; k0 += sc) {
+    const int kw = min(sc, n - k0), rows = n - k0;
     batched_copy<8, kBatThreads, T>(
         kw * rows, tid,
         [&](int e) { const int c = e / rows, r = e - c * rows; return A[(size_t)(k0 + r) + (size_t)(k0 + c) * lda]; },
@@ -399,8 +407,8 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
     __syncthreads();
   }
   // U (non-unit upper): chunks from the bottom, rows 0..k1-1
-  for (int k1 = n; k1 > 0; k1 -= kBatSolveChunk) {
-    const int k0 = max(0, k1 - kBatSolveChunk), kw = k1 - k0, rows = k1;
+  for (int k1 = n; k1 > 0; k1 -= sc) {
+    const int k0 = max(0, k1 - sc), kw = k1 - k0, rows = k1;
     batched_copy<8, kBatThreads, T>(
         kw * rows, tid,
         [&](int e) { const int c = e / rows, r = e - c * rows; return A[(size_t)r + (size_t)(k0 + c) * lda]; },
