@@ -23,7 +23,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TABLE = os.path.join(HERE, "autotune.json")
-CANDIDATES = {0: [8, 16, 32], 1: [8, 16, 32]}          # per dtype code (0 double, 1 float); both panels hold 32 columns
+CANDIDATES = {0: [8, 16], 1: [8, 16, 32]}      # per dtype code (0 double, 1 float): the panel capacities
 
 
 def _time_batch(g, As, Bs, dtype, reps=3):

@@ -25,10 +25,11 @@
 namespace gb {
 
 // threads per CTA: 256 (eight warps: the block-row solve takes eight
-// columns per warp over a 64-column chunk).  FP32 fits two CTAs per SM
-// (128 registers, 83 KB of shared memory with a 32-column panel), so two
-// systems' per-column latencies overlap on every SM; one 512-thread CTA per
-// SM with a 64-column panel was 1.6x slower over the uneven batch.
+// columns per warp over a 64-column chunk), two CTAs per SM (128
+// registers; 83 KB of shared memory with a 32-column FP32 panel, 94 KB with
+// a 16-column FP64 one), so two systems' per-column latencies overlap on
+// every SM.  One CTA per SM was 1.6x slower for FP32 (512 threads, 64-column
+// panel) and 1.2x for FP64 (32-column panel).
 template <typename T>
 constexpr int bat_threads() { return 256; }
 constexpr int kBatMaxN = 512;
@@ -50,7 +51,7 @@ constexpr size_t batched_smem_bytes(int cap) {
          sizeof(int) * (4 * kBatMaxNb + kBatMaxN) + 64;
 }
 template <typename T>
-constexpr int batched_cap() { return 32; }
+constexpr int batched_cap() { return sizeof(T) == 8 ? 16 : 32; }
 
 template <typename T>
 struct BatchArgs {
@@ -435,7 +436,7 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
 }
 
 template <typename T, bool EXACT>
-__global__ void __launch_bounds__(bat_threads<T>())
+__global__ void __launch_bounds__(bat_threads<T>(), 2)
 batched_gesv_kernel(BatchArgs<T> a) {
   extern __shared__ __align__(16) unsigned char bat_smem[];
   __shared__ int sys_s;
