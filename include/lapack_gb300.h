@@ -450,14 +450,16 @@ int gb300_vbatched_profile_read(unsigned long long* cycles);
  * after it, [5] the update.  gb300_leaf_profile_read copies the six sums
  * and clears them.  Returns the previous switch / 0, or -1. */
 int gb300_leaf_profile(int on);
-/* Timeline of the host-pointer DSGESV's fed factorization (test and bench
- * hook, no reference counterpart): with gb300_feed_trace(1) later calls
- * record, on the device, the start of the copies (kind 3), each chunk
- * landed and converted (kind 2, idx = chunk), each chunk taken into the
- * factorization (kind 1, idx = chunk, aux = the block-column step it
- * joined at) and each step's end (kind 0, idx = step, aux = columns taken
- * in); gb300_feed_trace_read returns up to cap records with their times in
- * ms after the first (waits for the last), or -1. */
+/* Timeline of the look-ahead FP32 factorization and of the host-pointer
+ * DSGESV's copies (test and bench hook, no reference counterpart): with
+ * gb300_feed_trace(1) later calls record, on the device, the start of the
+ * copies (kind 3), each chunk landed and converted (kind 2, idx = chunk),
+ * each chunk taken into the factorization (kind 1, idx = chunk, aux = the
+ * block-column step it joined at), each panel's start and end (kinds 6, 7,
+ * idx = step), the next block column ready for the next panel (kind 5) and
+ * each step's end (kind 0, idx = step, aux = columns taken in);
+ * gb300_feed_trace_read returns up to cap records with their times in ms
+ * after the first (waits for the last), or -1. */
 int gb300_feed_trace(int on);
 int gb300_feed_trace_read(int* kind, int* idx, int* aux, double* ms, int cap);
 int gb300_leaf_profile_read(unsigned long long* cycles);

@@ -614,6 +614,22 @@ static int block_row_u(T* dA, int lda, int j, int jb, int c_beg, int c_end, cons
   return trsm_llnu_dev<T>(jb, c_end - c_beg, Ajj, lda, U, lda, s, gemm_mode);
 }
 
+// The U rows of the block column next to j (the look-ahead's critical
+// path: the next panel waits for them).  In the BF16x3 mode they come from
+// FP32 substitution in the one-launch 128-row solves (no L11^{-1} to form
+// first: the inverse, which the wider rest of the block row uses, is formed
+// after the next panel has been released); otherwise as block_row_u.  Both
+// schedules (look-ahead or not) use this for the next block column and
+// block_row_u for the rest, so they compute the same.
+template <typename T>
+static int next_block_row_u(T* dA, int lda, int j, int jb, int c_beg, int c_end, bool linv_mode, cudaStream_t s,
+                            int gemm_mode) {
+  if (c_end <= c_beg) return 0;
+  if (!linv_mode) return block_row_u<T>(dA, lda, j, jb, c_beg, c_end, nullptr, s, gemm_mode);
+  T* Ajj = dA + j + (size_t)j * lda;
+  return trsm_llnu_dev<T>(jb, c_end - c_beg, Ajj, lda, dA + j + (size_t)c_beg * lda, lda, s, kMixedFp32, false);
+}
+
 template <typename T>
 static int form_linv(T* dA, int lda, int j, int jb, T* linv, cudaStream_t s) {
   if constexpr (sizeof(T) == 4) {
@@ -870,16 +886,16 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       cx.log_cnt = lcnt + b * kMaxLogSlots;
       cx.log.nslots = 0;
       GB_CUDA_TRY(cudaMemsetAsync(cx.log_cnt, 0, sizeof(int) * kMaxLogSlots, sp));
+      if (g_feed_trace.on) g_feed_trace.add(6, k, 0, sp);   // panel k starts
       int rc = getrf_rec<T>(dA, lda, m, n, j, jb, dIpiv, dInfo, cx, sp, gemm_mode);
       if (rc) return rc;
+      if (g_feed_trace.on) g_feed_trace.add(7, k, 0, sp);   // panel k done
       GB_CUDA_TRY(cudaEventRecord(lr->P[b], sp));
       GB_CUDA_TRY(cudaStreamWaitEvent(s, lr->P[b], 0));
       const int j2 = j + jb;
       const int nb2 = j2 < mn ? std::min(nb, mn - j2) : 0;   // next block column
       T* Ajj = dA + j + (size_t)j * lda;
       T* lv = linv_hist ? linv_hist + (size_t)k * nb * nb : linv;
-      rc = form_linv<T>(dA, lda, j, jb, lv, s);
-      if (rc) return rc;
       // the BF16 split of A21, made once for both updates of this block column
       // (stream s orders it after the previous column's updates that read the buffer)
       const bool presplit = a21buf.p && j2 < m;
@@ -900,11 +916,15 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       // next block column first
       if (nb2 > 0) {
         rc = laswp_log<T>(dA, lda, j2, j2 + nb2, 0, 0, cx, nullptr, s);
-        if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, lv, s, gemm_mode);
+        if (!rc) rc = next_block_row_u<T>(dA, lda, j, jb, j2, j2 + nb2, lv != nullptr, s, gemm_mode);
         if (!rc && j2 < m) rc = update(nb2, jb);
         if (rc) return rc;
       }
       GB_CUDA_TRY(cudaEventRecord(lr->L[b], s));
+      if (g_feed_trace.on) g_feed_trace.add(5, k, 0, s);    // next block column ready for panel k+1
+      // L11^{-1} for the rest of the block row, off the next panel's path
+      rc = form_linv<T>(dA, lda, j, jb, lv, s);
+      if (rc) return rc;
       const int c2 = j2 + nb2;
       if (feed) {
         // the columns the next step needs (the block column after the next
@@ -929,7 +949,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       }
       if (rc) return rc;
       if (feed) GB_CUDA_TRY(cudaEventRecord(steps.e[k & 3], s));
-      if (feed && g_feed_trace.on) g_feed_trace.add(0, k, win, s);
+      if (g_feed_trace.on) g_feed_trace.add(0, k, win, s);
     }
     // columns right of min(m, n) still outside (wide matrices)
     if (feed) {
@@ -948,7 +968,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
       const int j2 = j + jb;
       const int c2 = j2 + (j2 < mn ? std::min(nb, mn - j2) : 0);   // next block column, then the rest
       rc = form_linv<T>(dA, lda, j, jb, linv, s);
-      if (!rc) rc = block_row_u<T>(dA, lda, j, jb, j2, std::min(c2, n), linv, s, gemm_mode);
+      if (!rc) rc = next_block_row_u<T>(dA, lda, j, jb, j2, std::min(c2, n), linv != nullptr, s, gemm_mode);
       if (!rc) rc = block_row_u<T>(dA, lda, j, jb, c2, n, linv, s, gemm_mode);
       if (rc) return rc;
       if (j + jb < m) {
@@ -1210,8 +1230,9 @@ int gb300_feed_trace(int on) {
   gb::g_feed_trace.on = on != 0;
   return old;
 }
-// Up to cap records of the last fed factorizations: kind (0 step end, 1
-// chunk taken in, 2 chunk landed and converted, 3 start of the copies),
+// Up to cap records of the last look-ahead factorizations: kind (0 step end,
+// 1 chunk taken in, 2 chunk landed and converted, 3 start of the copies, 5
+// next block column ready, 6 panel start, 7 panel end),
 // index (step or chunk), aux (columns in the window, or the step a chunk
 // joined at), milliseconds after the first record.
 int gb300_feed_trace_read(int* kind, int* idx, int* aux, double* ms, int cap) {
