@@ -720,7 +720,8 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   const size_t log_ints = (size_t)kMaxLogSlots * 2 * kLeafMax;
   size_t o_log = carve(sizeof(int) * 4 * log_ints);
   size_t o_lcnt = carve(sizeof(int) * 2 * kMaxLogSlots);
-  size_t o_linv = carve(sizeof(T) * 256 * 256);
+  const int nb_inv = std::min(std::max(nb, 1), 512);   // L11^{-1} up to 512 x 512 (BF16x3 mode)
+  size_t o_linv = carve(sizeof(T) * (size_t)nb_inv * nb_inv);
   size_t o_node = carve(sizeof(int));
   DevScratch ws(bytes, s);
   if (!ws.p) return (int)cudaErrorMemoryAllocation;
@@ -762,7 +763,7 @@ int getrf_dev(int m, int n, T* dA, int lda, int* dIpiv, int* dInfo, cudaStream_t
   }
   // inverse of the block column's unit lower triangle (BF16x3 mode only:
   // the exact and FP32 modes keep the substitution of SRC/dgetrf.f:204)
-  T* linv = (sizeof(T) == 4 && gemm_mode == kMixedBf16x3 && !options().exact && nb <= 256)
+  T* linv = (sizeof(T) == 4 && gemm_mode == kMixedBf16x3 && !options().exact && nb <= 512)
                 ? reinterpret_cast<T*>(base + o_linv)
                 : nullptr;
   LookaheadRes* lr = la ? lookahead_res() : nullptr;
