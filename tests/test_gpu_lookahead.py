@@ -48,7 +48,7 @@ def test_lookahead_exact_bitwise_vs_oracle(gpu, exact_mode, m, n, nb):
 
 
 @pytest.mark.parametrize("mode", [1, 0])            # sgetrf on FP32 CUDA cores / on BF16x3 tensor cores
-@pytest.mark.parametrize("m,n,nb", [(1536, 1536, 256), (1300, 1100, 128), (3000, 3000, 256)])
+@pytest.mark.parametrize("m,n,nb", [(1536, 1536, 256), (1300, 1100, 128), (3000, 3000, 256), (2500, 2500, 384)])
 def test_lookahead_on_off_identical(gpu, mode, m, n, nb):
     a = _rand(m, n, 3 + m)
     with _opts(gpu, nb32=nb, sgetrf=mode, lookahead=0):
