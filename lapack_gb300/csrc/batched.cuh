@@ -103,6 +103,29 @@ template <> struct Vec16<double> {
 
 // Shared-memory layout, sized for the widest panel `cap`:
 // [panel cap x 512][U12 chunk cap x kBatUStride][B 4 x 512][labels 512][pairs 2 x 128]
+// Copies a rows x cols block element (r, c) from src(r, c) to dst(r, c, v):
+// warp w takes columns w, w + NT/32, ..., its lanes the rows, 32 bytes of
+// loads per lane in flight before the stores (no index division per element).
+template <int NT, typename T, typename Src, typename Dst>
+__device__ __forceinline__ void colwise_copy(int rows, int cols, int tid, Src src, Dst dst) {
+  constexpr int U = 32 / (int)sizeof(T);
+  const int warp = tid >> 5, lane = tid & 31;
+  for (int c = warp; c < cols; c += NT / 32)
+    for (int r0 = 0; r0 < rows; r0 += 32 * U) {
+      T v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + lane + 32 * u;
+        if (r < rows) v[u] = src(r, c);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + lane + 32 * u;
+        if (r < rows) dst(r, c, v[u]);
+      }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ T* bat_panel(unsigned char* smem) { return reinterpret_cast<T*>(smem); }
 template <typename T>
@@ -138,9 +161,9 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     const int M = n - j;
     const int Mp = (M + 3) & ~3;          // panel column stride: 16-byte aligned columns
     // 1. stage the panel and factor it column by column
-    batched_copy<8, kBatThreads, T>(
-        jb * M, tid, [&](int e) { const int c = e / M, r = e - c * M; return A[(size_t)(j + r) + (size_t)(j + c) * lda]; },
-        [&](int e, T v) { const int c = e / M, r = e - c * M; P[c * Mp + r] = v; });
+    colwise_copy<kBatThreads, T>(
+        M, jb, tid, [&](int r, int c) { return A[(size_t)(j + r) + (size_t)(j + c) * lda]; },
+        [&](int r, int c, T v) { P[c * Mp + r] = v; });
     for (int r = tid; r < M; r += kBatThreads) lab[r] = r;
     __syncthreads();
     clk.mark(kBatPhStage);
@@ -234,10 +257,9 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     __syncthreads();
     clk.mark(kBatPhPanel);
     // write the factored panel back
-    for (int e = tid; e < jb * M; e += kBatThreads) {
-      const int c = e / M, r = e - c * M;
-      A[(size_t)(j + r) + (size_t)(j + c) * lda] = P[c * Mp + r];
-    }
+    colwise_copy<kBatThreads, T>(
+        M, jb, tid, [&](int r, int c) { return P[c * Mp + r]; },
+        [&](int r, int c, T v) { A[(size_t)(j + r) + (size_t)(j + c) * lda] = v; });
     // 2. interchanges of the other columns as a gather over the moved rows
     // (at most 2 jb rows moved; their order in the list does not matter:
     // every source is read before any destination is written)
@@ -288,10 +310,9 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     //    increasing kk, the order of BLAS/SRC/dtrsm.f:290-300).
     for (int cb = 0; cb < ncol; cb += kBatUChunk) {
       const int cw = min(kBatUChunk, ncol - cb);
-      batched_copy<8, kBatThreads, T>(
-          jb * cw, tid,
-          [&](int e) { const int c = e / jb, r = e - c * jb; return A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda]; },
-          [&](int e, T v) { const int c = e / jb, r = e - c * jb; U[r * kBatUStride + c] = v; });
+      colwise_copy<kBatThreads, T>(
+          jb, cw, tid, [&](int r, int c) { return A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda]; },
+          [&](int r, int c, T v) { U[r * kBatUStride + c] = v; });
       __syncthreads();
       {
         const int lane = tid & 31, c = 8 * (tid >> 5) + (lane & 7), q = lane >> 3;
@@ -307,10 +328,9 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
         }
       }
       __syncthreads();
-      for (int e = tid; e < jb * cw; e += kBatThreads) {
-        const int c = e / jb, r = e - c * jb;
-        A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] = U[r * kBatUStride + c];
-      }
+      colwise_copy<kBatThreads, T>(
+          jb, cw, tid, [&](int r, int c) { return U[r * kBatUStride + c]; },
+          [&](int r, int c, T v) { A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] = v; });
       clk.mark(kBatPhTrsm);
       // each thread: a 4 x 4 tile of the chunk per pass, its operands read
       // from shared memory with 16-byte loads.  Tile rows start at the
@@ -376,10 +396,9 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
   T* Lc = bat_panel<T>(smem);                               // [sc][n] chunk of factors, sc <= cap
   const int sc = min(kBatSolveChunk, cap);
   T* Bs = bat_rhs<T>(smem, cap);                            // [nrhs][kBatMaxN]
-  for (int e = tid; e < n * nrhs; e += kBatThreads) {
-    const int q = e / n, r = e - q * n;
-    Bs[q * kBatMaxN + r] = B[(size_t)r + (size_t)q * ldb];
-  }
+  colwise_copy<kBatThreads, T>(
+      n, nrhs, tid, [&](int r, int q) { return B[(size_t)r + (size_t)q * ldb]; },
+      [&](int r, int q, T v) { Bs[q * kBatMaxN + r] = v; });
   __syncthreads();
   if (warp < nrhs && lane == 0) {
     T* x = Bs + warp * kBatMaxN;
@@ -392,10 +411,9 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
   // L (unit lower): columns k0..k0+31 staged, rows k0..n-1
   for (int k0 = 0; k0 < n; k0 += sc) {
     const int kw = min(sc, n - k0), rows = n - k0;
-    batched_copy<8, kBatThreads, T>(
-        kw * rows, tid,
-        [&](int e) { const int c = e / rows, r = e - c * rows; return A[(size_t)(k0 + r) + (size_t)(k0 + c) * lda]; },
-        [&](int e, T v) { const int c = e / rows, r = e - c * rows; Lc[c * rows + r] = v; });
+    colwise_copy<kBatThreads, T>(
+        rows, kw, tid, [&](int r, int c) { return A[(size_t)(k0 + r) + (size_t)(k0 + c) * lda]; },
+        [&](int r, int c, T v) { Lc[c * rows + r] = v; });
     __syncthreads();
     if (warp < nrhs) {
       T* x = Bs + warp * kBatMaxN;
@@ -410,10 +428,9 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
   // U (non-unit upper): chunks from the bottom, rows 0..k1-1
   for (int k1 = n; k1 > 0; k1 -= sc) {
     const int k0 = max(0, k1 - sc), kw = k1 - k0, rows = k1;
-    batched_copy<8, kBatThreads, T>(
-        kw * rows, tid,
-        [&](int e) { const int c = e / rows, r = e - c * rows; return A[(size_t)r + (size_t)(k0 + c) * lda]; },
-        [&](int e, T v) { const int c = e / rows, r = e - c * rows; Lc[c * rows + r] = v; });
+    colwise_copy<kBatThreads, T>(
+        rows, kw, tid, [&](int r, int c) { return A[(size_t)r + (size_t)(k0 + c) * lda]; },
+        [&](int r, int c, T v) { Lc[c * rows + r] = v; });
     __syncthreads();
     if (warp < nrhs) {
       T* x = Bs + warp * kBatMaxN;
@@ -428,10 +445,9 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
     }
     __syncthreads();
   }
-  for (int e = tid; e < n * nrhs; e += kBatThreads) {
-    const int q = e / n, r = e - q * n;
-    B[(size_t)r + (size_t)q * ldb] = Bs[q * kBatMaxN + r];
-  }
+  colwise_copy<kBatThreads, T>(
+      n, nrhs, tid, [&](int r, int q) { return Bs[q * kBatMaxN + r]; },
+      [&](int r, int q, T v) { B[(size_t)r + (size_t)q * ldb] = v; });
   __syncthreads();
 }
 
