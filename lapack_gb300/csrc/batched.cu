@@ -30,7 +30,7 @@ unsigned long long* phase_buffer() {
   return g_phase[dev];
 }
 int g_nb_table[2][kBatBuckets] = {
-    {16, 32, 32, 32, 32, 32, 32, 32},   // double (capacity 32)
+    {16, 16, 16, 16, 16, 16, 16, 16},   // double (capacity 16)
     {16, 32, 32, 32, 32, 32, 32, 32},   // float (capacity 32)
 };
 

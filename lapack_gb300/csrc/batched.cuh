@@ -24,23 +24,27 @@
 
 namespace gb {
 
-// threads per CTA: 256 (eight warps: the block-row solve takes eight
-// columns per warp over a 64-column chunk), two CTAs per SM (128
-// registers; 83 KB of shared memory with a 32-column FP32 panel, 94 KB with
-// a 16-column FP64 one), so two systems' per-column latencies overlap on
-// every SM.  One CTA per SM was 1.6x slower for FP32 (512 threads, 64-column
-// panel) and 1.2x for FP64 (32-column panel).
+// Threads per CTA and CTAs per SM: two CTAs of 256 threads (eight warps)
+// per SM, 128 registers per thread; a 32-column FP32 panel (83 KB of
+// shared memory per CTA) or a 16-column FP64 one (94 KB).  Two systems per
+// SM overlap their per-column latencies: one 512-thread FP32 CTA per SM with
+// a 64-column panel was 1.7x slower, four 128-thread ones 1.07x; one FP64
+// CTA per SM 1.2x.
 template <typename T>
 constexpr int bat_threads() { return 256; }
+template <typename T>
+constexpr int bat_ctas_per_sm() { return 2; }
 constexpr int kBatMaxN = 512;
 constexpr int kBatMaxNb = 64;               // panel width cap (FP64 is limited to 32 by shared memory)
 constexpr int kBatMaxRhs = 4;
 constexpr int kBatBuckets = kBatMaxN / 64;   // size buckets of 64 rows
-constexpr int kBatUChunk = 64;               // U12 columns staged per chunk
-constexpr int kBatUStride = kBatUChunk + 8;  // row stride of the staged chunk (spreads the solve's lanes over the banks)
+// U12 columns staged per chunk: the block-row solve takes eight columns per warp
+template <typename T>
+constexpr int bat_uchunk_cols() { return bat_threads<T>() / 32 * 8; }
+constexpr int kBatUStride = 64 + 8;          // row stride of the staged chunk (spreads the solve's lanes over the banks)
 constexpr int kBatDefer = 4;                 // panel columns whose rank-1 updates are applied together
-static_assert(bat_threads<float>() / 32 * 8 >= kBatUChunk && bat_threads<double>() / 32 * 8 >= kBatUChunk,
-              "the block-row solve takes eight columns per warp");
+static_assert(bat_uchunk_cols<float>() + 8 <= kBatUStride && bat_uchunk_cols<double>() + 8 <= kBatUStride,
+              "the staged U12 chunk fits its row stride");
 static_assert(bat_threads<float>() >= kBatMaxNb && bat_threads<double>() >= kBatMaxNb,
               "the pivot-row step takes one thread per panel column");
 
@@ -301,15 +305,16 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     clk.mark(kBatPhSwap);
     const int ncol = n - j - jb;
     if (ncol <= 0) continue;
-    // 3 + 4. per chunk of kBatUChunk columns of the block row: stage A12 in
+    // 3 + 4. per chunk of bat_uchunk_cols columns of the block row: stage A12 in
     //    shared memory, U12 = L11^{-1} A12 there (SRC/dgetrf.f:204), write
     //    U12 back, then A22 -= A21 * U12 (SRC/dgetrf.f:212-216) with U12 read
     //    from shared memory.  The triangular solve: warp w takes columns
     //    8w..8w+7, the four lane groups of eight the rows of one residue mod
     //    4, one step per column kk of L11 (every element gets its updates in
     //    increasing kk, the order of BLAS/SRC/dtrsm.f:290-300).
-    for (int cb = 0; cb < ncol; cb += kBatUChunk) {
-      const int cw = min(kBatUChunk, ncol - cb);
+    constexpr int kUChunk = bat_uchunk_cols<T>();
+    for (int cb = 0; cb < ncol; cb += kUChunk) {
+      const int cw = min(kUChunk, ncol - cb);
       colwise_copy<kBatThreads, T>(
           jb, cw, tid, [&](int r, int c) { return A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda]; },
           [&](int r, int c, T v) { U[r * kBatUStride + c] = v; });
@@ -452,7 +457,7 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
 }
 
 template <typename T, bool EXACT>
-__global__ void __launch_bounds__(bat_threads<T>(), 2)
+__global__ void __launch_bounds__(bat_threads<T>(), bat_ctas_per_sm<T>())
 batched_gesv_kernel(BatchArgs<T> a) {
   extern __shared__ __align__(16) unsigned char bat_smem[];
   __shared__ int sys_s;
