@@ -102,3 +102,21 @@ def test_panel_variants_exact_bitwise(gpu, exact_mode, cluster_panel, m, n, nb):
     assert info_g == info_r
     np.testing.assert_array_equal(ip_g, ip_r)
     assert lu_g.tobytes(order="F") == lu_r.tobytes(order="F")
+
+
+@pytest.mark.parametrize("cluster_panel", [1, 2, 3])
+@pytest.mark.parametrize("m,n,nb", [(30000, 256, 256), (9000, 300, 256), (1500, 1500, 256)])
+def test_panel_variants_default_mode_identical(gpu, cluster_panel, m, n, nb):
+    """In the default (fused multiply-add) mode every leaf kernel still gives
+    each element its updates in increasing k, one FMA each (the cluster
+    leaves defer them in groups of four and apply the group in order), so
+    SGETRF on the FP32 CUDA cores is bitwise the same whichever kernel
+    factors the leaves."""
+    a = _rand(m, n, 7 + m + n)
+    with _opts(gpu, nb32=nb, sgetrf=1, cluster_panel=0):
+        lu0, ip0, info0 = gpu.getrf(a)
+    with _opts(gpu, nb32=nb, sgetrf=1, cluster_panel=cluster_panel):
+        lu1, ip1, info1 = gpu.getrf(a)
+    assert info0 == info1
+    np.testing.assert_array_equal(ip0, ip1)
+    assert lu0.tobytes(order="F") == lu1.tobytes(order="F")
