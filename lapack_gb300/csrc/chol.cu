@@ -5,11 +5,15 @@
 // The factorization follows the reference's left-looking block order: for
 // each block column, a DSYRK of the diagonal block with the columns to its
 // left, DPOTRF2 of the diagonal block, then the DGEMM and DTRSM of the
-// block below (lower) or to the right (upper).  Every step is one kernel
-// whose threads each compute one element, one row or one column through
-// the shared host/device functions of potrf_seq.h (checked against the
-// oracle on the CPU); the diagonal blocks (at most NB = 64 columns) are
-// factored on one thread.  The solves use the library's triangular solve
+// block below (lower) or to the right (upper).  The DGEMM -- the O(n^3)
+// part -- and the DSYRK of the diagonal block run on the tiled update kernel
+// in the reference's per-element orders with separately rounded products
+// (the DSYRK stores one triangle and, in the lower form, skips the terms
+// whose A(J,L) is zero, as BLAS/SRC/dsyrk.f:313-320 does).  The DTRSM and the
+// diagonal blocks' DPOTRF2 (at most NB = 64 columns, on one thread over
+// shared memory) are kernels whose threads each compute one row or column
+// through the shared host/device functions of potrf_seq.h (checked against
+// the oracle on the CPU).  The solves use the library's triangular solve
 // kernels.  DSPOSV mirrors DSGESV: FP32 Cholesky and solves, FP64 residual
 // with the reference's DSYMM order, the same convergence test, the FP64
 // fallback.
@@ -28,30 +32,50 @@ unsigned nblocks(size_t n, int per = 256) { return (unsigned)((n + per - 1) / pe
 
 constexpr int kCholNb = 64;   // ILAENV(1, 'xPOTRF')
 
-// DSYRK of the jb x jb diagonal block: one thread per element of its triangle.
+// DPOTRF2 of a diagonal block.  On the GPU a block of up to 64 x 64 is
+// staged in shared memory and factored by the whole CTA (potrf2_par: the
+// rows or columns of each DTRSM and the elements of each DSYRK spread over
+// the threads, the recursion's order per element unchanged), then written
+// back; a larger one is factored by one thread in place.
+constexpr int kPotrf2Threads = 256;
+#ifdef __CUDA_ARCH__
+struct CtaSync {
+  __device__ void operator()() const { __syncthreads(); }
+};
+#endif
 template <typename T>
-__global__ void syrk_tri_kernel(int upper, int jb, int k, const T* __restrict__ Aop, int lda, T* __restrict__ C,
-                                int ldc) {
-  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)jb * jb) return;
-  const int j = (int)(e / jb), i = (int)(e - (size_t)j * jb);
-  if (upper ? (i > j) : (i < j)) return;
-  syrk_elem(upper, i, j, k, T(-1), Aop, lda, C, ldc);
+__global__ void __launch_bounds__(kPotrf2Threads) potrf2_kernel(int upper, int n, T* __restrict__ A, int lda,
+                                                                int* __restrict__ info) {
+#ifdef __CUDA_ARCH__
+  if (n <= 64) {
+    __shared__ T D[64 * 64];
+    for (int e = threadIdx.x; e < n * n; e += kPotrf2Threads) {
+      const int c = e / n, r = e - c * n;
+      D[r + c * n] = A[(size_t)r + (size_t)c * lda];
+    }
+    __syncthreads();
+    const int r = potrf2_par(upper, n, D, n, (int)threadIdx.x, kPotrf2Threads, CtaSync{});
+    if (threadIdx.x == 0) *info = r;
+    __syncthreads();
+    for (int e = threadIdx.x; e < n * n; e += kPotrf2Threads) {
+      const int c = e / n, r = e - c * n;
+      A[(size_t)r + (size_t)c * lda] = D[r + c * n];
+    }
+    return;
+  }
+#endif
+  if (blockIdx.x == 0 && threadIdx.x == 0) *info = potrf2_seq(upper, n, A, lda);
 }
 
+// dst(c, r) = src(r, c) for an rows x cols block: the transposed operand of
+// DPOTRF's DGEMM update, which the tiled update kernel reads untransposed.
 template <typename T>
-__global__ void __launch_bounds__(1) potrf2_kernel(int upper, int n, T* __restrict__ A, int lda, int* __restrict__ info) {
-  *info = potrf2_seq(upper, n, A, lda);
-}
-
-// DPOTRF's DGEMM update of an m x ncols block: one thread per element.
-template <typename T>
-__global__ void gemm_chol_kernel(int upper, int m, int ncols, int k, const T* __restrict__ A, int lda,
-                                 const T* __restrict__ B, int ldb, T* __restrict__ C, int ldc) {
+__global__ void transpose_kernel(int rows, int cols, const T* __restrict__ src, int lds, T* __restrict__ dst,
+                                 int ldd) {
   const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)m * ncols) return;
-  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
-  gemm_chol_elem(upper, i, j, k, T(-1), A, lda, B, ldb, C, ldc);
+  if (e >= (size_t)rows * cols) return;
+  const int c = (int)(e / rows), r = (int)(e - (size_t)c * rows);
+  dst[(size_t)c + (size_t)r * ldd] = src[(size_t)r + (size_t)c * lds];
 }
 
 template <typename T>
@@ -115,7 +139,7 @@ int potrf_dev(bool upper, int n, T* A, int lda, int nb, int* info, cudaStream_t 
   int* dinfo = ib.as<int>();
   const int up = upper ? 1 : 0;
   auto diag_factor = [&](int off, int jb) -> int {
-    GB_LAUNCH(potrf2_kernel<T><<<1, 1, 0, s>>>(up, jb, A + off + (size_t)off * lda, lda, dinfo));
+    GB_LAUNCH(potrf2_kernel<T><<<1, kPotrf2Threads, 0, s>>>(up, jb, A + off + (size_t)off * lda, lda, dinfo));
     int h = 0;
     GB_CUDA_TRY(cudaMemcpyAsync(&h, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
     GB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -123,29 +147,50 @@ int potrf_dev(bool upper, int n, T* A, int lda, int nb, int* info, cudaStream_t 
     return 0;
   };
   if (nb <= 1 || nb >= n) return diag_factor(0, n);
+  // the transposed jb x j operand of the DGEMM update (at most nb x n)
+  DevScratch tb(sizeof(T) * (size_t)nb * n, s);
+  if (!tb.p) return (int)cudaErrorMemoryAllocation;
+  T* Tt = tb.as<T>();
   for (int j = 0; j < n; j += nb) {
     const int jb = std::min(nb, n - j);
     T* d = A + j + (size_t)j * lda;
+    int rc = 0;
     if (j > 0) {
-      const T* aop = upper ? A + (size_t)j * lda : A + j;
-      GB_LAUNCH(syrk_tri_kernel<T><<<nblocks((size_t)jb * jb), 256, 0, s>>>(up, jb, j, aop, lda, d, lda));
+      // the block's left (L) or upper (U) neighbour transposed, for the DSYRK
+      // and the DGEMM: L: A(j:j+jb, 0:j)^T (j x jb); U: A(0:j, j:j+jb)^T (jb x j)
+      if (!upper) {
+        GB_LAUNCH(transpose_kernel<T><<<nblocks((size_t)jb * j), 256, 0, s>>>(jb, j, A + j, lda, Tt, j));
+        rc = syrk_exact_dev<T>(false, jb, j, A + j, lda, Tt, j, d, lda, s);
+      } else {
+        GB_LAUNCH(transpose_kernel<T><<<nblocks((size_t)j * jb), 256, 0, s>>>(j, jb, A + (size_t)j * lda, lda, Tt,
+                                                                                 jb));
+        rc = syrk_exact_dev<T>(true, jb, j, Tt, jb, A + (size_t)j * lda, lda, d, lda, s);
+      }
+      if (rc) return rc;
     }
-    int rc = diag_factor(j, jb);
+    rc = diag_factor(j, jb);
     if (rc || *info) return rc;
     const int rest = n - j - jb;
     if (rest <= 0) continue;
+    // the DGEMM update on the tiled update kernel, in the reference's
+    // per-element order (dgemm.f: 'N','T' products subtracted in turn for L,
+    // 'T','N' products summed then subtracted for U), then the DTRSM
     if (!upper) {
       T* c = A + (j + jb) + (size_t)j * lda;
-      if (j > 0)
-        GB_LAUNCH(gemm_chol_kernel<T><<<nblocks((size_t)rest * jb), 256, 0, s>>>(0, rest, jb, j, A + j + jb, lda,
-                                                                                  A + j, lda, c, lda));
-      GB_LAUNCH(trsm_rltn_kernel<T><<<nblocks(rest), 256, 0, s>>>(rest, jb, d, lda, c, lda));
+      if (j > 0) {
+        // C(rest x jb) -= A(j+jb:n, 0:j) * A(j:j+jb, 0:j)^T
+        rc = gemm_exact_dev<T>(false, rest, jb, j, A + j + jb, lda, Tt, j, c, lda, s);
+        if (rc) return rc;
+      }
+      GB_LAUNCH(trsm_rltn_kernel<T><<<nblocks(rest, 64), 64, 0, s>>>(rest, jb, d, lda, c, lda));
     } else {
       T* c = A + j + (size_t)(j + jb) * lda;
-      if (j > 0)
-        GB_LAUNCH(gemm_chol_kernel<T><<<nblocks((size_t)jb * rest), 256, 0, s>>>(
-            1, jb, rest, j, A + (size_t)j * lda, lda, A + (size_t)(j + jb) * lda, lda, c, lda));
-      GB_LAUNCH(trsm_lutn_kernel<T><<<nblocks(rest), 256, 0, s>>>(rest, jb, d, lda, c, lda));
+      if (j > 0) {
+        // C(jb x rest) -= A(0:j, j:j+jb)^T * A(0:j, j+jb:n)
+        rc = gemm_exact_dev<T>(true, jb, rest, j, Tt, jb, A + (size_t)(j + jb) * lda, lda, c, lda, s);
+        if (rc) return rc;
+      }
+      GB_LAUNCH(trsm_lutn_kernel<T><<<nblocks(rest, 64), 64, 0, s>>>(rest, jb, d, lda, c, lda));
     }
   }
   return (int)cudaGetLastError();

@@ -16,7 +16,14 @@
 
 namespace gb {
 
-template <typename T, int BM, int BN, int BK, int TM, int TN, bool EXACT>
+// SUM_FIRST: the products are summed from zero in increasing k and the sum
+// subtracted from C once (the 'T','N' form of BLAS/SRC/dgemm.f:348-360 with
+// ALPHA = -1, BETA = 1) instead of each product subtracted in turn.
+// TRI: 1 stores only the elements on or below the diagonal of C, 2 only
+// those on or above it (DSYRK's triangle).  SKIPZ: a term whose B element is
+// zero is skipped (BLAS/SRC/dsyrk.f:313-320, IF (A(J,L).NE.ZERO)).
+template <typename T, int BM, int BN, int BK, int TM, int TN, bool EXACT, bool SUM_FIRST = false, int TRI = 0,
+          bool SKIPZ = false>
 __global__ void __launch_bounds__((BM / TM) * (BN / TN), 1)
 gemm_nn_update_kernel(int M, int N, int K, const T* __restrict__ A, int lda,
                       const T* __restrict__ B, int ldb, T* __restrict__ C, int ldc) {
@@ -27,6 +34,7 @@ gemm_nn_update_kernel(int M, int N, int K, const T* __restrict__ A, int lda,
   const int tid = threadIdx.x;
   const int tx = tid % TX, ty = tid / TX;
   const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  if ((TRI == 1 && m0 + BM <= n0) || (TRI == 2 && m0 >= n0 + BN)) return;   // tile outside the triangle
 
   T acc[TM][TN];
 #pragma unroll
@@ -35,7 +43,7 @@ gemm_nn_update_kernel(int M, int N, int K, const T* __restrict__ A, int lda,
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       int m = m0 + tx + i * TX;
-      acc[i][j] = (m < M && n < N) ? C[(size_t)m + (size_t)n * ldc] : T(0);
+      acc[i][j] = (!SUM_FIRST && m < M && n < N) ? C[(size_t)m + (size_t)n * ldc] : T(0);
     }
   }
 
@@ -91,7 +99,10 @@ gemm_nn_update_kernel(int M, int N, int K, const T* __restrict__ A, int lda,
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < TN; ++j) acc[i][j] = fnmadd<EXACT>(a[i], b[j], acc[i][j]);
+        for (int j = 0; j < TN; ++j) {
+          const T r = SUM_FIRST ? fmadd<EXACT>(a[i], b[j], acc[i][j]) : fnmadd<EXACT>(a[i], b[j], acc[i][j]);
+          acc[i][j] = (SKIPZ && b[j] == T(0)) ? acc[i][j] : r;
+        }
     }
     if (t + 1 < nk) {
       store_shared(buf ^ 1);
@@ -104,7 +115,11 @@ gemm_nn_update_kernel(int M, int N, int K, const T* __restrict__ A, int lda,
 #pragma unroll
     for (int i = 0; i < TM; ++i) {
       int m = m0 + tx + i * TX;
-      if (m < M && n < N) C[(size_t)m + (size_t)n * ldc] = acc[i][j];
+      if (m < M && n < N && (TRI != 1 || m >= n) && (TRI != 2 || m <= n)) {
+        T* pc = C + (size_t)m + (size_t)n * ldc;
+        if constexpr (SUM_FIRST) *pc = fnmadd<EXACT>(T(1), acc[i][j], *pc);   // C - sum, one rounding
+        else *pc = acc[i][j];
+      }
     }
   }
 }

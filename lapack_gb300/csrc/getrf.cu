@@ -176,6 +176,68 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
 }
 
 
+// C -= A*B with separately rounded products in the reference DGEMM orders
+// (the Cholesky factorization's updates, SRC/dpotrf.f): sum_first false,
+// each product subtracted from C in increasing k ('N','T' form,
+// BLAS/SRC/dgemm.f:367-383); true, the products summed from zero in
+// increasing k and the sum subtracted once ('T','N' form, dgemm.f:348-360).
+template <typename T, int BM, int BN, int TM, int TN, bool SF, int TRI, bool SKIPZ>
+static void launch_update_tile(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+                               cudaStream_t s) {
+  dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
+  GB_LAUNCH(gemm_nn_update_kernel<T, BM, BN, 16, TM, TN, true, SF, TRI, SKIPZ>
+            <<<grid, (BM / TM) * (BN / TN), 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+}
+
+// The tile is the largest of 128 x 64, 32 x 32 and 16 x 16 that still gives
+// every SM a CTA: the Cholesky's updates are thin (N or M = NB = 64) with a
+// long K, so the CTA count, not the per-CTA reuse, limits them.  The
+// per-element order does not depend on the tile.
+template <typename T, bool SF>
+static void launch_update_by_size(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+                                  cudaStream_t s) {
+  const long sms = device_sm_count();
+  auto ctas = [&](int bm, int bn) { return (long)((M + bm - 1) / bm) * ((N + bn - 1) / bn); };
+  if (ctas(128, 64) >= sms)
+    launch_update_tile<T, 128, 64, 8, 4, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  else if (ctas(32, 32) >= sms)
+    launch_update_tile<T, 32, 32, 2, 2, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  else
+    launch_update_tile<T, 16, 16, 1, 1, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+}
+
+template <typename T>
+int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+                   cudaStream_t s) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  prof_begin(sizeof(T) == 8 ? kProfGemmF64 : kProfGemmF32, s);
+  if (sum_first) launch_update_by_size<T, true>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  else launch_update_by_size<T, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  prof_end(sizeof(T) == 8 ? kProfGemmF64 : kProfGemmF32, s, 2.0 * M * N * (double)K,
+           sizeof(T) * ((double)M * K + (double)K * N + 2.0 * M * N));
+  return (int)cudaGetLastError();
+}
+// DSYRK of the Cholesky's diagonal block in the reference orders, with the
+// other operand transposed: lower ('L','N', dsyrk.f:313-320) C -= A*B on and
+// below the diagonal, each product subtracted in turn, terms with a zero B
+// element skipped; upper ('U','T', dsyrk.f:327-339) the products summed and
+// the sum subtracted, on and above the diagonal.  8 x 8 tiles of 64 threads
+// (one element each): the n x n block (n <= 64) with a K of up to the order
+// of the matrix is spread over as many SMs as it has tiles in its triangle.
+template <typename T>
+int syrk_exact_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t s) {
+  if (n <= 0 || K <= 0) return 0;
+  if (upper) launch_update_tile<T, 8, 8, 1, 1, true, 2, false>(n, n, K, A, lda, B, ldb, C, ldc, s);
+  else launch_update_tile<T, 8, 8, 1, 1, false, 1, true>(n, n, K, A, lda, B, ldb, C, ldc, s);
+  return (int)cudaGetLastError();
+}
+template int syrk_exact_dev<double>(bool, int, int, const double*, int, const double*, int, double*, int, cudaStream_t);
+template int syrk_exact_dev<float>(bool, int, int, const float*, int, const float*, int, float*, int, cudaStream_t);
+template int gemm_exact_dev<double>(bool, int, int, int, const double*, int, const double*, int, double*, int,
+                                    cudaStream_t);
+template int gemm_exact_dev<float>(bool, int, int, int, const float*, int, const float*, int, float*, int,
+                                   cudaStream_t);
+
 // ------------------------------------------------------------------ panel
 template <typename T>
 struct PanelCtx {

@@ -77,13 +77,21 @@ GB_HD inline void trsm_lutn_col(int j, int m, const T* A, int lda, T* B, int ldb
   }
 }
 
-// DPOTRF2 (SRC/dpotrf2.f:168-205) of an n x n block on one thread; returns
-// INFO (the order of the first leading minor that is not positive).  The
-// reference recursion (factor A11 of order N/2, DTRSM, DSYRK, factor A22)
-// runs as a loop over an explicit stack of blocks, so the device code needs
-// no call stack for it.
-template <typename T>
-GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
+// DPOTRF2 (SRC/dpotrf2.f:168-205) of an n x n block; returns INFO (the
+// order of the first leading minor that is not positive).  The reference
+// recursion (factor A11 of order N/2, DTRSM, DSYRK, factor A22) runs as a
+// loop over an explicit stack of blocks, so the device code needs no call
+// stack for it.  The nthr threads of a CTA (thread tid) share the work: each
+// DTRSM row (lower) or column (upper) and each DSYRK element is one thread's,
+// computed in the reference order as above, with sync() (a CTA barrier)
+// between the dependent steps; every thread walks the same stack and returns
+// the same INFO.  With tid = 0, nthr = 1 and no barrier it is the reference's
+// sequential order step for step.
+struct NoSync {
+  GB_HD void operator()() const {}
+};
+template <typename T, typename Sync>
+GB_HD inline int potrf2_par(int upper, int n, T* A, int lda, int tid, int nthr, Sync sync) {
   if (n == 0) return 0;
   struct Blk { int off, n, phase; };
   Blk st[40];                          // depth <= log2(n) + 1
@@ -94,8 +102,10 @@ GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
     T* a11 = A + b.off + (size_t)b.off * lda;
     if (b.n == 1) {
       const T a = a11[0];
+      sync();                          // every thread has read A(off, off)
       if (a <= T(0) || a != a) return b.off + 1;
-      a11[0] = rn_sqrt(a);
+      if (tid == 0) a11[0] = rn_sqrt(a);
+      sync();
       --top;
       continue;
     }
@@ -107,14 +117,21 @@ GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
       T* a12 = upper ? a11 + (size_t)n1 * lda : a11 + n1;   // A(1, N1+1) or A(N1+1, 1) of the block
       T* a22 = a11 + n1 + (size_t)n1 * lda;
       if (upper) {
-        for (int j = 0; j < n2; ++j) trsm_lutn_col(j, n1, a11, lda, a12, lda);
-        for (int j = 0; j < n2; ++j)
-          for (int i = 0; i <= j; ++i) syrk_elem(1, i, j, n1, T(-1), a12, lda, a22, lda);
+        for (int j = tid; j < n2; j += nthr) trsm_lutn_col(j, n1, a11, lda, a12, lda);
+        sync();
+        for (int e = tid; e < n2 * n2; e += nthr) {
+          const int j = e / n2, i = e - j * n2;
+          if (i <= j) syrk_elem(1, i, j, n1, T(-1), a12, lda, a22, lda);
+        }
       } else {
-        for (int i = 0; i < n2; ++i) trsm_rltn_row(i, n1, a11, lda, a12, lda);
-        for (int j = 0; j < n2; ++j)
-          for (int i = j; i < n2; ++i) syrk_elem(0, i, j, n1, T(-1), a12, lda, a22, lda);
+        for (int i = tid; i < n2; i += nthr) trsm_rltn_row(i, n1, a11, lda, a12, lda);
+        sync();
+        for (int e = tid; e < n2 * n2; e += nthr) {
+          const int j = e / n2, i = e - j * n2;
+          if (i >= j) syrk_elem(0, i, j, n1, T(-1), a12, lda, a22, lda);
+        }
       }
+      sync();
       b.phase = 2;
       st[top++] = Blk{b.off + n1, n2, 0};
     } else {
@@ -122,6 +139,12 @@ GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
     }
   }
   return 0;
+}
+
+// DPOTRF2 on one thread: the reference's sequential order.
+template <typename T>
+GB_HD inline int potrf2_seq(int upper, int n, T* A, int lda) {
+  return potrf2_par(upper, n, A, lda, 0, 1, NoSync{});
 }
 
 // Row sum i of DLANSY('I') (SRC/dlansy.f:159-186) in the order the reference

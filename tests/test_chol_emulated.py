@@ -2,9 +2,11 @@
 lapack_gb300/csrc/chol.cu) run on the CPU.
 
 Its kernels are one-dimensional launches whose threads touch disjoint data
-(one thread per element of a DSYRK or DGEMM update, per row or column of a
-DTRSM, one thread for each diagonal block's DPOTRF2), so running blocks and
-threads one after another computes what the GPU computes.  The test takes
+(one thread per element of a DSYRK update or of an operand transpose, per
+row or column of a DTRSM, one thread for each diagonal block's DPOTRF2), so
+running blocks and threads one after another computes what the GPU
+computes; the DGEMM update, on the tiled update kernel, is a stand-in in the
+same order.  The test takes
 chol.cu up to the factorization (the solves use the library's blocked
 triangular-solve kernels, which cooperate through shared memory and are not
 run here), rewrites its launches into a sequential launcher over a stand-in
@@ -40,13 +42,62 @@ int emu_spotrf(int upper, int n, float* a, int lda, int nb) {
 """
 
 
+# The DGEMM and DSYRK updates of chol.cu run on the library's tiled update
+# kernel (it cooperates through shared memory and is not run here; the GB300
+# tests check its bits against the oracle); these stand-ins compute them in
+# the same per-element orders with separately rounded products (DSYRK's zero
+# skip and triangle included), so what is checked
+# here is chol.cu's own part: the operand transposes, offsets and the
+# sequence of steps.
+GEMM_STANDIN = r"""
+namespace gb {
+template <typename T>
+int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+                   cudaStream_t) {
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < M; ++i) {
+      T* c = C + i + (size_t)j * ldc;
+      if (!sum_first) {
+        T acc = *c;
+        for (int l = 0; l < K; ++l) acc = acc - A[i + (size_t)l * lda] * B[l + (size_t)j * ldb];
+        *c = acc;
+      } else {
+        T t = 0;
+        for (int l = 0; l < K; ++l) t = t + A[i + (size_t)l * lda] * B[l + (size_t)j * ldb];
+        *c = *c - t;
+      }
+    }
+  return 0;
+}
+template <typename T>
+int syrk_exact_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t) {
+  for (int j = 0; j < n; ++j)
+    for (int i = upper ? 0 : j; i < (upper ? j + 1 : n); ++i) {
+      T* c = C + i + (size_t)j * ldc;
+      if (!upper) {
+        T acc = *c;
+        for (int l = 0; l < K; ++l)
+          if (B[l + (size_t)j * ldb] != T(0)) acc = acc - A[i + (size_t)l * lda] * B[l + (size_t)j * ldb];
+        *c = acc;
+      } else {
+        T t = 0;
+        for (int l = 0; l < K; ++l) t = t + A[i + (size_t)l * lda] * B[l + (size_t)j * ldb];
+        *c = *c - t;
+      }
+    }
+  return 0;
+}
+}  // namespace gb
+"""
+
+
 @pytest.fixture(scope="module")
 def emu(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("needs g++")
     src = open(os.path.join(CSRC, "chol.cu")).read()
     cut = src.index("template <typename T>\nint potrs_dev(")
-    src = src[:cut] + "}  // namespace gb\n"
+    src = GEMM_STANDIN + src[:cut] + "}  // namespace gb\n"
     src = cuda_emu.translate(src, drop_includes=("driver.h", "prof.h", "solve_kernels.cuh"), min_launches=5)
     so = cuda_emu.build(str(tmp_path_factory.mktemp("cholemu")), "cholemu", src + ENTRY, [CSRC])
     L = ctypes.CDLL(so)
@@ -178,7 +229,7 @@ def emu_sposv(tmp_path_factory):
     if shutil.which("g++") is None:
         pytest.skip("needs g++")
     src = open(os.path.join(CSRC, "chol.cu")).read()
-    src = SOLVE_STANDINS + src
+    src = GEMM_STANDIN + SOLVE_STANDINS + src
     src = cuda_emu.translate(src, drop_includes=("driver.h", "prof.h", "solve_kernels.cuh"), min_launches=10)
     oracle.lib()
     so = cuda_emu.build(str(tmp_path_factory.mktemp("sposvemu")), "sposvemu", src + SPOSV_ENTRY, [CSRC])
