@@ -16,7 +16,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host-side arithmetic then rounds the same on x86-64 and on AArch64
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=default",
           "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
-SOURCES = ["getrf.cu", "trsm.cu", "panel_node.cu", "panel_node_f64.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "refine.cu", "chol.cu", "zlu.cu", "lapacke.cpp"]
+SOURCES = ["getrf.cu", "trsm.cu", "panel_node.cu", "panel_node_f64.cu", "mixed.cu", "gemm_tc.cu", "capi.cu", "prof.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "refine.cu", "chol.cu", "zlu.cu", "zlu_tiles.cu", "lapacke.cpp"]
 
 
 def _sources():

@@ -5,16 +5,15 @@
 //
 // The schedules (block loop, panel recursion, solve sequence, refinement
 // loop) are the host-side templates of zlu_seq.h; here each of their steps
-// is one kernel launch on the caller's stream: ZLASWP and ZTRSM with one
-// thread per column, the ZGEMM update and the conversions with one thread
-// per element, ZLANGE with one thread per row, the pivot step of a panel
-// column and ZLANGE's maximum on one thread, the convergence test with one
-// thread per right-hand side.  Every thread runs the shared per-thread
-// function in the reference loop order with separately rounded operations,
-// so the results equal the reference's bit for bit (the CPU tests run the
-// same schedules and functions against the oracle).  This is the
-// correctness-first form of the complex path: no tiling and no tensor cores
-// yet.
+// is one kernel launch on the caller's stream: the ZGEMM update on shared-
+// memory tiles and the pivot step of a panel column on one CTA (both in
+// zlu_tiles.cu), ZLASWP and ZTRSM with one thread per column, the
+// conversions with one thread per element, ZLANGE with one thread per row
+// and its maximum on one thread, the convergence test with one thread per
+// right-hand side.  Every element is computed in the reference loop order
+// with separately rounded operations, so the results equal the reference's
+// bit for bit (the CPU tests run the same schedules and functions against
+// the oracle).  No tensor cores: the complex FMA units carry the update.
 #include "common.cuh"
 #include "driver.h"
 #include "zlu_seq.h"
@@ -23,15 +22,21 @@
 
 namespace gb {
 
+// zlu_tiles.cu: the tiled ZGEMM update (C -= A*B) and the pivot step of one
+// panel column (a zero pivot records INFO = gcol by atomicMin).
+template <typename R>
+int zgemm_tile_dev(int m, int n, int k, const cpx<R>* A, int lda, const cpx<R>* B, int ldb, cpx<R>* C, int ldc,
+                   cudaStream_t s);
+template <typename R>
+int zcol_cta_dev(int m, cpx<R>* a, int* ipiv, int gcol, int* info, cudaStream_t s);
+// One CTA per column of a ZTRSM; false (nothing launched) for 'T'/'C' lower.
+template <typename R>
+bool ztrsm_cta_dev(int upper, int trans, int unit, int m, int ncols, const cpx<R>* A, int lda, cpx<R>* B, int ldb,
+                   cudaStream_t s, int* rc);
+
 namespace {
 
 unsigned zblocks(size_t n, int per = 128) { return (unsigned)((n + per - 1) / per); }
-
-template <typename R>
-__global__ void __launch_bounds__(1) zcol_kernel(int m, cpx<R>* __restrict__ a, int* __restrict__ ipiv, int gcol,
-                                                 int* __restrict__ info) {
-  if (zgetrf2_col(m, a, ipiv)) atomicMin(info, gcol);
-}
 
 template <typename R>
 __global__ void zlaswp_kernel(int ncols, cpx<R>* __restrict__ A, int lda, int k1, int k2, const int* __restrict__ ipiv,
@@ -45,15 +50,6 @@ __global__ void ztrsm_kernel(int upper, int trans, int unit, int m, int ncols, c
                              cpx<R>* __restrict__ B, int ldb) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < ncols) ztrsm_left_col(upper, trans, unit, m, A, lda, B + (size_t)j * ldb);
-}
-
-template <typename R>
-__global__ void zgemm_kernel(int m, int n, int k, const cpx<R>* __restrict__ A, int lda, const cpx<R>* __restrict__ B,
-                             int ldb, cpx<R>* __restrict__ C, int ldc) {
-  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (size_t)m * n) return;
-  const int j = (int)(e / m), i = (int)(e - (size_t)j * m);
-  zgemm_nn_elem(i, j, k, A, lda, B, ldb, C, ldc);
 }
 
 __global__ void zipiv_add_kernel(int* __restrict__ ipiv, int cnt, int off) {
@@ -119,26 +115,28 @@ struct GpuZOps {
   }
   template <typename R>
   int col(int m, cpx<R>* a, int* ipiv, int gcol) {
-    GB_LAUNCH(zcol_kernel<R><<<1, 1, 0, s>>>(m, a, ipiv, gcol, w.info));
-    return (int)cudaGetLastError();
+    return zcol_cta_dev<R>(m, a, ipiv, gcol, w.info, s);
   }
   template <typename R>
   int laswp(int ncols, cpx<R>* A, int lda, int k1, int k2, const int* ipiv, int incx) {
     if (ncols <= 0 || k2 < k1) return 0;
-    GB_LAUNCH(zlaswp_kernel<R><<<zblocks(ncols), 128, 0, s>>>(ncols, A, lda, k1, k2, ipiv, incx));
+    GB_LAUNCH(zlaswp_kernel<R><<<zblocks(ncols, 64), 64, 0, s>>>(ncols, A, lda, k1, k2, ipiv, incx));
     return (int)cudaGetLastError();
   }
   template <typename R>
   int trsm(int upper, int trans, int unit, int m, int ncols, const cpx<R>* A, int lda, cpx<R>* B, int ldb) {
     if (m <= 0 || ncols <= 0) return 0;
-    GB_LAUNCH(ztrsm_kernel<R><<<zblocks(ncols), 128, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
+    // long columns (ZGETRS): a CTA per column; the panel's and the block
+    // row's short ones (m <= NB): a thread per column
+    int rc = 0;
+    if (m > 128 && ztrsm_cta_dev<R>(upper, trans, unit, m, ncols, A, lda, B, ldb, s, &rc)) return rc;
+    GB_LAUNCH(ztrsm_kernel<R><<<zblocks(ncols, 64), 64, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
     return (int)cudaGetLastError();
   }
   template <typename R>
   int gemm(int m, int n, int k, const cpx<R>* A, int lda, const cpx<R>* B, int ldb, cpx<R>* C, int ldc) {
     if (m <= 0 || n <= 0 || k <= 0) return 0;   // ZGEMM's quick return (BETA = ONE)
-    GB_LAUNCH(zgemm_kernel<R><<<zblocks((size_t)m * n, 256), 256, 0, s>>>(m, n, k, A, lda, B, ldb, C, ldc));
-    return (int)cudaGetLastError();
+    return zgemm_tile_dev<R>(m, n, k, A, lda, B, ldb, C, ldc, s);
   }
   int ipiv_add(int* ipiv, int cnt, int off) {
     if (cnt <= 0) return 0;

@@ -113,6 +113,89 @@ GB_HD inline int izamax_seq(int n, const cpx<R>* x) {
   return best;
 }
 
+// IZAMAX split over nt threads (thread t scans i = t, t + nt, ... in
+// increasing order) and combined in any order: what izamax_seq returns,
+// restated as independent reductions.  izamax_seq returns the first NaN if
+// there is one (an infinite part only starts a search for a later NaN);
+// else the first infinite part; else, when some |re| + |im| overflows (the
+// first such index s), the first maximum of the scaled sums over i >= s
+// (every earlier sum is finite and smaller); else the first maximum of the
+// sums.  kNone marks an empty minimum.
+constexpr int kZamaxNone = 0x7fffffff;
+template <typename R>
+struct ZamaxPart {
+  int nan, inf, over;   // first index with a NaN part / an infinite part / an overflowing sum
+  R val;                // the largest finite sum seen, at the first index idx
+  int idx;
+};
+template <typename R>
+GB_HD inline ZamaxPart<R> zamax_part(int n, const cpx<R>* x, int t, int nt) {
+  const R hugeval = CpxLim<R>::huge;
+  ZamaxPart<R> p{kZamaxNone, kZamaxNone, kZamaxNone, R(-1), kZamaxNone};
+  for (int i = t; i < n; i += nt) {
+    const R ar = fabs(x[i].re), ai = fabs(x[i].im);
+    if (x[i].re != x[i].re || x[i].im != x[i].im) {
+      if (p.nan == kZamaxNone) p.nan = i;
+      continue;
+    }
+    if (ar > hugeval || ai > hugeval) {
+      if (p.inf == kZamaxNone) p.inf = i;
+      continue;
+    }
+    const R val = rn_add(ar, ai);
+    if (val > hugeval) {
+      if (p.over == kZamaxNone) p.over = i;
+    } else if (val > p.val) {
+      p.val = val;
+      p.idx = i;
+    }
+  }
+  return p;
+}
+// the larger value wins, the smaller index on a tie
+template <typename R>
+GB_HD inline void zamax_pick(R& val, int& idx, R v2, int i2) {
+  if (v2 > val || (v2 == val && i2 < idx)) {
+    val = v2;
+    idx = i2;
+  }
+}
+template <typename R>
+GB_HD inline ZamaxPart<R> zamax_combine(ZamaxPart<R> a, const ZamaxPart<R>& b) {
+  a.nan = a.nan < b.nan ? a.nan : b.nan;
+  a.inf = a.inf < b.inf ? a.inf : b.inf;
+  a.over = a.over < b.over ? a.over : b.over;
+  zamax_pick(a.val, a.idx, b.val, b.idx);
+  return a;
+}
+// The scaled pass (only when some sum overflowed, from index s): the first
+// maximum of 0.25|re| + 0.25|im| over this thread's i >= s.
+template <typename R>
+GB_HD inline void zamax_scaled_part(int n, const cpx<R>* x, int s, int t, int nt, R* val, int* idx) {
+  const R q = R(0.25);
+  *val = R(-1);
+  *idx = kZamaxNone;
+  int i0 = t;
+  if (i0 < s) i0 += (s - i0 + nt - 1) / nt * nt;
+  for (int i = i0; i < n; i += nt) {
+    const R ar = fabs(x[i].re), ai = fabs(x[i].im);
+    const R v = rn_add(rn_mul(q, ar), rn_mul(q, ai));
+    if (v > *val) {
+      *val = v;
+      *idx = i;
+    }
+  }
+}
+// 1-based result from the combined first pass (n >= 2); the scaled pass is
+// consulted only when p.nan and p.inf are empty and p.over is not.
+template <typename R>
+GB_HD inline int zamax_result(const ZamaxPart<R>& p, int scaled_idx) {
+  if (p.nan != kZamaxNone) return p.nan + 1;
+  if (p.inf != kZamaxNone) return p.inf + 1;
+  if (p.over != kZamaxNone) return scaled_idx + 1;
+  return p.idx + 1;
+}
+
 // The one-column step of ZGETRF2 (SRC/zgetrf2.f:176-211): the M = 1 branch
 // (IPIV = 1, a zero flagged) or the N = 1 branch (pivot search, swap, and
 // the column scaled by the reciprocal of the pivot when |pivot| >= SFMIN,

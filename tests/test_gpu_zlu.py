@@ -80,6 +80,27 @@ def test_zgetrs_bitwise(gpu, trans, n, nrhs):
     assert _same_bits(x_g, x_r)
 
 
+@pytest.mark.parametrize("trans", "NTC")
+@pytest.mark.parametrize("n,nrhs,dtype", [(3000, 2, np.complex128), (6200, 1, np.complex128),
+                                          (12300, 1, np.complex64)])
+def test_zgetrs_long_columns_bitwise(gpu, trans, n, nrhs, dtype):
+    """Long columns take the one-CTA-per-column solve ('N' both triangles,
+    'T'/'C' upper; the column in shared memory up to 96 KB -- 6144
+    COMPLEX*16 or 12288 COMPLEX elements -- else in place): X bitwise the
+    oracle's.  The factors are a synthetic diagonally dominant LU with valid
+    pivots (ZGETRS reads nothing else), so no large factorization runs."""
+    rng = np.random.default_rng(n)
+    lu = (rng.uniform(-1, 1, (n, n)) + 1j * rng.uniform(-1, 1, (n, n))) / n
+    lu[np.diag_indices(n)] += 2.0 + 0.5j
+    lu = lu.astype(dtype)
+    ip = (np.arange(n) + 1 + rng.integers(0, 4, n)).clip(max=n).astype(np.int32)
+    b = oracle.random_zmatrix(n, nrhs, 7 + n).astype(dtype)
+    x_r, _ = oracle.zgetrs(lu, ip, b, trans)
+    x_g, info = gpu.zgetrs(lu, ip, b, trans)
+    assert info == 0
+    assert _same_bits(x_g, x_r)
+
+
 @pytest.mark.parametrize("imat", range(1, 12))
 def test_zgesv_zchkge_ratios(gpu, imat):
     """ZCHKGE tests 1 and 3 on the GPU: INFO = IZERO for the zero-column

@@ -98,6 +98,31 @@ template <typename R> void getrs_t(int trans, int n, int nrhs, const R *a, int l
   gb::zgetrs_sched(ops, trans, n, nrhs, reinterpret_cast<const cpx<R> *>(a), lda, ipiv, reinterpret_cast<cpx<R> *>(b),
                    ldb);
 }
+template <typename R> int izamax_split_t(int n, const R *xr, int nt) {
+  // the pivot kernel's IZAMAX: nt thread parts, combined pairwise as its
+  // shared-memory tree does (nt a power of two) or in a row
+  const cpx<R> *x = reinterpret_cast<const cpx<R> *>(xr);
+  std::vector<gb::ZamaxPart<R>> part(nt);
+  for (int t = 0; t < nt; ++t) part[t] = gb::zamax_part(n, x, t, nt);
+  const bool pow2 = (nt & (nt - 1)) == 0;
+  if (pow2)
+    for (int h = nt / 2; h > 0; h >>= 1)
+      for (int t = 0; t < h; ++t) part[t] = gb::zamax_combine(part[t], part[t + h]);
+  else
+    for (int t = 1; t < nt; ++t) part[0] = gb::zamax_combine(part[0], part[t]);
+  const gb::ZamaxPart<R> all = part[0];
+  int sidx = gb::kZamaxNone;
+  if (all.nan == gb::kZamaxNone && all.inf == gb::kZamaxNone && all.over != gb::kZamaxNone) {
+    R best = R(-1);
+    for (int t = nt - 1; t >= 0; --t) {
+      R v;
+      int i;
+      gb::zamax_scaled_part(n, x, all.over, t, nt, &v, &i);
+      gb::zamax_pick(best, sidx, v, i);
+    }
+  }
+  return gb::zamax_result(all, sidx);
+}
 extern "C" {
 int seq_zgetrf(int m, int n, double *a, int lda, int *ipiv, int nb) { return getrf_t(m, n, a, lda, ipiv, nb); }
 int seq_cgetrf(int m, int n, float *a, int lda, int *ipiv, int nb) { return getrf_t(m, n, a, lda, ipiv, nb); }
@@ -109,6 +134,8 @@ void seq_cgetrs(int trans, int n, int nrhs, const float *a, int lda, const int *
 }
 int seq_izamax(int n, const double *x) { return gb::izamax_seq(n, reinterpret_cast<const zdc *>(x)); }
 int seq_icamax(int n, const float *x) { return gb::izamax_seq(n, reinterpret_cast<const cfc *>(x)); }
+int seq_izamax_split(int n, const double *x, int nt) { return izamax_split_t(n, x, nt); }
+int seq_icamax_split(int n, const float *x, int nt) { return izamax_split_t(n, x, nt); }
 int seq_zcgesv(int n, int nrhs, double *a, int lda, int *ipiv, const double *b, int ldb, double *x, int ldx,
                int *iter) {
   CpuOps ops;
@@ -140,6 +167,8 @@ def seq(tmp_path_factory):
     L.seq_zgetrs.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int]
     L.seq_izamax.argtypes = [ctypes.c_int, p]
     L.seq_icamax.argtypes = [ctypes.c_int, p]
+    L.seq_izamax_split.argtypes = [ctypes.c_int, p, ctypes.c_int]
+    L.seq_icamax_split.argtypes = [ctypes.c_int, p, ctypes.c_int]
     L.seq_cgetrf.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, ctypes.c_int]
     L.seq_cgetrs.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int]
     L.seq_zcgesv.argtypes = [ctypes.c_int, ctypes.c_int, p, ctypes.c_int, p, p, ctypes.c_int, p, ctypes.c_int, p]
@@ -249,6 +278,50 @@ def test_izamax_seq_matches_oracle(seq):
     for x in cases:
         x = np.ascontiguousarray(x, dtype=np.complex128)
         assert seq.seq_izamax(x.size, _ptr(x)) == oracle.izamax(x)
+
+
+def _izamax_cases(rng, big):
+    cases = []
+    for n in (2, 3, 5, 17, 64, 255, 256, 257, 1000):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        cases.append(x)
+        t = x.copy()
+        t[rng.integers(0, n, 3)] = 4 + 4j                    # ties of the maximum
+        cases.append(t)
+        t = np.round(x)                                     # many exact ties, zeros
+        cases.append(t)
+        for bad in (complex(np.nan, 0), complex(0, np.inf), complex(-np.inf, np.nan)):
+            t = x.copy()
+            t[rng.integers(0, n)] = bad
+            cases.append(t)
+        t = x.copy()
+        t[rng.integers(0, n, 2)] = complex(np.inf, 0)
+        t[rng.integers(0, n)] = complex(np.nan, 1)           # a NaN before or after the infinities
+        cases.append(t)
+        t = x * (big / 8)                                   # large finite sums, then some that overflow
+        t[rng.integers(0, n, 3)] = complex(0.75 * big, 0.75 * big)
+        t[rng.integers(0, n)] = complex(0.8 * big, 0.7 * big)
+        cases.append(t)
+        t = np.full(n, complex(0.75 * big, 0.75 * big))    # all overflowing and tied
+        cases.append(t)
+        cases.append(np.zeros(n, dtype=complex))
+    return cases
+
+
+@pytest.mark.parametrize("nt", [1, 2, 3, 7, 32, 256])
+def test_izamax_split_equals_sequential(seq, nt):
+    """The pivot kernel's IZAMAX, split over nt threads (first NaN, first
+    infinity, first overflowing sum and the largest finite sum per thread,
+    then the scaled pass), returns izamax_seq's index on ties, NaNs,
+    infinities and overflowing sums, in both precisions."""
+    rng = np.random.default_rng(nt)
+    for x in _izamax_cases(rng, 1.7976931348623157e308):
+        x = np.ascontiguousarray(x, dtype=np.complex128)
+        assert seq.seq_izamax_split(x.size, _ptr(x), nt) == seq.seq_izamax(x.size, _ptr(x)), x
+    for x in _izamax_cases(rng, 3.4028234663852886e38):
+        with np.errstate(over="ignore", invalid="ignore"):
+            x = np.ascontiguousarray(x, dtype=np.complex64)
+        assert seq.seq_icamax_split(x.size, _ptr(x), nt) == seq.seq_icamax(x.size, _ptr(x)), x
 
 
 @pytest.mark.parametrize("nb", [1, 20, 64])
