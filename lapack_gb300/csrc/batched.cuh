@@ -281,23 +281,33 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     __syncthreads();
     const int np = min(npairs_s, 2 * kBatMaxNb);
     if (np > 0) {
-      // one warp per column, the lanes over the moved rows (np <= 128)
+      // a warp moves kG columns at a time, the lanes over the moved rows
+      // (np <= 128): all kG columns' sources are loaded before any of their
+      // destinations is written, so the loads of a round are in flight together
       const int warp = tid >> 5, lane = tid & 31;
-      constexpr int kPer = 2 * kBatMaxNb / 32;
-      for (int c = warp; c < n; c += kBatThreads / 32) {
-        if (c >= j && c < j + jb) continue;
-        T* Ac = A + (size_t)c * lda;
-        T v[kPer];
+      constexpr int kPer = 2 * kBatMaxNb / 32, kG = sizeof(T) == 4 ? 4 : 2, kW = kBatThreads / 32;
+      for (int c0 = warp * kG; c0 < n; c0 += kW * kG) {
+        T v[kG][kPer];
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-          const int i = lane + 32 * q;
-          if (i < np) v[q] = Ac[ps[i]];
+        for (int g = 0; g < kG; ++g) {
+          const int c = c0 + g;
+          const bool live = c < n && (c < j || c >= j + jb);
+#pragma unroll
+          for (int q = 0; q < kPer; ++q) {
+            const int i = lane + 32 * q;
+            if (live && i < np) v[g][q] = A[(size_t)c * lda + ps[i]];
+          }
         }
         __syncwarp();
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-          const int i = lane + 32 * q;
-          if (i < np) Ac[pd[i]] = v[q];
+        for (int g = 0; g < kG; ++g) {
+          const int c = c0 + g;
+          const bool live = c < n && (c < j || c >= j + jb);
+#pragma unroll
+          for (int q = 0; q < kPer; ++q) {
+            const int i = lane + 32 * q;
+            if (live && i < np) A[(size_t)c * lda + pd[i]] = v[g][q];
+          }
         }
       }
     }
@@ -379,8 +389,8 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
           }
       }
       __syncthreads();
+      clk.mark(kBatPhUpdate);
     }
-    clk.mark(kBatPhUpdate);
   }
   if (tid == 0) *info = first_zero;
   __syncthreads();
@@ -392,6 +402,23 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
 // panel buffer so the sequential steps read shared memory, not L2.  The
 // per-element order is the reference one (BLAS/SRC/dtrsm.f:278-300).
 constexpr int kBatSolveChunk = 32;
+
+// x[r] -= xk * l[r] for the rows r = r0, r0 + 32, ... below rend (one lane's
+// share of a column step): the loads of four rows are issued before their
+// updates, one update per element as in the loop form.
+template <bool EXACT, typename T>
+__device__ __forceinline__ void axpy_rows(T xk, const T* __restrict__ l, T* __restrict__ x, int r0, int rend) {
+  int r = r0;
+  for (; r + 96 < rend; r += 128) {
+    const T l0 = l[r], l1 = l[r + 32], l2 = l[r + 64], l3 = l[r + 96];
+    const T x0 = x[r], x1 = x[r + 32], x2 = x[r + 64], x3 = x[r + 96];
+    x[r] = fnmadd<EXACT>(xk, l0, x0);
+    x[r + 32] = fnmadd<EXACT>(xk, l1, x1);
+    x[r + 64] = fnmadd<EXACT>(xk, l2, x2);
+    x[r + 96] = fnmadd<EXACT>(xk, l3, x3);
+  }
+  for (; r < rend; r += 32) x[r] = fnmadd<EXACT>(xk, l[r], x[r]);
+}
 
 template <typename T, bool EXACT>
 __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int lda, const int* __restrict__ ipiv,
@@ -421,10 +448,10 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
         [&](int r, int c, T v) { Lc[c * rows + r] = v; });
     __syncthreads();
     if (warp < nrhs) {
-      T* x = Bs + warp * kBatMaxN;
+      T* __restrict__ x = Bs + warp * kBatMaxN + k0;
       for (int c = 0; c < kw; ++c) {
-        const T xk = x[k0 + c];
-        for (int r = c + 1 + lane; r < rows; r += 32) x[k0 + r] = fnmadd<EXACT>(xk, Lc[c * rows + r], x[k0 + r]);
+        const T xk = x[c];
+        axpy_rows<EXACT>(xk, Lc + c * rows, x, c + 1 + lane, rows);
         __syncwarp();
       }
     }
@@ -438,13 +465,13 @@ __device__ void batched_getrs_one(int n, int nrhs, const T* __restrict__ A, int 
         [&](int r, int c, T v) { Lc[c * rows + r] = v; });
     __syncthreads();
     if (warp < nrhs) {
-      T* x = Bs + warp * kBatMaxN;
+      T* __restrict__ x = Bs + warp * kBatMaxN;
       for (int c = kw - 1; c >= 0; --c) {
         const int k = k0 + c;
-        if (lane == 0) x[k] = x[k] / Lc[c * rows + k];
+        const T xk = x[k] / Lc[c * rows + k];    // every lane divides the same operands
         __syncwarp();
-        const T xk = x[k];
-        for (int r = lane; r < k; r += 32) x[r] = fnmadd<EXACT>(xk, Lc[c * rows + r], x[r]);
+        if (lane == 0) x[k] = xk;
+        axpy_rows<EXACT>(xk, Lc + c * rows, x, lane, k);
         __syncwarp();
       }
     }
