@@ -48,10 +48,10 @@ static_assert(bat_uchunk_cols<float>() + 8 <= kBatUStride && bat_uchunk_cols<dou
 static_assert(bat_threads<float>() >= kBatMaxNb && bat_threads<double>() >= kBatMaxNb,
               "the pivot-row step takes one thread per panel column");
 
-// panel [cap][512] + U12 chunk [cap][kBatUStride] + B [4][512] + labels and pairs
+// panel [cap][512] + two U12 chunks [cap][kBatUStride] + B [4][512] + labels and pairs
 template <typename T>
 constexpr size_t batched_smem_bytes(int cap) {
-  return sizeof(T) * ((size_t)cap * kBatMaxN + (size_t)cap * kBatUStride + (size_t)kBatMaxN * kBatMaxRhs) +
+  return sizeof(T) * ((size_t)cap * kBatMaxN + 2 * (size_t)cap * kBatUStride + (size_t)kBatMaxN * kBatMaxRhs) +
          sizeof(int) * (4 * kBatMaxNb + kBatMaxN) + 64;
 }
 template <typename T>
@@ -138,7 +138,7 @@ __device__ __forceinline__ T* bat_uchunk(unsigned char* smem, int cap) {
 }
 template <typename T>
 __device__ __forceinline__ T* bat_rhs(unsigned char* smem, int cap) {
-  return bat_uchunk<T>(smem, cap) + (size_t)cap * kBatUStride;
+  return bat_uchunk<T>(smem, cap) + 2 * (size_t)cap * kBatUStride;
 }
 template <typename T>
 __device__ __forceinline__ int* bat_labels(unsigned char* smem, int cap) {
@@ -151,7 +151,7 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
   constexpr int kBatThreads = bat_threads<T>();
   const int tid = threadIdx.x;
   T* P = bat_panel<T>(smem);                                // panel [nb][M]
-  T* U = bat_uchunk<T>(smem, cap);                          // U12 chunk [nb][kBatUStride]
+  T* const Ubuf = bat_uchunk<T>(smem, cap);                 // two U12 chunks [nb][kBatUStride]
   int* lab = bat_labels<T>(smem, cap);                      // [kBatMaxN]
   int* pd = lab + kBatMaxN;                                 // pair dst [2nb]
   int* ps = pd + 2 * kBatMaxNb;                             // pair src [2nb]
@@ -322,12 +322,24 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
     //    8w..8w+7, the four lane groups of eight the rows of one residue mod
     //    4, one step per column kk of L11 (every element gets its updates in
     //    increasing kk, the order of BLAS/SRC/dtrsm.f:290-300).
+    //    The chunks alternate between two buffers: the next chunk's A12
+    //    (final once the interchanges are done; the current chunk's update
+    //    writes only rows below the block row) is loaded with cp.async while
+    //    the current chunk is written back and updated.
     constexpr int kUChunk = bat_uchunk_cols<T>();
-    for (int cb = 0; cb < ncol; cb += kUChunk) {
+    auto prefetch = [&](int cb, T* dst) {
       const int cw = min(kUChunk, ncol - cb);
-      colwise_copy<kBatThreads, T>(
-          jb, cw, tid, [&](int r, int c) { return A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda]; },
-          [&](int r, int c, T v) { U[r * kBatUStride + c] = v; });
+      for (int e = tid; e < jb * cw; e += kBatThreads) {
+        const int c = e / jb, r = e - c * jb;
+        cp_async_elem_zfill(dst + r * kBatUStride + c, A + (size_t)(j + r) + (size_t)(j + jb + cb + c) * lda, true);
+      }
+      cp_async_commit();
+    };
+    prefetch(0, Ubuf);
+    for (int cb = 0, it = 0; cb < ncol; cb += kUChunk, ++it) {
+      const int cw = min(kUChunk, ncol - cb);
+      T* U = Ubuf + (size_t)(it & 1) * cap * kBatUStride;
+      cp_async_wait<0>();
       __syncthreads();
       {
         const int lane = tid & 31, c = 8 * (tid >> 5) + (lane & 7), q = lane >> 3;
@@ -343,6 +355,7 @@ __device__ void batched_getrf_one(int n, T* __restrict__ A, int lda, int* __rest
         }
       }
       __syncthreads();
+      if (cb + kUChunk < ncol) prefetch(cb + kUChunk, Ubuf + (size_t)((it + 1) & 1) * cap * kBatUStride);
       colwise_copy<kBatThreads, T>(
           jb, cw, tid, [&](int r, int c) { return U[r * kBatUStride + c]; },
           [&](int r, int c, T v) { A[(size_t)(j + r) + (size_t)(j + jb + cb + c) * lda] = v; });
