@@ -7,9 +7,10 @@
 // left, DPOTRF2 of the diagonal block, then the DGEMM and DTRSM of the
 // block below (lower) or to the right (upper).  The DGEMM -- the O(n^3)
 // part -- and the DSYRK of the diagonal block run on the tiled update kernel
-// in the reference's per-element orders with separately rounded products
-// (the DSYRK stores one triangle and, in the lower form, skips the terms
-// whose A(J,L) is zero, as BLAS/SRC/dsyrk.f:313-320 does).  The DTRSM and the
+// in the reference's per-element orders, with separately rounded products
+// in exact mode and fused multiply-adds otherwise (the DSYRK stores one
+// triangle and, in the lower form, skips the terms whose A(J,L) is zero, as
+// BLAS/SRC/dsyrk.f:313-320 does).  The DTRSM and the
 // diagonal blocks' DPOTRF2 (at most NB = 64 columns, on one thread over
 // shared memory) are kernels whose threads each compute one row or column
 // through the shared host/device functions of potrf_seq.h (checked against
@@ -78,15 +79,82 @@ __global__ void transpose_kernel(int rows, int cols, const T* __restrict__ src, 
   dst[(size_t)c + (size_t)r * ldd] = src[(size_t)r + (size_t)c * lds];
 }
 
+// The DTRSM of the block below (lower: one thread per row of B) or to the
+// right (upper: one thread per column).  On the GPU each thread's row or
+// column of B (and, in FP32, the diagonal block, n <= 64) is staged in shared memory
+// (stride 65: a warp's 32 rows or columns fall in different banks) and the
+// solve runs over restrict-qualified copies, so the loads of a step can be
+// issued ahead of its updates; the operations and their order are those of
+// trsm_rltn_row / trsm_lutn_col.  64 threads per CTA.
+constexpr int kCholTrsmThreads = 64;
+constexpr int kCholTrsmLd = 65;
+// the diagonal block is staged too in FP32 (2 x 16.6 KB); in FP64 only B
+// (33 KB), the diagonal block read through the L1 cache
 template <typename T>
-__global__ void trsm_rltn_kernel(int rows, int n, const T* __restrict__ A, int lda, T* __restrict__ B, int ldb) {
+constexpr bool kStageA = sizeof(T) == 4;
+template <typename T>
+__global__ void __launch_bounds__(kCholTrsmThreads) trsm_rltn_kernel(int rows, int n, const T* __restrict__ A,
+                                                                     int lda, T* __restrict__ B, int ldb) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+#ifdef __CUDA_ARCH__
+  if (n <= 64) {
+    __shared__ T As[kStageA<T> ? kCholTrsmLd * 64 : 1];   // As[j + k * 65] = A(j, k)
+    __shared__ T Bs[kCholTrsmLd * 64];                    // Bs[t + k * 65] = B(i, k)
+    if constexpr (kStageA<T>) {
+      for (int e = threadIdx.x; e < n * n; e += kCholTrsmThreads) {
+        const int k = e / n, j = e - k * n;
+        As[j + k * kCholTrsmLd] = A[(size_t)j + (size_t)k * lda];
+      }
+      __syncthreads();
+    }
+    if (i >= rows) return;
+    T* __restrict__ b = Bs + threadIdx.x;
+    const T* __restrict__ a = kStageA<T> ? As : A;
+    const int la = kStageA<T> ? kCholTrsmLd : lda;
+    for (int k = 0; k < n; ++k) b[k * kCholTrsmLd] = B[(size_t)i + (size_t)k * ldb];
+    for (int k = 0; k < n; ++k) {                         // BLAS/SRC/dtrsm.f:389-403
+      const T bk = rn_div(b[k * kCholTrsmLd], a[k + (size_t)k * la]);
+      b[k * kCholTrsmLd] = bk;
+#pragma unroll 4
+      for (int j = k + 1; j < n; ++j)
+        b[j * kCholTrsmLd] = rn_sub(b[j * kCholTrsmLd], rn_mul(a[j + (size_t)k * la], bk));
+    }
+    for (int k = 0; k < n; ++k) B[(size_t)i + (size_t)k * ldb] = b[k * kCholTrsmLd];
+    return;
+  }
+#endif
   if (i < rows) trsm_rltn_row(i, n, A, lda, B, ldb);
 }
 
 template <typename T>
-__global__ void trsm_lutn_kernel(int cols, int m, const T* __restrict__ A, int lda, T* __restrict__ B, int ldb) {
+__global__ void __launch_bounds__(kCholTrsmThreads) trsm_lutn_kernel(int cols, int m, const T* __restrict__ A,
+                                                                     int lda, T* __restrict__ B, int ldb) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+#ifdef __CUDA_ARCH__
+  if (m <= 64) {
+    __shared__ T As[kStageA<T> ? kCholTrsmLd * 64 : 1];   // As[k + i * 65] = A(k, i)
+    __shared__ T Bs[kCholTrsmLd * 64];                    // Bs[t * 65 + k] = B(k, j)
+    if constexpr (kStageA<T>) {
+      for (int e = threadIdx.x; e < m * m; e += kCholTrsmThreads) {
+        const int c = e / m, r = e - c * m;
+        As[r + c * kCholTrsmLd] = A[(size_t)r + (size_t)c * lda];
+      }
+      __syncthreads();
+    }
+    if (j >= cols) return;
+    T* __restrict__ b = Bs + threadIdx.x * kCholTrsmLd;
+    const T* __restrict__ a = kStageA<T> ? As : A;
+    const int la = kStageA<T> ? kCholTrsmLd : lda;
+    for (int k = 0; k < m; ++k) b[k] = B[(size_t)k + (size_t)j * ldb];
+    for (int i = 0; i < m; ++i) {                         // BLAS/SRC/dtrsm.f:306-316
+      T temp = b[i];
+      for (int k = 0; k < i; ++k) temp = rn_sub(temp, rn_mul(a[k + (size_t)i * la], b[k]));
+      b[i] = rn_div(temp, a[i + (size_t)i * la]);
+    }
+    for (int k = 0; k < m; ++k) B[(size_t)k + (size_t)j * ldb] = b[k];
+    return;
+  }
+#endif
   if (j < cols) trsm_lutn_col(j, m, A, lda, B, ldb);
 }
 
@@ -160,11 +228,11 @@ int potrf_dev(bool upper, int n, T* A, int lda, int nb, int* info, cudaStream_t 
       // and the DGEMM: L: A(j:j+jb, 0:j)^T (j x jb); U: A(0:j, j:j+jb)^T (jb x j)
       if (!upper) {
         GB_LAUNCH(transpose_kernel<T><<<nblocks((size_t)jb * j), 256, 0, s>>>(jb, j, A + j, lda, Tt, j));
-        rc = syrk_exact_dev<T>(false, jb, j, A + j, lda, Tt, j, d, lda, s);
+        rc = syrk_ordered_dev<T>(false, jb, j, A + j, lda, Tt, j, d, lda, s);
       } else {
         GB_LAUNCH(transpose_kernel<T><<<nblocks((size_t)j * jb), 256, 0, s>>>(j, jb, A + (size_t)j * lda, lda, Tt,
                                                                                  jb));
-        rc = syrk_exact_dev<T>(true, jb, j, Tt, jb, A + (size_t)j * lda, lda, d, lda, s);
+        rc = syrk_ordered_dev<T>(true, jb, j, Tt, jb, A + (size_t)j * lda, lda, d, lda, s);
       }
       if (rc) return rc;
     }
@@ -172,6 +240,7 @@ int potrf_dev(bool upper, int n, T* A, int lda, int nb, int* info, cudaStream_t 
     if (rc || *info) return rc;
     const int rest = n - j - jb;
     if (rest <= 0) continue;
+    const unsigned tg = nblocks(rest, kCholTrsmThreads);
     // the DGEMM update on the tiled update kernel, in the reference's
     // per-element order (dgemm.f: 'N','T' products subtracted in turn for L,
     // 'T','N' products summed then subtracted for U), then the DTRSM
@@ -179,18 +248,18 @@ int potrf_dev(bool upper, int n, T* A, int lda, int nb, int* info, cudaStream_t 
       T* c = A + (j + jb) + (size_t)j * lda;
       if (j > 0) {
         // C(rest x jb) -= A(j+jb:n, 0:j) * A(j:j+jb, 0:j)^T
-        rc = gemm_exact_dev<T>(false, rest, jb, j, A + j + jb, lda, Tt, j, c, lda, s);
+        rc = gemm_ordered_dev<T>(false, rest, jb, j, A + j + jb, lda, Tt, j, c, lda, s);
         if (rc) return rc;
       }
-      GB_LAUNCH(trsm_rltn_kernel<T><<<nblocks(rest, 64), 64, 0, s>>>(rest, jb, d, lda, c, lda));
+      GB_LAUNCH(trsm_rltn_kernel<T><<<tg, kCholTrsmThreads, 0, s>>>(rest, jb, d, lda, c, lda));
     } else {
       T* c = A + j + (size_t)(j + jb) * lda;
       if (j > 0) {
         // C(jb x rest) -= A(0:j, j:j+jb)^T * A(0:j, j+jb:n)
-        rc = gemm_exact_dev<T>(true, jb, rest, j, Tt, jb, A + (size_t)(j + jb) * lda, lda, c, lda, s);
+        rc = gemm_ordered_dev<T>(true, jb, rest, j, Tt, jb, A + (size_t)(j + jb) * lda, lda, c, lda, s);
         if (rc) return rc;
       }
-      GB_LAUNCH(trsm_lutn_kernel<T><<<nblocks(rest, 64), 64, 0, s>>>(rest, jb, d, lda, c, lda));
+      GB_LAUNCH(trsm_lutn_kernel<T><<<tg, kCholTrsmThreads, 0, s>>>(rest, jb, d, lda, c, lda));
     }
   }
   return (int)cudaGetLastError();

@@ -163,18 +163,19 @@ struct HostOperands {
   const double* b;
   int ldb;
 };
-// C -= A*B with separately rounded products in the reference DGEMM orders:
-// sum_first false, each product subtracted in turn ('N','T'); true, the
-// products summed and the sum subtracted once ('T','N').  Tiled (the
-// Cholesky factorization's updates).
+// C -= A*B in the reference DGEMM orders: sum_first false, each product
+// subtracted in turn ('N','T'); true, the products summed and the sum
+// subtracted once ('T','N').  Products separately rounded in exact mode,
+// fused otherwise.  Tiled (the Cholesky factorization's updates).
 template <typename T>
-int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+int gemm_ordered_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                    cudaStream_t s);
 // DSYRK of an n x n diagonal block (the other operand given transposed, B =
 // op(A)^T): lower C -= A*B on and below the diagonal with dsyrk.f's zero
-// skip, upper C -= (A*B summed first) on and above it.  Tiled.
+// skip, upper C -= (A*B summed first) on and above it.  Rounding as
+// gemm_ordered_dev.  Tiled.
 template <typename T>
-int syrk_exact_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t s);
+int syrk_ordered_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t s);
 // DSGESV on device memory.  *iter and *info are host outputs.  With host,
 // dA and dB are filled from host->a and host->b first.
 int dsgesv_dev(int n, int nrhs, double* dA, int lda, int* dIpiv, const double* dB, int ldb, double* dX, int ldx,

@@ -176,38 +176,51 @@ int gemm_update_dev<float>(int M, int N, int K, const float* A, int lda, const f
 }
 
 
-// C -= A*B with separately rounded products in the reference DGEMM orders
-// (the Cholesky factorization's updates, SRC/dpotrf.f): sum_first false,
-// each product subtracted from C in increasing k ('N','T' form,
-// BLAS/SRC/dgemm.f:367-383); true, the products summed from zero in
-// increasing k and the sum subtracted once ('T','N' form, dgemm.f:348-360).
-template <typename T, int BM, int BN, int TM, int TN, bool SF, int TRI, bool SKIPZ>
+// C -= A*B in the reference DGEMM orders (the Cholesky factorization's
+// updates, SRC/dpotrf.f): sum_first false, each product subtracted from C in
+// increasing k ('N','T' form, BLAS/SRC/dgemm.f:367-383); true, the products
+// summed from zero in increasing k and the sum subtracted once ('T','N'
+// form, dgemm.f:348-360).  Products separately rounded in exact mode, fused
+// into one FMA otherwise (as the LU's updates).
+// BK: the K depth staged per round.  The thin tiles run one or two CTAs per
+// SM with a K of up to the matrix order, so each element's K chain waits on
+// the next round's global loads unless a round covers many k: deeper rounds
+// for the 16 x 16 and 8 x 8 tiles (within 48 KB of shared memory); 16 for
+// the 128 x 64 and 32 x 32 tiles (deeper measured slower there).
+template <typename T, int BM, int BN, int BK, int TM, int TN, bool SF, int TRI, bool SKIPZ>
 static void launch_update_tile(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                                cudaStream_t s) {
   dim3 grid((M + BM - 1) / BM, (N + BN - 1) / BN);
-  GB_LAUNCH(gemm_nn_update_kernel<T, BM, BN, 16, TM, TN, true, SF, TRI, SKIPZ>
-            <<<grid, (BM / TM) * (BN / TN), 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  if (options().exact)
+    GB_LAUNCH(gemm_nn_update_kernel<T, BM, BN, BK, TM, TN, true, SF, TRI, SKIPZ>
+              <<<grid, (BM / TM) * (BN / TN), 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
+  else
+    GB_LAUNCH(gemm_nn_update_kernel<T, BM, BN, BK, TM, TN, false, SF, TRI, SKIPZ>
+              <<<grid, (BM / TM) * (BN / TN), 0, s>>>(M, N, K, A, lda, B, ldb, C, ldc));
 }
 
-// The tile is the largest of 128 x 64, 32 x 32 and 16 x 16 that still gives
-// every SM a CTA: the Cholesky's updates are thin (N or M = NB = 64) with a
-// long K, so the CTA count, not the per-CTA reuse, limits them.  The
+// The tile is the largest of 128 x 64 (M at least 128: the upper form's
+// M = NB = 64 would leave half of it padding), 32 x 32 and 16 x 16 that
+// still gives every SM a CTA: the Cholesky's updates are thin (N or M = NB =
+// 64) with a long K, so the CTA count, not the per-CTA reuse, limits them
+// (a 64 x 64 tile measured slower than 32 x 32 for these shapes).  The
 // per-element order does not depend on the tile.
 template <typename T, bool SF>
 static void launch_update_by_size(int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                                   cudaStream_t s) {
   const long sms = device_sm_count();
   auto ctas = [&](int bm, int bn) { return (long)((M + bm - 1) / bm) * ((N + bn - 1) / bn); };
-  if (ctas(128, 64) >= sms)
-    launch_update_tile<T, 128, 64, 8, 4, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+  constexpr int bk16 = sizeof(T) == 4 ? 128 : 64;
+  if (M >= 128 && ctas(128, 64) >= sms)
+    launch_update_tile<T, 128, 64, 16, 8, 4, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
   else if (ctas(32, 32) >= sms)
-    launch_update_tile<T, 32, 32, 2, 2, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+    launch_update_tile<T, 32, 32, 16, 2, 2, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
   else
-    launch_update_tile<T, 16, 16, 1, 1, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
+    launch_update_tile<T, 16, 16, bk16, 1, 1, SF, 0, false>(M, N, K, A, lda, B, ldb, C, ldc, s);
 }
 
 template <typename T>
-int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+int gemm_ordered_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                    cudaStream_t s) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   prof_begin(sizeof(T) == 8 ? kProfGemmF64 : kProfGemmF32, s);
@@ -225,17 +238,17 @@ int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, con
 // (one element each): the n x n block (n <= 64) with a K of up to the order
 // of the matrix is spread over as many SMs as it has tiles in its triangle.
 template <typename T>
-int syrk_exact_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t s) {
+int syrk_ordered_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t s) {
   if (n <= 0 || K <= 0) return 0;
-  if (upper) launch_update_tile<T, 8, 8, 1, 1, true, 2, false>(n, n, K, A, lda, B, ldb, C, ldc, s);
-  else launch_update_tile<T, 8, 8, 1, 1, false, 1, true>(n, n, K, A, lda, B, ldb, C, ldc, s);
+  if (upper) launch_update_tile<T, 8, 8, 128, 1, 1, true, 2, false>(n, n, K, A, lda, B, ldb, C, ldc, s);
+  else launch_update_tile<T, 8, 8, 128, 1, 1, false, 1, true>(n, n, K, A, lda, B, ldb, C, ldc, s);
   return (int)cudaGetLastError();
 }
-template int syrk_exact_dev<double>(bool, int, int, const double*, int, const double*, int, double*, int, cudaStream_t);
-template int syrk_exact_dev<float>(bool, int, int, const float*, int, const float*, int, float*, int, cudaStream_t);
-template int gemm_exact_dev<double>(bool, int, int, int, const double*, int, const double*, int, double*, int,
+template int syrk_ordered_dev<double>(bool, int, int, const double*, int, const double*, int, double*, int, cudaStream_t);
+template int syrk_ordered_dev<float>(bool, int, int, const float*, int, const float*, int, float*, int, cudaStream_t);
+template int gemm_ordered_dev<double>(bool, int, int, int, const double*, int, const double*, int, double*, int,
                                     cudaStream_t);
-template int gemm_exact_dev<float>(bool, int, int, int, const float*, int, const float*, int, float*, int,
+template int gemm_ordered_dev<float>(bool, int, int, int, const float*, int, const float*, int, float*, int,
                                    cudaStream_t);
 
 // ------------------------------------------------------------------ panel

@@ -52,7 +52,7 @@ int emu_spotrf(int upper, int n, float* a, int lda, int nb) {
 GEMM_STANDIN = r"""
 namespace gb {
 template <typename T>
-int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
+int gemm_ordered_dev(bool sum_first, int M, int N, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc,
                    cudaStream_t) {
   for (int j = 0; j < N; ++j)
     for (int i = 0; i < M; ++i) {
@@ -70,7 +70,7 @@ int gemm_exact_dev(bool sum_first, int M, int N, int K, const T* A, int lda, con
   return 0;
 }
 template <typename T>
-int syrk_exact_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t) {
+int syrk_ordered_dev(bool upper, int n, int K, const T* A, int lda, const T* B, int ldb, T* C, int ldc, cudaStream_t) {
   for (int j = 0; j < n; ++j)
     for (int i = upper ? 0 : j; i < (upper ? j + 1 : n); ++i) {
       T* c = C + i + (size_t)j * ldc;
