@@ -19,11 +19,16 @@ GB_HD inline T& el(T* A, int lda, int i, int j) { return A[(size_t)i + (size_t)j
 template <typename T>
 GB_HD inline T elc(const T* A, int lda, int i, int j) { return A[(size_t)i + (size_t)j * lda]; }
 
+// The operands of these functions never overlap (a block and the block
+// beside or below it), so they are restrict-qualified: the loads of a step
+// can then be issued ahead of its stores.
+//
 // One element (i, j) of C += ALPHA*A*A**T (lower, 'L','N': i >= j; each
 // term skipped when A(j, l) = 0, BLAS/SRC/dsyrk.f:313-320) or of
 // C := ALPHA*(A**T*A)(i, j) + C (upper, 'U','T': i <= j, dsyrk.f:327-339).
 template <typename T>
-GB_HD inline void syrk_elem(int upper, int i, int j, int k, T alpha, const T* A, int lda, T* C, int ldc) {
+GB_HD inline void syrk_elem(int upper, int i, int j, int k, T alpha, const T* __restrict__ A, int lda,
+                            T* __restrict__ C, int ldc) {
   if (!upper) {
     T c = elc(C, ldc, i, j);
     for (int l = 0; l < k; ++l) {
@@ -58,7 +63,7 @@ GB_HD inline void gemm_chol_elem(int upper, int i, int j, int k, T alpha, const 
 // Row i of B := B*inv(A**T), A lower non-unit n x n ('R','L','T','N',
 // BLAS/SRC/dtrsm.f:389-403, ALPHA = 1).
 template <typename T>
-GB_HD inline void trsm_rltn_row(int i, int n, const T* A, int lda, T* B, int ldb) {
+GB_HD inline void trsm_rltn_row(int i, int n, const T* __restrict__ A, int lda, T* __restrict__ B, int ldb) {
   for (int k = 0; k < n; ++k) {
     el(B, ldb, i, k) = rn_div(elc(B, ldb, i, k), elc(A, lda, k, k));
     const T bk = elc(B, ldb, i, k);
@@ -69,7 +74,7 @@ GB_HD inline void trsm_rltn_row(int i, int n, const T* A, int lda, T* B, int ldb
 // Column j of B := inv(A**T)*B, A upper non-unit m x m ('L','U','T','N',
 // dtrsm.f:306-316, ALPHA = 1).
 template <typename T>
-GB_HD inline void trsm_lutn_col(int j, int m, const T* A, int lda, T* B, int ldb) {
+GB_HD inline void trsm_lutn_col(int j, int m, const T* __restrict__ A, int lda, T* __restrict__ B, int ldb) {
   for (int i = 0; i < m; ++i) {
     T temp = elc(B, ldb, i, j);
     for (int k = 0; k < i; ++k) temp = rn_sub(temp, rn_mul(elc(A, lda, k, i), elc(B, ldb, k, j)));
