@@ -52,6 +52,37 @@ __global__ void ztrsm_kernel(int upper, int trans, int unit, int m, int ncols, c
   if (j < ncols) ztrsm_left_col(upper, trans, unit, m, A, lda, B + (size_t)j * ldb);
 }
 
+// The same for a triangle of order m <= 32 (the panel recursion's ZTRSM):
+// on the GPU the triangle and each thread's column are staged in shared
+// memory first (one round of global loads), so the solve's steps wait on
+// shared memory, not on reloads of the column it has just stored.  32
+// threads per CTA; the operations are those of ztrsm_left_col.
+constexpr int kZtrsmSmall = 32;
+template <typename R>
+__global__ void __launch_bounds__(kZtrsmSmall) ztrsm_small_kernel(int upper, int trans, int unit, int m, int ncols,
+                                                                  const cpx<R>* __restrict__ A, int lda,
+                                                                  cpx<R>* __restrict__ B, int ldb) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+#ifdef __CUDA_ARCH__
+  __shared__ cpx<R> As[kZtrsmSmall * kZtrsmSmall];
+  __shared__ cpx<R> Bs[kZtrsmSmall * (kZtrsmSmall + 1)];
+  for (int e = threadIdx.x; e < m * m; e += kZtrsmSmall) {
+    const int c = e / m, r = e - c * m;
+    As[r + c * kZtrsmSmall] = A[(size_t)r + (size_t)c * lda];
+  }
+  cpx<R>* b = Bs + threadIdx.x * (kZtrsmSmall + 1);
+  if (j < ncols)
+    for (int i = 0; i < m; ++i) b[i] = B[(size_t)i + (size_t)j * ldb];
+  __syncthreads();
+  if (j < ncols) {
+    ztrsm_left_col(upper, trans, unit, m, As, kZtrsmSmall, b);
+    for (int i = 0; i < m; ++i) B[(size_t)i + (size_t)j * ldb] = b[i];
+  }
+#else
+  if (j < ncols) ztrsm_left_col(upper, trans, unit, m, A, lda, B + (size_t)j * ldb);
+#endif
+}
+
 __global__ void zipiv_add_kernel(int* __restrict__ ipiv, int cnt, int off) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < cnt) ipiv[i] += off;
@@ -130,6 +161,11 @@ struct GpuZOps {
     // row's short ones (m <= NB): a thread per column
     int rc = 0;
     if (m > 128 && ztrsm_cta_dev<R>(upper, trans, unit, m, ncols, A, lda, B, ldb, s, &rc)) return rc;
+    if (m <= kZtrsmSmall) {
+      const unsigned g = zblocks(ncols, kZtrsmSmall);
+      GB_LAUNCH(ztrsm_small_kernel<R><<<g, kZtrsmSmall, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
+      return (int)cudaGetLastError();
+    }
     GB_LAUNCH(ztrsm_kernel<R><<<zblocks(ncols, 64), 64, 0, s>>>(upper, trans, unit, m, ncols, A, lda, B, ldb));
     return (int)cudaGetLastError();
   }

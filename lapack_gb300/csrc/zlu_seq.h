@@ -252,9 +252,11 @@ GB_HD inline void zlaswp_col(cpx<R>* col, int k1, int k2, const int* ipiv, int i
 
 // One column b of ZTRSM('L', UPLO, TRANSA, DIAG) with ALPHA = ONE
 // (BLAS/SRC/ztrsm.f:272-345): trans 0 = 'N', 1 = 'T', 2 = 'C'.  The column
-// is first multiplied by ALPHA, as the reference does.
+// is first multiplied by ALPHA, as the reference does.  The triangle and the
+// column never overlap (restrict: a step's loads can be issued ahead).
 template <typename R>
-GB_HD inline void ztrsm_left_col(int upper, int trans, int unit, int m, const cpx<R>* A, int lda, cpx<R>* b) {
+GB_HD inline void ztrsm_left_col(int upper, int trans, int unit, int m, const cpx<R>* __restrict__ A, int lda,
+                                 cpx<R>* __restrict__ b) {
   auto a = [&](int i, int j) -> cpx<R> { return A[(size_t)i + (size_t)j * lda]; };
   const cpx<R> one = zmk(R(1), R(0));
   if (trans == 0) {

@@ -102,31 +102,51 @@ __global__ void __launch_bounds__(kZcolThreads) zcol_cta_kernel(int m, cpx<R>* _
     }
     return;
   }
-  __shared__ ZamaxPart<R> part[kZcolThreads];
+  constexpr int kWarps = kZcolThreads / 32;
+  __shared__ ZamaxPart<R> part[kWarps];
   __shared__ int p_s, mode_s;      // pivot row (1-based); 0 zero pivot, 1 no scaling, 2 multiply, 3 divide
   __shared__ cpx<R> r_s;
-  part[tid] = zamax_part(m, a, tid, kZcolThreads);
+  const int lane = tid & 31, warp = tid >> 5;
+  // the parts combined within each warp by shuffles, then the warps' by warp
+  // 0 (the combination is associative, commutative and idempotent: a lane
+  // past the end combines with its own value)
+  auto warp_combine = [&](ZamaxPart<R> p) {
+    for (int off = 16; off > 0; off >>= 1) {
+      ZamaxPart<R> o;
+      o.nan = __shfl_down_sync(0xffffffffu, p.nan, off);
+      o.inf = __shfl_down_sync(0xffffffffu, p.inf, off);
+      o.over = __shfl_down_sync(0xffffffffu, p.over, off);
+      o.val = __shfl_down_sync(0xffffffffu, p.val, off);
+      o.idx = __shfl_down_sync(0xffffffffu, p.idx, off);
+      p = zamax_combine(p, o);
+    }
+    return p;
+  };
+  ZamaxPart<R> mine = warp_combine(zamax_part(m, a, tid, kZcolThreads));
+  if (lane == 0) part[warp] = mine;
   __syncthreads();
-  for (int h = kZcolThreads / 2; h > 0; h >>= 1) {
-    if (tid < h) part[tid] = zamax_combine(part[tid], part[tid + h]);
-    __syncthreads();
+  if (warp == 0) {
+    mine = warp_combine(part[lane < kWarps ? lane : 0]);
+    if (lane == 0) part[0] = mine;
   }
+  __syncthreads();
   const ZamaxPart<R> all = part[0];
   int sidx = kZamaxNone;
   if (all.nan == kZamaxNone && all.inf == kZamaxNone && all.over != kZamaxNone) {
-    // the scaled pass from the first overflowing sum (reuses part[].val/idx)
-    __syncthreads();
+    // the scaled pass from the first overflowing sum
+    __shared__ R sv[kWarps];
+    __shared__ int si[kWarps];
     R v;
     int i;
     zamax_scaled_part(m, a, all.over, tid, kZcolThreads, &v, &i);
-    part[tid].val = v;
-    part[tid].idx = i;
+    for (int off = 16; off > 0; off >>= 1)
+      zamax_pick(v, i, __shfl_down_sync(0xffffffffu, v, off), __shfl_down_sync(0xffffffffu, i, off));
+    if (lane == 0) { sv[warp] = v; si[warp] = i; }
     __syncthreads();
-    for (int h = kZcolThreads / 2; h > 0; h >>= 1) {
-      if (tid < h) zamax_pick(part[tid].val, part[tid].idx, part[tid + h].val, part[tid + h].idx);
-      __syncthreads();
-    }
-    sidx = part[0].idx;
+    v = sv[0];
+    i = si[0];
+    for (int w = 1; w < kWarps; ++w) zamax_pick(v, i, sv[w], si[w]);
+    sidx = i;
   }
   if (tid == 0) {
     const int p = zamax_result(all, sidx);

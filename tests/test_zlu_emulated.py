@@ -1,9 +1,10 @@
 """The complex LU's GPU source (lapack_gb300/csrc/zlu.cu) run on the CPU.
 
 Every kernel in zlu.cu is a one-dimensional launch whose threads touch
-disjoint data (no shared memory, no barriers, the one shared word updated by
-atomicMin or by identical stores), so running its blocks and threads one
-after another computes what the GPU computes.  The test rewrites each
+disjoint data (no barriers, the one shared word updated by atomicMin or by
+identical stores; the small-triangle ZTRSM stages through shared memory on
+the GPU only and runs its direct form here), so running its blocks and
+threads one after another computes what the GPU computes.  The test rewrites each
 `kernel<<<grid, block, smem, stream>>>(args)` of the file into a call of a
 sequential launcher, compiles the file with g++ over a small stand-in for
 the CUDA runtime calls it makes (copies, memsets, synchronisation, stream-
