@@ -17,6 +17,7 @@ Inputs are synthetic, drawn from numpy's PCG64 with a fixed seed.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
     python bench.py --workload batched|adjoint|update|leaf ...   (one configuration or kernel class alone)
+    python bench.py --workload dsposv|zgetrf [--wn N]            (the Cholesky and complex rows, device memory)
 """
 import argparse
 import ctypes
@@ -64,9 +65,11 @@ def parse():
     p.add_argument("--no-sweep", action="store_true", help="skip the per-kappa records (1e2, 1e6, 1e10)")
     p.add_argument("--no-sub", action="store_true", help="skip the batched and adjoint records of the default run")
     p.add_argument("--cpu-n", type=int, default=4096, help="size of the CPU baseline sample")
-    p.add_argument("--workload", default="dsgesv", choices=["dsgesv", "batched", "adjoint", "update", "leaf", "dgetrf"],
+    p.add_argument("--workload", default="dsgesv",
+                   choices=["dsgesv", "batched", "adjoint", "update", "leaf", "dgetrf", "dsposv", "zgetrf"],
                    help="dsgesv: the headline n=32768 solve; batched: 20000 uneven systems in one launch")
     p.add_argument("--dtype", default="d", choices=["d", "s"], help="precision of the batched workload")
+    p.add_argument("--wn", type=int, default=0, help="order of the dsposv / zgetrf workloads (0: 8192 / 4096)")
     p.add_argument("--batch", type=int, default=20000)
     p.add_argument("--fixed-n", type=int, default=0, help="batched: every system of this size (0: uniform 8..512)")
     p.add_argument("--m", type=int, default=8192, help="update / leaf: rows (update: M = N)")
@@ -793,6 +796,68 @@ def run_adjoint(args):
                          "work": "4*n^2*nrhs flop per system"}}
 
 
+def run_widened(args):
+    """The widened rows on device memory, one call per step, the inputs
+    restored before each call outside the timed region: 'dsposv' is
+    DSPOSV('L') of the SPD system A = X X^T/64 + I (X: 64 columns uniform in
+    [-1, 1]), b = A*1; 'zgetrf' is ZGETRF of a matrix whose real and
+    imaginary parts are uniform in [-1, 1].  Times are CUDA events on the
+    launching stream; the value is the median over the steps."""
+    import torch
+    import lapack_gb300 as g
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    L = g.lib()
+    vp = ctypes.c_void_p
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    gen = torch.Generator(device=dev).manual_seed(args.seed)
+    it, info = ctypes.c_int(0), ctypes.c_int(0)
+    if args.workload == "dsposv":
+        n = args.wn or 8192
+        Xr = torch.rand(n, 64, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+        A0 = Xr @ Xr.t() / 64 + torch.eye(n, dtype=torch.float64, device=dev)
+        B = A0.sum(1).contiguous()
+        X = torch.empty_like(B)
+        A = torch.empty_like(A0)
+
+        def call():
+            return L.gb300_dsposv_dev(ctypes.c_char(b"L"), n, 1, vp(A.data_ptr()), n, vp(B.data_ptr()), n,
+                                      vp(X.data_ptr()), n, ctypes.byref(it), ctypes.byref(info), s)
+        flops, metric, dtype = n ** 3 / 3.0, f"DSPOSV('L') n={n} nrhs=1 on device memory", "f32 factor + f64 refine"
+    else:
+        n = args.wn or 4096
+        A0 = torch.complex(torch.rand(n, n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1,
+                           torch.rand(n, n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1)
+        A = torch.empty_like(A0)
+        ip = torch.empty(n, dtype=torch.int32, device=dev)
+
+        def call():
+            return L.gb300_zgetrf_dev(n, n, vp(A.data_ptr()), n, vp(ip.data_ptr()), ctypes.byref(info), s)
+        flops, metric, dtype = 8.0 / 3.0 * n ** 3, f"ZGETRF n={n} on device memory", "c128"
+    times = []
+    for k in range(args.warmup + args.steps):
+        A.copy_(A0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rc = call()
+        e1.record()
+        torch.cuda.synchronize()
+        if rc:
+            raise RuntimeError(f"{args.workload} status {rc}")
+        if k >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    out = {"metric": metric, "value": ms * 1e-3, "unit": "s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "dtype": dtype,
+           "data": "synthetic", "config": {"workload": args.workload, "n": n, "exact": g.get_option("exact")},
+           "tflops": flops / ms / 1e9, "info": info.value}
+    if args.workload == "dsposv":
+        out["iter"] = it.value
+        out["max_abs_error_vs_ones"] = (X - 1).abs().max().item()
+    return out
+
+
 def run_kernel_case(args):
     """One kernel class alone, for timing and profiling: 'update' is the
     BF16x3 trailing update C -= A B of an M x M matrix with K = k
@@ -890,6 +955,9 @@ def main():
     args = parse()
     if args.workload in ("update", "leaf", "dgetrf"):
         print(json.dumps(run_kernel_case(args)))
+        return
+    if args.workload in ("dsposv", "zgetrf"):
+        print(json.dumps(run_widened(args)))
         return
     if args.workload == "batched" and args.impl == "gb300":
         world = int(os.environ.get("WORLD_SIZE", "1"))
