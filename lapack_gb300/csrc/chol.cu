@@ -10,12 +10,13 @@
 // in the reference's per-element orders, with separately rounded products
 // in exact mode and fused multiply-adds otherwise (the DSYRK stores one
 // triangle and, in the lower form, skips the terms whose A(J,L) is zero, as
-// BLAS/SRC/dsyrk.f:313-320 does).  The DTRSM and the
-// diagonal blocks' DPOTRF2 (at most NB = 64 columns, on one thread over
-// shared memory) are kernels whose threads each compute one row or column
-// through the shared host/device functions of potrf_seq.h (checked against
-// the oracle on the CPU).  The solves use the library's triangular solve
-// kernels.  DSPOSV mirrors DSGESV: FP32 Cholesky and solves, FP64 residual
+// BLAS/SRC/dsyrk.f:313-320 does).  The DTRSM (one thread per row or
+// column, staged in shared memory) and the diagonal blocks' DPOTRF2 (at
+// most NB = 64 columns, one CTA over shared memory, each recursion step's
+// rows and elements spread over its threads) compute every element through
+// the operations of the shared host/device functions of potrf_seq.h
+// (checked against the oracle on the CPU).  The solves use the library's
+// triangular solve kernels.  DSPOSV mirrors DSGESV: FP32 Cholesky and solves, FP64 residual
 // with the reference's DSYMM order, the same convergence test, the FP64
 // fallback.
 #include "driver.h"

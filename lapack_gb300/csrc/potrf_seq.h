@@ -3,8 +3,8 @@
 // SRC/dsposv.f:237-420), written once for host and device and templated on
 // the element type (DPOTRF / SPOTRF).  Each function computes what one GPU
 // thread computes — one element of a DSYRK / DGEMM update, one row or
-// column of a DTRSM, one row sum of DLANSY, one element of DSYMM, or a whole
-// DPOTRF2 of a diagonal block — in the reference loop order with separately
+// column of a DTRSM, one row sum of DLANSY, one element of DSYMM, or its
+// share of a DPOTRF2 of a diagonal block — in the reference loop order with separately
 // rounded operations, so that the CPU tests can compose them exactly as the
 // GPU driver does and compare with the oracle bit for bit.
 #pragma once
